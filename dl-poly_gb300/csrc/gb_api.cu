@@ -1,0 +1,641 @@
+// gb_api.cu - the C-ABI of the GB300 DL_POLY force/update path
+// (include/gb300_dlpoly.h): device context, interpolation tables, the
+// exported entry points and the resident md_vv step loop.
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gb_common.cuh"
+
+Dev g;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr double kR4pie0 = 138935.4835;  // constants.F90:100
+
+inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+// -------------------------------------------------------------- reductions
+__global__ void k_reduce_blocks(const double* blk, int nb, int nv, double* out) {
+  // one warp per value; fixed order -> deterministic
+  int v = blockIdx.x;
+  if (v >= nv) return;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s += blk[(size_t)b * nv + v];
+  __shared__ double red[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    t = warp_sum(t);
+    if (threadIdx.x == 0) out[v] = t;
+  }
+}
+
+__global__ void k_scan_excl(const int* in, int* out, int n) {
+  __shared__ int part[1024];
+  const int T = blockDim.x;
+  const int per = (n + T - 1) / T;
+  const int b = threadIdx.x * per;
+  int s = 0;
+  for (int k = 0; k < per; ++k) if (b + k < n) s += in[b + k];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < T; o <<= 1) {
+    int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = part[threadIdx.x] - s;
+  for (int k = 0; k < per; ++k)
+    if (b + k < n) { out[b + k] = run; run += in[b + k]; }
+}
+
+__global__ void k_gather_parts(int n, const unsigned char* parts, double* x, double* y, double* z) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* r = reinterpret_cast<const double*>(parts + (size_t)i * 64);
+  x[i] = r[0]; y[i] = r[1]; z[i] = r[2];
+}
+
+__global__ void k_nonfinite(int n, const double* a, const double* b, const double* c, int* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!isfinite(a[i]) || !isfinite(b[i]) || !isfinite(c[i])) atomicOr(status, ST_NONFINITE);
+}
+
+std::vector<double> h_tmp;
+int* d_scratch = nullptr;
+size_t d_scratch_n = 0;
+
+template <typename T>
+void dalloc(T** p, size_t n) {
+  GB_CUDA(cudaMalloc(p, sizeof(T) * std::max<size_t>(n, 1)));
+  GB_CUDA(cudaMemset(*p, 0, sizeof(T) * std::max<size_t>(n, 1)));
+}
+
+void free_all() {
+  void* ptrs[] = {g.x, g.y, g.z, g.xf, g.fx, g.fy, g.fz, g.fixp, g.vx, g.vy, g.vz, g.chge, g.weight, g.ltype, g.ltg,
+                  g.lfrzn, g.ixyz, g.src, g.shcode, g.xbg, g.ybg, g.zbg, g.ox, g.oy, g.oz, g.which_cell,
+                  g.cell_count, g.cell_start, g.cell_fill, g.at_list, g.sorted_pos, g.xs, g.xsf, g.list, g.blk,
+                  g.list_excl, g.flist, g.fcount, g.fstart, g.erfc_coef, g.erfc_coef_f, g.vdw_coef, g.vdw_coef_f,
+                  g.vdw_kind, g.vdw_eps, g.vdw_sig, g.spl, g.nidx, g.brick_of, g.brick_count, g.brick_start,
+                  g.brick_fill, g.brick_atoms, g.Q, g.G, g.Qf, g.Gf, g.theta, g.psi, g.theta_f, g.psi_f, g.tw1, g.tw2,
+                  g.tw3, g.tw1f, g.tw2f, g.tw3f, g.fspme, g.blkacc, g.con_i, g.con_j, g.con_d0, g.dxx, g.dyy,
+                  g.dzz, g.dxt, g.dyt, g.dzt, g.dt2, g.gam, g.listot, g.acon_start, g.acon_list, g.sc, d_scratch};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (g.hsc) cudaFreeHost(g.hsc);
+  if (g.stream) {
+    for (int k = 0; k < 8; ++k) cudaEventDestroy(g.ev[k]);
+    cudaStreamDestroy(g.stream);
+  }
+  d_scratch = nullptr;
+  d_scratch_n = 0;
+  g = Dev();
+}
+
+// quadratic coefficients of the 3-point interpolant over points k, k+1, k+2
+inline void quad_coef(double p1, double p2, double p3, double* c) {
+  double c2 = 0.5 * (p3 - 2.0 * p2 + p1);
+  c[0] = p1;
+  c[1] = (p2 - p1) - c2;
+  c[2] = c2;
+}
+
+double calc_erfc_n(double x) {  // numerics.F90:3647-3667
+  const double a1 = 0.254829592, a2 = -0.284496736, a3 = 1.421413741, a4 = -1.453152027, a5 = 1.061405429,
+               pp = 0.3275911;
+  double tt = 1.0 / (1.0 + pp * x);
+  return tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5)))) * std::exp(-(x * x));
+}
+
+void build_tables(const double* vdw_prm) {
+  const double rcut = g.p.rcut, alpha = g.p.alpha;
+  // erfc(ar)/r and derivative tables, table(i) = f(i*h), i = 1..n (electrostatic.F90:88-127)
+  const int n = g.nsamples;
+  std::vector<double> te(n + 3, 0.0), td(n + 3, 0.0);
+  const double h = rcut / (double)(n - 4);
+  g.erfc_rdr = 1.0 / h;
+  const double rsqrpi = 1.0 / std::sqrt(kPi);
+  for (int i = 1; i <= n; ++i) {
+    double r = (double)i * h;
+    te[i] = calc_erfc_n(alpha * r) / r;
+    td[i] = (calc_erfc_n(alpha * r) / r + alpha * (2.0 * std::exp(-((alpha * r) * (alpha * r))) * rsqrpi)) / (r * r);
+  }
+  std::vector<double> ec((size_t)(n + 1) * 6, 0.0);
+  for (int k = 0; k + 2 <= n; ++k) {
+    quad_coef(te[k], te[k + 1], te[k + 2], &ec[(size_t)k * 6]);
+    quad_coef(td[k], td[k + 1], td[k + 2], &ec[(size_t)k * 6 + 3]);
+  }
+  // vdW tables (vdw.F90:1397-1460): tab(i) = lj(i*dlr), i = 1..max_grid
+  const int mg = g.max_grid;
+  const double dl = g.p.rvdw / (double)(mg - 4);
+  g.vdw_rdr = 1.0 / dl;
+  g.nkey = g.p.ntypes * (g.p.ntypes + 1) / 2;
+  const int vstride = (mg + 3) * 6;
+  std::vector<double> vc((size_t)g.nkey * vstride, 0.0);
+  g.h_vdw_kind.assign(g.nkey, 0);
+  g.h_vdw_eps.assign(g.nkey, 0.0);
+  g.h_vdw_sig.assign(g.nkey, 0.0);
+  for (int key = 0; key < g.nkey; ++key) {
+    g.h_vdw_kind[key] = (int)vdw_prm[3 * key];
+    g.h_vdw_eps[key] = vdw_prm[3 * key + 1];
+    g.h_vdw_sig[key] = vdw_prm[3 * key + 2];
+    if (g.h_vdw_kind[key] != 1) continue;
+    std::vector<double> tf(mg + 3, 0.0), tp(mg + 3, 0.0);
+    for (int i = 1; i <= mg; ++i) {
+      double r = (double)i * dl;
+      double sor = g.h_vdw_sig[key] / r;
+      double sor6 = sor * sor * sor * sor * sor * sor;
+      tp[i] = 4.0 * g.h_vdw_eps[key] * sor6 * (sor6 - 1.0);
+      tf[i] = 24.0 * g.h_vdw_eps[key] * sor6 * (2.0 * sor6 - 1.0);
+    }
+    for (int k = 1; k + 2 <= mg; ++k) {
+      quad_coef(tf[k], tf[k + 1], tf[k + 2], &vc[(size_t)key * vstride + (size_t)k * 6]);
+      quad_coef(tp[k], tp[k + 1], tp[k + 2], &vc[(size_t)key * vstride + (size_t)k * 6 + 3]);
+    }
+  }
+  dalloc(&g.erfc_coef, ec.size());
+  dalloc(&g.erfc_coef_f, ec.size());
+  dalloc(&g.vdw_coef, vc.size());
+  dalloc(&g.vdw_coef_f, vc.size());
+  GB_CUDA(cudaMemcpy(g.erfc_coef, ec.data(), sizeof(double) * ec.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(g.vdw_coef, vc.data(), sizeof(double) * vc.size(), cudaMemcpyHostToDevice));
+  std::vector<float> ecf(ec.begin(), ec.end()), vcf(vc.begin(), vc.end());
+  GB_CUDA(cudaMemcpy(g.erfc_coef_f, ecf.data(), sizeof(float) * ecf.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(g.vdw_coef_f, vcf.data(), sizeof(float) * vcf.size(), cudaMemcpyHostToDevice));
+  dalloc(&g.vdw_kind, g.nkey);
+  dalloc(&g.vdw_eps, g.nkey);
+  dalloc(&g.vdw_sig, g.nkey);
+  GB_CUDA(cudaMemcpy(g.vdw_kind, g.h_vdw_kind.data(), sizeof(int) * g.nkey, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(g.vdw_eps, g.h_vdw_eps.data(), sizeof(double) * g.nkey, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(g.vdw_sig, g.h_vdw_sig.data(), sizeof(double) * g.nkey, cudaMemcpyHostToDevice));
+}
+
+template <typename F>
+int guarded(F&& f) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  try {
+    return f();
+  } catch (int e) {
+    return e;
+  }
+}
+
+// forces for the current positions: SPME then the pair loop (drivers.F90:655-786)
+int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real) {
+
+  double st[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double erc = 0, vrc = 0;
+  double e6[6] = {0, 0, 0, 0, 0, 0};
+  integ_zero_forces();
+  if (g.precision == GB_MIXED) list_pos_f32();
+  if (do_spme) spme_forces(&erc, &vrc, st);
+  if (do_real) pair_forces(e6, st);
+  if (g.precision == GB_MIXED) integ_forces_to_fp64();
+  if (eng8) {
+    eng8[0] = erc; eng8[1] = vrc;
+    eng8[2] = e6[0]; eng8[3] = e6[1]; eng8[4] = e6[2]; eng8[5] = e6[3]; eng8[6] = e6[4]; eng8[7] = e6[5];
+  }
+  if (stress9) for (int k = 0; k < 9; ++k) stress9[k] = st[k];
+  return GB_OK;
+}
+
+int do_refresh(int32_t* update) {
+  int upd = integ_vnl_check();
+  if (update) *update = upd;
+  if (upd) return list_relocate_and_halo();
+  return list_refresh_halo();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------- shared helpers
+void dcell_host(const double* aaa, double* bbb) {
+  bbb[0] = std::sqrt(aaa[0] * aaa[0] + aaa[1] * aaa[1] + aaa[2] * aaa[2]);
+  bbb[1] = std::sqrt(aaa[3] * aaa[3] + aaa[4] * aaa[4] + aaa[5] * aaa[5]);
+  bbb[2] = std::sqrt(aaa[6] * aaa[6] + aaa[7] * aaa[7] + aaa[8] * aaa[8]);
+  bbb[3] = (aaa[0] * aaa[3] + aaa[1] * aaa[4] + aaa[2] * aaa[5]) / (bbb[0] * bbb[1]);
+  bbb[4] = (aaa[0] * aaa[6] + aaa[1] * aaa[7] + aaa[2] * aaa[8]) / (bbb[0] * bbb[2]);
+  bbb[5] = (aaa[3] * aaa[6] + aaa[4] * aaa[7] + aaa[5] * aaa[8]) / (bbb[1] * bbb[2]);
+  double axb1 = aaa[1] * aaa[5] - aaa[2] * aaa[4], axb2 = aaa[2] * aaa[3] - aaa[0] * aaa[5],
+         axb3 = aaa[0] * aaa[4] - aaa[1] * aaa[3];
+  double bxc1 = aaa[4] * aaa[8] - aaa[5] * aaa[7], bxc2 = aaa[5] * aaa[6] - aaa[3] * aaa[8],
+         bxc3 = aaa[3] * aaa[7] - aaa[4] * aaa[6];
+  double cxa1 = aaa[7] * aaa[2] - aaa[8] * aaa[1], cxa2 = aaa[8] * aaa[0] - aaa[6] * aaa[2],
+         cxa3 = aaa[6] * aaa[1] - aaa[7] * aaa[0];
+  bbb[9] = std::fabs(aaa[0] * bxc1 + aaa[1] * bxc2 + aaa[2] * bxc3);
+  double d[3] = {bbb[9] / std::sqrt(bxc1 * bxc1 + bxc2 * bxc2 + bxc3 * bxc3),
+                 bbb[9] / std::sqrt(cxa1 * cxa1 + cxa2 * cxa2 + cxa3 * cxa3),
+                 bbb[9] / std::sqrt(axb1 * axb1 + axb2 * axb2 + axb3 * axb3)};
+  double x[3] = {std::fabs(aaa[0]) / bbb[0], std::fabs(aaa[3]) / bbb[1], std::fabs(aaa[6]) / bbb[2]};
+  double y[3] = {std::fabs(aaa[1]) / bbb[0], std::fabs(aaa[4]) / bbb[1], std::fabs(aaa[7]) / bbb[2]};
+  if (x[0] >= x[1] && x[0] >= x[2]) {
+    bbb[6] = d[0];
+    if (y[1] >= y[2]) { bbb[7] = d[1]; bbb[8] = d[2]; } else { bbb[7] = d[2]; bbb[8] = d[1]; }
+  } else if (x[1] >= x[0] && x[1] >= x[2]) {
+    bbb[6] = d[1];
+    if (y[0] >= y[2]) { bbb[7] = d[0]; bbb[8] = d[2]; } else { bbb[7] = d[2]; bbb[8] = d[0]; }
+  } else {
+    bbb[6] = d[2];
+    if (y[0] >= y[1]) { bbb[7] = d[0]; bbb[8] = d[1]; } else { bbb[7] = d[1]; bbb[8] = d[0]; }
+  }
+}
+
+void invert_host(const double* a, double* b, double* d) {
+  b[0] = a[4] * a[8] - a[5] * a[7]; b[1] = a[2] * a[7] - a[1] * a[8]; b[2] = a[1] * a[5] - a[2] * a[4];
+  b[3] = a[5] * a[6] - a[3] * a[8]; b[4] = a[0] * a[8] - a[2] * a[6]; b[5] = a[2] * a[3] - a[0] * a[5];
+  b[6] = a[3] * a[7] - a[4] * a[6]; b[7] = a[1] * a[6] - a[0] * a[7]; b[8] = a[0] * a[4] - a[1] * a[3];
+  *d = a[0] * b[0] + a[3] * b[1] + a[6] * b[2];
+  double r = 0.0;
+  if (std::fabs(*d) > 0.0) r = 1.0 / *d;
+  for (int i = 0; i < 9; ++i) b[i] = r * b[i];
+}
+
+void gb_sync_scalars() {
+  GB_CUDA(cudaMemcpyAsync(g.hsc, g.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, g.stream));
+  GB_CUDA(cudaStreamSynchronize(g.stream));
+}
+
+double* gb_blkacc(int n) {
+  if (n > g.blkacc_n) {
+    if (g.blkacc) {
+      GB_CUDA(cudaStreamSynchronize(g.stream));
+      cudaFree(g.blkacc);
+    }
+    g.blkacc_n = n + 4096;
+    GB_CUDA(cudaMalloc(&g.blkacc, sizeof(double) * g.blkacc_n));
+  }
+  return g.blkacc;
+}
+
+void gb_reduce_blocks(const double* blk, int nblocks_, int nv, double* out_dev) {
+  k_reduce_blocks<<<nv, 256, 0, g.stream>>>(blk, nblocks_, nv, out_dev);
+  GB_LAUNCHED();
+}
+
+int* gb_scan_scratch(int n) {
+  if ((size_t)n > d_scratch_n) {
+    if (d_scratch) {
+      GB_CUDA(cudaStreamSynchronize(g.stream));
+      cudaFree(d_scratch);
+    }
+    d_scratch_n = (size_t)n + 4096;
+    GB_CUDA(cudaMalloc(&d_scratch, sizeof(int) * d_scratch_n));
+  }
+  return d_scratch;
+}
+
+void scan_exclusive(const int* in, int* out, int n) {
+  k_scan_excl<<<1, 1024, 0, g.stream>>>(in, out, n);
+  GB_LAUNCHED();
+}
+
+// ================================================================== C-ABI
+extern "C" {
+
+int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double* chge, const double* weight,
+            const int32_t* lfrzn, const double* vdw_prm, int ntcons, const int32_t* listcon, const double* prmcon,
+            const int32_t* list_excl) {
+  if (!prm || natms <= 0 || !ltype || !chge || !weight || !vdw_prm) return GB_ERR_ARG;
+  if (g.init) free_all();
+  try {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return GB_ERR_NO_DEVICE;
+    GB_CUDA(cudaSetDevice(0));
+    cudaDeviceProp prop;
+    GB_CUDA(cudaGetDeviceProperties(&prop, 0));
+    g.nsm = prop.multiProcessorCount;
+    g.p = *prm;
+    g.natms = natms;
+    g.mxatms = std::max(prm->mxatms, natms);
+    g.precision = prm->precision;
+    std::memcpy(g.cell, prm->cell, sizeof(g.cell));
+    double det;
+    invert_host(g.cell, g.rcell, &det);
+    dcell_host(g.cell, g.celprp);
+    g.volm = g.celprp[9];
+    g.cubic = (g.cell[0] == g.cell[4] && g.cell[0] == g.cell[8]);
+    bool ortho = g.cell[1] == 0 && g.cell[2] == 0 && g.cell[3] == 0 && g.cell[5] == 0 && g.cell[6] == 0 && g.cell[7] == 0;
+    if (!ortho || !g.cubic) { free_all(); return GB_ERR_ARG; }  // cubic cells (imcon 1) only
+    g.rcutx = prm->rcut + prm->rpad;
+    if (g.rcutx >= std::min(g.celprp[6], std::min(g.celprp[7], g.celprp[8])) / 2.0) { free_all(); return GB_ERR_CUTOFF_CELL; }
+    GB_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 8; ++k) GB_CUDA(cudaEventCreate(&g.ev[k]));
+    const int mx = g.mxatms;
+    dalloc(&g.x, mx); dalloc(&g.y, mx); dalloc(&g.z, mx);
+    dalloc(&g.xf, mx);
+    dalloc(&g.fx, natms); dalloc(&g.fy, natms); dalloc(&g.fz, natms);
+    dalloc(&g.fixp, 3 * (size_t)natms);
+    dalloc(&g.vx, natms); dalloc(&g.vy, natms); dalloc(&g.vz, natms);
+    dalloc(&g.chge, mx); dalloc(&g.weight, mx);
+    dalloc(&g.ltype, mx); dalloc(&g.ltg, mx); dalloc(&g.lfrzn, mx);
+    dalloc(&g.ixyz, mx); dalloc(&g.src, mx); dalloc(&g.shcode, mx);
+    dalloc(&g.xbg, natms); dalloc(&g.ybg, natms); dalloc(&g.zbg, natms);
+    dalloc(&g.ox, natms); dalloc(&g.oy, natms); dalloc(&g.oz, natms);
+    dalloc(&g.which_cell, mx); dalloc(&g.at_list, mx); dalloc(&g.sorted_pos, mx);
+    dalloc(&g.xs, mx); dalloc(&g.xsf, mx);
+    g.ld = prm->max_list + 4;
+    dalloc(&g.list, (size_t)g.ld * natms);
+    dalloc(&g.fcount, natms + 1);
+    dalloc(&g.fstart, natms + 1);
+    dalloc(&g.sc, 1);
+    GB_CUDA(cudaMallocHost(&g.hsc, sizeof(DevScalars)));
+    std::memset(g.hsc, 0, sizeof(DevScalars));
+    // topology
+    std::vector<int> ltg(natms);
+    g.megfrz = 0;
+    for (int i = 0; i < natms; ++i) { ltg[i] = i + 1; if (lfrzn && lfrzn[i]) g.megfrz++; }
+    GB_CUDA(cudaMemcpy(g.ltg, ltg.data(), sizeof(int) * natms, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(g.ltype, ltype, sizeof(int) * natms, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(g.chge, chge, sizeof(double) * natms, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(g.weight, weight, sizeof(double) * natms, cudaMemcpyHostToDevice));
+    if (lfrzn) GB_CUDA(cudaMemcpy(g.lfrzn, lfrzn, sizeof(int) * natms, cudaMemcpyHostToDevice));
+    const int ldx = prm->max_exclude + 1;
+    dalloc(&g.list_excl, (size_t)ldx * natms);
+    g.lbook = false;
+    if (list_excl) {
+      GB_CUDA(cudaMemcpy(g.list_excl, list_excl, sizeof(int) * (size_t)ldx * natms, cudaMemcpyHostToDevice));
+      for (int i = 0; i < natms; ++i) if (list_excl[(size_t)i * ldx] > 0) { g.lbook = true; break; }
+    }
+    // tables and constants
+    g.nsamples = std::max(1004, (int)std::lround(prm->rcut / 0.01) + 4);   // bounds.F90:811
+    g.max_grid = std::max(1004, (int)std::lround(prm->rvdw / 0.01) + 4);   // bounds.F90:820
+    build_tables(vdw_prm);
+    g.scaling = kR4pie0 / prm->epsq;
+    double sq2 = 0.0;
+    for (int i = 0; i < natms; ++i) sq2 += chge[i] * chge[i];
+    g.self_interaction = -sq2 * (g.scaling * prm->alpha * (1.0 / 1.7724538509055161040) / 1.0);  // spme.F90:159-231
+    g.ntcons = ntcons;
+    if (ntcons > 0) integ_setup_constraints(listcon, prmcon);
+    list_setup();
+    spme_setup();
+    g.init = true;
+    g.launches = 0;
+    return GB_OK;
+  } catch (int e) {
+    free_all();
+    return e;
+  }
+}
+
+int gb_upload_state(const double* x, const double* y, const double* z, const double* vx, const double* vy,
+                    const double* vz) {
+  return guarded([&]() {
+    const size_t b = sizeof(double) * g.natms;
+    if (!x || !y || !z) return (int)GB_ERR_ARG;
+    GB_CUDA(cudaMemcpyAsync(g.x, x, b, cudaMemcpyHostToDevice, g.stream));
+    GB_CUDA(cudaMemcpyAsync(g.y, y, b, cudaMemcpyHostToDevice, g.stream));
+    GB_CUDA(cudaMemcpyAsync(g.z, z, b, cudaMemcpyHostToDevice, g.stream));
+    if (vx && vy && vz) {
+      GB_CUDA(cudaMemcpyAsync(g.vx, vx, b, cudaMemcpyHostToDevice, g.stream));
+      GB_CUDA(cudaMemcpyAsync(g.vy, vy, b, cudaMemcpyHostToDevice, g.stream));
+      GB_CUDA(cudaMemcpyAsync(g.vz, vz, b, cudaMemcpyHostToDevice, g.stream));
+    }
+    GB_CUDA(cudaStreamSynchronize(g.stream));
+    GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
+    k_nonfinite<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, g.x, g.y, g.z, &g.sc->status);
+    GB_LAUNCHED();
+    gb_sync_scalars();
+    if (g.hsc->status & ST_NONFINITE) return (int)GB_ERR_NONFINITE;
+    return (int)GB_OK;
+  });
+}
+
+int gb_upload_parts(const void* parts, const double* vx, const double* vy, const double* vz) {
+  return guarded([&]() {
+    if (!parts) return (int)GB_ERR_ARG;
+    unsigned char* d = nullptr;
+    GB_CUDA(cudaMalloc(&d, (size_t)64 * g.natms));
+    GB_CUDA(cudaMemcpy(d, parts, (size_t)64 * g.natms, cudaMemcpyHostToDevice));
+    k_gather_parts<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, d, g.x, g.y, g.z);
+    GB_LAUNCHED();
+    GB_CUDA(cudaStreamSynchronize(g.stream));
+    cudaFree(d);
+    const size_t b = sizeof(double) * g.natms;
+    if (vx && vy && vz) {
+      GB_CUDA(cudaMemcpy(g.vx, vx, b, cudaMemcpyHostToDevice));
+      GB_CUDA(cudaMemcpy(g.vy, vy, b, cudaMemcpyHostToDevice));
+      GB_CUDA(cudaMemcpy(g.vz, vz, b, cudaMemcpyHostToDevice));
+    }
+    return (int)GB_OK;
+  });
+}
+
+int gb_download_state(double* x, double* y, double* z, double* vx, double* vy, double* vz, double* fx, double* fy,
+                      double* fz) {
+  return guarded([&]() {
+    const size_t b = sizeof(double) * g.natms;
+    if (x) GB_CUDA(cudaMemcpyAsync(x, g.x, b, cudaMemcpyDeviceToHost, g.stream));
+    if (y) GB_CUDA(cudaMemcpyAsync(y, g.y, b, cudaMemcpyDeviceToHost, g.stream));
+    if (z) GB_CUDA(cudaMemcpyAsync(z, g.z, b, cudaMemcpyDeviceToHost, g.stream));
+    if (vx) GB_CUDA(cudaMemcpyAsync(vx, g.vx, b, cudaMemcpyDeviceToHost, g.stream));
+    if (vy) GB_CUDA(cudaMemcpyAsync(vy, g.vy, b, cudaMemcpyDeviceToHost, g.stream));
+    if (vz) GB_CUDA(cudaMemcpyAsync(vz, g.vz, b, cudaMemcpyDeviceToHost, g.stream));
+    if (fx) GB_CUDA(cudaMemcpyAsync(fx, g.fx, b, cudaMemcpyDeviceToHost, g.stream));
+    if (fy) GB_CUDA(cudaMemcpyAsync(fy, g.fy, b, cudaMemcpyDeviceToHost, g.stream));
+    if (fz) GB_CUDA(cudaMemcpyAsync(fz, g.fz, b, cudaMemcpyDeviceToHost, g.stream));
+    GB_CUDA(cudaStreamSynchronize(g.stream));
+    return (int)GB_OK;
+  });
+}
+
+int gb_download_parts(void* parts, double* vx, double* vy, double* vz) {
+  return guarded([&]() {
+    if (!parts) return (int)GB_ERR_ARG;
+    const int n = g.natms;
+    std::vector<double> a(7 * (size_t)n);
+    double* p[7] = {&a[0], &a[n], &a[2 * (size_t)n], &a[3 * (size_t)n], &a[4 * (size_t)n], &a[5 * (size_t)n],
+                    &a[6 * (size_t)n]};
+    const size_t b = sizeof(double) * n;
+    GB_CUDA(cudaMemcpy(p[0], g.x, b, cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemcpy(p[1], g.y, b, cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemcpy(p[2], g.z, b, cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemcpy(p[3], g.fx, b, cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemcpy(p[4], g.fy, b, cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemcpy(p[5], g.fz, b, cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemcpy(p[6], g.chge, b, cudaMemcpyDeviceToHost));
+    unsigned char* out = static_cast<unsigned char*>(parts);
+    for (int i = 0; i < n; ++i) {
+      double* r = reinterpret_cast<double*>(out + (size_t)i * 64);
+      for (int k = 0; k < 7; ++k) r[k] = p[k][i];
+    }
+    if (vx) GB_CUDA(cudaMemcpy(vx, g.vx, b, cudaMemcpyDeviceToHost));
+    if (vy) GB_CUDA(cudaMemcpy(vy, g.vy, b, cudaMemcpyDeviceToHost));
+    if (vz) GB_CUDA(cudaMemcpy(vz, g.vz, b, cudaMemcpyDeviceToHost));
+    return (int)GB_OK;
+  });
+}
+
+int gb_relocate(void) {
+  return guarded([&]() { return list_relocate_and_halo(); });
+}
+
+int gb_list_build(int32_t* list_out, int ldlist, int32_t* max_list_io) {
+  return guarded([&]() {
+    GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
+    int st = list_build();
+    if (st == GB_ERR_LIST_OVERFLOW) {
+      if (max_list_io) *max_list_io = g.hsc->ibig;
+      return st;
+    }
+    if (st) return st;
+    if (list_out) {
+      if (ldlist != g.ld) return (int)GB_ERR_ARG;
+      GB_CUDA(cudaMemcpy(list_out, g.list, sizeof(int) * (size_t)g.ld * g.natms, cudaMemcpyDeviceToHost));
+    }
+    return (int)GB_OK;
+  });
+}
+
+int gb_vnl_check(int32_t* update) {
+  return guarded([&]() {
+    int u = integ_vnl_check();
+    if (update) *update = u;
+    return (int)GB_OK;
+  });
+}
+
+int gb_refresh(int32_t* update) {
+  return guarded([&]() { return do_refresh(update); });
+}
+
+int gb_forces(double* eng_out, double* stress_out) {
+  return guarded([&]() { return compute_forces(eng_out, stress_out, true, true); });
+}
+
+int gb_spme(double* eng_rc, double* vir_rc, double* stress_out) {
+  return guarded([&]() {
+    double e8[8], s9[9];
+    int st = compute_forces(e8, s9, true, false);
+    if (eng_rc) *eng_rc = e8[0];
+    if (vir_rc) *vir_rc = e8[1];
+    if (stress_out) for (int k = 0; k < 9; ++k) stress_out[k] = s9[k];
+    return st;
+  });
+}
+
+int gb_real(double* eng_out, double* stress_out) {
+  return guarded([&]() {
+    double e8[8], s9[9];
+    int st = compute_forces(e8, s9, false, true);
+    if (eng_out) for (int k = 0; k < 6; ++k) eng_out[k] = e8[2 + k];
+    if (stress_out) for (int k = 0; k < 9; ++k) stress_out[k] = s9[k];
+    return st;
+  });
+}
+
+int gb_vv(int stage, double* strkin, double* engke, int32_t* iters, double* vircon, double* strcon) {
+  return guarded([&]() {
+    if (stage != 1 && stage != 2) return (int)GB_ERR_ARG;
+    GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
+    int it = 0;
+    integ_vv(stage, strkin, engke, &it, vircon, strcon);
+    if (iters) *iters = it;
+    return (int)GB_OK;
+  });
+}
+
+int gb_md_run(int nsteps, gb_step_stats* stats) {
+  return guarded([&]() {
+    if (nsteps < 0) return (int)GB_ERR_ARG;
+    double tl[5] = {0, 0, 0, 0, 0};
+    for (int s = 0; s < nsteps; ++s) {
+      gb_step_stats S;
+      std::memset(&S, 0, sizeof(S));
+      GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
+      GB_CUDA(cudaEventRecord(g.ev[0], g.stream));
+      int it = 0;
+      integ_vv(1, nullptr, nullptr, &it, &S.vircon, nullptr);
+      S.shake_iters = it;
+      GB_CUDA(cudaEventRecord(g.ev[1], g.stream));
+      int32_t upd = 0;
+      int st = do_refresh(&upd);
+      if (st) return st;
+      S.list_rebuilt = upd;
+      if (upd) {
+        st = list_build();
+        if (st) return st;
+      }
+      GB_CUDA(cudaEventRecord(g.ev[2], g.stream));
+      double e8[8], s9[9];
+      compute_forces(e8, s9, true, true);
+      GB_CUDA(cudaEventRecord(g.ev[3], g.stream));
+      S.engcpe_rc = e8[0]; S.vircpe_rc = e8[1]; S.engcpe_rl = e8[2]; S.vircpe_rl = e8[3];
+      S.engcpe_ex = e8[4]; S.vircpe_ex = e8[5]; S.engvdw = e8[6]; S.virvdw = e8[7];
+      for (int k = 0; k < 9; ++k) S.stress[k] = s9[k];
+      integ_vv(2, S.strkin, &S.engke, &it, nullptr, nullptr);
+      S.rattle_iters = it;
+      S.mts_full = 1;
+      GB_CUDA(cudaEventRecord(g.ev[4], g.stream));
+      GB_CUDA(cudaEventSynchronize(g.ev[4]));
+      float ms;
+      cudaEventElapsedTime(&ms, g.ev[1], g.ev[2]); tl[0] += ms;
+      cudaEventElapsedTime(&ms, g.ev[2], g.ev[3]); tl[1] += ms;
+      cudaEventElapsedTime(&ms, g.ev[0], g.ev[1]); tl[3] += ms;
+      cudaEventElapsedTime(&ms, g.ev[3], g.ev[4]); tl[3] += ms;
+      cudaEventElapsedTime(&ms, g.ev[0], g.ev[4]); tl[4] += ms;
+      if (stats) stats[s] = S;
+    }
+    for (int k = 0; k < 5; ++k) g.last_ms[k] = tl[k];
+    return (int)GB_OK;
+  });
+}
+
+int gb_mts_config(int k, double tol, int train_steps) {
+  return guarded([&]() {
+    if (k < 1) return (int)GB_ERR_ARG;
+    g.mts_k = k;
+    g.mts_tol = tol;
+    g.mts_train = train_steps;
+    return (int)GB_OK;
+  });
+}
+
+int gb_set_precision(int precision) {
+  return guarded([&]() {
+    if (precision != GB_FP64 && precision != GB_MIXED) return (int)GB_ERR_ARG;
+    bool was = g.precision;
+    g.precision = precision;
+    if (precision == GB_MIXED && was != GB_MIXED) list_full_build();
+    return (int)GB_OK;
+  });
+}
+
+int gb_last_timings(double* ms, int n) {
+  if (!ms) return GB_ERR_ARG;
+  for (int k = 0; k < n && k < 8; ++k) ms[k] = g.last_ms[k];
+  return GB_OK;
+}
+
+int64_t gb_kernel_launches(void) { return g.launches; }
+
+void gb_finalize(void) {
+  if (g.init || g.stream) free_all();
+}
+
+const char* gb_strerror(int status) {
+  switch (status) {
+    case GB_OK: return "success";
+    case GB_ERR_CUTOFF_CELL: return "cutoff_extended >= half of the minimum cell width (error 95)";
+    case GB_ERR_SHAKE: return "SHAKE did not converge (error 105)";
+    case GB_ERR_LIST_OVERFLOW: return "Verlet list overflow, max_list too small (error 106)";
+    case GB_ERR_LINK_CELLS: return "link cells per domain < 1 (error 307)";
+    case GB_ERR_UNSAFE: return "unsafe state (error 505)";
+    case GB_ERR_RATTLE: return "RATTLE did not converge (error 515)";
+    case GB_ERR_HALO: return "halo exceeds mxatms (error 56)";
+    case GB_ERR_NOT_INIT: return "library not initialised (gb_init)";
+    case GB_ERR_CUDA: return "CUDA runtime error";
+    case GB_ERR_ARG: return "invalid argument";
+    case GB_ERR_NO_DEVICE: return "no CUDA device";
+    case GB_ERR_NONFINITE: return "non-finite positions";
+    default: return "unknown status";
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,252 @@
+// gb_common.cuh - shared device context, error handling and small device
+// helpers for the GB300 DL_POLY force/update path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <vector>
+
+#include "../../include/gb300_dlpoly.h"
+
+#define GB_WARP 32
+
+// Status word bits written by kernels (read back by the host after a stage).
+enum : int {
+  ST_LIST_OVERFLOW = 1,
+  ST_HALO_OVERFLOW = 2,
+  ST_SHAKE_FAIL = 4,
+  ST_RATTLE_FAIL = 8,
+  ST_NONFINITE = 16,
+  ST_CELL_RANGE = 32,
+  ST_SPME_RANGE = 64,
+};
+
+// Device-resident scalars: one small block so a single copy returns them all.
+struct DevScalars {
+  int nlast;        // local + halo atoms
+  int nlast_prev;   // halo size before the current export direction
+  int status;       // ST_* bits
+  int ibig;         // largest list length seen (overflow report)
+  int update;       // vnl_check decision
+  int shake_iters;
+  int rattle_iters;
+  int converged;    // constraint iteration flag
+  int ncand_fp64;   // list-build candidates resolved in FP64
+  int pad[7];
+  double maxdisp;   // largest displacement since the last rebuild
+  double acc[64];   // energy / virial / stress accumulators
+};
+
+// accumulator slots in DevScalars::acc
+enum {
+  A_PAIR = 0,         // 10 slots: engvdw, virvdw, engrl, virrl, stress(6)
+  A_EXCL = 10,        // 8 slots: engex, virex, stress(6)
+  A_SPME_STR = 20,    // 6 slots: reciprocal stress (before scale)
+  A_GATHER = 30,      // 4 slots: reciprocal energy, net force (before scale)
+  A_STRKIN = 40,      // 6 slots
+  A_STRCON = 50,      // 6 slots
+  A_NSLOTS = 64
+};
+
+// All device pointers of the context.  Arrays of size mxatms hold local atoms
+// in [0, natms) followed by halo images in [natms, nlast).
+struct Dev {
+  bool init = false;
+  gb_params p{};
+  int natms = 0, mxatms = 0;
+  double cell[9], rcell[9], celprp[10], volm = 0, rcutx = 0;
+  bool cubic = true;
+  int precision = GB_FP64;
+  cudaStream_t stream = nullptr;
+  int nsm = 0;
+  int64_t launches = 0;
+
+  // atoms
+  double *x = nullptr, *y = nullptr, *z = nullptr;  // mxatms
+  float4* xf = nullptr;                             // FP32 copy (x,y,z,q) for prefilter / mixed
+  double *fx = nullptr, *fy = nullptr, *fz = nullptr;  // natms, FP64 forces
+  long long* fixp = nullptr;                        // 3*natms fixed-point forces (mixed)
+  double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+  double *chge = nullptr, *weight = nullptr;        // mxatms
+  int *ltype = nullptr, *ltg = nullptr, *lfrzn = nullptr;  // mxatms
+  int *ixyz = nullptr, *src = nullptr;              // mxatms
+  int* shcode = nullptr;                            // halo shift code (sx+1)+3(sy+1)+9(sz+1)
+  double *xbg = nullptr, *ybg = nullptr, *zbg = nullptr;  // natms
+  double *ox = nullptr, *oy = nullptr, *oz = nullptr;     // natms (SHAKE)
+
+  // link cells / list
+  int nlx = 0, nly = 0, nlz = 0, nlp = 0, NX = 0, NY = 0, NZ = 0, ncells = 0, nsbcll = 0;
+  int* which_cell = nullptr;   // mxatms
+  int* cell_count = nullptr;   // ncells+2
+  int* cell_start = nullptr;   // ncells+2 (0-based start)
+  int* cell_fill = nullptr;    // ncells+2
+  int* at_list = nullptr;      // mxatms (sorted atom ids)
+  int* sorted_pos = nullptr;   // mxatms: position of atom in at_list
+  double4_32a* xs = nullptr;       // mxatms sorted FP64 coordinates (x,y,z,pad)
+  float4* xsf = nullptr;       // mxatms sorted FP32 coordinates
+  int* list = nullptr;         // (max_list+4) * natms, Fortran layout, 1-based values
+  int ld = 0;
+  int cells_alloc = 0;
+  int* blk = nullptr;          // scan scratch (blocks)
+  int nblk_alloc = 0;
+  int* list_excl = nullptr;    // (max_exclude+1)*natms
+  bool lbook = false;
+  int megfrz = 0;
+  // mixed-precision full list (derived, transposed by atom)
+  int* flist = nullptr;        // full list entries
+  int* fcount = nullptr;       // per atom count
+  int* fstart = nullptr;       // per atom start
+  long long flist_cap = 0;
+
+  // tables
+  int nsamples = 0, max_grid = 0, nkey = 0;
+  double erfc_rdr = 0, vdw_rdr = 0;
+  double* erfc_coef = nullptr;   // per interval: e0,e1,e2,d0,d1,d2 (erfc/r and its derivative)
+  float* erfc_coef_f = nullptr;
+  double* vdw_coef = nullptr;    // per key per interval: f0,f1,f2,v0,v1,v2
+  float* vdw_coef_f = nullptr;
+  int* vdw_kind = nullptr;
+  double* vdw_eps = nullptr;
+  double* vdw_sig = nullptr;
+  std::vector<int> h_vdw_kind;
+  std::vector<double> h_vdw_eps, h_vdw_sig;
+  double elrc = 0, vlrc = 0, self_interaction = 0, scaling = 0;
+
+  // SPME
+  int K1 = 0, K2 = 0, K3 = 0, B1 = 0, B2 = 0, B3 = 0, nb1 = 0, nb2 = 0, nb3 = 0, nbricks = 0;
+  double* spl = nullptr;       // natms * 3 * p spread splines (floor convention)
+  int* nidx = nullptr;         // natms * 3 grid indices
+  int* brick_of = nullptr;     // natms
+  int* brick_count = nullptr;  // nbricks+1
+  int* brick_start = nullptr;
+  int* brick_fill = nullptr;
+  int* brick_atoms = nullptr;  // natms sorted by brick
+  double* Q = nullptr;         // real charge grid K1*K2*K3
+  double2* G = nullptr;        // complex grid K1*K2*K3
+  float* Qf = nullptr;
+  float2* Gf = nullptr;
+  double* theta = nullptr;     // influence function (FP64, precomputed)
+  double* psi = nullptr;       // theta * (-2(1+f^2)/k^2) for the stress
+  float* theta_f = nullptr;
+  float* psi_f = nullptr;
+  double2* tw1 = nullptr;      // twiddles per dimension (K_d entries, e^{+2 pi i t/K})
+  double2* tw2 = nullptr;
+  double2* tw3 = nullptr;
+  float2 *tw1f = nullptr, *tw2f = nullptr, *tw3f = nullptr;
+  double* fspme = nullptr;     // 3*natms reciprocal forces (before scale, net removal)
+  double* blkacc = nullptr;    // per-block partial accumulators
+  int blkacc_n = 0;
+  double* ncombk = nullptr;
+
+  // constraints
+  int ntcons = 0;
+  int *con_i = nullptr, *con_j = nullptr;
+  double* con_d0 = nullptr;
+  double *dxx = nullptr, *dyy = nullptr, *dzz = nullptr;
+  double *dxt = nullptr, *dyt = nullptr, *dzt = nullptr, *dt2 = nullptr, *gam = nullptr;
+  int* listot = nullptr;
+  int *acon_start = nullptr, *acon_list = nullptr;  // per-atom constraint CSR (ordered by k)
+  double *cxt = nullptr, *cyt = nullptr, *czt = nullptr;  // per-atom corrections
+
+  DevScalars* sc = nullptr;    // device scalars
+  DevScalars* hsc = nullptr;   // pinned host mirror
+
+  // timing
+  cudaEvent_t ev[8];
+  double last_ms[8];
+
+  // learned MTS
+  int mts_k = 1;
+  double mts_tol = 1e-4;
+  int mts_train = 0;
+  void* mts = nullptr;
+};
+
+extern Dev g;
+
+#define GB_CUDA(call)                                                              \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      std::fprintf(stderr, "gb300: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), \
+                   __FILE__, __LINE__);                                            \
+      throw (int)GB_ERR_CUDA;                                                      \
+    }                                                                              \
+  } while (0)
+
+#define GB_LAUNCHED() \
+  do {                \
+    ++g.launches;     \
+    GB_CUDA(cudaGetLastError()); \
+  } while (0)
+
+// ------------------------------------------------------------ device helpers
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ int warp_sumi(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Exact-rounding FP64 helpers (never contracted into FMA): used wherever the
+// result must match the FP64 oracle bit for bit (binning, pair-set tests).
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// Block-wide reduction of NV doubles into per-block slots out[blockIdx.x*NV + k].
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* out) {
+  __shared__ double red[32][NV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) red[wid][k] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = lane < nw ? red[lane][k] : 0.0;
+      t = warp_sum(t);
+      if (lane == 0) out[(size_t)blockIdx.x * NV + k] = t;
+    }
+  }
+}
+
+// host helpers implemented in gb_api.cu
+void gb_sync_scalars();           // copy device scalars to the pinned mirror (synchronises)
+double* gb_blkacc(int n);         // per-block accumulator scratch with n doubles
+void gb_reduce_blocks(const double* blk, int nblocks, int nv, double* out_dev);  // sums into out_dev[0..nv)
+int* gb_scan_scratch(int n);
+
+// module entry points (host)
+int list_relocate_and_halo();     // pbcshift + halo + vnl_set_check (gb_list.cu)
+int list_refresh_halo();          // refresh halo positions (gb_list.cu)
+int list_build();                 // binning + pairs (gb_list.cu)
+void list_setup();                // link-cell geometry (gb_list.cu)
+void list_full_build();           // derived full list for the mixed path
+void list_pos_f32();              // FP32 copy of positions and charges (mixed path)
+void scan_exclusive(const int* in, int* out, int n);
+void pair_forces(double* eng6, double* stress9);  // gb_pair.cu (adds into forces)
+void spme_setup();                // gb_spme.cu
+void spme_forces(double* eng_rc, double* vir_rc, double* stress9);  // adds into forces
+void integ_vv(int stage, double* strkin, double* engke, int* iters, double* vircon, double* strcon);
+int integ_vnl_check();
+void integ_zero_forces();
+void integ_forces_to_fp64();      // mixed: fixed point -> FP64 forces
+void integ_setup_constraints(const int32_t* listcon, const double* prmcon);

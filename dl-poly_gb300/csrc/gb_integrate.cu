@@ -1,0 +1,402 @@
+// gb_integrate.cu - NVE velocity Verlet, SHAKE/RATTLE, kinetic stress and the
+// Verlet-list displacement check on the device.
+//
+// Follows:
+//   nve_0_vv            source/nve.F90:38-235 (stage 1 :131-174, stage 2 :198-217)
+//   constraints_tags    source/constraints.F90:438-586
+//   constraints_shake_vv source/constraints.F90:777-1030, apply_shake :1071-1200
+//   constraints_rattle  source/constraints.F90:587-775, apply_rattle :1032-1069
+//   kinstress           source/kinetics.F90:218-262
+//   vnl_check           source/neighbours.F90:123-296
+// SHAKE and RATTLE are Jacobi iterations with one global convergence test per
+// sweep, exactly as the reference: a cooperative-grid kernel runs the sweeps
+// with grid-wide barriers, at most shake_maxit of them, and returns the
+// iteration count and a status bit instead of spinning.  Per-atom corrections
+// are summed in constraint order from a per-atom constraint table, and applied
+// listot(i) times, so positions round as the reference's do.
+#include <cooperative_groups.h>
+
+#include <cfloat>
+
+#include "gb_common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace {
+
+inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+__device__ __forceinline__ double image1(double d, double c, double a) {
+  // images, cubic branch (numerics.F90:1527-1532): d - c*Anint(a*d)
+  return sub_rn(d, mul_rn(c, round(mul_rn(a, d))));
+}
+
+__global__ void k_vv1(int n, double hstep, double tstep, const double* w, const double* fx, const double* fy,
+                      const double* fz, double* vx, double* vy, double* vz, double* x, double* y, double* z) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (w[i] > 1.0e-6) {
+    double tmp = hstep / w[i];
+    vx[i] = vx[i] + tmp * fx[i];
+    vy[i] = vy[i] + tmp * fy[i];
+    vz[i] = vz[i] + tmp * fz[i];
+    x[i] = x[i] + tstep * vx[i];
+    y[i] = y[i] + tstep * vy[i];
+    z[i] = z[i] + tstep * vz[i];
+  }
+}
+
+__global__ void k_vv2(int n, double hstep, const double* w, const double* fx, const double* fy, const double* fz,
+                      double* vx, double* vy, double* vz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (w[i] > 1.0e-6) {
+    double tmp = hstep / w[i];
+    vx[i] = vx[i] + tmp * fx[i];
+    vy[i] = vy[i] + tmp * fy[i];
+    vz[i] = vz[i] + tmp * fz[i];
+  }
+}
+
+__global__ void k_kinstress(int n, const double* w, const int* lfrzn, const double* vx, const double* vy,
+                            const double* vz, double* blk) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  if (i < n && lfrzn[i] == 0) {
+    double m = w[i];
+    a[0] = m * vx[i] * vx[i]; a[1] = m * vx[i] * vy[i]; a[2] = m * vx[i] * vz[i];
+    a[3] = m * vy[i] * vy[i]; a[4] = m * vy[i] * vz[i]; a[5] = m * vz[i] * vz[i];
+  }
+  block_reduce_store<6>(a, blk);
+}
+
+// largest |r - r_checkpoint| with minimum image; doubles >= 0 order as their bits
+__global__ void k_maxdisp(int n, const double* x, const double* y, const double* z, const double* xb,
+                          const double* yb, const double* zb, double c0, double a0, unsigned long long* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double r = 0.0;
+  if (i < n) {
+    double dx = image1(x[i] - xb[i], c0, a0), dy = image1(y[i] - yb[i], c0, a0), dz = image1(z[i] - zb[i], c0, a0);
+    r = sqrt(dx * dx + dy * dy + dz * dz);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(r));
+}
+
+__global__ void k_zero3(int n, double* a, double* b, double* c) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) { a[i] = 0.0; b[i] = 0.0; c[i] = 0.0; }
+}
+
+__global__ void k_fix_to_fp64(int n, const long long* fixp, double* fx, double* fy, double* fz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double s = 1.0 / 1099511627776.0;
+  fx[i] = (double)fixp[3 * i] * s;
+  fy[i] = (double)fixp[3 * i + 1] * s;
+  fz[i] = (double)fixp[3 * i + 2] * s;
+}
+
+// constraints_tags: bond vectors at the start of the stage (min image)
+__global__ void k_con_tags(int nc, const int* ci, const int* cj, const double* x, const double* y, const double* z,
+                           double c0, double a0, double* dxx, double* dyy, double* dzz) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  int i = ci[k], j = cj[k];
+  dxx[k] = image1(x[i] - x[j], c0, a0);
+  dyy[k] = image1(y[i] - y[j], c0, a0);
+  dzz[k] = image1(z[i] - z[j], c0, a0);
+}
+
+struct ConArgs {
+  int nc, natms, maxit;
+  const int *ci, *cj, *listot, *astart, *alist, *lfrzn;
+  const double* d0;
+  double *dxx, *dyy, *dzz, *dxt, *dyt, *dzt, *dt2, *gam;
+  double *x, *y, *z, *vx, *vy, *vz;
+  const double* w;
+  double tstep, tol, c0, a0;
+  int* flags;      // maxit+1 ints, zeroed
+  DevScalars* sc;
+  double* blk;     // per-block stress partials (6)
+};
+
+// constraints_shake_vv: Jacobi sweeps until every |d^2 - d0^2|/2 < tol*d0
+__global__ void k_shake(ConArgs A) {
+  cg::grid_group grid = cg::this_grid();
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nth = gridDim.x * blockDim.x;
+  const double tstep2 = A.tstep * A.tstep;
+  double st[6] = {0, 0, 0, 0, 0, 0};
+  int it = 0;
+  bool safe = false;
+  while (!safe && it < A.maxit) {
+    ++it;
+    for (int k = tid; k < A.nc; k += nth) {
+      int i = A.ci[k], j = A.cj[k];
+      double dx = image1(A.x[i] - A.x[j], A.c0, A.a0);
+      double dy = image1(A.y[i] - A.y[j], A.c0, A.a0);
+      double dz = image1(A.z[i] - A.z[j], A.c0, A.a0);
+      A.dxt[k] = dx; A.dyt[k] = dy; A.dzt[k] = dz;
+      double d0 = A.d0[k];
+      double d2 = dx * dx + dy * dy + dz * dz - d0 * d0;
+      A.dt2[k] = d2;
+      if (!(0.5 * fabs(d2) < A.tol * d0)) A.flags[it] = 1;
+    }
+    grid.sync();
+    safe = (A.flags[it] == 0);
+    if (!safe) {
+      for (int k = tid; k < A.nc; k += nth) {
+        int i = A.ci[k], j = A.cj[k];
+        double amti = tstep2 / A.w[i], amtj = tstep2 / A.w[j];
+        if (A.lfrzn[i] != 0) amti = 0.0;
+        if (A.lfrzn[j] != 0) amtj = 0.0;
+        double gamma = A.dt2[k] / ((amti + amtj) * (A.dxx[k] * A.dxt[k] + A.dyy[k] * A.dyt[k] + A.dzz[k] * A.dzt[k]));
+        A.gam[k] = gamma;
+        st[0] -= gamma * A.dxx[k] * A.dxx[k]; st[1] -= gamma * A.dxx[k] * A.dyy[k];
+        st[2] -= gamma * A.dxx[k] * A.dzz[k]; st[3] -= gamma * A.dyy[k] * A.dyy[k];
+        st[4] -= gamma * A.dyy[k] * A.dzz[k]; st[5] -= gamma * A.dzz[k] * A.dzz[k];
+      }
+      grid.sync();
+      for (int i = tid; i < A.natms; i += nth) {
+        const int s = A.astart[i], e = A.astart[i + 1];
+        if (s == e || A.lfrzn[i] != 0) continue;
+        double xt = 0.0, yt = 0.0, zt = 0.0;
+        const double amt = tstep2 / A.w[i];
+        for (int t = s; t < e; ++t) {
+          int code = A.alist[t];
+          int k = code >> 1;
+          double g = A.gam[k];
+          double f = (code & 1) ? 0.5 * g * amt : -0.5 * g * amt;
+          xt += A.dxx[k] * f; yt += A.dyy[k] * f; zt += A.dzz[k] * f;
+        }
+        const double dli = 1.0 / (double)A.listot[i];
+        double px = A.x[i], py = A.y[i], pz = A.z[i];
+        for (int r = 0; r < A.listot[i]; ++r) { px += xt * dli; py += yt * dli; pz += zt * dli; }
+        A.x[i] = px; A.y[i] = py; A.z[i] = pz;
+      }
+      grid.sync();
+    }
+  }
+  if (tid == 0) {
+    A.sc->shake_iters = it;
+    if (!safe) A.sc->status |= ST_SHAKE_FAIL;
+  }
+  block_reduce_store<6>(st, A.blk);
+}
+
+// constraints_rattle: normalise the bond vectors, then Jacobi sweeps on v
+__global__ void k_rattle(ConArgs A) {
+  cg::grid_group grid = cg::this_grid();
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nth = gridDim.x * blockDim.x;
+  for (int k = tid; k < A.nc; k += nth) {
+    double dis = 1.0 / sqrt(A.dxx[k] * A.dxx[k] + A.dyy[k] * A.dyy[k] + A.dzz[k] * A.dzz[k]);
+    A.dxx[k] *= dis; A.dyy[k] *= dis; A.dzz[k] *= dis;
+  }
+  grid.sync();
+  int it = 0;
+  bool safe = false;
+  while (!safe && it < A.maxit) {
+    ++it;
+    for (int k = tid; k < A.nc; k += nth) {
+      int i = A.ci[k], j = A.cj[k];
+      double amti = A.tstep / A.w[i], amtj = A.tstep / A.w[j];
+      if (A.lfrzn[i] != 0) amti = 0.0;
+      if (A.lfrzn[j] != 0) amtj = 0.0;
+      double gamma = A.dxx[k] * (A.vx[i] - A.vx[j]) + A.dyy[k] * (A.vy[i] - A.vy[j]) + A.dzz[k] * (A.vz[i] - A.vz[j]);
+      if (!(0.5 * A.tstep * fabs(gamma) < A.tol)) A.flags[it] = 1;
+      A.gam[k] = gamma / (amti + amtj);
+    }
+    grid.sync();
+    safe = (A.flags[it] == 0);
+    if (!safe) {
+      for (int i = tid; i < A.natms; i += nth) {
+        const int s = A.astart[i], e = A.astart[i + 1];
+        if (s == e || A.lfrzn[i] != 0) continue;
+        double xt = 0.0, yt = 0.0, zt = 0.0;
+        const double amt = A.tstep / A.w[i];
+        for (int t = s; t < e; ++t) {
+          int code = A.alist[t];
+          int k = code >> 1;
+          double g = A.gam[k];
+          double f = (code & 1) ? g * amt : -g * amt;
+          xt += A.dxx[k] * f; yt += A.dyy[k] * f; zt += A.dzz[k] * f;
+        }
+        const double dli = 1.0 / (double)A.listot[i];
+        double px = A.vx[i], py = A.vy[i], pz = A.vz[i];
+        for (int r = 0; r < A.listot[i]; ++r) { px += xt * dli; py += yt * dli; pz += zt * dli; }
+        A.vx[i] = px; A.vy[i] = py; A.vz[i] = pz;
+      }
+      grid.sync();
+    }
+  }
+  if (tid == 0) {
+    A.sc->rattle_iters = it;
+    if (!safe) A.sc->status |= ST_RATTLE_FAIL;
+  }
+}
+
+// apply_shake epilogue: v += dr/dt, f += dr/dt * m/(dt/2) for constrained atoms
+__global__ void k_shake_post(int n, const int* astart, const int* lfrzn, double rstep, double hstep, const double* w,
+                             const double* x, const double* y, const double* z, const double* ox, const double* oy,
+                             const double* oz, double* vx, double* vy, double* vz, double* fx, double* fy,
+                             double* fz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (astart[i + 1] == astart[i] || lfrzn[i] != 0) return;
+  double xt = (x[i] - ox[i]) * rstep, yt = (y[i] - oy[i]) * rstep, zt = (z[i] - oz[i]) * rstep;
+  vx[i] += xt; vy[i] += yt; vz[i] += zt;
+  double tmp = w[i] / hstep;
+  fx[i] += xt * tmp; fy[i] += yt * tmp; fz[i] += zt * tmp;
+}
+
+__global__ void k_copy3(int n, const double* a, const double* b, const double* c, double* oa, double* ob, double* oc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) { oa[i] = a[i]; ob[i] = b[i]; oc[i] = c[i]; }
+}
+
+int* d_flags = nullptr;
+int coop_blocks_shake = 0, coop_blocks_rattle = 0;
+
+}  // namespace
+
+// ===================================================================== host
+void integ_setup_constraints(const int32_t* listcon, const double* prmcon) {
+  const int nc = g.ntcons;
+  if (nc == 0) return;
+  std::vector<int> ci(nc), cj(nc), lt(g.natms, 0);
+  std::vector<double> d0(nc);
+  for (int k = 0; k < nc; ++k) {
+    ci[k] = listcon[3 * k + 1] - 1;
+    cj[k] = listcon[3 * k + 2] - 1;
+    d0[k] = prmcon[listcon[3 * k] - 1];
+    lt[ci[k]]++; lt[cj[k]]++;
+  }
+  // per-atom constraint table in constraint order; bit 0 = atom is the j end
+  std::vector<int> start(g.natms + 1, 0), list;
+  for (int i = 0; i < g.natms; ++i) start[i + 1] = start[i] + lt[i];
+  list.resize(start[g.natms]);
+  std::vector<int> fill(g.natms, 0);
+  for (int k = 0; k < nc; ++k) {
+    list[start[ci[k]] + fill[ci[k]]++] = (k << 1) | 0;
+    list[start[cj[k]] + fill[cj[k]]++] = (k << 1) | 1;
+  }
+  GB_CUDA(cudaMalloc(&g.con_i, sizeof(int) * nc));
+  GB_CUDA(cudaMalloc(&g.con_j, sizeof(int) * nc));
+  GB_CUDA(cudaMalloc(&g.con_d0, sizeof(double) * nc));
+  GB_CUDA(cudaMalloc(&g.listot, sizeof(int) * g.natms));
+  GB_CUDA(cudaMalloc(&g.acon_start, sizeof(int) * (g.natms + 1)));
+  GB_CUDA(cudaMalloc(&g.acon_list, sizeof(int) * std::max<size_t>(1, list.size())));
+  for (double** p : {&g.dxx, &g.dyy, &g.dzz, &g.dxt, &g.dyt, &g.dzt, &g.dt2, &g.gam})
+    GB_CUDA(cudaMalloc(p, sizeof(double) * nc));
+  GB_CUDA(cudaMemcpy(g.con_i, ci.data(), sizeof(int) * nc, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(g.con_j, cj.data(), sizeof(int) * nc, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(g.con_d0, d0.data(), sizeof(double) * nc, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(g.listot, lt.data(), sizeof(int) * g.natms, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(g.acon_start, start.data(), sizeof(int) * (g.natms + 1), cudaMemcpyHostToDevice));
+  if (!list.empty())
+    GB_CUDA(cudaMemcpy(g.acon_list, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMalloc(&d_flags, sizeof(int) * (g.p.shake_maxit + 2)));
+  int bps = 0;
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_shake, 256, 0));
+  coop_blocks_shake = std::max(1, std::min(bps * g.nsm, nblocks(std::max(nc, g.natms), 256)));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_rattle, 256, 0));
+  coop_blocks_rattle = std::max(1, std::min(bps * g.nsm, nblocks(std::max(nc, g.natms), 256)));
+}
+
+void integ_zero_forces() {
+  if (g.precision == GB_FP64) {
+    k_zero3<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, g.fx, g.fy, g.fz);
+    GB_LAUNCHED();
+  } else {
+    GB_CUDA(cudaMemsetAsync(g.fixp, 0, sizeof(long long) * 3 * (size_t)g.natms, g.stream));
+  }
+}
+
+void integ_forces_to_fp64() {
+  k_fix_to_fp64<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, g.fixp, g.fx, g.fy, g.fz);
+  GB_LAUNCHED();
+}
+
+int integ_vnl_check() {
+  GB_CUDA(cudaMemsetAsync(&g.sc->maxdisp, 0, sizeof(double), g.stream));
+  k_maxdisp<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, g.x, g.y, g.z, g.xbg, g.ybg, g.zbg, g.cell[0],
+                                                          1.0 / g.cell[0], (unsigned long long*)&g.sc->maxdisp);
+  GB_LAUNCHED();
+  gb_sync_scalars();
+  return g.hsc->maxdisp >= std::nextafter(0.5, 0.0) * g.p.rpad ? 1 : 0;
+}
+
+static void con_args(ConArgs& A) {
+  A.nc = g.ntcons; A.natms = g.natms; A.maxit = g.p.shake_maxit;
+  A.ci = g.con_i; A.cj = g.con_j; A.listot = g.listot; A.astart = g.acon_start; A.alist = g.acon_list;
+  A.lfrzn = g.lfrzn; A.d0 = g.con_d0;
+  A.dxx = g.dxx; A.dyy = g.dyy; A.dzz = g.dzz; A.dxt = g.dxt; A.dyt = g.dyt; A.dzt = g.dzt;
+  A.dt2 = g.dt2; A.gam = g.gam;
+  A.x = g.x; A.y = g.y; A.z = g.z; A.vx = g.vx; A.vy = g.vy; A.vz = g.vz; A.w = g.weight;
+  A.tstep = g.p.tstep; A.tol = g.p.shake_tol; A.c0 = g.cell[0]; A.a0 = 1.0 / g.cell[0];
+  A.flags = d_flags; A.sc = g.sc; A.blk = nullptr;
+}
+
+void integ_vv(int stage, double* strkin, double* engke, int* iters, double* vircon, double* strcon) {
+  cudaStream_t st = g.stream;
+  const int n = g.natms;
+  const double tstep = g.p.tstep, hstep = 0.5 * tstep, rstep = 1.0 / tstep;
+  if (iters) *iters = 0;
+  if (g.ntcons > 0) {
+    k_con_tags<<<nblocks(g.ntcons, 256), 256, 0, st>>>(g.ntcons, g.con_i, g.con_j, g.x, g.y, g.z, g.cell[0],
+                                                         1.0 / g.cell[0], g.dxx, g.dyy, g.dzz);
+    GB_LAUNCHED();
+  }
+  if (stage == 1) {
+    k_vv1<<<nblocks(n, 256), 256, 0, st>>>(n, hstep, tstep, g.weight, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz, g.x, g.y, g.z);
+    GB_LAUNCHED();
+    if (g.ntcons > 0) {
+      k_copy3<<<nblocks(n, 256), 256, 0, st>>>(n, g.x, g.y, g.z, g.ox, g.oy, g.oz);
+      GB_LAUNCHED();
+      GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + 2), st));
+      ConArgs A;
+      con_args(A);
+      A.blk = gb_blkacc(coop_blocks_shake * 6);
+      void* args[] = {&A};
+      GB_CUDA(cudaLaunchCooperativeKernel((void*)k_shake, coop_blocks_shake, 256, args, 0, st));
+      GB_LAUNCHED();
+      gb_reduce_blocks(A.blk, coop_blocks_shake, 6, &g.sc->acc[A_STRCON]);
+      k_shake_post<<<nblocks(n, 256), 256, 0, st>>>(n, g.acon_start, g.lfrzn, rstep, hstep, g.weight, g.x, g.y, g.z,
+                                                     g.ox, g.oy, g.oz, g.vx, g.vy, g.vz, g.fx, g.fy, g.fz);
+      GB_LAUNCHED();
+      gb_sync_scalars();
+      if (iters) *iters = g.hsc->shake_iters;
+      const double* s = &g.hsc->acc[A_STRCON];
+      double str[9] = {s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]};
+      if (strcon) for (int k = 0; k < 9; ++k) strcon[k] = str[k];
+      if (vircon) *vircon = -(str[0] + str[4] + str[8]);
+      if (g.hsc->status & ST_SHAKE_FAIL) throw (int)GB_ERR_SHAKE;
+    }
+  } else {
+    k_vv2<<<nblocks(n, 256), 256, 0, st>>>(n, hstep, g.weight, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz);
+    GB_LAUNCHED();
+    if (g.ntcons > 0) {
+      GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + 2), st));
+      ConArgs A;
+      con_args(A);
+      void* args[] = {&A};
+      GB_CUDA(cudaLaunchCooperativeKernel((void*)k_rattle, coop_blocks_rattle, 256, args, 0, st));
+      GB_LAUNCHED();
+    }
+    const int nb = nblocks(n, 256);
+    double* blk = gb_blkacc(nb * 6);
+    k_kinstress<<<nb, 256, 0, st>>>(n, g.weight, g.lfrzn, g.vx, g.vy, g.vz, blk);
+    GB_LAUNCHED();
+    gb_reduce_blocks(blk, nb, 6, &g.sc->acc[A_STRKIN]);
+    gb_sync_scalars();
+    if (iters && g.ntcons > 0) *iters = g.hsc->rattle_iters;
+    const double* s = &g.hsc->acc[A_STRKIN];
+    double sk[9] = {s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]};
+    if (strkin) for (int k = 0; k < 9; ++k) strkin[k] = sk[k];
+    if (engke) *engke = 0.5 * (sk[0] + sk[4] + sk[8]);
+    if (g.ntcons > 0 && (g.hsc->status & ST_RATTLE_FAIL)) throw (int)GB_ERR_RATTLE;
+  }
+}

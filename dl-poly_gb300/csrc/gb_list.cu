@@ -1,0 +1,722 @@
+// gb_list.cu - halo images and the link-cell Verlet list on the device.
+//
+// Follows, in serial (one-domain) semantics:
+//   pbcshift            source/numerics.F90:1851-1907
+//   set_halo_particles  source/halo.F90:153-356 (+ export_atomic_data deport_data.F90:1673-1900)
+//   refresh_halo_positions source/halo.F90:47-114
+//   link_cell_pairs     source/neighbours.F90:356-1414
+// Every quantity that decides membership (cell index, halo flag, rsq <= rcsq)
+// is computed with explicitly rounded FP64 operations (no FMA contraction) in
+// the reference's operation order, so the pair set is bit-identical to the
+// FP64 oracle.  Distance tests run first in FP32 with a proven error margin;
+// only candidates inside the margin band are re-tested in exact FP64.
+#include <cfloat>
+#include <cmath>
+
+#include "gb_common.cuh"
+
+namespace {
+
+constexpr int SCAN_BLOCK = 1024;
+constexpr int MAX_SBC = 1024;  // semi-ball offsets capacity
+
+__constant__ int c_off[MAX_SBC];   // linear cell offset of each semi-ball cell
+__constant__ int c_nix[MAX_SBC], c_niy[MAX_SBC], c_niz[MAX_SBC];
+__constant__ unsigned char c_nir[MAX_SBC];
+
+struct HaloGeom {
+  double rc[9];
+  double ecw[3], cw[3];
+};
+
+struct CellGeom {
+  double rc[9];
+  double xdc, ydc, zdc;
+  int nlp, nlx, nly, nlz, NX, NY, NZ;
+  double rcsq;
+  float rcsq_lo, rcsq_hi;
+  double half_plus;
+};
+
+HaloGeom h_halo;
+CellGeom h_cg;
+double h_add[6][3];  // export add vectors for mdir -1,1,-2,2,-3,3
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_pbcshift(int n, double* x, double* y, double* z, double a0, double a4, double a8,
+                           double c0, double c4, double c8, double half_minus) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double xss = mul_rn(a0, x[i]), yss = mul_rn(a4, y[i]), zss = mul_rn(a8, z[i]);
+  xss = sub_rn(xss, round(xss)); if (xss >= half_minus) xss = -xss;
+  yss = sub_rn(yss, round(yss)); if (yss >= half_minus) yss = -yss;
+  zss = sub_rn(zss, round(zss)); if (zss >= half_minus) zss = -zss;
+  x[i] = mul_rn(c0, xss);
+  y[i] = mul_rn(c4, yss);
+  z[i] = mul_rn(c8, zss);
+}
+
+__device__ __forceinline__ double red_coord(const double* rc, int d, double x, double y, double z) {
+  return add_rn(add_rn(mul_rn(rc[d], x), mul_rn(rc[d + 3], y)), mul_rn(rc[d + 6], z));
+}
+
+__global__ void k_halo_flags(int n, const double* x, const double* y, const double* z, HaloGeom hg,
+                             int* ixyz, int* src, int* shcode, DevScalars* sc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) { sc->nlast = n; sc->nlast_prev = n; }
+  if (i >= n) return;
+  double xx = red_coord(hg.rc, 0, x[i], y[i], z[i]);
+  double yy = red_coord(hg.rc, 1, x[i], y[i], z[i]);
+  double zz = red_coord(hg.rc, 2, x[i], y[i], z[i]);
+  int v = 0;
+  if (xx <= hg.ecw[0]) v += 1;
+  if (xx >= hg.cw[0]) v += 2;
+  if (yy <= hg.ecw[1]) v += 10;
+  if (yy >= hg.cw[1]) v += 20;
+  if (zz <= hg.ecw[2]) v += 100;
+  if (zz >= hg.cw[2]) v += 200;
+  ixyz[i] = v;
+  src[i] = i;
+  shcode[i] = 13;
+}
+
+__device__ __forceinline__ bool export_sel(int v, int kx, int ky, int kz, int jxyz) {
+  if (v <= 0) return false;
+  int ix = v % 10;
+  int iy = (v - ix) % 100;
+  int iz = (v - (ix + iy)) % 1000;
+  int j = ix * kx + iy * ky + iz * kz;
+  return (j == jxyz) || (j > jxyz && j % 3 == 0);
+}
+
+__global__ void k_export_count(const int* ixyz, const DevScalars* sc, int kx, int ky, int kz, int jxyz,
+                               int* blkcount) {
+  const int n = sc->nlast;
+  const int base = blockIdx.x * SCAN_BLOCK;
+  int cnt = 0;
+  for (int t = threadIdx.x; t < SCAN_BLOCK; t += blockDim.x) {
+    int i = base + t;
+    if (i < n && export_sel(ixyz[i], kx, ky, kz, jxyz)) ++cnt;
+  }
+  cnt = warp_sumi(cnt);
+  __shared__ int s[32];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s[w];
+    blkcount[blockIdx.x] = tot;
+  }
+}
+
+// Exclusive scan of n ints in a single block (n up to a few million).
+__global__ void k_scan_single(const int* in, int* out, int n, int* total) {
+  __shared__ int part[1024];
+  const int T = blockDim.x;
+  const int per = (n + T - 1) / T;
+  const int b = threadIdx.x * per;
+  int s = 0;
+  for (int k = 0; k < per; ++k) if (b + k < n) s += in[b + k];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < T; o <<= 1) {
+    int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = part[threadIdx.x] - s;
+  for (int k = 0; k < per; ++k)
+    if (b + k < n) { out[b + k] = run; run += in[b + k]; }
+  if (threadIdx.x == T - 1 && total) *total = part[T - 1];
+}
+
+__global__ void k_export_commit(const int* blkcount, int nblk, int* blkoff, DevScalars* sc, int mxatms) {
+  // single thread: offsets were produced by k_scan_single into blkoff; grow nlast
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int tot = blkoff[nblk - 1] + blkcount[nblk - 1];
+  int n = sc->nlast;
+  sc->nlast_prev = n;
+  if (n + tot > mxatms) {
+    sc->status |= ST_HALO_OVERFLOW;
+    tot = mxatms - n;
+  }
+  sc->nlast = n + tot;
+}
+
+__global__ void k_export_write(double* x, double* y, double* z, int* ltg, int* src, int* shcode, int* ixyz,
+                               const int* blkoff, const DevScalars* sc, int kx, int ky, int kz, int jxyz,
+                               int kxyz, double ax, double ay, double az, int dshift, int mxatms) {
+  const int n = sc->nlast_prev;
+  const int base = blockIdx.x * SCAN_BLOCK;
+  __shared__ int wsum[32];
+  __shared__ int chunk_base;
+  if (threadIdx.x == 0) chunk_base = 0;
+  __syncthreads();
+  // process the block's 1024 items in chunks of blockDim, preserving order
+  for (int c = 0; c < SCAN_BLOCK; c += blockDim.x) {
+    int i = base + c + threadIdx.x;
+    int v = (i < n && c + threadIdx.x < SCAN_BLOCK) ? ixyz[i] : 0;
+    bool sel = (i < n) && export_sel(v, kx, ky, kz, jxyz);
+    unsigned m = __ballot_sync(0xffffffffu, sel);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int pre = __popc(m & ((1u << lane) - 1u));
+    if (lane == 0) wsum[w] = __popc(m);
+    __syncthreads();
+    int wpre = 0;
+    for (int k = 0; k < w; ++k) wpre += wsum[k];
+    if (sel) {
+      int dst = n + blkoff[blockIdx.x] + chunk_base + wpre + pre;
+      if (dst < mxatms) {
+        x[dst] = add_rn(x[i], ax);
+        y[dst] = add_rn(y[i], ay);
+        z[dst] = add_rn(z[i], az);
+        ltg[dst] = ltg[i];
+        src[dst] = src[i];
+        shcode[dst] = shcode[i] + dshift;
+        int ix = v % 10, iy = (v - ix) % 100, iz = (v - (ix + iy)) % 1000;
+        int j = ix * kx + iy * ky + iz * kz;
+        ixyz[dst] = v - (j == jxyz ? jxyz : kxyz);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += wsum[k];
+      chunk_base += t;
+    }
+    __syncthreads();
+  }
+}
+
+// halo properties from the local source atom
+__global__ void k_halo_props(int natms, const DevScalars* sc, const int* src, int* ltype, double* chge,
+                             double* weight, int* lfrzn) {
+  int i = natms + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= sc->nlast) return;
+  int s = src[i];
+  ltype[i] = ltype[s];
+  chge[i] = chge[s];
+  weight[i] = weight[s];
+  lfrzn[i] = lfrzn[s];
+}
+
+// refresh_halo_positions: the same export chain applied to the source position
+__global__ void k_halo_refresh(int natms, const DevScalars* sc, const int* src, const int* shcode, double* x,
+                               double* y, double* z, const double* adds /*6x3*/) {
+  int i = natms + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= sc->nlast) return;
+  int s = src[i], c = shcode[i];
+  int sx = c % 3 - 1, sy = (c / 3) % 3 - 1, sz = c / 9 - 1;
+  double xx = x[s], yy = y[s], zz = z[s];
+  // adds[0..2] is the -x export (image at +L), adds[3..5] the +x export (image at -L), etc.
+  if (sx != 0) { const double* a = adds + 3 * (sx > 0 ? 0 : 1); xx = add_rn(xx, a[0]); yy = add_rn(yy, a[1]); zz = add_rn(zz, a[2]); }
+  if (sy != 0) { const double* a = adds + 3 * (sy > 0 ? 2 : 3); xx = add_rn(xx, a[0]); yy = add_rn(yy, a[1]); zz = add_rn(zz, a[2]); }
+  if (sz != 0) { const double* a = adds + 3 * (sz > 0 ? 4 : 5); xx = add_rn(xx, a[0]); yy = add_rn(yy, a[1]); zz = add_rn(zz, a[2]); }
+  x[i] = xx; y[i] = yy; z[i] = zz;
+}
+
+__global__ void k_set_check(int n, const double* x, const double* y, const double* z, double* xb, double* yb,
+                            double* zb) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  xb[i] = x[i]; yb[i] = y[i]; zb[i] = z[i];
+}
+
+// ----------------------------------------------------------------- binning
+__global__ void k_bin(int natms, const DevScalars* sc, const double* x, const double* y, const double* z,
+                      CellGeom cg, int* which_cell, int* count) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nlast = sc->nlast;
+  if (i >= nlast) return;
+  const double xx = red_coord(cg.rc, 0, x[i], y[i], z[i]);
+  const double yy = red_coord(cg.rc, 1, x[i], y[i], z[i]);
+  const double zz = red_coord(cg.rc, 2, x[i], y[i], z[i]);
+  const int nlp = cg.nlp, jx0 = nlp, jy0 = nlp, jz0 = nlp;
+  const int nlx0e = nlp - 1, nly0e = nlp - 1, nlz0e = nlp - 1;
+  const int nlx1s = cg.nlx + nlp, nly1s = cg.nly + nlp, nlz1s = cg.nlz + nlp;
+  const int nlx1e = cg.nlx + 2 * nlp - 1, nly1e = cg.nly + 2 * nlp - 1, nlz1e = cg.nlz + 2 * nlp - 1;
+  int icell;
+  if (i < natms) {
+    int ix = __double2int_rz(mul_rn(cg.xdc, add_rn(xx, 0.5))) + jx0;
+    int iy = __double2int_rz(mul_rn(cg.ydc, add_rn(yy, 0.5))) + jy0;
+    int iz = __double2int_rz(mul_rn(cg.zdc, add_rn(zz, 0.5))) + jz0;
+    ix = max(min(ix, nlx1s - 1), nlx0e + 1);
+    iy = max(min(iy, nly1s - 1), nly0e + 1);
+    iz = max(min(iz, nlz1s - 1), nlz0e + 1);
+    icell = 1 + ix + cg.NX * (iy + cg.NY * iz);
+  } else {
+    double dx, dy, dz;
+    int ix, iy, iz;
+    if (xx > -cg.half_plus) { dx = mul_rn(cg.xdc, add_rn(xx, 0.5)); ix = __double2int_rz(dx) + jx0; }
+    else { dx = mul_rn(cg.xdc, fabs(add_rn(xx, 0.5))); ix = -__double2int_rz(dx) + jx0 - 1; }
+    if (yy > -cg.half_plus) { dy = mul_rn(cg.ydc, add_rn(yy, 0.5)); iy = __double2int_rz(dy) + jy0; }
+    else { dy = mul_rn(cg.ydc, fabs(add_rn(yy, 0.5))); iy = -__double2int_rz(dy) + jy0 - 1; }
+    if (zz > -cg.half_plus) { dz = mul_rn(cg.zdc, add_rn(zz, 0.5)); iz = __double2int_rz(dz) + jz0; }
+    else { dz = mul_rn(cg.zdc, fabs(add_rn(zz, 0.5))); iz = -__double2int_rz(dz) + jz0 - 1; }
+    if (ix >= 0 && iy >= 0 && iz >= 0) {
+      bool lx0 = ix > nlx0e, lx1 = ix < nlx1s, ly0 = iy > nly0e, ly1 = iy < nly1s, lz0 = iz > nlz0e, lz1 = iz < nlz1s;
+      if ((lx0 && lx1) && (ly0 && ly1) && (lz0 && lz1)) {
+        double x0 = fabs(sub_rn(dx, 0.0)), x1 = fabs(sub_rn(dx, (double)cg.nlx));
+        dx = fmin(x0, x1);
+        double y0 = fabs(sub_rn(dy, 0.0)), y1 = fabs(sub_rn(dy, (double)cg.nly));
+        dy = fmin(y0, y1);
+        double z0 = fabs(sub_rn(dz, 0.0)), z1 = fabs(sub_rn(dz, (double)cg.nlz));
+        dz = fmin(z0, z1);
+        if (dx <= dy && dx <= dz) {
+          ix = x0 < x1 ? nlx0e : nlx1s;
+          if (fabs(sub_rn(dx, dy)) < DBL_EPSILON) iy = y0 < y1 ? nly0e : nly1s;
+          if (fabs(sub_rn(dx, dz)) < DBL_EPSILON) iz = z0 < z1 ? nlz0e : nlz1s;
+        } else if (dy <= dx && dy <= dz) {
+          iy = y0 < y1 ? nly0e : nly1s;
+          if (fabs(sub_rn(dy, dz)) < DBL_EPSILON) iz = z0 < z1 ? nlz0e : nlz1s;
+        } else {
+          iz = z0 < z1 ? nlz0e : nlz1s;
+        }
+      }
+      bool out = ix < 0 || ix > nlx1e || iy < 0 || iy > nly1e || iz < 0 || iz > nlz1e;
+      icell = out ? 0 : 1 + ix + cg.NX * (iy + cg.NY * iz);
+    } else {
+      icell = 0;
+    }
+  }
+  which_cell[i] = icell;
+  atomicAdd(&count[icell], 1);
+}
+
+__global__ void k_cell_scatter(const DevScalars* sc, const int* which_cell, const int* start, int* fill,
+                               int* tmp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= sc->nlast) return;
+  int c = which_cell[i];
+  int slot = atomicAdd(&fill[c], 1);
+  tmp[start[c] + slot] = i;
+}
+
+// Stable order inside each cell (ascending atom index, as the reference's
+// counting sort over i = 1..nlast): rank of each member by counting.
+__global__ void k_cell_sort(int ncells_p1, const int* start, const int* tmp, int* at_list, int* sorted_pos,
+                            const double* x, const double* y, const double* z, double4_32a* xs, float4* xsf) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= ncells_p1) return;
+  int s = start[warp], e = start[warp + 1], n = e - s;
+  if (warp == 0) {  // residual halo cell: never a neighbour cell, order irrelevant
+    for (int a = lane; a < n; a += 32) {
+      int v = tmp[s + a];
+      at_list[s + a] = v;
+      sorted_pos[v] = s + a;
+      xs[s + a] = make_double4_32a(x[v], y[v], z[v], 0.0);
+      xsf[s + a] = make_float4((float)x[v], (float)y[v], (float)z[v], 0.0f);
+    }
+    return;
+  }
+  for (int a = lane; a < n; a += 32) {
+    int v = tmp[s + a];
+    int r = 0;
+    for (int b = 0; b < n; ++b) r += (tmp[s + b] < v);
+    int pos = s + r;
+    at_list[pos] = v;
+    sorted_pos[v] = pos;
+    double xv = x[v], yv = y[v], zv = z[v];
+    xs[pos] = make_double4_32a(xv, yv, zv, 0.0);
+    xsf[pos] = make_float4((float)xv, (float)yv, (float)zv, 0.0f);
+  }
+}
+
+// Half-shell Verlet list (neighbours.F90:876-1184): one warp per local atom.
+// Entries are appended in the reference order (semi-ball cell by cell, each
+// cell's members in ascending order), with ballot-based compaction.
+__global__ void __launch_bounds__(256) k_list_pairs(int natms, const DevScalars* sc_c, CellGeom cg, int nsbcll,
+                                                    const int* at_list, const int* which_cell, const int* start,
+                                                    const double4_32a* xs, const float4* xsf, int* list, int ld,
+                                                    int max_list, DevScalars* sc) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nlast = sc_c->nlast;
+  if (warp >= nlast) return;
+  const int p = warp;  // sorted position
+  const int i = at_list[p];
+  if (i >= natms) return;
+  const int ic = which_cell[i];
+  const int icm = ic - 1;
+  const int ix = icm % cg.NX;
+  const int iz = icm / (cg.NX * cg.NY);
+  const int iy = icm / cg.NX - cg.NY * iz;
+  const double4_32a xi = xs[p];
+  const float4 xif = xsf[p];
+  const int nlp = cg.nlp;
+  const int nlx0e = nlp - 1, nly0e = nlp - 1, nlz0e = nlp - 1;
+  const int nlx1s = cg.nlx + nlp, nly1s = cg.nly + nlp, nlz1s = cg.nlz + nlp;
+  int* li = list + (size_t)i * ld + 3;  // li[k] == list(k, i)
+  int count = 0;
+  int ncand64 = 0;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int pass = 1; pass <= 2; ++pass) {
+    if (pass == 2) {
+      const int ix1 = ix - nlx0e, ix2 = ix - nlx1s, iy1 = iy - nly0e, iy2 = iy - nly1s, iz1 = iz - nlz0e,
+                iz2 = iz - nlz1s;
+      bool border = (ix1 >= 1 && ix1 <= nlp) || (ix2 <= -1 && ix2 >= -nlp) || (iy1 >= 1 && iy1 <= nlp) ||
+                    (iy2 <= -1 && iy2 >= -nlp) || (iz1 >= 1 && iz1 <= nlp) || (iz2 <= -1 && iz2 >= -nlp);
+      if (!border) break;
+    }
+    for (int kk = (pass == 1 ? 0 : 1); kk < nsbcll; ++kk) {
+      int jc, s;
+      if (pass == 1) {
+        jc = ic + c_off[kk];
+        s = (jc != ic) ? start[jc] : p + 1;
+      } else {
+        int jx = ix - c_nix[kk], jy = iy - c_niy[kk], jz = iz - c_niz[kk];
+        if (!(jx <= nlx0e || jx >= nlx1s || jy <= nly0e || jy >= nly1s || jz <= nlz0e || jz >= nlz1s)) continue;
+        jc = ic - c_off[kk];
+        s = start[jc];
+      }
+      const int e = start[jc + 1];
+      const bool nir = c_nir[kk] != 0;
+      for (int b = s; b < e; b += 32) {
+        const int jj = b + lane;
+        bool acc = false;
+        if (jj < e) {
+          if (nir) {
+            acc = true;
+          } else {
+            float4 xj = xsf[jj];
+            float dx = xj.x - xif.x, dy = xj.y - xif.y, dz = xj.z - xif.z;
+            float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 < cg.rcsq_lo) {
+              acc = true;
+            } else if (r2 <= cg.rcsq_hi) {
+              double4_32a xd = xs[jj];
+              double ddx = sub_rn(xd.x, xi.x), ddy = sub_rn(xd.y, xi.y), ddz = sub_rn(xd.z, xi.z);
+              double rsq = add_rn(add_rn(mul_rn(ddx, ddx), mul_rn(ddy, ddy)), mul_rn(ddz, ddz));
+              acc = rsq <= cg.rcsq;
+              ++ncand64;
+            }
+          }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, acc);
+        if (acc) {
+          const int k = count + __popc(m & lt) + 1;
+          if (k <= max_list) li[k] = at_list[jj] + 1;
+        }
+        count += __popc(m);
+      }
+    }
+  }
+  ncand64 = warp_sumi(ncand64);
+  if (lane == 0) {
+    // the stored length never exceeds max_list, so no later kernel can read
+    // past the column even when the overflow status is ignored
+    const int stored = min(count, max_list);
+    li[0] = stored;
+    li[-1] = stored;
+    li[-2] = stored;
+    li[-3] = stored;
+    if (count > max_list) {
+      atomicOr(&sc->status, ST_LIST_OVERFLOW);
+      atomicMax(&sc->ibig, count);
+    }
+    if (ncand64) atomicAdd(&sc->ncand_fp64, ncand64);
+  }
+}
+
+// Frozen (neighbours.F90:1198-1225) and excluded (:1229-1306) reordering, one
+// thread per atom, sequential exactly as the reference swaps.
+__global__ void k_list_reorder(int natms, int* list, int ld, const int* lfrzn, const int* ltg,
+                               const int* list_excl, int ldx, int megfrz, int lbook) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natms) return;
+  int* li = list + (size_t)i * ld + 3;
+  int l_end = li[0], m_end = l_end;
+  if (megfrz > 1 && lfrzn[i] > 0) {
+    for (int kk = l_end; kk >= 1; --kk) {
+      int j = li[kk];
+      if (lfrzn[j - 1] > 0) {
+        if (kk < m_end) { li[kk] = li[m_end]; li[m_end] = j; }
+        --m_end;
+      }
+    }
+  }
+  li[-2] = li[0];
+  li[0] = m_end;
+  if (lbook) {
+    l_end = li[0];
+    m_end = l_end;
+    const int* ex = list_excl + (size_t)i * ldx;
+    int ii = ex[0];
+    if (ii > 0) {
+      for (int kk = l_end; kk >= 1; --kk) {
+        int j = li[kk];
+        int jj = ltg[j - 1];
+        bool hit = false;
+        for (int t = 1; t <= ii; ++t) hit |= (ex[t] == jj);
+        if (hit) {
+          if (kk < m_end) { li[kk] = li[m_end]; li[m_end] = j; }
+          --m_end;
+        }
+      }
+    }
+    li[-1] = li[0];
+    li[0] = m_end;
+    li[-3] = li[0];
+  } else {
+    li[-1] = li[0];
+    li[-3] = li[0];
+  }
+}
+
+// FP32 copy of positions + charge (mixed path and prefilter helpers)
+__global__ void k_pos_f32(const DevScalars* sc, const double* x, const double* y, const double* z,
+                          const double* q, float4* xf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= sc->nlast) return;
+  xf[i] = make_float4((float)x[i], (float)y[i], (float)z[i], (float)q[i]);
+}
+
+// ------------------------------------------------------ derived full list
+// Count, for every local atom, the entries of the full (symmetric) list: its
+// own half-list entries plus the reverse of every entry that names it.
+__global__ void k_full_count(int natms, const int* list, int ld, int* fcount) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= natms) return;
+  const int* li = list + (size_t)warp * ld + 3;
+  const int n = li[-1];  // non-frozen part incl. excluded (excluded are filtered below)
+  const int nx = li[0];
+  for (int k = lane; k < nx; k += 32) {
+    int j = li[k + 1] - 1;
+    if (j < natms) atomicAdd(&fcount[j], 1);
+  }
+  if (lane == 0) atomicAdd(&fcount[warp], nx);
+  (void)n;
+}
+
+__global__ void k_full_fill(int natms, const int* list, int ld, const int* fstart, int* ffill, int* flist) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= natms) return;
+  const int* li = list + (size_t)warp * ld + 3;
+  const int nx = li[0];
+  for (int k = lane; k < nx; k += 32) {
+    int j = li[k + 1] - 1;
+    int slot = atomicAdd(&ffill[warp], 1);
+    flist[fstart[warp] + slot] = j;
+    if (j < natms) {
+      int s2 = atomicAdd(&ffill[j], 1);
+      flist[fstart[j] + s2] = warp;
+    }
+  }
+}
+
+inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+// ====================================================================== host
+extern void dcell_host(const double* aaa, double* bbb);
+extern void invert_host(const double* a, double* b, double* d);
+
+void list_setup() {
+  // set_halo_particles constants (halo.F90:184-247)
+  double cut = g.rcutx + 1.0e-6;
+  double cp[10];
+  dcell_host(g.cell, cp);
+  int nl[3];
+  for (int d = 0; d < 3; ++d) nl[d] = (int)(cp[6 + d] / (cut * 1.0));
+  double det;
+  invert_host(g.cell, h_halo.rc, &det);
+  for (int d = 0; d < 3; ++d) {
+    double cw = 1.0 / (double)(nl[d] * 1);
+    double ecw = (double)g.p.spline_pad / (double)g.p.kmax[d];
+    ecw = std::max(cw, ecw);
+    h_halo.ecw[d] = std::nextafter((-0.5 + ecw) + 0.0 * 1.0, 2.0) + DBL_MIN;
+    h_halo.cw[d] = std::nextafter((-0.5 - cw) + 1.0 * 1.0, -2.0) - DBL_MIN - (nl[d] == 1 ? cw * 1.0e-10 : 0.0);
+  }
+  // export add vectors (deport_data.F90:1790-1796)
+  const double* c = g.cell;
+  const double sh[6][3] = {{+1, 0, 0}, {-1, 0, 0}, {0, +1, 0}, {0, -1, 0}, {0, 0, +1}, {0, 0, -1}};
+  for (int m = 0; m < 6; ++m) {
+    double u = sh[m][0], v = sh[m][1], w = sh[m][2];
+    h_add[m][0] = c[0] * u + c[3] * v + c[6] * w;
+    h_add[m][1] = c[1] * u + c[4] * v + c[7] * w;
+    h_add[m][2] = c[2] * u + c[5] * v + c[8] * w;
+  }
+  // link-cell geometry (neighbours.F90:396-463)
+  double cut2 = g.rcutx + 1.0e-6;
+  double disp[3] = {1.0 * cp[6] / cut2, 1.0 * cp[7] / cut2, 1.0 * cp[8] / cut2};
+  int nlx = (int)disp[0], nly = (int)disp[1], nlz = (int)disp[2];
+  int nlp = 1;
+  double nlr2 = (double)g.natms;
+  double dd = (nlx * nly * nlz) ? nlr2 / (double)(nlx * nly * nlz) : 0.0;
+  while (nlx * nly * nlz > 0 && dd > g.p.pdplnc) {
+    nlp = nlp + 1;
+    double rr = (double)nlp;
+    nlx = (int)(disp[0] * rr); nly = (int)(disp[1] * rr); nlz = (int)(disp[2] * rr);
+    dd = nlr2 / (double)(nlx * nly * nlz);
+  }
+  g.nlx = nlx; g.nly = nly; g.nlz = nlz; g.nlp = nlp;
+  g.NX = nlx + 2 * nlp; g.NY = nly + 2 * nlp; g.NZ = nlz + 2 * nlp;
+  g.ncells = g.NX * g.NY * g.NZ;
+  std::vector<int> off, nix, niy, niz;
+  std::vector<unsigned char> nir;
+  int nlp2 = nlp * nlp, nlp3 = (nlp - 1) * (nlp - 1);
+  for (int iz = 0; iz <= nlp; ++iz) {
+    int iz1 = iz > 0 ? (iz - 1) * (iz - 1) : 0, jz = iz * iz;
+    for (int iy = -nlp; iy <= nlp; ++iy) {
+      if (iz == 0 && iy < 0) continue;
+      int a = std::abs(iy), iy1 = a > 0 ? (a - 1) * (a - 1) : 0, ll = iz1 + iy1;
+      if (ll > nlp2) continue;
+      int jy = jz + iy * iy;
+      for (int ix = -nlp; ix <= nlp; ++ix) {
+        if (iz == 0 && iy == 0 && ix < 0) continue;
+        int b = std::abs(ix), ix1 = b > 0 ? (b - 1) * (b - 1) : 0;
+        if (ll + ix1 > nlp2) continue;
+        int jx = jy + ix * ix;
+        nix.push_back(ix); niy.push_back(iy); niz.push_back(iz);
+        nir.push_back(jx < nlp3 ? 1 : 0);
+        off.push_back(ix + g.NX * (iy + g.NY * iz));
+      }
+    }
+  }
+  g.nsbcll = (int)off.size();
+  if (g.nsbcll > MAX_SBC) throw (int)GB_ERR_ARG;
+  GB_CUDA(cudaMemcpyToSymbol(c_off, off.data(), sizeof(int) * off.size()));
+  GB_CUDA(cudaMemcpyToSymbol(c_nix, nix.data(), sizeof(int) * nix.size()));
+  GB_CUDA(cudaMemcpyToSymbol(c_niy, niy.data(), sizeof(int) * niy.size()));
+  GB_CUDA(cudaMemcpyToSymbol(c_niz, niz.data(), sizeof(int) * niz.size()));
+  GB_CUDA(cudaMemcpyToSymbol(c_nir, nir.data(), nir.size()));
+  for (int k = 0; k < 9; ++k) h_cg.rc[k] = h_halo.rc[k];
+  h_cg.xdc = (double)(nlx * 1); h_cg.ydc = (double)(nly * 1); h_cg.zdc = (double)(nlz * 1);
+  h_cg.nlp = nlp; h_cg.nlx = nlx; h_cg.nly = nly; h_cg.nlz = nlz;
+  h_cg.NX = g.NX; h_cg.NY = g.NY; h_cg.NZ = g.NZ;
+  h_cg.rcsq = g.rcutx * g.rcutx;
+  // FP32 prefilter band: the FP32 rsq of a pair differs from the exact FP64
+  // one by < 4e-4 A^2 for |coordinates| < 300 A and r ~ rc (rounding of the
+  // coordinates to FP32 plus the FP32 arithmetic); take 25x that bound, scaled
+  // with the box size.
+  double Lmax = std::max(std::max(cp[0], cp[1]), cp[2]) + 2.0 * g.rcutx;
+  double band = 0.01 * std::max(1.0, Lmax / 300.0) * std::max(1.0, g.rcutx / 13.0);
+  h_cg.rcsq_lo = (float)(h_cg.rcsq - band);
+  h_cg.rcsq_hi = (float)(h_cg.rcsq + band);
+  h_cg.half_plus = std::nextafter(0.5, 1.0);
+  if (g.cells_alloc < g.ncells + 2) {
+    cudaFree(g.cell_count); cudaFree(g.cell_start); cudaFree(g.cell_fill);
+    GB_CUDA(cudaMalloc(&g.cell_count, sizeof(int) * (g.ncells + 2)));
+    GB_CUDA(cudaMalloc(&g.cell_start, sizeof(int) * (g.ncells + 2)));
+    GB_CUDA(cudaMalloc(&g.cell_fill, sizeof(int) * (g.ncells + 2)));
+    g.cells_alloc = g.ncells + 2;
+  }
+}
+
+int list_relocate_and_halo() {
+  const int n = g.natms;
+  const int T = 256;
+  cudaStream_t st = g.stream;
+  // relocate_particles in serial: pbcshift (deport_data.F90:3190)
+  {
+    double a0 = 1.0 / g.cell[0], a4 = 1.0 / g.cell[4], a8 = 1.0 / g.cell[8];
+    if (g.cubic) { a4 = a0; a8 = a0; }
+    double c4 = g.cubic ? g.cell[0] : g.cell[4], c8 = g.cubic ? g.cell[0] : g.cell[8];
+    k_pbcshift<<<nblocks(n, T), T, 0, st>>>(n, g.x, g.y, g.z, a0, a4, a8, g.cell[0], c4, c8,
+                                            std::nextafter(0.5, 0.0));
+    GB_LAUNCHED();
+  }
+  k_halo_flags<<<nblocks(n, T), T, 0, st>>>(n, g.x, g.y, g.z, h_halo, g.ixyz, g.src, g.shcode, g.sc);
+  GB_LAUNCHED();
+  const int nblk = nblocks(g.mxatms, SCAN_BLOCK);
+  int* blkcount = gb_scan_scratch(2 * nblk + 2);
+  int* blkoff = blkcount + nblk + 1;
+  const int mdirs[6][5] = {{1, 0, 0, 1, 3}, {1, 0, 0, 2, 3}, {0, 1, 0, 10, 30},
+                           {0, 1, 0, 20, 30}, {0, 0, 1, 100, 300}, {0, 0, 1, 200, 300}};
+  const int dsh[6] = {+1, -1, +3, -3, +9, -9};
+  for (int m = 0; m < 6; ++m) {
+    const int* md = mdirs[m];
+    k_export_count<<<nblk, 256, 0, st>>>(g.ixyz, g.sc, md[0], md[1], md[2], md[3], blkcount);
+    GB_LAUNCHED();
+    k_scan_single<<<1, 1024, 0, st>>>(blkcount, blkoff, nblk, nullptr);
+    GB_LAUNCHED();
+    k_export_commit<<<1, 32, 0, st>>>(blkcount, nblk, blkoff, g.sc, g.mxatms);
+    GB_LAUNCHED();
+    k_export_write<<<nblk, 256, 0, st>>>(g.x, g.y, g.z, g.ltg, g.src, g.shcode, g.ixyz, blkoff, g.sc, md[0], md[1],
+                                          md[2], md[3], md[4], h_add[m][0], h_add[m][1], h_add[m][2], dsh[m],
+                                          g.mxatms);
+    GB_LAUNCHED();
+  }
+  k_halo_props<<<nblocks(g.mxatms - n, T), T, 0, st>>>(n, g.sc, g.src, g.ltype, g.chge, g.weight, g.lfrzn);
+  GB_LAUNCHED();
+  // vnl_set_check (neighbours.F90:305-343): local positions are the checkpoint
+  k_set_check<<<nblocks(n, T), T, 0, st>>>(n, g.x, g.y, g.z, g.xbg, g.ybg, g.zbg);
+  GB_LAUNCHED();
+  gb_sync_scalars();
+  if (g.hsc->status & ST_HALO_OVERFLOW) return GB_ERR_HALO;
+  return GB_OK;
+}
+
+int list_refresh_halo() {
+  static double* d_adds = nullptr;
+  if (!d_adds) {
+    GB_CUDA(cudaMalloc(&d_adds, sizeof(double) * 18));
+  }
+  GB_CUDA(cudaMemcpyAsync(d_adds, h_add, sizeof(double) * 18, cudaMemcpyHostToDevice, g.stream));
+  k_halo_refresh<<<nblocks(g.mxatms - g.natms, 256), 256, 0, g.stream>>>(g.natms, g.sc, g.src, g.shcode, g.x, g.y,
+                                                                          g.z, d_adds);
+  GB_LAUNCHED();
+  return GB_OK;
+}
+
+int list_build() {
+  const int T = 256;
+  cudaStream_t st = g.stream;
+  const int mx = g.mxatms;
+  GB_CUDA(cudaMemsetAsync(g.cell_count, 0, sizeof(int) * (g.ncells + 2), st));
+  GB_CUDA(cudaMemsetAsync(g.cell_fill, 0, sizeof(int) * (g.ncells + 2), st));
+  k_bin<<<nblocks(mx, T), T, 0, st>>>(g.natms, g.sc, g.x, g.y, g.z, h_cg, g.which_cell, g.cell_count);
+  GB_LAUNCHED();
+  k_scan_single<<<1, 1024, 0, st>>>(g.cell_count, g.cell_start, g.ncells + 2, nullptr);
+  GB_LAUNCHED();
+  int* tmp = gb_scan_scratch(mx + 1);
+  k_cell_scatter<<<nblocks(mx, T), T, 0, st>>>(g.sc, g.which_cell, g.cell_start, g.cell_fill, tmp);
+  GB_LAUNCHED();
+  k_cell_sort<<<nblocks((long long)(g.ncells + 1) * 32, T), T, 0, st>>>(g.ncells + 1, g.cell_start, tmp, g.at_list,
+                                                                       g.sorted_pos, g.x, g.y, g.z, g.xs, g.xsf);
+  GB_LAUNCHED();
+  GB_CUDA(cudaMemsetAsync(&g.sc->ibig, 0, sizeof(int), st));
+  k_list_pairs<<<nblocks((long long)mx * 32, T), T, 0, st>>>(g.natms, g.sc, h_cg, g.nsbcll, g.at_list, g.which_cell,
+                                                             g.cell_start, g.xs, g.xsf, g.list, g.ld, g.p.max_list,
+                                                             g.sc);
+  GB_LAUNCHED();
+  gb_sync_scalars();
+  if (g.hsc->status & ST_LIST_OVERFLOW) return GB_ERR_LIST_OVERFLOW;
+  if (g.lbook || g.megfrz > 1) {
+    k_list_reorder<<<nblocks(g.natms, 128), 128, 0, st>>>(g.natms, g.list, g.ld, g.lfrzn, g.ltg, g.list_excl,
+                                                          g.p.max_exclude + 1, g.megfrz, g.lbook ? 1 : 0);
+    GB_LAUNCHED();
+  }
+  if (g.precision == GB_MIXED) list_full_build();
+  return GB_OK;
+}
+
+void list_pos_f32() {
+  k_pos_f32<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(g.sc, g.x, g.y, g.z, g.chge, g.xf);
+  GB_LAUNCHED();
+}
+
+void list_full_build() {
+  const int n = g.natms;
+  cudaStream_t st = g.stream;
+  GB_CUDA(cudaMemsetAsync(g.fcount, 0, sizeof(int) * (n + 1), st));
+  k_full_count<<<nblocks((long long)n * 32, 256), 256, 0, st>>>(n, g.list, g.ld, g.fcount);
+  GB_LAUNCHED();
+  k_scan_single<<<1, 1024, 0, st>>>(g.fcount, g.fstart, n + 1, nullptr);
+  GB_LAUNCHED();
+  int total = 0;
+  GB_CUDA(cudaMemcpyAsync(&total, g.fstart + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if ((long long)total > g.flist_cap) {
+    cudaFree(g.flist);
+    g.flist_cap = (long long)(total * 1.25) + 1024;
+    GB_CUDA(cudaMalloc(&g.flist, sizeof(int) * g.flist_cap));
+  }
+  int* fill = gb_scan_scratch(n + 1);
+  GB_CUDA(cudaMemsetAsync(fill, 0, sizeof(int) * (n + 1), st));
+  k_full_fill<<<nblocks((long long)n * 32, 256), 256, 0, st>>>(n, g.list, g.ld, g.fstart, fill, g.flist);
+  GB_LAUNCHED();
+}

@@ -1,0 +1,436 @@
+// gb_pair.cu - real-space vdW + erfc-damped Coulomb pair forces.
+//
+// Follows the pair loop of two_body_forces (source/two_body.F90:339-606):
+//   vdw_forces_tab        source/vdw.F90:1790-2024 (default, 3-point tables)
+//   vdw_forces_direct     source/vdw.F90:1578-1788 (analytic 12-6 LJ)
+//   ewald_real_forces_coul source/ewald_spole.F90:58-242 (tabulated erfc(ar)/r)
+//   ewald_excl_forces     source/ewald_spole.F90:479-679 (direct A&S erfc)
+// The 3-point interpolation of three_p_interp (numerics.F90:250-290) is the
+// quadratic through table points k, k+1, k+2; it is evaluated here from its
+// per-interval coefficients c0 + d*(c1 + d*c2), precomputed in FP64 from the
+// same table values (identical polynomial, rounding differs by ~1e-16).
+//
+// FP64 form: one warp per local atom walks the reference half list.  Pairs
+// with a halo image j are evaluated once, by the atom with the smaller global
+// id, and applied to both atoms (the reference evaluates such a pair from both
+// sides, each side keeping only its own force; the sum is the same).
+// Mixed form: one warp per atom walks the derived full list in FP32 and sums
+// the pair forces as int64 fixed point (scale 2^40): order independent, no
+// atomics per pair, bit-reproducible.
+#include <cfloat>
+
+#include "gb_common.cuh"
+
+namespace {
+
+constexpr float FIX_SCALE_F = 1099511627776.0f;
+
+struct PairGeom {
+  double rc2, rv2;           // cutoffs squared
+  double rc2_lo, rc2_hi;     // band where sqrt(rsq) < rc is decided exactly
+  double rv2_lo, rv2_hi;
+  double rcut, rvdw;
+  double erdr, vrdr;         // reciprocal table spacings
+  double scaling;            // r4pie0 / eps
+  int vdw_direct;
+  int nsamples, max_grid, ntypes;
+};
+
+__device__ __forceinline__ int vkey(int ai, int aj) {
+  return ai > aj ? ai * (ai - 1) / 2 + aj : aj * (aj - 1) / 2 + ai;
+}
+
+// exact 3-point formula (numerics.F90:277-288), used for the first interval
+__device__ double three_p_exact(const double* c, double d, double r) {
+  // c holds (c0,c1,c2) of interval 0 built from (t0*?, t1, t2); rebuild points
+  double p1 = c[0], p2 = c[0] + c[1] + c[2], p3 = c[0] + 2.0 * c[1] + 4.0 * c[2];
+  p1 = p1 * r;
+  double t1 = p1 + (p2 - p1) * d;
+  double t2 = p2 + (p3 - p2) * (d - 1.0);
+  return t1 + (t2 - t1) * d * 0.5;
+}
+
+template <int NV>
+__device__ __forceinline__ void acc_store(double (&v)[NV], double* blk) {
+  block_reduce_store<NV>(v, blk);
+}
+
+// --------------------------------------------------------------- FP64 form
+// accumulator layout per block: engvdw, virvdw, engrl, virrl, str(6)
+constexpr int NACC = 10;
+
+__global__ void __launch_bounds__(256) k_pair_fp64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
+                                                   const int* __restrict__ list, int ld,
+                                                   const double* __restrict__ x, const double* __restrict__ y,
+                                                   const double* __restrict__ z, const double* __restrict__ q,
+                                                   const int* __restrict__ ltype, const int* __restrict__ ltg,
+                                                   const int* __restrict__ src, const double* __restrict__ ecoef,
+                                                   const double* __restrict__ vcoef, const int* __restrict__ vkind,
+                                                   const double* __restrict__ veps, const double* __restrict__ vsig,
+                                                   PairGeom pg, double* fx, double* fy, double* fz, double* blk) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  double acc[NACC];
+#pragma unroll
+  for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
+  const int nlast = sc->nlast;
+  int i = -1;
+  if (warp < nlast) i = at_list[warp];
+  if (i >= 0 && i < natms) {
+    const double xi = x[i], yi = y[i], zi = z[i], qi = q[i] * pg.scaling;
+    const int ai = ltype[i], gi = ltg[i];
+    const int* li = list + (size_t)i * ld + 3;
+    const int n = li[0];
+    double fix = 0.0, fiy = 0.0, fiz = 0.0;
+    const int vstride = (pg.max_grid + 3) * 6;
+    for (int m = lane + 1; m <= n; m += 32) {
+      int j = li[m] - 1;
+      int jf = j;  // atom receiving the reaction force
+      if (j >= natms) {
+        if (gi > ltg[j]) continue;  // evaluated from the other side
+        jf = src[j];
+      }
+      const double dx = xi - x[j], dy = yi - y[j], dz = zi - z[j];
+      const double rsq = dx * dx + dy * dy + dz * dz;
+      if (rsq >= pg.rc2_hi && rsq >= pg.rv2) continue;
+      // 1/r: FP32 seed + one Newton step (relative error < 3e-14)
+      double rinv = (double)rsqrtf((float)rsq);
+      rinv = rinv * fma(-0.5 * rsq * rinv, rinv, 1.5);
+      double rrr = rsq * rinv;
+      bool in_c = rsq < pg.rc2_lo || (rsq < pg.rc2_hi && sqrt(rsq) < pg.rcut);
+      double gam = 0.0, ee = 0.0, ev = 0.0, gvir_c = 0.0, gvir_v = 0.0;
+      const double qj = q[j];
+      // real-space Coulomb (ewald_spole.F90:131-176)
+      if (in_c && fabs(qj) > DBL_MIN && fabs(qi) >= DBL_MIN) {
+        double ppp = rrr * pg.erdr;
+        int k = (int)ppp;
+        double d = ppp - (double)k;
+        const double* c = ecoef + (size_t)k * 6;
+        double pre = qi * qj;
+        double eg, ec;
+        if (k > 0) {
+          eg = pre * fma(d, fma(d, c[5], c[4]), c[3]);
+          ec = pre * fma(d, fma(d, c[2], c[1]), c[0]);
+        } else {
+          eg = pre * three_p_exact(c + 3, d, rrr);
+          ec = pre * three_p_exact(c, d, rrr);
+        }
+        gam += eg;
+        ee = ec;
+        gvir_c = eg;
+      }
+      // van der Waals (vdw.F90:1881-1962 tabulated / :1670-1700 direct)
+      if (rsq < pg.rv2) {
+        const int aj = ltype[j];
+        const int key = vkey(ai, aj) - 1;
+        if (vkind[key] != 0) {
+          if (rsq < pg.rv2_lo || (rsq < pg.rv2_hi && sqrt(rsq) < pg.rvdw)) {
+            double r_rsq = rinv * rinv;
+            double gv, e;
+            if (pg.vdw_direct) {
+              double sr = vsig[key] * rinv;
+              double s2 = sr * sr, s6 = s2 * s2 * s2;
+              e = 4.0 * veps[key] * s6 * (s6 - 1.0);
+              gv = 24.0 * veps[key] * s6 * (2.0 * s6 - 1.0) * r_rsq;
+            } else {
+              double ppp = rrr * pg.vrdr;
+              int k = (int)ppp;
+              double d = ppp - (double)k;
+              const double* c = vcoef + (size_t)key * vstride + (size_t)k * 6;
+              if (k > 0) {
+                gv = fma(d, fma(d, c[2], c[1]), c[0]) * r_rsq;
+                e = fma(d, fma(d, c[5], c[4]), c[3]);
+              } else {
+                gv = three_p_exact(c, d, rrr) * r_rsq;
+                e = three_p_exact(c + 3, d, rrr);
+              }
+            }
+            gam += gv;
+            ev = e;
+            gvir_v = gv;
+          }
+        }
+      }
+      if (gam == 0.0 && ee == 0.0 && ev == 0.0) continue;
+      const double fx_ = gam * dx, fy_ = gam * dy, fz_ = gam * dz;
+      fix += fx_; fiy += fy_; fiz += fz_;
+      atomicAdd(&fx[jf], -fx_);
+      atomicAdd(&fy[jf], -fy_);
+      atomicAdd(&fz[jf], -fz_);
+      acc[0] += ev;
+      acc[1] -= gvir_v * rsq;
+      acc[2] += ee;
+      acc[3] -= gvir_c * rsq;
+      acc[4] += dx * fx_; acc[5] += dx * fy_; acc[6] += dx * fz_;
+      acc[7] += dy * fy_; acc[8] += dy * fz_; acc[9] += dz * fz_;
+    }
+    fix = warp_sum(fix); fiy = warp_sum(fiy); fiz = warp_sum(fiz);
+    if (lane == 0) {
+      atomicAdd(&fx[i], fix);
+      atomicAdd(&fy[i], fiy);
+      atomicAdd(&fz[i], fiz);
+    }
+  }
+  block_reduce_store<NACC>(acc, blk);
+}
+
+// exclusion correction (FP64), one thread per atom over its excluded section
+__global__ void k_excl_fp64(int natms, const int* list, int ld, const double* x, const double* y, const double* z,
+                            const double* q, const int* ltg, const int* src, double alpha, double scaling,
+                            double rcut, double* fx, double* fy, double* fz, double* blk) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (i < natms) {
+    const int* li = list + (size_t)i * ld + 3;
+    int lim = li[-1] - li[0];
+    double chgea = q[i];
+    if (lim > 0 && fabs(chgea) > DBL_MIN) {
+      chgea *= scaling;
+      const double a1 = 0.254829592, a2 = -0.284496736, a3 = 1.421413741, a4 = -1.453152027,
+                   a5 = 1.061405429, pp = 0.3275911, r10 = 0.1, r216 = 1.0 / 216.0, r42 = 1.0 / 42.0,
+                   rr3 = 1.0 / 3.0, sqrpi = 1.7724538509055160273;
+      double fix = 0, fiy = 0, fiz = 0;
+      for (int m = 1; m <= lim; ++m) {
+        int j = li[li[0] + m] - 1;
+        double xx = x[i] - x[j], yy = y[i] - y[j], zz = z[i] - z[j];
+        double rrr = sqrt(xx * xx + yy * yy + zz * zz);
+        double chgprd = q[j];
+        if (fabs(chgprd) > DBL_MIN && rrr < rcut) {
+          chgprd *= chgea;
+          double rsq = rrr * rrr, alpr = rrr * alpha, alpr2 = alpr * alpr, erfr, egamma;
+          if (alpr < 1.0e-2) {
+            erfr = 2.0 * chgprd * (alpha / sqrpi) * (1.0 + alpr2 * (-rr3 + alpr2 * (r10 + alpr2 * (-r42 + alpr2 * r216))));
+            egamma = -4.0 * chgprd * (alpha * alpha * alpha / sqrpi) *
+                     (rr3 + alpr2 * (-2.0 * r10 + alpr2 * (3.0 * r42 - 4.0 * alpr2 * r216)));
+          } else {
+            double exp1 = exp(-(alpha * rrr) * (alpha * rrr));
+            double tt = 1.0 / (1.0 + pp * alpha * rrr);
+            erfr = chgprd * (1.0 - tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5)))) * exp1) / rrr;
+            egamma = -(erfr - 2.0 * chgprd * (alpha / sqrpi) * exp1) / rsq;
+          }
+          double fx_ = egamma * xx, fy_ = egamma * yy, fz_ = egamma * zz;
+          fix += fx_; fiy += fy_; fiz += fz_;
+          if (j < natms) {
+            atomicAdd(&fx[j], -fx_); atomicAdd(&fy[j], -fy_); atomicAdd(&fz[j], -fz_);
+          }
+          if (j < natms || ltg[i] < ltg[j]) {
+            acc[0] -= erfr;
+            acc[1] -= egamma * rsq;
+            acc[2] += xx * fx_; acc[3] += xx * fy_; acc[4] += xx * fz_;
+            acc[5] += yy * fy_; acc[6] += yy * fz_; acc[7] += zz * fz_;
+          }
+        }
+      }
+      atomicAdd(&fx[i], fix); atomicAdd(&fy[i], fiy); atomicAdd(&fz[i], fiz);
+    }
+  }
+  block_reduce_store<8>(acc, blk);
+}
+
+// -------------------------------------------------------------- mixed form
+// Full list, FP32 arithmetic, int64 fixed-point force sums; energies and
+// virials are summed per lane in FP32 and reduced in FP64 (x0.5: every pair
+// appears twice in the full list).
+__global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __restrict__ fstart,
+                                                    const int* __restrict__ fcount, const int* __restrict__ flist,
+                                                    const float4* __restrict__ xf, const int* __restrict__ ltype,
+                                                    const float* __restrict__ ecoef, const float* __restrict__ vcoef,
+                                                    const int* __restrict__ vkind, float rc2, float rv2, float erdr,
+                                                    float vrdr, float scaling, int max_grid,
+                                                    unsigned long long* fixp, double* blk) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  double acc[NACC];
+#pragma unroll
+  for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
+  if (warp < natms) {
+    const int i = warp;
+    const float4 pi = xf[i];
+    const float qi = pi.w * scaling;
+    const int ai = ltype[i];
+    const int s = fstart[i], n = fcount[i];
+    long long sx = 0, sy = 0, sz = 0;
+    float a0 = 0, a1 = 0, a2 = 0, a3 = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
+    const int vstride = (max_grid + 3) * 6;
+    for (int m = lane; m < n; m += 32) {
+      const int j = flist[s + m];
+      const float4 pj = xf[j];
+      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      const float rsq = dx * dx + dy * dy + dz * dz;
+      if (rsq >= rc2 && rsq >= rv2) continue;
+      const float rinv = rsqrtf(rsq);
+      const float rrr = rsq * rinv;
+      float gam = 0.f;
+      if (rsq < rc2 && pj.w != 0.f) {
+        float ppp = rrr * erdr;
+        int k = (int)ppp;
+        float d = ppp - (float)k;
+        const float* c = ecoef + (size_t)k * 6;
+        float pre = qi * pj.w;
+        float eg = pre * fmaf(d, fmaf(d, c[5], c[4]), c[3]);
+        float ec = pre * fmaf(d, fmaf(d, c[2], c[1]), c[0]);
+        gam += eg;
+        a2 += ec;
+        a3 -= eg * rsq;
+      }
+      if (rsq < rv2) {
+        const int key = vkey(ai, ltype[j]) - 1;
+        if (vkind[key] != 0) {
+          float ppp = rrr * vrdr;
+          int k = (int)ppp;
+          float d = ppp - (float)k;
+          const float* c = vcoef + (size_t)key * vstride + (size_t)k * 6;
+          float gv = fmaf(d, fmaf(d, c[2], c[1]), c[0]) * rinv * rinv;
+          float e = fmaf(d, fmaf(d, c[5], c[4]), c[3]);
+          gam += gv;
+          a0 += e;
+          a1 -= gv * rsq;
+        }
+      }
+      const float fx_ = gam * dx, fy_ = gam * dy, fz_ = gam * dz;
+      sx += __float2ll_rn(fx_ * FIX_SCALE_F);
+      sy += __float2ll_rn(fy_ * FIX_SCALE_F);
+      sz += __float2ll_rn(fz_ * FIX_SCALE_F);
+      s0 += dx * fx_; s1 += dx * fy_; s2 += dx * fz_; s3 += dy * fy_; s4 += dy * fz_; s5 += dz * fz_;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, o);
+      sy += __shfl_xor_sync(0xffffffffu, sy, o);
+      sz += __shfl_xor_sync(0xffffffffu, sz, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&fixp[3 * i + 0], (unsigned long long)sx);
+      atomicAdd(&fixp[3 * i + 1], (unsigned long long)sy);
+      atomicAdd(&fixp[3 * i + 2], (unsigned long long)sz);
+    }
+    acc[0] = 0.5 * a0; acc[1] = 0.5 * a1; acc[2] = 0.5 * a2; acc[3] = 0.5 * a3;
+    acc[4] = 0.5 * s0; acc[5] = 0.5 * s1; acc[6] = 0.5 * s2; acc[7] = 0.5 * s3; acc[8] = 0.5 * s4; acc[9] = 0.5 * s5;
+  }
+  block_reduce_store<NACC>(acc, blk);
+}
+
+// exclusion correction (mixed): FP32 arithmetic, fixed-point forces
+__global__ void k_excl_mixed(int natms, const int* list, int ld, const float4* xf, const int* ltg, float alpha,
+                             float scaling, float rcut, unsigned long long* fixp, double* blk) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (i < natms) {
+    const int* li = list + (size_t)i * ld + 3;
+    int lim = li[-1] - li[0];
+    float4 pi = xf[i];
+    if (lim > 0 && pi.w != 0.f) {
+      const float chgea = pi.w * scaling;
+      const float a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f, a4 = -1.453152027f,
+                  a5 = 1.061405429f, pp = 0.3275911f, sqrpi = 1.7724538509f;
+      long long sx = 0, sy = 0, sz = 0;
+      for (int m = 1; m <= lim; ++m) {
+        int j = li[li[0] + m] - 1;
+        float4 pj = xf[j];
+        float xx = pi.x - pj.x, yy = pi.y - pj.y, zz = pi.z - pj.z;
+        float rsq = xx * xx + yy * yy + zz * zz;
+        float rrr = sqrtf(rsq);
+        if (pj.w != 0.f && rrr < rcut) {
+          float chgprd = pj.w * chgea;
+          float exp1 = __expf(-(alpha * rrr) * (alpha * rrr));
+          float tt = 1.0f / (1.0f + pp * alpha * rrr);
+          float erfr = chgprd * (1.0f - tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5)))) * exp1) / rrr;
+          float egamma = -(erfr - 2.0f * chgprd * (alpha / sqrpi) * exp1) / rsq;
+          float fx_ = egamma * xx, fy_ = egamma * yy, fz_ = egamma * zz;
+          long long ix = __float2ll_rn(fx_ * FIX_SCALE_F), iy = __float2ll_rn(fy_ * FIX_SCALE_F),
+                    iz = __float2ll_rn(fz_ * FIX_SCALE_F);
+          sx += ix; sy += iy; sz += iz;
+          if (j < natms) {
+            atomicAdd(&fixp[3 * j + 0], (unsigned long long)(-ix));
+            atomicAdd(&fixp[3 * j + 1], (unsigned long long)(-iy));
+            atomicAdd(&fixp[3 * j + 2], (unsigned long long)(-iz));
+          }
+          if (j < natms || ltg[i] < ltg[j]) {
+            acc[0] -= erfr;
+            acc[1] -= egamma * rsq;
+            acc[2] += xx * fx_; acc[3] += xx * fy_; acc[4] += xx * fz_;
+            acc[5] += yy * fy_; acc[6] += yy * fz_; acc[7] += zz * fz_;
+          }
+        }
+      }
+      atomicAdd(&fixp[3 * i + 0], (unsigned long long)sx);
+      atomicAdd(&fixp[3 * i + 1], (unsigned long long)sy);
+      atomicAdd(&fixp[3 * i + 2], (unsigned long long)sz);
+    }
+  }
+  block_reduce_store<8>(acc, blk);
+}
+
+inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+// ===================================================================== host
+// eng6: engrl, virrl, engex, virex, engvdw, virvdw; stress9 accumulates.
+void pair_forces(double* eng6, double* stress9) {
+  PairGeom pg;
+  pg.rcut = g.p.rcut;
+  pg.rvdw = g.p.rvdw;
+  pg.rc2 = g.p.rcut * g.p.rcut;
+  pg.rv2 = g.p.rvdw * g.p.rvdw;
+  // decide sqrt(rsq) < rc exactly only inside a narrow band around rc^2
+  pg.rc2_lo = pg.rc2 * (1.0 - 1e-12);
+  pg.rc2_hi = std::max(pg.rc2, pg.rv2) * (1.0 + 1e-12);
+  pg.rv2_lo = pg.rv2 * (1.0 - 1e-12);
+  pg.rv2_hi = pg.rv2 * (1.0 + 1e-12);
+  pg.erdr = g.erfc_rdr;
+  pg.vrdr = g.vdw_rdr;
+  pg.scaling = g.scaling;
+  pg.vdw_direct = g.p.vdw_direct;
+  pg.nsamples = g.nsamples;
+  pg.max_grid = g.max_grid;
+  pg.ntypes = g.p.ntypes;
+  cudaStream_t st = g.stream;
+  const int T = 256;
+  double res[NACC];
+  double ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (g.precision == GB_FP64) {
+    int nb = nblocks((long long)g.mxatms * 32, T);
+    double* blk = gb_blkacc(nb * NACC);
+    k_pair_fp64<<<nb, T, 0, st>>>(g.natms, g.sc, g.at_list, g.list, g.ld, g.x, g.y, g.z, g.chge, g.ltype, g.ltg,
+                                  g.src, g.erfc_coef, g.vdw_coef, g.vdw_kind, g.vdw_eps, g.vdw_sig, pg, g.fx, g.fy,
+                                  g.fz, blk);
+    GB_LAUNCHED();
+    gb_reduce_blocks(blk, nb, NACC, &g.sc->acc[A_PAIR]);
+    if (g.lbook) {
+      int nb2 = nblocks(g.natms, 128);
+      double* blk2 = gb_blkacc(nb * NACC + nb2 * 8) + (size_t)nb * NACC;
+      k_excl_fp64<<<nb2, 128, 0, st>>>(g.natms, g.list, g.ld, g.x, g.y, g.z, g.chge, g.ltg, g.src, g.p.alpha,
+                                       g.scaling, g.p.rcut, g.fx, g.fy, g.fz, blk2);
+      GB_LAUNCHED();
+      gb_reduce_blocks(blk2, nb2, 8, &g.sc->acc[A_EXCL]);
+    }
+  } else {
+    int nb = nblocks((long long)g.natms * 32, T);
+    double* blk = gb_blkacc(nb * NACC);
+    k_pair_mixed<<<nb, T, 0, st>>>(g.natms, g.fstart, g.fcount, g.flist, g.xf, g.ltype, g.erfc_coef_f, g.vdw_coef_f,
+                                   g.vdw_kind, (float)pg.rc2, (float)pg.rv2, (float)pg.erdr, (float)pg.vrdr,
+                                   (float)pg.scaling, g.max_grid, (unsigned long long*)g.fixp, blk);
+    GB_LAUNCHED();
+    gb_reduce_blocks(blk, nb, NACC, &g.sc->acc[A_PAIR]);
+    if (g.lbook) {
+      int nb2 = nblocks(g.natms, 128);
+      double* blk2 = gb_blkacc(nb * NACC + nb2 * 8) + (size_t)nb * NACC;
+      k_excl_mixed<<<nb2, 128, 0, st>>>(g.natms, g.list, g.ld, g.xf, g.ltg, (float)g.p.alpha, (float)g.scaling,
+                                        (float)g.p.rcut, (unsigned long long*)g.fixp, blk2);
+      GB_LAUNCHED();
+      gb_reduce_blocks(blk2, nb2, 8, &g.sc->acc[A_EXCL]);
+    }
+  }
+  gb_sync_scalars();
+  for (int k = 0; k < NACC; ++k) res[k] = g.hsc->acc[A_PAIR + k];
+  if (g.lbook) for (int k = 0; k < 8; ++k) ex[k] = g.hsc->acc[A_EXCL + k];
+  eng6[0] = res[2]; eng6[1] = res[3];
+  eng6[2] = ex[0]; eng6[3] = ex[1];
+  eng6[4] = res[0]; eng6[5] = res[1];
+  double s6[6];
+  for (int k = 0; k < 6; ++k) s6[k] = res[4 + k] + ex[2 + k];
+  stress9[0] += s6[0]; stress9[1] += s6[1]; stress9[2] += s6[2];
+  stress9[3] += s6[1]; stress9[4] += s6[3]; stress9[5] += s6[4];
+  stress9[6] += s6[2]; stress9[7] += s6[4]; stress9[8] += s6[5];
+}

@@ -1,0 +1,742 @@
+// gb_spme.cu - SPME reciprocal space on the device.
+//
+// Follows ewald_spme_forces_coul (source/ewald_spole.F90:244-477):
+//   fractional coordinates u = K (rcell . r + 1/2)            (:364-370)
+//   B-splines of order p            bspline_splines_gen (bspline.F90:192-306)
+//   charge spreading                spme_construct_charge_array (ewald_general.F90:517-576)
+//   FFT, influence function, stress spme_construct_potential_grid_coul (ewald_spole.F90:1257-1386)
+//   force / energy gather, net-force removal spme_calc_force_energy (ewald_general.F90:717-869)
+//
+// The reference spreads local atoms and their positive halo images with the
+// grid clamped to [0,K); that is the periodic spread of every atom with
+// floor-based splines, which is what the brick kernel computes (no halo
+// needed).  The gather uses the reference's own truncation convention
+// (n = Int(u), w = u - Aint(u)) and periodic grid reads, so atoms that drifted
+// out of the cell between relocations get the same spline values.
+//
+// Spreading is atomic free: atoms are sorted by grid brick (B >= p-1 points
+// per side); one CTA owns a brick and gathers from the 2x2x2 source bricks
+// whose atoms can reach it, one thread per grid row along x.
+//
+// The 3-D FFT is an in-shared-memory Stockham transform (radix 4, 3, 5, 2)
+// along x, y and z; the z pass applies the influence function theta(m)
+// (precomputed in FP64 on the host: |b(m)|^2 exp(-pi^2 m^2/a^2)/(sqrt(pi) f^2)
+// inside the spherical cut) and accumulates the reciprocal stress, then runs
+// the inverse z transform on the same tile before writing it back.
+#include <cfloat>
+#include <cmath>
+
+#include "gb_common.cuh"
+
+namespace {
+
+constexpr int PMAX = 12;
+constexpr int TX = 4;  // columns per tile in the strided passes
+
+template <typename T> struct V2;
+template <> struct V2<double> { using t = double2; };
+template <> struct V2<float> { using t = float2; };
+
+template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
+  T2 r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { T2 r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { T2 r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+// multiply by s*i
+template <typename T2> __device__ __forceinline__ T2 cmuli(T2 a, int s) { T2 r; r.x = -s * a.y; r.y = s * a.x; return r; }
+
+struct FftPlan {
+  int N;
+  int nrad;
+  int rad[16];
+};
+
+// one Stockham stage over nlines lines of length N held in shared memory
+template <typename T, typename T2>
+__device__ void fft_stage(const T2* __restrict__ in, T2* __restrict__ out, int N, int nlines, int R, int Ns,
+                          const T2* __restrict__ tw, int isign) {
+  const int T_ = N / R;
+  const int total = nlines * T_;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int line = idx / T_;
+    const int j = idx - line * T_;
+    const int k = j % Ns;
+    const T2* src = in + line * N;
+    T2* dst = out + line * N;
+    T2 v[5];
+#pragma unroll 5
+    for (int r = 0; r < 5; ++r)
+      if (r < R) v[r] = src[j + r * T_];
+    if (Ns > 1) {
+      const int step = N / (Ns * R);
+#pragma unroll 5
+      for (int r = 1; r < 5; ++r) {
+        if (r < R) {
+          T2 w = tw[(r * k * step) % N];
+          if (isign < 0) w.y = -w.y;
+          v[r] = cmul(v[r], w);
+        }
+      }
+    }
+    T2 o[5];
+    if (R == 4) {
+      T2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]), c = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+      T2 di = cmuli(d, isign);
+      o[0] = cadd(a, c); o[2] = csub(a, c); o[1] = cadd(b, di); o[3] = csub(b, di);
+    } else if (R == 2) {
+      o[0] = cadd(v[0], v[1]); o[1] = csub(v[0], v[1]);
+    } else if (R == 3) {
+      const T h = (T)0.86602540378443864676;
+      T2 t = cadd(v[1], v[2]), u = csub(v[1], v[2]);
+      T2 m;
+      m.x = v[0].x - (T)0.5 * t.x; m.y = v[0].y - (T)0.5 * t.y;
+      T2 ui = cmuli(u, isign);
+      ui.x *= h; ui.y *= h;
+      o[0] = cadd(v[0], t); o[1] = cadd(m, ui); o[2] = csub(m, ui);
+    } else {  // R == 5
+      const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+      const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;
+      T2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]), t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+      o[0] = cadd(v[0], cadd(t1, t2));
+      T2 a1, a2, b1, b2;
+      a1.x = v[0].x + c1 * t1.x + c2 * t2.x; a1.y = v[0].y + c1 * t1.y + c2 * t2.y;
+      a2.x = v[0].x + c2 * t1.x + c1 * t2.x; a2.y = v[0].y + c2 * t1.y + c1 * t2.y;
+      b1.x = s1 * t3.x + s2 * t4.x; b1.y = s1 * t3.y + s2 * t4.y;
+      b2.x = s2 * t3.x - s1 * t4.x; b2.y = s2 * t3.y - s1 * t4.y;
+      T2 ib1 = cmuli(b1, isign), ib2 = cmuli(b2, isign);
+      o[1] = cadd(a1, ib1); o[4] = csub(a1, ib1); o[2] = cadd(a2, ib2); o[3] = csub(a2, ib2);
+    }
+    const int base = (j / Ns) * Ns * R + k;
+#pragma unroll 5
+    for (int r = 0; r < 5; ++r)
+      if (r < R) dst[base + r * Ns] = o[r];
+  }
+}
+
+// full transform of nlines lines; returns the buffer holding the result
+template <typename T, typename T2>
+__device__ T2* fft_lines(T2* a, T2* b, const FftPlan& pl, int nlines, const T2* tw, int isign) {
+  int Ns = 1;
+  for (int s = 0; s < pl.nrad; ++s) {
+    __syncthreads();
+    fft_stage<T, T2>(a, b, pl.N, nlines, pl.rad[s], Ns, tw, isign);
+    Ns *= pl.rad[s];
+    T2* t = a; a = b; b = t;
+  }
+  __syncthreads();
+  return a;
+}
+
+// ------------------------------------------------------------ spline prep
+// Cardinal B-spline values M_p(w + p - 1 - t), t = 0..p-1, by the order
+// recursion of bspline_splines_gen (bspline.F90:227-245), valid as the
+// polynomial pieces for any w (the reference also feeds w outside [0,1)).
+template <typename T>
+__device__ __forceinline__ void bspline_vals(T w, int p, T* m /*p*/, T* dm /*p or null*/) {
+  // z[j], j = 1..p as in the reference (z[p] <-> M(w), z[1] <-> M(w+p-1))
+  T z[PMAX + 2];
+#pragma unroll
+  for (int j = 0; j < PMAX + 2; ++j) z[j] = (T)0;
+  z[p] = w;
+  z[p - 1] = (T)1 - w;
+  // raise from order 2 to order p-1
+  for (int n = 3; n <= p - 1; ++n) {
+    const T rn = (T)1 / (T)(n - 1);
+    for (int j = p - n + 1; j <= p - 1; ++j) {
+      const T pt = w + (T)(p - j);
+      z[j] = (pt * z[j] + ((T)n - pt) * z[j + 1]) * rn;
+    }
+    z[p] = z[p] * w * rn;
+  }
+  if (dm) {
+    // derivative of order p from order p-1 values: M_{p-1}(x) - M_{p-1}(x-1)
+    for (int j = 1; j <= p; ++j) dm[j - 1] = z[j] - z[j + 1];
+  }
+  {
+    const int n = p;
+    const T rn = (T)1 / (T)(n - 1);
+    for (int j = 1; j <= p - 1; ++j) {
+      const T pt = w + (T)(p - j);
+      z[j] = (pt * z[j] + ((T)n - pt) * z[j + 1]) * rn;
+    }
+    z[p] = z[p] * w * rn;
+  }
+  // output in grid order t = 0..p-1  <->  reference spline index s = t+1
+  for (int t = 0; t < p; ++t) m[t] = z[t + 1];
+}
+
+struct SpmeGeom {
+  double rc[9];
+  double Kr[3];
+  int K[3], B[3], nb[3], p;
+};
+
+template <typename T>
+__global__ void k_spme_prep(int natms, const double* __restrict__ x, const double* __restrict__ y,
+                            const double* __restrict__ z, const double* __restrict__ q, SpmeGeom sg, T* spl,
+                            int* nidx, int* brick_of, int* brick_count) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natms) return;
+  const int p = sg.p;
+  int bidx[3];
+  for (int d = 0; d < 3; ++d) {
+    double u = sg.Kr[d] * (((sg.rc[d] * x[i] + sg.rc[d + 3] * y[i]) + sg.rc[d + 6] * z[i]) + 0.5);
+    double fl = floor(u);
+    int n = (int)fl;
+    T w = (T)(u - fl);
+    T m[PMAX];
+    bspline_vals<T>(w, p, m, nullptr);
+    for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t];
+    int nw = n % sg.K[d];
+    if (nw < 0) nw += sg.K[d];
+    nidx[3 * i + d] = nw;
+    bidx[d] = nw / sg.B[d];
+  }
+  int b = bidx[0] + sg.nb[0] * (bidx[1] + sg.nb[1] * bidx[2]);
+  if (fabs(q[i]) <= DBL_MIN) b = -1;
+  brick_of[i] = b;
+  if (b >= 0) atomicAdd(&brick_count[b], 1);
+}
+
+__global__ void k_brick_scatter(int natms, const int* brick_of, const int* start, int* fill, int* tmp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natms) return;
+  int b = brick_of[i];
+  if (b < 0) return;
+  int s = atomicAdd(&fill[b], 1);
+  tmp[start[b] + s] = i;
+}
+
+__global__ void k_brick_sort(int nbricks, const int* start, const int* tmp, int* out) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nbricks) return;
+  int s = start[warp], n = start[warp + 1] - s;
+  for (int a = lane; a < n; a += 32) {
+    int v = tmp[s + a], r = 0;
+    for (int b = 0; b < n; ++b) r += tmp[s + b] < v;
+    out[s + r] = v;
+  }
+}
+
+// ------------------------------------------------------------- spreading
+// CTA = one brick; thread = one (y,z) row of B0 points along x.
+constexpr int SPREAD_CH = 32;
+constexpr int BMAX = 16;
+
+template <typename T>
+__global__ void k_spme_spread(SpmeGeom sg, const int* __restrict__ bstart, const int* __restrict__ batoms,
+                              const T* __restrict__ spl, const int* __restrict__ nidx, const double* __restrict__ q,
+                              T* __restrict__ Q) {
+  const int b = blockIdx.x;
+  const int bx = b % sg.nb[0], by = (b / sg.nb[0]) % sg.nb[1], bz = b / (sg.nb[0] * sg.nb[1]);
+  const int B0 = sg.B[0], B1 = sg.B[1], B2 = sg.B[2], p = sg.p;
+  const int g0x = bx * B0, g0y = by * B1, g0z = bz * B2;
+  const int ty = threadIdx.x % B1, tz = threadIdx.x / B1;
+  const bool active = threadIdx.x < B1 * B2;
+  __shared__ T wx[SPREAD_CH][BMAX], wy[SPREAD_CH][BMAX], wz[SPREAD_CH][BMAX];
+  T acc[BMAX];
+#pragma unroll
+  for (int k = 0; k < BMAX; ++k) acc[k] = (T)0;
+  for (int sb = 0; sb < 8; ++sb) {
+    const int sx = (bx + (sb & 1)) % sg.nb[0], sy = (by + ((sb >> 1) & 1)) % sg.nb[1],
+              sz = (bz + ((sb >> 2) & 1)) % sg.nb[2];
+    // skip duplicates when a dimension has a single brick
+    if (((sb & 1) && sg.nb[0] == 1) || (((sb >> 1) & 1) && sg.nb[1] == 1) || (((sb >> 2) & 1) && sg.nb[2] == 1))
+      continue;
+    const int src = sx + sg.nb[0] * (sy + sg.nb[1] * sz);
+    const int s0 = bstart[src], s1 = bstart[src + 1];
+    for (int c = s0; c < s1; c += SPREAD_CH) {
+      const int nc = min(SPREAD_CH, s1 - c);
+      __syncthreads();
+      // stage brick-aligned weights: w[d][k] for grid point g0+k
+      for (int e = threadIdx.x; e < nc * (B0 + B1 + B2); e += blockDim.x) {
+        const int a = e / (B0 + B1 + B2);
+        int k = e - a * (B0 + B1 + B2);
+        int d = 0, Bd = B0, g0 = g0x;
+        if (k >= B0) { k -= B0; d = 1; Bd = B1; g0 = g0y; if (k >= B1) { k -= B1; d = 2; Bd = B2; g0 = g0z; } }
+        (void)Bd;
+        const int i = batoms[c + a];
+        const int n = nidx[3 * i + d];
+        int t = (g0 + k) - n + p - 1;
+        const int K = sg.K[d];
+        t %= K; if (t < 0) t += K;
+        T w = (t < p) ? spl[((size_t)i * 3 + d) * p + t] : (T)0;
+        if (d == 2 && t < p) w *= (T)q[i];
+        if (d == 0) wx[a][k] = w; else if (d == 1) wy[a][k] = w; else wz[a][k] = w;
+      }
+      __syncthreads();
+      if (active) {
+        for (int a = 0; a < nc; ++a) {
+          const T wyz = wy[a][ty] * wz[a][tz];
+          if (wyz != (T)0) {
+#pragma unroll
+            for (int k = 0; k < BMAX; ++k)
+              if (k < B0) acc[k] += wyz * wx[a][k];
+          }
+        }
+      }
+    }
+  }
+  if (active) {
+    T* row = Q + ((size_t)(g0z + tz) * sg.K[1] + (g0y + ty)) * sg.K[0] + g0x;
+#pragma unroll
+    for (int k = 0; k < BMAX; ++k)
+      if (k < B0) row[k] = acc[k];
+  }
+}
+
+// ---------------------------------------------------------------- FFT passes
+// X pass forward: real rows -> complex rows
+template <typename T, typename T2>
+__global__ void k_fft_x_fwd(const T* __restrict__ Q, T2* __restrict__ G, FftPlan pl, const T2* __restrict__ tw,
+                            int nrows, int lines) {
+  extern __shared__ unsigned char smem_raw[];
+  T2* a = reinterpret_cast<T2*>(smem_raw);
+  T2* b = a + lines * pl.N;
+  const int N = pl.N;
+  const size_t row0 = (size_t)blockIdx.x * lines;
+  const int nl = (int)min((size_t)lines, (size_t)nrows - row0);
+  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
+    T2 v; v.x = Q[row0 * N + e]; v.y = (T)0;
+    a[e] = v;
+  }
+  T2* r = fft_lines<T, T2>(a, b, pl, nl, tw, +1);
+  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) G[row0 * N + e] = r[e];
+}
+
+// X pass inverse: complex rows -> real part
+template <typename T, typename T2>
+__global__ void k_fft_x_inv(const T2* __restrict__ G, T* __restrict__ Q, FftPlan pl, const T2* __restrict__ tw,
+                            int nrows, int lines) {
+  extern __shared__ unsigned char smem_raw[];
+  T2* a = reinterpret_cast<T2*>(smem_raw);
+  T2* b = a + lines * pl.N;
+  const int N = pl.N;
+  const size_t row0 = (size_t)blockIdx.x * lines;
+  const int nl = (int)min((size_t)lines, (size_t)nrows - row0);
+  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) a[e] = G[row0 * N + e];
+  T2* r = fft_lines<T, T2>(a, b, pl, nl, tw, -1);
+  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) Q[row0 * N + e] = r[e].x;
+}
+
+// Y pass (stride K1): tile of TX columns x N lines, in place
+template <typename T, typename T2>
+__global__ void k_fft_y(T2* __restrict__ G, int K1, int K2, FftPlan pl, const T2* __restrict__ tw, int isign) {
+  extern __shared__ unsigned char smem_raw[];
+  T2* a = reinterpret_cast<T2*>(smem_raw);
+  T2* b = a + TX * pl.N;
+  const int ntx = K1 / TX;
+  const int x0 = (blockIdx.x % ntx) * TX;
+  const int zz = blockIdx.x / ntx;
+  T2* base = G + (size_t)zz * K1 * K2 + x0;
+  for (int e = threadIdx.x; e < TX * K2; e += blockDim.x) {
+    int yy = e / TX, t = e - yy * TX;
+    a[t * K2 + yy] = base[(size_t)yy * K1 + t];
+  }
+  T2* r = fft_lines<T, T2>(a, b, pl, TX, tw, isign);
+  for (int e = threadIdx.x; e < TX * K2; e += blockDim.x) {
+    int yy = e / TX, t = e - yy * TX;
+    base[(size_t)yy * K1 + t] = r[t * K2 + yy];
+  }
+}
+
+// Z pass: forward z FFT, influence function + stress, inverse z FFT
+template <typename T, typename T2>
+__global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan pl, const T2* __restrict__ tw,
+                             const T* __restrict__ theta, const T* __restrict__ psi, SpmeGeom sg, double* blk) {
+  extern __shared__ unsigned char smem_raw[];
+  T2* a = reinterpret_cast<T2*>(smem_raw);
+  T2* b = a + TX * pl.N;
+  const int ntx = K1 / TX;
+  const int x0 = (blockIdx.x % ntx) * TX;
+  const int yy = blockIdx.x / ntx;
+  const size_t plane = (size_t)K1 * K2;
+  T2* base = G + (size_t)yy * K1 + x0;
+  for (int e = threadIdx.x; e < TX * K3; e += blockDim.x) {
+    int zz = e / TX, t = e - zz * TX;
+    a[t * K3 + zz] = base[(size_t)zz * plane + t];
+  }
+  T2* r = fft_lines<T, T2>(a, b, pl, TX, tw, +1);
+  double st[6] = {0, 0, 0, 0, 0, 0};
+  for (int e = threadIdx.x; e < TX * K3; e += blockDim.x) {
+    int t = e / K3, zz = e - t * K3;
+    const size_t gi = (size_t)zz * plane + (size_t)yy * K1 + x0 + t;
+    const T th = theta[gi];
+    T2 v = r[e];
+    if (th != (T)0) {
+      const double pv = (double)psi[gi] * ((double)v.x * v.x + (double)v.y * v.y);
+      int jj = x0 + t; if (2 * jj > K1) jj -= K1;
+      int kk = yy; if (2 * kk > K2) kk -= K2;
+      int ll = zz; if (2 * ll > K3) ll -= K3;
+      double rp[3];
+      for (int c = 0; c < 3; ++c) rp[c] = (double)jj * sg.rc[3 * c] + (double)kk * sg.rc[3 * c + 1] + (double)ll * sg.rc[3 * c + 2];
+      st[0] += rp[0] * rp[0] * pv; st[1] += rp[0] * rp[1] * pv; st[2] += rp[0] * rp[2] * pv;
+      st[3] += rp[1] * rp[1] * pv; st[4] += rp[1] * rp[2] * pv; st[5] += rp[2] * rp[2] * pv;
+      v.x *= th; v.y *= th;
+    } else {
+      v.x = (T)0; v.y = (T)0;
+    }
+    r[e] = v;
+  }
+  T2* o = (r == a) ? b : a;
+  T2* r2 = fft_lines<T, T2>(r, o, pl, TX, tw, -1);
+  for (int e = threadIdx.x; e < TX * K3; e += blockDim.x) {
+    int zz = e / TX, t = e - zz * TX;
+    base[(size_t)zz * plane + t] = r2[t * K3 + zz];
+  }
+  block_reduce_store<6>(st, blk);
+}
+
+// --------------------------------------------------------------- gather
+// per atom: trunc-based splines (Int(u), u - Aint(u)), p^3 periodic grid
+// reads of the real potential, separable sums.  Writes the unscaled force
+// -(K.rcell) q sum dM M M phi and accumulates energy and net force.
+template <typename T>
+__global__ void k_spme_gather(int natms, const double* __restrict__ x, const double* __restrict__ y,
+                              const double* __restrict__ z, const double* __restrict__ q, SpmeGeom sg,
+                              const T* __restrict__ phi, double rk0, double rk1, double rk2, double* fout,
+                              double* blk) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[4] = {0, 0, 0, 0};
+  if (i < natms && fabs(q[i]) > DBL_MIN) {
+    const int p = sg.p;
+    T m[3][PMAX], dm[3][PMAX];
+    int n0[3];
+    for (int d = 0; d < 3; ++d) {
+      double u = sg.Kr[d] * (((sg.rc[d] * x[i] + sg.rc[d + 3] * y[i]) + sg.rc[d + 6] * z[i]) + 0.5);
+      double tr = trunc(u);
+      int n = (int)tr;
+      bspline_vals<T>((T)(u - tr), p, m[d], dm[d]);
+      n0[d] = n - p + 1;
+    }
+    const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
+    int ix[PMAX];
+    for (int t = 0; t < p; ++t) { int v = (n0[0] + t) % K0; if (v < 0) v += K0; ix[t] = v; }
+    const T qi = (T)q[i];
+    T e = 0, fxs = 0, fys = 0, fzs = 0;
+    for (int l = 0; l < p; ++l) {
+      int zz = (n0[2] + l) % K2; if (zz < 0) zz += K2;
+      for (int k = 0; k < p; ++k) {
+        int yy = (n0[1] + k) % K1; if (yy < 0) yy += K1;
+        const T* row = phi + ((size_t)zz * K1 + yy) * K0;
+        T s0 = 0, s1 = 0;
+#pragma unroll
+        for (int t = 0; t < PMAX; ++t) {
+          if (t < p) {
+            const T ph = row[ix[t]];
+            s0 += m[0][t] * ph;
+            s1 += dm[0][t] * ph;
+          }
+        }
+        const T myz = m[1][k] * m[2][l];
+        e += myz * s0;
+        fxs += myz * s1;
+        fys += dm[1][k] * m[2][l] * s0;
+        fzs += m[1][k] * dm[2][l] * s0;
+      }
+    }
+    const double fx_ = -(double)qi * (double)fxs * rk0, fy_ = -(double)qi * (double)fys * rk1,
+                 fz_ = -(double)qi * (double)fzs * rk2;
+    fout[3 * i] = fx_; fout[3 * i + 1] = fy_; fout[3 * i + 2] = fz_;
+    acc[0] = (double)qi * (double)e;
+    acc[1] = fx_; acc[2] = fy_; acc[3] = fz_;
+  } else if (i < natms) {
+    fout[3 * i] = 0; fout[3 * i + 1] = 0; fout[3 * i + 2] = 0;
+  }
+  block_reduce_store<4>(acc, blk);
+}
+
+// forces += (F - Fnet/N) * 2 * scale
+__global__ void k_spme_apply(int natms, const double* __restrict__ f, const double* __restrict__ sums, double scale2,
+                             double rn, double* fx, double* fy, double* fz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natms) return;
+  const double m0 = sums[1] * rn, m1 = sums[2] * rn, m2 = sums[3] * rn;
+  fx[i] += (f[3 * i] - m0) * scale2;
+  fy[i] += (f[3 * i + 1] - m1) * scale2;
+  fz[i] += (f[3 * i + 2] - m2) * scale2;
+}
+
+__global__ void k_spme_apply_fix(int natms, const double* __restrict__ f, const double* __restrict__ sums,
+                                 double scale2, double rn, unsigned long long* fixp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natms) return;
+  const double s = 1099511627776.0;
+  for (int d = 0; d < 3; ++d) {
+    double v = (f[3 * i + d] - sums[1 + d] * rn) * scale2;
+    atomicAdd(&fixp[3 * i + d], (unsigned long long)__double2ll_rn(v * s));
+  }
+}
+
+template <typename T>
+__global__ void k_cvt(const double* a, T* b, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (T)a[i];
+}
+
+inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+FftPlan make_plan(int N) {
+  FftPlan pl{};
+  pl.N = N;
+  int m = N;
+  while (m % 4 == 0) { pl.rad[pl.nrad++] = 4; m /= 4; }
+  while (m % 3 == 0) { pl.rad[pl.nrad++] = 3; m /= 3; }
+  while (m % 5 == 0) { pl.rad[pl.nrad++] = 5; m /= 5; }
+  while (m % 2 == 0) { pl.rad[pl.nrad++] = 2; m /= 2; }
+  if (m != 1) throw (int)GB_ERR_ARG;  // only 2^a 3^b 5^c lengths (parallel_fft.F90:2031)
+  return pl;
+}
+
+FftPlan plan1, plan2, plan3;
+SpmeGeom h_sg;
+
+int choose_brick(int K, int p) {
+  for (int B = p - 1; B <= BMAX; ++B)
+    if (K % B == 0) return B;
+  return -1;
+}
+
+size_t fft_smem(int N, int lines, size_t esz) { return (size_t)2 * lines * N * esz; }
+
+}  // namespace
+
+extern void invert_host(const double* a, double* b, double* d);
+extern void dcell_host(const double* aaa, double* bbb);
+
+// ====================================================================== host
+void spme_setup() {
+  const int p = g.p.nsplines;
+  if (p > PMAX || p < 3) throw (int)GB_ERR_ARG;
+  g.K1 = g.p.kmax[0]; g.K2 = g.p.kmax[1]; g.K3 = g.p.kmax[2];
+  if (g.K1 % TX || g.K2 % TX) throw (int)GB_ERR_ARG;
+  plan1 = make_plan(g.K1); plan2 = make_plan(g.K2); plan3 = make_plan(g.K3);
+  int Bs[3] = {choose_brick(g.K1, p), choose_brick(g.K2, p), choose_brick(g.K3, p)};
+  for (int d = 0; d < 3; ++d) {
+    if (Bs[d] < 0) {
+      // fall back to the whole dimension as one brick if it is small enough
+      if (g.p.kmax[d] <= BMAX) Bs[d] = g.p.kmax[d];
+      else throw (int)GB_ERR_ARG;
+    }
+  }
+  g.B1 = Bs[0]; g.B2 = Bs[1]; g.B3 = Bs[2];
+  g.nb1 = g.K1 / g.B1; g.nb2 = g.K2 / g.B2; g.nb3 = g.K3 / g.B3;
+  g.nbricks = g.nb1 * g.nb2 * g.nb3;
+  double det;
+  invert_host(g.cell, h_sg.rc, &det);
+  for (int d = 0; d < 3; ++d) {
+    h_sg.K[d] = g.p.kmax[d];
+    h_sg.Kr[d] = (double)g.p.kmax[d];
+  }
+  h_sg.B[0] = g.B1; h_sg.B[1] = g.B2; h_sg.B[2] = g.B3;
+  h_sg.nb[0] = g.nb1; h_sg.nb[1] = g.nb2; h_sg.nb[2] = g.nb3;
+  h_sg.p = p;
+  const size_t NG = (size_t)g.K1 * g.K2 * g.K3;
+  GB_CUDA(cudaMalloc(&g.spl, sizeof(double) * (size_t)g.natms * 3 * p));
+  GB_CUDA(cudaMalloc(&g.nidx, sizeof(int) * 3 * (size_t)g.natms));
+  GB_CUDA(cudaMalloc(&g.brick_of, sizeof(int) * (size_t)g.natms));
+  GB_CUDA(cudaMalloc(&g.brick_count, sizeof(int) * (g.nbricks + 2)));
+  GB_CUDA(cudaMalloc(&g.brick_start, sizeof(int) * (g.nbricks + 2)));
+  GB_CUDA(cudaMalloc(&g.brick_fill, sizeof(int) * (g.nbricks + 2)));
+  GB_CUDA(cudaMalloc(&g.brick_atoms, sizeof(int) * (size_t)g.natms));
+  GB_CUDA(cudaMalloc(&g.Q, sizeof(double) * NG));
+  GB_CUDA(cudaMalloc(&g.G, sizeof(double2) * NG));
+  GB_CUDA(cudaMalloc(&g.theta, sizeof(double) * NG));
+  GB_CUDA(cudaMalloc(&g.psi, sizeof(double) * NG));
+  GB_CUDA(cudaMalloc(&g.fspme, sizeof(double) * 3 * (size_t)g.natms));
+  // |b(m)|^2 (bspline_coeffs_gen, bspline.F90:73-190) on the host in FP64
+  std::vector<double> norm2[3];
+  {
+    std::vector<double> cs(p + 1, 0.0);
+    cs[2] = 1.0;
+    for (int k = 3; k <= p; ++k)
+      for (int j = k; j >= 2; --j) cs[j] = ((double)(j - 1) * cs[j] + (double)(k - j + 1) * cs[j - 1]) * (1.0 / (double)(k - 1));
+    const double twopi = 2.0 * 3.14159265358979323846264338327950288;
+    for (int d = 0; d < 3; ++d) {
+      int K = g.p.kmax[d];
+      std::vector<double> wr(K), wi(K);
+      wr[0] = 1.0; wi[0] = 0.0;
+      for (int i = 1; i <= K / 2; ++i) {
+        double arg = (twopi / (double)K) * (double)i;
+        wr[i] = std::cos(arg); wi[i] = std::sin(arg);
+        wr[K - i] = wr[i]; wi[K - i] = -wi[i];
+      }
+      norm2[d].resize(K);
+      for (int i = 0; i < K; ++i) {
+        double tr = 0, ti = 0;
+        for (int k = 0; k <= p - 2; ++k) {
+          int id = (int)(((long)i * k) % K);
+          tr += cs[k + 2] * wr[id]; ti += cs[k + 2] * wi[id];
+        }
+        int id = (int)(((long)i * (p - 1)) % K);
+        double nr = wr[id], ni = wi[id];
+        double den = tr * tr + ti * ti;
+        double cr = (nr * tr + ni * ti) / den, ci = (ni * tr - nr * ti) / den;
+        norm2[d][i] = cr * cr + ci * ci;
+      }
+    }
+  }
+  // influence function theta and stress factor psi (ewald_spole.F90:1306-1374)
+  {
+    const double pi = 3.14159265358979323846264338327950288, sqrpi = std::sqrt(pi);
+    double rc[9];
+    invert_host(g.cell, rc, &det);
+    double rcp[10];
+    dcell_host(rc, rcp);
+    double recip_conv_fac = pi / g.p.alpha;
+    double test_fac = (1.0e-6 / recip_conv_fac) * (1.0e-6 / recip_conv_fac);
+    double cut = 0.5 * 1.05 * std::min((double)g.K1 * rcp[6], std::min((double)g.K2 * rcp[7], (double)g.K3 * rcp[8]));
+    double cut2 = cut * cut;
+    std::vector<double> th(NG), ps(NG);
+    for (int l = 0; l < g.K3; ++l) {
+      int ll = l; if (2 * ll > g.K3) ll -= g.K3;
+      for (int k = 0; k < g.K2; ++k) {
+        int kk = k; if (2 * kk > g.K2) kk -= g.K2;
+        for (int j = 0; j < g.K1; ++j) {
+          int jj = j; if (2 * jj > g.K1) jj -= g.K1;
+          double r0 = (double)ll * rc[2] + (double)kk * rc[1] + (double)jj * rc[0];
+          double r1 = (double)ll * rc[5] + (double)kk * rc[4] + (double)jj * rc[3];
+          double r2 = (double)ll * rc[8] + (double)kk * rc[7] + (double)jj * rc[6];
+          double k2 = r0 * r0 + r1 * r1 + r2 * r2;
+          size_t gi = ((size_t)l * g.K2 + k) * g.K1 + j;
+          if (k2 <= cut2 && k2 > test_fac) {
+            double bb = norm2[2][l] * norm2[1][k] * norm2[0][j];
+            double f = std::sqrt(k2) * recip_conv_fac;
+            th[gi] = bb * std::exp(-(f * f)) / (sqrpi * f * f);
+            ps[gi] = th[gi] * (-2.0 * ((1.0 + f * f) / k2));
+          } else {
+            th[gi] = 0.0; ps[gi] = 0.0;
+          }
+        }
+      }
+    }
+    GB_CUDA(cudaMemcpy(g.theta, th.data(), sizeof(double) * NG, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(g.psi, ps.data(), sizeof(double) * NG, cudaMemcpyHostToDevice));
+  }
+  // twiddles e^{+2 pi i t / K}
+  auto mk_tw = [](int K, double2** dd, float2** df) {
+    std::vector<double2> t(K);
+    std::vector<float2> tf(K);
+    const double twopi = 2.0 * 3.14159265358979323846264338327950288;
+    for (int i = 0; i < K; ++i) {
+      double a = twopi * (double)i / (double)K;
+      t[i] = make_double2(std::cos(a), std::sin(a));
+      tf[i] = make_float2((float)t[i].x, (float)t[i].y);
+    }
+    GB_CUDA(cudaMalloc(dd, sizeof(double2) * K));
+    GB_CUDA(cudaMalloc(df, sizeof(float2) * K));
+    GB_CUDA(cudaMemcpy(*dd, t.data(), sizeof(double2) * K, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(*df, tf.data(), sizeof(float2) * K, cudaMemcpyHostToDevice));
+  };
+  mk_tw(g.K1, &g.tw1, &g.tw1f);
+  mk_tw(g.K2, &g.tw2, &g.tw2f);
+  mk_tw(g.K3, &g.tw3, &g.tw3f);
+  // FP32 copies for the mixed form
+  GB_CUDA(cudaMalloc(&g.Qf, sizeof(float) * NG));
+  GB_CUDA(cudaMalloc(&g.Gf, sizeof(float2) * NG));
+  GB_CUDA(cudaMalloc(&g.theta_f, sizeof(float) * NG));
+  GB_CUDA(cudaMalloc(&g.psi_f, sizeof(float) * NG));
+  k_cvt<float><<<nblocks((long long)NG, 256), 256, 0, g.stream>>>(g.theta, g.theta_f, NG);
+  GB_LAUNCHED();
+  k_cvt<float><<<nblocks((long long)NG, 256), 256, 0, g.stream>>>(g.psi, g.psi_f, NG);
+  GB_LAUNCHED();
+  // dynamic shared memory limits
+  const int maxN = std::max(g.K1, std::max(g.K2, g.K3));
+  int smem = (int)std::max(fft_smem(maxN, TX, sizeof(double2)), fft_smem(g.K1, 8, sizeof(double2)));
+  smem = std::max(smem, 48 * 1024);
+  GB_CUDA(cudaFuncSetAttribute(k_fft_x_fwd<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_x_inv<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_y<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_z_conv<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_x_fwd<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_x_inv<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_y<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_z_conv<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+}
+
+template <typename T, typename T2>
+static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
+  cudaStream_t st = g.stream;
+  const int n = g.natms, p = g.p.nsplines;
+  T* spl = reinterpret_cast<T*>(g.spl);
+  T* Q = std::is_same<T, double>::value ? reinterpret_cast<T*>(g.Q) : reinterpret_cast<T*>(g.Qf);
+  T2* G = std::is_same<T, double>::value ? reinterpret_cast<T2*>(g.G) : reinterpret_cast<T2*>(g.Gf);
+  const T* th = std::is_same<T, double>::value ? reinterpret_cast<const T*>(g.theta) : reinterpret_cast<const T*>(g.theta_f);
+  const T* ps = std::is_same<T, double>::value ? reinterpret_cast<const T*>(g.psi) : reinterpret_cast<const T*>(g.psi_f);
+  const T2* tw1 = std::is_same<T, double>::value ? reinterpret_cast<const T2*>(g.tw1) : reinterpret_cast<const T2*>(g.tw1f);
+  const T2* tw2 = std::is_same<T, double>::value ? reinterpret_cast<const T2*>(g.tw2) : reinterpret_cast<const T2*>(g.tw2f);
+  const T2* tw3 = std::is_same<T, double>::value ? reinterpret_cast<const T2*>(g.tw3) : reinterpret_cast<const T2*>(g.tw3f);
+  // splines + brick binning
+  GB_CUDA(cudaMemsetAsync(g.brick_count, 0, sizeof(int) * (g.nbricks + 2), st));
+  GB_CUDA(cudaMemsetAsync(g.brick_fill, 0, sizeof(int) * (g.nbricks + 2), st));
+  k_spme_prep<T><<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, h_sg, spl, g.nidx, g.brick_of,
+                                                   g.brick_count);
+  GB_LAUNCHED();
+
+  scan_exclusive(g.brick_count, g.brick_start, g.nbricks + 1);
+  int* tmp = gb_scan_scratch(n + 1);
+  k_brick_scatter<<<nblocks(n, 256), 256, 0, st>>>(n, g.brick_of, g.brick_start, g.brick_fill, tmp);
+  GB_LAUNCHED();
+  k_brick_sort<<<nblocks((long long)g.nbricks * 32, 256), 256, 0, st>>>(g.nbricks, g.brick_start, tmp, g.brick_atoms);
+  GB_LAUNCHED();
+  // spreading
+  {
+    int threads = ((g.B2 * g.B3 + 31) / 32) * 32;
+    k_spme_spread<T><<<g.nbricks, threads, 0, st>>>(h_sg, g.brick_start, g.brick_atoms, spl, g.nidx, g.chge, Q);
+    GB_LAUNCHED();
+  }
+  // FFT + convolution
+  const int lines = 8;
+  const int rows = g.K2 * g.K3;
+  k_fft_x_fwd<T, T2><<<nblocks(rows, lines), 256, fft_smem(g.K1, lines, sizeof(T2)), st>>>(Q, G, plan1, tw1, rows, lines);
+  GB_LAUNCHED();
+  k_fft_y<T, T2><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2, +1);
+  GB_LAUNCHED();
+  const int nbz = (g.K1 / TX) * g.K2;
+  double* blkz = gb_blkacc(nbz * 6 + nblocks(n, 128) * 4);
+  k_fft_z_conv<T, T2><<<nbz, 256, fft_smem(g.K3, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, g.K3, plan3, tw3, th, ps, h_sg, blkz);
+  GB_LAUNCHED();
+  k_fft_y<T, T2><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2, -1);
+  GB_LAUNCHED();
+  k_fft_x_inv<T, T2><<<nblocks(rows, lines), 256, fft_smem(g.K1, lines, sizeof(T2)), st>>>(G, Q, plan1, tw1, rows, lines);
+  GB_LAUNCHED();
+  // gather
+  double rc[9];
+  for (int k = 0; k < 9; ++k) rc[k] = h_sg.rc[k];
+  double rk[3];
+  for (int a = 0; a < 3; ++a) rk[a] = rc[a] * h_sg.Kr[0] + rc[a + 3] * h_sg.Kr[1] + rc[a + 6] * h_sg.Kr[2];
+  const int nbg = nblocks(n, 128);
+  double* blkg = blkz + (size_t)nbz * 6;
+  k_spme_gather<T><<<nbg, 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, h_sg, Q, rk[0], rk[1], rk[2], g.fspme, blkg);
+  GB_LAUNCHED();
+  gb_reduce_blocks(blkz, nbz, 6, &g.sc->acc[A_SPME_STR]);
+  gb_reduce_blocks(blkg, nbg, 4, &g.sc->acc[A_GATHER]);
+  const double pi = 3.14159265358979323846264338327950288;
+  const double scale = pi * std::sqrt(pi) * std::pow(g.p.alpha, 1 - 3) * (0.5 / g.volm) * g.scaling;
+  if (g.precision == GB_FP64) {
+    k_spme_apply<<<nblocks(n, 256), 256, 0, st>>>(n, g.fspme, &g.sc->acc[A_GATHER], 2.0 * scale, 1.0 / (double)n,
+                                                   g.fx, g.fy, g.fz);
+  } else {
+    k_spme_apply_fix<<<nblocks(n, 256), 256, 0, st>>>(n, g.fspme, &g.sc->acc[A_GATHER], 2.0 * scale,
+                                                       1.0 / (double)n, (unsigned long long*)g.fixp);
+  }
+  GB_LAUNCHED();
+  gb_sync_scalars();
+  const double* A = g.hsc->acc;
+  double eng = A[A_GATHER] * scale;
+  double s6[6];
+  for (int k = 0; k < 6; ++k) s6[k] = A[A_SPME_STR + k] * scale;
+  double stt[9] = {s6[0], s6[1], s6[2], s6[1], s6[3], s6[4], s6[2], s6[4], s6[5]};
+  *eng_rc = eng + g.self_interaction;
+  stt[0] += eng; stt[4] += eng; stt[8] += eng;
+  for (int k = 0; k < 9; ++k) stress9[k] += stt[k];
+  *vir_rc = -(stt[0] + stt[4] + stt[8]);
+}
+
+void spme_forces(double* eng_rc, double* vir_rc, double* stress9) {
+  if (g.precision == GB_FP64) spme_run<double, double2>(eng_rc, vir_rc, stress9);
+  else spme_run<float, float2>(eng_rc, vir_rc, stress9);
+}

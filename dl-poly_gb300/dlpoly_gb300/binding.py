@@ -1,0 +1,190 @@
+"""ctypes binding of the path's C-ABI (include/gb300_dlpoly.h).
+
+`PathLib` wraps one shared library whose exports follow the gb_* signatures
+under a name prefix.  The GB300 library exports them as gb_*; the method names
+mirror the reference's Fortran routines that each export replaces, so a test
+reads like the reference's own call sequence:
+
+    relocate()            relocate_particles + set_halo_particles (halo.F90:153)
+    link_cell_pairs()     neighbours.F90:356
+    two_body_forces()     drivers.F90:655-786 (SPME + pair loop)
+    ewald_spme_forces()   ewald_spole.F90:244
+    nve_0_vv(stage)       nve.F90:38 (with apply_shake / apply_rattle)
+    md_vv(nsteps)         drivers.F90:2059 resident loop
+
+Every non-zero status raises `PathError` carrying the DL_POLY error code.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_double, c_int, c_int32, c_int64, c_void_p
+
+import numpy as np
+
+from .systems import GbParams, GbStepStats, System
+
+_d = POINTER(c_double)
+_i = POINTER(c_int32)
+
+
+class PathError(RuntimeError):
+    def __init__(self, code: int, where: str, text: str = ""):
+        super().__init__(f"{where}: status {code} {text}".strip())
+        self.code = code
+
+
+def _ptr(a, t):
+    if a is None:
+        return None
+    return a.ctypes.data_as(t)
+
+
+SIGNATURES = {
+    "init": (c_int, [POINTER(GbParams), c_int, _i, _d, _d, _i, _d, c_int, _i, _d, _i]),
+    "upload_state": (c_int, [_d, _d, _d, _d, _d, _d]),
+    "download_state": (c_int, [_d, _d, _d, _d, _d, _d, _d, _d, _d]),
+    "relocate": (c_int, []),
+    "list_build": (c_int, [_i, c_int, _i]),
+    "vnl_check": (c_int, [_i]),
+    "refresh": (c_int, [_i]),
+    "forces": (c_int, [_d, _d]),
+    "spme": (c_int, [_d, _d, _d]),
+    "real": (c_int, [_d, _d]),
+    "vv": (c_int, [c_int, _d, _d, _i, _d, _d]),
+    "md_run": (c_int, [c_int, POINTER(GbStepStats)]),
+    "finalize": (None, []),
+}
+
+
+class PathLib:
+    """One loaded implementation of the path (library + symbol prefix)."""
+
+    def __init__(self, lib: ctypes.CDLL, prefix: str):
+        self.lib = lib
+        self.prefix = prefix
+        self.fn = {}
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, prefix + name)
+            f.restype = res
+            f.argtypes = args
+            self.fn[name] = f
+        self.sys: System | None = None
+        self.params: GbParams | None = None
+
+    def _call(self, name, *args):
+        st = self.fn[name](*args)
+        if st != 0:
+            raise PathError(st, self.prefix + name, self.strerror(st))
+        return st
+
+    def strerror(self, st):
+        f = getattr(self.lib, self.prefix + "strerror", None)
+        if f is None:
+            return ""
+        f.restype = ctypes.c_char_p
+        f.argtypes = [c_int]
+        return (f(st) or b"").decode()
+
+    # ---------------------------------------------------------------- set-up
+    def init(self, s: System, precision: int = 0, max_list: int | None = None):
+        p = s.params(precision, max_list)
+        self.params = p
+        self.sys = s
+        excl = s.excl_array(p)
+        lc = s.listcon.astype(np.int32) if s.ntcons else np.zeros(3, np.int32)
+        pc = s.prmcon.astype(np.float64) if s.ntcons else np.zeros(1)
+        self._keep = [s.ltype, s.chge, s.weight, s.lfrzn, s.vdw_prm, lc, pc, excl]
+        self._call("init", ctypes.byref(p), s.natms, _ptr(s.ltype, _i), _ptr(s.chge, _d),
+                   _ptr(s.weight, _d), _ptr(s.lfrzn, _i), _ptr(s.vdw_prm, _d), s.ntcons,
+                   _ptr(lc, _i), _ptr(pc, _d), _ptr(excl, _i))
+        self.upload(s.x, s.y, s.z, s.vx, s.vy, s.vz)
+
+    def upload(self, x, y, z, vx=None, vy=None, vz=None):
+        a = [np.ascontiguousarray(v, np.float64) if v is not None else None for v in (x, y, z, vx, vy, vz)]
+        self._call("upload_state", *[_ptr(v, _d) for v in a])
+
+    def download(self):
+        n = self.sys.natms
+        out = [np.empty(n) for _ in range(9)]
+        self._call("download_state", *[_ptr(v, _d) for v in out])
+        return dict(zip(("x", "y", "z", "vx", "vy", "vz", "fx", "fy", "fz"), out))
+
+    # ----------------------------------------------------------- path calls
+    def relocate(self):
+        self._call("relocate")
+
+    def link_cell_pairs(self, want_list: bool = True):
+        p = self.params
+        ld = p.max_list + 4
+        out = np.zeros(ld * self.sys.natms, np.int32) if want_list else None
+        need = np.zeros(1, np.int32)
+        self._call("list_build", _ptr(out, _i), ld, _ptr(need, _i))
+        return None if out is None else out.reshape(self.sys.natms, ld)
+
+    def list_build_status(self):
+        """Build and return (status, needed max_list) without raising."""
+        p = self.params
+        need = np.zeros(1, np.int32)
+        st = self.fn["list_build"](None, p.max_list + 4, _ptr(need, _i))
+        return st, int(need[0])
+
+    def vnl_check(self) -> bool:
+        u = np.zeros(1, np.int32)
+        self._call("vnl_check", _ptr(u, _i))
+        return bool(u[0])
+
+    def refresh(self) -> bool:
+        u = np.zeros(1, np.int32)
+        self._call("refresh", _ptr(u, _i))
+        return bool(u[0])
+
+    def two_body_forces(self):
+        e = np.zeros(8)
+        s = np.zeros(9)
+        self._call("forces", _ptr(e, _d), _ptr(s, _d))
+        keys = ("engcpe_rc", "vircpe_rc", "engcpe_rl", "vircpe_rl", "engcpe_ex", "vircpe_ex", "engvdw", "virvdw")
+        return dict(zip(keys, e)), s
+
+    def ewald_spme_forces(self):
+        e = np.zeros(1)
+        v = np.zeros(1)
+        s = np.zeros(9)
+        self._call("spme", _ptr(e, _d), _ptr(v, _d), _ptr(s, _d))
+        return float(e[0]), float(v[0]), s
+
+    def real_space_forces(self):
+        e = np.zeros(6)
+        s = np.zeros(9)
+        self._call("real", _ptr(e, _d), _ptr(s, _d))
+        keys = ("engcpe_rl", "vircpe_rl", "engcpe_ex", "vircpe_ex", "engvdw", "virvdw")
+        return dict(zip(keys, e)), s
+
+    def nve_0_vv(self, stage: int):
+        sk = np.zeros(9)
+        ek = np.zeros(1)
+        it = np.zeros(1, np.int32)
+        vc = np.zeros(1)
+        sc = np.zeros(9)
+        self._call("vv", stage, _ptr(sk, _d), _ptr(ek, _d), _ptr(it, _i), _ptr(vc, _d), _ptr(sc, _d))
+        return dict(strkin=sk, engke=float(ek[0]), iters=int(it[0]), vircon=float(vc[0]), strcon=sc)
+
+    def md_vv(self, nsteps: int):
+        arr = (GbStepStats * max(1, nsteps))()
+        self._call("md_run", nsteps, arr)
+        return [arr[k] for k in range(nsteps)]
+
+    def start(self):
+        """Start-up as the reference does before md_vv: wrap, halo, list, forces."""
+        self.relocate()
+        self.link_cell_pairs(want_list=False)
+        return self.two_body_forces()
+
+    def finalize(self):
+        self.fn["finalize"]()
+
+
+def stats_to_dict(s: GbStepStats) -> dict:
+    d = {k: getattr(s, k) for k, _ in GbStepStats._fields_ if k not in ("stress", "strkin")}
+    d["stress"] = np.array(s.stress[:])
+    d["strkin"] = np.array(s.strkin[:])
+    return d

@@ -1,0 +1,203 @@
+/*
+ * gb300_dlpoly.h - C-ABI of the GB300 (sm_103a) per-timestep force and update
+ * path of DL_POLY 5: link-cell Verlet list, real-space vdW + erfc-Coulomb
+ * pairs, SPME reciprocal space, NVE velocity Verlet and SHAKE/RATTLE.
+ *
+ * The library keeps one device context (one GPU, one CUDA stream), exactly as
+ * a serial DL_POLY rank keeps one configuration.  Positions, velocities,
+ * forces, halo images, the Verlet list and the SPME grids stay resident in HBM
+ * between calls; host arrays are borrowed only for the duration of a call.
+ *
+ * Conventions shared with the Fortran side (ISO_C_BINDING):
+ *   - every array is a plain pointer plus a size, column-major where the
+ *     Fortran array is 2-D, and index VALUES are 1-based (the Verlet list
+ *     stores Fortran atom indices, list_excl stores global atom ids);
+ *   - every entry point returns an int status: 0 = success, a positive value
+ *     is the DL_POLY error code the caller passes to error(kode)
+ *     (source/errors_warnings.F90:840), a negative value is a library error
+ *     described by gb_strerror();
+ *   - no exception, exit or device trap crosses the boundary.
+ */
+#ifndef GB300_DLPOLY_H
+#define GB300_DLPOLY_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* DL_POLY error codes returned through the ABI (errors_warnings.F90). */
+#define GB_OK 0
+#define GB_ERR_CUTOFF_CELL 95     /* cutoff_extended >= half cell width (neighbours.F90:410) */
+#define GB_ERR_SHAKE 105          /* SHAKE did not converge (constraints.F90:996) */
+#define GB_ERR_LIST_OVERFLOW 106  /* Verlet list overflow (neighbours.F90:1193) */
+#define GB_ERR_LINK_CELLS 307     /* fewer than one link cell per direction (neighbours.F90:428) */
+#define GB_ERR_UNSAFE 505         /* unsafe pair/grid state (two_body.F90:751) */
+#define GB_ERR_RATTLE 515         /* RATTLE did not converge (constraints.F90:748) */
+#define GB_ERR_HALO 56            /* halo larger than mxatms (deport_data.F90:1870) */
+/* library errors */
+#define GB_ERR_NOT_INIT (-1)
+#define GB_ERR_CUDA (-2)
+#define GB_ERR_ARG (-3)
+#define GB_ERR_NO_DEVICE (-4)
+#define GB_ERR_NONFINITE (-5)
+
+/* Precision forms of the force path. */
+#define GB_FP64 0   /* plain: FP64 throughout */
+#define GB_MIXED 1  /* FP32 pair/spline/FFT arithmetic, int64 fixed-point forces (2^40) */
+
+/*
+ * Run parameters.  Mirrors the CONTROL/FIELD-derived scalars the reference
+ * keeps in neigh%, ewld%, electro%, vdws%, cons% and thermo%.
+ */
+typedef struct gb_params {
+  double cell[9];       /* config%cell(1:9), cell vectors as rows (configuration.F90) */
+  double rcut;          /* neigh%cutoff: real-space Coulomb cutoff */
+  double rpad;          /* neigh%padding: Verlet skin */
+  double rvdw;          /* vdws%cutoff */
+  double alpha;         /* ewld%alpha (1/Angstrom) */
+  double epsq;          /* electro%eps, relative dielectric constant */
+  double tstep;         /* thermo%tstep (ps) */
+  double shake_tol;     /* cons%tolerance (Angstrom) */
+  double pdplnc;        /* neigh%pdplnc, sub-celling threshold density (default 50) */
+  int32_t kmax[3];      /* ewld%kspace%k_vec_dim, SPME grid */
+  int32_t nsplines;     /* ewld%bspline%num_splines, B-spline order p */
+  int32_t spline_pad;   /* ewld%bspline%num_spline_pad (halo width for SPME) */
+  int32_t vdw_direct;   /* 0 = tabulated vdW (default, vdw.F90:1790), 1 = direct (vdw.F90:1578) */
+  int32_t shake_maxit;  /* cons%max_iter_shake (default 250) */
+  int32_t max_list;     /* neigh%max_list */
+  int32_t max_exclude;  /* neigh%max_exclude */
+  int32_t mxatms;       /* config%mxatms: capacity for local + halo atoms */
+  int32_t precision;    /* GB_FP64 or GB_MIXED */
+  int32_t ntypes;       /* sites%ntype_atom */
+  int32_t reserved[7];
+} gb_params;
+
+/* Per-step scalars returned by the resident MD loop. */
+typedef struct gb_step_stats {
+  double engcpe_rc, vircpe_rc;  /* SPME reciprocal + self energy, virial */
+  double engcpe_rl, vircpe_rl;  /* real-space Ewald */
+  double engcpe_ex, vircpe_ex;  /* exclusion correction */
+  double engvdw, virvdw;        /* van der Waals (without long-range correction) */
+  double engke;                 /* kinetic energy (kinetics.F90:218) */
+  double vircon;                /* constraint virial */
+  double stress[9];             /* configurational stress (two-body + SPME) */
+  double strkin[9];             /* kinetic stress */
+  int32_t list_rebuilt;         /* 1 if the Verlet list was rebuilt this step */
+  int32_t shake_iters, rattle_iters;
+  int32_t mts_full;             /* 1 if full SPME ran this step (learned-MTS form) */
+} gb_step_stats;
+
+/*
+ * Replaces the start-up sequence molecular_dynamics_initialise ->
+ * set_halo_particles (source/meta.F90:324-427) for the data the hot path
+ * needs: uploads topology, builds the erfc and vdW interpolation tables
+ * (electrostatic.F90:88, vdw.F90:1397), the SPME |b(m)|^2 table
+ * (bspline.F90:73) and the self-interaction energy (spme.F90:159).
+ *   ltype[natms]     1-based atom type (config%ltype)
+ *   chge/weight      charge (e) and mass (amu) per atom
+ *   lfrzn[natms]     frozen flag
+ *   vdw_prm[3*nkey]  per type-pair key ai*(ai-1)/2+aj: (kind 0=none,1=lj, epsilon [internal units], sigma)
+ *   listcon[3*ntcons] (type, global i, global j) as cons%listcon(0:2,k)
+ *   prmcon[ntcontypes] constraint bond lengths (cons%prmcon)
+ *   list_excl[(max_exclude+1)*natms] neigh%list_excl, column-major, sorted global ids
+ */
+int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double* chge,
+            const double* weight, const int32_t* lfrzn, const double* vdw_prm, int ntcons,
+            const int32_t* listcon, const double* prmcon, const int32_t* list_excl);
+
+/* Upload positions (x,y,z) and velocities for the natms local atoms.
+ * Replaces the host copies read by read_config (configuration.F90:846). */
+int gb_upload_state(const double* x, const double* y, const double* z, const double* vx,
+                    const double* vy, const double* vz);
+
+/* Same, from the reference's 64-byte corePart records (particle.F90:13-19):
+ * xxx,yyy,zzz,fxx,fyy,fzz,chge (f64) + 2 x int32 pad.  Forces are ignored. */
+int gb_upload_parts(const void* parts, const double* vx, const double* vy, const double* vz);
+
+/* Download positions, velocities and forces of the local atoms (any pointer may be NULL). */
+int gb_download_state(double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                      double* fx, double* fy, double* fz);
+
+/* Download into corePart records (positions, forces, charge). */
+int gb_download_parts(void* parts, double* vx, double* vy, double* vz);
+
+/*
+ * relocate_particles + set_halo_particles in serial form
+ * (deport_data.F90:2870 -> numerics.F90:1851 pbcshift; halo.F90:153) and
+ * vnl_set_check (neighbours.F90:305): wrap into the cell, rebuild the halo
+ * images on the device, set the displacement checkpoint.
+ */
+int gb_relocate(void);
+
+/*
+ * link_cell_pairs (neighbours.F90:356-1414) on the device: half-shell Verlet
+ * list with sub-celling, nir bypass cells, frozen and excluded reordering.
+ * If list_out != NULL the list is copied back in the reference layout
+ * list(-3:max_list, 1:natms) column-major (ldlist must be max_list+4).
+ * On overflow returns 106 and writes the needed max_list into *max_list_io.
+ */
+int gb_list_build(int32_t* list_out, int ldlist, int32_t* max_list_io);
+
+/* vnl_check (neighbours.F90:123): sets *update = 1 when the largest
+ * displacement since the last rebuild reaches half the padding. */
+int gb_vnl_check(int32_t* update);
+
+/* refresh_mappings (drivers.F90:1009) serial form: vnl_check, then either
+ * relocate + halo rebuild (update) or refresh_halo_positions (halo.F90:47). */
+int gb_refresh(int32_t* update);
+
+/*
+ * calculate_forces force part (drivers.F90:655-786): zero forces, SPME
+ * reciprocal (ewald_spme_forces_coul, ewald_spole.F90:244), then the
+ * two_body_forces pair loop (two_body.F90:339-606).
+ *   eng_out[8] = engcpe_rc, vircpe_rc, engcpe_rl, vircpe_rl, engcpe_ex, vircpe_ex, engvdw, virvdw
+ *   stress_out[9] configurational stress
+ */
+int gb_forces(double* eng_out, double* stress_out);
+
+/* ewald_spme_forces_coul alone (forces zeroed first); for component tests. */
+int gb_spme(double* eng_rc, double* vir_rc, double* stress_out);
+
+/* two_body pair loop alone (forces zeroed first, no SPME); for component tests.
+ * eng_out[6] = engcpe_rl, vircpe_rl, engcpe_ex, vircpe_ex, engvdw, virvdw */
+int gb_real(double* eng_out, double* stress_out);
+
+/* nve_0_vv (nve.F90:38): stage 1 = half kick + drift + SHAKE (apply_shake,
+ * constraints.F90:1071); stage 2 = half kick + RATTLE (apply_rattle,
+ * constraints.F90:1032) + kinstress (kinetics.F90:218). */
+int gb_vv(int stage, double* strkin, double* engke, int32_t* iters, double* vircon,
+          double* strcon);
+
+/* Resident MD loop (md_vv, drivers.F90:2059-2288): nsteps of VV1+SHAKE,
+ * refresh, forces, VV2+RATTLE with no host round trip; stats[nsteps] may be NULL. */
+int gb_md_run(int nsteps, gb_step_stats* stats);
+
+/* Learned multiple-time-step form: full SPME every k steps, the per-atom MLP
+ * predicts the reciprocal-force increment on inner steps, and plain SPME is the
+ * fallback when the checked RMS error exceeds tol (relative).  k = 1 disables. */
+int gb_mts_config(int k, double tol, int train_steps);
+
+/* Switch the force path between GB_FP64 and GB_MIXED after gb_init. */
+int gb_set_precision(int precision);
+
+/* Device time (ms) of the last gb_md_run per region, CUDA events on the
+ * library stream: [0] list+halo, [1] real-space, [2] SPME, [3] integrate,
+ * [4] total.  n = number of slots to copy. */
+int gb_last_timings(double* ms, int n);
+
+/* Number of kernels the library launched since gb_init (its own count). */
+int64_t gb_kernel_launches(void);
+
+/* Release device memory; gb_init may be called again afterwards. */
+void gb_finalize(void);
+
+/* Human-readable text for a status code. */
+const char* gb_strerror(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300_DLPOLY_H */

@@ -1,0 +1,173 @@
+"""GPU parity: the CUDA path against the FP64 oracle on the same seeded inputs,
+through the C-ABI (gb_* entry points).
+
+Bars (BASELINE the benchmark spec): pair sets bit-exact; FP64 forces within 1e-10 of
+the oracle (max |dF| relative to the rms force); energies and virials within
+1e-10 relative; mixed form rms force error <= 1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+from conftest import force_dev, force_rms_rel
+from dlpoly_gb300 import systems
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+CASES = {
+    "nacl_4096": lambda: systems.nacl_melt(16),
+    "water_1536": lambda: systems.spce_water(8),
+    "water_5184": lambda: systems.spce_water(12),
+    "nacl_13824": lambda: systems.nacl_melt(24, kmax=72),
+}
+
+
+def _pair(gpu_lib, oracle_lib, s, precision=0, **kw):
+    gpu_lib.init(s, precision=precision, **kw)
+    oracle_lib.init(s, **kw)
+    gpu_lib.relocate()
+    oracle_lib.relocate()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_pair_set_bit_exact(gpu_lib, oracle_lib, name):
+    s = CASES[name]()
+    _pair(gpu_lib, oracle_lib, s)
+    ld = gpu_lib.link_cell_pairs()
+    lr = oracle_lib.link_cell_pairs()
+    # the whole list(-3:max_list, natms) array: markers, entries and their order
+    assert np.array_equal(ld, lr)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_forces_fp64(gpu_lib, oracle_lib, name):
+    s = CASES[name]()
+    _pair(gpu_lib, oracle_lib, s)
+    gpu_lib.link_cell_pairs(want_list=False)
+    oracle_lib.link_cell_pairs(want_list=False)
+    ed, sd = gpu_lib.two_body_forces()
+    er, sr = oracle_lib.two_body_forces()
+    assert force_dev(gpu_lib.download(), oracle_lib.download()) < FP64_TOL
+    for k in er:
+        assert abs(ed[k] - er[k]) <= FP64_TOL * max(abs(er[k]), 1.0), (k, ed[k], er[k])
+    assert np.abs(sd - sr).max() <= FP64_TOL * np.abs(sr).max()
+
+
+def test_spme_alone_fp64(gpu_lib, oracle_lib):
+    s = systems.nacl_melt(16)
+    _pair(gpu_lib, oracle_lib, s)
+    ed, vd, sd = gpu_lib.ewald_spme_forces()
+    er, vr, sr = oracle_lib.ewald_spme_forces()
+    assert ed == pytest.approx(er, rel=FP64_TOL)
+    assert vd == pytest.approx(vr, rel=1e-9)
+    assert force_dev(gpu_lib.download(), oracle_lib.download()) < FP64_TOL
+
+
+def test_vdw_known_answer_on_gpu(gpu_lib):
+    """source/unit_tests/test_vdw.F90:46-59 entry 2 (LJ eps=1 sigma=2 at r=1) through the device path."""
+    s = systems.lj_pair(eps=1.0, sigma=2.0, r=1.0)
+    gpu_lib.init(s)
+    gpu_lib.relocate()
+    gpu_lib.link_cell_pairs(want_list=False)
+    e, _ = gpu_lib.real_space_forces()
+    assert e["engvdw"] == pytest.approx(16128.0, rel=1e-13)
+    assert e["virvdw"] == pytest.approx(-195072.0, rel=1e-13)
+    d = gpu_lib.download()
+    assert d["fx"][1] == pytest.approx(195072.0, rel=1e-13)
+
+
+@pytest.mark.parametrize("name,nsteps", [("nacl_4096", 30), ("water_1536", 12)])
+def test_md_steps_fp64(gpu_lib, oracle_lib, name, nsteps):
+    """Resident md_vv loop (VV + SHAKE/RATTLE + conditional list rebuild) step by step."""
+    s = CASES[name]()
+    gpu_lib.init(s)
+    oracle_lib.init(s)
+    gpu_lib.start()
+    oracle_lib.start()
+    sd = gpu_lib.md_vv(nsteps)
+    sr = oracle_lib.md_vv(nsteps)
+    assert [x.list_rebuilt for x in sd] == [x.list_rebuilt for x in sr]
+    assert any(x.list_rebuilt for x in sr) or name.startswith("water")
+    assert [x.shake_iters for x in sd] == [x.shake_iters for x in sr]
+    assert [x.rattle_iters for x in sd] == [x.rattle_iters for x in sr]
+    a, b = gpu_lib.download(), oracle_lib.download()
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        scale = np.abs(b[k]).max()
+        assert np.abs(a[k] - b[k]).max() <= 1e-9 * scale, k
+    assert force_dev(a, b) < 1e-8
+    for x, y in zip(sd, sr):
+        assert x.engke == pytest.approx(y.engke, rel=1e-9)
+        assert x.engcpe_rl == pytest.approx(y.engcpe_rl, rel=1e-9)
+
+
+def test_md_matches_golden(gpu_lib):
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "nacl_4096.npz"))
+    s = systems.nacl_melt(16)
+    gpu_lib.init(s)
+    gpu_lib.relocate()
+    lst = gpu_lib.link_cell_pairs()
+    assert np.array_equal(lst[:, 3], g["list_count"])
+    gpu_lib.two_body_forces()
+    d = gpu_lib.download()
+    F = np.stack([d["fx"], d["fy"], d["fz"]], 1)
+    assert np.abs(F - g["f0"]).max() / np.sqrt((g["f0"] ** 2).sum(1).mean()) < FP64_TOL
+    gpu_lib.md_vv(5)
+    d = gpu_lib.download()
+    assert np.abs(np.stack([d["x"], d["y"], d["z"]], 1) - g["x5"]).max() < 1e-9
+
+
+@pytest.mark.parametrize("name", ["nacl_4096", "water_5184"])
+def test_mixed_force_error(gpu_lib, oracle_lib, name):
+    s = CASES[name]()
+    _pair(gpu_lib, oracle_lib, s, precision=1)
+    gpu_lib.link_cell_pairs(want_list=False)
+    oracle_lib.link_cell_pairs(want_list=False)
+    ed, _ = gpu_lib.two_body_forces()
+    er, _ = oracle_lib.two_body_forces()
+    a, b = gpu_lib.download(), oracle_lib.download()
+    assert force_rms_rel(a, b) <= 1e-5
+    tot_d = sum(ed[k] for k in ("engcpe_rc", "engcpe_rl", "engcpe_ex", "engvdw"))
+    tot_r = sum(er[k] for k in ("engcpe_rc", "engcpe_rl", "engcpe_ex", "engvdw"))
+    assert tot_d == pytest.approx(tot_r, rel=1e-6)
+
+
+def test_mixed_is_deterministic(gpu_lib):
+    """Fixed-point force sums: two runs give bit-identical forces and trajectories."""
+    out = []
+    for _ in range(2):
+        gpu_lib.init(systems.nacl_melt(16), precision=1)
+        gpu_lib.start()
+        gpu_lib.md_vv(10)
+        out.append(gpu_lib.download())
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_list_overflow_status(gpu_lib):
+    s = systems.nacl_melt(16)
+    gpu_lib.init(s, max_list=50)
+    gpu_lib.relocate()
+    st, need = gpu_lib.list_build_status()
+    assert st == 106 and need > 50
+    # the context stays usable: a later call with a fresh init works
+    gpu_lib.init(s)
+    gpu_lib.relocate()
+    assert gpu_lib.list_build_status()[0] == 0
+
+
+def test_nonfinite_positions_rejected(gpu_lib):
+    s = systems.nacl_melt(16)
+    gpu_lib.init(s)
+    x = s.x.copy()
+    x[7] = np.nan
+    with pytest.raises(Exception) as e:
+        gpu_lib.upload(x, s.y, s.z)
+    assert getattr(e.value, "code", None) == -5
+
+
+def test_cutoff_larger_than_half_cell_rejected(gpu_lib):
+    s = systems.nacl_melt(16)
+    s.rcut = 22.0
+    with pytest.raises(Exception) as e:
+        gpu_lib.init(s)
+    assert getattr(e.value, "code", None) == 95
