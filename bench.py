@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 DL_POLY per-timestep force and update path.
+
+Metric: atom-steps/s (and ns/day at dt = 2 fs) of the NVE velocity-Verlet MD
+step: VV stage 1, conditional Verlet-list rebuild (link cells + halo images),
+SPME reciprocal forces (order-8 B-splines, 3-D FFT + influence function),
+real-space vdW + erfc-Coulomb pair forces, VV stage 2.
+
+Default workload (one GPU): the 262,144-ion NaCl-like melt (64^3 rock-salt
+sites, 180.48 A box, SPME grid 192^3, order 8, rc 12 A, skin 1 A), plain FP64,
+seeded synthetic start at 1500 K.  `--form mixed` runs the FP32/fixed-point
+form of the same workload.  The working set (Verlet list ~0.8 GB, grids
+~0.5 GB) exceeds the 129 MB L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference] [--form fp64|mixed]
+
+N > 1 (torchrun, one rank per GPU) runs N independent replicas: the path does
+not shard (one GPU per DL_POLY rank); value = total atom-steps / max rank time.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "dl-poly_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+from dlpoly_gb300 import systems  # noqa: E402
+
+DT_PS = 0.002
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def workload(name):
+    if name == "nacl_262144":
+        return systems.nacl_melt(64), "NaCl melt 262,144 ions, box 180.48 A, SPME 192^3 p=8, rc 12 A, skin 1 A"
+    if name == "nacl_4096":
+        return systems.nacl_melt(16), "NaCl melt 4,096 ions, box 45.12 A, SPME 48^3 p=8, rc 12 A, skin 1 A"
+    if name == "water_98304":
+        return (systems.spce_water(32),
+                "SPC/E-style water 32,768 molecules (98,304 atoms), box 99.3 A, SPME 100^3 p=8, rc 10 A, SHAKE/RATTLE")
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ------------------------------------------------------------------ dist
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------ clock samples
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for k, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(k)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- roofline
+def kernel_work(name, s, cnt, form):
+    """Algorithmic (flops, bytes) of one launch of a kernel (fixed counting convention)."""
+    N = s.natms
+    K = s.kmax
+    K3 = K[0] * K[1] * K[2]
+    p = s.nsplines
+    esz = 8 if form == "fp64" else 4
+    P_list, P_rc = cnt
+    if name == "pair_forces":
+        return 10.0 * P_list + 55.0 * P_rc, N * (24 + 8 + 4 + 24) + 4.0 * P_list
+    if name == "fft_x_fwd" or name == "fft_x_inv":
+        return 5.0 * K3 * math.log2(K[0]), K3 * (esz + 2 * esz)
+    if name == "fft_y":
+        return 5.0 * K3 * math.log2(K[1]), K3 * 2 * (2 * esz)
+    if name == "fft_z_conv":
+        return 10.0 * K3 * math.log2(K[2]) + 6.0 * K3, K3 * (2 * 2 * 2 * esz + 2 * esz)
+    if name == "spme_spread":
+        return 2.0 * p ** 3 * N, N * (16 + 3 * p * esz) + K3 * esz
+    if name == "spme_gather":
+        return 8.0 * p ** 3 * N, K3 * esz + N * (32 + 24)
+    if name == "spme_prep":
+        return 3.0 * N * (p * p + 3 * p), N * (32 + 3 * p * esz + 16)
+    if name == "list_pairs":
+        return 10.0 * P_list, 4.0 * P_list + N * 48
+    return None
+
+
+def read_peaks():
+    try:
+        return json.load(open(PEAKS_FILE))
+    except (OSError, ValueError):
+        return {}
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_sample(s, steps_max, budget_s):
+    """Time the FP64 oracle (OpenMP, all host cores) on the same workload."""
+    import oracle
+
+    o = oracle.load(openmp=True)
+    cores = os.cpu_count() or 1
+    o.lib.orc_set_threads(cores)
+    o.init(s)
+    o.start()
+    t0 = time.perf_counter()
+    o.md_vv(1)
+    t1 = time.perf_counter()
+    per = t1 - t0
+    n = max(1, min(steps_max, int(budget_s / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    o.md_vv(n)
+    dt = time.perf_counter() - t0
+    o.finalize()
+    return s.natms * n / dt, cores, n, dt
+
+
+def run_reference(args, dist):
+    s, desc = workload(args.workload)
+    if dist.rank != 0:
+        return
+    steps_cap = max(1, args.steps)
+    val, cores, n, dt = cpu_sample(s, steps_cap, budget_s=float(os.environ.get("GB_REF_BUDGET_S", "90")))
+    line = {
+        "impl": "reference",
+        "metric": "atom-steps/s",
+        "value": val,
+        "unit": "atom-steps/s",
+        "n_gpus": args.gpus,
+        "steps": n,
+        "warmup": 1,
+        "ms_per_step": 1e3 * dt / n,
+        "ns_per_day": (n / dt) * DT_PS * 86400 / 1000,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": desc, "form": "fp64", "natms": s.natms},
+        "cpu_baseline": {"value": val, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{n} full MD steps of the same workload after one untimed step "
+                                   "(C++ FP64 restatement with OpenMP; the Fortran reference has no compiler here)"},
+        "e2e": {"value": val, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU arm
+def run_gb(args, dist):
+    import dlpoly_gb300 as gb
+
+    s, desc = workload(args.workload)
+    precision = 0 if args.form == "fp64" else 1
+    lib = gb.load()
+    L = lib.lib
+    L.gb_profile.argtypes = [ctypes.c_int]
+    L.gb_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
+                                  ctypes.c_int]
+    L.gb_pair_counts.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]
+    L.gb_fp64_peak_tflops.restype = ctypes.c_double
+    device = dist.local
+    lib.init(s, precision=precision, device=device)
+    lib.start()
+    lib.md_vv(max(3, args.warmup))
+    # ---- timed region: K resident MD steps (kernels timed with CUDA events)
+    L.gb_profile(1)
+    clocks = Clocks(device)
+    dist.barrier()
+    l0 = L.gb_kernel_launches()
+    w0 = time.perf_counter()
+    stats = lib.md_vv(args.steps)
+    w1 = time.perf_counter()
+    l1 = L.gb_kernel_launches()
+    tm = (ctypes.c_double * 8)()
+    L.gb_last_timings(tm, 8)
+    span_s = tm[5] * 1e-3
+    dist.barrier()
+    clk = clocks.stop()
+    names = ctypes.create_string_buffer(32 * 32)
+    ms = (ctypes.c_double * 32)()
+    nl = (ctypes.c_int64 * 32)()
+    nk = L.gb_profile_read(names, ms, nl, 32)
+    L.gb_profile(0)
+    prof = {}
+    for k in range(nk):
+        nm = names.raw[32 * k:32 * (k + 1)].split(b"\0")[0].decode()
+        if nl[k]:
+            prof[nm] = (ms[k], int(nl[k]))
+    cnt = (ctypes.c_int64 * 3)()
+    L.gb_pair_counts(cnt, 3)
+    P_list, P_rc = int(cnt[0]), int(cnt[1])
+    if precision == 1:
+        P_list //= 2
+        P_rc //= 2
+    tmax = dist.max(span_s)
+    value = dist.world * s.natms * args.steps / tmax
+    rebuilds = sum(x.list_rebuilt for x in stats)
+    # ---- end to end through the C-ABI with host buffers (H2D state, D2H state + forces)
+    ke = max(1, min(args.steps, 10))
+    try:
+        import torch
+
+        def pinned(a):
+            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            return t.numpy()
+    except Exception:  # noqa: BLE001
+        def pinned(a):
+            return np.ascontiguousarray(a)
+    d = lib.download()
+    host = {k: pinned(v) for k, v in d.items()}
+    dist.barrier()
+    e0 = time.perf_counter()
+    for _ in range(ke):
+        lib.upload(host["x"], host["y"], host["z"], host["vx"], host["vy"], host["vz"])
+        lib.md_vv(1)
+        out = lib.download()
+        for k in host:
+            host[k][:] = out[k]
+    e1 = time.perf_counter()
+    emax = dist.max(e1 - e0)
+    e2e = {"value": dist.world * s.natms * ke / emax, "unit": "atom-steps/s",
+           "h2d_bytes_per_step": 6 * 8 * s.natms, "d2h_bytes_per_step": 9 * 8 * s.natms,
+           "steps": ke, "path": "gb_upload_state + gb_md_run(1) + gb_download_state per step"}
+    # ---- roofline of the dominant kernel
+    peaks = read_peaks()
+    hbm = peaks.get("hbm_gbs")
+    fp64_peak = L.gb_fp64_peak_tflops()
+    dom = max(prof.items(), key=lambda kv: kv[1][0])[0] if prof else None
+    roof = None
+    kernels = {}
+    for nm, (t_ms, n_l) in prof.items():
+        w = kernel_work(nm, s, (P_list, P_rc), args.form)
+        entry = {"ms_total": t_ms, "launches": n_l, "ms_per_launch": t_ms / n_l,
+                 "share": t_ms / max(1e-9, sum(v[0] for v in prof.values()))}
+        if w:
+            fl, by = w
+            sec = t_ms / n_l * 1e-3
+            entry["tflops"] = fl / sec / 1e12
+            entry["gbs"] = by / sec / 1e9
+        kernels[nm] = entry
+    if dom and kernel_work(dom, s, (P_list, P_rc), args.form):
+        fl, by = kernel_work(dom, s, (P_list, P_rc), args.form)
+        sec = prof[dom][0] / prof[dom][1] * 1e-3
+        if args.form == "fp64" and fp64_peak and fp64_peak > 0 and fl / by > fp64_peak * 1e3 / (hbm or 6751.1):
+            roof = {"bound": "fp64", "kernel": dom, "achieved": fl / sec / 1e12, "peak": fp64_peak,
+                    "unit": "TFLOP/s", "frac": fl / sec / 1e12 / fp64_peak, "traffic": None,
+                    "peak_source": "FP64 DFMA loop measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+                    "hbm_view": {"achieved": by / sec / 1e9, "peak": hbm, "unit": "GB/s",
+                                 "frac": (by / sec / 1e9) / hbm if hbm else None}}
+        else:
+            roof = {"bound": "hbm", "kernel": dom, "achieved": by / sec / 1e9, "peak": hbm or 6800.0, "unit": "GB/s",
+                    "frac": (by / sec / 1e9) / (hbm or 6800.0), "traffic": None,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else "fallback 6.8 TB/s"}
+        roof["algorithmic"] = {"flops_per_launch": fl, "bytes_per_launch": by, "launch_ms": sec * 1e3}
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        try:
+            v, cores, n, dt = cpu_sample(s, 2, budget_s=30.0)
+            cpu = {"value": v, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                   "sample": f"{n} full MD steps of the same workload, C++ FP64 oracle with OpenMP on {cores} host threads"}
+        except Exception as e:  # noqa: BLE001
+            cpu = {"value": None, "error": str(e)}
+    lib.finalize()
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": "atom-steps/s",
+        "value": value,
+        "unit": "atom-steps/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": max(3, args.warmup),
+        "ms_per_step": tmax * 1e3 / args.steps,
+        "ns_per_day": (args.steps / tmax) * DT_PS * 86400 / 1000,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if precision == 0 else "f32+i64",
+        "data": "synthetic (seeded lattice + Maxwell-Boltzmann start)",
+        "config": {"workload": desc, "form": args.form, "natms": s.natms, "dt_fs": 2.0,
+                   "list_rebuilds_in_timed_steps": rebuilds, "parallelism": "replicas" if dist.world > 1 else "single",
+                   "l2": "working set > 129 MB L2 (list ~%.0f MB), no flush" % (4.0 * P_list / 1e6)},
+        "e2e": e2e,
+        "gpu_launches": int(l1 - l0),
+        "clocks": clk,
+        "roofline": roof,
+        "kernels": kernels,
+        "pairs": {"list_entries": P_list, "within_rc": P_rc},
+        "wall_s_timed": w1 - w0,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="nacl_262144", choices=["nacl_262144", "nacl_4096", "water_98304"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_gb(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

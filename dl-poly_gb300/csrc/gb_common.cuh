@@ -36,6 +36,8 @@ struct DevScalars {
   int ncand_fp64;   // list-build candidates resolved in FP64
   int pad[7];
   double maxdisp;   // largest displacement since the last rebuild
+  unsigned long long npairs_list;  // half-list entries walked by the pair kernel
+  unsigned long long npairs_rc;    // unique pairs inside the cutoff
   double acc[64];   // energy / virial / stress accumulators
 };
 
@@ -49,6 +51,14 @@ enum {
   A_STRCON = 50,      // 6 slots
   A_NSLOTS = 64
 };
+
+// Kernel regions timed with CUDA events when profiling is on.
+enum ProfId {
+  P_HALO = 0, P_BIN, P_LIST, P_FULLLIST, P_PAIR, P_EXCL, P_SPME_PREP, P_SPME_SPREAD, P_FFT_XF, P_FFT_Y,
+  P_FFT_Z, P_FFT_XI, P_SPME_GATHER, P_VV, P_SHAKE, P_RATTLE, P_MLP, P_NPROF
+};
+void prof_begin(int id);
+void prof_end(int id);
 
 // All device pointers of the context.  Arrays of size mxatms hold local atoms
 // in [0, natms) followed by halo images in [natms, nlast).
@@ -156,6 +166,15 @@ struct Dev {
   // timing
   cudaEvent_t ev[8];
   double last_ms[8];
+
+  // profiling
+  bool prof_on = false;
+  double prof_ms[P_NPROF];
+  long long prof_n[P_NPROF];
+  std::vector<cudaEvent_t> evpool;
+  std::vector<int> pend;  // triples (id, ev_begin, ev_end)
+  int ev_used = 0;
+  int open_ev[P_NPROF];
 
   // learned MTS
   int mts_k = 1;

@@ -351,8 +351,10 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
     GB_LAUNCHED();
   }
   if (stage == 1) {
+    prof_begin(P_VV);
     k_vv1<<<nblocks(n, 256), 256, 0, st>>>(n, hstep, tstep, g.weight, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz, g.x, g.y, g.z);
     GB_LAUNCHED();
+    prof_end(P_VV);
     if (g.ntcons > 0) {
       k_copy3<<<nblocks(n, 256), 256, 0, st>>>(n, g.x, g.y, g.z, g.ox, g.oy, g.oz);
       GB_LAUNCHED();
@@ -361,8 +363,10 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
       con_args(A);
       A.blk = gb_blkacc(coop_blocks_shake * 6);
       void* args[] = {&A};
+      prof_begin(P_SHAKE);
       GB_CUDA(cudaLaunchCooperativeKernel((void*)k_shake, coop_blocks_shake, 256, args, 0, st));
       GB_LAUNCHED();
+      prof_end(P_SHAKE);
       gb_reduce_blocks(A.blk, coop_blocks_shake, 6, &g.sc->acc[A_STRCON]);
       k_shake_post<<<nblocks(n, 256), 256, 0, st>>>(n, g.acon_start, g.lfrzn, rstep, hstep, g.weight, g.x, g.y, g.z,
                                                      g.ox, g.oy, g.oz, g.vx, g.vy, g.vz, g.fx, g.fy, g.fz);
@@ -376,15 +380,19 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
       if (g.hsc->status & ST_SHAKE_FAIL) throw (int)GB_ERR_SHAKE;
     }
   } else {
+    prof_begin(P_VV);
     k_vv2<<<nblocks(n, 256), 256, 0, st>>>(n, hstep, g.weight, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz);
     GB_LAUNCHED();
+    prof_end(P_VV);
     if (g.ntcons > 0) {
       GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + 2), st));
       ConArgs A;
       con_args(A);
       void* args[] = {&A};
+      prof_begin(P_RATTLE);
       GB_CUDA(cudaLaunchCooperativeKernel((void*)k_rattle, coop_blocks_rattle, 256, args, 0, st));
       GB_LAUNCHED();
+      prof_end(P_RATTLE);
     }
     const int nb = nblocks(n, 256);
     double* blk = gb_blkacc(nb * 6);

@@ -610,6 +610,7 @@ int list_relocate_and_halo() {
   const int n = g.natms;
   const int T = 256;
   cudaStream_t st = g.stream;
+  prof_begin(P_HALO);
   // relocate_particles in serial: pbcshift (deport_data.F90:3190)
   {
     double a0 = 1.0 / g.cell[0], a4 = 1.0 / g.cell[4], a8 = 1.0 / g.cell[8];
@@ -645,6 +646,7 @@ int list_relocate_and_halo() {
   // vnl_set_check (neighbours.F90:305-343): local positions are the checkpoint
   k_set_check<<<nblocks(n, T), T, 0, st>>>(n, g.x, g.y, g.z, g.xbg, g.ybg, g.zbg);
   GB_LAUNCHED();
+  prof_end(P_HALO);
   gb_sync_scalars();
   if (g.hsc->status & ST_HALO_OVERFLOW) return GB_ERR_HALO;
   return GB_OK;
@@ -668,6 +670,7 @@ int list_build() {
   const int mx = g.mxatms;
   GB_CUDA(cudaMemsetAsync(g.cell_count, 0, sizeof(int) * (g.ncells + 2), st));
   GB_CUDA(cudaMemsetAsync(g.cell_fill, 0, sizeof(int) * (g.ncells + 2), st));
+  prof_begin(P_BIN);
   k_bin<<<nblocks(mx, T), T, 0, st>>>(g.natms, g.sc, g.x, g.y, g.z, h_cg, g.which_cell, g.cell_count);
   GB_LAUNCHED();
   k_scan_single<<<1, 1024, 0, st>>>(g.cell_count, g.cell_start, g.ncells + 2, nullptr);
@@ -678,19 +681,26 @@ int list_build() {
   k_cell_sort<<<nblocks((long long)(g.ncells + 1) * 32, T), T, 0, st>>>(g.ncells + 1, g.cell_start, tmp, g.at_list,
                                                                        g.sorted_pos, g.x, g.y, g.z, g.xs, g.xsf);
   GB_LAUNCHED();
+  prof_end(P_BIN);
   GB_CUDA(cudaMemsetAsync(&g.sc->ibig, 0, sizeof(int), st));
+  prof_begin(P_LIST);
   k_list_pairs<<<nblocks((long long)mx * 32, T), T, 0, st>>>(g.natms, g.sc, h_cg, g.nsbcll, g.at_list, g.which_cell,
                                                              g.cell_start, g.xs, g.xsf, g.list, g.ld, g.p.max_list,
                                                              g.sc);
   GB_LAUNCHED();
-  gb_sync_scalars();
-  if (g.hsc->status & ST_LIST_OVERFLOW) return GB_ERR_LIST_OVERFLOW;
   if (g.lbook || g.megfrz > 1) {
     k_list_reorder<<<nblocks(g.natms, 128), 128, 0, st>>>(g.natms, g.list, g.ld, g.lfrzn, g.ltg, g.list_excl,
                                                           g.p.max_exclude + 1, g.megfrz, g.lbook ? 1 : 0);
     GB_LAUNCHED();
   }
-  if (g.precision == GB_MIXED) list_full_build();
+  prof_end(P_LIST);
+  gb_sync_scalars();
+  if (g.hsc->status & ST_LIST_OVERFLOW) return GB_ERR_LIST_OVERFLOW;
+  if (g.precision == GB_MIXED) {
+    prof_begin(P_FULLLIST);
+    list_full_build();
+    prof_end(P_FULLLIST);
+  }
   return GB_OK;
 }
 

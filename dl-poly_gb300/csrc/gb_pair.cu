@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(256) k_pair_fp64(int natms, const DevScalars* 
                                                    const int* __restrict__ src, const double* __restrict__ ecoef,
                                                    const double* __restrict__ vcoef, const int* __restrict__ vkind,
                                                    const double* __restrict__ veps, const double* __restrict__ vsig,
-                                                   PairGeom pg, double* fx, double* fy, double* fz, double* blk) {
+                                                   PairGeom pg, double* fx, double* fy, double* fz, double* blk,
+                                                   unsigned long long* cnt) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   double acc[NACC];
@@ -83,6 +84,7 @@ __global__ void __launch_bounds__(256) k_pair_fp64(int natms, const DevScalars* 
     const int n = li[0];
     double fix = 0.0, fiy = 0.0, fiz = 0.0;
     const int vstride = (pg.max_grid + 3) * 6;
+    int nrc = 0;
     for (int m = lane + 1; m <= n; m += 32) {
       int j = li[m] - 1;
       int jf = j;  // atom receiving the reaction force
@@ -152,6 +154,7 @@ __global__ void __launch_bounds__(256) k_pair_fp64(int natms, const DevScalars* 
         }
       }
       if (gam == 0.0 && ee == 0.0 && ev == 0.0) continue;
+      ++nrc;
       const double fx_ = gam * dx, fy_ = gam * dy, fz_ = gam * dz;
       fix += fx_; fiy += fy_; fiz += fz_;
       atomicAdd(&fx[jf], -fx_);
@@ -165,19 +168,26 @@ __global__ void __launch_bounds__(256) k_pair_fp64(int natms, const DevScalars* 
       acc[7] += dy * fy_; acc[8] += dy * fz_; acc[9] += dz * fz_;
     }
     fix = warp_sum(fix); fiy = warp_sum(fiy); fiz = warp_sum(fiz);
+    nrc = warp_sumi(nrc);
     if (lane == 0) {
       atomicAdd(&fx[i], fix);
       atomicAdd(&fy[i], fiy);
       atomicAdd(&fz[i], fiz);
+      atomicAdd(&cnt[0], (unsigned long long)n);
+      atomicAdd(&cnt[1], (unsigned long long)nrc);
     }
   }
   block_reduce_store<NACC>(acc, blk);
 }
 
 // exclusion correction (FP64), one thread per atom over its excluded section
+// In the mixed form the same FP64 kernel writes fixed-point forces (fixp != 0):
+// the intramolecular exclusion terms cancel against the reciprocal energy
+// (tens of millions of internal units for water), so they stay in FP64.
 __global__ void k_excl_fp64(int natms, const int* list, int ld, const double* x, const double* y, const double* z,
                             const double* q, const int* ltg, const int* src, double alpha, double scaling,
-                            double rcut, double* fx, double* fy, double* fz, double* blk) {
+                            double rcut, double* fx, double* fy, double* fz, double* blk,
+                            unsigned long long* fixp) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (i < natms) {
@@ -211,7 +221,14 @@ __global__ void k_excl_fp64(int natms, const int* list, int ld, const double* x,
           double fx_ = egamma * xx, fy_ = egamma * yy, fz_ = egamma * zz;
           fix += fx_; fiy += fy_; fiz += fz_;
           if (j < natms) {
-            atomicAdd(&fx[j], -fx_); atomicAdd(&fy[j], -fy_); atomicAdd(&fz[j], -fz_);
+            if (fixp) {
+              const double sc = 1099511627776.0;
+              atomicAdd(&fixp[3 * j + 0], (unsigned long long)(-__double2ll_rn(fx_ * sc)));
+              atomicAdd(&fixp[3 * j + 1], (unsigned long long)(-__double2ll_rn(fy_ * sc)));
+              atomicAdd(&fixp[3 * j + 2], (unsigned long long)(-__double2ll_rn(fz_ * sc)));
+            } else {
+              atomicAdd(&fx[j], -fx_); atomicAdd(&fy[j], -fy_); atomicAdd(&fz[j], -fz_);
+            }
           }
           if (j < natms || ltg[i] < ltg[j]) {
             acc[0] -= erfr;
@@ -221,7 +238,14 @@ __global__ void k_excl_fp64(int natms, const int* list, int ld, const double* x,
           }
         }
       }
-      atomicAdd(&fx[i], fix); atomicAdd(&fy[i], fiy); atomicAdd(&fz[i], fiz);
+      if (fixp) {
+        const double sc = 1099511627776.0;
+        atomicAdd(&fixp[3 * i + 0], (unsigned long long)__double2ll_rn(fix * sc));
+        atomicAdd(&fixp[3 * i + 1], (unsigned long long)__double2ll_rn(fiy * sc));
+        atomicAdd(&fixp[3 * i + 2], (unsigned long long)__double2ll_rn(fiz * sc));
+      } else {
+        atomicAdd(&fx[i], fix); atomicAdd(&fy[i], fiy); atomicAdd(&fz[i], fiz);
+      }
     }
   }
   block_reduce_store<8>(acc, blk);
@@ -237,7 +261,8 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
                                                     const float* __restrict__ ecoef, const float* __restrict__ vcoef,
                                                     const int* __restrict__ vkind, float rc2, float rv2, float erdr,
                                                     float vrdr, float scaling, int max_grid,
-                                                    unsigned long long* fixp, double* blk) {
+                                                    unsigned long long* fixp, double* blk,
+                                                    unsigned long long* cnt) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   double acc[NACC];
@@ -252,6 +277,7 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
     long long sx = 0, sy = 0, sz = 0;
     float a0 = 0, a1 = 0, a2 = 0, a3 = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
     const int vstride = (max_grid + 3) * 6;
+    int nrc = 0;
     for (int m = lane; m < n; m += 32) {
       const int j = flist[s + m];
       const float4 pj = xf[j];
@@ -287,6 +313,7 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
           a1 -= gv * rsq;
         }
       }
+      ++nrc;
       const float fx_ = gam * dx, fy_ = gam * dy, fz_ = gam * dz;
       sx += __float2ll_rn(fx_ * FIX_SCALE_F);
       sy += __float2ll_rn(fy_ * FIX_SCALE_F);
@@ -299,66 +326,18 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
       sy += __shfl_xor_sync(0xffffffffu, sy, o);
       sz += __shfl_xor_sync(0xffffffffu, sz, o);
     }
+    nrc = warp_sumi(nrc);
     if (lane == 0) {
       atomicAdd(&fixp[3 * i + 0], (unsigned long long)sx);
       atomicAdd(&fixp[3 * i + 1], (unsigned long long)sy);
       atomicAdd(&fixp[3 * i + 2], (unsigned long long)sz);
+      atomicAdd(&cnt[0], (unsigned long long)n);
+      atomicAdd(&cnt[1], (unsigned long long)nrc);
     }
     acc[0] = 0.5 * a0; acc[1] = 0.5 * a1; acc[2] = 0.5 * a2; acc[3] = 0.5 * a3;
     acc[4] = 0.5 * s0; acc[5] = 0.5 * s1; acc[6] = 0.5 * s2; acc[7] = 0.5 * s3; acc[8] = 0.5 * s4; acc[9] = 0.5 * s5;
   }
   block_reduce_store<NACC>(acc, blk);
-}
-
-// exclusion correction (mixed): FP32 arithmetic, fixed-point forces
-__global__ void k_excl_mixed(int natms, const int* list, int ld, const float4* xf, const int* ltg, float alpha,
-                             float scaling, float rcut, unsigned long long* fixp, double* blk) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (i < natms) {
-    const int* li = list + (size_t)i * ld + 3;
-    int lim = li[-1] - li[0];
-    float4 pi = xf[i];
-    if (lim > 0 && pi.w != 0.f) {
-      const float chgea = pi.w * scaling;
-      const float a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f, a4 = -1.453152027f,
-                  a5 = 1.061405429f, pp = 0.3275911f, sqrpi = 1.7724538509f;
-      long long sx = 0, sy = 0, sz = 0;
-      for (int m = 1; m <= lim; ++m) {
-        int j = li[li[0] + m] - 1;
-        float4 pj = xf[j];
-        float xx = pi.x - pj.x, yy = pi.y - pj.y, zz = pi.z - pj.z;
-        float rsq = xx * xx + yy * yy + zz * zz;
-        float rrr = sqrtf(rsq);
-        if (pj.w != 0.f && rrr < rcut) {
-          float chgprd = pj.w * chgea;
-          float exp1 = __expf(-(alpha * rrr) * (alpha * rrr));
-          float tt = 1.0f / (1.0f + pp * alpha * rrr);
-          float erfr = chgprd * (1.0f - tt * (a1 + tt * (a2 + tt * (a3 + tt * (a4 + tt * a5)))) * exp1) / rrr;
-          float egamma = -(erfr - 2.0f * chgprd * (alpha / sqrpi) * exp1) / rsq;
-          float fx_ = egamma * xx, fy_ = egamma * yy, fz_ = egamma * zz;
-          long long ix = __float2ll_rn(fx_ * FIX_SCALE_F), iy = __float2ll_rn(fy_ * FIX_SCALE_F),
-                    iz = __float2ll_rn(fz_ * FIX_SCALE_F);
-          sx += ix; sy += iy; sz += iz;
-          if (j < natms) {
-            atomicAdd(&fixp[3 * j + 0], (unsigned long long)(-ix));
-            atomicAdd(&fixp[3 * j + 1], (unsigned long long)(-iy));
-            atomicAdd(&fixp[3 * j + 2], (unsigned long long)(-iz));
-          }
-          if (j < natms || ltg[i] < ltg[j]) {
-            acc[0] -= erfr;
-            acc[1] -= egamma * rsq;
-            acc[2] += xx * fx_; acc[3] += xx * fy_; acc[4] += xx * fz_;
-            acc[5] += yy * fy_; acc[6] += yy * fz_; acc[7] += zz * fz_;
-          }
-        }
-      }
-      atomicAdd(&fixp[3 * i + 0], (unsigned long long)sx);
-      atomicAdd(&fixp[3 * i + 1], (unsigned long long)sy);
-      atomicAdd(&fixp[3 * i + 2], (unsigned long long)sz);
-    }
-  }
-  block_reduce_store<8>(acc, blk);
 }
 
 inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
@@ -389,36 +368,45 @@ void pair_forces(double* eng6, double* stress9) {
   const int T = 256;
   double res[NACC];
   double ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int nb2 = nblocks(g.natms, 128);
+  GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
   if (g.precision == GB_FP64) {
     int nb = nblocks((long long)g.mxatms * 32, T);
-    double* blk = gb_blkacc(nb * NACC);
+    double* blk = gb_blkacc(nb * NACC + nb2 * 8);
+    prof_begin(P_PAIR);
     k_pair_fp64<<<nb, T, 0, st>>>(g.natms, g.sc, g.at_list, g.list, g.ld, g.x, g.y, g.z, g.chge, g.ltype, g.ltg,
                                   g.src, g.erfc_coef, g.vdw_coef, g.vdw_kind, g.vdw_eps, g.vdw_sig, pg, g.fx, g.fy,
-                                  g.fz, blk);
+                                  g.fz, blk, &g.sc->npairs_list);
     GB_LAUNCHED();
+    prof_end(P_PAIR);
     gb_reduce_blocks(blk, nb, NACC, &g.sc->acc[A_PAIR]);
     if (g.lbook) {
-      int nb2 = nblocks(g.natms, 128);
-      double* blk2 = gb_blkacc(nb * NACC + nb2 * 8) + (size_t)nb * NACC;
+      double* blk2 = blk + (size_t)nb * NACC;
+      prof_begin(P_EXCL);
       k_excl_fp64<<<nb2, 128, 0, st>>>(g.natms, g.list, g.ld, g.x, g.y, g.z, g.chge, g.ltg, g.src, g.p.alpha,
-                                       g.scaling, g.p.rcut, g.fx, g.fy, g.fz, blk2);
+                                       g.scaling, g.p.rcut, g.fx, g.fy, g.fz, blk2, nullptr);
       GB_LAUNCHED();
+      prof_end(P_EXCL);
       gb_reduce_blocks(blk2, nb2, 8, &g.sc->acc[A_EXCL]);
     }
   } else {
     int nb = nblocks((long long)g.natms * 32, T);
-    double* blk = gb_blkacc(nb * NACC);
+    double* blk = gb_blkacc(nb * NACC + nb2 * 8);
+    prof_begin(P_PAIR);
     k_pair_mixed<<<nb, T, 0, st>>>(g.natms, g.fstart, g.fcount, g.flist, g.xf, g.ltype, g.erfc_coef_f, g.vdw_coef_f,
                                    g.vdw_kind, (float)pg.rc2, (float)pg.rv2, (float)pg.erdr, (float)pg.vrdr,
-                                   (float)pg.scaling, g.max_grid, (unsigned long long*)g.fixp, blk);
+                                   (float)pg.scaling, g.max_grid, (unsigned long long*)g.fixp, blk,
+                                   &g.sc->npairs_list);
     GB_LAUNCHED();
+    prof_end(P_PAIR);
     gb_reduce_blocks(blk, nb, NACC, &g.sc->acc[A_PAIR]);
     if (g.lbook) {
-      int nb2 = nblocks(g.natms, 128);
-      double* blk2 = gb_blkacc(nb * NACC + nb2 * 8) + (size_t)nb * NACC;
-      k_excl_mixed<<<nb2, 128, 0, st>>>(g.natms, g.list, g.ld, g.xf, g.ltg, (float)g.p.alpha, (float)g.scaling,
-                                        (float)g.p.rcut, (unsigned long long*)g.fixp, blk2);
+      double* blk2 = blk + (size_t)nb * NACC;
+      prof_begin(P_EXCL);
+      k_excl_fp64<<<nb2, 128, 0, st>>>(g.natms, g.list, g.ld, g.x, g.y, g.z, g.chge, g.ltg, g.src, g.p.alpha,
+                                       g.scaling, g.p.rcut, g.fx, g.fy, g.fz, blk2, (unsigned long long*)g.fixp);
       GB_LAUNCHED();
+      prof_end(P_EXCL);
       gb_reduce_blocks(blk2, nb2, 8, &g.sc->acc[A_EXCL]);
     }
   }

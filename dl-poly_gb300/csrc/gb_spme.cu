@@ -672,6 +672,7 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
   // splines + brick binning
   GB_CUDA(cudaMemsetAsync(g.brick_count, 0, sizeof(int) * (g.nbricks + 2), st));
   GB_CUDA(cudaMemsetAsync(g.brick_fill, 0, sizeof(int) * (g.nbricks + 2), st));
+  prof_begin(P_SPME_PREP);
   k_spme_prep<T><<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, h_sg, spl, g.nidx, g.brick_of,
                                                    g.brick_count);
   GB_LAUNCHED();
@@ -682,27 +683,40 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
   GB_LAUNCHED();
   k_brick_sort<<<nblocks((long long)g.nbricks * 32, 256), 256, 0, st>>>(g.nbricks, g.brick_start, tmp, g.brick_atoms);
   GB_LAUNCHED();
+  prof_end(P_SPME_PREP);
   // spreading
   {
     int threads = ((g.B2 * g.B3 + 31) / 32) * 32;
+    prof_begin(P_SPME_SPREAD);
     k_spme_spread<T><<<g.nbricks, threads, 0, st>>>(h_sg, g.brick_start, g.brick_atoms, spl, g.nidx, g.chge, Q);
     GB_LAUNCHED();
+    prof_end(P_SPME_SPREAD);
   }
   // FFT + convolution
   const int lines = 8;
   const int rows = g.K2 * g.K3;
+  prof_begin(P_FFT_XF);
   k_fft_x_fwd<T, T2><<<nblocks(rows, lines), 256, fft_smem(g.K1, lines, sizeof(T2)), st>>>(Q, G, plan1, tw1, rows, lines);
   GB_LAUNCHED();
+  prof_end(P_FFT_XF);
+  prof_begin(P_FFT_Y);
   k_fft_y<T, T2><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2, +1);
   GB_LAUNCHED();
+  prof_end(P_FFT_Y);
   const int nbz = (g.K1 / TX) * g.K2;
   double* blkz = gb_blkacc(nbz * 6 + nblocks(n, 128) * 4);
+  prof_begin(P_FFT_Z);
   k_fft_z_conv<T, T2><<<nbz, 256, fft_smem(g.K3, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, g.K3, plan3, tw3, th, ps, h_sg, blkz);
   GB_LAUNCHED();
+  prof_end(P_FFT_Z);
+  prof_begin(P_FFT_Y);
   k_fft_y<T, T2><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2, -1);
   GB_LAUNCHED();
+  prof_end(P_FFT_Y);
+  prof_begin(P_FFT_XI);
   k_fft_x_inv<T, T2><<<nblocks(rows, lines), 256, fft_smem(g.K1, lines, sizeof(T2)), st>>>(G, Q, plan1, tw1, rows, lines);
   GB_LAUNCHED();
+  prof_end(P_FFT_XI);
   // gather
   double rc[9];
   for (int k = 0; k < 9; ++k) rc[k] = h_sg.rc[k];
@@ -710,8 +724,10 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
   for (int a = 0; a < 3; ++a) rk[a] = rc[a] * h_sg.Kr[0] + rc[a + 3] * h_sg.Kr[1] + rc[a + 6] * h_sg.Kr[2];
   const int nbg = nblocks(n, 128);
   double* blkg = blkz + (size_t)nbz * 6;
+  prof_begin(P_SPME_GATHER);
   k_spme_gather<T><<<nbg, 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, h_sg, Q, rk[0], rk[1], rk[2], g.fspme, blkg);
   GB_LAUNCHED();
+  prof_end(P_SPME_GATHER);
   gb_reduce_blocks(blkz, nbz, 6, &g.sc->acc[A_SPME_STR]);
   gb_reduce_blocks(blkg, nbg, 4, &g.sc->acc[A_GATHER]);
   const double pi = 3.14159265358979323846264338327950288;

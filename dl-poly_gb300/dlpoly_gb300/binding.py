@@ -86,8 +86,8 @@ class PathLib:
         return (f(st) or b"").decode()
 
     # ---------------------------------------------------------------- set-up
-    def init(self, s: System, precision: int = 0, max_list: int | None = None):
-        p = s.params(precision, max_list)
+    def init(self, s: System, precision: int = 0, max_list: int | None = None, device: int = 0):
+        p = s.params(precision, max_list, device)
         self.params = p
         self.sys = s
         excl = s.excl_array(p)

@@ -48,7 +48,8 @@ class GbParams(ctypes.Structure):
         ("mxatms", ctypes.c_int32),
         ("precision", ctypes.c_int32),
         ("ntypes", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("device", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
     ]
 
 
@@ -116,8 +117,9 @@ class System:
         c = self.cell.reshape(3, 3)
         return abs(float(np.linalg.det(c)))
 
-    def params(self, precision: int = 0, max_list: int | None = None) -> GbParams:
+    def params(self, precision: int = 0, max_list: int | None = None, device: int = 0) -> GbParams:
         p = GbParams()
+        p.device = device
         for k in range(9):
             p.cell[k] = float(self.cell[k])
         p.rcut = self.rcut

@@ -71,7 +71,8 @@ typedef struct gb_params {
   int32_t mxatms;       /* config%mxatms: capacity for local + halo atoms */
   int32_t precision;    /* GB_FP64 or GB_MIXED */
   int32_t ntypes;       /* sites%ntype_atom */
-  int32_t reserved[7];
+  int32_t device;       /* CUDA device ordinal this context uses (one GPU per process) */
+  int32_t reserved[6];
 } gb_params;
 
 /* Per-step scalars returned by the resident MD loop. */
@@ -189,6 +190,21 @@ int gb_last_timings(double* ms, int n);
 
 /* Number of kernels the library launched since gb_init (its own count). */
 int64_t gb_kernel_launches(void);
+
+/* Per-kernel CUDA-event timing on the library stream (the CHRONO timers of
+ * timer.F90:335-476 as device events).  gb_profile(1) starts collecting and
+ * clears the totals; gb_profile_read copies, for up to max entries, the
+ * kernel name (32 bytes each), total milliseconds and launch count. */
+int gb_profile(int enable);
+int gb_profile_read(char* names, double* ms, int64_t* launches, int max);
+
+/* Work counters of the last force evaluation: [0] half-list entries,
+ * [1] unique pairs inside rc, [2] list-build candidates tested in exact FP64. */
+int gb_pair_counts(int64_t* out, int n);
+
+/* FP64 FMA throughput of this device in TFLOP/s, measured by a register-
+ * resident DFMA loop (the FP64 roofline denominator; not used by the path). */
+double gb_fp64_peak_tflops(void);
 
 /* Release device memory; gb_init may be called again afterwards. */
 void gb_finalize(void);

@@ -126,9 +126,13 @@ def test_mixed_force_error(gpu_lib, oracle_lib, name):
     er, _ = oracle_lib.two_body_forces()
     a, b = gpu_lib.download(), oracle_lib.download()
     assert force_rms_rel(a, b) <= 1e-5
-    tot_d = sum(ed[k] for k in ("engcpe_rc", "engcpe_rl", "engcpe_ex", "engvdw"))
-    tot_r = sum(er[k] for k in ("engcpe_rc", "engcpe_rl", "engcpe_ex", "engvdw"))
-    assert tot_d == pytest.approx(tot_r, rel=1e-6)
+    keys = ("engcpe_rc", "engcpe_rl", "engcpe_ex", "engvdw")
+    tot_d = sum(ed[k] for k in keys)
+    tot_r = sum(er[k] for k in keys)
+    # FP32 pair/grid energies: error bounded by the magnitude of the terms,
+    # which cancel heavily for water (reciprocal vs exclusion correction)
+    assert abs(tot_d - tot_r) <= 2e-6 * sum(abs(er[k]) for k in keys)
+    assert ed["engcpe_ex"] == pytest.approx(er["engcpe_ex"], rel=1e-10)  # FP64 in both forms
 
 
 def test_mixed_is_deterministic(gpu_lib):
