@@ -761,6 +761,7 @@ const char* gb_strerror(int status) {
     case GB_ERR_ARG: return "invalid argument";
     case GB_ERR_NO_DEVICE: return "no CUDA device";
     case GB_ERR_NONFINITE: return "non-finite positions";
+    case GB_ERR_TOO_LARGE: return "size exceeds the fixed scratch limit of gb_kinstress_noalloc (1,048,576 atoms)";
     default: return "unknown status";
   }
 }

@@ -42,6 +42,7 @@ extern "C" {
 #define GB_ERR_ARG (-3)
 #define GB_ERR_NO_DEVICE (-4)
 #define GB_ERR_NONFINITE (-5)
+#define GB_ERR_TOO_LARGE (-6)  /* size beyond a fixed scratch limit (gb_kinstress_noalloc) */
 
 /* Precision forms of the force path. */
 #define GB_FP64 0   /* plain: FP64 throughout */
@@ -205,6 +206,27 @@ int gb_pair_counts(int64_t* out, int n);
 /* FP64 FMA throughput of this device in TFLOP/s, measured by a register-
  * resident DFMA loop (the FP64 roofline denominator; not used by the path). */
 double gb_fp64_peak_tflops(void);
+
+/*
+ * Kinetic stress of n atoms (the sum kinstress forms) for callers that cannot
+ * allocate device memory: a host program whose device memory belongs to a
+ * pool it does not control, or that must not allocate once a run is under
+ * way.  This entry point has no counterpart in the reference.
+ *   vx, vy, vz, weight, lfrzn (may be NULL: no frozen atoms) and strkin_out
+ *   (9 doubles, the symmetric 3x3 tensor) are DEVICE pointers; stream may be
+ *   NULL (the default stream).  The call only enqueues work: synchronise the
+ *   stream before reading strkin_out.  It needs no gb_init.
+ * It allocates nothing.  Its scratch is a fixed array of 4096 x 6 doubles
+ * (196,608 bytes) in the library's device memory, held on every GPU that loads
+ * the library until the process exits, so n is limited to 1,048,576 atoms;
+ * larger n returns GB_ERR_TOO_LARGE and launches nothing.  The first call on
+ * each device looks up the address of that array; make that first call before
+ * any stream capture.  All calls share the one array: calls that overlap on
+ * the GPU (concurrent streams, or another host thread) race and give wrong
+ * results, so serialise them.
+ */
+int gb_kinstress_noalloc(const double* vx, const double* vy, const double* vz, const double* weight,
+                         const int32_t* lfrzn, int n, double* strkin_out, void* stream);
 
 /* Release device memory; gb_init may be called again afterwards. */
 void gb_finalize(void);
