@@ -424,6 +424,7 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     g.nsamples = std::max(1004, (int)std::lround(prm->rcut / 0.01) + 4);   // bounds.F90:811
     g.max_grid = std::max(1004, (int)std::lround(prm->rvdw / 0.01) + 4);   // bounds.F90:820
     build_tables(vdw_prm);
+    pair_setup();
     g.scaling = kR4pie0 / prm->epsq;
     double sq2 = 0.0;
     for (int i = 0; i < natms; ++i) sq2 += chge[i] * chge[i];

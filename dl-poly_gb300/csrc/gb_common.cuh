@@ -224,6 +224,19 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 
+// x * 2^40 as int64, rounded toward zero, by integer operations only (on this
+// part a float -> int64 conversion runs on the slow FP64 unit).  |x| < 2^23,
+// the range of the 2^40 fixed-point format used for forces and grid charges.
+__device__ __forceinline__ long long fix40(float x) {
+  const unsigned u = __float_as_uint(x);
+  const int sh = (int)((u >> 23) & 0xFFu) - 127 + 17;  // x = m 2^(e-23), m 24-bit: x 2^40 = m 2^(e+17)
+  const long long m = (long long)((u & 0x7FFFFFu) | 0x800000u);
+  long long v = 0;
+  if (sh >= 0) v = m << min(sh, 39);
+  else if (sh > -24) v = m >> (-sh);
+  return (u >> 31) ? -v : v;
+}
+
 // Block-wide reduction of NV doubles into per-block slots out[blockIdx.x*NV + k].
 template <int NV>
 __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* out) {
@@ -262,6 +275,7 @@ void list_full_build();           // derived full list for the mixed path
 void list_pos_f32();              // FP32 copy of positions and charges (mixed path)
 void scan_exclusive(const int* in, int* out, int n);
 void pair_forces(double* eng6, double* stress9);  // gb_pair.cu (adds into forces)
+void pair_setup();                // gb_pair.cu: per-key constants
 void spme_setup();                // gb_spme.cu
 void spme_forces(double* eng_rc, double* vir_rc, double* stress9);  // adds into forces
 void integ_vv(int stage, double* strkin, double* engke, int* iters, double* vircon, double* strcon);

@@ -18,6 +18,7 @@
 // the pair forces as int64 fixed point (scale 2^40): order independent, no
 // atomics per pair, bit-reproducible.
 #include <cfloat>
+#include <cstring>
 
 #include "gb_common.cuh"
 
@@ -29,12 +30,38 @@ struct PairGeom {
   double rc2, rv2;           // cutoffs squared
   double rc2_lo, rc2_hi;     // band where sqrt(rsq) < rc is decided exactly
   double rv2_lo, rv2_hi;
+  long long b_rc2_lo, b_rc2_hi, b_rv2_lo, b_rv2_hi, b_hi;  // the same bounds as IEEE bit patterns
   double rcut, rvdw;
   double erdr, vrdr;         // reciprocal table spacings
   double scaling;            // r4pie0 / eps
   int vdw_direct;
+  int same_grid;             // erdr == vrdr: one table coordinate serves both tables
   int nsamples, max_grid, ntypes;
 };
+
+constexpr long long DBL_MIN_BITS = 0x0010000000000000ll;  // bits of DBL_MIN
+constexpr long long ONE_BITS = 0x3FF0000000000000ll;      // bits of 1.0
+
+// exact double of 0 <= k < 2^31 from its bits: (2^52 + k) - 2^52, one FP64 add
+__device__ __forceinline__ double int_to_dbl(int k) {
+  return __longlong_as_double(0x4330000000000000ll + (long long)k) - 4503599627370496.0;
+}
+
+// FP32 value of a positive normal double, mantissa truncated, by integer ops
+__device__ __forceinline__ float dbl_to_flt_trunc(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned e = ((hi >> 20) & 0x7FFu) - 1023u + 127u;
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | ((unsigned)b >> 29);
+  return __uint_as_float((e << 23) | m);
+}
+
+// exact FP64 value of a positive normal float, by integer ops
+__device__ __forceinline__ double flt_to_dbl(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long e = (unsigned long long)(((u >> 23) & 0xFFu) - 127u + 1023u);
+  return __longlong_as_double((long long)((e << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
 
 __device__ __forceinline__ int vkey(int ai, int aj) {
   return ai > aj ? ai * (ai - 1) / 2 + aj : aj * (aj - 1) / 2 + ai;
@@ -59,7 +86,7 @@ __device__ __forceinline__ void acc_store(double (&v)[NV], double* blk) {
 // accumulator layout per block: engvdw, virvdw, engrl, virrl, str(6)
 constexpr int NACC = 10;
 
-__global__ void __launch_bounds__(256) k_pair_fp64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
+__global__ void __launch_bounds__(256, 3) k_pair_fp64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
                                                    const int* __restrict__ list, int ld,
                                                    const double* __restrict__ x, const double* __restrict__ y,
                                                    const double* __restrict__ z, const double* __restrict__ q,
@@ -69,16 +96,18 @@ __global__ void __launch_bounds__(256) k_pair_fp64(int natms, const DevScalars* 
                                                    const double* __restrict__ veps, const double* __restrict__ vsig,
                                                    PairGeom pg, double* fx, double* fy, double* fz, double* blk,
                                                    unsigned long long* cnt) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   double acc[NACC];
 #pragma unroll
   for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
   const int nlast = sc->nlast;
-  int i = -1;
-  if (warp < nlast) i = at_list[warp];
-  if (i >= 0 && i < natms) {
+  // persistent warps walk the atoms in cell order (neighbouring atoms share j data in L1)
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nlast; w += nwarps) {
+    const int i = at_list[w];
+    if (i >= natms) continue;
     const double xi = x[i], yi = y[i], zi = z[i], qi = q[i] * pg.scaling;
+    const bool qi_on = (__double_as_longlong(qi) & 0x7FFFFFFFFFFFFFFFll) >= DBL_MIN_BITS;
     const int ai = ltype[i], gi = ltg[i];
     const int* li = list + (size_t)i * ld + 3;
     const int n = li[0];
@@ -92,23 +121,39 @@ __global__ void __launch_bounds__(256) k_pair_fp64(int natms, const DevScalars* 
         if (gi > ltg[j]) continue;  // evaluated from the other side
         jf = src[j];
       }
+      // On this part an FP64 compare or conversion costs a full FP64 issue
+      // slot, so range tests use the IEEE bit patterns (rsq >= 0 orders like
+      // its bits) and the rsqrt seed is built with integer operations.
       const double dx = xi - x[j], dy = yi - y[j], dz = zi - z[j];
       const double rsq = dx * dx + dy * dy + dz * dz;
-      if (rsq >= pg.rc2_hi && rsq >= pg.rv2) continue;
-      // 1/r: FP32 seed + one Newton step (relative error < 3e-14)
-      double rinv = (double)rsqrtf((float)rsq);
+      const long long rb = __double_as_longlong(rsq);
+      if (rb >= pg.b_hi) continue;
+      // 1/r: FP32 rsqrt of the truncated value, one FP64 Newton step (rel. error < 1e-13)
+      double rinv = flt_to_dbl(rsqrtf(dbl_to_flt_trunc(rsq)));
       rinv = rinv * fma(-0.5 * rsq * rinv, rinv, 1.5);
-      double rrr = rsq * rinv;
-      bool in_c = rsq < pg.rc2_lo || (rsq < pg.rc2_hi && sqrt(rsq) < pg.rcut);
-      double gam = 0.0, ee = 0.0, ev = 0.0, gvir_c = 0.0, gvir_v = 0.0;
+      const double rrr = rsq * rinv;
+      const bool in_c = rb < pg.b_rc2_lo || (rb < pg.b_rc2_hi && sqrt(rsq) < pg.rcut);
+      const bool in_v = rb < pg.b_rv2_lo || (rb < pg.b_rv2_hi && sqrt(rsq) < pg.rvdw);
       const double qj = q[j];
+      const bool do_c = in_c && qi_on && ((__double_as_longlong(qj) & 0x7FFFFFFFFFFFFFFFll) > DBL_MIN_BITS);
+      int key = -1;
+      if (in_v) {
+        key = vkey(ai, ltype[j]) - 1;
+        if (vkind[key] == 0) key = -1;
+      }
+      if (!do_c && key < 0) continue;
+      // shared table coordinate (the erfc and vdW grids coincide when rvdw == rcut);
+      // k = Int(ppp) without FP64 conversions: FP32 floor of the truncated value
+      // (never above ppp), exact double of k from its bits, one fix-up step
+      const double ppp = rrr * pg.erdr;
+      int k = (int)dbl_to_flt_trunc(ppp);
+      double d = ppp - int_to_dbl(k);
+      if (__double_as_longlong(d) >= ONE_BITS) { ++k; d -= 1.0; }
+      double gam = 0.0, ee = 0.0, ev = 0.0, gvir_c = 0.0, gvir_v = 0.0;
       // real-space Coulomb (ewald_spole.F90:131-176)
-      if (in_c && fabs(qj) > DBL_MIN && fabs(qi) >= DBL_MIN) {
-        double ppp = rrr * pg.erdr;
-        int k = (int)ppp;
-        double d = ppp - (double)k;
+      if (do_c) {
         const double* c = ecoef + (size_t)k * 6;
-        double pre = qi * qj;
+        const double pre = qi * qj;
         double eg, ec;
         if (k > 0) {
           eg = pre * fma(d, fma(d, c[5], c[4]), c[3]);
@@ -117,55 +162,53 @@ __global__ void __launch_bounds__(256) k_pair_fp64(int natms, const DevScalars* 
           eg = pre * three_p_exact(c + 3, d, rrr);
           ec = pre * three_p_exact(c, d, rrr);
         }
-        gam += eg;
+        gam = eg;
         ee = ec;
         gvir_c = eg;
       }
       // van der Waals (vdw.F90:1881-1962 tabulated / :1670-1700 direct)
-      if (rsq < pg.rv2) {
-        const int aj = ltype[j];
-        const int key = vkey(ai, aj) - 1;
-        if (vkind[key] != 0) {
-          if (rsq < pg.rv2_lo || (rsq < pg.rv2_hi && sqrt(rsq) < pg.rvdw)) {
-            double r_rsq = rinv * rinv;
-            double gv, e;
-            if (pg.vdw_direct) {
-              double sr = vsig[key] * rinv;
-              double s2 = sr * sr, s6 = s2 * s2 * s2;
-              e = 4.0 * veps[key] * s6 * (s6 - 1.0);
-              gv = 24.0 * veps[key] * s6 * (2.0 * s6 - 1.0) * r_rsq;
-            } else {
-              double ppp = rrr * pg.vrdr;
-              int k = (int)ppp;
-              double d = ppp - (double)k;
-              const double* c = vcoef + (size_t)key * vstride + (size_t)k * 6;
-              if (k > 0) {
-                gv = fma(d, fma(d, c[2], c[1]), c[0]) * r_rsq;
-                e = fma(d, fma(d, c[5], c[4]), c[3]);
-              } else {
-                gv = three_p_exact(c, d, rrr) * r_rsq;
-                e = three_p_exact(c + 3, d, rrr);
-              }
-            }
-            gam += gv;
-            ev = e;
-            gvir_v = gv;
+      if (key >= 0) {
+        const double r_rsq = rinv * rinv;
+        double gv, e;
+        if (pg.vdw_direct) {
+          const double sr = vsig[key] * rinv;
+          const double s2 = sr * sr, s6 = s2 * s2 * s2;
+          e = 4.0 * veps[key] * s6 * (s6 - 1.0);
+          gv = 24.0 * veps[key] * s6 * (2.0 * s6 - 1.0) * r_rsq;
+        } else {
+          int kv = k;
+          double dv = d;
+          if (!pg.same_grid) {
+            const double pv = rrr * pg.vrdr;
+            kv = (int)pv;
+            dv = pv - (double)kv;
+          }
+          const double* c = vcoef + (size_t)key * vstride + (size_t)kv * 6;
+          if (kv > 0) {
+            gv = fma(dv, fma(dv, c[2], c[1]), c[0]) * r_rsq;
+            e = fma(dv, fma(dv, c[5], c[4]), c[3]);
+          } else {
+            gv = three_p_exact(c, dv, rrr) * r_rsq;
+            e = three_p_exact(c + 3, dv, rrr);
           }
         }
+        gam += gv;
+        ev = e;
+        gvir_v = gv;
       }
-      if (gam == 0.0 && ee == 0.0 && ev == 0.0) continue;
       ++nrc;
-      const double fx_ = gam * dx, fy_ = gam * dy, fz_ = gam * dz;
-      fix += fx_; fiy += fy_; fiz += fz_;
-      atomicAdd(&fx[jf], -fx_);
-      atomicAdd(&fy[jf], -fy_);
-      atomicAdd(&fz[jf], -fz_);
+      // reaction force on j (negations fold into the operands: no extra FP64 op)
+      const double nfx = (-gam) * dx, nfy = (-gam) * dy, nfz = (-gam) * dz;
+      fix -= nfx; fiy -= nfy; fiz -= nfz;
+      atomicAdd(&fx[jf], nfx);
+      atomicAdd(&fy[jf], nfy);
+      atomicAdd(&fz[jf], nfz);
       acc[0] += ev;
-      acc[1] -= gvir_v * rsq;
+      acc[1] = fma(-gvir_v, rsq, acc[1]);
       acc[2] += ee;
-      acc[3] -= gvir_c * rsq;
-      acc[4] += dx * fx_; acc[5] += dx * fy_; acc[6] += dx * fz_;
-      acc[7] += dy * fy_; acc[8] += dy * fz_; acc[9] += dz * fz_;
+      acc[3] = fma(-gvir_c, rsq, acc[3]);
+      acc[4] = fma(-dx, nfx, acc[4]); acc[5] = fma(-dx, nfy, acc[5]); acc[6] = fma(-dx, nfz, acc[6]);
+      acc[7] = fma(-dy, nfy, acc[7]); acc[8] = fma(-dy, nfz, acc[8]); acc[9] = fma(-dz, nfz, acc[9]);
     }
     fix = warp_sum(fix); fiy = warp_sum(fiy); fiz = warp_sum(fiz);
     nrc = warp_sumi(nrc);
@@ -254,29 +297,34 @@ __global__ void k_excl_fp64(int natms, const int* list, int ld, const double* x,
 // -------------------------------------------------------------- mixed form
 // Full list, FP32 arithmetic, int64 fixed-point force sums; energies and
 // virials are summed per lane in FP32 and reduced in FP64 (x0.5: every pair
-// appears twice in the full list).
+// appears twice in the full list).  The erfc and LJ functions are evaluated
+// directly: on this part FP32 math and MUFU are far cheaper than the random
+// table reads the FP64 form's exact interpolation needs.
+constexpr float AS_A1 = 0.254829592f, AS_A2 = -0.284496736f, AS_A3 = 1.421413741f, AS_A4 = -1.453152027f,
+                AS_A5 = 1.061405429f, AS_P = 0.3275911f;
+constexpr int MAX_KEYS = 64;
+__constant__ float4 c_lj[MAX_KEYS];
 __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __restrict__ fstart,
                                                     const int* __restrict__ fcount, const int* __restrict__ flist,
                                                     const float4* __restrict__ xf, const int* __restrict__ ltype,
-                                                    const float* __restrict__ ecoef, const float* __restrict__ vcoef,
-                                                    const int* __restrict__ vkind, float rc2, float rv2, float erdr,
-                                                    float vrdr, float scaling, int max_grid,
+                                                    const int* __restrict__ vkind, float rc2, float rv2, float alpha,
+                                                    float alpha2rsqrpi, float scaling,
                                                     unsigned long long* fixp, double* blk,
                                                     unsigned long long* cnt) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   double acc[NACC];
 #pragma unroll
   for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
-  if (warp < natms) {
-    const int i = warp;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < natms; i += nwarps) {
     const float4 pi = xf[i];
     const float qi = pi.w * scaling;
     const int ai = ltype[i];
     const int s = fstart[i], n = fcount[i];
     long long sx = 0, sy = 0, sz = 0;
-    float a0 = 0, a1 = 0, a2 = 0, a3 = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
-    const int vstride = (max_grid + 3) * 6;
+    float a[NACC];
+#pragma unroll
+    for (int k = 0; k < NACC; ++k) a[k] = 0.f;
     int nrc = 0;
     for (int m = lane; m < n; m += 32) {
       const int j = flist[s + m];
@@ -286,39 +334,44 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
       if (rsq >= rc2 && rsq >= rv2) continue;
       const float rinv = rsqrtf(rsq);
       const float rrr = rsq * rinv;
+      const float r2i = rinv * rinv;
       float gam = 0.f;
+      // real-space Coulomb: the function the reference tabulates
+      // (electrostatic.F90:88-127, A&S erfc numerics.F90:3647), evaluated
+      // directly in FP32 (MUFU exp/rcp) instead of interpolated from tables
       if (rsq < rc2 && pj.w != 0.f) {
-        float ppp = rrr * erdr;
-        int k = (int)ppp;
-        float d = ppp - (float)k;
-        const float* c = ecoef + (size_t)k * 6;
-        float pre = qi * pj.w;
-        float eg = pre * fmaf(d, fmaf(d, c[5], c[4]), c[3]);
-        float ec = pre * fmaf(d, fmaf(d, c[2], c[1]), c[0]);
+        const float x = alpha * rrr;
+        const float ex = __expf(-x * x);
+        const float tt = __frcp_rn(fmaf(AS_P, x, 1.0f));
+        const float poly = tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, AS_A5, AS_A4), AS_A3), AS_A2), AS_A1);
+        const float pre = qi * pj.w;
+        const float ec = pre * poly * ex * rinv;                       // q q erfc(ar)/r
+        const float eg = fmaf(pre * alpha2rsqrpi, ex, ec) * r2i;        // (erfc/r + 2a/sqrt(pi) e^-x^2)/r^2
         gam += eg;
-        a2 += ec;
-        a3 -= eg * rsq;
+        a[2] += ec;
+        a[3] = fmaf(-eg, rsq, a[3]);
       }
       if (rsq < rv2) {
         const int key = vkey(ai, ltype[j]) - 1;
         if (vkind[key] != 0) {
-          float ppp = rrr * vrdr;
-          int k = (int)ppp;
-          float d = ppp - (float)k;
-          const float* c = vcoef + (size_t)key * vstride + (size_t)k * 6;
-          float gv = fmaf(d, fmaf(d, c[2], c[1]), c[0]) * rinv * rinv;
-          float e = fmaf(d, fmaf(d, c[5], c[4]), c[3]);
+          // 12-6 Lennard-Jones (two_body_potentials.F90:260-270)
+          const float4 lj = c_lj[key];  // (4 eps, 24 eps, sigma^2, -)
+          const float s2 = lj.z * r2i;
+          const float s6 = s2 * s2 * s2;
+          const float e = lj.x * s6 * (s6 - 1.0f);
+          const float gv = lj.y * s6 * fmaf(2.0f, s6, -1.0f) * r2i;
           gam += gv;
-          a0 += e;
-          a1 -= gv * rsq;
+          a[0] += e;
+          a[1] = fmaf(-gv, rsq, a[1]);
         }
       }
       ++nrc;
       const float fx_ = gam * dx, fy_ = gam * dy, fz_ = gam * dz;
-      sx += __float2ll_rn(fx_ * FIX_SCALE_F);
-      sy += __float2ll_rn(fy_ * FIX_SCALE_F);
-      sz += __float2ll_rn(fz_ * FIX_SCALE_F);
-      s0 += dx * fx_; s1 += dx * fy_; s2 += dx * fz_; s3 += dy * fy_; s4 += dy * fz_; s5 += dz * fz_;
+      sx += fix40(fx_);
+      sy += fix40(fy_);
+      sz += fix40(fz_);
+      a[4] = fmaf(dx, fx_, a[4]); a[5] = fmaf(dx, fy_, a[5]); a[6] = fmaf(dx, fz_, a[6]);
+      a[7] = fmaf(dy, fy_, a[7]); a[8] = fmaf(dy, fz_, a[8]); a[9] = fmaf(dz, fz_, a[9]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -326,6 +379,8 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
       sy += __shfl_xor_sync(0xffffffffu, sy, o);
       sz += __shfl_xor_sync(0xffffffffu, sz, o);
     }
+#pragma unroll
+    for (int k = 0; k < NACC; ++k) a[k] = warp_sumf(a[k]);
     nrc = warp_sumi(nrc);
     if (lane == 0) {
       atomicAdd(&fixp[3 * i + 0], (unsigned long long)sx);
@@ -333,9 +388,10 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
       atomicAdd(&fixp[3 * i + 2], (unsigned long long)sz);
       atomicAdd(&cnt[0], (unsigned long long)n);
       atomicAdd(&cnt[1], (unsigned long long)nrc);
+      // FP64 reduction of the per-atom sums (x0.5: every pair appears twice)
+#pragma unroll
+      for (int k = 0; k < NACC; ++k) acc[k] += 0.5 * (double)a[k];
     }
-    acc[0] = 0.5 * a0; acc[1] = 0.5 * a1; acc[2] = 0.5 * a2; acc[3] = 0.5 * a3;
-    acc[4] = 0.5 * s0; acc[5] = 0.5 * s1; acc[6] = 0.5 * s2; acc[7] = 0.5 * s3; acc[8] = 0.5 * s4; acc[9] = 0.5 * s5;
   }
   block_reduce_store<NACC>(acc, blk);
 }
@@ -345,6 +401,18 @@ inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
 }  // namespace
 
 // ===================================================================== host
+// per-key LJ constants for the mixed form (4 eps, 24 eps, sigma^2)
+void pair_setup() {
+  if (g.nkey > MAX_KEYS) throw (int)GB_ERR_ARG;
+  float4 lj[MAX_KEYS];
+  for (int k = 0; k < MAX_KEYS; ++k) lj[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k = 0; k < g.nkey; ++k) {
+    const double e = g.h_vdw_eps[k], s = g.h_vdw_sig[k];
+    lj[k] = make_float4((float)(4.0 * e), (float)(24.0 * e), (float)(s * s), 0.f);
+  }
+  GB_CUDA(cudaMemcpyToSymbol(c_lj, lj, sizeof(lj)));
+}
+
 // eng6: engrl, virrl, engex, virex, engvdw, virvdw; stress9 accumulates.
 void pair_forces(double* eng6, double* stress9) {
   PairGeom pg;
@@ -357,10 +425,17 @@ void pair_forces(double* eng6, double* stress9) {
   pg.rc2_hi = std::max(pg.rc2, pg.rv2) * (1.0 + 1e-12);
   pg.rv2_lo = pg.rv2 * (1.0 - 1e-12);
   pg.rv2_hi = pg.rv2 * (1.0 + 1e-12);
+  auto bits = [](double v) { long long b; std::memcpy(&b, &v, 8); return b; };
+  pg.b_rc2_lo = bits(pg.rc2_lo);
+  pg.b_rc2_hi = bits(pg.rc2 * (1.0 + 1e-12));
+  pg.b_rv2_lo = bits(pg.rv2_lo);
+  pg.b_rv2_hi = bits(pg.rv2_hi);
+  pg.b_hi = bits(pg.rc2_hi);
   pg.erdr = g.erfc_rdr;
   pg.vrdr = g.vdw_rdr;
   pg.scaling = g.scaling;
   pg.vdw_direct = g.p.vdw_direct;
+  pg.same_grid = (g.erfc_rdr == g.vdw_rdr) ? 1 : 0;
   pg.nsamples = g.nsamples;
   pg.max_grid = g.max_grid;
   pg.ntypes = g.p.ntypes;
@@ -371,7 +446,9 @@ void pair_forces(double* eng6, double* stress9) {
   const int nb2 = nblocks(g.natms, 128);
   GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
   if (g.precision == GB_FP64) {
-    int nb = nblocks((long long)g.mxatms * 32, T);
+    static int occ64 = 0;
+    if (!occ64) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_pair_fp64, T, 0));
+    int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, T), occ64 * g.nsm));
     double* blk = gb_blkacc(nb * NACC + nb2 * 8);
     prof_begin(P_PAIR);
     k_pair_fp64<<<nb, T, 0, st>>>(g.natms, g.sc, g.at_list, g.list, g.ld, g.x, g.y, g.z, g.chge, g.ltype, g.ltg,
@@ -390,13 +467,15 @@ void pair_forces(double* eng6, double* stress9) {
       gb_reduce_blocks(blk2, nb2, 8, &g.sc->acc[A_EXCL]);
     }
   } else {
-    int nb = nblocks((long long)g.natms * 32, T);
+    static int occ32 = 0;
+    if (!occ32) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_pair_mixed, T, 0));
+    int nb = std::max(1, std::min(nblocks((long long)g.natms * 32, T), occ32 * g.nsm));
     double* blk = gb_blkacc(nb * NACC + nb2 * 8);
     prof_begin(P_PAIR);
-    k_pair_mixed<<<nb, T, 0, st>>>(g.natms, g.fstart, g.fcount, g.flist, g.xf, g.ltype, g.erfc_coef_f, g.vdw_coef_f,
-                                   g.vdw_kind, (float)pg.rc2, (float)pg.rv2, (float)pg.erdr, (float)pg.vrdr,
-                                   (float)pg.scaling, g.max_grid, (unsigned long long*)g.fixp, blk,
-                                   &g.sc->npairs_list);
+    const double a2rp = g.p.alpha * 2.0 / std::sqrt(3.14159265358979323846264338327950288);
+    k_pair_mixed<<<nb, T, 0, st>>>(g.natms, g.fstart, g.fcount, g.flist, g.xf, g.ltype, g.vdw_kind, (float)pg.rc2,
+                                   (float)pg.rv2, (float)g.p.alpha, (float)a2rp, (float)pg.scaling,
+                                   (unsigned long long*)g.fixp, blk, &g.sc->npairs_list);
     GB_LAUNCHED();
     prof_end(P_PAIR);
     gb_reduce_blocks(blk, nb, NACC, &g.sc->acc[A_PAIR]);

@@ -46,7 +46,16 @@ template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
 template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { T2 r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { T2 r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
 // multiply by s*i
-template <typename T2> __device__ __forceinline__ T2 cmuli(T2 a, int s) { T2 r; r.x = -s * a.y; r.y = s * a.x; return r; }
+// multiply by S*i with S = +1 or -1 known at compile time (a free operand negation)
+template <int S, typename T2> __device__ __forceinline__ T2 cmuli(T2 a) {
+  T2 r;
+  if (S > 0) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; }
+  return r;
+}
+
+// x != 0 tested on the bit pattern (no FP64 compare instruction)
+__device__ __forceinline__ bool nonzero_bits(double v) { return (__double_as_longlong(v) << 1) != 0; }
+__device__ __forceinline__ bool nonzero_bits(float v) { return (__float_as_uint(v) << 1) != 0u; }
 
 struct FftPlan {
   int N;
@@ -55,9 +64,9 @@ struct FftPlan {
 };
 
 // one Stockham stage over nlines lines of length N held in shared memory
-template <typename T, typename T2>
+template <typename T, typename T2, int ISIGN>
 __device__ void fft_stage(const T2* __restrict__ in, T2* __restrict__ out, int N, int nlines, int R, int Ns,
-                          const T2* __restrict__ tw, int isign) {
+                          const T2* __restrict__ tw) {
   const int T_ = N / R;
   const int total = nlines * T_;
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
@@ -76,7 +85,7 @@ __device__ void fft_stage(const T2* __restrict__ in, T2* __restrict__ out, int N
       for (int r = 1; r < 5; ++r) {
         if (r < R) {
           T2 w = tw[(r * k * step) % N];
-          if (isign < 0) w.y = -w.y;
+          if (ISIGN < 0) w.y = -w.y;
           v[r] = cmul(v[r], w);
         }
       }
@@ -84,7 +93,7 @@ __device__ void fft_stage(const T2* __restrict__ in, T2* __restrict__ out, int N
     T2 o[5];
     if (R == 4) {
       T2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]), c = cadd(v[1], v[3]), d = csub(v[1], v[3]);
-      T2 di = cmuli(d, isign);
+      T2 di = cmuli<ISIGN>(d);
       o[0] = cadd(a, c); o[2] = csub(a, c); o[1] = cadd(b, di); o[3] = csub(b, di);
     } else if (R == 2) {
       o[0] = cadd(v[0], v[1]); o[1] = csub(v[0], v[1]);
@@ -93,7 +102,7 @@ __device__ void fft_stage(const T2* __restrict__ in, T2* __restrict__ out, int N
       T2 t = cadd(v[1], v[2]), u = csub(v[1], v[2]);
       T2 m;
       m.x = v[0].x - (T)0.5 * t.x; m.y = v[0].y - (T)0.5 * t.y;
-      T2 ui = cmuli(u, isign);
+      T2 ui = cmuli<ISIGN>(u);
       ui.x *= h; ui.y *= h;
       o[0] = cadd(v[0], t); o[1] = cadd(m, ui); o[2] = csub(m, ui);
     } else {  // R == 5
@@ -106,7 +115,7 @@ __device__ void fft_stage(const T2* __restrict__ in, T2* __restrict__ out, int N
       a2.x = v[0].x + c2 * t1.x + c1 * t2.x; a2.y = v[0].y + c2 * t1.y + c1 * t2.y;
       b1.x = s1 * t3.x + s2 * t4.x; b1.y = s1 * t3.y + s2 * t4.y;
       b2.x = s2 * t3.x - s1 * t4.x; b2.y = s2 * t3.y - s1 * t4.y;
-      T2 ib1 = cmuli(b1, isign), ib2 = cmuli(b2, isign);
+      T2 ib1 = cmuli<ISIGN>(b1), ib2 = cmuli<ISIGN>(b2);
       o[1] = cadd(a1, ib1); o[4] = csub(a1, ib1); o[2] = cadd(a2, ib2); o[3] = csub(a2, ib2);
     }
     const int base = (j / Ns) * Ns * R + k;
@@ -117,12 +126,12 @@ __device__ void fft_stage(const T2* __restrict__ in, T2* __restrict__ out, int N
 }
 
 // full transform of nlines lines; returns the buffer holding the result
-template <typename T, typename T2>
-__device__ T2* fft_lines(T2* a, T2* b, const FftPlan& pl, int nlines, const T2* tw, int isign) {
+template <typename T, typename T2, int ISIGN>
+__device__ T2* fft_lines(T2* a, T2* b, const FftPlan& pl, int nlines, const T2* tw) {
   int Ns = 1;
   for (int s = 0; s < pl.nrad; ++s) {
     __syncthreads();
-    fft_stage<T, T2>(a, b, pl.N, nlines, pl.rad[s], Ns, tw, isign);
+    fft_stage<T, T2, ISIGN>(a, b, pl.N, nlines, pl.rad[s], Ns, tw);
     Ns *= pl.rad[s];
     T2* t = a; a = b; b = t;
   }
@@ -222,70 +231,175 @@ __global__ void k_brick_sort(int nbricks, const int* start, const int* tmp, int*
 }
 
 // ------------------------------------------------------------- spreading
-// CTA = one brick; thread = one (y,z) row of B0 points along x.
 constexpr int SPREAD_CH = 32;
 constexpr int BMAX = 16;
 
+// Tile scatter: CTA = one brick and the atoms whose floor(u) lies in it.  The
+// CTA owns a (B+p-1)^3 shared-memory tile covering the brick plus the p-1
+// points below it that its atoms reach; atoms are scattered one after another
+// (one FMA per grid point, all lanes busy, no atomics), then the tile is
+// written to its own slot of `ext` for the halo reduction below.
 template <typename T>
-__global__ void k_spme_spread(SpmeGeom sg, const int* __restrict__ bstart, const int* __restrict__ batoms,
-                              const T* __restrict__ spl, const int* __restrict__ nidx, const double* __restrict__ q,
-                              T* __restrict__ Q) {
+__global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, const int* __restrict__ batoms,
+                                   const T* __restrict__ spl, const int* __restrict__ nidx,
+                                   const double* __restrict__ q, T* __restrict__ ext) {
+  extern __shared__ unsigned char smem_raw[];
+  const int p = sg.p;
   const int b = blockIdx.x;
   const int bx = b % sg.nb[0], by = (b / sg.nb[0]) % sg.nb[1], bz = b / (sg.nb[0] * sg.nb[1]);
-  const int B0 = sg.B[0], B1 = sg.B[1], B2 = sg.B[2], p = sg.p;
-  const int g0x = bx * B0, g0y = by * B1, g0z = bz * B2;
-  const int ty = threadIdx.x % B1, tz = threadIdx.x / B1;
-  const bool active = threadIdx.x < B1 * B2;
-  __shared__ T wx[SPREAD_CH][BMAX], wy[SPREAD_CH][BMAX], wz[SPREAD_CH][BMAX];
-  T acc[BMAX];
-#pragma unroll
-  for (int k = 0; k < BMAX; ++k) acc[k] = (T)0;
-  for (int sb = 0; sb < 8; ++sb) {
-    const int sx = (bx + (sb & 1)) % sg.nb[0], sy = (by + ((sb >> 1) & 1)) % sg.nb[1],
-              sz = (bz + ((sb >> 2) & 1)) % sg.nb[2];
-    // skip duplicates when a dimension has a single brick
-    if (((sb & 1) && sg.nb[0] == 1) || (((sb >> 1) & 1) && sg.nb[1] == 1) || (((sb >> 2) & 1) && sg.nb[2] == 1))
-      continue;
-    const int src = sx + sg.nb[0] * (sy + sg.nb[1] * sz);
-    const int s0 = bstart[src], s1 = bstart[src + 1];
-    for (int c = s0; c < s1; c += SPREAD_CH) {
-      const int nc = min(SPREAD_CH, s1 - c);
-      __syncthreads();
-      // stage brick-aligned weights: w[d][k] for grid point g0+k
-      for (int e = threadIdx.x; e < nc * (B0 + B1 + B2); e += blockDim.x) {
-        const int a = e / (B0 + B1 + B2);
-        int k = e - a * (B0 + B1 + B2);
-        int d = 0, Bd = B0, g0 = g0x;
-        if (k >= B0) { k -= B0; d = 1; Bd = B1; g0 = g0y; if (k >= B1) { k -= B1; d = 2; Bd = B2; g0 = g0z; } }
-        (void)Bd;
-        const int i = batoms[c + a];
-        const int n = nidx[3 * i + d];
-        int t = (g0 + k) - n + p - 1;
-        const int K = sg.K[d];
-        t %= K; if (t < 0) t += K;
-        T w = (t < p) ? spl[((size_t)i * 3 + d) * p + t] : (T)0;
-        if (d == 2 && t < p) w *= (T)q[i];
-        if (d == 0) wx[a][k] = w; else if (d == 1) wy[a][k] = w; else wz[a][k] = w;
-      }
-      __syncthreads();
-      if (active) {
-        for (int a = 0; a < nc; ++a) {
-          const T wyz = wy[a][ty] * wz[a][tz];
-          if (wyz != (T)0) {
-#pragma unroll
-            for (int k = 0; k < BMAX; ++k)
-              if (k < B0) acc[k] += wyz * wx[a][k];
-          }
-        }
+  const int g0x = bx * sg.B[0], g0y = by * sg.B[1], g0z = bz * sg.B[2];
+  const int TXd = sg.B[0] + p - 1, TYd = sg.B[1] + p - 1, TZd = sg.B[2] + p - 1;
+  const int tsize = TXd * TYd * TZd;
+  T* tile = reinterpret_cast<T*>(smem_raw);
+  T* Pkl = tile + tsize;                     // [SPREAD_CH][p*p] My(k) * q Mz(l)
+  T* Mx = Pkl + SPREAD_CH * p * p;           // [SPREAD_CH][p]
+  int* off = reinterpret_cast<int*>(Mx + SPREAD_CH * p);  // [SPREAD_CH][3] tile offsets
+  for (int e = threadIdx.x; e < tsize; e += blockDim.x) tile[e] = (T)0;
+  const int s0 = bstart[b], s1 = bstart[b + 1];
+  const int p2 = p * p, p3 = p2 * p;
+  for (int c = s0; c < s1; c += SPREAD_CH) {
+    const int nc = min(SPREAD_CH, s1 - c);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nc * p; e += blockDim.x) {
+      const int a = e / p, t = e - a * p;
+      const int i = batoms[c + a];
+      Mx[a * p + t] = spl[((size_t)i * 3 + 0) * p + t];
+      if (t == 0) {
+        off[a * 3 + 0] = nidx[3 * i + 0] - g0x;
+        off[a * 3 + 1] = nidx[3 * i + 1] - g0y;
+        off[a * 3 + 2] = nidx[3 * i + 2] - g0z;
       }
     }
+    for (int e = threadIdx.x; e < nc * p2; e += blockDim.x) {
+      const int a = e / p2, kl = e - a * p2, k = kl % p, l = kl / p;
+      const int i = batoms[c + a];
+      Pkl[a * p2 + kl] = spl[((size_t)i * 3 + 1) * p + k] * (spl[((size_t)i * 3 + 2) * p + l] * (T)q[i]);
+    }
+    __syncthreads();
+    for (int a = 0; a < nc; ++a) {
+      const int ox = off[a * 3], oy = off[a * 3 + 1], oz = off[a * 3 + 2];
+      for (int e = threadIdx.x; e < p3; e += blockDim.x) {
+        const int j = e % p, kl = e / p, k = kl % p, l = kl / p;
+        T* dst = tile + ((oz + l) * TYd + (oy + k)) * TXd + (ox + j);
+        *dst = fma(Mx[a * p + j], Pkl[a * p2 + kl], *dst);
+      }
+      __syncthreads();
+    }
   }
-  if (active) {
-    T* row = Q + ((size_t)(g0z + tz) * sg.K[1] + (g0y + ty)) * sg.K[0] + g0x;
-#pragma unroll
-    for (int k = 0; k < BMAX; ++k)
-      if (k < B0) row[k] = acc[k];
+  __syncthreads();
+  T* out = ext + (size_t)b * tsize;
+  for (int e = threadIdx.x; e < tsize; e += blockDim.x) out[e] = tile[e];
+}
+
+// Mixed form: the same tile decomposition, but warps scatter different atoms
+// concurrently with 64-bit integer shared-memory atomics on a 2^-40 fixed-point
+// tile (no barrier per atom; integer sums are order independent, so the grid
+// is bit-reproducible).  The tile goes to `ext` as int64.
+__global__ void k_spme_spread_fix(SpmeGeom sg, const int* __restrict__ bstart, const int* __restrict__ batoms,
+                                  const float* __restrict__ spl, const int* __restrict__ nidx,
+                                  const double* __restrict__ q, long long* __restrict__ ext) {
+  extern __shared__ unsigned char smem_raw[];
+  const int p = sg.p;
+  const int b = blockIdx.x;
+  const int bx = b % sg.nb[0], by = (b / sg.nb[0]) % sg.nb[1], bz = b / (sg.nb[0] * sg.nb[1]);
+  const int g0x = bx * sg.B[0], g0y = by * sg.B[1], g0z = bz * sg.B[2];
+  const int TXd = sg.B[0] + p - 1, TYd = sg.B[1] + p - 1, TZd = sg.B[2] + p - 1;
+  const int tsize = TXd * TYd * TZd;
+  long long* tile = reinterpret_cast<long long*>(smem_raw);
+  for (int e = threadIdx.x; e < tsize; e += blockDim.x) tile[e] = 0;
+  __syncthreads();
+  const int s0 = bstart[b], s1 = bstart[b + 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int p2 = p * p, p3 = p2 * p;
+  for (int a = s0 + wid; a < s1; a += nw) {
+    const int i = batoms[a];
+    const float* sx = spl + ((size_t)i * 3 + 0) * p;
+    const float* sy = sx + p;
+    const float* sz = sy + p;
+    const float qi = (float)q[i];
+    const int ox = nidx[3 * i] - g0x, oy = nidx[3 * i + 1] - g0y, oz = nidx[3 * i + 2] - g0z;
+    for (int e = lane; e < p3; e += 32) {
+      const int j = e % p, kl = e / p, k = kl % p, l = kl / p;
+      const float w = sx[j] * (sy[k] * (sz[l] * qi));
+      atomicAdd((unsigned long long*)&tile[((oz + l) * TYd + (oy + k)) * TXd + (ox + j)],
+                (unsigned long long)fix40(w));
+    }
+    (void)p2;
   }
+  __syncthreads();
+  long long* out = ext + (size_t)b * tsize;
+  for (int e = threadIdx.x; e < tsize; e += blockDim.x) out[e] = tile[e];
+}
+
+// fixed-point halo reduction for the mixed form (int64 sums, one conversion per point)
+__global__ void k_spme_tile_reduce_fix(SpmeGeom sg, const long long* __restrict__ ext, float* __restrict__ Q) {
+  const size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
+  if (gid >= (size_t)K0 * K1 * K2) return;
+  const int gg[3] = {(int)(gid % K0), (int)((gid / K0) % K1), (int)(gid / ((size_t)K0 * K1))};
+  const int p = sg.p;
+  const int TXd = sg.B[0] + p - 1, TYd = sg.B[1] + p - 1, TZd = sg.B[2] + p - 1;
+  const size_t tsize = (size_t)TXd * TYd * TZd;
+  int bb[3][2], tc[3][2], nbr[3];
+  for (int d = 0; d < 3; ++d) {
+    const int B = sg.B[d];
+    const int b0 = gg[d] / B;
+    bb[d][0] = b0;
+    tc[d][0] = gg[d] - b0 * B + p - 1;
+    nbr[d] = 1;
+    const int t1 = gg[d] - (b0 + 1) * B + p - 1;
+    if (t1 >= 0) { bb[d][1] = (b0 + 1) % sg.nb[d]; tc[d][1] = t1; nbr[d] = 2; }
+  }
+  long long s = 0;
+  for (int cz = 0; cz < nbr[2]; ++cz)
+    for (int cy = 0; cy < nbr[1]; ++cy)
+      for (int cx = 0; cx < nbr[0]; ++cx) {
+        const int b = bb[0][cx] + sg.nb[0] * (bb[1][cy] + sg.nb[1] * bb[2][cz]);
+        s += ext[(size_t)b * tsize + ((size_t)tc[2][cz] * TYd + tc[1][cy]) * TXd + tc[0][cx]];
+      }
+  Q[gid] = (float)s * 9.094947017729282e-13f;  // 2^-40
+  (void)TZd;
+}
+
+// Halo reduction: every grid point sums, in a fixed order, the tile entries of
+// the (at most 2 per dimension) bricks whose tiles cover it.
+template <typename T>
+__global__ void k_spme_tile_reduce(SpmeGeom sg, const T* __restrict__ ext, T* __restrict__ Q) {
+  const size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
+  if (gid >= (size_t)K0 * K1 * K2) return;
+  const int gx = (int)(gid % K0), gy = (int)((gid / K0) % K1), gz = (int)(gid / ((size_t)K0 * K1));
+  const int p = sg.p;
+  const int TXd = sg.B[0] + p - 1, TYd = sg.B[1] + p - 1, TZd = sg.B[2] + p - 1;
+  const size_t tsize = (size_t)TXd * TYd * TZd;
+  int bb[3][2], tc[3][2], nbr[3];
+  const int gg[3] = {gx, gy, gz};
+  for (int d = 0; d < 3; ++d) {
+    const int B = sg.B[d];
+    const int b0 = gg[d] / B;
+    bb[d][0] = b0;
+    tc[d][0] = gg[d] - b0 * B + p - 1;
+    nbr[d] = 1;
+    const int t1 = gg[d] - (b0 + 1) * B + p - 1;
+    if (t1 >= 0) {
+      bb[d][1] = (b0 + 1) % sg.nb[d];
+      tc[d][1] = t1;
+      nbr[d] = 2;
+    }
+  }
+  T s = (T)0;
+  for (int cz = 0; cz < nbr[2]; ++cz)
+    for (int cy = 0; cy < nbr[1]; ++cy)
+      for (int cx = 0; cx < nbr[0]; ++cx) {
+        const int b = bb[0][cx] + sg.nb[0] * (bb[1][cy] + sg.nb[1] * bb[2][cz]);
+        s += ext[(size_t)b * tsize + ((size_t)tc[2][cz] * TYd + tc[1][cy]) * TXd + tc[0][cx]];
+      }
+  Q[gid] = s;
+}
+
+inline size_t spread_smem(int B0, int B1, int B2, int p, size_t esz) {
+  const size_t tsize = (size_t)(B0 + p - 1) * (B1 + p - 1) * (B2 + p - 1);
+  return esz * (tsize + (size_t)SPREAD_CH * p * p + (size_t)SPREAD_CH * p) + sizeof(int) * 3 * SPREAD_CH;
 }
 
 // ---------------------------------------------------------------- FFT passes
@@ -303,7 +417,7 @@ __global__ void k_fft_x_fwd(const T* __restrict__ Q, T2* __restrict__ G, FftPlan
     T2 v; v.x = Q[row0 * N + e]; v.y = (T)0;
     a[e] = v;
   }
-  T2* r = fft_lines<T, T2>(a, b, pl, nl, tw, +1);
+  T2* r = fft_lines<T, T2, +1>(a, b, pl, nl, tw);
   for (int e = threadIdx.x; e < nl * N; e += blockDim.x) G[row0 * N + e] = r[e];
 }
 
@@ -318,13 +432,13 @@ __global__ void k_fft_x_inv(const T2* __restrict__ G, T* __restrict__ Q, FftPlan
   const size_t row0 = (size_t)blockIdx.x * lines;
   const int nl = (int)min((size_t)lines, (size_t)nrows - row0);
   for (int e = threadIdx.x; e < nl * N; e += blockDim.x) a[e] = G[row0 * N + e];
-  T2* r = fft_lines<T, T2>(a, b, pl, nl, tw, -1);
+  T2* r = fft_lines<T, T2, -1>(a, b, pl, nl, tw);
   for (int e = threadIdx.x; e < nl * N; e += blockDim.x) Q[row0 * N + e] = r[e].x;
 }
 
 // Y pass (stride K1): tile of TX columns x N lines, in place
-template <typename T, typename T2>
-__global__ void k_fft_y(T2* __restrict__ G, int K1, int K2, FftPlan pl, const T2* __restrict__ tw, int isign) {
+template <typename T, typename T2, int ISIGN>
+__global__ void k_fft_y(T2* __restrict__ G, int K1, int K2, FftPlan pl, const T2* __restrict__ tw) {
   extern __shared__ unsigned char smem_raw[];
   T2* a = reinterpret_cast<T2*>(smem_raw);
   T2* b = a + TX * pl.N;
@@ -336,7 +450,7 @@ __global__ void k_fft_y(T2* __restrict__ G, int K1, int K2, FftPlan pl, const T2
     int yy = e / TX, t = e - yy * TX;
     a[t * K2 + yy] = base[(size_t)yy * K1 + t];
   }
-  T2* r = fft_lines<T, T2>(a, b, pl, TX, tw, isign);
+  T2* r = fft_lines<T, T2, ISIGN>(a, b, pl, TX, tw);
   for (int e = threadIdx.x; e < TX * K2; e += blockDim.x) {
     int yy = e / TX, t = e - yy * TX;
     base[(size_t)yy * K1 + t] = r[t * K2 + yy];
@@ -359,30 +473,49 @@ __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan
     int zz = e / TX, t = e - zz * TX;
     a[t * K3 + zz] = base[(size_t)zz * plane + t];
   }
-  T2* r = fft_lines<T, T2>(a, b, pl, TX, tw, +1);
-  double st[6] = {0, 0, 0, 0, 0, 0};
-  for (int e = threadIdx.x; e < TX * K3; e += blockDim.x) {
-    int t = e / K3, zz = e - t * K3;
-    const size_t gi = (size_t)zz * plane + (size_t)yy * K1 + x0 + t;
-    const T th = theta[gi];
-    T2 v = r[e];
-    if (th != (T)0) {
-      const double pv = (double)psi[gi] * ((double)v.x * v.x + (double)v.y * v.y);
-      int jj = x0 + t; if (2 * jj > K1) jj -= K1;
-      int kk = yy; if (2 * kk > K2) kk -= K2;
-      int ll = zz; if (2 * ll > K3) ll -= K3;
-      double rp[3];
-      for (int c = 0; c < 3; ++c) rp[c] = (double)jj * sg.rc[3 * c] + (double)kk * sg.rc[3 * c + 1] + (double)ll * sg.rc[3 * c + 2];
-      st[0] += rp[0] * rp[0] * pv; st[1] += rp[0] * rp[1] * pv; st[2] += rp[0] * rp[2] * pv;
-      st[3] += rp[1] * rp[1] * pv; st[4] += rp[1] * rp[2] * pv; st[5] += rp[2] * rp[2] * pv;
-      v.x *= th; v.y *= th;
-    } else {
-      v.x = (T)0; v.y = (T)0;
+  // m_z = ll * rcell(9) for the cubic cell (gb_init accepts cubic cells only)
+  T* rzt = reinterpret_cast<T*>(b + TX * pl.N);
+  for (int zz = threadIdx.x; zz < K3; zz += blockDim.x) {
+    int ll = zz; if (2 * ll > K3) ll -= K3;
+    rzt[zz] = (T)((double)ll * sg.rc[8]);
+  }
+  T2* r = fft_lines<T, T2, +1>(a, b, pl, TX, tw);
+  // Reciprocal stress sum_m m_a m_b psi |Q(m)|^2 (ewald_spole.F90:1362-1371): with
+  // m = (mx, my, mz) and mx, my fixed along a z line, each line needs only
+  // A = sum psi|Q|^2, B = sum mz psi|Q|^2, C = sum mz^2 psi|Q|^2.
+  const int tpl = blockDim.x / TX;          // threads per line
+  const int t = threadIdx.x / tpl;          // this thread's line
+  T A = 0, B = 0, C = 0;
+  if (t < TX) {
+    const size_t line0 = (size_t)yy * K1 + x0 + t;
+    T2* rl = r + t * K3;
+    for (int zz = threadIdx.x - t * tpl; zz < K3; zz += tpl) {
+      const size_t gi = line0 * K3 + zz;  // theta/psi are stored z-contiguous per (x,y) line
+      const T th = theta[gi];
+      T2 v = rl[zz];
+      if (nonzero_bits(th)) {
+        const T pv = psi[gi] * (v.x * v.x + v.y * v.y);
+        const T u = pv * rzt[zz];
+        A += pv;
+        B += u;
+        C = fma(u, rzt[zz], C);
+        v.x *= th; v.y *= th;
+      } else {
+        v.x = (T)0; v.y = (T)0;
+      }
+      rl[zz] = v;
     }
-    r[e] = v;
+  }
+  double st[6] = {0, 0, 0, 0, 0, 0};
+  if (t < TX) {
+    int jj = x0 + t; if (2 * jj > K1) jj -= K1;
+    int kk = yy; if (2 * kk > K2) kk -= K2;
+    const double rx = (double)jj * sg.rc[0], ry = (double)kk * sg.rc[4];
+    st[0] = rx * rx * (double)A; st[1] = rx * ry * (double)A; st[2] = rx * (double)B;
+    st[3] = ry * ry * (double)A; st[4] = ry * (double)B; st[5] = (double)C;
   }
   T2* o = (r == a) ? b : a;
-  T2* r2 = fft_lines<T, T2>(r, o, pl, TX, tw, -1);
+  T2* r2 = fft_lines<T, T2, -1>(r, o, pl, TX, tw);
   for (int e = threadIdx.x; e < TX * K3; e += blockDim.x) {
     int zz = e / TX, t = e - zz * TX;
     base[(size_t)zz * plane + t] = r2[t * K3 + zz];
@@ -416,9 +549,11 @@ __global__ void k_spme_gather(int natms, const double* __restrict__ x, const dou
     int ix[PMAX];
     for (int t = 0; t < p; ++t) { int v = (n0[0] + t) % K0; if (v < 0) v += K0; ix[t] = v; }
     const T qi = (T)q[i];
+    // separable sums: rows along x first, then y within a z plane, then z
     T e = 0, fxs = 0, fys = 0, fzs = 0;
     for (int l = 0; l < p; ++l) {
       int zz = (n0[2] + l) % K2; if (zz < 0) zz += K2;
+      T a0 = 0, a1 = 0, a2 = 0;
       for (int k = 0; k < p; ++k) {
         int yy = (n0[1] + k) % K1; if (yy < 0) yy += K1;
         const T* row = phi + ((size_t)zz * K1 + yy) * K0;
@@ -427,16 +562,18 @@ __global__ void k_spme_gather(int natms, const double* __restrict__ x, const dou
         for (int t = 0; t < PMAX; ++t) {
           if (t < p) {
             const T ph = row[ix[t]];
-            s0 += m[0][t] * ph;
-            s1 += dm[0][t] * ph;
+            s0 = fma(m[0][t], ph, s0);
+            s1 = fma(dm[0][t], ph, s1);
           }
         }
-        const T myz = m[1][k] * m[2][l];
-        e += myz * s0;
-        fxs += myz * s1;
-        fys += dm[1][k] * m[2][l] * s0;
-        fzs += m[1][k] * dm[2][l] * s0;
+        a0 = fma(m[1][k], s0, a0);   // sum My Mx phi
+        a1 = fma(m[1][k], s1, a1);   // sum My dMx phi
+        a2 = fma(dm[1][k], s0, a2);  // sum dMy Mx phi
       }
+      e = fma(m[2][l], a0, e);
+      fxs = fma(m[2][l], a1, fxs);
+      fys = fma(m[2][l], a2, fys);
+      fzs = fma(dm[2][l], a0, fzs);
     }
     const double fx_ = -(double)qi * (double)fxs * rk0, fy_ = -(double)qi * (double)fys * rk1,
                  fz_ = -(double)qi * (double)fzs * rk2;
@@ -493,6 +630,7 @@ FftPlan make_plan(int N) {
 
 FftPlan plan1, plan2, plan3;
 SpmeGeom h_sg;
+void* g_spread_ext = nullptr;  // per-brick spread tiles (nbricks x (B+p-1)^3)
 
 int choose_brick(int K, int p) {
   for (int B = p - 1; B <= BMAX; ++B)
@@ -547,6 +685,17 @@ void spme_setup() {
   GB_CUDA(cudaMalloc(&g.theta, sizeof(double) * NG));
   GB_CUDA(cudaMalloc(&g.psi, sizeof(double) * NG));
   GB_CUDA(cudaMalloc(&g.fspme, sizeof(double) * 3 * (size_t)g.natms));
+  {
+    const size_t tsize = (size_t)(g.B1 + p - 1) * (g.B2 + p - 1) * (g.B3 + p - 1);
+    if (g_spread_ext) cudaFree(g_spread_ext);
+    GB_CUDA(cudaMalloc(&g_spread_ext, sizeof(double) * tsize * g.nbricks));
+    const int sm64 = (int)spread_smem(g.B1, g.B2, g.B3, p, sizeof(double));
+    const int sm32 = (int)spread_smem(g.B1, g.B2, g.B3, p, sizeof(float));
+    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64));
+    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
+    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_fix, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(tsize * sizeof(long long))));
+  }
   // |b(m)|^2 (bspline_coeffs_gen, bspline.F90:73-190) on the host in FP64
   std::vector<double> norm2[3];
   {
@@ -601,7 +750,7 @@ void spme_setup() {
           double r1 = (double)ll * rc[5] + (double)kk * rc[4] + (double)jj * rc[3];
           double r2 = (double)ll * rc[8] + (double)kk * rc[7] + (double)jj * rc[6];
           double k2 = r0 * r0 + r1 * r1 + r2 * r2;
-          size_t gi = ((size_t)l * g.K2 + k) * g.K1 + j;
+          size_t gi = ((size_t)k * g.K1 + j) * g.K3 + l;  // z-contiguous per (x,y) line for the z pass
           if (k2 <= cut2 && k2 > test_fac) {
             double bb = norm2[2][l] * norm2[1][k] * norm2[0][j];
             double f = std::sqrt(k2) * recip_conv_fac;
@@ -649,11 +798,13 @@ void spme_setup() {
   smem = std::max(smem, 48 * 1024);
   GB_CUDA(cudaFuncSetAttribute(k_fft_x_fwd<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   GB_CUDA(cudaFuncSetAttribute(k_fft_x_inv<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_y<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_y<double, double2, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_y<double, double2, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   GB_CUDA(cudaFuncSetAttribute(k_fft_z_conv<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   GB_CUDA(cudaFuncSetAttribute(k_fft_x_fwd<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   GB_CUDA(cudaFuncSetAttribute(k_fft_x_inv<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_y<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_y<float, float2, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  GB_CUDA(cudaFuncSetAttribute(k_fft_y<float, float2, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   GB_CUDA(cudaFuncSetAttribute(k_fft_z_conv<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
 }
 
@@ -684,12 +835,27 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
   k_brick_sort<<<nblocks((long long)g.nbricks * 32, 256), 256, 0, st>>>(g.nbricks, g.brick_start, tmp, g.brick_atoms);
   GB_LAUNCHED();
   prof_end(P_SPME_PREP);
-  // spreading
+  // spreading: tile scatter per brick, then the fixed-order halo reduction
   {
-    int threads = ((g.B2 * g.B3 + 31) / 32) * 32;
+    T* ext = reinterpret_cast<T*>(g_spread_ext);
+    const size_t smem = spread_smem(g.B1, g.B2, g.B3, p, sizeof(T));
+    const size_t NG = (size_t)g.K1 * g.K2 * g.K3;
     prof_begin(P_SPME_SPREAD);
-    k_spme_spread<T><<<g.nbricks, threads, 0, st>>>(h_sg, g.brick_start, g.brick_atoms, spl, g.nidx, g.chge, Q);
-    GB_LAUNCHED();
+    if (std::is_same<T, double>::value) {
+      k_spme_spread_tile<T><<<g.nbricks, 512, smem, st>>>(h_sg, g.brick_start, g.brick_atoms, spl, g.nidx, g.chge,
+                                                          ext);
+      GB_LAUNCHED();
+      k_spme_tile_reduce<T><<<nblocks((long long)NG, 256), 256, 0, st>>>(h_sg, ext, Q);
+      GB_LAUNCHED();
+    } else {
+      long long* exti = reinterpret_cast<long long*>(g_spread_ext);
+      const size_t tsz = (size_t)(g.B1 + p - 1) * (g.B2 + p - 1) * (g.B3 + p - 1);
+      k_spme_spread_fix<<<g.nbricks, 256, tsz * sizeof(long long), st>>>(
+          h_sg, g.brick_start, g.brick_atoms, reinterpret_cast<const float*>(spl), g.nidx, g.chge, exti);
+      GB_LAUNCHED();
+      k_spme_tile_reduce_fix<<<nblocks((long long)NG, 256), 256, 0, st>>>(h_sg, exti, reinterpret_cast<float*>(Q));
+      GB_LAUNCHED();
+    }
     prof_end(P_SPME_SPREAD);
   }
   // FFT + convolution
@@ -700,17 +866,18 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
   GB_LAUNCHED();
   prof_end(P_FFT_XF);
   prof_begin(P_FFT_Y);
-  k_fft_y<T, T2><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2, +1);
+  k_fft_y<T, T2, +1><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2);
   GB_LAUNCHED();
   prof_end(P_FFT_Y);
   const int nbz = (g.K1 / TX) * g.K2;
   double* blkz = gb_blkacc(nbz * 6 + nblocks(n, 128) * 4);
   prof_begin(P_FFT_Z);
-  k_fft_z_conv<T, T2><<<nbz, 256, fft_smem(g.K3, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, g.K3, plan3, tw3, th, ps, h_sg, blkz);
+  k_fft_z_conv<T, T2><<<nbz, 256, fft_smem(g.K3, TX, sizeof(T2)) + g.K3 * sizeof(T), st>>>(G, g.K1, g.K2, g.K3, plan3,
+                                                                                        tw3, th, ps, h_sg, blkz);
   GB_LAUNCHED();
   prof_end(P_FFT_Z);
   prof_begin(P_FFT_Y);
-  k_fft_y<T, T2><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2, -1);
+  k_fft_y<T, T2, -1><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2);
   GB_LAUNCHED();
   prof_end(P_FFT_Y);
   prof_begin(P_FFT_XI);
