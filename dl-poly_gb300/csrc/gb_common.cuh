@@ -230,11 +230,12 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 __device__ __forceinline__ long long fix40(float x) {
   const unsigned u = __float_as_uint(x);
   const int sh = (int)((u >> 23) & 0xFFu) - 127 + 17;  // x = m 2^(e-23), m 24-bit: x 2^40 = m 2^(e+17)
-  const long long m = (long long)((u & 0x7FFFFFu) | 0x800000u);
-  long long v = 0;
-  if (sh >= 0) v = m << min(sh, 39);
-  else if (sh > -24) v = m >> (-sh);
-  return (u >> 31) ? -v : v;
+  const unsigned m = (u & 0x7FFFFFu) | 0x800000u;
+  // branchless: left shift for sh >= 0 (<= 39 in range), right shift otherwise (>= 24 gives 0)
+  const unsigned long long up = (unsigned long long)m << min(max(sh, 0), 39);
+  const unsigned long long dn = (unsigned long long)(m >> min(max(-sh, 0), 31));
+  const long long v = (long long)(sh >= 0 ? up : dn);
+  return (int)u < 0 ? -v : v;
 }
 
 // Block-wide reduction of NV doubles into per-block slots out[blockIdx.x*NV + k].
@@ -256,6 +257,30 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* out)
       double t = lane < nw ? red[lane][k] : 0.0;
       t = warp_sum(t);
       if (lane == 0) out[(size_t)blockIdx.x * NV + k] = t;
+    }
+  }
+}
+
+// FP32 variant: sums in FP32 and converts only the NV block totals (one thread)
+// to FP64, so an FP32 kernel issues no FP64 instruction per warp.
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(float (&v)[NV], double* out) {
+  __shared__ float redf[32][NV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sumf(v[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) redf[wid][k] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      float t = lane < nw ? redf[lane][k] : 0.f;
+      t = warp_sumf(t);
+      if (lane == 0) out[(size_t)blockIdx.x * NV + k] = (double)t;
     }
   }
 }

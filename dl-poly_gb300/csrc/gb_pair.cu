@@ -303,29 +303,39 @@ __global__ void k_excl_fp64(int natms, const int* list, int ld, const double* x,
 constexpr float AS_A1 = 0.254829592f, AS_A2 = -0.284496736f, AS_A3 = 1.421413741f, AS_A4 = -1.453152027f,
                 AS_A5 = 1.061405429f, AS_P = 0.3275911f;
 constexpr int MAX_KEYS = 64;
+constexpr int MAX_TYPES = 10;  // 55 type-pair keys
 __constant__ float4 c_lj[MAX_KEYS];
 __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __restrict__ fstart,
                                                     const int* __restrict__ fcount, const int* __restrict__ flist,
                                                     const float4* __restrict__ xf, const int* __restrict__ ltype,
-                                                    const int* __restrict__ vkind, float rc2, float rv2, float alpha,
+                                                    int ntypes, float rc2, float rv2, float alpha,
                                                     float alpha2rsqrpi, float scaling,
                                                     unsigned long long* fixp, double* blk,
                                                     unsigned long long* cnt) {
+  // LJ constants per ordered type pair in shared memory (uniform-free indexing);
+  // .w = 1 where a 12-6 potential exists
+  __shared__ float4 s_lj[MAX_TYPES * MAX_TYPES];
+  for (int e = threadIdx.x; e < ntypes * ntypes; e += blockDim.x) {
+    const int ai = e / ntypes + 1, aj = e % ntypes + 1;
+    s_lj[e] = c_lj[vkey(ai, aj) - 1];
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  double acc[NACC];
+  // per-lane FP32 energy/virial/stress sums with compensation (no FP64 op in the loop)
+  float a[NACC], c[NACC];
 #pragma unroll
-  for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
+  for (int k = 0; k < NACC; ++k) { a[k] = 0.f; c[k] = 0.f; }
+  unsigned long long n_list = 0, n_rc = 0;
   for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < natms; i += nwarps) {
     const float4 pi = xf[i];
     const float qi = pi.w * scaling;
-    const int ai = ltype[i];
+    const int row = (ltype[i] - 1) * ntypes - 1;
     const int s = fstart[i], n = fcount[i];
     long long sx = 0, sy = 0, sz = 0;
-    float a[NACC];
+    float t[NACC];
 #pragma unroll
-    for (int k = 0; k < NACC; ++k) a[k] = 0.f;
-    int nrc = 0;
+    for (int k = 0; k < NACC; ++k) t[k] = 0.f;
     for (int m = lane; m < n; m += 32) {
       const int j = flist[s + m];
       const float4 pj = xf[j];
@@ -348,30 +358,34 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
         const float ec = pre * poly * ex * rinv;                       // q q erfc(ar)/r
         const float eg = fmaf(pre * alpha2rsqrpi, ex, ec) * r2i;        // (erfc/r + 2a/sqrt(pi) e^-x^2)/r^2
         gam += eg;
-        a[2] += ec;
-        a[3] = fmaf(-eg, rsq, a[3]);
+        t[2] += ec;
+        t[3] = fmaf(-eg, rsq, t[3]);
       }
       if (rsq < rv2) {
-        const int key = vkey(ai, ltype[j]) - 1;
-        if (vkind[key] != 0) {
+        const float4 lj = s_lj[row + ltype[j]];  // (4 eps, 24 eps, sigma^2, present)
+        if (lj.w != 0.f) {
           // 12-6 Lennard-Jones (two_body_potentials.F90:260-270)
-          const float4 lj = c_lj[key];  // (4 eps, 24 eps, sigma^2, -)
           const float s2 = lj.z * r2i;
           const float s6 = s2 * s2 * s2;
-          const float e = lj.x * s6 * (s6 - 1.0f);
           const float gv = lj.y * s6 * fmaf(2.0f, s6, -1.0f) * r2i;
           gam += gv;
-          a[0] += e;
-          a[1] = fmaf(-gv, rsq, a[1]);
+          t[0] = fmaf(lj.x * s6, s6 - 1.0f, t[0]);
+          t[1] = fmaf(-gv, rsq, t[1]);
         }
       }
-      ++nrc;
+      ++n_rc;
       const float fx_ = gam * dx, fy_ = gam * dy, fz_ = gam * dz;
       sx += fix40(fx_);
       sy += fix40(fy_);
       sz += fix40(fz_);
-      a[4] = fmaf(dx, fx_, a[4]); a[5] = fmaf(dx, fy_, a[5]); a[6] = fmaf(dx, fz_, a[6]);
-      a[7] = fmaf(dy, fy_, a[7]); a[8] = fmaf(dy, fz_, a[8]); a[9] = fmaf(dz, fz_, a[9]);
+      t[4] = fmaf(dx, fx_, t[4]); t[5] = fmaf(dx, fy_, t[5]); t[6] = fmaf(dx, fz_, t[6]);
+      t[7] = fmaf(dy, fy_, t[7]); t[8] = fmaf(dy, fz_, t[8]); t[9] = fmaf(dz, fz_, t[9]);
+    }
+#pragma unroll
+    for (int k = 0; k < NACC; ++k) {  // compensated add of this atom's share
+      const float y = t[k] - c[k], tt = a[k] + y;
+      c[k] = (tt - a[k]) - y;
+      a[k] = tt;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -379,19 +393,21 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
       sy += __shfl_xor_sync(0xffffffffu, sy, o);
       sz += __shfl_xor_sync(0xffffffffu, sz, o);
     }
-#pragma unroll
-    for (int k = 0; k < NACC; ++k) a[k] = warp_sumf(a[k]);
-    nrc = warp_sumi(nrc);
     if (lane == 0) {
       atomicAdd(&fixp[3 * i + 0], (unsigned long long)sx);
       atomicAdd(&fixp[3 * i + 1], (unsigned long long)sy);
       atomicAdd(&fixp[3 * i + 2], (unsigned long long)sz);
-      atomicAdd(&cnt[0], (unsigned long long)n);
-      atomicAdd(&cnt[1], (unsigned long long)nrc);
-      // FP64 reduction of the per-atom sums (x0.5: every pair appears twice)
-#pragma unroll
-      for (int k = 0; k < NACC; ++k) acc[k] += 0.5 * (double)a[k];
+      n_list += (unsigned long long)n;
     }
+  }
+  // FP64 only here, once per thread: x0.5 because every pair appears twice
+  double acc[NACC];
+#pragma unroll
+  for (int k = 0; k < NACC; ++k) acc[k] = 0.5 * ((double)a[k] - (double)c[k]);
+  n_rc = (unsigned long long)warp_sumi((int)n_rc);
+  if (lane == 0) {
+    atomicAdd(&cnt[0], n_list);
+    atomicAdd(&cnt[1], n_rc);
   }
   block_reduce_store<NACC>(acc, blk);
 }
@@ -403,12 +419,13 @@ inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
 // ===================================================================== host
 // per-key LJ constants for the mixed form (4 eps, 24 eps, sigma^2)
 void pair_setup() {
-  if (g.nkey > MAX_KEYS) throw (int)GB_ERR_ARG;
+  if (g.nkey > MAX_KEYS || g.p.ntypes > MAX_TYPES) throw (int)GB_ERR_ARG;
   float4 lj[MAX_KEYS];
   for (int k = 0; k < MAX_KEYS; ++k) lj[k] = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int k = 0; k < g.nkey; ++k) {
     const double e = g.h_vdw_eps[k], s = g.h_vdw_sig[k];
-    lj[k] = make_float4((float)(4.0 * e), (float)(24.0 * e), (float)(s * s), 0.f);
+    const float present = g.h_vdw_kind[k] != 0 ? 1.f : 0.f;
+    lj[k] = make_float4((float)(4.0 * e), (float)(24.0 * e), (float)(s * s), present);
   }
   GB_CUDA(cudaMemcpyToSymbol(c_lj, lj, sizeof(lj)));
 }
@@ -473,7 +490,7 @@ void pair_forces(double* eng6, double* stress9) {
     double* blk = gb_blkacc(nb * NACC + nb2 * 8);
     prof_begin(P_PAIR);
     const double a2rp = g.p.alpha * 2.0 / std::sqrt(3.14159265358979323846264338327950288);
-    k_pair_mixed<<<nb, T, 0, st>>>(g.natms, g.fstart, g.fcount, g.flist, g.xf, g.ltype, g.vdw_kind, (float)pg.rc2,
+    k_pair_mixed<<<nb, T, 0, st>>>(g.natms, g.fstart, g.fcount, g.flist, g.xf, g.ltype, g.p.ntypes, (float)pg.rc2,
                                    (float)pg.rv2, (float)g.p.alpha, (float)a2rp, (float)pg.scaling,
                                    (unsigned long long*)g.fixp, blk, &g.sc->npairs_list);
     GB_LAUNCHED();

@@ -186,7 +186,7 @@ struct SpmeGeom {
 template <typename T>
 __global__ void k_spme_prep(int natms, const double* __restrict__ x, const double* __restrict__ y,
                             const double* __restrict__ z, const double* __restrict__ q, SpmeGeom sg, T* spl,
-                            int* nidx, int* brick_of, int* brick_count) {
+                            int* nidx, int* brick_of, int* brick_count, int* gidx, float* gw) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natms) return;
   const int p = sg.p;
@@ -196,6 +196,14 @@ __global__ void k_spme_prep(int natms, const double* __restrict__ x, const doubl
     double fl = floor(u);
     int n = (int)fl;
     T w = (T)(u - fl);
+    if (gidx) {
+      // the gather's own convention: Int(u), u - Aint(u) (ewald_spole.F90:387, bspline.F90:216)
+      const double tr = trunc(u);
+      int g0 = ((int)tr - p + 1) % sg.K[d];
+      if (g0 < 0) g0 += sg.K[d];
+      gidx[3 * i + d] = g0;
+      gw[3 * i + d] = (float)(u - tr);
+    }
     T m[PMAX];
     bspline_vals<T>(w, p, m, nullptr);
     for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t];
@@ -295,11 +303,12 @@ __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, 
 // concurrently with 64-bit integer shared-memory atomics on a 2^-40 fixed-point
 // tile (no barrier per atom; integer sums are order independent, so the grid
 // is bit-reproducible).  The tile goes to `ext` as int64.
+template <int P>  // spline order known at compile time (0: taken from sg.p)
 __global__ void k_spme_spread_fix(SpmeGeom sg, const int* __restrict__ bstart, const int* __restrict__ batoms,
                                   const float* __restrict__ spl, const int* __restrict__ nidx,
                                   const double* __restrict__ q, long long* __restrict__ ext) {
   extern __shared__ unsigned char smem_raw[];
-  const int p = sg.p;
+  const int p = P ? P : sg.p;
   const int b = blockIdx.x;
   const int bx = b % sg.nb[0], by = (b / sg.nb[0]) % sg.nb[1], bz = b / (sg.nb[0] * sg.nb[1]);
   const int g0x = bx * sg.B[0], g0y = by * sg.B[1], g0z = bz * sg.B[2];
@@ -477,7 +486,7 @@ __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan
   T* rzt = reinterpret_cast<T*>(b + TX * pl.N);
   for (int zz = threadIdx.x; zz < K3; zz += blockDim.x) {
     int ll = zz; if (2 * ll > K3) ll -= K3;
-    rzt[zz] = (T)((double)ll * sg.rc[8]);
+    rzt[zz] = (T)ll * (T)sg.rc[8];
   }
   T2* r = fft_lines<T, T2, +1>(a, b, pl, TX, tw);
   // Reciprocal stress sum_m m_a m_b psi |Q(m)|^2 (ewald_spole.F90:1362-1371): with
@@ -506,13 +515,14 @@ __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan
       rl[zz] = v;
     }
   }
-  double st[6] = {0, 0, 0, 0, 0, 0};
+  // in the working precision T: the FP32 form issues no FP64 instruction here
+  T st[6] = {0, 0, 0, 0, 0, 0};
   if (t < TX) {
     int jj = x0 + t; if (2 * jj > K1) jj -= K1;
     int kk = yy; if (2 * kk > K2) kk -= K2;
-    const double rx = (double)jj * sg.rc[0], ry = (double)kk * sg.rc[4];
-    st[0] = rx * rx * (double)A; st[1] = rx * ry * (double)A; st[2] = rx * (double)B;
-    st[3] = ry * ry * (double)A; st[4] = ry * (double)B; st[5] = (double)C;
+    const T rx = (T)jj * (T)sg.rc[0], ry = (T)kk * (T)sg.rc[4];
+    st[0] = rx * rx * A; st[1] = rx * ry * A; st[2] = rx * B;
+    st[3] = ry * ry * A; st[4] = ry * B; st[5] = C;
   }
   T2* o = (r == a) ? b : a;
   T2* r2 = fft_lines<T, T2, -1>(r, o, pl, TX, tw);
@@ -586,6 +596,74 @@ __global__ void k_spme_gather(int natms, const double* __restrict__ x, const dou
   block_reduce_store<4>(acc, blk);
 }
 
+// FP32 gather, one warp per atom.  Lane (j, k) = (lane & 7, lane >> 3) and
+// (j, k + 4) cover the p x p (x,y) rows for p = 8, so each warp load reads four
+// 8-wide rows (coalesced); lanes 0..2 build the splines of one dimension each
+// from the stored truncation-convention fraction.  No FP64 instruction.
+__global__ void __launch_bounds__(256) k_spme_gather_f32(int natms, const float* __restrict__ q4, SpmeGeom sg,
+                                                         const int* __restrict__ gidx, const float* __restrict__ gw,
+                                                         const float* __restrict__ phi, float rk0, float rk1,
+                                                         float rk2, float* __restrict__ fout, double* blk) {
+  constexpr int P = 8;
+  __shared__ float sp[8][2][3][P];  // per warp: value/derivative, dimension, point
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
+  const int j = lane & 7, k0 = lane >> 3;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < natms; i += nwarps) {
+    const float qi = q4[4 * i + 3];
+    if (lane < 3) {
+      float m[PMAX], dm[PMAX];
+      bspline_vals<float>(gw[3 * i + lane], P, m, dm);
+      for (int t = 0; t < P; ++t) { sp[wid][0][lane][t] = m[t]; sp[wid][1][lane][t] = dm[t]; }
+    }
+    __syncwarp();
+    const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
+    int xx = gx + j; if (xx >= K0) xx -= K0;
+    int ya = gy + k0; if (ya >= K1) ya -= K1;
+    int yb = gy + k0 + 4; if (yb >= K1) yb -= K1;
+    const float mx = sp[wid][0][0][j], dmx = sp[wid][1][0][j];
+    const float mya = sp[wid][0][1][k0], dmya = sp[wid][1][1][k0];
+    const float myb = sp[wid][0][1][k0 + 4], dmyb = sp[wid][1][1][k0 + 4];
+    const float p0a = mx * mya, p1a = dmx * mya, p2a = mx * dmya;
+    const float p0b = mx * myb, p1b = dmx * myb, p2b = mx * dmyb;
+    float e = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+    for (int l = 0; l < P; ++l) {
+      int zz = gz + l; if (zz >= K2) zz -= K2;
+      const float* plane = phi + (size_t)zz * K1 * K0;
+      const float pa = plane[(size_t)ya * K0 + xx], pb = plane[(size_t)yb * K0 + xx];
+      const float mz = sp[wid][0][2][l], dmz = sp[wid][1][2][l];
+      const float ta = mz * pa, tb = mz * pb, ua = dmz * pa, ub = dmz * pb;
+      e = fmaf(p0a, ta, fmaf(p0b, tb, e));
+      fx = fmaf(p1a, ta, fmaf(p1b, tb, fx));
+      fy = fmaf(p2a, ta, fmaf(p2b, tb, fy));
+      fz = fmaf(p0a, ua, fmaf(p0b, ub, fz));
+    }
+    e = warp_sumf(e); fx = warp_sumf(fx); fy = warp_sumf(fy); fz = warp_sumf(fz);
+    const float f0 = -qi * fx * rk0, f1 = -qi * fy * rk1, f2 = -qi * fz * rk2;
+    if (lane == 0) {
+      fout[3 * i] = f0; fout[3 * i + 1] = f1; fout[3 * i + 2] = f2;
+      acc[0] += qi * e; acc[1] += f0; acc[2] += f1; acc[3] += f2;
+    }
+    __syncwarp();
+  }
+  block_reduce_store<4>(acc, blk);
+}
+
+// mixed form: forces += (F - Fnet/N) * 2 * scale as 2^40 fixed point (FP32 math)
+__global__ void k_spme_apply_fix_f32(int natms, const float* __restrict__ f, const double* __restrict__ sums,
+                                     float scale2, float rn, unsigned long long* fixp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natms) return;
+  // the three net-force means are read as FP64 and converted once per thread
+  const float m0 = (float)sums[1] * rn, m1 = (float)sums[2] * rn, m2 = (float)sums[3] * rn;
+  atomicAdd(&fixp[3 * i + 0], (unsigned long long)fix40((f[3 * i] - m0) * scale2));
+  atomicAdd(&fixp[3 * i + 1], (unsigned long long)fix40((f[3 * i + 1] - m1) * scale2));
+  atomicAdd(&fixp[3 * i + 2], (unsigned long long)fix40((f[3 * i + 2] - m2) * scale2));
+}
+
 // forces += (F - Fnet/N) * 2 * scale
 __global__ void k_spme_apply(int natms, const double* __restrict__ f, const double* __restrict__ sums, double scale2,
                              double rn, double* fx, double* fy, double* fz) {
@@ -631,6 +709,9 @@ FftPlan make_plan(int N) {
 FftPlan plan1, plan2, plan3;
 SpmeGeom h_sg;
 void* g_spread_ext = nullptr;  // per-brick spread tiles (nbricks x (B+p-1)^3)
+int* g_gidx = nullptr;         // mixed gather: first grid index per dimension (truncation convention)
+float* g_gw = nullptr;         // mixed gather: fractional coordinate per dimension
+float* g_fout_f = nullptr;     // mixed gather: unscaled reciprocal forces
 
 int choose_brick(int K, int p) {
   for (int B = p - 1; B <= BMAX; ++B)
@@ -685,6 +766,10 @@ void spme_setup() {
   GB_CUDA(cudaMalloc(&g.theta, sizeof(double) * NG));
   GB_CUDA(cudaMalloc(&g.psi, sizeof(double) * NG));
   GB_CUDA(cudaMalloc(&g.fspme, sizeof(double) * 3 * (size_t)g.natms));
+  if (g_gidx) { cudaFree(g_gidx); cudaFree(g_gw); cudaFree(g_fout_f); }
+  GB_CUDA(cudaMalloc(&g_gidx, sizeof(int) * 3 * (size_t)g.natms));
+  GB_CUDA(cudaMalloc(&g_gw, sizeof(float) * 3 * (size_t)g.natms));
+  GB_CUDA(cudaMalloc(&g_fout_f, sizeof(float) * 3 * (size_t)g.natms));
   {
     const size_t tsize = (size_t)(g.B1 + p - 1) * (g.B2 + p - 1) * (g.B3 + p - 1);
     if (g_spread_ext) cudaFree(g_spread_ext);
@@ -693,7 +778,9 @@ void spme_setup() {
     const int sm32 = (int)spread_smem(g.B1, g.B2, g.B3, p, sizeof(float));
     GB_CUDA(cudaFuncSetAttribute(k_spme_spread_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64));
     GB_CUDA(cudaFuncSetAttribute(k_spme_spread_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
-    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_fix, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_fix<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(tsize * sizeof(long long))));
+    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_fix<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(tsize * sizeof(long long))));
   }
   // |b(m)|^2 (bspline_coeffs_gen, bspline.F90:73-190) on the host in FP64
@@ -824,8 +911,10 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
   GB_CUDA(cudaMemsetAsync(g.brick_count, 0, sizeof(int) * (g.nbricks + 2), st));
   GB_CUDA(cudaMemsetAsync(g.brick_fill, 0, sizeof(int) * (g.nbricks + 2), st));
   prof_begin(P_SPME_PREP);
+  const bool warp_gather = !std::is_same<T, double>::value && p == 8;
   k_spme_prep<T><<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, h_sg, spl, g.nidx, g.brick_of,
-                                                   g.brick_count);
+                                                   g.brick_count, warp_gather ? g_gidx : nullptr,
+                                                   warp_gather ? g_gw : nullptr);
   GB_LAUNCHED();
 
   scan_exclusive(g.brick_count, g.brick_start, g.nbricks + 1);
@@ -850,8 +939,12 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
     } else {
       long long* exti = reinterpret_cast<long long*>(g_spread_ext);
       const size_t tsz = (size_t)(g.B1 + p - 1) * (g.B2 + p - 1) * (g.B3 + p - 1);
-      k_spme_spread_fix<<<g.nbricks, 256, tsz * sizeof(long long), st>>>(
-          h_sg, g.brick_start, g.brick_atoms, reinterpret_cast<const float*>(spl), g.nidx, g.chge, exti);
+      if (p == 8)
+        k_spme_spread_fix<8><<<g.nbricks, 256, tsz * sizeof(long long), st>>>(
+            h_sg, g.brick_start, g.brick_atoms, reinterpret_cast<const float*>(spl), g.nidx, g.chge, exti);
+      else
+        k_spme_spread_fix<0><<<g.nbricks, 256, tsz * sizeof(long long), st>>>(
+            h_sg, g.brick_start, g.brick_atoms, reinterpret_cast<const float*>(spl), g.nidx, g.chge, exti);
       GB_LAUNCHED();
       k_spme_tile_reduce_fix<<<nblocks((long long)NG, 256), 256, 0, st>>>(h_sg, exti, reinterpret_cast<float*>(Q));
       GB_LAUNCHED();
@@ -889,10 +982,18 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
   for (int k = 0; k < 9; ++k) rc[k] = h_sg.rc[k];
   double rk[3];
   for (int a = 0; a < 3; ++a) rk[a] = rc[a] * h_sg.Kr[0] + rc[a + 3] * h_sg.Kr[1] + rc[a + 6] * h_sg.Kr[2];
-  const int nbg = nblocks(n, 128);
+  static int occ_g = 0;
+  if (!occ_g) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g, k_spme_gather_f32, 256, 0));
+  const int nbg = warp_gather ? std::max(1, std::min(occ_g * g.nsm, nblocks((long long)n * 32, 256))) : nblocks(n, 128);
   double* blkg = blkz + (size_t)nbz * 6;
   prof_begin(P_SPME_GATHER);
-  k_spme_gather<T><<<nbg, 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, h_sg, Q, rk[0], rk[1], rk[2], g.fspme, blkg);
+  if (warp_gather) {
+    k_spme_gather_f32<<<nbg, 256, 0, st>>>(n, reinterpret_cast<const float*>(g.xf), h_sg, g_gidx, g_gw,
+                                            reinterpret_cast<const float*>(Q), (float)rk[0], (float)rk[1],
+                                            (float)rk[2], g_fout_f, blkg);
+  } else {
+    k_spme_gather<T><<<nbg, 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, h_sg, Q, rk[0], rk[1], rk[2], g.fspme, blkg);
+  }
   GB_LAUNCHED();
   prof_end(P_SPME_GATHER);
   gb_reduce_blocks(blkz, nbz, 6, &g.sc->acc[A_SPME_STR]);
@@ -902,6 +1003,9 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
   if (g.precision == GB_FP64) {
     k_spme_apply<<<nblocks(n, 256), 256, 0, st>>>(n, g.fspme, &g.sc->acc[A_GATHER], 2.0 * scale, 1.0 / (double)n,
                                                    g.fx, g.fy, g.fz);
+  } else if (warp_gather) {
+    k_spme_apply_fix_f32<<<nblocks(n, 256), 256, 0, st>>>(n, g_fout_f, &g.sc->acc[A_GATHER], (float)(2.0 * scale),
+                                                           (float)(1.0 / (double)n), (unsigned long long*)g.fixp);
   } else {
     k_spme_apply_fix<<<nblocks(n, 256), 256, 0, st>>>(n, g.fspme, &g.sc->acc[A_GATHER], 2.0 * scale,
                                                        1.0 / (double)n, (unsigned long long*)g.fixp);
