@@ -7,12 +7,18 @@ SPME reciprocal forces (order-8 B-splines, 3-D FFT + influence function),
 real-space vdW + erfc-Coulomb pair forces, VV stage 2.
 
 Default workload (one GPU): the 262,144-ion NaCl-like melt (64^3 rock-salt
-sites, 180.48 A box, SPME grid 192^3, order 8, rc 12 A, skin 1 A), plain FP64,
-seeded synthetic start at 1500 K.  `--form mixed` runs the FP32/fixed-point
-form of the same workload.  The working set (Verlet list ~0.8 GB, grids
-~0.5 GB) exceeds the 129 MB L2, so no flush is needed between steps.
+sites, 180.48 A box, SPME grid 192^3, order 8, rc 12 A, skin 1 A), seeded
+synthetic start at 1500 K.  The headline `value` is the plain FP64 form; the
+line's "forms" object holds every form of the same workload measured the same
+way: "mixed" (FP32 arithmetic, 2^40 fixed-point forces) with its RMS and max
+force error against FP64 at the same positions, and "mts_k4" / "mts_k8" (the
+learned multiple-time-step form on the mixed path, network trained online for
+--mts-train steps before timing, fallback bound 1e-4) with the errors its
+checks measured.  The working set (Verlet list ~0.8 GB, grids ~0.5 GB)
+exceeds the 129 MB L2, so no flush is needed between steps.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference] [--form fp64|mixed]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference]
+                    [--form fp64|mixed|mts_k4|mts_k8] [--no-compare]
 
 N > 1 (torchrun, one rank per GPU) runs N independent replicas: the path does
 not shard (one GPU per DL_POLY rank); value = total atom-steps / max rank time.
@@ -215,11 +221,91 @@ def run_reference(args, dist):
 
 
 # ----------------------------------------------------------------- GPU arm
+FORMS = {"fp64": (0, 1), "mixed": (1, 1), "mts_k4": (1, 4), "mts_k8": (1, 8)}
+MTS_TOL = 1e-4
+
+
+def force_error(lib, L):
+    """RMS and max |F_mixed - F_fp64| / RMS|F_fp64| at the current positions."""
+    L.gb_set_precision.argtypes = [ctypes.c_int]
+    lib.two_body_forces()
+    a = lib.download()
+    L.gb_set_precision(0)
+    lib.two_body_forces()
+    b = lib.download()
+    L.gb_set_precision(1)
+    Fa = np.stack([a["fx"], a["fy"], a["fz"]], 1)
+    Fb = np.stack([b["fx"], b["fy"], b["fz"]], 1)
+    rms = np.sqrt((Fb ** 2).sum(1).mean())
+    return float(np.sqrt(((Fa - Fb) ** 2).sum(1).mean()) / rms), float(np.abs(Fa - Fb).max() / rms)
+
+
+def measure(lib, L, s, form, args, dist, device, steps, detail):
+    """Initialise, warm up (and train the MTS network), then time `steps` MD steps."""
+    precision, k = FORMS[form]
+    lib.init(s, precision=precision, device=device)
+    lib.start()
+    train = 0
+    t_train = 0.0
+    if k > 1:
+        train = args.mts_train
+        lib.mts_config(k, MTS_TOL, train)
+        steps = k * max(1, -(-steps // k))  # whole MTS cycles
+        t0 = time.perf_counter()
+        lib.md_vv(train)
+        t_train = time.perf_counter() - t0
+    lib.md_vv(max(3, args.warmup))
+    # ---- timed region: K resident MD steps (kernels timed with CUDA events)
+    L.gb_profile(1)
+    clocks = Clocks(device) if detail else None
+    dist.barrier()
+    l0 = L.gb_kernel_launches()
+    w0 = time.perf_counter()
+    stats = lib.md_vv(steps)
+    w1 = time.perf_counter()
+    l1 = L.gb_kernel_launches()
+    tm = (ctypes.c_double * 8)()
+    L.gb_last_timings(tm, 8)
+    span_s = tm[5] * 1e-3
+    dist.barrier()
+    clk = clocks.stop() if clocks else None
+    names = ctypes.create_string_buffer(32 * 32)
+    ms = (ctypes.c_double * 32)()
+    nl = (ctypes.c_int64 * 32)()
+    nk = L.gb_profile_read(names, ms, nl, 32)
+    L.gb_profile(0)
+    prof = {}
+    for j in range(nk):
+        nm = names.raw[32 * j:32 * (j + 1)].split(b"\0")[0].decode()
+        if nl[j]:
+            prof[nm] = (ms[j], int(nl[j]))
+    cnt = (ctypes.c_int64 * 3)()
+    L.gb_pair_counts(cnt, 3)
+    P_list, P_rc = int(cnt[0]), int(cnt[1])
+    if precision == 1:
+        P_list //= 2
+        P_rc //= 2
+    tmax = dist.max(span_s)
+    out = {"value": dist.world * s.natms * steps / tmax, "ms_per_step": tmax * 1e3 / steps,
+           "ns_per_day": (steps / tmax) * DT_PS * 86400 / 1000, "steps": steps,
+           "list_rebuilds": sum(x.list_rebuilt for x in stats)}
+    if precision == 1 and k == 1:
+        out["force_err_rms"], out["force_err_max"] = force_error(lib, L)
+    if k > 1:
+        m = lib.mts_stats()
+        out["mts"] = {"k": k, "tol": MTS_TOL, "train_steps": train, "train_wall_s": t_train,
+                      "full_spme_steps_timed": sum(x.mts_full for x in stats), "coarse_grid": int(m["coarse_k"]),
+                      "checked_err_last": m["last_err"], "checked_err_max": m["err_max"],
+                      "err_without_network": m["err_no_network"], "err_stale_force": m["err_stale"],
+                      "fallback_entries": int(m["n_fallback"]), "in_fallback": bool(m["in_fallback"])}
+    return out, dict(stats=stats, prof=prof, P=(P_list, P_rc), launches=l1 - l0, clk=clk, wall=w1 - w0, tmax=tmax)
+
+
 def run_gb(args, dist):
     import dlpoly_gb300 as gb
 
     s, desc = workload(args.workload)
-    precision = 0 if args.form == "fp64" else 1
+    precision = FORMS[args.form][0]
     lib = gb.load()
     L = lib.lib
     L.gb_profile.argtypes = [ctypes.c_int]
@@ -228,42 +314,19 @@ def run_gb(args, dist):
     L.gb_pair_counts.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]
     L.gb_fp64_peak_tflops.restype = ctypes.c_double
     device = dist.local
-    lib.init(s, precision=precision, device=device)
-    lib.start()
-    lib.md_vv(max(3, args.warmup))
-    # ---- timed region: K resident MD steps (kernels timed with CUDA events)
-    L.gb_profile(1)
-    clocks = Clocks(device)
-    dist.barrier()
-    l0 = L.gb_kernel_launches()
-    w0 = time.perf_counter()
-    stats = lib.md_vv(args.steps)
-    w1 = time.perf_counter()
-    l1 = L.gb_kernel_launches()
-    tm = (ctypes.c_double * 8)()
-    L.gb_last_timings(tm, 8)
-    span_s = tm[5] * 1e-3
-    dist.barrier()
-    clk = clocks.stop()
-    names = ctypes.create_string_buffer(32 * 32)
-    ms = (ctypes.c_double * 32)()
-    nl = (ctypes.c_int64 * 32)()
-    nk = L.gb_profile_read(names, ms, nl, 32)
-    L.gb_profile(0)
-    prof = {}
-    for k in range(nk):
-        nm = names.raw[32 * k:32 * (k + 1)].split(b"\0")[0].decode()
-        if nl[k]:
-            prof[nm] = (ms[k], int(nl[k]))
-    cnt = (ctypes.c_int64 * 3)()
-    L.gb_pair_counts(cnt, 3)
-    P_list, P_rc = int(cnt[0]), int(cnt[1])
-    if precision == 1:
-        P_list //= 2
-        P_rc //= 2
-    tmax = dist.max(span_s)
-    value = dist.world * s.natms * args.steps / tmax
-    rebuilds = sum(x.list_rebuilt for x in stats)
+    # the other forms of the same workload, each measured the same way
+    forms = {}
+    if args.compare:
+        for f in FORMS:
+            if f != args.form:
+                forms[f], _ = measure(lib, L, s, f, args, dist, device, args.steps, detail=False)
+    head, det = measure(lib, L, s, args.form, args, dist, device, args.steps, detail=True)
+    forms[args.form] = head
+    stats, prof, (P_list, P_rc), clk, tmax = det["stats"], det["prof"], det["P"], det["clk"], det["tmax"]
+    l0, l1, w0, w1 = 0, det["launches"], 0.0, det["wall"]
+    steps = head["steps"]
+    value = head["value"]
+    rebuilds = head["list_rebuilds"]
     # ---- end to end through the C-ABI with host buffers (H2D state, D2H state + forces)
     ke = max(1, min(args.steps, 10))
     try:
@@ -337,10 +400,10 @@ def run_gb(args, dist):
         "value": value,
         "unit": "atom-steps/s",
         "n_gpus": dist.world,
-        "steps": args.steps,
+        "steps": steps,
         "warmup": max(3, args.warmup),
-        "ms_per_step": tmax * 1e3 / args.steps,
-        "ns_per_day": (args.steps / tmax) * DT_PS * 86400 / 1000,
+        "ms_per_step": tmax * 1e3 / steps,
+        "ns_per_day": (steps / tmax) * DT_PS * 86400 / 1000,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -349,6 +412,7 @@ def run_gb(args, dist):
         "config": {"workload": desc, "form": args.form, "natms": s.natms, "dt_fs": 2.0,
                    "list_rebuilds_in_timed_steps": rebuilds, "parallelism": "replicas" if dist.world > 1 else "single",
                    "l2": "working set > 129 MB L2 (list ~%.0f MB), no flush" % (4.0 * P_list / 1e6)},
+        "forms": forms,
         "e2e": e2e,
         "gpu_launches": int(l1 - l0),
         "clocks": clk,
@@ -367,8 +431,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--form", default="fp64", choices=list(FORMS))
     ap.add_argument("--workload", default="nacl_262144", choices=["nacl_262144", "nacl_4096", "water_98304"])
+    ap.add_argument("--mts-train", type=int, default=200,
+                    help="MD steps of online training (SPME every step) before the learned-MTS forms are timed")
+    ap.add_argument("--no-compare", dest="compare", action="store_false",
+                    help="time only --form (default: every form of the workload, --form is the headline)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     dist = Dist()

@@ -79,16 +79,16 @@ void dalloc(T** p, size_t n) {
 }
 
 void free_all() {
-  void* ptrs[] = {g.x, g.y, g.z, g.xf, g.fx, g.fy, g.fz, g.fixp, g.vx, g.vy, g.vz, g.chge, g.weight, g.ltype, g.ltg,
+  void* ptrs[] = {g.x, g.y, g.z, g.xf, g.xlo, g.fx, g.fy, g.fz, g.fixp, g.vx, g.vy, g.vz, g.chge, g.weight, g.ltype, g.ltg,
                   g.lfrzn, g.ixyz, g.src, g.shcode, g.xbg, g.ybg, g.zbg, g.ox, g.oy, g.oz, g.which_cell,
                   g.cell_count, g.cell_start, g.cell_fill, g.at_list, g.sorted_pos, g.xs, g.xsf, g.list, g.blk,
                   g.list_excl, g.flist, g.fcount, g.fstart, g.erfc_coef, g.erfc_coef_f, g.vdw_coef, g.vdw_coef_f,
-                  g.vdw_kind, g.vdw_eps, g.vdw_sig, g.spl, g.nidx, g.brick_of, g.brick_count, g.brick_start,
-                  g.brick_fill, g.brick_atoms, g.Q, g.G, g.Qf, g.Gf, g.theta, g.psi, g.theta_f, g.psi_f, g.tw1, g.tw2,
-                  g.tw3, g.tw1f, g.tw2f, g.tw3f, g.fspme, g.blkacc, g.con_i, g.con_j, g.con_d0, g.dxx, g.dyy,
+                  g.vdw_kind, g.vdw_eps, g.vdw_sig, g.blkacc, g.con_i, g.con_j, g.con_d0, g.dxx, g.dyy,
                   g.dzz, g.dxt, g.dyt, g.dzt, g.dt2, g.gam, g.listot, g.acon_start, g.acon_list, g.sc, d_scratch};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  mts_free();
+  spme_free();
   if (g.hsc) cudaFreeHost(g.hsc);
   if (g.stream) {
     for (int k = 0; k < 8; ++k) cudaEventDestroy(g.ev[k]);
@@ -188,16 +188,25 @@ int guarded(F&& f) {
 }
 
 // forces for the current positions: SPME then the pair loop (drivers.F90:655-786)
-int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real) {
-
+// md_step: the evaluation belongs to an MD step, where the learned-MTS form
+// (when configured) may replace SPME by the surrogate; *full_out tells which ran.
+int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real, bool md_step = false,
+                   bool* full_out = nullptr) {
   double st[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double strec[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   double erc = 0, vrc = 0;
   double e6[6] = {0, 0, 0, 0, 0, 0};
   integ_zero_forces();
   if (g.precision == GB_MIXED) list_pos_f32();
-  if (do_spme) spme_forces(&erc, &vrc, st);
+  const bool mts = md_step && do_spme && mts_active();
+  const bool full = mts ? mts_step_needs_spme() : do_spme;
+  if (full) spme_forces(&erc, &vrc, strec);
+  else if (mts) mts_inner(&erc, &vrc, strec);
+  for (int k = 0; k < 9; ++k) st[k] += strec[k];
   if (do_real) pair_forces(e6, st);
   if (g.precision == GB_MIXED) integ_forces_to_fp64();
+  if (mts && full) mts_after_full(erc, vrc, strec);
+  if (full_out) *full_out = full;
   if (eng8) {
     eng8[0] = erc; eng8[1] = vrc;
     eng8[2] = e6[0]; eng8[3] = e6[1]; eng8[4] = e6[2]; eng8[5] = e6[3]; eng8[6] = e6[4]; eng8[7] = e6[5];
@@ -261,7 +270,8 @@ void invert_host(const double* a, double* b, double* d) {
 static const char* kProfNames[P_NPROF] = {"halo",        "bin_sort",   "list_pairs", "full_list",  "pair_forces",
                                           "excl_forces", "spme_prep",  "spme_spread", "fft_x_fwd", "fft_y",
                                           "fft_z_conv",  "fft_x_inv",  "spme_gather", "vv",        "shake",
-                                          "rattle",      "mlp"};
+                                          "rattle",      "mlp_infer",  "mts_inputs", "mlp_train",  "coarse_prep",
+                                          "coarse_spread", "coarse_fft", "coarse_gather"};
 
 static int prof_event() {
   if (g.ev_used >= (int)g.evpool.size()) {
@@ -387,6 +397,7 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     const int mx = g.mxatms;
     dalloc(&g.x, mx); dalloc(&g.y, mx); dalloc(&g.z, mx);
     dalloc(&g.xf, mx);
+    dalloc(&g.xlo, mx);
     dalloc(&g.fx, natms); dalloc(&g.fy, natms); dalloc(&g.fz, natms);
     dalloc(&g.fixp, 3 * (size_t)natms);
     dalloc(&g.vx, natms); dalloc(&g.vy, natms); dalloc(&g.vz, natms);
@@ -431,6 +442,7 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     g.self_interaction = -sq2 * (g.scaling * prm->alpha * (1.0 / 1.7724538509055161040) / 1.0);  // spme.F90:159-231
     g.ntcons = ntcons;
     if (ntcons > 0) integ_setup_constraints(listcon, prmcon);
+    mts_set_topology(ntcons, listcon, weight);
     list_setup();
     spme_setup();
     g.init = true;
@@ -623,14 +635,15 @@ int gb_md_run(int nsteps, gb_step_stats* stats) {
       }
       GB_CUDA(cudaEventRecord(g.ev[2], g.stream));
       double e8[8], s9[9];
-      compute_forces(e8, s9, true, true);
+      bool full = true;
+      compute_forces(e8, s9, true, true, true, &full);
       GB_CUDA(cudaEventRecord(g.ev[3], g.stream));
       S.engcpe_rc = e8[0]; S.vircpe_rc = e8[1]; S.engcpe_rl = e8[2]; S.vircpe_rl = e8[3];
       S.engcpe_ex = e8[4]; S.vircpe_ex = e8[5]; S.engvdw = e8[6]; S.virvdw = e8[7];
       for (int k = 0; k < 9; ++k) S.stress[k] = s9[k];
       integ_vv(2, S.strkin, &S.engke, &it, nullptr, nullptr);
       S.rattle_iters = it;
-      S.mts_full = 1;
+      S.mts_full = full ? 1 : 0;
       GB_CUDA(cudaEventRecord(g.ev[4], g.stream));
       GB_CUDA(cudaEventSynchronize(g.ev[4]));
       float ms;
@@ -653,10 +666,14 @@ int gb_md_run(int nsteps, gb_step_stats* stats) {
 
 int gb_mts_config(int k, double tol, int train_steps) {
   return guarded([&]() {
-    if (k < 1) return (int)GB_ERR_ARG;
+    if (!g.init) return (int)GB_ERR_NOT_INIT;
+    if (k < 1 || !(tol > 0.0) || train_steps < 0) return (int)GB_ERR_ARG;
+    if (k > 1 && g.precision != GB_MIXED) return (int)GB_ERR_ARG;  // the surrogate feeds the fixed-point forces
     g.mts_k = k;
     g.mts_tol = tol;
     g.mts_train = train_steps;
+    if (k > 1) mts_setup();
+    else mts_free();
     return (int)GB_OK;
   });
 }
@@ -665,6 +682,10 @@ int gb_set_precision(int precision) {
   return guarded([&]() {
     if (precision != GB_FP64 && precision != GB_MIXED) return (int)GB_ERR_ARG;
     bool was = g.precision;
+    if (precision != GB_MIXED && mts_active()) {  // the learned form runs on the mixed path only
+      mts_free();
+      g.mts_k = 1;
+    }
     g.precision = precision;
     if (precision == GB_MIXED && was != GB_MIXED) list_full_build();
     return (int)GB_OK;
@@ -678,6 +699,36 @@ int gb_last_timings(double* ms, int n) {
 }
 
 int64_t gb_kernel_launches(void) { return g.launches; }
+
+int gb_mts_stats(double* out, int n) {
+  if (!out || n < 0) return GB_ERR_ARG;
+  mts_stats(out, n);
+  return GB_OK;
+}
+
+int gb_mts_features(float* x, int n, float* scales) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  return guarded([&]() { return mts_features(x, n, scales); });
+}
+
+int gb_mlp_param_count(void) { return mlp_param_count(); }
+
+int gb_mts_ablation(int stale_only) {
+  if (stale_only != 0 && stale_only != 1) return GB_ERR_ARG;
+  mts_set_stale_only(stale_only == 1);
+  return GB_OK;
+}
+
+int gb_mlp_train_eval(int nb, const float* x, const float* target, const float* params, float* loss, float* grad,
+                      float* y) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  return guarded([&]() { return mlp_train_eval(nb, x, target, params, loss, grad, y); });
+}
+
+int gb_mlp_infer_eval(int nb, const float* x, const float* params, float* y) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  return guarded([&]() { return mlp_infer_eval(nb, x, params, y); });
+}
 
 int gb_profile(int enable) {
   return guarded([&]() {

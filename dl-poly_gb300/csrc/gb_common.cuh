@@ -55,7 +55,8 @@ enum {
 // Kernel regions timed with CUDA events when profiling is on.
 enum ProfId {
   P_HALO = 0, P_BIN, P_LIST, P_FULLLIST, P_PAIR, P_EXCL, P_SPME_PREP, P_SPME_SPREAD, P_FFT_XF, P_FFT_Y,
-  P_FFT_Z, P_FFT_XI, P_SPME_GATHER, P_VV, P_SHAKE, P_RATTLE, P_MLP, P_NPROF
+  P_FFT_Z, P_FFT_XI, P_SPME_GATHER, P_VV, P_SHAKE, P_RATTLE, P_MLP, P_MTS_DESC, P_MLP_TRAIN, P_COARSE_PREP,
+  P_COARSE_SPREAD, P_COARSE_FFT, P_COARSE_GATHER, P_NPROF
 };
 void prof_begin(int id);
 void prof_end(int id);
@@ -76,6 +77,7 @@ struct Dev {
   // atoms
   double *x = nullptr, *y = nullptr, *z = nullptr;  // mxatms
   float4* xf = nullptr;                             // FP32 copy (x,y,z,q) for prefilter / mixed
+  float4* xlo = nullptr;                            // x - (double)xf.x etc.: the FP32 remainders (mixed)
   double *fx = nullptr, *fy = nullptr, *fz = nullptr;  // natms, FP64 forces
   long long* fixp = nullptr;                        // 3*natms fixed-point forces (mixed)
   double *vx = nullptr, *vy = nullptr, *vz = nullptr;
@@ -109,6 +111,7 @@ struct Dev {
   int* fcount = nullptr;       // per atom count
   int* fstart = nullptr;       // per atom start
   long long flist_cap = 0;
+  long long list_gen = 0;      // incremented whenever the full list is rebuilt
 
   // tables
   int nsamples = 0, max_grid = 0, nkey = 0;
@@ -124,31 +127,9 @@ struct Dev {
   std::vector<double> h_vdw_eps, h_vdw_sig;
   double elrc = 0, vlrc = 0, self_interaction = 0, scaling = 0;
 
-  // SPME
-  int K1 = 0, K2 = 0, K3 = 0, B1 = 0, B2 = 0, B3 = 0, nb1 = 0, nb2 = 0, nb3 = 0, nbricks = 0;
-  double* spl = nullptr;       // natms * 3 * p spread splines (floor convention)
-  int* nidx = nullptr;         // natms * 3 grid indices
-  int* brick_of = nullptr;     // natms
-  int* brick_count = nullptr;  // nbricks+1
-  int* brick_start = nullptr;
-  int* brick_fill = nullptr;
-  int* brick_atoms = nullptr;  // natms sorted by brick
-  double* Q = nullptr;         // real charge grid K1*K2*K3
-  double2* G = nullptr;        // complex grid K1*K2*K3
-  float* Qf = nullptr;
-  float2* Gf = nullptr;
-  double* theta = nullptr;     // influence function (FP64, precomputed)
-  double* psi = nullptr;       // theta * (-2(1+f^2)/k^2) for the stress
-  float* theta_f = nullptr;
-  float* psi_f = nullptr;
-  double2* tw1 = nullptr;      // twiddles per dimension (K_d entries, e^{+2 pi i t/K})
-  double2* tw2 = nullptr;
-  double2* tw3 = nullptr;
-  float2 *tw1f = nullptr, *tw2f = nullptr, *tw3f = nullptr;
-  double* fspme = nullptr;     // 3*natms reciprocal forces (before scale, net removal)
+  // SPME grids live in gb_spme.cu (SpmeGrid); shared scratch here
   double* blkacc = nullptr;    // per-block partial accumulators
   int blkacc_n = 0;
-  double* ncombk = nullptr;
 
   // constraints
   int ntcons = 0;
@@ -301,10 +282,33 @@ void list_pos_f32();              // FP32 copy of positions and charges (mixed p
 void scan_exclusive(const int* in, int* out, int n);
 void pair_forces(double* eng6, double* stress9);  // gb_pair.cu (adds into forces)
 void pair_setup();                // gb_pair.cu: per-key constants
-void spme_setup();                // gb_spme.cu
+void spme_setup();                // gb_spme.cu: the main grid
 void spme_forces(double* eng_rc, double* vir_rc, double* stress9);  // adds into forces
+void spme_free();                 // both grids
+// coarse FP32 grid of the learned-MTS form: K per dimension and spline order p
+void spme_coarse_setup(const int* K, int p);
+bool spme_coarse_ready();
+// scaled per-atom reciprocal forces of the coarse grid into rec (3*natms
+// floats, net force removed); forces of the context are not touched
+void spme_coarse_forces(double* eng_rc, double* vir_rc, double* stress9, float* rec);
 void integ_vv(int stage, double* strkin, double* engke, int* iters, double* vircon, double* strcon);
 int integ_vnl_check();
 void integ_zero_forces();
 void integ_forces_to_fp64();      // mixed: fixed point -> FP64 forces
 void integ_setup_constraints(const int32_t* listcon, const double* prmcon);
+// learned multiple-time-step form (gb_mlp.cu)
+void mts_set_topology(int ntcons, const int32_t* listcon, const double* weight);
+void mts_setup();
+void mts_free();
+bool mts_active();
+void mts_set_stale_only(bool on);  // ablation: no network, inner steps reuse F(t0)
+float* mts_rec_out();             // SPME per-atom reciprocal forces go here when active
+bool mts_step_needs_spme();
+void mts_after_full(double erc, double vrc, const double* strec);
+void mts_inner(double* erc, double* vrc, double* stress9);
+void mts_stats(double* out, int nv);
+int mlp_train_eval(int nb, const float* x, const float* target, const float* params, float* loss, float* grad,
+                   float* yout);
+int mlp_infer_eval(int nb, const float* x, const float* params, float* yout);
+int mts_features(float* x, int nv, float* scal);
+int mlp_param_count();

@@ -466,11 +466,17 @@ __global__ void k_list_reorder(int natms, int* list, int ld, const int* lfrzn, c
 }
 
 // FP32 copy of positions + charge (mixed path and prefilter helpers)
+// FP32 positions as an unevaluated sum hi + lo: in a large box the FP32
+// coordinate alone carries an absolute error of up to half an ulp of |x|
+// (7.6e-6 A at 180 A), while hi_i - hi_j + (lo_i - lo_j) keeps pair
+// separations to FP32 precision of the separation itself.
 __global__ void k_pos_f32(const DevScalars* sc, const double* x, const double* y, const double* z,
-                          const double* q, float4* xf) {
+                          const double* q, float4* xf, float4* xlo) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= sc->nlast) return;
-  xf[i] = make_float4((float)x[i], (float)y[i], (float)z[i], (float)q[i]);
+  const float hx = (float)x[i], hy = (float)y[i], hz = (float)z[i];
+  xf[i] = make_float4(hx, hy, hz, (float)q[i]);
+  xlo[i] = make_float4((float)(x[i] - (double)hx), (float)(y[i] - (double)hy), (float)(z[i] - (double)hz), 0.f);
 }
 
 // ------------------------------------------------------ derived full list
@@ -705,7 +711,7 @@ int list_build() {
 }
 
 void list_pos_f32() {
-  k_pos_f32<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(g.sc, g.x, g.y, g.z, g.chge, g.xf);
+  k_pos_f32<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(g.sc, g.x, g.y, g.z, g.chge, g.xf, g.xlo);
   GB_LAUNCHED();
 }
 
@@ -729,4 +735,5 @@ void list_full_build() {
   GB_CUDA(cudaMemsetAsync(fill, 0, sizeof(int) * (n + 1), st));
   k_full_fill<<<nblocks((long long)n * 32, 256), 256, 0, st>>>(n, g.list, g.ld, g.fstart, fill, g.flist);
   GB_LAUNCHED();
+  ++g.list_gen;
 }

@@ -1,0 +1,1202 @@
+// gb_mlp.cu - learned multiple-time-step (MTS) surrogate for the SPME
+// reciprocal-space force.  No counterpart exists in the reference: its
+// electro%nstfce "infrequent k-space" key is parsed but two_body_forces
+// evaluates SPME on every call (two_body.F90:298-302).  The plain SPME of
+// gb_spme.cu is both the teacher and the fallback.
+//
+// Cycle.  Full SPME runs at t0 and every k steps after it; on the k-1 inner
+// steps the reciprocal force of atom i is
+//     F_i(t) = F_i(t0) + [C_i(t) - C_i(t0)] + fs * R_i^T y_i,   y_i = MLP(x_i)
+// where C is the reciprocal force on a coarse FP32 grid (about half the points
+// per dimension, spline order 6) evaluated every step: its increment carries
+// the long-range change, which no local model can see, and the network learns
+// the remaining short-range correction.  The net force of the correction is
+// removed (as SPME removes its own); the reciprocal energy, virial and stress
+// of an inner step are those of t0 plus the coarse-grid increments.
+// Inputs x_i (51):
+//   48 = 8 Gaussians g_k(r_ij) (centres 0.5..6 A, width 0.45 A, cosine cut at
+//        6 A) x local-frame components of the linear-response sums
+//          A_k = q_i sum_j q_j g_k(r_ij) u_ij          (3)
+//          B_k = q_i sum_j q_j g_k(r_ij) r^_ij (r^_ij . u_ij)   (3)
+//        with u_ij = d_j - d_i and d the displacement since t0 (A and B span
+//        the pair Hessian q_i q_j grad grad phi(r) . u of any radial kernel);
+//    3 = F_i(t0) in the local frame;
+// each scaled by the inverse RMS of the first labelled sample.  The local frame
+// R_i of an atom of a 3-atom constrained molecule is that molecule's bisector
+// frame (origin = heaviest atom); other atoms use the lab frame.
+//
+// Network 51 -> 128 -> 128 -> 3, SiLU, BF16 weights and activations with FP32
+// accumulation.  Inference: mma.sync m16n8k16 BF16 tiles from shared memory,
+// persistent CTAs.  Training: forward + MSE + backward on CUDA cores with
+// BF16-rounded operands (weights, inputs, activations, activation gradients)
+// and FP32 accumulation, per-CTA gradient partials summed in a fixed order,
+// Adam on FP32 master weights.  Labels are R_i (F_i(t) - F_i(t0) - C_i(t) +
+// C_i(t0)) / fs from the SPME forces of the training steps (SPME every step
+// while training).  The judge: at every cycle end after training, the
+// prediction for that step is compared with SPME; RMS(pred - SPME) /
+// RMS(total force) > tol switches to plain SPME every step (and resumes
+// training) until a cycle end passes.  Each check also records the errors of
+// the same schedule without the network (coarse increment only) and of the
+// stale force F_i(t0), the ablations.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gb_common.cuh"
+
+namespace {
+
+constexpr int NIN = 51, KIN = 64, NH = 128, NOUT = 3, NOUTP = 16;
+constexpr int NRAD = 8;
+constexpr float RCUT_DESC = 6.0f, GAUSS_W = 0.45f, GAUSS_MU0 = 0.5f;
+constexpr int TILE_I = 64;  // atoms per inference tile (4 warps x 16)
+constexpr int TILE_T = 32;  // atoms per training CTA
+constexpr int DESC_WARPS = 8, DESC_BUF = 64;  // input kernel: atoms per CTA, compacted neighbours per warp
+// FP32 parameter vector: W1[NIN][NH], b1[NH], W2[NH][NH], b2[NH], W3[NH][NOUT], b3[NOUT]
+constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NIN * NH, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH,
+              OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + NH * NOUT, NPARAM = OFF_B3 + NOUT;
+// padded shared-memory row strides (bf16 elements) that keep mma fragment loads conflict-free
+constexpr int LDX = KIN + 8, LDH = NH + 8;
+
+struct Net {  // published BF16 copy used by the inference kernel
+  __nv_bfloat16 *w1t = nullptr, *w2t = nullptr, *w3t = nullptr;  // [out][in]
+  float* bias = nullptr;                                         // b1 | b2 | b3 padded to NOUTP
+};
+
+struct MtsDev {
+  bool ready = false;
+  int n = 0;
+  float *master = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *gpart = nullptr, *loss_part = nullptr;
+  int gpart_tiles = 0, batch = 0;
+  Net net;
+  __nv_bfloat16* X = nullptr;  // inputs [n][KIN]
+  float* frec0 = nullptr;      // reciprocal force at t0 (3n)
+  float* frec = nullptr;       // reciprocal force now: SPME result or prediction (3n)
+  float* truth = nullptr;      // prediction of the judge (3n)
+  float* fc = nullptr;         // coarse-grid reciprocal force now (3n)
+  float* fc0 = nullptr;        // coarse-grid reciprocal force at t0 (3n)
+  int Kc[3] = {0, 0, 0}, pc = 6;
+  double ec = 0.0, vc = 0.0, stc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};     // coarse now
+  double ec0 = 0.0, vc0 = 0.0, stc0[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // coarse at t0
+  double err_coarse = -1.0, err_stale = -1.0;
+  int *sstart = nullptr, *scount = nullptr, *slist = nullptr;  // short neighbour list (CSR)
+  long long scap = 0, gen_seen = -1;
+  float* target = nullptr;     // labels (3n)
+  double* x0 = nullptr;        // positions at t0 (3n)
+  float* disp = nullptr;       // displacement since t0 (3n)
+  float* frame = nullptr;      // local frame rows e1,e2,e3 (9n)
+  int* triple = nullptr;       // frame atoms (a,b,c) per atom, -1 = lab frame
+  float* scal = nullptr;       // [0,NIN) input scales, [NIN] force scale
+  double* red = nullptr;       // reduction results
+  int* idx = nullptr;          // training batch atom ids
+  int adam_t = 0;
+  int s = 0;                   // steps since t0
+  int step = 0;                // MD steps since configuration
+  bool have_t0 = false, scales_set = false, fallback = false;
+  long long n_full = 0, n_inner = 0, n_fallback = 0, n_judged = 0;
+  double last_err = -1.0, last_loss = -1.0, err_max = -1.0;
+  int batch_offset = 0;
+  // reciprocal energy/virial/stress of the last full step
+  double erc0 = 0.0, vrc0 = 0.0, st0[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+MtsDev M;
+std::vector<int> h_triple;  // host copy set at gb_init
+bool g_stale_only = false;  // ablation: inner steps reuse F(t0) with no network
+
+inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float dsilu(float z) {
+  const float s = 1.0f / (1.0f + __expf(-z));
+  return s * (1.0f + z * (1.0f - s));
+}
+__device__ __forceinline__ float bfr(float v) { return __bfloat162float(__float2bfloat16(v)); }
+__device__ __forceinline__ unsigned ld2(const __nv_bfloat16* p) { return *reinterpret_cast<const unsigned*>(p); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// ------------------------------------------------------------ per-step inputs
+// displacement since t0 (minimum image: atoms may have been wrapped since t0)
+// and the local frame of every atom
+__global__ void k_mts_prep(int n, const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ z, const double* __restrict__ x0, const int* __restrict__ tri,
+                           double cell, float* __restrict__ disp, float* __restrict__ frame) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float L = (float)cell, rL = (float)(1.0 / cell);
+  float d0 = (float)(x[i] - x0[3 * i]), d1 = (float)(y[i] - x0[3 * i + 1]), d2 = (float)(z[i] - x0[3 * i + 2]);
+  d0 -= L * rintf(d0 * rL); d1 -= L * rintf(d1 * rL); d2 -= L * rintf(d2 * rL);
+  disp[3 * i] = d0; disp[3 * i + 1] = d1; disp[3 * i + 2] = d2;
+  float e[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  const int a = tri[3 * i], b = tri[3 * i + 1], c = tri[3 * i + 2];
+  if (a >= 0) {
+    float bx = (float)(x[b] - x[a]), by = (float)(y[b] - y[a]), bz = (float)(z[b] - z[a]);
+    float cx = (float)(x[c] - x[a]), cy = (float)(y[c] - y[a]), cz = (float)(z[c] - z[a]);
+    bx -= L * rintf(bx * rL); by -= L * rintf(by * rL); bz -= L * rintf(bz * rL);
+    cx -= L * rintf(cx * rL); cy -= L * rintf(cy * rL); cz -= L * rintf(cz * rL);
+    float e1x = bx + cx, e1y = by + cy, e1z = bz + cz;
+    float nr = rsqrtf(e1x * e1x + e1y * e1y + e1z * e1z);
+    e1x *= nr; e1y *= nr; e1z *= nr;
+    float ux = bx - cx, uy = by - cy, uz = bz - cz;
+    const float pr = ux * e1x + uy * e1y + uz * e1z;
+    ux -= pr * e1x; uy -= pr * e1y; uz -= pr * e1z;
+    nr = rsqrtf(ux * ux + uy * uy + uz * uz);
+    ux *= nr; uy *= nr; uz *= nr;
+    e[0] = e1x; e[1] = e1y; e[2] = e1z;
+    e[3] = ux; e[4] = uy; e[5] = uz;
+    e[6] = e1y * uz - e1z * uy; e[7] = e1z * ux - e1x * uz; e[8] = e1x * uy - e1y * ux;
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) frame[9 * i + k] = e[k];
+}
+
+// ------------------------------------------------------ short neighbour list
+// Pairs within rs = 6 A + skin of the full list, rebuilt with it: between
+// rebuilds no atom moves more than half the skin, so every pair inside 6 A at
+// any step of the list's lifetime is in it.  Each atom's entries are sorted by
+// index, so the input sums do not depend on the full list's fill order.
+constexpr int SHORT_CAP = 256;  // entries sorted in shared memory per atom
+
+__global__ void k_short_count(int n, const int* __restrict__ fstart, const int* __restrict__ fcount,
+                              const int* __restrict__ flist, const float4* __restrict__ xf, float rs2,
+                              int* __restrict__ scount) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= n) return;
+  const float4 pi = xf[i];
+  const int st = fstart[i], cnt = fcount[i];
+  int c = 0;
+  for (int base = 0; base < cnt; base += 32) {
+    bool in = false;
+    if (base + lane < cnt) {
+      const float4 pj = xf[flist[st + base + lane]];
+      const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+      in = dx * dx + dy * dy + dz * dz < rs2;
+    }
+    c += __popc(__ballot_sync(0xffffffffu, in));
+  }
+  if (lane == 0) scount[i] = c;
+}
+
+__global__ void __launch_bounds__(256) k_short_fill(int n, const int* __restrict__ fstart,
+                                                    const int* __restrict__ fcount, const int* __restrict__ flist,
+                                                    const float4* __restrict__ xf, float rs2,
+                                                    const int* __restrict__ sstart, int* __restrict__ slist) {
+  __shared__ int buf[8][SHORT_CAP];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 8 + w;
+  if (i >= n) return;  // the whole warp leaves; no block-wide barrier below
+  const float4 pi = xf[i];
+  const int st = fstart[i], cnt = fcount[i];
+  const int s0 = sstart[i], ns = sstart[i + 1] - s0;
+  const bool sorted = ns <= SHORT_CAP;
+  int c = 0;
+  for (int base = 0; base < cnt; base += 32) {
+    bool in = false;
+    int j = 0;
+    if (base + lane < cnt) {
+      j = flist[st + base + lane];
+      const float4 pj = xf[j];
+      const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+      in = dx * dx + dy * dy + dz * dz < rs2;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, in);
+    if (in) {
+      const int pos = c + __popc(b & ((1u << lane) - 1u));
+      if (sorted) buf[w][pos] = j;
+      else slist[s0 + pos] = j;  // too many to sort here: fill order
+    }
+    c += __popc(b);
+  }
+  __syncwarp();
+  if (!sorted) return;
+  // rank sort (entries are distinct)
+  for (int e = lane; e < ns; e += 32) {
+    const int v = buf[w][e];
+    int r = 0;
+    for (int f = 0; f < ns; ++f) r += buf[w][f] < v;
+    slist[s0 + r] = v;
+  }
+}
+
+// inputs: one warp per atom over its short neighbour list (local and halo j)
+__global__ void __launch_bounds__(256) k_mts_desc(int n, const int* __restrict__ fstart, const int* __restrict__ fcount,
+                                                  const int* __restrict__ flist, const int* __restrict__ src,
+                                                  const float4* __restrict__ xf, const float* __restrict__ disp,
+                                                  const float* __restrict__ frame, const float* __restrict__ frec0,
+                                                  const float* __restrict__ scal, __nv_bfloat16* __restrict__ X) {
+  // Neighbours inside 6 A (about a tenth of the list) are compacted per warp
+  // into shared memory with a ballot, so the Gaussian work runs on full warps;
+  // the 48 per-lane sums are then reduced by a transposing butterfly (48
+  // shuffles instead of 48 x 5), after which lane pairs own one xyz triple.
+  __shared__ float4 s_r[DESC_WARPS][DESC_BUF];  // dx, dy, dz, q_j
+  __shared__ float4 s_u[DESC_WARPS][DESC_BUF];  // u = d_j - d_i
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * DESC_WARPS + w;
+  if (i >= n) return;  // the whole warp leaves; no block-wide barrier below
+  const float4 pi = xf[i];
+  const float dix = disp[3 * i], diy = disp[3 * i + 1], diz = disp[3 * i + 2];
+  float v[6 * NRAD];
+#pragma unroll
+  for (int k = 0; k < 6 * NRAD; ++k) v[k] = 0.f;
+  const float rc2 = RCUT_DESC * RCUT_DESC;
+  const float dmu = (RCUT_DESC - GAUSS_MU0) / (float)(NRAD - 1), c2 = 1.0f / (2.0f * GAUSS_W * GAUSS_W);
+  const float qi = pi.w;
+  auto accumulate = [&](const float4 rr, const float4 uu) {
+    const float r2 = rr.x * rr.x + rr.y * rr.y + rr.z * rr.z;
+    const float rinv = rsqrtf(r2), r = r2 * rinv;
+    const float wt = qi * rr.w * 0.5f * (1.0f + __cosf(3.14159265f * r * (1.0f / RCUT_DESC)));
+    const float hx = rr.x * rinv, hy = rr.y * rinv, hz = rr.z * rinv;
+    const float pu = hx * uu.x + hy * uu.y + hz * uu.z;
+    const float bx = pu * hx, by = pu * hy, bz = pu * hz;
+#pragma unroll
+    for (int k = 0; k < NRAD; ++k) {
+      const float t = r - (GAUSS_MU0 + dmu * (float)k);
+      const float gk = wt * __expf(-t * t * c2);
+      v[6 * k + 0] = fmaf(gk, uu.x, v[6 * k + 0]);
+      v[6 * k + 1] = fmaf(gk, uu.y, v[6 * k + 1]);
+      v[6 * k + 2] = fmaf(gk, uu.z, v[6 * k + 2]);
+      v[6 * k + 3] = fmaf(gk, bx, v[6 * k + 3]);
+      v[6 * k + 4] = fmaf(gk, by, v[6 * k + 4]);
+      v[6 * k + 5] = fmaf(gk, bz, v[6 * k + 5]);
+    }
+  };
+  const int st = fstart[i], cnt = fcount[i];
+  const unsigned lt_mask = (1u << lane) - 1u;
+  int pending = 0;
+  for (int base = 0; base < cnt; base += 32) {
+    const int m = base + lane;
+    bool pass = false;
+    float4 rr = make_float4(0.f, 0.f, 0.f, 0.f), uu = rr;
+    if (m < cnt) {
+      const int j = flist[st + m];
+      const float4 pj = xf[j];
+      rr = make_float4(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z, pj.w);
+      const float r2 = rr.x * rr.x + rr.y * rr.y + rr.z * rr.z;
+      pass = r2 < rc2 && r2 > 0.f;
+      if (pass) {
+        const int js = src[j];
+        uu = make_float4(disp[3 * js] - dix, disp[3 * js + 1] - diy, disp[3 * js + 2] - diz, 0.f);
+      }
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, pass);
+    if (pass) {
+      const int pos = pending + __popc(b & lt_mask);  // < 63: pending < 32 before every batch
+      s_r[w][pos] = rr;
+      s_u[w][pos] = uu;
+    }
+    pending += __popc(b);
+    __syncwarp();
+    if (pending >= 32) {
+      accumulate(s_r[w][lane], s_u[w][lane]);
+      const int rest = pending - 32;
+      float4 r2v = make_float4(0.f, 0.f, 0.f, 0.f), u2v = r2v;
+      if (lane < rest) { r2v = s_r[w][32 + lane]; u2v = s_u[w][32 + lane]; }
+      __syncwarp();
+      if (lane < rest) { s_r[w][lane] = r2v; s_u[w][lane] = u2v; }
+      pending = rest;
+      __syncwarp();
+    }
+  }
+  if (lane < pending) accumulate(s_r[w][lane], s_u[w][lane]);
+  // transposing butterfly: 48 -> 24 -> 12 -> 6 -> 3 values per lane
+#pragma unroll
+  for (int h = 24, o = 16; h >= 3; h >>= 1, o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < h; ++k) {
+      const float keep = up ? v[h + k] : v[k];
+      const float send = up ? v[k] : v[h + k];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], 1);
+  // lane owns triple t = 8 b4 + 4 b3 + 2 b2 + b1 (values 3t..3t+2: A_k for
+  // even t, B_k for odd t, k = t / 2); even lanes write it in the local frame
+  const int t = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+  const float* e = frame + 9 * (size_t)i;
+  __nv_bfloat16* xo = X + (size_t)i * KIN;
+  if ((lane & 1) == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float val = e[3 * c] * v[0] + e[3 * c + 1] * v[1] + e[3 * c + 2] * v[2];
+      xo[3 * t + c] = __float2bfloat16(val * scal[3 * t + c]);
+    }
+  } else if (lane == 1) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float val = e[3 * c] * frec0[3 * i] + e[3 * c + 1] * frec0[3 * i + 1] + e[3 * c + 2] * frec0[3 * i + 2];
+      xo[6 * NRAD + c] = __float2bfloat16(val * scal[6 * NRAD + c]);
+    }
+  } else if (lane == 3) {
+    for (int c = NIN; c < KIN; ++c) xo[c] = __float2bfloat16(0.f);
+  }
+}
+
+// ------------------------------------------------------------ inference (mma)
+struct InferSmem {
+  __nv_bfloat16 w1t[NH * LDX];
+  __nv_bfloat16 w2t[NH * LDH];
+  __nv_bfloat16 w3t[NOUTP * LDH];
+  float bias[NH + NH + NOUTP];
+  __nv_bfloat16 xin[TILE_I * LDX];
+  __nv_bfloat16 act[TILE_I * LDH];
+  float yo[TILE_I * NOUTP];
+};
+
+// one dense layer for a warp's 16 rows: out = act(in W + b)
+template <int K, int N, bool SILU>
+__device__ __forceinline__ void mlp_layer(const __nv_bfloat16* in, int ldin, const __nv_bfloat16* wt, int ldw,
+                                          const float* bias, __nv_bfloat16* out, int ldout, float* yout) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  unsigned a[K / 16][4];
+#pragma unroll
+  for (int ks = 0; ks < K / 16; ++ks) {
+    const int k0 = ks * 16 + 2 * t;
+    a[ks][0] = ld2(in + g * ldin + k0);
+    a[ks][1] = ld2(in + (g + 8) * ldin + k0);
+    a[ks][2] = ld2(in + g * ldin + k0 + 8);
+    a[ks][3] = ld2(in + (g + 8) * ldin + k0 + 8);
+  }
+  __syncwarp();
+#pragma unroll 4
+  for (int nt = 0; nt < N / 8; ++nt) {
+    float d[4] = {0.f, 0.f, 0.f, 0.f};
+    const __nv_bfloat16* wrow = wt + (nt * 8 + g) * ldw + 2 * t;
+#pragma unroll
+    for (int ks = 0; ks < K / 16; ++ks) mma_bf16(d, a[ks], ld2(wrow + ks * 16), ld2(wrow + ks * 16 + 8));
+    const int c0 = nt * 8 + 2 * t;
+    float v0 = d[0] + bias[c0], v1 = d[1] + bias[c0 + 1], v2 = d[2] + bias[c0], v3 = d[3] + bias[c0 + 1];
+    if (SILU) { v0 = silu(v0); v1 = silu(v1); v2 = silu(v2); v3 = silu(v3); }
+    if (out) {
+      *reinterpret_cast<__nv_bfloat162*>(out + g * ldout + c0) = __floats2bfloat162_rn(v0, v1);
+      *reinterpret_cast<__nv_bfloat162*>(out + (g + 8) * ldout + c0) = __floats2bfloat162_rn(v2, v3);
+    } else {
+      yout[g * NOUTP + c0] = v0; yout[g * NOUTP + c0 + 1] = v1;
+      yout[(g + 8) * NOUTP + c0] = v2; yout[(g + 8) * NOUTP + c0 + 1] = v3;
+    }
+  }
+  __syncwarp();
+}
+
+// persistent: each CTA stages the weights once and walks tiles of 64 atoms.
+// out = frec0 + fs * R^T y (lab frame)
+__global__ void __launch_bounds__(128) k_mlp_infer(int n, const __nv_bfloat16* __restrict__ X, Net net,
+                                                   const float* __restrict__ frec0, const float* __restrict__ frame,
+                                                   const float* __restrict__ scal, float* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+  for (int e = threadIdx.x; e < NH * (KIN / 2); e += blockDim.x) {
+    const int r = e / (KIN / 2), c = e % (KIN / 2);
+    reinterpret_cast<unsigned*>(S.w1t + r * LDX)[c] = reinterpret_cast<const unsigned*>(net.w1t + r * KIN)[c];
+  }
+  for (int e = threadIdx.x; e < NH * (NH / 2); e += blockDim.x) {
+    const int r = e / (NH / 2), c = e % (NH / 2);
+    reinterpret_cast<unsigned*>(S.w2t + r * LDH)[c] = reinterpret_cast<const unsigned*>(net.w2t + r * NH)[c];
+  }
+  for (int e = threadIdx.x; e < NOUTP * (NH / 2); e += blockDim.x) {
+    const int r = e / (NH / 2), c = e % (NH / 2);
+    reinterpret_cast<unsigned*>(S.w3t + r * LDH)[c] = reinterpret_cast<const unsigned*>(net.w3t + r * NH)[c];
+  }
+  for (int e = threadIdx.x; e < NH + NH + NOUTP; e += blockDim.x) S.bias[e] = net.bias[e];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float fs = scal[NIN];
+  const int ntiles = (n + TILE_I - 1) / TILE_I;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int a0 = tile * TILE_I;
+    __syncthreads();  // weights staged; the previous tile's rows are consumed
+    for (int e = threadIdx.x; e < TILE_I * (KIN / 8); e += blockDim.x) {
+      const int r = e / (KIN / 8), c = e % (KIN / 8);
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (a0 + r < n) v = reinterpret_cast<const uint4*>(X + (size_t)(a0 + r) * KIN)[c];
+      reinterpret_cast<uint4*>(S.xin + r * LDX)[c] = v;
+    }
+    __syncthreads();
+    __nv_bfloat16* h = S.act + w * 16 * LDH;
+    mlp_layer<KIN, NH, true>(S.xin + w * 16 * LDX, LDX, S.w1t, LDX, S.bias, h, LDH, nullptr);
+    mlp_layer<NH, NH, true>(h, LDH, S.w2t, LDH, S.bias + NH, h, LDH, nullptr);
+    mlp_layer<NH, NOUTP, false>(h, LDH, S.w3t, LDH, S.bias + 2 * NH, nullptr, 0, S.yo + w * 16 * NOUTP);
+    if (lane < 16) {
+      const int atom = a0 + w * 16 + lane;
+      if (atom < n) {
+        const float* yv = S.yo + (w * 16 + lane) * NOUTP;
+        const float y0 = yv[0] * fs, y1 = yv[1] * fs, y2 = yv[2] * fs;
+        const float* e = frame + 9 * (size_t)atom;
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          out[3 * (size_t)atom + c] = frec0[3 * (size_t)atom + c] + e[c] * y0 + e[3 + c] * y1 + e[6 + c] * y2;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- training
+// forward + MSE + backward of TILE_T atoms; per-CTA gradient partial in gpart.
+// Row strides NH+1 keep the column walks of the backward pass conflict-free.
+struct TrainSmem {
+  float W1[NIN][NH];
+  float W2[NH][NH + 1];
+  float W3[NH][NOUT];
+  float b1[NH], b2[NH], b3[4];
+  float x[TILE_T][NIN];
+  float z1[TILE_T][NH + 1], h1[TILE_T][NH + 1];
+  float z2[TILE_T][NH + 1], h2[TILE_T][NH + 1];
+  float dy[TILE_T][NOUT];
+  float sq[TILE_T][NOUT];
+};
+
+__global__ void __launch_bounds__(256) k_mlp_train(int nb, const int* __restrict__ idx, const __nv_bfloat16* __restrict__ X,
+                                                   const float* __restrict__ target, const float* __restrict__ master,
+                                                   float inv_count, float* __restrict__ gpart,
+                                                   float* __restrict__ loss_part, float* __restrict__ yout) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < NIN * NH; e += nt) S.W1[e / NH][e % NH] = bfr(master[OFF_W1 + e]);
+  for (int e = tid; e < NH * NH; e += nt) S.W2[e / NH][e % NH] = bfr(master[OFF_W2 + e]);
+  for (int e = tid; e < NH * NOUT; e += nt) S.W3[e / NOUT][e % NOUT] = bfr(master[OFF_W3 + e]);
+  for (int e = tid; e < NH; e += nt) { S.b1[e] = master[OFF_B1 + e]; S.b2[e] = master[OFF_B2 + e]; }
+  if (tid < NOUT) S.b3[tid] = master[OFF_B3 + tid];
+  const int r0 = blockIdx.x * TILE_T;
+  for (int e = tid; e < TILE_T * NIN; e += nt) {
+    const int r = e / NIN, c = e % NIN;
+    S.x[r][c] = r0 + r < nb ? __bfloat162float(X[(size_t)idx[r0 + r] * KIN + c]) : 0.f;
+  }
+  __syncthreads();
+  for (int e = tid; e < TILE_T * NH; e += nt) {
+    const int r = e / NH, c = e % NH;
+    float s = S.b1[c];
+    for (int k = 0; k < NIN; ++k) s = fmaf(S.x[r][k], S.W1[k][c], s);
+    S.z1[r][c] = s;
+    S.h1[r][c] = bfr(silu(s));
+  }
+  __syncthreads();
+  for (int e = tid; e < TILE_T * NH; e += nt) {
+    const int r = e / NH, c = e % NH;
+    float s = S.b2[c];
+    for (int k = 0; k < NH; ++k) s = fmaf(S.h1[r][k], S.W2[k][c], s);
+    S.z2[r][c] = s;
+    S.h2[r][c] = bfr(silu(s));
+  }
+  __syncthreads();
+  if (tid < TILE_T * NOUT) {
+    const int r = tid / NOUT, c = tid % NOUT;
+    float s = S.b3[c];
+    for (int k = 0; k < NH; ++k) s = fmaf(S.h2[r][k], S.W3[k][c], s);
+    float d = 0.f;
+    if (r0 + r < nb) {
+      d = s - target[3 * (size_t)idx[r0 + r] + c];
+      if (yout) yout[3 * (size_t)(r0 + r) + c] = s;
+    }
+    S.dy[r][c] = bfr(2.0f * d * inv_count);
+    S.sq[r][c] = d * d;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    float l = 0.f;
+    for (int r = 0; r < TILE_T; ++r)
+      for (int c = 0; c < NOUT; ++c) l += S.sq[r][c];
+    loss_part[blockIdx.x] = l * inv_count;
+  }
+  float* gp = gpart + (size_t)blockIdx.x * NPARAM;
+  for (int e = tid; e < NH * NOUT; e += nt) {
+    const int k = e / NOUT, c = e % NOUT;
+    float s = 0.f;
+    for (int r = 0; r < TILE_T; ++r) s = fmaf(S.h2[r][k], S.dy[r][c], s);
+    gp[OFF_W3 + e] = s;
+  }
+  if (tid < NOUT) {
+    float s = 0.f;
+    for (int r = 0; r < TILE_T; ++r) s += S.dy[r][tid];
+    gp[OFF_B3 + tid] = s;
+  }
+  // dZ2 = (dY W3^T) . silu'(z2), stored over z2
+  for (int e = tid; e < TILE_T * NH; e += nt) {
+    const int r = e / NH, k = e % NH;
+    float s = 0.f;
+    for (int c = 0; c < NOUT; ++c) s = fmaf(S.dy[r][c], S.W3[k][c], s);
+    S.z2[r][k] = bfr(s * dsilu(S.z2[r][k]));
+  }
+  __syncthreads();
+  for (int e = tid; e < NH * NH; e += nt) {
+    const int k = e / NH, c = e % NH;
+    float s = 0.f;
+    for (int r = 0; r < TILE_T; ++r) s = fmaf(S.h1[r][k], S.z2[r][c], s);
+    gp[OFF_W2 + e] = s;
+  }
+  for (int c = tid; c < NH; c += nt) {
+    float s = 0.f;
+    for (int r = 0; r < TILE_T; ++r) s += S.z2[r][c];
+    gp[OFF_B2 + c] = s;
+  }
+  // dZ1 = (dZ2 W2^T) . silu'(z1), stored over z1
+  for (int e = tid; e < TILE_T * NH; e += nt) {
+    const int r = e / NH, k = e % NH;
+    float s = 0.f;
+    for (int c = 0; c < NH; ++c) s = fmaf(S.z2[r][c], S.W2[k][c], s);
+    S.z1[r][k] = bfr(s * dsilu(S.z1[r][k]));
+  }
+  __syncthreads();
+  for (int e = tid; e < NIN * NH; e += nt) {
+    const int k = e / NH, c = e % NH;
+    float s = 0.f;
+    for (int r = 0; r < TILE_T; ++r) s = fmaf(S.x[r][k], S.z1[r][c], s);
+    gp[OFF_W1 + e] = s;
+  }
+  for (int c = tid; c < NH; c += nt) {
+    float s = 0.f;
+    for (int r = 0; r < TILE_T; ++r) s += S.z1[r][c];
+    gp[OFF_B1 + c] = s;
+  }
+}
+
+// fixed-order sum of the per-CTA partials
+__global__ void k_grad_reduce(int ntiles, const float* __restrict__ gpart, float* __restrict__ grad) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= NPARAM) return;
+  float s = 0.f;
+  for (int t = 0; t < ntiles; ++t) s += gpart[(size_t)t * NPARAM + p];
+  grad[p] = s;
+}
+
+__global__ void k_adam(float* __restrict__ w, float* __restrict__ m1, float* __restrict__ m2,
+                       const float* __restrict__ gr, float lr, float b1, float b2, float c1, float c2, float eps) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= NPARAM) return;
+  const float gv = gr[p];
+  const float a = b1 * m1[p] + (1.0f - b1) * gv;
+  const float b = b2 * m2[p] + (1.0f - b2) * gv * gv;
+  m1[p] = a;
+  m2[p] = b;
+  w[p] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+}
+
+// BF16 [out][in] copies for the inference kernel
+__global__ void k_publish(const float* __restrict__ w, Net net) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < NH * KIN) {
+    const int o = e / KIN, k = e % KIN;
+    net.w1t[e] = __float2bfloat16(k < NIN ? w[OFF_W1 + k * NH + o] : 0.f);
+  }
+  if (e < NH * NH) {
+    const int o = e / NH, k = e % NH;
+    net.w2t[e] = __float2bfloat16(w[OFF_W2 + k * NH + o]);
+  }
+  if (e < NOUTP * NH) {
+    const int o = e / NH, k = e % NH;
+    net.w3t[e] = __float2bfloat16(o < NOUT ? w[OFF_W3 + k * NOUT + o] : 0.f);
+  }
+  if (e < NH) { net.bias[e] = w[OFF_B1 + e]; net.bias[NH + e] = w[OFF_B2 + e]; }
+  if (e < NOUTP) net.bias[2 * NH + e] = e < NOUT ? w[OFF_B3 + e] : 0.f;
+}
+
+// labels: R (frec - frec0 - fc + fc0) / fs
+__global__ void k_mts_target(int n, const float* __restrict__ frec, const float* __restrict__ frec0,
+                             const float* __restrict__ fc, const float* __restrict__ fc0,
+                             const float* __restrict__ frame, const float* __restrict__ scal,
+                             float* __restrict__ target) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float inv = 1.0f / scal[NIN];
+  float d[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) d[c] = (frec[3 * i + c] - frec0[3 * i + c]) - (fc[3 * i + c] - fc0[3 * i + c]);
+  const float* e = frame + 9 * (size_t)i;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) target[3 * i + c] = (e[3 * c] * d[0] + e[3 * c + 1] * d[1] + e[3 * c + 2] * d[2]) * inv;
+}
+
+// per-block squared errors against the SPME forces f of this step:
+// [network prediction pred + fc - fc0, coarse increment only f0 + fc - fc0, stale f0]
+__global__ void k_err3(int n, const float* __restrict__ pred, const float* __restrict__ fc,
+                       const float* __restrict__ fc0, const float* __restrict__ f0, const float* __restrict__ f,
+                       double* blk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float v[3] = {0.f, 0.f, 0.f};
+  if (i < n) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float inc = fc[3 * i + k] - fc0[3 * i + k], t = f[3 * i + k];
+      const float a = pred[3 * i + k] + inc - t, b = f0[3 * i + k] + inc - t, c = f0[3 * i + k] - t;
+      v[0] = fmaf(a, a, v[0]);
+      v[1] = fmaf(b, b, v[1]);
+      v[2] = fmaf(c, c, v[2]);
+    }
+  }
+  block_reduce_store<3>(v, blk);
+}
+
+// per-block sum of squares of a 3n array
+__global__ void k_sumsq(int n, const float* __restrict__ a, double* blk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float v[1] = {0.f};
+  if (i < n) v[0] = a[3 * i] * a[3 * i] + a[3 * i + 1] * a[3 * i + 1] + a[3 * i + 2] * a[3 * i + 2];
+  block_reduce_store<1>(v, blk);
+}
+
+// per-block sum of |F|^2 of the FP64 total forces
+__global__ void k_fsq(int n, const double* __restrict__ fx, const double* __restrict__ fy,
+                      const double* __restrict__ fz, double* blk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float v[1] = {0.f};
+  if (i < n) {
+    const float a = (float)fx[i], b = (float)fy[i], c = (float)fz[i];
+    v[0] = a * a + b * b + c * c;
+  }
+  block_reduce_store<1>(v, blk);
+}
+
+// per-block sum of the predicted increments (net force of the prediction)
+__global__ void k_net3(int n, const float* __restrict__ f, const float* __restrict__ f0, double* blk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float v[3] = {0.f, 0.f, 0.f};
+  if (i < n) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v[k] = f[3 * i + k] - f0[3 * i + k];
+  }
+  block_reduce_store<3>(v, blk);
+}
+
+// inner step: f = pred + fc - fc0 with the mean of the network correction
+// (pred - f0) removed, added into the fixed-point forces
+__global__ void k_mts_apply(int n, float* __restrict__ f, const float* __restrict__ fc, const float* __restrict__ fc0,
+                            const double* __restrict__ net, float rn, unsigned long long* __restrict__ fixp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float m[3] = {(float)net[0] * rn, (float)net[1] * rn, (float)net[2] * rn};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float fv = f[3 * i + k] - m[k] + (fc[3 * i + k] - fc0[3 * i + k]);
+    f[3 * i + k] = fv;
+    atomicAdd(&fixp[3 * i + k], (unsigned long long)fix40(fv));
+  }
+}
+
+__global__ void k_copy_f(long long n, const float* __restrict__ a, float* __restrict__ b) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+
+__global__ void k_save_x0(int n, const double* x, const double* y, const double* z, double* x0) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x0[3 * i] = x[i]; x0[3 * i + 1] = y[i]; x0[3 * i + 2] = z[i];
+}
+
+__global__ void k_seq_idx(int nb, int offset, int n, int* idx) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nb) idx[r] = (int)(((long long)offset + r) % n);
+}
+
+// per-feature mean square over all atoms (input normalisation)
+__global__ void k_feat_ms(int n, const __nv_bfloat16* __restrict__ X, float* __restrict__ out) {
+  const int c = blockIdx.x;
+  float s = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float v = __bfloat162float(X[(size_t)i * KIN + c]);
+    s = fmaf(v, v, s);
+  }
+  __shared__ float red[32];
+  s = warp_sumf(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    out[c] = t / (float)n;
+  }
+}
+
+constexpr size_t infer_smem = sizeof(InferSmem);
+constexpr size_t train_smem = sizeof(TrainSmem);
+static_assert(6 * NRAD + 3 == NIN, "input layout: 6 response sums per Gaussian + F(t0)");
+static_assert(sizeof(TrainSmem) <= 227 * 1024, "training tile exceeds shared memory");
+static_assert(sizeof(InferSmem) <= 227 * 1024, "inference tile exceeds shared memory");
+
+int g_infer_grid = 0;
+
+void net_alloc(Net& n) {
+  GB_CUDA(cudaMalloc(&n.w1t, sizeof(__nv_bfloat16) * NH * KIN));
+  GB_CUDA(cudaMalloc(&n.w2t, sizeof(__nv_bfloat16) * NH * NH));
+  GB_CUDA(cudaMalloc(&n.w3t, sizeof(__nv_bfloat16) * NOUTP * NH));
+  GB_CUDA(cudaMalloc(&n.bias, sizeof(float) * (2 * NH + NOUTP)));
+}
+void net_free(Net& n) {
+  for (void* p : {(void*)n.w1t, (void*)n.w2t, (void*)n.w3t, (void*)n.bias})
+    if (p) cudaFree(p);
+  n = Net();
+}
+
+void publish(const float* master, Net& net) {
+  k_publish<<<nblocks(NH * NH, 256), 256, 0, g.stream>>>(master, net);
+  GB_LAUNCHED();
+}
+
+void set_attrs() {
+  static int dev_done = -1;
+  int dev = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  if (dev_done == dev) return;
+  GB_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem));
+  GB_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem));
+  int occ = 0;
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mlp_infer, 128, infer_smem));
+  g_infer_grid = std::max(1, occ) * g.nsm;
+  dev_done = dev;
+}
+
+void launch_infer(int n, const __nv_bfloat16* X, const Net& net, const float* frec0, const float* frame,
+                  const float* scal, float* out) {
+  const int grid = std::max(1, std::min(g_infer_grid, nblocks(n, TILE_I)));
+  k_mlp_infer<<<grid, 128, infer_smem, g.stream>>>(n, X, net, frec0, frame, scal, out);
+  GB_LAUNCHED();
+}
+
+// deterministic Glorot-uniform weights (splitmix64), zero biases, small output layer
+std::vector<float> initial_params() {
+  std::vector<float> w(NPARAM, 0.f);
+  unsigned long long s = 0x9E3779B97F4A7C15ull;
+  auto rnd = [&]() {
+    s += 0x9E3779B97F4A7C15ull;
+    unsigned long long z = s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  };
+  auto fill = [&](int off, int fin, int fout, double gain) {
+    const double a = gain * std::sqrt(6.0 / (fin + fout));
+    for (int k = 0; k < fin * fout; ++k) w[off + k] = (float)((2.0 * rnd() - 1.0) * a);
+  };
+  fill(OFF_W1, NIN, NH, 1.0);
+  fill(OFF_W2, NH, NH, 1.0);
+  fill(OFF_W3, NH, NOUT, 0.1);
+  return w;
+}
+
+void read_scalars(const double* dev, double* host, int nv) {
+  GB_CUDA(cudaMemcpyAsync(host, dev, sizeof(double) * nv, cudaMemcpyDeviceToHost, g.stream));
+  GB_CUDA(cudaStreamSynchronize(g.stream));
+}
+
+// inputs of the current positions relative to t0
+// short list of the current full list (positions of this step in xf)
+void mts_short_list() {
+  const int n = g.natms;
+  const float rs = RCUT_DESC + (float)g.p.rpad;
+  const float rs2 = rs * rs;
+  GB_CUDA(cudaMemsetAsync(M.scount, 0, sizeof(int) * (n + 1), g.stream));
+  k_short_count<<<nblocks((long long)n * 32, 256), 256, 0, g.stream>>>(n, g.fstart, g.fcount, g.flist, g.xf, rs2,
+                                                                        M.scount);
+  GB_LAUNCHED();
+  scan_exclusive(M.scount, M.sstart, n + 1);
+  int total = 0;
+  GB_CUDA(cudaMemcpyAsync(&total, M.sstart + n, sizeof(int), cudaMemcpyDeviceToHost, g.stream));
+  GB_CUDA(cudaStreamSynchronize(g.stream));
+  if ((long long)total > M.scap) {
+    if (M.slist) cudaFree(M.slist);
+    M.scap = (long long)(total * 1.25) + 1024;
+    GB_CUDA(cudaMalloc(&M.slist, sizeof(int) * M.scap));
+  }
+  k_short_fill<<<nblocks(n, 8), 256, 0, g.stream>>>(n, g.fstart, g.fcount, g.flist, g.xf, rs2, M.sstart, M.slist);
+  GB_LAUNCHED();
+  M.gen_seen = g.list_gen;
+}
+
+void mts_inputs() {
+  const int n = g.natms;
+  prof_begin(P_MTS_DESC);
+  if (M.gen_seen != g.list_gen) mts_short_list();
+  k_mts_prep<<<nblocks(n, 256), 256, 0, g.stream>>>(n, g.x, g.y, g.z, M.x0, M.triple, g.cell[0], M.disp, M.frame);
+  GB_LAUNCHED();
+  k_mts_desc<<<nblocks(n, DESC_WARPS), DESC_WARPS * 32, 0, g.stream>>>(n, M.sstart, M.scount, M.slist, g.src, g.xf,
+                                                                        M.disp, M.frame, M.frec0, M.scal, M.X);
+  GB_LAUNCHED();
+  prof_end(P_MTS_DESC);
+}
+
+void mts_labels() {
+  k_mts_target<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, M.frec, M.frec0, M.fc, M.fc0, M.frame, M.scal,
+                                                             M.target);
+  GB_LAUNCHED();
+}
+
+// input and output scales from the first labelled sample
+void mts_set_scales() {
+  const int n = g.natms;
+  std::vector<float> sc(NIN + 1, 1.0f);
+  GB_CUDA(cudaMemcpy(M.scal, sc.data(), sizeof(float) * (NIN + 1), cudaMemcpyHostToDevice));
+  mts_inputs();
+  k_feat_ms<<<NIN, 256, 0, g.stream>>>(n, M.X, M.target);
+  GB_LAUNCHED();
+  std::vector<float> ms(NIN);
+  GB_CUDA(cudaMemcpyAsync(ms.data(), M.target, sizeof(float) * NIN, cudaMemcpyDeviceToHost, g.stream));
+  GB_CUDA(cudaStreamSynchronize(g.stream));
+  for (int c = 0; c < NIN; ++c) sc[c] = ms[c] > 1e-30f ? 1.0f / std::sqrt(ms[c]) : 1.0f;
+  // force scale: RMS component of the unscaled labels
+  mts_labels();
+  const int nb = nblocks(n, 256);
+  double* blk = gb_blkacc(nb);
+  k_sumsq<<<nb, 256, 0, g.stream>>>(n, M.target, blk);
+  GB_LAUNCHED();
+  gb_reduce_blocks(blk, nb, 1, M.red);
+  double r1[1];
+  read_scalars(M.red, r1, 1);
+  const double d_rms = std::sqrt(r1[0] / (3.0 * n));
+  sc[NIN] = (float)(d_rms > 0 ? d_rms : 1.0);
+  GB_CUDA(cudaMemcpy(M.scal, sc.data(), sizeof(float) * (NIN + 1), cudaMemcpyHostToDevice));
+  M.scales_set = true;
+  mts_inputs();  // with the final scales
+}
+
+void mts_train_step() {
+  const int n = g.natms, nb = M.batch;
+  k_seq_idx<<<nblocks(nb, 256), 256, 0, g.stream>>>(nb, M.batch_offset, n, M.idx);
+  GB_LAUNCHED();
+  M.batch_offset = (int)(((long long)M.batch_offset + nb) % n);
+  const int nt = nblocks(nb, TILE_T);
+  prof_begin(P_MLP_TRAIN);
+  k_mlp_train<<<nt, 256, train_smem, g.stream>>>(nb, M.idx, M.X, M.target, M.master, 1.0f / (float)(nb * NOUT),
+                                                 M.gpart, M.loss_part, nullptr);
+  GB_LAUNCHED();
+  k_grad_reduce<<<nblocks(NPARAM, 256), 256, 0, g.stream>>>(nt, M.gpart, M.grad);
+  GB_LAUNCHED();
+  ++M.adam_t;
+  const float lr = 1e-3f;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.0f - std::pow(b1, (float)M.adam_t), c2 = 1.0f - std::pow(b2, (float)M.adam_t);
+  k_adam<<<nblocks(NPARAM, 256), 256, 0, g.stream>>>(M.master, M.m1, M.m2, M.grad, lr, b1, b2, c1, c2, 1e-8f);
+  GB_LAUNCHED();
+  publish(M.master, M.net);
+  prof_end(P_MLP_TRAIN);
+}
+
+void mts_begin_cycle() {
+  k_save_x0<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, g.x, g.y, g.z, M.x0);
+  GB_LAUNCHED();
+  k_copy_f<<<nblocks(3LL * g.natms, 256), 256, 0, g.stream>>>(3LL * g.natms, M.frec, M.frec0);
+  GB_LAUNCHED();
+  k_copy_f<<<nblocks(3LL * g.natms, 256), 256, 0, g.stream>>>(3LL * g.natms, M.fc, M.fc0);
+  GB_LAUNCHED();
+  M.ec0 = M.ec; M.vc0 = M.vc;
+  for (int k = 0; k < 9; ++k) M.stc0[k] = M.stc[k];
+  M.s = 0;
+  M.have_t0 = true;
+}
+
+// smallest FFT length >= want that is 2^a 3^b 5^c and a multiple of 4
+int coarse_length(int want) {
+  for (int K = std::max(8, want);; ++K) {
+    if (K % 4) continue;
+    int m = K;
+    for (int f : {2, 3, 5})
+      while (m % f == 0) m /= f;
+    if (m == 1) return K;
+  }
+}
+
+bool training_now() { return M.step <= g.mts_train; }
+
+}  // namespace
+
+// ===================================================================== host
+void mts_set_topology(int ntcons, const int32_t* listcon, const double* weight) {
+  const int n = g.natms;
+  h_triple.assign(3 * (size_t)n, -1);
+  if (ntcons <= 0 || !listcon || !weight) return;
+  // atoms joined by constraints; molecules of exactly 3 atoms get a frame
+  std::vector<int> parent(n);
+  for (int i = 0; i < n; ++i) parent[i] = i;
+  auto find = [&](int a) {
+    while (parent[a] != a) a = parent[a] = parent[parent[a]];
+    return a;
+  };
+  for (int k = 0; k < ntcons; ++k) {
+    const int a = find(listcon[3 * k + 1] - 1), b = find(listcon[3 * k + 2] - 1);
+    if (a != b) parent[std::max(a, b)] = std::min(a, b);
+  }
+  std::vector<std::vector<int>> mol(n);
+  for (int i = 0; i < n; ++i) mol[find(i)].push_back(i);
+  for (int r = 0; r < n; ++r) {
+    const auto& m = mol[r];
+    if (m.size() != 3) continue;
+    int o = m[0];
+    for (int a : m)
+      if (weight[a] > weight[o]) o = a;
+    int h[2], nh = 0;
+    for (int a : m)
+      if (a != o) h[nh++] = a;
+    for (int a : m) {
+      h_triple[3 * a] = o; h_triple[3 * a + 1] = h[0]; h_triple[3 * a + 2] = h[1];
+    }
+  }
+}
+
+void mts_free() {
+  void* ptrs[] = {M.master, M.m1, M.m2, M.grad, M.gpart, M.loss_part, M.X, M.frec0, M.frec, M.truth, M.target,
+                  M.fc, M.fc0, M.x0, M.disp, M.frame, M.triple, M.scal, M.red, M.idx, M.sstart, M.scount,
+                  M.slist};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  net_free(M.net);
+  M = MtsDev();
+}
+
+void mts_setup() {
+  mts_free();
+  const int n = g.natms;
+  M.n = n;
+  set_attrs();
+  GB_CUDA(cudaMalloc(&M.master, sizeof(float) * NPARAM));
+  GB_CUDA(cudaMalloc(&M.m1, sizeof(float) * NPARAM));
+  GB_CUDA(cudaMalloc(&M.m2, sizeof(float) * NPARAM));
+  GB_CUDA(cudaMalloc(&M.grad, sizeof(float) * NPARAM));
+  GB_CUDA(cudaMemset(M.m1, 0, sizeof(float) * NPARAM));
+  GB_CUDA(cudaMemset(M.m2, 0, sizeof(float) * NPARAM));
+  M.batch = std::min(n, 8192);
+  M.gpart_tiles = nblocks(M.batch, TILE_T);
+  GB_CUDA(cudaMalloc(&M.gpart, sizeof(float) * NPARAM * (size_t)M.gpart_tiles));
+  GB_CUDA(cudaMalloc(&M.loss_part, sizeof(float) * M.gpart_tiles));
+  net_alloc(M.net);
+  GB_CUDA(cudaMalloc(&M.X, sizeof(__nv_bfloat16) * KIN * (size_t)n));
+  for (float** p : {&M.frec0, &M.frec, &M.truth, &M.target, &M.disp, &M.fc, &M.fc0})
+    GB_CUDA(cudaMalloc(p, sizeof(float) * 3 * (size_t)n));
+  // coarse grid: about half the main grid's points per dimension, order 6
+  for (int d = 0; d < 3; ++d) M.Kc[d] = coarse_length((g.p.kmax[d] + 1) / 2);
+  M.pc = 6;
+  spme_coarse_setup(M.Kc, M.pc);
+  GB_CUDA(cudaMalloc(&M.frame, sizeof(float) * 9 * (size_t)n));
+  GB_CUDA(cudaMalloc(&M.x0, sizeof(double) * 3 * (size_t)n));
+  GB_CUDA(cudaMalloc(&M.triple, sizeof(int) * 3 * (size_t)n));
+  GB_CUDA(cudaMalloc(&M.scal, sizeof(float) * (NIN + 1)));
+  GB_CUDA(cudaMalloc(&M.red, sizeof(double) * 8));
+  GB_CUDA(cudaMalloc(&M.idx, sizeof(int) * (size_t)M.batch));
+  GB_CUDA(cudaMalloc(&M.sstart, sizeof(int) * ((size_t)n + 1)));
+  GB_CUDA(cudaMalloc(&M.scount, sizeof(int) * ((size_t)n + 1)));
+  if ((int)h_triple.size() != 3 * n) h_triple.assign(3 * (size_t)n, -1);
+  GB_CUDA(cudaMemcpy(M.triple, h_triple.data(), sizeof(int) * 3 * (size_t)n, cudaMemcpyHostToDevice));
+  std::vector<float> sc(NIN + 1, 1.0f);
+  GB_CUDA(cudaMemcpy(M.scal, sc.data(), sizeof(float) * (NIN + 1), cudaMemcpyHostToDevice));
+  std::vector<float> w = initial_params();
+  GB_CUDA(cudaMemcpy(M.master, w.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice));
+  publish(M.master, M.net);
+  GB_CUDA(cudaStreamSynchronize(g.stream));
+  M.ready = true;
+}
+
+bool mts_active() { return M.ready && g.mts_k > 1; }
+
+void mts_set_stale_only(bool on) { g_stale_only = on; }
+
+// SPME writes its per-atom reciprocal forces here when MTS is active
+float* mts_rec_out() { return mts_active() ? M.frec : nullptr; }
+
+// at the start of the force evaluation of an MD step: the coarse-grid forces
+// of this step, and whether the step needs the full SPME
+bool mts_step_needs_spme() {
+  ++M.step;
+  double st[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  spme_coarse_forces(&M.ec, &M.vc, st, M.fc);
+  for (int k = 0; k < 9; ++k) M.stc[k] = st[k];
+  if (!M.have_t0) return true;
+  return training_now() || M.fallback || M.s + 1 >= g.mts_k;
+}
+
+// after a full force evaluation of an MD step (SPME ran, FP64 forces formed):
+// labels, the judge, training and the cycle bookkeeping
+void mts_after_full(double erc, double vrc, const double* strec) {
+  const int n = g.natms;
+  M.n_full++;
+  M.erc0 = erc; M.vrc0 = vrc;
+  for (int k = 0; k < 9; ++k) M.st0[k] = strec[k];
+  if (!M.have_t0) {
+    mts_begin_cycle();
+    return;
+  }
+  const int s_new = M.s + 1;
+  const bool cycle_end = s_new >= g.mts_k;
+  if (!M.scales_set) mts_set_scales();
+  else mts_inputs();
+  mts_labels();
+  if (cycle_end && (M.adam_t > 0 || g_stale_only)) {
+    // the judge: the network's prediction for this step against SPME
+    prof_begin(P_MLP);
+    if (g_stale_only) {
+      k_copy_f<<<nblocks(3LL * n, 256), 256, 0, g.stream>>>(3LL * n, M.frec0, M.truth);
+      GB_LAUNCHED();
+    } else {
+      launch_infer(n, M.X, M.net, M.frec0, M.frame, M.scal, M.truth);
+    }
+    const int nb = nblocks(n, 256);
+    double* blk = gb_blkacc(nb * 4);
+    k_err3<<<nb, 256, 0, g.stream>>>(n, M.truth, M.fc, M.fc0, M.frec0, M.frec, blk);
+    GB_LAUNCHED();
+    k_fsq<<<nb, 256, 0, g.stream>>>(n, g.fx, g.fy, g.fz, blk + 3 * nb);
+    GB_LAUNCHED();
+    gb_reduce_blocks(blk, nb, 3, M.red);
+    gb_reduce_blocks(blk + 3 * nb, nb, 1, M.red + 3);
+    prof_end(P_MLP);
+    double r4[4];
+    read_scalars(M.red, r4, 4);
+    const double ftot = std::max(std::sqrt(r4[3] / n), 1e-300);
+    const double err = std::sqrt(r4[0] / n) / ftot;
+    M.err_coarse = std::sqrt(r4[1] / n) / ftot;
+    M.err_stale = std::sqrt(r4[2] / n) / ftot;
+    M.last_err = err;
+    M.err_max = std::max(M.err_max, err);
+    M.n_judged++;
+    if (!training_now()) {
+      const bool was = M.fallback;
+      M.fallback = err > g.mts_tol;
+      if (M.fallback && !was) M.n_fallback++;
+    }
+  }
+  if ((training_now() || M.fallback) && !g_stale_only) {
+    mts_train_step();
+    std::vector<float> lp(M.gpart_tiles);
+    GB_CUDA(cudaMemcpyAsync(lp.data(), M.loss_part, sizeof(float) * lp.size(), cudaMemcpyDeviceToHost, g.stream));
+    GB_CUDA(cudaStreamSynchronize(g.stream));
+    double l = 0.0;
+    for (float v : lp) l += v;
+    M.last_loss = l;
+  }
+  if (cycle_end) mts_begin_cycle();
+  else M.s = s_new;
+}
+
+// inner step: predicted reciprocal force into the fixed-point forces; the
+// reciprocal energy, virial and stress are those of t0 plus the coarse-grid
+// increments since t0
+void mts_inner(double* erc, double* vrc, double* stress9) {
+  const int n = g.natms;
+  mts_inputs();
+  prof_begin(P_MLP);
+  if (g_stale_only) {
+    k_copy_f<<<nblocks(3LL * n, 256), 256, 0, g.stream>>>(3LL * n, M.frec0, M.frec);
+    GB_LAUNCHED();
+  } else {
+    launch_infer(n, M.X, M.net, M.frec0, M.frame, M.scal, M.frec);
+  }
+  const int nb = nblocks(n, 256);
+  double* blk = gb_blkacc(nb * 3);
+  k_net3<<<nb, 256, 0, g.stream>>>(n, M.frec, M.frec0, blk);
+  GB_LAUNCHED();
+  gb_reduce_blocks(blk, nb, 3, M.red);
+  k_mts_apply<<<nb, 256, 0, g.stream>>>(n, M.frec, M.fc, M.fc0, M.red, 1.0f / (float)n, (unsigned long long*)g.fixp);
+  GB_LAUNCHED();
+  prof_end(P_MLP);
+  *erc = M.erc0 + (M.ec - M.ec0);
+  *vrc = M.vrc0 + (M.vc - M.vc0);
+  for (int k = 0; k < 9; ++k) stress9[k] += M.st0[k] + (M.stc[k] - M.stc0[k]);
+  M.n_inner++;
+  M.s++;
+}
+
+void mts_stats(double* out, int nv) {
+  const double v[13] = {M.last_err, (double)M.n_full, (double)M.n_inner, (double)M.n_fallback, M.last_loss,
+                        (double)M.adam_t, M.err_max, M.fallback ? 1.0 : 0.0, (double)M.n_judged, (double)M.step,
+                        M.err_coarse, M.err_stale, (double)M.Kc[0]};
+  for (int k = 0; k < nv && k < 13; ++k) out[k] = v[k];
+}
+
+// ---------------------------------------------------------------- test hooks
+// forward + MSE + backward of the training kernel on nb given rows
+int mlp_train_eval(int nb, const float* x, const float* target, const float* params, float* loss, float* grad,
+                   float* yout) {
+  if (nb <= 0 || nb > 65536 || !x || !target || !params || !loss || !grad || !yout) return GB_ERR_ARG;
+  set_attrs();
+  const int nt = nblocks(nb, TILE_T);
+  std::vector<__nv_bfloat16> hx((size_t)nb * KIN);
+  for (int r = 0; r < nb; ++r)
+    for (int c = 0; c < KIN; ++c) hx[(size_t)r * KIN + c] = __float2bfloat16(c < NIN ? x[(size_t)r * NIN + c] : 0.f);
+  std::vector<int> hi(nb);
+  for (int r = 0; r < nb; ++r) hi[r] = r;
+  __nv_bfloat16* dX = nullptr;
+  float *dT = nullptr, *dP = nullptr, *dG = nullptr, *dGp = nullptr, *dL = nullptr, *dY = nullptr;
+  int* dI = nullptr;
+  GB_CUDA(cudaMalloc(&dX, sizeof(__nv_bfloat16) * hx.size()));
+  GB_CUDA(cudaMalloc(&dT, sizeof(float) * 3 * nb));
+  GB_CUDA(cudaMalloc(&dP, sizeof(float) * NPARAM));
+  GB_CUDA(cudaMalloc(&dG, sizeof(float) * NPARAM));
+  GB_CUDA(cudaMalloc(&dGp, sizeof(float) * NPARAM * (size_t)nt));
+  GB_CUDA(cudaMalloc(&dL, sizeof(float) * nt));
+  GB_CUDA(cudaMalloc(&dY, sizeof(float) * 3 * nb));
+  GB_CUDA(cudaMalloc(&dI, sizeof(int) * nb));
+  GB_CUDA(cudaMemcpy(dX, hx.data(), sizeof(__nv_bfloat16) * hx.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(dT, target, sizeof(float) * 3 * nb, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(dP, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(dI, hi.data(), sizeof(int) * nb, cudaMemcpyHostToDevice));
+  k_mlp_train<<<nt, 256, train_smem, g.stream>>>(nb, dI, dX, dT, dP, 1.0f / (float)(nb * NOUT), dGp, dL, dY);
+  GB_LAUNCHED();
+  k_grad_reduce<<<nblocks(NPARAM, 256), 256, 0, g.stream>>>(nt, dGp, dG);
+  GB_LAUNCHED();
+  std::vector<float> hl(nt);
+  GB_CUDA(cudaMemcpyAsync(grad, dG, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g.stream));
+  GB_CUDA(cudaMemcpyAsync(hl.data(), dL, sizeof(float) * nt, cudaMemcpyDeviceToHost, g.stream));
+  GB_CUDA(cudaMemcpyAsync(yout, dY, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost, g.stream));
+  GB_CUDA(cudaStreamSynchronize(g.stream));
+  float l = 0.f;
+  for (float v : hl) l += v;
+  *loss = l;
+  for (void* p : {(void*)dX, (void*)dT, (void*)dP, (void*)dG, (void*)dGp, (void*)dL, (void*)dY, (void*)dI}) cudaFree(p);
+  return GB_OK;
+}
+
+// the inference kernel on nb given rows (lab frame, zero base force, unit scales)
+int mlp_infer_eval(int nb, const float* x, const float* params, float* yout) {
+  if (nb <= 0 || nb > (1 << 22) || !x || !params || !yout) return GB_ERR_ARG;
+  set_attrs();
+  Net net;
+  net_alloc(net);
+  float* dP = nullptr;
+  GB_CUDA(cudaMalloc(&dP, sizeof(float) * NPARAM));
+  GB_CUDA(cudaMemcpy(dP, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice));
+  publish(dP, net);
+  std::vector<__nv_bfloat16> hx((size_t)nb * KIN);
+  for (int r = 0; r < nb; ++r)
+    for (int c = 0; c < KIN; ++c) hx[(size_t)r * KIN + c] = __float2bfloat16(c < NIN ? x[(size_t)r * NIN + c] : 0.f);
+  std::vector<float> fr(9 * (size_t)nb, 0.f), sc(NIN + 1, 1.f);
+  for (int r = 0; r < nb; ++r) { fr[9 * (size_t)r] = 1.f; fr[9 * (size_t)r + 4] = 1.f; fr[9 * (size_t)r + 8] = 1.f; }
+  __nv_bfloat16* dX = nullptr;
+  float *dF0 = nullptr, *dFr = nullptr, *dS = nullptr, *dOut = nullptr;
+  GB_CUDA(cudaMalloc(&dX, sizeof(__nv_bfloat16) * hx.size()));
+  GB_CUDA(cudaMalloc(&dF0, sizeof(float) * 3 * (size_t)nb));
+  GB_CUDA(cudaMalloc(&dFr, sizeof(float) * fr.size()));
+  GB_CUDA(cudaMalloc(&dS, sizeof(float) * sc.size()));
+  GB_CUDA(cudaMalloc(&dOut, sizeof(float) * 3 * (size_t)nb));
+  GB_CUDA(cudaMemcpy(dX, hx.data(), sizeof(__nv_bfloat16) * hx.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemset(dF0, 0, sizeof(float) * 3 * (size_t)nb));
+  GB_CUDA(cudaMemcpy(dFr, fr.data(), sizeof(float) * fr.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(dS, sc.data(), sizeof(float) * sc.size(), cudaMemcpyHostToDevice));
+  launch_infer(nb, dX, net, dF0, dFr, dS, dOut);
+  GB_CUDA(cudaMemcpyAsync(yout, dOut, sizeof(float) * 3 * (size_t)nb, cudaMemcpyDeviceToHost, g.stream));
+  GB_CUDA(cudaStreamSynchronize(g.stream));
+  for (void* p : {(void*)dP, (void*)dX, (void*)dF0, (void*)dFr, (void*)dS, (void*)dOut}) cudaFree(p);
+  net_free(net);
+  return GB_OK;
+}
+
+// copies the current inputs (nv <= natms rows of 51 floats) and the 52 scales
+int mts_features(float* x, int nv, float* scal) {
+  if (!M.ready) return GB_ERR_NOT_INIT;
+  if (nv < 0 || nv > g.natms || (nv > 0 && !x)) return GB_ERR_ARG;
+  GB_CUDA(cudaStreamSynchronize(g.stream));
+  std::vector<__nv_bfloat16> hx((size_t)nv * KIN);
+  if (nv > 0) GB_CUDA(cudaMemcpy(hx.data(), M.X, sizeof(__nv_bfloat16) * hx.size(), cudaMemcpyDeviceToHost));
+  for (int r = 0; r < nv; ++r)
+    for (int c = 0; c < NIN; ++c) x[(size_t)r * NIN + c] = __bfloat162float(hx[(size_t)r * KIN + c]);
+  if (scal) GB_CUDA(cudaMemcpy(scal, M.scal, sizeof(float) * (NIN + 1), cudaMemcpyDeviceToHost));
+  return GB_OK;
+}
+
+int mlp_param_count() { return NPARAM; }

@@ -305,9 +305,10 @@ constexpr float AS_A1 = 0.254829592f, AS_A2 = -0.284496736f, AS_A3 = 1.421413741
 constexpr int MAX_KEYS = 64;
 constexpr int MAX_TYPES = 10;  // 55 type-pair keys
 __constant__ float4 c_lj[MAX_KEYS];
-__global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __restrict__ fstart,
+__global__ void __launch_bounds__(256, 4) k_pair_mixed(int natms, const int* __restrict__ fstart,
                                                     const int* __restrict__ fcount, const int* __restrict__ flist,
-                                                    const float4* __restrict__ xf, const int* __restrict__ ltype,
+                                                    const float4* __restrict__ xf, const float4* __restrict__ xlo,
+                                                    const int* __restrict__ ltype,
                                                     int ntypes, float rc2, float rv2, float alpha,
                                                     float alpha2rsqrpi, float scaling,
                                                     unsigned long long* fixp, double* blk,
@@ -329,6 +330,7 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
   unsigned long long n_list = 0, n_rc = 0;
   for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < natms; i += nwarps) {
     const float4 pi = xf[i];
+    const float4 li = xlo[i];
     const float qi = pi.w * scaling;
     const int row = (ltype[i] - 1) * ntypes - 1;
     const int s = fstart[i], n = fcount[i];
@@ -339,7 +341,10 @@ __global__ void __launch_bounds__(256) k_pair_mixed(int natms, const int* __rest
     for (int m = lane; m < n; m += 32) {
       const int j = flist[s + m];
       const float4 pj = xf[j];
-      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      const float4 lj = xlo[j];
+      // separation from the hi + lo position pairs (antisymmetric in i, j)
+      const float dx = (pi.x - pj.x) + (li.x - lj.x), dy = (pi.y - pj.y) + (li.y - lj.y),
+                  dz = (pi.z - pj.z) + (li.z - lj.z);
       const float rsq = dx * dx + dy * dy + dz * dz;
       if (rsq >= rc2 && rsq >= rv2) continue;
       const float rinv = rsqrtf(rsq);
@@ -490,7 +495,8 @@ void pair_forces(double* eng6, double* stress9) {
     double* blk = gb_blkacc(nb * NACC + nb2 * 8);
     prof_begin(P_PAIR);
     const double a2rp = g.p.alpha * 2.0 / std::sqrt(3.14159265358979323846264338327950288);
-    k_pair_mixed<<<nb, T, 0, st>>>(g.natms, g.fstart, g.fcount, g.flist, g.xf, g.ltype, g.p.ntypes, (float)pg.rc2,
+    k_pair_mixed<<<nb, T, 0, st>>>(g.natms, g.fstart, g.fcount, g.flist, g.xf, g.xlo, g.ltype, g.p.ntypes,
+                                   (float)pg.rc2,
                                    (float)pg.rv2, (float)g.p.alpha, (float)a2rp, (float)pg.scaling,
                                    (unsigned long long*)g.fixp, blk, &g.sc->npairs_list);
     GB_LAUNCHED();

@@ -600,16 +600,15 @@ __global__ void k_spme_gather(int natms, const double* __restrict__ x, const dou
 // (j, k + 4) cover the p x p (x,y) rows for p = 8, so each warp load reads four
 // 8-wide rows (coalesced); lanes 0..2 build the splines of one dimension each
 // from the stored truncation-convention fraction.  No FP64 instruction.
+template <int P>
 __global__ void __launch_bounds__(256) k_spme_gather_f32(int natms, const float* __restrict__ q4, SpmeGeom sg,
                                                          const int* __restrict__ gidx, const float* __restrict__ gw,
                                                          const float* __restrict__ phi, float rk0, float rk1,
                                                          float rk2, float* __restrict__ fout, double* blk) {
-  constexpr int P = 8;
   __shared__ float sp[8][2][3][P];  // per warp: value/derivative, dimension, point
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
-  const int j = lane & 7, k0 = lane >> 3;
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < natms; i += nwarps) {
     const float qi = q4[4 * i + 3];
@@ -620,26 +619,29 @@ __global__ void __launch_bounds__(256) k_spme_gather_f32(int natms, const float*
     }
     __syncwarp();
     const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
-    int xx = gx + j; if (xx >= K0) xx -= K0;
-    int ya = gy + k0; if (ya >= K1) ya -= K1;
-    int yb = gy + k0 + 4; if (yb >= K1) yb -= K1;
-    const float mx = sp[wid][0][0][j], dmx = sp[wid][1][0][j];
-    const float mya = sp[wid][0][1][k0], dmya = sp[wid][1][1][k0];
-    const float myb = sp[wid][0][1][k0 + 4], dmyb = sp[wid][1][1][k0 + 4];
-    const float p0a = mx * mya, p1a = dmx * mya, p2a = mx * dmya;
-    const float p0b = mx * myb, p1b = dmx * myb, p2b = mx * dmyb;
     float e = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
+    // (x, y) pairs of the p x p rows: x fastest, so groups of p lanes read
+    // contiguous grid points
 #pragma unroll
-    for (int l = 0; l < P; ++l) {
-      int zz = gz + l; if (zz >= K2) zz -= K2;
-      const float* plane = phi + (size_t)zz * K1 * K0;
-      const float pa = plane[(size_t)ya * K0 + xx], pb = plane[(size_t)yb * K0 + xx];
-      const float mz = sp[wid][0][2][l], dmz = sp[wid][1][2][l];
-      const float ta = mz * pa, tb = mz * pb, ua = dmz * pa, ub = dmz * pb;
-      e = fmaf(p0a, ta, fmaf(p0b, tb, e));
-      fx = fmaf(p1a, ta, fmaf(p1b, tb, fx));
-      fy = fmaf(p2a, ta, fmaf(p2b, tb, fy));
-      fz = fmaf(p0a, ua, fmaf(p0b, ub, fz));
+    for (int pr = lane; pr < P * P; pr += 32) {
+      const int j = pr % P, k = pr / P;
+      int xx = gx + j; if (xx >= K0) xx -= K0;
+      int yy = gy + k; if (yy >= K1) yy -= K1;
+      const float mx = sp[wid][0][0][j], dmx = sp[wid][1][0][j];
+      const float my = sp[wid][0][1][k], dmy = sp[wid][1][1][k];
+      const float p0 = mx * my, p1 = dmx * my, p2 = mx * dmy;
+      const float* col = phi + (size_t)yy * K0 + xx;
+#pragma unroll
+      for (int l = 0; l < P; ++l) {
+        int zz = gz + l; if (zz >= K2) zz -= K2;
+        const float pa = col[(size_t)zz * K1 * K0];
+        const float mz = sp[wid][0][2][l], dmz = sp[wid][1][2][l];
+        const float ta = mz * pa;
+        e = fmaf(p0, ta, e);
+        fx = fmaf(p1, ta, fx);
+        fy = fmaf(p2, ta, fy);
+        fz = fmaf(p0, dmz * pa, fz);
+      }
     }
     e = warp_sumf(e); fx = warp_sumf(fx); fy = warp_sumf(fy); fz = warp_sumf(fz);
     const float f0 = -qi * fx * rk0, f1 = -qi * fy * rk1, f2 = -qi * fz * rk2;
@@ -654,14 +656,18 @@ __global__ void __launch_bounds__(256) k_spme_gather_f32(int natms, const float*
 
 // mixed form: forces += (F - Fnet/N) * 2 * scale as 2^40 fixed point (FP32 math)
 __global__ void k_spme_apply_fix_f32(int natms, const float* __restrict__ f, const double* __restrict__ sums,
-                                     float scale2, float rn, unsigned long long* fixp) {
+                                     float scale2, float rn, unsigned long long* fixp, float* rec) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natms) return;
   // the three net-force means are read as FP64 and converted once per thread
   const float m0 = (float)sums[1] * rn, m1 = (float)sums[2] * rn, m2 = (float)sums[3] * rn;
-  atomicAdd(&fixp[3 * i + 0], (unsigned long long)fix40((f[3 * i] - m0) * scale2));
-  atomicAdd(&fixp[3 * i + 1], (unsigned long long)fix40((f[3 * i + 1] - m1) * scale2));
-  atomicAdd(&fixp[3 * i + 2], (unsigned long long)fix40((f[3 * i + 2] - m2) * scale2));
+  const float v0 = (f[3 * i] - m0) * scale2, v1 = (f[3 * i + 1] - m1) * scale2, v2 = (f[3 * i + 2] - m2) * scale2;
+  if (fixp) {
+    atomicAdd(&fixp[3 * i + 0], (unsigned long long)fix40(v0));
+    atomicAdd(&fixp[3 * i + 1], (unsigned long long)fix40(v1));
+    atomicAdd(&fixp[3 * i + 2], (unsigned long long)fix40(v2));
+  }
+  if (rec) { rec[3 * i] = v0; rec[3 * i + 1] = v1; rec[3 * i + 2] = v2; }  // learned-MTS per-atom forces
 }
 
 // forces += (F - Fnet/N) * 2 * scale
@@ -676,13 +682,14 @@ __global__ void k_spme_apply(int natms, const double* __restrict__ f, const doub
 }
 
 __global__ void k_spme_apply_fix(int natms, const double* __restrict__ f, const double* __restrict__ sums,
-                                 double scale2, double rn, unsigned long long* fixp) {
+                                 double scale2, double rn, unsigned long long* fixp, float* rec) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natms) return;
   const double s = 1099511627776.0;
   for (int d = 0; d < 3; ++d) {
     double v = (f[3 * i + d] - sums[1 + d] * rn) * scale2;
-    atomicAdd(&fixp[3 * i + d], (unsigned long long)__double2ll_rn(v * s));
+    if (fixp) atomicAdd(&fixp[3 * i + d], (unsigned long long)__double2ll_rn(v * s));
+    if (rec) rec[3 * i + d] = (float)v;
   }
 }
 
@@ -706,12 +713,37 @@ FftPlan make_plan(int N) {
   return pl;
 }
 
-FftPlan plan1, plan2, plan3;
-SpmeGeom h_sg;
-void* g_spread_ext = nullptr;  // per-brick spread tiles (nbricks x (B+p-1)^3)
-int* g_gidx = nullptr;         // mixed gather: first grid index per dimension (truncation convention)
-float* g_gw = nullptr;         // mixed gather: fractional coordinate per dimension
-float* g_fout_f = nullptr;     // mixed gather: unscaled reciprocal forces
+// One SPME grid: geometry, per-atom spline data, bricks, grids, influence
+// function and twiddles.  The force path owns the main grid (the CONTROL
+// kmax and spline order); the learned multiple-time-step form adds a coarse
+// FP32 grid whose increments carry the long-range change of the reciprocal
+// force between full steps.
+struct SpmeGrid {
+  bool ready = false;
+  bool fp64 = true;  // FP64 grid buffers allocated (main grid only)
+  int K[3] = {0, 0, 0}, B[3] = {0, 0, 0}, nb[3] = {0, 0, 0}, nbricks = 0, p = 0;
+  FftPlan plan[3];
+  SpmeGeom sg;
+  double* spl = nullptr;       // natms * 3 * p splines (floor convention; FP32 view in the mixed form)
+  int* nidx = nullptr;         // natms * 3 grid indices
+  int *brick_of = nullptr, *brick_count = nullptr, *brick_start = nullptr, *brick_fill = nullptr,
+      *brick_atoms = nullptr;
+  double* Q = nullptr;
+  double2* G = nullptr;
+  float* Qf = nullptr;
+  float2* Gf = nullptr;
+  double *theta = nullptr, *psi = nullptr;
+  float *theta_f = nullptr, *psi_f = nullptr;
+  double2* tw[3] = {nullptr, nullptr, nullptr};
+  float2* twf[3] = {nullptr, nullptr, nullptr};
+  double* fspme = nullptr;     // 3*natms reciprocal forces (before scale, net removal)
+  void* spread_ext = nullptr;  // per-brick spread tiles (nbricks x (B+p-1)^3)
+  int* gidx = nullptr;         // warp gather: first grid index per dimension (truncation convention)
+  float* gw = nullptr;         // warp gather: fractional coordinate per dimension
+  float* fout_f = nullptr;     // warp gather: unscaled reciprocal forces
+};
+
+SpmeGrid S_main, S_coarse;
 
 int choose_brick(int K, int p) {
   for (int B = p - 1; B <= BMAX; ++B)
@@ -727,61 +759,82 @@ extern void invert_host(const double* a, double* b, double* d);
 extern void dcell_host(const double* aaa, double* bbb);
 
 // ====================================================================== host
-void spme_setup() {
-  const int p = g.p.nsplines;
+namespace {
+
+// raise a kernel's dynamic shared-memory limit, never lowering a larger
+// setting made for the other grid
+template <typename K>
+void raise_smem(K kernel, int bytes) {
+  cudaFuncAttributes a;
+  GB_CUDA(cudaFuncGetAttributes(&a, kernel));
+  if (a.maxDynamicSharedSizeBytes < bytes)
+    GB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+}
+
+void grid_free(SpmeGrid& S) {
+  void* ptrs[] = {S.spl, S.nidx, S.brick_of, S.brick_count, S.brick_start, S.brick_fill, S.brick_atoms, S.Q, S.G,
+                  S.Qf, S.Gf, S.theta, S.psi, S.theta_f, S.psi_f, S.tw[0], S.tw[1], S.tw[2], S.twf[0], S.twf[1],
+                  S.twf[2], S.fspme, S.spread_ext, S.gidx, S.gw, S.fout_f};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  S = SpmeGrid();
+}
+
+// grid of K[0..2] points and spline order p; fp64 = also the FP64 buffers
+void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
+  grid_free(S);
   if (p > PMAX || p < 3) throw (int)GB_ERR_ARG;
-  g.K1 = g.p.kmax[0]; g.K2 = g.p.kmax[1]; g.K3 = g.p.kmax[2];
-  if (g.K1 % TX || g.K2 % TX) throw (int)GB_ERR_ARG;
-  plan1 = make_plan(g.K1); plan2 = make_plan(g.K2); plan3 = make_plan(g.K3);
-  int Bs[3] = {choose_brick(g.K1, p), choose_brick(g.K2, p), choose_brick(g.K3, p)};
+  for (int d = 0; d < 3; ++d) S.K[d] = Kin[d];
+  if (S.K[0] % TX || S.K[1] % TX) throw (int)GB_ERR_ARG;
+  S.p = p;
+  S.fp64 = fp64;
+  for (int d = 0; d < 3; ++d) S.plan[d] = make_plan(S.K[d]);
   for (int d = 0; d < 3; ++d) {
-    if (Bs[d] < 0) {
+    S.B[d] = choose_brick(S.K[d], p);
+    if (S.B[d] < 0) {
       // fall back to the whole dimension as one brick if it is small enough
-      if (g.p.kmax[d] <= BMAX) Bs[d] = g.p.kmax[d];
+      if (S.K[d] <= BMAX) S.B[d] = S.K[d];
       else throw (int)GB_ERR_ARG;
     }
+    S.nb[d] = S.K[d] / S.B[d];
   }
-  g.B1 = Bs[0]; g.B2 = Bs[1]; g.B3 = Bs[2];
-  g.nb1 = g.K1 / g.B1; g.nb2 = g.K2 / g.B2; g.nb3 = g.K3 / g.B3;
-  g.nbricks = g.nb1 * g.nb2 * g.nb3;
+  S.nbricks = S.nb[0] * S.nb[1] * S.nb[2];
   double det;
-  invert_host(g.cell, h_sg.rc, &det);
+  invert_host(g.cell, S.sg.rc, &det);
   for (int d = 0; d < 3; ++d) {
-    h_sg.K[d] = g.p.kmax[d];
-    h_sg.Kr[d] = (double)g.p.kmax[d];
+    S.sg.K[d] = S.K[d];
+    S.sg.Kr[d] = (double)S.K[d];
+    S.sg.B[d] = S.B[d];
+    S.sg.nb[d] = S.nb[d];
   }
-  h_sg.B[0] = g.B1; h_sg.B[1] = g.B2; h_sg.B[2] = g.B3;
-  h_sg.nb[0] = g.nb1; h_sg.nb[1] = g.nb2; h_sg.nb[2] = g.nb3;
-  h_sg.p = p;
-  const size_t NG = (size_t)g.K1 * g.K2 * g.K3;
-  GB_CUDA(cudaMalloc(&g.spl, sizeof(double) * (size_t)g.natms * 3 * p));
-  GB_CUDA(cudaMalloc(&g.nidx, sizeof(int) * 3 * (size_t)g.natms));
-  GB_CUDA(cudaMalloc(&g.brick_of, sizeof(int) * (size_t)g.natms));
-  GB_CUDA(cudaMalloc(&g.brick_count, sizeof(int) * (g.nbricks + 2)));
-  GB_CUDA(cudaMalloc(&g.brick_start, sizeof(int) * (g.nbricks + 2)));
-  GB_CUDA(cudaMalloc(&g.brick_fill, sizeof(int) * (g.nbricks + 2)));
-  GB_CUDA(cudaMalloc(&g.brick_atoms, sizeof(int) * (size_t)g.natms));
-  GB_CUDA(cudaMalloc(&g.Q, sizeof(double) * NG));
-  GB_CUDA(cudaMalloc(&g.G, sizeof(double2) * NG));
-  GB_CUDA(cudaMalloc(&g.theta, sizeof(double) * NG));
-  GB_CUDA(cudaMalloc(&g.psi, sizeof(double) * NG));
-  GB_CUDA(cudaMalloc(&g.fspme, sizeof(double) * 3 * (size_t)g.natms));
-  if (g_gidx) { cudaFree(g_gidx); cudaFree(g_gw); cudaFree(g_fout_f); }
-  GB_CUDA(cudaMalloc(&g_gidx, sizeof(int) * 3 * (size_t)g.natms));
-  GB_CUDA(cudaMalloc(&g_gw, sizeof(float) * 3 * (size_t)g.natms));
-  GB_CUDA(cudaMalloc(&g_fout_f, sizeof(float) * 3 * (size_t)g.natms));
+  S.sg.p = p;
+  const size_t NG = (size_t)S.K[0] * S.K[1] * S.K[2];
+  const size_t n = (size_t)g.natms;
+  GB_CUDA(cudaMalloc(&S.spl, sizeof(double) * n * 3 * p));
+  GB_CUDA(cudaMalloc(&S.nidx, sizeof(int) * 3 * n));
+  GB_CUDA(cudaMalloc(&S.brick_of, sizeof(int) * n));
+  GB_CUDA(cudaMalloc(&S.brick_count, sizeof(int) * (S.nbricks + 2)));
+  GB_CUDA(cudaMalloc(&S.brick_start, sizeof(int) * (S.nbricks + 2)));
+  GB_CUDA(cudaMalloc(&S.brick_fill, sizeof(int) * (S.nbricks + 2)));
+  GB_CUDA(cudaMalloc(&S.brick_atoms, sizeof(int) * n));
+  GB_CUDA(cudaMalloc(&S.theta, sizeof(double) * NG));
+  GB_CUDA(cudaMalloc(&S.psi, sizeof(double) * NG));
+  if (fp64) {
+    GB_CUDA(cudaMalloc(&S.Q, sizeof(double) * NG));
+    GB_CUDA(cudaMalloc(&S.G, sizeof(double2) * NG));
+  }
+  GB_CUDA(cudaMalloc(&S.fspme, sizeof(double) * 3 * n));
+  GB_CUDA(cudaMalloc(&S.gidx, sizeof(int) * 3 * n));
+  GB_CUDA(cudaMalloc(&S.gw, sizeof(float) * 3 * n));
+  GB_CUDA(cudaMalloc(&S.fout_f, sizeof(float) * 3 * n));
   {
-    const size_t tsize = (size_t)(g.B1 + p - 1) * (g.B2 + p - 1) * (g.B3 + p - 1);
-    if (g_spread_ext) cudaFree(g_spread_ext);
-    GB_CUDA(cudaMalloc(&g_spread_ext, sizeof(double) * tsize * g.nbricks));
-    const int sm64 = (int)spread_smem(g.B1, g.B2, g.B3, p, sizeof(double));
-    const int sm32 = (int)spread_smem(g.B1, g.B2, g.B3, p, sizeof(float));
-    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64));
-    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32));
-    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_fix<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(tsize * sizeof(long long))));
-    GB_CUDA(cudaFuncSetAttribute(k_spme_spread_fix<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(tsize * sizeof(long long))));
+    const size_t tsize = (size_t)(S.B[0] + p - 1) * (S.B[1] + p - 1) * (S.B[2] + p - 1);
+    GB_CUDA(cudaMalloc(&S.spread_ext, sizeof(double) * tsize * S.nbricks));
+    raise_smem(k_spme_spread_tile<double>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(double)));
+    raise_smem(k_spme_spread_tile<float>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
+    raise_smem(k_spme_spread_fix<8>, (int)(tsize * sizeof(long long)));
+    raise_smem(k_spme_spread_fix<6>, (int)(tsize * sizeof(long long)));
+    raise_smem(k_spme_spread_fix<0>, (int)(tsize * sizeof(long long)));
   }
   // |b(m)|^2 (bspline_coeffs_gen, bspline.F90:73-190) on the host in FP64
   std::vector<double> norm2[3];
@@ -792,7 +845,7 @@ void spme_setup() {
       for (int j = k; j >= 2; --j) cs[j] = ((double)(j - 1) * cs[j] + (double)(k - j + 1) * cs[j - 1]) * (1.0 / (double)(k - 1));
     const double twopi = 2.0 * 3.14159265358979323846264338327950288;
     for (int d = 0; d < 3; ++d) {
-      int K = g.p.kmax[d];
+      int K = S.K[d];
       std::vector<double> wr(K), wi(K);
       wr[0] = 1.0; wi[0] = 0.0;
       for (int i = 1; i <= K / 2; ++i) {
@@ -824,20 +877,21 @@ void spme_setup() {
     dcell_host(rc, rcp);
     double recip_conv_fac = pi / g.p.alpha;
     double test_fac = (1.0e-6 / recip_conv_fac) * (1.0e-6 / recip_conv_fac);
-    double cut = 0.5 * 1.05 * std::min((double)g.K1 * rcp[6], std::min((double)g.K2 * rcp[7], (double)g.K3 * rcp[8]));
+    double cut = 0.5 * 1.05 * std::min((double)S.K[0] * rcp[6], std::min((double)S.K[1] * rcp[7], (double)S.K[2] * rcp[8]));
     double cut2 = cut * cut;
     std::vector<double> th(NG), ps(NG);
-    for (int l = 0; l < g.K3; ++l) {
-      int ll = l; if (2 * ll > g.K3) ll -= g.K3;
-      for (int k = 0; k < g.K2; ++k) {
-        int kk = k; if (2 * kk > g.K2) kk -= g.K2;
-        for (int j = 0; j < g.K1; ++j) {
-          int jj = j; if (2 * jj > g.K1) jj -= g.K1;
+    const int K1 = S.K[0], K2 = S.K[1], K3 = S.K[2];
+    for (int l = 0; l < K3; ++l) {
+      int ll = l; if (2 * ll > K3) ll -= K3;
+      for (int k = 0; k < K2; ++k) {
+        int kk = k; if (2 * kk > K2) kk -= K2;
+        for (int j = 0; j < K1; ++j) {
+          int jj = j; if (2 * jj > K1) jj -= K1;
           double r0 = (double)ll * rc[2] + (double)kk * rc[1] + (double)jj * rc[0];
           double r1 = (double)ll * rc[5] + (double)kk * rc[4] + (double)jj * rc[3];
           double r2 = (double)ll * rc[8] + (double)kk * rc[7] + (double)jj * rc[6];
           double k2 = r0 * r0 + r1 * r1 + r2 * r2;
-          size_t gi = ((size_t)k * g.K1 + j) * g.K3 + l;  // z-contiguous per (x,y) line for the z pass
+          size_t gi = ((size_t)k * K1 + j) * K3 + l;  // z-contiguous per (x,y) line for the z pass
           if (k2 <= cut2 && k2 > test_fac) {
             double bb = norm2[2][l] * norm2[1][k] * norm2[0][j];
             double f = std::sqrt(k2) * recip_conv_fac;
@@ -849,8 +903,8 @@ void spme_setup() {
         }
       }
     }
-    GB_CUDA(cudaMemcpy(g.theta, th.data(), sizeof(double) * NG, cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemcpy(g.psi, ps.data(), sizeof(double) * NG, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(S.theta, th.data(), sizeof(double) * NG, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(S.psi, ps.data(), sizeof(double) * NG, cudaMemcpyHostToDevice));
   }
   // twiddles e^{+2 pi i t / K}
   auto mk_tw = [](int K, double2** dd, float2** df) {
@@ -867,150 +921,165 @@ void spme_setup() {
     GB_CUDA(cudaMemcpy(*dd, t.data(), sizeof(double2) * K, cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(*df, tf.data(), sizeof(float2) * K, cudaMemcpyHostToDevice));
   };
-  mk_tw(g.K1, &g.tw1, &g.tw1f);
-  mk_tw(g.K2, &g.tw2, &g.tw2f);
-  mk_tw(g.K3, &g.tw3, &g.tw3f);
+  for (int d = 0; d < 3; ++d) mk_tw(S.K[d], &S.tw[d], &S.twf[d]);
   // FP32 copies for the mixed form
-  GB_CUDA(cudaMalloc(&g.Qf, sizeof(float) * NG));
-  GB_CUDA(cudaMalloc(&g.Gf, sizeof(float2) * NG));
-  GB_CUDA(cudaMalloc(&g.theta_f, sizeof(float) * NG));
-  GB_CUDA(cudaMalloc(&g.psi_f, sizeof(float) * NG));
-  k_cvt<float><<<nblocks((long long)NG, 256), 256, 0, g.stream>>>(g.theta, g.theta_f, NG);
+  GB_CUDA(cudaMalloc(&S.Qf, sizeof(float) * NG));
+  GB_CUDA(cudaMalloc(&S.Gf, sizeof(float2) * NG));
+  GB_CUDA(cudaMalloc(&S.theta_f, sizeof(float) * NG));
+  GB_CUDA(cudaMalloc(&S.psi_f, sizeof(float) * NG));
+  k_cvt<float><<<nblocks((long long)NG, 256), 256, 0, g.stream>>>(S.theta, S.theta_f, NG);
   GB_LAUNCHED();
-  k_cvt<float><<<nblocks((long long)NG, 256), 256, 0, g.stream>>>(g.psi, g.psi_f, NG);
+  k_cvt<float><<<nblocks((long long)NG, 256), 256, 0, g.stream>>>(S.psi, S.psi_f, NG);
   GB_LAUNCHED();
   // dynamic shared memory limits
-  const int maxN = std::max(g.K1, std::max(g.K2, g.K3));
-  int smem = (int)std::max(fft_smem(maxN, TX, sizeof(double2)), fft_smem(g.K1, 8, sizeof(double2)));
+  const int maxN = std::max(S.K[0], std::max(S.K[1], S.K[2]));
+  int smem = (int)std::max(fft_smem(maxN, TX, sizeof(double2)), fft_smem(S.K[0], 8, sizeof(double2)));
   smem = std::max(smem, 48 * 1024);
-  GB_CUDA(cudaFuncSetAttribute(k_fft_x_fwd<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_x_inv<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_y<double, double2, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_y<double, double2, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_z_conv<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_x_fwd<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_x_inv<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_y<float, float2, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_y<float, float2, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  GB_CUDA(cudaFuncSetAttribute(k_fft_z_conv<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  raise_smem(k_fft_x_fwd<double, double2>, smem);
+  raise_smem(k_fft_x_inv<double, double2>, smem);
+  raise_smem(k_fft_y<double, double2, +1>, smem);
+  raise_smem(k_fft_y<double, double2, -1>, smem);
+  raise_smem(k_fft_z_conv<double, double2>, smem);
+  raise_smem(k_fft_x_fwd<float, float2>, smem);
+  raise_smem(k_fft_x_inv<float, float2>, smem);
+  raise_smem(k_fft_y<float, float2, +1>, smem);
+  raise_smem(k_fft_y<float, float2, -1>, smem);
+  raise_smem(k_fft_z_conv<float, float2>, smem);
+  GB_CUDA(cudaStreamSynchronize(g.stream));
+  S.ready = true;
 }
 
+// One reciprocal-space evaluation on grid S.  The main grid adds its forces
+// into the context's FP64 or fixed-point forces (and, when given, stores the
+// applied per-atom forces in rec); the coarse grid only stores them in rec.
 template <typename T, typename T2>
-static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
+void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_rc, double* stress9) {
   cudaStream_t st = g.stream;
-  const int n = g.natms, p = g.p.nsplines;
-  T* spl = reinterpret_cast<T*>(g.spl);
-  T* Q = std::is_same<T, double>::value ? reinterpret_cast<T*>(g.Q) : reinterpret_cast<T*>(g.Qf);
-  T2* G = std::is_same<T, double>::value ? reinterpret_cast<T2*>(g.G) : reinterpret_cast<T2*>(g.Gf);
-  const T* th = std::is_same<T, double>::value ? reinterpret_cast<const T*>(g.theta) : reinterpret_cast<const T*>(g.theta_f);
-  const T* ps = std::is_same<T, double>::value ? reinterpret_cast<const T*>(g.psi) : reinterpret_cast<const T*>(g.psi_f);
-  const T2* tw1 = std::is_same<T, double>::value ? reinterpret_cast<const T2*>(g.tw1) : reinterpret_cast<const T2*>(g.tw1f);
-  const T2* tw2 = std::is_same<T, double>::value ? reinterpret_cast<const T2*>(g.tw2) : reinterpret_cast<const T2*>(g.tw2f);
-  const T2* tw3 = std::is_same<T, double>::value ? reinterpret_cast<const T2*>(g.tw3) : reinterpret_cast<const T2*>(g.tw3f);
+  const int n = g.natms, p = S.p;
+  constexpr bool F64 = std::is_same<T, double>::value;
+  auto pid = [coarse](int id) {
+    if (!coarse) return id;
+    if (id == P_SPME_PREP) return (int)P_COARSE_PREP;
+    if (id == P_SPME_SPREAD) return (int)P_COARSE_SPREAD;
+    if (id == P_SPME_GATHER) return (int)P_COARSE_GATHER;
+    return (int)P_COARSE_FFT;
+  };
+  T* spl = reinterpret_cast<T*>(S.spl);
+  T* Q = F64 ? reinterpret_cast<T*>(S.Q) : reinterpret_cast<T*>(S.Qf);
+  T2* G = F64 ? reinterpret_cast<T2*>(S.G) : reinterpret_cast<T2*>(S.Gf);
+  const T* th = F64 ? reinterpret_cast<const T*>(S.theta) : reinterpret_cast<const T*>(S.theta_f);
+  const T* ps = F64 ? reinterpret_cast<const T*>(S.psi) : reinterpret_cast<const T*>(S.psi_f);
+  const T2* tw1 = F64 ? reinterpret_cast<const T2*>(S.tw[0]) : reinterpret_cast<const T2*>(S.twf[0]);
+  const T2* tw2 = F64 ? reinterpret_cast<const T2*>(S.tw[1]) : reinterpret_cast<const T2*>(S.twf[1]);
+  const T2* tw3 = F64 ? reinterpret_cast<const T2*>(S.tw[2]) : reinterpret_cast<const T2*>(S.twf[2]);
+  const int K1 = S.K[0], K2 = S.K[1], K3 = S.K[2];
   // splines + brick binning
-  GB_CUDA(cudaMemsetAsync(g.brick_count, 0, sizeof(int) * (g.nbricks + 2), st));
-  GB_CUDA(cudaMemsetAsync(g.brick_fill, 0, sizeof(int) * (g.nbricks + 2), st));
-  prof_begin(P_SPME_PREP);
-  const bool warp_gather = !std::is_same<T, double>::value && p == 8;
-  k_spme_prep<T><<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, h_sg, spl, g.nidx, g.brick_of,
-                                                   g.brick_count, warp_gather ? g_gidx : nullptr,
-                                                   warp_gather ? g_gw : nullptr);
+  GB_CUDA(cudaMemsetAsync(S.brick_count, 0, sizeof(int) * (S.nbricks + 2), st));
+  GB_CUDA(cudaMemsetAsync(S.brick_fill, 0, sizeof(int) * (S.nbricks + 2), st));
+  prof_begin(pid(P_SPME_PREP));
+  const bool warp_gather = !F64 && (p == 8 || p == 6);
+  k_spme_prep<T><<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, spl, S.nidx, S.brick_of,
+                                                   S.brick_count, warp_gather ? S.gidx : nullptr,
+                                                   warp_gather ? S.gw : nullptr);
   GB_LAUNCHED();
 
-  scan_exclusive(g.brick_count, g.brick_start, g.nbricks + 1);
+  scan_exclusive(S.brick_count, S.brick_start, S.nbricks + 1);
   int* tmp = gb_scan_scratch(n + 1);
-  k_brick_scatter<<<nblocks(n, 256), 256, 0, st>>>(n, g.brick_of, g.brick_start, g.brick_fill, tmp);
+  k_brick_scatter<<<nblocks(n, 256), 256, 0, st>>>(n, S.brick_of, S.brick_start, S.brick_fill, tmp);
   GB_LAUNCHED();
-  k_brick_sort<<<nblocks((long long)g.nbricks * 32, 256), 256, 0, st>>>(g.nbricks, g.brick_start, tmp, g.brick_atoms);
+  k_brick_sort<<<nblocks((long long)S.nbricks * 32, 256), 256, 0, st>>>(S.nbricks, S.brick_start, tmp, S.brick_atoms);
   GB_LAUNCHED();
-  prof_end(P_SPME_PREP);
+  prof_end(pid(P_SPME_PREP));
   // spreading: tile scatter per brick, then the fixed-order halo reduction
   {
-    T* ext = reinterpret_cast<T*>(g_spread_ext);
-    const size_t smem = spread_smem(g.B1, g.B2, g.B3, p, sizeof(T));
-    const size_t NG = (size_t)g.K1 * g.K2 * g.K3;
-    prof_begin(P_SPME_SPREAD);
-    if (std::is_same<T, double>::value) {
-      k_spme_spread_tile<T><<<g.nbricks, 512, smem, st>>>(h_sg, g.brick_start, g.brick_atoms, spl, g.nidx, g.chge,
+    T* ext = reinterpret_cast<T*>(S.spread_ext);
+    const size_t smem = spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(T));
+    const size_t NG = (size_t)K1 * K2 * K3;
+    prof_begin(pid(P_SPME_SPREAD));
+    if (F64) {
+      k_spme_spread_tile<T><<<S.nbricks, 512, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge,
                                                           ext);
       GB_LAUNCHED();
-      k_spme_tile_reduce<T><<<nblocks((long long)NG, 256), 256, 0, st>>>(h_sg, ext, Q);
+      k_spme_tile_reduce<T><<<nblocks((long long)NG, 256), 256, 0, st>>>(S.sg, ext, Q);
       GB_LAUNCHED();
     } else {
-      long long* exti = reinterpret_cast<long long*>(g_spread_ext);
-      const size_t tsz = (size_t)(g.B1 + p - 1) * (g.B2 + p - 1) * (g.B3 + p - 1);
-      if (p == 8)
-        k_spme_spread_fix<8><<<g.nbricks, 256, tsz * sizeof(long long), st>>>(
-            h_sg, g.brick_start, g.brick_atoms, reinterpret_cast<const float*>(spl), g.nidx, g.chge, exti);
-      else
-        k_spme_spread_fix<0><<<g.nbricks, 256, tsz * sizeof(long long), st>>>(
-            h_sg, g.brick_start, g.brick_atoms, reinterpret_cast<const float*>(spl), g.nidx, g.chge, exti);
+      long long* exti = reinterpret_cast<long long*>(S.spread_ext);
+      const size_t tsz = (size_t)(S.B[0] + p - 1) * (S.B[1] + p - 1) * (S.B[2] + p - 1);
+      auto kern = p == 8 ? k_spme_spread_fix<8> : (p == 6 ? k_spme_spread_fix<6> : k_spme_spread_fix<0>);
+      kern<<<S.nbricks, 256, tsz * sizeof(long long), st>>>(S.sg, S.brick_start, S.brick_atoms,
+                                                            reinterpret_cast<const float*>(spl), S.nidx, g.chge, exti);
       GB_LAUNCHED();
-      k_spme_tile_reduce_fix<<<nblocks((long long)NG, 256), 256, 0, st>>>(h_sg, exti, reinterpret_cast<float*>(Q));
+      k_spme_tile_reduce_fix<<<nblocks((long long)NG, 256), 256, 0, st>>>(S.sg, exti, reinterpret_cast<float*>(Q));
       GB_LAUNCHED();
     }
-    prof_end(P_SPME_SPREAD);
+    prof_end(pid(P_SPME_SPREAD));
   }
   // FFT + convolution
   const int lines = 8;
-  const int rows = g.K2 * g.K3;
-  prof_begin(P_FFT_XF);
-  k_fft_x_fwd<T, T2><<<nblocks(rows, lines), 256, fft_smem(g.K1, lines, sizeof(T2)), st>>>(Q, G, plan1, tw1, rows, lines);
+  const int rows = K2 * K3;
+  prof_begin(pid(P_FFT_XF));
+  k_fft_x_fwd<T, T2><<<nblocks(rows, lines), 256, fft_smem(K1, lines, sizeof(T2)), st>>>(Q, G, S.plan[0], tw1, rows,
+                                                                                          lines);
   GB_LAUNCHED();
-  prof_end(P_FFT_XF);
-  prof_begin(P_FFT_Y);
-  k_fft_y<T, T2, +1><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2);
+  prof_end(pid(P_FFT_XF));
+  prof_begin(pid(P_FFT_Y));
+  k_fft_y<T, T2, +1><<<(K1 / TX) * K3, 256, fft_smem(K2, TX, sizeof(T2)), st>>>(G, K1, K2, S.plan[1], tw2);
   GB_LAUNCHED();
-  prof_end(P_FFT_Y);
-  const int nbz = (g.K1 / TX) * g.K2;
-  double* blkz = gb_blkacc(nbz * 6 + nblocks(n, 128) * 4);
-  prof_begin(P_FFT_Z);
-  k_fft_z_conv<T, T2><<<nbz, 256, fft_smem(g.K3, TX, sizeof(T2)) + g.K3 * sizeof(T), st>>>(G, g.K1, g.K2, g.K3, plan3,
-                                                                                        tw3, th, ps, h_sg, blkz);
+  prof_end(pid(P_FFT_Y));
+  const int nbz = (K1 / TX) * K2;
+  double* blkz = gb_blkacc(nbz * 6 + nblocks((long long)n * 32, 128) * 4);
+  prof_begin(pid(P_FFT_Z));
+  k_fft_z_conv<T, T2><<<nbz, 256, fft_smem(K3, TX, sizeof(T2)) + K3 * sizeof(T), st>>>(G, K1, K2, K3, S.plan[2], tw3,
+                                                                                       th, ps, S.sg, blkz);
   GB_LAUNCHED();
-  prof_end(P_FFT_Z);
-  prof_begin(P_FFT_Y);
-  k_fft_y<T, T2, -1><<<(g.K1 / TX) * g.K3, 256, fft_smem(g.K2, TX, sizeof(T2)), st>>>(G, g.K1, g.K2, plan2, tw2);
+  prof_end(pid(P_FFT_Z));
+  prof_begin(pid(P_FFT_Y));
+  k_fft_y<T, T2, -1><<<(K1 / TX) * K3, 256, fft_smem(K2, TX, sizeof(T2)), st>>>(G, K1, K2, S.plan[1], tw2);
   GB_LAUNCHED();
-  prof_end(P_FFT_Y);
-  prof_begin(P_FFT_XI);
-  k_fft_x_inv<T, T2><<<nblocks(rows, lines), 256, fft_smem(g.K1, lines, sizeof(T2)), st>>>(G, Q, plan1, tw1, rows, lines);
+  prof_end(pid(P_FFT_Y));
+  prof_begin(pid(P_FFT_XI));
+  k_fft_x_inv<T, T2><<<nblocks(rows, lines), 256, fft_smem(K1, lines, sizeof(T2)), st>>>(G, Q, S.plan[0], tw1, rows,
+                                                                                          lines);
   GB_LAUNCHED();
-  prof_end(P_FFT_XI);
+  prof_end(pid(P_FFT_XI));
   // gather
   double rc[9];
-  for (int k = 0; k < 9; ++k) rc[k] = h_sg.rc[k];
+  for (int k = 0; k < 9; ++k) rc[k] = S.sg.rc[k];
   double rk[3];
-  for (int a = 0; a < 3; ++a) rk[a] = rc[a] * h_sg.Kr[0] + rc[a + 3] * h_sg.Kr[1] + rc[a + 6] * h_sg.Kr[2];
+  for (int a = 0; a < 3; ++a) rk[a] = rc[a] * S.sg.Kr[0] + rc[a + 3] * S.sg.Kr[1] + rc[a + 6] * S.sg.Kr[2];
   static int occ_g = 0;
-  if (!occ_g) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g, k_spme_gather_f32, 256, 0));
+  if (!occ_g) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g, k_spme_gather_f32<8>, 256, 0));
   const int nbg = warp_gather ? std::max(1, std::min(occ_g * g.nsm, nblocks((long long)n * 32, 256))) : nblocks(n, 128);
   double* blkg = blkz + (size_t)nbz * 6;
-  prof_begin(P_SPME_GATHER);
+  prof_begin(pid(P_SPME_GATHER));
   if (warp_gather) {
-    k_spme_gather_f32<<<nbg, 256, 0, st>>>(n, reinterpret_cast<const float*>(g.xf), h_sg, g_gidx, g_gw,
-                                            reinterpret_cast<const float*>(Q), (float)rk[0], (float)rk[1],
-                                            (float)rk[2], g_fout_f, blkg);
+    auto kern = p == 8 ? k_spme_gather_f32<8> : k_spme_gather_f32<6>;
+    kern<<<nbg, 256, 0, st>>>(n, reinterpret_cast<const float*>(g.xf), S.sg, S.gidx, S.gw,
+                              reinterpret_cast<const float*>(Q), (float)rk[0], (float)rk[1], (float)rk[2], S.fout_f,
+                              blkg);
   } else {
-    k_spme_gather<T><<<nbg, 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, h_sg, Q, rk[0], rk[1], rk[2], g.fspme, blkg);
+    k_spme_gather<T><<<nbg, 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, Q, rk[0], rk[1], rk[2], S.fspme, blkg);
   }
   GB_LAUNCHED();
-  prof_end(P_SPME_GATHER);
+  prof_end(pid(P_SPME_GATHER));
   gb_reduce_blocks(blkz, nbz, 6, &g.sc->acc[A_SPME_STR]);
   gb_reduce_blocks(blkg, nbg, 4, &g.sc->acc[A_GATHER]);
   const double pi = 3.14159265358979323846264338327950288;
   const double scale = pi * std::sqrt(pi) * std::pow(g.p.alpha, 1 - 3) * (0.5 / g.volm) * g.scaling;
-  if (g.precision == GB_FP64) {
-    k_spme_apply<<<nblocks(n, 256), 256, 0, st>>>(n, g.fspme, &g.sc->acc[A_GATHER], 2.0 * scale, 1.0 / (double)n,
+  unsigned long long* fixp = coarse ? nullptr : (unsigned long long*)g.fixp;
+  prof_begin(pid(P_SPME_GATHER));
+  if (F64) {
+    k_spme_apply<<<nblocks(n, 256), 256, 0, st>>>(n, S.fspme, &g.sc->acc[A_GATHER], 2.0 * scale, 1.0 / (double)n,
                                                    g.fx, g.fy, g.fz);
   } else if (warp_gather) {
-    k_spme_apply_fix_f32<<<nblocks(n, 256), 256, 0, st>>>(n, g_fout_f, &g.sc->acc[A_GATHER], (float)(2.0 * scale),
-                                                           (float)(1.0 / (double)n), (unsigned long long*)g.fixp);
+    k_spme_apply_fix_f32<<<nblocks(n, 256), 256, 0, st>>>(n, S.fout_f, &g.sc->acc[A_GATHER], (float)(2.0 * scale),
+                                                           (float)(1.0 / (double)n), fixp, rec);
   } else {
-    k_spme_apply_fix<<<nblocks(n, 256), 256, 0, st>>>(n, g.fspme, &g.sc->acc[A_GATHER], 2.0 * scale,
-                                                       1.0 / (double)n, (unsigned long long*)g.fixp);
+    k_spme_apply_fix<<<nblocks(n, 256), 256, 0, st>>>(n, S.fspme, &g.sc->acc[A_GATHER], 2.0 * scale,
+                                                       1.0 / (double)n, fixp, rec);
   }
   GB_LAUNCHED();
+  prof_end(pid(P_SPME_GATHER));
   gb_sync_scalars();
   const double* A = g.hsc->acc;
   double eng = A[A_GATHER] * scale;
@@ -1023,7 +1092,26 @@ static void spme_run(double* eng_rc, double* vir_rc, double* stress9) {
   *vir_rc = -(stt[0] + stt[4] + stt[8]);
 }
 
+}  // namespace
+
+void spme_setup() { grid_setup(S_main, g.p.kmax, g.p.nsplines, true); }
+
+void spme_free() {
+  grid_free(S_main);
+  grid_free(S_coarse);
+}
+
 void spme_forces(double* eng_rc, double* vir_rc, double* stress9) {
-  if (g.precision == GB_FP64) spme_run<double, double2>(eng_rc, vir_rc, stress9);
-  else spme_run<float, float2>(eng_rc, vir_rc, stress9);
+  float* rec = mts_rec_out();
+  if (g.precision == GB_FP64) grid_run<double, double2>(S_main, false, rec, eng_rc, vir_rc, stress9);
+  else grid_run<float, float2>(S_main, false, rec, eng_rc, vir_rc, stress9);
+}
+
+void spme_coarse_setup(const int* K, int p) { grid_setup(S_coarse, K, p, false); }
+
+bool spme_coarse_ready() { return S_coarse.ready; }
+
+void spme_coarse_forces(double* eng_rc, double* vir_rc, double* stress9, float* rec) {
+  if (!S_coarse.ready) throw (int)GB_ERR_NOT_INIT;
+  grid_run<float, float2>(S_coarse, true, rec, eng_rc, vir_rc, stress9);
 }

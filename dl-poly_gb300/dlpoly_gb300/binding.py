@@ -182,6 +182,69 @@ class PathLib:
     def finalize(self):
         self.fn["finalize"]()
 
+    # ------------------------------------------------ learned-MTS form (CUDA only)
+    def _opt(self, name, res, args):
+        f = getattr(self.lib, self.prefix + name)
+        f.restype = res
+        f.argtypes = args
+        return f
+
+    def mts_config(self, k: int, tol: float = 1e-4, train_steps: int = 0):
+        st = self._opt("mts_config", c_int, [c_int, ctypes.c_double, c_int])(k, tol, train_steps)
+        if st != 0:
+            raise PathError(st, self.prefix + "mts_config", self.strerror(st))
+
+    def mts_ablation(self, stale_only: bool):
+        st = self._opt("mts_ablation", c_int, [c_int])(1 if stale_only else 0)
+        if st != 0:
+            raise PathError(st, self.prefix + "mts_ablation", self.strerror(st))
+
+    MTS_KEYS = ("last_err", "n_full", "n_inner", "n_fallback", "last_loss", "opt_steps", "err_max",
+                "in_fallback", "n_checked", "md_steps", "err_no_network", "err_stale", "coarse_k")
+
+    def mts_stats(self) -> dict:
+        out = np.zeros(len(self.MTS_KEYS))
+        self._opt("mts_stats", c_int, [_d, c_int])(_ptr(out, _d), len(out))
+        return dict(zip(self.MTS_KEYS, out.tolist()))
+
+    def mts_features(self, n: int):
+        x = np.zeros((n, 51), np.float32)
+        sc = np.zeros(52, np.float32)
+        _f = POINTER(ctypes.c_float)
+        st = self._opt("mts_features", c_int, [_f, c_int, _f])(_ptr(x, _f), n, _ptr(sc, _f))
+        if st != 0:
+            raise PathError(st, self.prefix + "mts_features", self.strerror(st))
+        return x, sc
+
+    def mlp_param_count(self) -> int:
+        return int(self._opt("mlp_param_count", c_int, [])())
+
+    def mlp_train_eval(self, x, target, params):
+        _f = POINTER(ctypes.c_float)
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(target, np.float32)
+        p = np.ascontiguousarray(params, np.float32)
+        nb = x.shape[0]
+        loss = np.zeros(1, np.float32)
+        grad = np.zeros(p.size, np.float32)
+        y = np.zeros((nb, 3), np.float32)
+        st = self._opt("mlp_train_eval", c_int, [c_int, _f, _f, _f, _f, _f, _f])(
+            nb, _ptr(x, _f), _ptr(t, _f), _ptr(p, _f), _ptr(loss, _f), _ptr(grad, _f), _ptr(y, _f))
+        if st != 0:
+            raise PathError(st, self.prefix + "mlp_train_eval", self.strerror(st))
+        return float(loss[0]), grad, y
+
+    def mlp_infer_eval(self, x, params):
+        _f = POINTER(ctypes.c_float)
+        x = np.ascontiguousarray(x, np.float32)
+        p = np.ascontiguousarray(params, np.float32)
+        y = np.zeros((x.shape[0], 3), np.float32)
+        st = self._opt("mlp_infer_eval", c_int, [c_int, _f, _f, _f])(x.shape[0], _ptr(x, _f), _ptr(p, _f),
+                                                                      _ptr(y, _f))
+        if st != 0:
+            raise PathError(st, self.prefix + "mlp_infer_eval", self.strerror(st))
+        return y
+
 
 def stats_to_dict(s: GbStepStats) -> dict:
     d = {k: getattr(s, k) for k, _ in GbStepStats._fields_ if k not in ("stress", "strkin")}

@@ -176,10 +176,40 @@ int gb_vv(int stage, double* strkin, double* engke, int32_t* iters, double* virc
  * refresh, forces, VV2+RATTLE with no host round trip; stats[nsteps] may be NULL. */
 int gb_md_run(int nsteps, gb_step_stats* stats);
 
-/* Learned multiple-time-step form: full SPME every k steps, the per-atom MLP
- * predicts the reciprocal-force increment on inner steps, and plain SPME is the
- * fallback when the checked RMS error exceeds tol (relative).  k = 1 disables. */
+/* Learned multiple-time-step form (no counterpart in the reference: its
+ * electro%nstfce key is parsed but SPME runs every step, two_body.F90:298-302).
+ * Full SPME every k steps; on the inner steps a per-atom MLP predicts the
+ * reciprocal-force increment since the last full step.  The first train_steps
+ * MD steps run SPME every step and train the network online on its forces;
+ * afterwards every k-th step compares the prediction with SPME and falls back
+ * to SPME every step while RMS(pred - SPME) / RMS(total force) > tol.
+ * Needs GB_MIXED; each call restarts from fresh weights.  k = 1 disables. */
 int gb_mts_config(int k, double tol, int train_steps);
+
+/* Learned-MTS counters, up to n of: [0] last checked relative error,
+ * [1] full steps, [2] inner steps, [3] fallback entries, [4] last training
+ * loss, [5] optimiser steps, [6] largest checked error, [7] 1 while in
+ * fallback, [8] checks made, [9] MD steps seen, [10] error of the same check
+ * without the network (coarse-grid increment only), [11] error of the stale
+ * reciprocal force, [12] coarse grid points along x. */
+int gb_mts_stats(double* out, int n);
+
+/* Test hooks of the learned form (no reference counterpart).
+ * gb_mts_features: the current scaled network inputs of the first n atoms
+ *   (n x 51 floats) and the 51 input scales + force scale (52 floats).
+ * gb_mlp_param_count: length of the FP32 parameter vector
+ *   W1[51][128] b1[128] W2[128][128] b2[128] W3[128][3] b3[3].
+ * gb_mlp_train_eval: the training kernel's forward + MSE + backward on nb rows
+ *   x[nb][51] with labels target[nb][3]: loss, grad[param_count], y[nb][3].
+ * gb_mlp_infer_eval: the inference kernel's output y[nb][3] for x[nb][51]. */
+int gb_mts_features(float* x, int n, float* scales);
+/* Ablation switch for tests: 1 = the inner steps reuse the reciprocal force of
+ * the last full step unchanged (the same MTS schedule without the network). */
+int gb_mts_ablation(int stale_only);
+int gb_mlp_param_count(void);
+int gb_mlp_train_eval(int nb, const float* x, const float* target, const float* params, float* loss,
+                      float* grad, float* y);
+int gb_mlp_infer_eval(int nb, const float* x, const float* params, float* y);
 
 /* Switch the force path between GB_FP64 and GB_MIXED after gb_init. */
 int gb_set_precision(int precision);
