@@ -49,6 +49,9 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 def workload(name):
     if name == "nacl_262144":
         return systems.nacl_melt(64), "NaCl melt 262,144 ions, box 180.48 A, SPME 192^3 p=8, rc 12 A, skin 1 A"
+    if name == "nacl_175616":  # profiling size: working set above the L2, a few GB on the device
+        return (systems.nacl_melt(56, kmax=160),
+                "NaCl melt 175,616 ions, box 157.92 A, SPME 160^3 p=8, rc 12 A, skin 1 A")
     if name == "nacl_4096":
         return systems.nacl_melt(16), "NaCl melt 4,096 ions, box 45.12 A, SPME 48^3 p=8, rc 12 A, skin 1 A"
     if name == "water_98304":
@@ -432,7 +435,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
     ap.add_argument("--form", default="fp64", choices=list(FORMS))
-    ap.add_argument("--workload", default="nacl_262144", choices=["nacl_262144", "nacl_4096", "water_98304"])
+    ap.add_argument("--workload", default="nacl_262144", choices=["nacl_262144", "nacl_175616", "nacl_4096", "water_98304"])
     ap.add_argument("--mts-train", type=int, default=200,
                     help="MD steps of online training (SPME every step) before the learned-MTS forms are timed")
     ap.add_argument("--no-compare", dest="compare", action="store_false",
