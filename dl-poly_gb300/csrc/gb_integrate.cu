@@ -16,7 +16,9 @@
 // listot(i) times, so positions round as the reference's do.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cfloat>
+#include <cstdlib>
 
 #include "gb_common.cuh"
 
@@ -238,6 +240,258 @@ __global__ void k_rattle(ConArgs A) {
   }
 }
 
+// ------------------------------------------------- cluster-local SHAKE/RATTLE
+// When every connected group of constraints (a "cluster": a rigid water, a
+// small molecule) has at most CL_MAXA atoms and CL_MAXC constraints, the
+// Jacobi sweeps of different clusters are independent: sweep `it` of a cluster
+// reads only that cluster's atoms.  One thread then owns a cluster and runs
+// its sweeps in registers; the only global quantity is the convergence test,
+// "every constraint of every cluster passes at sweep it".  Sweeps run in
+// chunks of CL_CHUNK: each cluster records the sweeps at which it fails in a
+// per-sweep flag word and applies every update of the chunk, saving the state
+// after each sweep in a per-cluster ring; one grid barrier per chunk then gives
+// the first sweep N at which nobody failed, and each cluster keeps the state
+// saved after sweep N-1.  Every update uses the per-sweep kernel's arithmetic,
+// so the result and the iteration count are those of the reference's global
+// sweeps (constraints.F90:898-969 and 1032-1071).
+//
+// FP64 instructions are expensive on this part, so tests that need no
+// arithmetic are done on the IEEE bit patterns: the minimum image of a bond
+// shorter than a quarter cell is the bond itself (round(d/L) = 0 exactly), and
+// the tolerance tests 0.5|x| < t are |x| < 2t, an integer compare of the
+// magnitudes' bits.
+constexpr int CL_MAXA = 4, CL_MAXC = 6, CL_CHUNK = 8;
+constexpr int CL_RING = CL_CHUNK + 1;       // state at chunk start + after each sweep
+constexpr int CL_SLOT = 3 * CL_MAXA + CL_MAXC;  // doubles per ring slot: state, then sweep gammas
+
+struct ClusterTab {
+  int atom[CL_MAXA];   // global atom ids, -1 padding
+  int con[CL_MAXC];    // global constraint ids in ascending order, -1 padding
+  int pair[CL_MAXC];   // local ends: li | lj << 4
+  int alist[CL_MAXA];  // per local atom: count | entries (local constraint << 1 | j end) in 4-bit fields from bit 4
+  int meta;            // na | nc << 4
+};
+
+__device__ __forceinline__ void warp_flag(bool fail, int* flag) {
+  const unsigned m = __activemask();
+  const unsigned b = __ballot_sync(m, fail);
+  if (b && (threadIdx.x & 31) == __ffs(m) - 1) atomicOr(flag, 1);
+}
+
+__device__ __forceinline__ long long absbits(double v) { return __double_as_longlong(v) & 0x7fffffffffffffffll; }
+
+// d - c*Anint(a*d), skipping the FP64 work when |d| < quarter (bits) makes the shift zero
+__device__ __forceinline__ double image_short(double d, long long quarter_bits, double c, double a) {
+  if (absbits(d) < quarter_bits) return d;
+  return image1(d, c, a);
+}
+
+// register-array reads with a runtime index, as selects (no local-memory copy)
+template <int N>
+__device__ __forceinline__ double sel(const double (&a)[N], int i) {
+  double r = a[0];
+#pragma unroll
+  for (int k = 1; k < N; ++k) r = (i == k) ? a[k] : r;
+  return r;
+}
+
+// per-cluster constants and state (positions for SHAKE, velocities for RATTLE)
+struct ClData {
+  int na, nc;
+  double x[CL_MAXA], y[CL_MAXA], z[CL_MAXA];
+  double bx[CL_MAXC], by[CL_MAXC], bz[CL_MAXC];
+  double d0sq[CL_MAXC];          // SHAKE: d0^2
+  long long tolb[CL_MAXC];       // bits of the tolerance bound on |d2| (SHAKE) or |gamma| (RATTLE)
+  double msum[CL_MAXC];          // amt_i + amt_j
+  double hm[CL_MAXA];            // per-atom update factor: 0.5 amt (SHAKE) or amt (RATTLE)
+  double dli[CL_MAXA];           // 1 / listot
+  bool active[CL_MAXA];          // has constraints and is not frozen
+};
+
+__device__ __forceinline__ void cl_load(const ConArgs& A, const ClusterTab& T, bool rattle, ClData& D) {
+  D.na = T.meta & 15;
+  D.nc = (T.meta >> 4) & 15;
+  const double amt_num = rattle ? A.tstep : A.tstep * A.tstep;
+  double amt[CL_MAXA];
+#pragma unroll
+  for (int a = 0; a < CL_MAXA; ++a) {
+    D.x[a] = D.y[a] = D.z[a] = 0.0;
+    amt[a] = 0.0; D.hm[a] = 0.0; D.dli[a] = 1.0; D.active[a] = false;
+    if (a < D.na) {
+      const int i = T.atom[a];
+      if (rattle) { D.x[a] = A.vx[i]; D.y[a] = A.vy[i]; D.z[a] = A.vz[i]; }
+      else { D.x[a] = A.x[i]; D.y[a] = A.y[i]; D.z[a] = A.z[i]; }
+      const bool frz = A.lfrzn[i] != 0;
+      amt[a] = frz ? 0.0 : amt_num / A.w[i];
+      const int cnt = T.alist[a] & 15;
+      D.active[a] = !frz && cnt > 0;
+      D.hm[a] = rattle ? amt[a] : 0.5 * amt[a];
+      D.dli[a] = 1.0 / (double)(cnt > 0 ? cnt : 1);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < CL_MAXC; ++c) {
+    D.bx[c] = D.by[c] = D.bz[c] = 0.0; D.d0sq[c] = 0.0; D.tolb[c] = 0; D.msum[c] = 1.0;
+    if (c < D.nc) {
+      const int k = T.con[c];
+      const int li = T.pair[c] & 15, lj = T.pair[c] >> 4;
+      double ux = A.dxx[k], uy = A.dyy[k], uz = A.dzz[k];
+      if (rattle) {
+        const double dis = 1.0 / sqrt(ux * ux + uy * uy + uz * uz);
+        ux *= dis; uy *= dis; uz *= dis;
+        // 0.5 tstep |gamma| < tol  <=>  |gamma| < (2 tol) / tstep, evaluated as the kernel does: 0.5*tstep*|g| < tol
+        D.tolb[c] = 0;  // unused: RATTLE keeps the FP64 comparison (tstep scaling is not exact)
+      } else {
+        const double d0 = A.d0[k];
+        D.d0sq[c] = d0 * d0;
+        D.tolb[c] = __double_as_longlong(2.0 * (A.tol * d0));  // 0.5|d2| < tol d0  <=>  |d2| < 2 (tol d0)
+      }
+      D.bx[c] = ux; D.by[c] = uy; D.bz[c] = uz;
+      D.msum[c] = sel(amt, li) + sel(amt, lj);
+    }
+  }
+}
+
+// one sweep: tests (returns true when a constraint fails), gammas, update of the state
+__device__ __forceinline__ bool cl_sweep(const ConArgs& A, const ClusterTab& T, bool rattle, long long quarter,
+                                         ClData& D, double (&gam)[CL_MAXC]) {
+  bool fail = false;
+#pragma unroll
+  for (int c = 0; c < CL_MAXC; ++c) {
+    gam[c] = 0.0;
+    if (c < D.nc) {
+      const int li = T.pair[c] & 15, lj = T.pair[c] >> 4;
+      if (rattle) {
+        const double gamma = D.bx[c] * (sel(D.x, li) - sel(D.x, lj)) + D.by[c] * (sel(D.y, li) - sel(D.y, lj)) +
+                             D.bz[c] * (sel(D.z, li) - sel(D.z, lj));
+        if (!(0.5 * A.tstep * fabs(gamma) < A.tol)) fail = true;
+        gam[c] = gamma / D.msum[c];
+      } else {
+        const double dx = image_short(sel(D.x, li) - sel(D.x, lj), quarter, A.c0, A.a0);
+        const double dy = image_short(sel(D.y, li) - sel(D.y, lj), quarter, A.c0, A.a0);
+        const double dz = image_short(sel(D.z, li) - sel(D.z, lj), quarter, A.c0, A.a0);
+        const double d2 = dx * dx + dy * dy + dz * dz - D.d0sq[c];
+        if (!(absbits(d2) < D.tolb[c])) fail = true;
+        gam[c] = d2 / (D.msum[c] * (D.bx[c] * dx + D.by[c] * dy + D.bz[c] * dz));
+      }
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < CL_MAXA; ++a) {
+    if (!D.active[a]) continue;
+    const int al = T.alist[a], cnt = al & 15;
+    double xt = 0.0, yt = 0.0, zt = 0.0;
+#pragma unroll
+    for (int e = 0; e < CL_MAXC; ++e) {
+      if (e < cnt) {
+        const int code = (al >> (4 + 4 * e)) & 15, c = code >> 1;
+        const double gh = sel(gam, c) * D.hm[a];
+        const double f = (code & 1) ? gh : -gh;
+        xt += sel(D.bx, c) * f; yt += sel(D.by, c) * f; zt += sel(D.bz, c) * f;
+      }
+    }
+    double px = D.x[a], py = D.y[a], pz = D.z[a];
+    for (int r = 0; r < cnt; ++r) { px += xt * D.dli[a]; py += yt * D.dli[a]; pz += zt * D.dli[a]; }
+    D.x[a] = px; D.y[a] = py; D.z[a] = pz;
+  }
+  return fail;
+}
+
+__device__ __forceinline__ void ring_put(double* slot, const ClData& D, const double (&gam)[CL_MAXC]) {
+#pragma unroll
+  for (int a = 0; a < CL_MAXA; ++a) { slot[3 * a] = D.x[a]; slot[3 * a + 1] = D.y[a]; slot[3 * a + 2] = D.z[a]; }
+#pragma unroll
+  for (int c = 0; c < CL_MAXC; ++c) slot[3 * CL_MAXA + c] = gam[c];
+}
+
+// SHAKE (rattle = false) or RATTLE (rattle = true) over all clusters; gsum
+// (CL_MAXC doubles per cluster) holds the committed gamma sums of SHAKE for
+// the constraint stress
+__global__ void __launch_bounds__(256) k_constrain_cl(ConArgs A, const ClusterTab* __restrict__ tabs, int ncl,
+                                                      double* __restrict__ ring, double* __restrict__ gsum,
+                                                      int rattle_i) {
+  cg::grid_group grid = cg::this_grid();
+  const bool rattle = rattle_i != 0;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nth = gridDim.x * blockDim.x;
+  const long long quarter = __double_as_longlong(0.25 * A.c0);
+  int it0 = 0, nfinal = -1;
+  for (;;) {
+    for (int cl = tid; cl < ncl; cl += nth) {
+      const ClusterTab T = tabs[cl];
+      ClData D;
+      cl_load(A, T, rattle, D);
+      double* rg = ring + (size_t)cl * CL_RING * CL_SLOT;
+      double gam[CL_MAXC];
+#pragma unroll
+      for (int c = 0; c < CL_MAXC; ++c) gam[c] = 0.0;
+      ring_put(rg, D, gam);
+      for (int s_ = 1; s_ <= CL_CHUNK; ++s_) {
+        if (it0 + s_ > A.maxit) break;
+        const bool fail = cl_sweep(A, T, rattle, quarter, D, gam);
+        warp_flag(fail, &A.flags[it0 + s_]);
+        ring_put(rg + s_ * CL_SLOT, D, gam);
+      }
+    }
+    grid.sync();
+    for (int s_ = 1; s_ <= CL_CHUNK && it0 + s_ <= A.maxit; ++s_)
+      if (A.flags[it0 + s_] == 0) { nfinal = it0 + s_; break; }
+    // committed sweeps of this chunk: all of them, or those before nfinal
+    const int last = nfinal > 0 ? nfinal - 1 - it0 : (A.maxit - it0 < CL_CHUNK ? A.maxit - it0 : CL_CHUNK);
+    for (int cl = tid; cl < ncl; cl += nth) {
+      const ClusterTab T = tabs[cl];
+      const int na = T.meta & 15, nc = (T.meta >> 4) & 15;
+      const double* rg = ring + (size_t)cl * CL_RING * CL_SLOT;
+      const double* fin = rg + last * CL_SLOT;
+#pragma unroll
+      for (int a = 0; a < CL_MAXA; ++a) {
+        if (a < na) {
+          const int i = T.atom[a];
+          if (rattle) { A.vx[i] = fin[3 * a]; A.vy[i] = fin[3 * a + 1]; A.vz[i] = fin[3 * a + 2]; }
+          else { A.x[i] = fin[3 * a]; A.y[i] = fin[3 * a + 1]; A.z[i] = fin[3 * a + 2]; }
+        }
+      }
+      if (!rattle) {
+        for (int s_ = 1; s_ <= last; ++s_)
+#pragma unroll
+          for (int c = 0; c < CL_MAXC; ++c)
+            if (c < nc) gsum[(size_t)cl * CL_MAXC + c] += rg[s_ * CL_SLOT + 3 * CL_MAXA + c];
+      }
+    }
+    if (nfinal > 0) break;
+    it0 += CL_CHUNK;
+    if (it0 >= A.maxit) break;
+    // no barrier needed here: a cluster is always handled by the same thread
+  }
+  if (tid == 0) {
+    if (rattle) {
+      A.sc->rattle_iters = nfinal > 0 ? nfinal : A.maxit;
+      if (nfinal < 0) A.sc->status |= ST_RATTLE_FAIL;
+    } else {
+      A.sc->shake_iters = nfinal > 0 ? nfinal : A.maxit;
+      if (nfinal < 0) A.sc->status |= ST_SHAKE_FAIL;
+    }
+  }
+  if (!rattle) {
+    // constraint stress: every committed update adds -gamma b b^T, b fixed during SHAKE
+    double st[6] = {0, 0, 0, 0, 0, 0};
+    for (int cl = tid; cl < ncl; cl += nth) {
+      const ClusterTab T = tabs[cl];
+      const int nc = (T.meta >> 4) & 15;
+#pragma unroll
+      for (int c = 0; c < CL_MAXC; ++c) {
+        if (c >= nc) continue;
+        const int k = T.con[c];
+        const double g = gsum[(size_t)cl * CL_MAXC + c];
+        const double bx = A.dxx[k], by = A.dyy[k], bz = A.dzz[k];
+        st[0] -= g * bx * bx; st[1] -= g * bx * by; st[2] -= g * bx * bz;
+        st[3] -= g * by * by; st[4] -= g * by * bz; st[5] -= g * bz * bz;
+      }
+    }
+    block_reduce_store<6>(st, A.blk);
+  }
+}
+
 // apply_shake epilogue: v += dr/dt, f += dr/dt * m/(dt/2) for constrained atoms
 __global__ void k_shake_post(int n, const int* astart, const int* lfrzn, double rstep, double hstep, const double* w,
                              const double* x, const double* y, const double* z, const double* ox, const double* oy,
@@ -259,6 +513,68 @@ __global__ void k_copy3(int n, const double* a, const double* b, const double* c
 
 int* d_flags = nullptr;
 int coop_blocks_shake = 0, coop_blocks_rattle = 0;
+// cluster-local path (used when every constraint cluster is small)
+ClusterTab* d_cltab = nullptr;
+double* d_clring = nullptr;  // per-cluster state ring (CL_RING slots of CL_SLOT doubles)
+double* d_clgsum = nullptr;  // per-cluster committed SHAKE gamma sums
+int n_clusters = 0, coop_blocks_cl = 0;
+
+// connected constraint clusters; false when one exceeds CL_MAXA atoms or CL_MAXC constraints
+bool build_clusters(const std::vector<int>& ci, const std::vector<int>& cj, std::vector<ClusterTab>& out) {
+  const int n = g.natms, nc = (int)ci.size();
+  std::vector<int> parent(n);
+  for (int i = 0; i < n; ++i) parent[i] = i;
+  auto find = [&](int a) {
+    while (parent[a] != a) a = parent[a] = parent[parent[a]];
+    return a;
+  };
+  for (int k = 0; k < nc; ++k) {
+    const int a = find(ci[k]), b = find(cj[k]);
+    if (a != b) parent[std::max(a, b)] = std::min(a, b);
+  }
+  std::vector<int> root_id(n, -1);
+  out.clear();
+  std::vector<std::vector<int>> atoms, cons;
+  for (int k = 0; k < nc; ++k) {  // clusters in order of their first constraint; constraints ascending
+    const int r = find(ci[k]);
+    if (root_id[r] < 0) {
+      root_id[r] = (int)atoms.size();
+      atoms.emplace_back();
+      cons.emplace_back();
+    }
+    cons[root_id[r]].push_back(k);
+  }
+  for (size_t c = 0; c < cons.size(); ++c) {
+    for (int k : cons[c])
+      for (int e : {ci[k], cj[k]})
+        if (std::find(atoms[c].begin(), atoms[c].end(), e) == atoms[c].end()) atoms[c].push_back(e);
+    if ((int)atoms[c].size() > CL_MAXA || (int)cons[c].size() > CL_MAXC) return false;
+  }
+  out.resize(cons.size());
+  for (size_t c = 0; c < cons.size(); ++c) {
+    ClusterTab& T = out[c];
+    for (int a = 0; a < CL_MAXA; ++a) { T.atom[a] = -1; T.alist[a] = 0; }
+    for (int q = 0; q < CL_MAXC; ++q) { T.con[q] = -1; T.pair[q] = 0; }
+    const int na = (int)atoms[c].size(), ncl = (int)cons[c].size();
+    for (int a = 0; a < na; ++a) T.atom[a] = atoms[c][a];
+    auto local = [&](int gid) { return (int)(std::find(atoms[c].begin(), atoms[c].end(), gid) - atoms[c].begin()); };
+    for (int q = 0; q < ncl; ++q) {
+      const int k = cons[c][q];
+      T.con[q] = k;
+      const int li = local(ci[k]), lj = local(cj[k]);
+      T.pair[q] = li | (lj << 4);
+      // per-atom entries in constraint order, as the global per-atom table holds them
+      for (int end = 0; end < 2; ++end) {
+        const int la = end ? lj : li;
+        const int cnt = T.alist[la] & 15;
+        T.alist[la] = (T.alist[la] & ~15) | (cnt + 1);
+        T.alist[la] |= ((q << 1) | end) << (4 + 4 * cnt);
+      }
+    }
+    T.meta = na | (ncl << 4);
+  }
+  return true;
+}
 
 }  // namespace
 
@@ -298,12 +614,29 @@ void integ_setup_constraints(const int32_t* listcon, const double* prmcon) {
   GB_CUDA(cudaMemcpy(g.acon_start, start.data(), sizeof(int) * (g.natms + 1), cudaMemcpyHostToDevice));
   if (!list.empty())
     GB_CUDA(cudaMemcpy(g.acon_list, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
-  GB_CUDA(cudaMalloc(&d_flags, sizeof(int) * (g.p.shake_maxit + 2)));
+  if (d_flags) cudaFree(d_flags);
+  GB_CUDA(cudaMalloc(&d_flags, sizeof(int) * (g.p.shake_maxit + CL_CHUNK + 2)));
   int bps = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_shake, 256, 0));
   coop_blocks_shake = std::max(1, std::min(bps * g.nsm, nblocks(std::max(nc, g.natms), 256)));
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_rattle, 256, 0));
   coop_blocks_rattle = std::max(1, std::min(bps * g.nsm, nblocks(std::max(nc, g.natms), 256)));
+  // cluster-local sweeps when every cluster is small (GB_SHAKE_GLOBAL=1 keeps the per-sweep kernels)
+  if (d_cltab) { cudaFree(d_cltab); d_cltab = nullptr; }
+  if (d_clring) { cudaFree(d_clring); d_clring = nullptr; }
+  if (d_clgsum) { cudaFree(d_clgsum); d_clgsum = nullptr; }
+  n_clusters = 0;
+  const char* env = std::getenv("GB_SHAKE_GLOBAL");
+  std::vector<ClusterTab> tabs;
+  if (!(env && env[0] == '1') && build_clusters(ci, cj, tabs)) {
+    n_clusters = (int)tabs.size();
+    GB_CUDA(cudaMalloc(&d_cltab, sizeof(ClusterTab) * tabs.size()));
+    GB_CUDA(cudaMemcpy(d_cltab, tabs.data(), sizeof(ClusterTab) * tabs.size(), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMalloc(&d_clring, sizeof(double) * CL_RING * CL_SLOT * tabs.size()));
+    GB_CUDA(cudaMalloc(&d_clgsum, sizeof(double) * CL_MAXC * tabs.size()));
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_constrain_cl, 256, 0));
+    coop_blocks_cl = std::max(1, std::min(bps * g.nsm, nblocks(n_clusters, 256)));
+  }
 }
 
 void integ_zero_forces() {
@@ -358,16 +691,26 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
     if (g.ntcons > 0) {
       k_copy3<<<nblocks(n, 256), 256, 0, st>>>(n, g.x, g.y, g.z, g.ox, g.oy, g.oz);
       GB_LAUNCHED();
-      GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + 2), st));
+      GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + CL_CHUNK + 2), st));
       ConArgs A;
       con_args(A);
-      A.blk = gb_blkacc(coop_blocks_shake * 6);
-      void* args[] = {&A};
+      const int nbs = n_clusters ? coop_blocks_cl : coop_blocks_shake;
+      A.blk = gb_blkacc(nbs * 6);
       prof_begin(P_SHAKE);
-      GB_CUDA(cudaLaunchCooperativeKernel((void*)k_shake, coop_blocks_shake, 256, args, 0, st));
+      if (n_clusters) {
+        const ClusterTab* tabs = d_cltab;
+        int ncl = n_clusters, rattle = 0;
+        double *ring = d_clring, *gsum = d_clgsum;
+        GB_CUDA(cudaMemsetAsync(d_clgsum, 0, sizeof(double) * CL_MAXC * n_clusters, st));
+        void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
+        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_constrain_cl, nbs, 256, args, 0, st));
+      } else {
+        void* args[] = {&A};
+        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_shake, nbs, 256, args, 0, st));
+      }
       GB_LAUNCHED();
       prof_end(P_SHAKE);
-      gb_reduce_blocks(A.blk, coop_blocks_shake, 6, &g.sc->acc[A_STRCON]);
+      gb_reduce_blocks(A.blk, nbs, 6, &g.sc->acc[A_STRCON]);
       k_shake_post<<<nblocks(n, 256), 256, 0, st>>>(n, g.acon_start, g.lfrzn, rstep, hstep, g.weight, g.x, g.y, g.z,
                                                      g.ox, g.oy, g.oz, g.vx, g.vy, g.vz, g.fx, g.fy, g.fz);
       GB_LAUNCHED();
@@ -385,12 +728,20 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
     GB_LAUNCHED();
     prof_end(P_VV);
     if (g.ntcons > 0) {
-      GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + 2), st));
+      GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + CL_CHUNK + 2), st));
       ConArgs A;
       con_args(A);
-      void* args[] = {&A};
       prof_begin(P_RATTLE);
-      GB_CUDA(cudaLaunchCooperativeKernel((void*)k_rattle, coop_blocks_rattle, 256, args, 0, st));
+      if (n_clusters) {
+        const ClusterTab* tabs = d_cltab;
+        int ncl = n_clusters, rattle = 1;
+        double *ring = d_clring, *gsum = d_clgsum;
+        void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
+        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_constrain_cl, coop_blocks_cl, 256, args, 0, st));
+      } else {
+        void* args[] = {&A};
+        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_rattle, coop_blocks_rattle, 256, args, 0, st));
+      }
       GB_LAUNCHED();
       prof_end(P_RATTLE);
     }
