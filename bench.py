@@ -304,6 +304,55 @@ def measure(lib, L, s, form, args, dist, device, steps, detail):
     return out, dict(stats=stats, prof=prof, P=(P_list, P_rc), launches=l1 - l0, clk=clk, wall=w1 - w0, tmax=tmax)
 
 
+KB_INTERNAL = 0.831446261815324  # Boltzmann constant in DL_POLY internal energy units (10 J/mol) per K
+
+
+def run_drift(args):
+    """NVE energy drift per form: slope of a linear fit to the total energy (after the first
+    tenth of the run, and after MTS training; MTS forms use the full-SPME steps, whose energies
+    are exact), in kT per ns per atom."""
+    import dlpoly_gb300 as gb
+
+    s, desc = workload(args.drift_workload)
+    temp = 1500.0 if args.drift_workload.startswith("nacl") else 300.0
+    lib = gb.load()
+    out = {"mode": "nve_drift", "workload": desc, "steps": args.drift_steps, "temperature_K": temp, "forms": {}}
+    for form in args.drift_forms.split(","):
+        precision, k = FORMS[form]
+        lib.init(s, precision=precision)
+        lib.start()
+        train = 0
+        if k > 1:
+            train = min(args.drift_train, args.drift_steps // 2)
+            lib.mts_config(k, MTS_TOL, train)
+        E, full = [], []
+        t0 = time.perf_counter()
+        done = 0
+        while done < args.drift_steps:
+            st = lib.md_vv(min(1000, args.drift_steps - done))
+            done += len(st)
+            for x in st:
+                E.append(x.engcpe_rc + x.engcpe_rl + x.engcpe_ex + x.engvdw + x.engke)
+                full.append(x.mts_full)
+        wall = time.perf_counter() - t0
+        E = np.array(E)
+        idx = np.arange(len(E))
+        sel = idx >= max(train + 10, len(E) // 10)
+        if k > 1:
+            sel &= np.array(full, bool)
+        slope = np.polyfit(idx[sel] * DT_PS, E[sel], 1)[0]  # energy units per ps
+        rec = {"drift_kT_per_ns_per_atom": float(slope * 1000.0 / (KB_INTERNAL * temp * s.natms)),
+               "energy_rel_std": float(np.std(E[sel]) / abs(np.mean(E[sel]))), "wall_s": wall}
+        if k > 1:
+            m = lib.mts_stats()
+            rec["mts"] = {"k": k, "train_steps": train, "checked_err_last": m["last_err"],
+                          "checked_err_max": m["err_max"], "err_without_network": m["err_no_network"],
+                          "inner_steps": int(m["n_inner"]), "fallback_entries": int(m["n_fallback"])}
+        out["forms"][form] = rec
+    lib.finalize()
+    print(json.dumps(out), flush=True)
+
+
 def run_gb(args, dist):
     import dlpoly_gb300 as gb
 
@@ -441,7 +490,15 @@ def main():
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="time only --form (default: every form of the workload, --form is the headline)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--drift", action="store_true", help="NVE energy drift per form instead of the throughput line")
+    ap.add_argument("--drift-workload", default="nacl_4096", choices=["nacl_4096", "nacl_262144", "water_98304"])
+    ap.add_argument("--drift-steps", type=int, default=10000)
+    ap.add_argument("--drift-train", type=int, default=2000)
+    ap.add_argument("--drift-forms", default="fp64,mixed,mts_k4,mts_k8")
     args = ap.parse_args()
+    if args.drift:
+        run_drift(args)
+        return
     dist = Dist()
     try:
         if args.impl == "reference":

@@ -32,7 +32,8 @@ Module gb300_interface
   Logical, Public :: gb_active = .false.
 
   Public :: gb_init, gb_upload_parts, gb_download_parts, gb_relocate, gb_list_build, gb_vnl_check, &
-            gb_refresh, gb_forces, gb_spme, gb_vv, gb_md_run, gb_mts_config, gb_finalize
+            gb_refresh, gb_forces, gb_spme, gb_vv, gb_md_run, gb_mts_config, gb_mts_stats, &
+            gb_set_precision, gb_finalize
 
   Interface
     Integer(c_int) Function gb_init(prm, natms, ltype, chge, weight, lfrzn, vdw_prm, ntcons, listcon, &
@@ -105,6 +106,17 @@ Module gb300_interface
       Integer(c_int), Value :: k, train_steps
       Real(c_double), Value :: tol
     End Function gb_mts_config
+
+    Integer(c_int) Function gb_mts_stats(out, n) Bind(C, name="gb_mts_stats")
+      Import :: c_int, c_double
+      Real(c_double), Intent(Out) :: out(*)
+      Integer(c_int), Value :: n
+    End Function gb_mts_stats
+
+    Integer(c_int) Function gb_set_precision(precision) Bind(C, name="gb_set_precision")
+      Import :: c_int
+      Integer(c_int), Value :: precision
+    End Function gb_set_precision
 
     Subroutine gb_finalize() Bind(C, name="gb_finalize")
     End Subroutine gb_finalize
