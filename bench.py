@@ -164,6 +164,20 @@ def kernel_work(name, s, cnt, form):
     return None
 
 
+# DRAM bytes (read + write) per half-list entry of the pair kernels, from one
+# ncu capture each on the 175,616-ion melt (the 262,144-ion launch is too large
+# for a full-section capture); traffic grows with the list, so the bench scales
+# it by this launch's list entries.
+MEASURED_TRAFFIC = {
+    ("pair_forces", "fp64"): ((200.795648e6 + 3.779072e6) / 40368337,
+                              "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_fp64 on nacl_175616 "
+                              "(profiles/pair_fp64_nacl175616.md), scaled by half-list entries"),
+    ("pair_forces", "mixed"): ((312.066816e6 + 6.53056e6) / 37054682,
+                               "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_mixed on nacl_175616 "
+                               "(profiles/pair_mixed_nacl175616.md), scaled by half-list entries"),
+}
+
+
 def read_peaks():
     try:
         return json.load(open(PEAKS_FILE))
@@ -436,6 +450,10 @@ def run_gb(args, dist):
                     "frac": (by / sec / 1e9) / (hbm or 6800.0), "traffic": None,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else "fallback 6.8 TB/s"}
         roof["algorithmic"] = {"flops_per_launch": fl, "bytes_per_launch": by, "launch_ms": sec * 1e3}
+        tr = MEASURED_TRAFFIC.get((dom, "fp64" if precision == 0 else "mixed"))
+        if tr:
+            roof["traffic"] = tr[0] * P_list
+            roof["traffic_source"] = tr[1]
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         try:
