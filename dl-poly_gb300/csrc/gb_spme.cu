@@ -143,8 +143,11 @@ __device__ T2* fft_lines(T2* a, T2* b, const FftPlan& pl, int nlines, const T2* 
 // Cardinal B-spline values M_p(w + p - 1 - t), t = 0..p-1, by the order
 // recursion of bspline_splines_gen (bspline.F90:227-245), valid as the
 // polynomial pieces for any w (the reference also feeds w outside [0,1)).
-template <typename T>
-__device__ __forceinline__ void bspline_vals(T w, int p, T* m /*p*/, T* dm /*p or null*/) {
+// P > 0 fixes the order at compile time: the recursion unrolls into registers
+// and 1/(n-1) folds to the same correctly rounded constant the division gives.
+template <typename T, int P = 0>
+__device__ __forceinline__ void bspline_vals(T w, int p_rt, T* m /*p*/, T* dm /*p or null*/) {
+  const int p = P ? P : p_rt;
   // z[j], j = 1..p as in the reference (z[p] <-> M(w), z[1] <-> M(w+p-1))
   T z[PMAX + 2];
 #pragma unroll
@@ -152,8 +155,10 @@ __device__ __forceinline__ void bspline_vals(T w, int p, T* m /*p*/, T* dm /*p o
   z[p] = w;
   z[p - 1] = (T)1 - w;
   // raise from order 2 to order p-1
+#pragma unroll
   for (int n = 3; n <= p - 1; ++n) {
     const T rn = (T)1 / (T)(n - 1);
+#pragma unroll
     for (int j = p - n + 1; j <= p - 1; ++j) {
       const T pt = w + (T)(p - j);
       z[j] = (pt * z[j] + ((T)n - pt) * z[j + 1]) * rn;
@@ -162,11 +167,13 @@ __device__ __forceinline__ void bspline_vals(T w, int p, T* m /*p*/, T* dm /*p o
   }
   if (dm) {
     // derivative of order p from order p-1 values: M_{p-1}(x) - M_{p-1}(x-1)
+#pragma unroll
     for (int j = 1; j <= p; ++j) dm[j - 1] = z[j] - z[j + 1];
   }
   {
     const int n = p;
     const T rn = (T)1 / (T)(n - 1);
+#pragma unroll
     for (int j = 1; j <= p - 1; ++j) {
       const T pt = w + (T)(p - j);
       z[j] = (pt * z[j] + ((T)n - pt) * z[j + 1]) * rn;
@@ -174,6 +181,7 @@ __device__ __forceinline__ void bspline_vals(T w, int p, T* m /*p*/, T* dm /*p o
     z[p] = z[p] * w * rn;
   }
   // output in grid order t = 0..p-1  <->  reference spline index s = t+1
+#pragma unroll
   for (int t = 0; t < p; ++t) m[t] = z[t + 1];
 }
 
@@ -183,13 +191,13 @@ struct SpmeGeom {
   int K[3], B[3], nb[3], p;
 };
 
-template <typename T>
+template <typename T, int P>
 __global__ void k_spme_prep(int natms, const double* __restrict__ x, const double* __restrict__ y,
                             const double* __restrict__ z, const double* __restrict__ q, SpmeGeom sg, T* spl,
                             int* nidx, int* brick_of, int* brick_count, int* gidx, float* gw) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natms) return;
-  const int p = sg.p;
+  const int p = P ? P : sg.p;
   int bidx[3];
   for (int d = 0; d < 3; ++d) {
     double u = sg.Kr[d] * (((sg.rc[d] * x[i] + sg.rc[d + 3] * y[i]) + sg.rc[d + 6] * z[i]) + 0.5);
@@ -205,7 +213,8 @@ __global__ void k_spme_prep(int natms, const double* __restrict__ x, const doubl
       gw[3 * i + d] = (float)(u - tr);
     }
     T m[PMAX];
-    bspline_vals<T>(w, p, m, nullptr);
+    bspline_vals<T, P>(w, p, m, nullptr);
+#pragma unroll
     for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t];
     int nw = n % sg.K[d];
     if (nw < 0) nw += sg.K[d];
@@ -247,12 +256,12 @@ constexpr int BMAX = 16;
 // points below it that its atoms reach; atoms are scattered one after another
 // (one FMA per grid point, all lanes busy, no atomics), then the tile is
 // written to its own slot of `ext` for the halo reduction below.
-template <typename T>
+template <typename T, int P>
 __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, const int* __restrict__ batoms,
                                    const T* __restrict__ spl, const int* __restrict__ nidx,
                                    const double* __restrict__ q, T* __restrict__ ext) {
   extern __shared__ unsigned char smem_raw[];
-  const int p = sg.p;
+  const int p = P ? P : sg.p;
   const int b = blockIdx.x;
   const int bx = b % sg.nb[0], by = (b / sg.nb[0]) % sg.nb[1], bz = b / (sg.nb[0] * sg.nb[1]);
   const int g0x = bx * sg.B[0], g0y = by * sg.B[1], g0z = bz * sg.B[2];
@@ -537,7 +546,7 @@ __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan
 // per atom: trunc-based splines (Int(u), u - Aint(u)), p^3 periodic grid
 // reads of the real potential, separable sums.  Writes the unscaled force
 // -(K.rcell) q sum dM M M phi and accumulates energy and net force.
-template <typename T>
+template <typename T, int P>
 __global__ void k_spme_gather(int natms, const double* __restrict__ x, const double* __restrict__ y,
                               const double* __restrict__ z, const double* __restrict__ q, SpmeGeom sg,
                               const T* __restrict__ phi, double rk0, double rk1, double rk2, double* fout,
@@ -545,25 +554,29 @@ __global__ void k_spme_gather(int natms, const double* __restrict__ x, const dou
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[4] = {0, 0, 0, 0};
   if (i < natms && fabs(q[i]) > DBL_MIN) {
-    const int p = sg.p;
+    const int p = P ? P : sg.p;
     T m[3][PMAX], dm[3][PMAX];
     int n0[3];
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
       double u = sg.Kr[d] * (((sg.rc[d] * x[i] + sg.rc[d + 3] * y[i]) + sg.rc[d + 6] * z[i]) + 0.5);
       double tr = trunc(u);
       int n = (int)tr;
-      bspline_vals<T>((T)(u - tr), p, m[d], dm[d]);
+      bspline_vals<T, P>((T)(u - tr), p, m[d], dm[d]);
       n0[d] = n - p + 1;
     }
     const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
     int ix[PMAX];
+#pragma unroll
     for (int t = 0; t < p; ++t) { int v = (n0[0] + t) % K0; if (v < 0) v += K0; ix[t] = v; }
     const T qi = (T)q[i];
     // separable sums: rows along x first, then y within a z plane, then z
     T e = 0, fxs = 0, fys = 0, fzs = 0;
+#pragma unroll
     for (int l = 0; l < p; ++l) {
       int zz = (n0[2] + l) % K2; if (zz < 0) zz += K2;
       T a0 = 0, a1 = 0, a2 = 0;
+#pragma unroll
       for (int k = 0; k < p; ++k) {
         int yy = (n0[1] + k) % K1; if (yy < 0) yy += K1;
         const T* row = phi + ((size_t)zz * K1 + yy) * K0;
@@ -614,7 +627,7 @@ __global__ void __launch_bounds__(256) k_spme_gather_f32(int natms, const float*
     const float qi = q4[4 * i + 3];
     if (lane < 3) {
       float m[PMAX], dm[PMAX];
-      bspline_vals<float>(gw[3 * i + lane], P, m, dm);
+      bspline_vals<float, P>(gw[3 * i + lane], P, m, dm);
       for (int t = 0; t < P; ++t) { sp[wid][0][lane][t] = m[t]; sp[wid][1][lane][t] = dm[t]; }
     }
     __syncwarp();
@@ -830,8 +843,10 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
   {
     const size_t tsize = (size_t)(S.B[0] + p - 1) * (S.B[1] + p - 1) * (S.B[2] + p - 1);
     GB_CUDA(cudaMalloc(&S.spread_ext, sizeof(double) * tsize * S.nbricks));
-    raise_smem(k_spme_spread_tile<double>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(double)));
-    raise_smem(k_spme_spread_tile<float>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
+    raise_smem(k_spme_spread_tile<double, 8>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(double)));
+    raise_smem(k_spme_spread_tile<double, 0>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(double)));
+    raise_smem(k_spme_spread_tile<float, 8>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
+    raise_smem(k_spme_spread_tile<float, 0>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
     raise_smem(k_spme_spread_fix<8>, (int)(tsize * sizeof(long long)));
     raise_smem(k_spme_spread_fix<6>, (int)(tsize * sizeof(long long)));
     raise_smem(k_spme_spread_fix<0>, (int)(tsize * sizeof(long long)));
@@ -978,9 +993,9 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   GB_CUDA(cudaMemsetAsync(S.brick_fill, 0, sizeof(int) * (S.nbricks + 2), st));
   prof_begin(pid(P_SPME_PREP));
   const bool warp_gather = !F64 && (p == 8 || p == 6);
-  k_spme_prep<T><<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, spl, S.nidx, S.brick_of,
-                                                   S.brick_count, warp_gather ? S.gidx : nullptr,
-                                                   warp_gather ? S.gw : nullptr);
+  auto prep = p == 8 ? k_spme_prep<T, 8> : (p == 6 ? k_spme_prep<T, 6> : k_spme_prep<T, 0>);
+  prep<<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, spl, S.nidx, S.brick_of, S.brick_count,
+                                         warp_gather ? S.gidx : nullptr, warp_gather ? S.gw : nullptr);
   GB_LAUNCHED();
 
   scan_exclusive(S.brick_count, S.brick_start, S.nbricks + 1);
@@ -997,8 +1012,8 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
     const size_t NG = (size_t)K1 * K2 * K3;
     prof_begin(pid(P_SPME_SPREAD));
     if (F64) {
-      k_spme_spread_tile<T><<<S.nbricks, 512, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge,
-                                                          ext);
+      auto spread = p == 8 ? k_spme_spread_tile<T, 8> : k_spme_spread_tile<T, 0>;
+      spread<<<S.nbricks, 512, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge, ext);
       GB_LAUNCHED();
       k_spme_tile_reduce<T><<<nblocks((long long)NG, 256), 256, 0, st>>>(S.sg, ext, Q);
       GB_LAUNCHED();
@@ -1058,7 +1073,8 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
                               reinterpret_cast<const float*>(Q), (float)rk[0], (float)rk[1], (float)rk[2], S.fout_f,
                               blkg);
   } else {
-    k_spme_gather<T><<<nbg, 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, Q, rk[0], rk[1], rk[2], S.fspme, blkg);
+    auto gather = p == 8 ? k_spme_gather<T, 8> : k_spme_gather<T, 0>;
+    gather<<<nbg, 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, Q, rk[0], rk[1], rk[2], S.fspme, blkg);
   }
   GB_LAUNCHED();
   prof_end(pid(P_SPME_GATHER));
