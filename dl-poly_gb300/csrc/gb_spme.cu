@@ -421,75 +421,114 @@ inline size_t spread_smem(int B0, int B1, int B2, int p, size_t esz) {
 }
 
 // ---------------------------------------------------------------- FFT passes
-// X pass forward: real rows -> complex rows
+// The charge grid is real, so the x pass is a real-to-complex transform: a row
+// of N = K1 reals is packed as M = N/2 complex values z_n = x_2n + i x_2n+1,
+// transformed with the half-length complex FFT and split into the N/2+1
+// non-redundant outputs
+//   X_k = E_k + w^k O_k,  E_k = (Z_k + conj Z_{M-k}) / 2,  O_k = (Z_k - conj Z_{M-k}) / 2i,
+// w = e^{+2 pi i/N} (the forward sign of the reference's transform).  The y and
+// z passes then run on Kx = N/2+1 columns.  The inverse rebuilds
+//   Z_k = (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) w^{-k},  k < M,
+// runs the half-length inverse and unpacks x_2n = Re z_n, x_2n+1 = Im z_n: the
+// real part of the full inverse transform, as before.
 template <typename T, typename T2>
 __global__ void k_fft_x_fwd(const T* __restrict__ Q, T2* __restrict__ G, FftPlan pl, const T2* __restrict__ tw,
-                            int nrows, int lines) {
+                            const T2* __restrict__ twN, int nrows, int lines) {
   extern __shared__ unsigned char smem_raw[];
   T2* a = reinterpret_cast<T2*>(smem_raw);
   T2* b = a + lines * pl.N;
-  const int N = pl.N;
+  const int M = pl.N, Kx = M + 1;
   const size_t row0 = (size_t)blockIdx.x * lines;
   const int nl = (int)min((size_t)lines, (size_t)nrows - row0);
-  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
-    T2 v; v.x = Q[row0 * N + e]; v.y = (T)0;
-    a[e] = v;
-  }
+  const T2* Qc = reinterpret_cast<const T2*>(Q);
+  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) a[e] = Qc[row0 * M + e];
   T2* r = fft_lines<T, T2, +1>(a, b, pl, nl, tw);
-  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) G[row0 * N + e] = r[e];
+  for (int e = threadIdx.x; e < nl * Kx; e += blockDim.x) {
+    const int line = e / Kx, k = e - line * Kx;
+    const T2 zk = r[line * M + (k == M ? 0 : k)];
+    const T2 zc = r[line * M + (k == 0 ? 0 : M - k)];  // Z_{M-k}, conjugated below
+    const T ex = (T)0.5 * (zk.x + zc.x), ey = (T)0.5 * (zk.y - zc.y);
+    const T ox = (T)0.5 * (zk.y + zc.y), oy = (T)0.5 * (zc.x - zk.x);
+    const T2 w = twN[k];
+    T2 v;
+    v.x = ex + (w.x * ox - w.y * oy);
+    v.y = ey + (w.x * oy + w.y * ox);
+    G[(row0 + line) * Kx + k] = v;
+  }
 }
 
-// X pass inverse: complex rows -> real part
 template <typename T, typename T2>
 __global__ void k_fft_x_inv(const T2* __restrict__ G, T* __restrict__ Q, FftPlan pl, const T2* __restrict__ tw,
-                            int nrows, int lines) {
+                            const T2* __restrict__ twN, int nrows, int lines) {
   extern __shared__ unsigned char smem_raw[];
   T2* a = reinterpret_cast<T2*>(smem_raw);
   T2* b = a + lines * pl.N;
-  const int N = pl.N;
+  const int M = pl.N, Kx = M + 1;
   const size_t row0 = (size_t)blockIdx.x * lines;
   const int nl = (int)min((size_t)lines, (size_t)nrows - row0);
-  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) a[e] = G[row0 * N + e];
+  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
+    const int line = e / M, k = e - line * M;
+    const T2 xk = G[(row0 + line) * Kx + k];
+    const T2 xc = G[(row0 + line) * Kx + (M - k)];  // X_{M-k}, conjugated below
+    const T ax = xk.x + xc.x, ay = xk.y - xc.y;     // X_k + conj X_{M-k}
+    const T dx = xk.x - xc.x, dy = xk.y + xc.y;     // X_k - conj X_{M-k}
+    const T2 w = twN[k];                            // w^{-k} = conj(w^k)
+    const T bx = dx * w.x + dy * w.y, by = dy * w.x - dx * w.y;
+    T2 v;
+    v.x = ax - by;
+    v.y = ay + bx;
+    a[e] = v;
+  }
   T2* r = fft_lines<T, T2, -1>(a, b, pl, nl, tw);
-  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) Q[row0 * N + e] = r[e].x;
+  T2* Qc = reinterpret_cast<T2*>(Q);
+  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) Qc[row0 * M + e] = r[e];
 }
 
-// Y pass (stride K1): tile of TX columns x N lines, in place
+// Y pass (stride Kx): tile of TX columns x N lines, in place
 template <typename T, typename T2, int ISIGN>
-__global__ void k_fft_y(T2* __restrict__ G, int K1, int K2, FftPlan pl, const T2* __restrict__ tw) {
+__global__ void k_fft_y(T2* __restrict__ G, int Kx, int K2, FftPlan pl, const T2* __restrict__ tw) {
   extern __shared__ unsigned char smem_raw[];
   T2* a = reinterpret_cast<T2*>(smem_raw);
   T2* b = a + TX * pl.N;
-  const int ntx = K1 / TX;
+  const int ntx = (Kx + TX - 1) / TX;
   const int x0 = (blockIdx.x % ntx) * TX;
   const int zz = blockIdx.x / ntx;
-  T2* base = G + (size_t)zz * K1 * K2 + x0;
+  const int nt = min(TX, Kx - x0);
+  T2* base = G + (size_t)zz * Kx * K2 + x0;
   for (int e = threadIdx.x; e < TX * K2; e += blockDim.x) {
     int yy = e / TX, t = e - yy * TX;
-    a[t * K2 + yy] = base[(size_t)yy * K1 + t];
+    T2 v; v.x = (T)0; v.y = (T)0;
+    if (t < nt) v = base[(size_t)yy * Kx + t];
+    a[t * K2 + yy] = v;
   }
   T2* r = fft_lines<T, T2, ISIGN>(a, b, pl, TX, tw);
   for (int e = threadIdx.x; e < TX * K2; e += blockDim.x) {
     int yy = e / TX, t = e - yy * TX;
-    base[(size_t)yy * K1 + t] = r[t * K2 + yy];
+    if (t < nt) base[(size_t)yy * Kx + t] = r[t * K2 + yy];
   }
 }
 
-// Z pass: forward z FFT, influence function + stress, inverse z FFT
+// Z pass: forward z FFT, influence function + stress, inverse z FFT on the
+// Kx = K1/2+1 columns of the half spectrum; columns 0 < x < K1/2 stand for
+// themselves and their conjugate mirror, so they count twice in the stress
 template <typename T, typename T2>
 __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan pl, const T2* __restrict__ tw,
                              const T* __restrict__ theta, const T* __restrict__ psi, SpmeGeom sg, double* blk) {
   extern __shared__ unsigned char smem_raw[];
   T2* a = reinterpret_cast<T2*>(smem_raw);
   T2* b = a + TX * pl.N;
-  const int ntx = K1 / TX;
+  const int Kx = K1 / 2 + 1;
+  const int ntx = (Kx + TX - 1) / TX;
   const int x0 = (blockIdx.x % ntx) * TX;
   const int yy = blockIdx.x / ntx;
-  const size_t plane = (size_t)K1 * K2;
-  T2* base = G + (size_t)yy * K1 + x0;
+  const int nt = min(TX, Kx - x0);
+  const size_t plane = (size_t)Kx * K2;
+  T2* base = G + (size_t)yy * Kx + x0;
   for (int e = threadIdx.x; e < TX * K3; e += blockDim.x) {
     int zz = e / TX, t = e - zz * TX;
-    a[t * K3 + zz] = base[(size_t)zz * plane + t];
+    T2 v; v.x = (T)0; v.y = (T)0;
+    if (t < nt) v = base[(size_t)zz * plane + t];
+    a[t * K3 + zz] = v;
   }
   // m_z = ll * rcell(9) for the cubic cell (gb_init accepts cubic cells only)
   T* rzt = reinterpret_cast<T*>(b + TX * pl.N);
@@ -503,9 +542,10 @@ __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan
   // A = sum psi|Q|^2, B = sum mz psi|Q|^2, C = sum mz^2 psi|Q|^2.
   const int tpl = blockDim.x / TX;          // threads per line
   const int t = threadIdx.x / tpl;          // this thread's line
-  T A = 0, B = 0, C = 0;
-  if (t < TX) {
-    const size_t line0 = (size_t)yy * K1 + x0 + t;
+  // Bn: the z-Nyquist point (mz = +K3/2 for a point and its mirror alike) kept apart
+  T A = 0, B = 0, Bn = 0, C = 0;
+  if (t < nt) {
+    const size_t line0 = (size_t)yy * Kx + x0 + t;
     T2* rl = r + t * K3;
     for (int zz = threadIdx.x - t * tpl; zz < K3; zz += tpl) {
       const size_t gi = line0 * K3 + zz;  // theta/psi are stored z-contiguous per (x,y) line
@@ -515,7 +555,8 @@ __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan
         const T pv = psi[gi] * (v.x * v.x + v.y * v.y);
         const T u = pv * rzt[zz];
         A += pv;
-        B += u;
+        if (2 * zz == K3) Bn += u;
+        else B += u;
         C = fma(u, rzt[zz], C);
         v.x *= th; v.y *= th;
       } else {
@@ -525,19 +566,36 @@ __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan
     }
   }
   // in the working precision T: the FP32 form issues no FP64 instruction here
+  // A line 0 < jx < K1/2 stands for itself and its mirror m' = -m, except that
+  // a Nyquist index (ky = K2/2, mz = K3/2) keeps its + sign in the mirror.
+  // The mirror's share of m_a m_b psi|Q|^2 is then +/- the line's own:
+  //   xx, yy, zz: +;  xy: - when ky is Nyquist;  xz: - for the Nyquist z point;
+  //   yz: - when exactly one of ky and the z point is Nyquist.
   T st[6] = {0, 0, 0, 0, 0, 0};
-  if (t < TX) {
-    int jj = x0 + t; if (2 * jj > K1) jj -= K1;
+  if (t < nt) {
+    const int jx = x0 + t;
+    int jj = jx; if (2 * jj > K1) jj -= K1;
     int kk = yy; if (2 * kk > K2) kk -= K2;
     const T rx = (T)jj * (T)sg.rc[0], ry = (T)kk * (T)sg.rc[4];
-    st[0] = rx * rx * A; st[1] = rx * ry * A; st[2] = rx * B;
-    st[3] = ry * ry * A; st[4] = ry * B; st[5] = C;
+    if (jx == 0 || 2 * jx == K1) {  // the line holds its own mirror: the full-spectrum sums
+      const T Ball = B + Bn;
+      st[0] = rx * rx * A; st[1] = rx * ry * A; st[2] = rx * Ball;
+      st[3] = ry * ry * A; st[4] = ry * Ball; st[5] = C;
+    } else {
+      const bool ny = 2 * yy == K2;
+      st[0] = (T)2 * rx * rx * A;
+      st[1] = ny ? (T)0 : (T)2 * rx * ry * A;
+      st[2] = (T)2 * rx * B;
+      st[3] = (T)2 * ry * ry * A;
+      st[4] = (T)2 * ry * (ny ? Bn : B);
+      st[5] = (T)2 * C;
+    }
   }
   T2* o = (r == a) ? b : a;
   T2* r2 = fft_lines<T, T2, -1>(r, o, pl, TX, tw);
   for (int e = threadIdx.x; e < TX * K3; e += blockDim.x) {
     int zz = e / TX, t = e - zz * TX;
-    base[(size_t)zz * plane + t] = r2[t * K3 + zz];
+    if (t < nt) base[(size_t)zz * plane + t] = r2[t * K3 + zz];
   }
   block_reduce_store<6>(st, blk);
 }
@@ -749,6 +807,10 @@ struct SpmeGrid {
   float *theta_f = nullptr, *psi_f = nullptr;
   double2* tw[3] = {nullptr, nullptr, nullptr};
   float2* twf[3] = {nullptr, nullptr, nullptr};
+  FftPlan planh;                 // x pass: half-length complex transform of the packed real rows
+  double2* twh = nullptr;        // its twiddles e^{+2 pi i t/(K1/2)}
+  float2* twhf = nullptr;
+  int Kx = 0;                    // K1/2 + 1 complex columns of the half spectrum
   double* fspme = nullptr;     // 3*natms reciprocal forces (before scale, net removal)
   void* spread_ext = nullptr;  // per-brick spread tiles (nbricks x (B+p-1)^3)
   int* gidx = nullptr;         // warp gather: first grid index per dimension (truncation convention)
@@ -787,7 +849,7 @@ void raise_smem(K kernel, int bytes) {
 void grid_free(SpmeGrid& S) {
   void* ptrs[] = {S.spl, S.nidx, S.brick_of, S.brick_count, S.brick_start, S.brick_fill, S.brick_atoms, S.Q, S.G,
                   S.Qf, S.Gf, S.theta, S.psi, S.theta_f, S.psi_f, S.tw[0], S.tw[1], S.tw[2], S.twf[0], S.twf[1],
-                  S.twf[2], S.fspme, S.spread_ext, S.gidx, S.gw, S.fout_f};
+                  S.twf[2], S.twh, S.twhf, S.fspme, S.spread_ext, S.gidx, S.gw, S.fout_f};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   S = SpmeGrid();
@@ -798,10 +860,12 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
   grid_free(S);
   if (p > PMAX || p < 3) throw (int)GB_ERR_ARG;
   for (int d = 0; d < 3; ++d) S.K[d] = Kin[d];
-  if (S.K[0] % TX || S.K[1] % TX) throw (int)GB_ERR_ARG;
+  if (S.K[0] % 2) throw (int)GB_ERR_ARG;  // real-to-complex x pass on packed pairs
   S.p = p;
   S.fp64 = fp64;
   for (int d = 0; d < 3; ++d) S.plan[d] = make_plan(S.K[d]);
+  S.planh = make_plan(S.K[0] / 2);
+  S.Kx = S.K[0] / 2 + 1;
   for (int d = 0; d < 3; ++d) {
     S.B[d] = choose_brick(S.K[d], p);
     if (S.B[d] < 0) {
@@ -900,13 +964,13 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
       int ll = l; if (2 * ll > K3) ll -= K3;
       for (int k = 0; k < K2; ++k) {
         int kk = k; if (2 * kk > K2) kk -= K2;
-        for (int j = 0; j < K1; ++j) {
+        for (int j = 0; j < S.Kx; ++j) {  // the half spectrum: m_x = 0..K1/2
           int jj = j; if (2 * jj > K1) jj -= K1;
           double r0 = (double)ll * rc[2] + (double)kk * rc[1] + (double)jj * rc[0];
           double r1 = (double)ll * rc[5] + (double)kk * rc[4] + (double)jj * rc[3];
           double r2 = (double)ll * rc[8] + (double)kk * rc[7] + (double)jj * rc[6];
           double k2 = r0 * r0 + r1 * r1 + r2 * r2;
-          size_t gi = ((size_t)k * K1 + j) * K3 + l;  // z-contiguous per (x,y) line for the z pass
+          size_t gi = ((size_t)k * S.Kx + j) * K3 + l;  // z-contiguous per (x,y) line for the z pass
           if (k2 <= cut2 && k2 > test_fac) {
             double bb = norm2[2][l] * norm2[1][k] * norm2[0][j];
             double f = std::sqrt(k2) * recip_conv_fac;
@@ -937,6 +1001,7 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
     GB_CUDA(cudaMemcpy(*df, tf.data(), sizeof(float2) * K, cudaMemcpyHostToDevice));
   };
   for (int d = 0; d < 3; ++d) mk_tw(S.K[d], &S.tw[d], &S.twf[d]);
+  mk_tw(S.K[0] / 2, &S.twh, &S.twhf);
   // FP32 copies for the mixed form
   GB_CUDA(cudaMalloc(&S.Qf, sizeof(float) * NG));
   GB_CUDA(cudaMalloc(&S.Gf, sizeof(float2) * NG));
@@ -1029,19 +1094,22 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
     }
     prof_end(pid(P_SPME_SPREAD));
   }
-  // FFT + convolution
+  // FFT + convolution: real-to-complex x pass, y and z passes on the Kx = K1/2+1 columns
   const int lines = 8;
   const int rows = K2 * K3;
+  const int Kx = S.Kx, M = K1 / 2;
+  const T2* twh = F64 ? reinterpret_cast<const T2*>(S.twh) : reinterpret_cast<const T2*>(S.twhf);
+  const int ntx = (Kx + TX - 1) / TX;
   prof_begin(pid(P_FFT_XF));
-  k_fft_x_fwd<T, T2><<<nblocks(rows, lines), 256, fft_smem(K1, lines, sizeof(T2)), st>>>(Q, G, S.plan[0], tw1, rows,
-                                                                                          lines);
+  k_fft_x_fwd<T, T2><<<nblocks(rows, lines), 256, fft_smem(M, lines, sizeof(T2)), st>>>(Q, G, S.planh, twh, tw1, rows,
+                                                                                         lines);
   GB_LAUNCHED();
   prof_end(pid(P_FFT_XF));
   prof_begin(pid(P_FFT_Y));
-  k_fft_y<T, T2, +1><<<(K1 / TX) * K3, 256, fft_smem(K2, TX, sizeof(T2)), st>>>(G, K1, K2, S.plan[1], tw2);
+  k_fft_y<T, T2, +1><<<ntx * K3, 256, fft_smem(K2, TX, sizeof(T2)), st>>>(G, Kx, K2, S.plan[1], tw2);
   GB_LAUNCHED();
   prof_end(pid(P_FFT_Y));
-  const int nbz = (K1 / TX) * K2;
+  const int nbz = ntx * K2;
   double* blkz = gb_blkacc(nbz * 6 + nblocks((long long)n * 32, 128) * 4);
   prof_begin(pid(P_FFT_Z));
   k_fft_z_conv<T, T2><<<nbz, 256, fft_smem(K3, TX, sizeof(T2)) + K3 * sizeof(T), st>>>(G, K1, K2, K3, S.plan[2], tw3,
@@ -1049,12 +1117,12 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   GB_LAUNCHED();
   prof_end(pid(P_FFT_Z));
   prof_begin(pid(P_FFT_Y));
-  k_fft_y<T, T2, -1><<<(K1 / TX) * K3, 256, fft_smem(K2, TX, sizeof(T2)), st>>>(G, K1, K2, S.plan[1], tw2);
+  k_fft_y<T, T2, -1><<<ntx * K3, 256, fft_smem(K2, TX, sizeof(T2)), st>>>(G, Kx, K2, S.plan[1], tw2);
   GB_LAUNCHED();
   prof_end(pid(P_FFT_Y));
   prof_begin(pid(P_FFT_XI));
-  k_fft_x_inv<T, T2><<<nblocks(rows, lines), 256, fft_smem(K1, lines, sizeof(T2)), st>>>(G, Q, S.plan[0], tw1, rows,
-                                                                                          lines);
+  k_fft_x_inv<T, T2><<<nblocks(rows, lines), 256, fft_smem(M, lines, sizeof(T2)), st>>>(G, Q, S.planh, twh, tw1, rows,
+                                                                                         lines);
   GB_LAUNCHED();
   prof_end(pid(P_FFT_XI));
   // gather
