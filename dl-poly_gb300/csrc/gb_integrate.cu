@@ -407,7 +407,7 @@ __device__ __forceinline__ void ring_put(double* slot, const ClData& D, const do
 // SHAKE (rattle = false) or RATTLE (rattle = true) over all clusters; gsum
 // (CL_MAXC doubles per cluster) holds the committed gamma sums of SHAKE for
 // the constraint stress
-__global__ void __launch_bounds__(256) k_constrain_cl(ConArgs A, const ClusterTab* __restrict__ tabs, int ncl,
+__global__ void __launch_bounds__(128) k_constrain_cl(ConArgs A, const ClusterTab* __restrict__ tabs, int ncl,
                                                       double* __restrict__ ring, double* __restrict__ gsum,
                                                       int rattle_i) {
   cg::grid_group grid = cg::this_grid();
@@ -518,6 +518,7 @@ ClusterTab* d_cltab = nullptr;
 double* d_clring = nullptr;  // per-cluster state ring (CL_RING slots of CL_SLOT doubles)
 double* d_clgsum = nullptr;  // per-cluster committed SHAKE gamma sums
 int n_clusters = 0, coop_blocks_cl = 0;
+constexpr int CL_THREADS = 128;  // small blocks spread the clusters over every SM
 
 // connected constraint clusters; false when one exceeds CL_MAXA atoms or CL_MAXC constraints
 bool build_clusters(const std::vector<int>& ci, const std::vector<int>& cj, std::vector<ClusterTab>& out) {
@@ -634,8 +635,8 @@ void integ_setup_constraints(const int32_t* listcon, const double* prmcon) {
     GB_CUDA(cudaMemcpy(d_cltab, tabs.data(), sizeof(ClusterTab) * tabs.size(), cudaMemcpyHostToDevice));
     GB_CUDA(cudaMalloc(&d_clring, sizeof(double) * CL_RING * CL_SLOT * tabs.size()));
     GB_CUDA(cudaMalloc(&d_clgsum, sizeof(double) * CL_MAXC * tabs.size()));
-    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_constrain_cl, 256, 0));
-    coop_blocks_cl = std::max(1, std::min(bps * g.nsm, nblocks(n_clusters, 256)));
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_constrain_cl, CL_THREADS, 0));
+    coop_blocks_cl = std::max(1, std::min(bps * g.nsm, nblocks(n_clusters, CL_THREADS)));
   }
 }
 
@@ -703,7 +704,7 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
         double *ring = d_clring, *gsum = d_clgsum;
         GB_CUDA(cudaMemsetAsync(d_clgsum, 0, sizeof(double) * CL_MAXC * n_clusters, st));
         void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
-        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_constrain_cl, nbs, 256, args, 0, st));
+        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_constrain_cl, nbs, CL_THREADS, args, 0, st));
       } else {
         void* args[] = {&A};
         GB_CUDA(cudaLaunchCooperativeKernel((void*)k_shake, nbs, 256, args, 0, st));
@@ -737,7 +738,7 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
         int ncl = n_clusters, rattle = 1;
         double *ring = d_clring, *gsum = d_clgsum;
         void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
-        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_constrain_cl, coop_blocks_cl, 256, args, 0, st));
+        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_constrain_cl, coop_blocks_cl, CL_THREADS, args, 0, st));
       } else {
         void* args[] = {&A};
         GB_CUDA(cudaLaunchCooperativeKernel((void*)k_rattle, coop_blocks_rattle, 256, args, 0, st));

@@ -496,18 +496,22 @@ __global__ void k_full_count(int natms, const int* list, int ld, int* fcount) {
   (void)n;
 }
 
+// An atom's full list: its own half-list entries first, in list order (no
+// atomic), then the reverse entries, appended with one atomic per entry on the
+// receiving atom.
 __global__ void k_full_fill(int natms, const int* list, int ld, const int* fstart, int* ffill, int* flist) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= natms) return;
   const int* li = list + (size_t)warp * ld + 3;
   const int nx = li[0];
+  const int own0 = fstart[warp];
   for (int k = lane; k < nx; k += 32) {
     int j = li[k + 1] - 1;
-    int slot = atomicAdd(&ffill[warp], 1);
-    flist[fstart[warp] + slot] = j;
+    flist[own0 + k] = j;
     if (j < natms) {
+      const int nxj = list[(size_t)j * ld + 3];
       int s2 = atomicAdd(&ffill[j], 1);
-      flist[fstart[j] + s2] = warp;
+      flist[fstart[j] + nxj + s2] = warp;
     }
   }
 }
