@@ -298,10 +298,7 @@ def measure(lib, L, s, form, args, dist, device, steps, detail):
             prof[nm] = (ms[j], int(nl[j]))
     cnt = (ctypes.c_int64 * 3)()
     L.gb_pair_counts(cnt, 3)
-    P_list, P_rc = int(cnt[0]), int(cnt[1])
-    if precision == 1:
-        P_list //= 2
-        P_rc //= 2
+    P_list, P_rc = int(cnt[0]), int(cnt[1])  # both forms walk the half list
     tmax = dist.max(span_s)
     out = {"value": dist.world * s.natms * steps / tmax, "ms_per_step": tmax * 1e3 / steps,
            "ns_per_day": (steps / tmax) * DT_PS * 86400 / 1000, "steps": steps,

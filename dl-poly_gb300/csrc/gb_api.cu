@@ -681,13 +681,11 @@ int gb_mts_config(int k, double tol, int train_steps) {
 int gb_set_precision(int precision) {
   return guarded([&]() {
     if (precision != GB_FP64 && precision != GB_MIXED) return (int)GB_ERR_ARG;
-    bool was = g.precision;
     if (precision != GB_MIXED && mts_active()) {  // the learned form runs on the mixed path only
       mts_free();
       g.mts_k = 1;
     }
     g.precision = precision;
-    if (precision == GB_MIXED && was != GB_MIXED) list_full_build();
     return (int)GB_OK;
   });
 }

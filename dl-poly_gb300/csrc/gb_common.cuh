@@ -111,7 +111,8 @@ struct Dev {
   int* fcount = nullptr;       // per atom count
   int* fstart = nullptr;       // per atom start
   long long flist_cap = 0;
-  long long list_gen = 0;      // incremented whenever the full list is rebuilt
+  long long list_gen = 0;      // incremented whenever the Verlet list is rebuilt
+  long long full_gen = -1;     // list generation the derived full list was built from
 
   // tables
   int nsamples = 0, max_grid = 0, nkey = 0;
@@ -277,7 +278,7 @@ int list_relocate_and_halo();     // pbcshift + halo + vnl_set_check (gb_list.cu
 int list_refresh_halo();          // refresh halo positions (gb_list.cu)
 int list_build();                 // binning + pairs (gb_list.cu)
 void list_setup();                // link-cell geometry (gb_list.cu)
-void list_full_build();           // derived full list for the mixed path
+void list_full_build();           // derived full (symmetric) list, for the learned-MTS inputs
 void list_pos_f32();              // FP32 copy of positions and charges (mixed path)
 void scan_exclusive(const int* in, int* out, int n);
 void pair_forces(double* eng6, double* stress9);  // gb_pair.cu (adds into forces)

@@ -706,11 +706,7 @@ int list_build() {
   prof_end(P_LIST);
   gb_sync_scalars();
   if (g.hsc->status & ST_LIST_OVERFLOW) return GB_ERR_LIST_OVERFLOW;
-  if (g.precision == GB_MIXED) {
-    prof_begin(P_FULLLIST);
-    list_full_build();
-    prof_end(P_FULLLIST);
-  }
+  ++g.list_gen;  // the derived full list (learned-MTS inputs) is rebuilt on demand
   return GB_OK;
 }
 
@@ -739,5 +735,5 @@ void list_full_build() {
   GB_CUDA(cudaMemsetAsync(fill, 0, sizeof(int) * (n + 1), st));
   k_full_fill<<<nblocks((long long)n * 32, 256), 256, 0, st>>>(n, g.list, g.ld, g.fstart, fill, g.flist);
   GB_LAUNCHED();
-  ++g.list_gen;
+  g.full_gen = g.list_gen;
 }

@@ -816,6 +816,11 @@ void mts_short_list() {
 void mts_inputs() {
   const int n = g.natms;
   prof_begin(P_MTS_DESC);
+  if (g.full_gen != g.list_gen) {
+    prof_begin(P_FULLLIST);
+    list_full_build();
+    prof_end(P_FULLLIST);
+  }
   if (M.gen_seen != g.list_gen) mts_short_list();
   k_mts_prep<<<nblocks(n, 256), 256, 0, g.stream>>>(n, g.x, g.y, g.z, M.x0, M.triple, g.cell[0], M.disp, M.frame);
   GB_LAUNCHED();

@@ -14,17 +14,15 @@
 // with a halo image j are evaluated once, by the atom with the smaller global
 // id, and applied to both atoms (the reference evaluates such a pair from both
 // sides, each side keeping only its own force; the sum is the same).
-// Mixed form: one warp per atom walks the derived full list in FP32 and sums
-// the pair forces as int64 fixed point (scale 2^40): order independent, no
-// atomics per pair, bit-reproducible.
+// Mixed form: one warp per atom walks the same half list in FP32 and sums the
+// pair forces as int64 fixed point (scale 2^40), the reaction on j with 64-bit
+// integer atomics: order independent and bit-reproducible.
 #include <cfloat>
 #include <cstring>
 
 #include "gb_common.cuh"
 
 namespace {
-
-constexpr float FIX_SCALE_F = 1099511627776.0f;
 
 struct PairGeom {
   double rc2, rv2;           // cutoffs squared
@@ -295,26 +293,30 @@ __global__ void k_excl_fp64(int natms, const int* list, int ld, const double* x,
 }
 
 // -------------------------------------------------------------- mixed form
-// Full list, FP32 arithmetic, int64 fixed-point force sums; energies and
-// virials are summed per lane in FP32 and reduced in FP64 (x0.5: every pair
-// appears twice in the full list).  The erfc and LJ functions are evaluated
-// directly: on this part FP32 math and MUFU are far cheaper than the random
-// table reads the FP64 form's exact interpolation needs.
+// FP32 arithmetic, int64 fixed-point force sums; energies and virials are
+// summed per lane in FP32 (compensated) and reduced in FP64.  The erfc and LJ
+// functions are evaluated directly: on this part FP32 math and MUFU are far
+// cheaper than the random table reads the FP64 form's exact interpolation needs.
 constexpr float AS_A1 = 0.254829592f, AS_A2 = -0.284496736f, AS_A3 = 1.421413741f, AS_A4 = -1.453152027f,
                 AS_A5 = 1.061405429f, AS_P = 0.3275911f;
 constexpr int MAX_KEYS = 64;
 constexpr int MAX_TYPES = 10;  // 55 type-pair keys
 __constant__ float4 c_lj[MAX_KEYS];
-__global__ void __launch_bounds__(256, 4) k_pair_mixed(int natms, const int* __restrict__ fstart,
-                                                    const int* __restrict__ fcount, const int* __restrict__ flist,
-                                                    const float4* __restrict__ xf, const float4* __restrict__ xlo,
-                                                    const int* __restrict__ ltype,
-                                                    int ntypes, float rc2, float rv2, float alpha,
-                                                    float alpha2rsqrpi, float scaling,
-                                                    unsigned long long* fixp, double* blk,
-                                                    unsigned long long* cnt) {
-  // LJ constants per ordered type pair in shared memory (uniform-free indexing);
-  // .w = 1 where a 12-6 potential exists
+// Mixed form on the half list: each pair is evaluated once and its force goes
+// to i (per-lane int64 sums) and, negated, to j (one 64-bit integer atomic
+// per component).  Integer addition is associative, so the forces are the
+// same whatever the order the warps and atomics run in.  Halo pairs are
+// evaluated from the side with the smaller global id and applied to the
+// image's source atom, as in the FP64 kernel.
+__global__ void __launch_bounds__(256, 3) k_pair_mixed_half(int natms, const DevScalars* sc,
+                                                         const int* __restrict__ at_list,
+                                                         const int* __restrict__ list, int ld,
+                                                         const float4* __restrict__ xf, const float4* __restrict__ xlo,
+                                                         const int* __restrict__ ltype, const int* __restrict__ ltg,
+                                                         const int* __restrict__ src, int ntypes, float rc2, float rv2,
+                                                         float alpha, float alpha2rsqrpi, float scaling,
+                                                         unsigned long long* fixp, double* blk,
+                                                         unsigned long long* cnt) {
   __shared__ float4 s_lj[MAX_TYPES * MAX_TYPES];
   for (int e = threadIdx.x; e < ntypes * ntypes; e += blockDim.x) {
     const int ai = e / ntypes + 1, aj = e % ntypes + 1;
@@ -323,26 +325,35 @@ __global__ void __launch_bounds__(256, 4) k_pair_mixed(int natms, const int* __r
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  // per-lane FP32 energy/virial/stress sums with compensation (no FP64 op in the loop)
   float a[NACC], c[NACC];
 #pragma unroll
   for (int k = 0; k < NACC; ++k) { a[k] = 0.f; c[k] = 0.f; }
   unsigned long long n_list = 0, n_rc = 0;
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < natms; i += nwarps) {
+  const int nlast = sc->nlast;
+  // persistent warps walk the atoms in cell order (neighbouring atoms share j data in L1)
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nlast; w += nwarps) {
+    const int i = at_list[w];
+    if (i >= natms) continue;
     const float4 pi = xf[i];
     const float4 li = xlo[i];
     const float qi = pi.w * scaling;
     const int row = (ltype[i] - 1) * ntypes - 1;
-    const int s = fstart[i], n = fcount[i];
+    const int gi = ltg[i];
+    const int* lst = list + (size_t)i * ld + 3;
+    const int n = lst[0];
     long long sx = 0, sy = 0, sz = 0;
     float t[NACC];
 #pragma unroll
     for (int k = 0; k < NACC; ++k) t[k] = 0.f;
-    for (int m = lane; m < n; m += 32) {
-      const int j = flist[s + m];
+    for (int m = lane + 1; m <= n; m += 32) {
+      const int j = lst[m] - 1;
+      int jf = j;
+      if (j >= natms) {
+        if (gi > ltg[j]) continue;  // evaluated from the other side
+        jf = src[j];
+      }
       const float4 pj = xf[j];
       const float4 lj = xlo[j];
-      // separation from the hi + lo position pairs (antisymmetric in i, j)
       const float dx = (pi.x - pj.x) + (li.x - lj.x), dy = (pi.y - pj.y) + (li.y - lj.y),
                   dz = (pi.z - pj.z) + (li.z - lj.z);
       const float rsq = dx * dx + dy * dy + dz * dz;
@@ -351,43 +362,41 @@ __global__ void __launch_bounds__(256, 4) k_pair_mixed(int natms, const int* __r
       const float rrr = rsq * rinv;
       const float r2i = rinv * rinv;
       float gam = 0.f;
-      // real-space Coulomb: the function the reference tabulates
-      // (electrostatic.F90:88-127, A&S erfc numerics.F90:3647), evaluated
-      // directly in FP32 (MUFU exp/rcp) instead of interpolated from tables
       if (rsq < rc2 && pj.w != 0.f) {
         const float x = alpha * rrr;
         const float ex = __expf(-x * x);
         const float tt = __frcp_rn(fmaf(AS_P, x, 1.0f));
         const float poly = tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, AS_A5, AS_A4), AS_A3), AS_A2), AS_A1);
         const float pre = qi * pj.w;
-        const float ec = pre * poly * ex * rinv;                       // q q erfc(ar)/r
-        const float eg = fmaf(pre * alpha2rsqrpi, ex, ec) * r2i;        // (erfc/r + 2a/sqrt(pi) e^-x^2)/r^2
+        const float ec = pre * poly * ex * rinv;
+        const float eg = fmaf(pre * alpha2rsqrpi, ex, ec) * r2i;
         gam += eg;
         t[2] += ec;
         t[3] = fmaf(-eg, rsq, t[3]);
       }
       if (rsq < rv2) {
-        const float4 lj = s_lj[row + ltype[j]];  // (4 eps, 24 eps, sigma^2, present)
-        if (lj.w != 0.f) {
-          // 12-6 Lennard-Jones (two_body_potentials.F90:260-270)
-          const float s2 = lj.z * r2i;
+        const float4 lj6 = s_lj[row + ltype[j]];
+        if (lj6.w != 0.f) {
+          const float s2 = lj6.z * r2i;
           const float s6 = s2 * s2 * s2;
-          const float gv = lj.y * s6 * fmaf(2.0f, s6, -1.0f) * r2i;
+          const float gv = lj6.y * s6 * fmaf(2.0f, s6, -1.0f) * r2i;
           gam += gv;
-          t[0] = fmaf(lj.x * s6, s6 - 1.0f, t[0]);
+          t[0] = fmaf(lj6.x * s6, s6 - 1.0f, t[0]);
           t[1] = fmaf(-gv, rsq, t[1]);
         }
       }
       ++n_rc;
       const float fx_ = gam * dx, fy_ = gam * dy, fz_ = gam * dz;
-      sx += fix40(fx_);
-      sy += fix40(fy_);
-      sz += fix40(fz_);
+      const long long ix = fix40(fx_), iy = fix40(fy_), iz = fix40(fz_);
+      sx += ix; sy += iy; sz += iz;
+      atomicAdd(&fixp[3 * jf + 0], (unsigned long long)(-ix));
+      atomicAdd(&fixp[3 * jf + 1], (unsigned long long)(-iy));
+      atomicAdd(&fixp[3 * jf + 2], (unsigned long long)(-iz));
       t[4] = fmaf(dx, fx_, t[4]); t[5] = fmaf(dx, fy_, t[5]); t[6] = fmaf(dx, fz_, t[6]);
       t[7] = fmaf(dy, fy_, t[7]); t[8] = fmaf(dy, fz_, t[8]); t[9] = fmaf(dz, fz_, t[9]);
     }
 #pragma unroll
-    for (int k = 0; k < NACC; ++k) {  // compensated add of this atom's share
+    for (int k = 0; k < NACC; ++k) {
       const float y = t[k] - c[k], tt = a[k] + y;
       c[k] = (tt - a[k]) - y;
       a[k] = tt;
@@ -405,10 +414,9 @@ __global__ void __launch_bounds__(256, 4) k_pair_mixed(int natms, const int* __r
       n_list += (unsigned long long)n;
     }
   }
-  // FP64 only here, once per thread: x0.5 because every pair appears twice
   double acc[NACC];
 #pragma unroll
-  for (int k = 0; k < NACC; ++k) acc[k] = 0.5 * ((double)a[k] - (double)c[k]);
+  for (int k = 0; k < NACC; ++k) acc[k] = (double)a[k] - (double)c[k];
   n_rc = (unsigned long long)warp_sumi((int)n_rc);
   if (lane == 0) {
     atomicAdd(&cnt[0], n_list);
@@ -490,15 +498,14 @@ void pair_forces(double* eng6, double* stress9) {
     }
   } else {
     static int occ32 = 0;
-    if (!occ32) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_pair_mixed, T, 0));
-    int nb = std::max(1, std::min(nblocks((long long)g.natms * 32, T), occ32 * g.nsm));
+    if (!occ32) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_pair_mixed_half, T, 0));
+    int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, T), occ32 * g.nsm));
     double* blk = gb_blkacc(nb * NACC + nb2 * 8);
     prof_begin(P_PAIR);
     const double a2rp = g.p.alpha * 2.0 / std::sqrt(3.14159265358979323846264338327950288);
-    k_pair_mixed<<<nb, T, 0, st>>>(g.natms, g.fstart, g.fcount, g.flist, g.xf, g.xlo, g.ltype, g.p.ntypes,
-                                   (float)pg.rc2,
-                                   (float)pg.rv2, (float)g.p.alpha, (float)a2rp, (float)pg.scaling,
-                                   (unsigned long long*)g.fixp, blk, &g.sc->npairs_list);
+    k_pair_mixed_half<<<nb, T, 0, st>>>(g.natms, g.sc, g.at_list, g.list, g.ld, g.xf, g.xlo, g.ltype, g.ltg, g.src,
+                                        g.p.ntypes, (float)pg.rc2, (float)pg.rv2, (float)g.p.alpha, (float)a2rp,
+                                        (float)pg.scaling, (unsigned long long*)g.fixp, blk, &g.sc->npairs_list);
     GB_LAUNCHED();
     prof_end(P_PAIR);
     gb_reduce_blocks(blk, nb, NACC, &g.sc->acc[A_PAIR]);
