@@ -820,7 +820,13 @@ struct SpmeGrid {
 
 SpmeGrid S_main, S_coarse;
 
+// Brick edge: a divisor of K of at least p-1 (a brick's atoms reach at most the
+// next brick).  Larger bricks cut the halo overlap (B+p-1)^3 / B^3 of the tiles
+// the fixed-order reduction reads back, so prefer one of at least BPREF.
+constexpr int BPREF = 12;
 int choose_brick(int K, int p) {
+  for (int B = std::max(p - 1, BPREF); B <= BMAX; ++B)
+    if (K % B == 0) return B;
   for (int B = p - 1; B <= BMAX; ++B)
     if (K % B == 0) return B;
   return -1;
