@@ -296,25 +296,27 @@ __device__ __forceinline__ double sel(const double (&a)[N], int i) {
 }
 
 // per-cluster constants and state (positions for SHAKE, velocities for RATTLE)
+template <int MA, int MC>
 struct ClData {
   int na, nc;
-  double x[CL_MAXA], y[CL_MAXA], z[CL_MAXA];
-  double bx[CL_MAXC], by[CL_MAXC], bz[CL_MAXC];
-  double d0sq[CL_MAXC];          // SHAKE: d0^2
-  long long tolb[CL_MAXC];       // bits of the tolerance bound on |d2| (SHAKE) or |gamma| (RATTLE)
-  double msum[CL_MAXC];          // amt_i + amt_j
-  double hm[CL_MAXA];            // per-atom update factor: 0.5 amt (SHAKE) or amt (RATTLE)
-  double dli[CL_MAXA];           // 1 / listot
-  bool active[CL_MAXA];          // has constraints and is not frozen
+  double x[MA], y[MA], z[MA];
+  double bx[MC], by[MC], bz[MC];
+  double d0sq[MC];          // SHAKE: d0^2
+  long long tolb[MC];       // bits of the tolerance bound on |d2| (SHAKE) or |gamma| (RATTLE)
+  double msum[MC];          // amt_i + amt_j
+  double hm[MA];            // per-atom update factor: 0.5 amt (SHAKE) or amt (RATTLE)
+  double dli[MA];           // 1 / listot
+  bool active[MA];          // has constraints and is not frozen
 };
 
-__device__ __forceinline__ void cl_load(const ConArgs& A, const ClusterTab& T, bool rattle, ClData& D) {
+template <int MA, int MC>
+__device__ __forceinline__ void cl_load(const ConArgs& A, const ClusterTab& T, bool rattle, ClData<MA, MC>& D) {
   D.na = T.meta & 15;
   D.nc = (T.meta >> 4) & 15;
   const double amt_num = rattle ? A.tstep : A.tstep * A.tstep;
-  double amt[CL_MAXA];
+  double amt[MA];
 #pragma unroll
-  for (int a = 0; a < CL_MAXA; ++a) {
+  for (int a = 0; a < MA; ++a) {
     D.x[a] = D.y[a] = D.z[a] = 0.0;
     amt[a] = 0.0; D.hm[a] = 0.0; D.dli[a] = 1.0; D.active[a] = false;
     if (a < D.na) {
@@ -330,7 +332,7 @@ __device__ __forceinline__ void cl_load(const ConArgs& A, const ClusterTab& T, b
     }
   }
 #pragma unroll
-  for (int c = 0; c < CL_MAXC; ++c) {
+  for (int c = 0; c < MC; ++c) {
     D.bx[c] = D.by[c] = D.bz[c] = 0.0; D.d0sq[c] = 0.0; D.tolb[c] = 0; D.msum[c] = 1.0;
     if (c < D.nc) {
       const int k = T.con[c];
@@ -353,11 +355,12 @@ __device__ __forceinline__ void cl_load(const ConArgs& A, const ClusterTab& T, b
 }
 
 // one sweep: tests (returns true when a constraint fails), gammas, update of the state
+template <int MA, int MC>
 __device__ __forceinline__ bool cl_sweep(const ConArgs& A, const ClusterTab& T, bool rattle, long long quarter,
-                                         ClData& D, double (&gam)[CL_MAXC]) {
+                                         ClData<MA, MC>& D, double (&gam)[MC]) {
   bool fail = false;
 #pragma unroll
-  for (int c = 0; c < CL_MAXC; ++c) {
+  for (int c = 0; c < MC; ++c) {
     gam[c] = 0.0;
     if (c < D.nc) {
       const int li = T.pair[c] & 15, lj = T.pair[c] >> 4;
@@ -377,12 +380,12 @@ __device__ __forceinline__ bool cl_sweep(const ConArgs& A, const ClusterTab& T, 
     }
   }
 #pragma unroll
-  for (int a = 0; a < CL_MAXA; ++a) {
+  for (int a = 0; a < MA; ++a) {
     if (!D.active[a]) continue;
     const int al = T.alist[a], cnt = al & 15;
     double xt = 0.0, yt = 0.0, zt = 0.0;
 #pragma unroll
-    for (int e = 0; e < CL_MAXC; ++e) {
+    for (int e = 0; e < MC; ++e) {
       if (e < cnt) {
         const int code = (al >> (4 + 4 * e)) & 15, c = code >> 1;
         const double gh = sel(gam, c) * D.hm[a];
@@ -397,16 +400,18 @@ __device__ __forceinline__ bool cl_sweep(const ConArgs& A, const ClusterTab& T, 
   return fail;
 }
 
-__device__ __forceinline__ void ring_put(double* slot, const ClData& D, const double (&gam)[CL_MAXC]) {
+template <int MA, int MC>
+__device__ __forceinline__ void ring_put(double* slot, const ClData<MA, MC>& D, const double (&gam)[MC]) {
 #pragma unroll
-  for (int a = 0; a < CL_MAXA; ++a) { slot[3 * a] = D.x[a]; slot[3 * a + 1] = D.y[a]; slot[3 * a + 2] = D.z[a]; }
+  for (int a = 0; a < MA; ++a) { slot[3 * a] = D.x[a]; slot[3 * a + 1] = D.y[a]; slot[3 * a + 2] = D.z[a]; }
 #pragma unroll
-  for (int c = 0; c < CL_MAXC; ++c) slot[3 * CL_MAXA + c] = gam[c];
+  for (int c = 0; c < MC; ++c) slot[3 * CL_MAXA + c] = gam[c];
 }
 
 // SHAKE (rattle = false) or RATTLE (rattle = true) over all clusters; gsum
-// (CL_MAXC doubles per cluster) holds the committed gamma sums of SHAKE for
+// (MC doubles per cluster) holds the committed gamma sums of SHAKE for
 // the constraint stress
+template <int MA, int MC>
 __global__ void __launch_bounds__(128) k_constrain_cl(ConArgs A, const ClusterTab* __restrict__ tabs, int ncl,
                                                       double* __restrict__ ring, double* __restrict__ gsum,
                                                       int rattle_i) {
@@ -419,12 +424,12 @@ __global__ void __launch_bounds__(128) k_constrain_cl(ConArgs A, const ClusterTa
   for (;;) {
     for (int cl = tid; cl < ncl; cl += nth) {
       const ClusterTab T = tabs[cl];
-      ClData D;
+      ClData<MA, MC> D;
       cl_load(A, T, rattle, D);
       double* rg = ring + (size_t)cl * CL_RING * CL_SLOT;
-      double gam[CL_MAXC];
+      double gam[MC];
 #pragma unroll
-      for (int c = 0; c < CL_MAXC; ++c) gam[c] = 0.0;
+      for (int c = 0; c < MC; ++c) gam[c] = 0.0;
       ring_put(rg, D, gam);
       for (int s_ = 1; s_ <= CL_CHUNK; ++s_) {
         if (it0 + s_ > A.maxit) break;
@@ -444,7 +449,7 @@ __global__ void __launch_bounds__(128) k_constrain_cl(ConArgs A, const ClusterTa
       const double* rg = ring + (size_t)cl * CL_RING * CL_SLOT;
       const double* fin = rg + last * CL_SLOT;
 #pragma unroll
-      for (int a = 0; a < CL_MAXA; ++a) {
+      for (int a = 0; a < MA; ++a) {
         if (a < na) {
           const int i = T.atom[a];
           if (rattle) { A.vx[i] = fin[3 * a]; A.vy[i] = fin[3 * a + 1]; A.vz[i] = fin[3 * a + 2]; }
@@ -454,7 +459,7 @@ __global__ void __launch_bounds__(128) k_constrain_cl(ConArgs A, const ClusterTa
       if (!rattle) {
         for (int s_ = 1; s_ <= last; ++s_)
 #pragma unroll
-          for (int c = 0; c < CL_MAXC; ++c)
+          for (int c = 0; c < MC; ++c)
             if (c < nc) gsum[(size_t)cl * CL_MAXC + c] += rg[s_ * CL_SLOT + 3 * CL_MAXA + c];
       }
     }
@@ -479,7 +484,7 @@ __global__ void __launch_bounds__(128) k_constrain_cl(ConArgs A, const ClusterTa
       const ClusterTab T = tabs[cl];
       const int nc = (T.meta >> 4) & 15;
 #pragma unroll
-      for (int c = 0; c < CL_MAXC; ++c) {
+      for (int c = 0; c < MC; ++c) {
         if (c >= nc) continue;
         const int k = T.con[c];
         const double g = gsum[(size_t)cl * CL_MAXC + c];
@@ -519,6 +524,7 @@ double* d_clring = nullptr;  // per-cluster state ring (CL_RING slots of CL_SLOT
 double* d_clgsum = nullptr;  // per-cluster committed SHAKE gamma sums
 int n_clusters = 0, coop_blocks_cl = 0;
 constexpr int CL_THREADS = 128;  // small blocks spread the clusters over every SM
+const void* cl_kernel = nullptr;  // k_constrain_cl instantiation for the largest cluster
 
 // connected constraint clusters; false when one exceeds CL_MAXA atoms or CL_MAXC constraints
 bool build_clusters(const std::vector<int>& ci, const std::vector<int>& cj, std::vector<ClusterTab>& out) {
@@ -635,7 +641,12 @@ void integ_setup_constraints(const int32_t* listcon, const double* prmcon) {
     GB_CUDA(cudaMemcpy(d_cltab, tabs.data(), sizeof(ClusterTab) * tabs.size(), cudaMemcpyHostToDevice));
     GB_CUDA(cudaMalloc(&d_clring, sizeof(double) * CL_RING * CL_SLOT * tabs.size()));
     GB_CUDA(cudaMalloc(&d_clgsum, sizeof(double) * CL_MAXC * tabs.size()));
-    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_constrain_cl, CL_THREADS, 0));
+    // rigid 3-site molecules get register arrays sized 3 x 3 (more resident warps)
+    bool small = true;
+    for (const ClusterTab& T : tabs)
+      if ((T.meta & 15) > 3 || ((T.meta >> 4) & 15) > 3) small = false;
+    cl_kernel = small ? (const void*)k_constrain_cl<3, 3> : (const void*)k_constrain_cl<CL_MAXA, CL_MAXC>;
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, cl_kernel, CL_THREADS, 0));
     coop_blocks_cl = std::max(1, std::min(bps * g.nsm, nblocks(n_clusters, CL_THREADS)));
   }
 }
@@ -704,7 +715,7 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
         double *ring = d_clring, *gsum = d_clgsum;
         GB_CUDA(cudaMemsetAsync(d_clgsum, 0, sizeof(double) * CL_MAXC * n_clusters, st));
         void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
-        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_constrain_cl, nbs, CL_THREADS, args, 0, st));
+        GB_CUDA(cudaLaunchCooperativeKernel(cl_kernel, nbs, CL_THREADS, args, 0, st));
       } else {
         void* args[] = {&A};
         GB_CUDA(cudaLaunchCooperativeKernel((void*)k_shake, nbs, 256, args, 0, st));
@@ -738,7 +749,7 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
         int ncl = n_clusters, rattle = 1;
         double *ring = d_clring, *gsum = d_clgsum;
         void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
-        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_constrain_cl, coop_blocks_cl, CL_THREADS, args, 0, st));
+        GB_CUDA(cudaLaunchCooperativeKernel(cl_kernel, coop_blocks_cl, CL_THREADS, args, 0, st));
       } else {
         void* args[] = {&A};
         GB_CUDA(cudaLaunchCooperativeKernel((void*)k_rattle, coop_blocks_rattle, 256, args, 0, st));

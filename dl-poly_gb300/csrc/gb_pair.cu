@@ -308,7 +308,7 @@ __constant__ float4 c_lj[MAX_KEYS];
 // same whatever the order the warps and atomics run in.  Halo pairs are
 // evaluated from the side with the smaller global id and applied to the
 // image's source atom, as in the FP64 kernel.
-__global__ void __launch_bounds__(256, 3) k_pair_mixed_half(int natms, const DevScalars* sc,
+__global__ void __launch_bounds__(256, 4) k_pair_mixed_half(int natms, const DevScalars* sc,
                                                          const int* __restrict__ at_list,
                                                          const int* __restrict__ list, int ld,
                                                          const float4* __restrict__ xf, const float4* __restrict__ xlo,
@@ -325,9 +325,9 @@ __global__ void __launch_bounds__(256, 3) k_pair_mixed_half(int natms, const Dev
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  float a[NACC], c[NACC];
-#pragma unroll
-  for (int k = 0; k < NACC; ++k) { a[k] = 0.f; c[k] = 0.f; }
+  // lane k < NACC keeps the compensated running sum of quantity k over the
+  // warp's atoms (2 registers instead of 2 x NACC per lane)
+  float a_k = 0.f, c_k = 0.f;
   unsigned long long n_list = 0, n_rc = 0;
   const int nlast = sc->nlast;
   // persistent warps walk the atoms in cell order (neighbouring atoms share j data in L1)
@@ -397,9 +397,12 @@ __global__ void __launch_bounds__(256, 3) k_pair_mixed_half(int natms, const Dev
     }
 #pragma unroll
     for (int k = 0; k < NACC; ++k) {
-      const float y = t[k] - c[k], tt = a[k] + y;
-      c[k] = (tt - a[k]) - y;
-      a[k] = tt;
+      const float v = warp_sumf(t[k]);  // this atom's share, in every lane
+      if (lane == k) {
+        const float y = v - c_k, tt = a_k + y;
+        c_k = (tt - a_k) - y;
+        a_k = tt;
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -415,8 +418,9 @@ __global__ void __launch_bounds__(256, 3) k_pair_mixed_half(int natms, const Dev
     }
   }
   double acc[NACC];
+  const double own = (double)a_k - (double)c_k;
 #pragma unroll
-  for (int k = 0; k < NACC; ++k) acc[k] = (double)a[k] - (double)c[k];
+  for (int k = 0; k < NACC; ++k) acc[k] = (lane == k) ? own : 0.0;
   n_rc = (unsigned long long)warp_sumi((int)n_rc);
   if (lane == 0) {
     atomicAdd(&cnt[0], n_list);
