@@ -510,7 +510,17 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=10000)
     ap.add_argument("--drift-train", type=int, default=2000)
     ap.add_argument("--drift-forms", default="fp64,mixed,mts_k4,mts_k8")
+    ap.add_argument("--emit", metavar="DIR", default=None,
+                    help="write the workload as DL_POLY CONFIG/FIELD/CONTROL plus raw arrays and exit")
     args = ap.parse_args()
+    if args.emit:
+        from dlpoly_gb300 import dlpoly_io
+
+        s, _ = workload(args.workload)
+        temp = 1500.0 if args.workload.startswith("nacl") else 300.0
+        dlpoly_io.emit_inputs(s, args.emit, steps=args.steps, temperature=temp, stats_every=1)
+        print(json.dumps({"emitted": args.emit, "workload": args.workload, "natms": s.natms}))
+        return
     if args.drift:
         run_drift(args)
         return

@@ -622,7 +622,7 @@ int gb_md_run(int nsteps, gb_step_stats* stats) {
       GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
       GB_CUDA(cudaEventRecord(g.ev[0], g.stream));
       int it = 0;
-      integ_vv(1, nullptr, nullptr, &it, &S.vircon, nullptr);
+      integ_vv(1, nullptr, nullptr, &it, &S.vircon, S.strcon);
       S.shake_iters = it;
       GB_CUDA(cudaEventRecord(g.ev[1], g.stream));
       int32_t upd = 0;

@@ -247,7 +247,8 @@ class PathLib:
 
 
 def stats_to_dict(s: GbStepStats) -> dict:
-    d = {k: getattr(s, k) for k, _ in GbStepStats._fields_ if k not in ("stress", "strkin")}
+    d = {k: getattr(s, k) for k, _ in GbStepStats._fields_ if k not in ("stress", "strkin", "strcon")}
     d["stress"] = np.array(s.stress[:])
     d["strkin"] = np.array(s.strkin[:])
+    d["strcon"] = np.array(s.strcon[:])
     return d

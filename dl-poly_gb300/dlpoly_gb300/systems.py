@@ -63,6 +63,7 @@ class GbStepStats(ctypes.Structure):
         ("engvdw", ctypes.c_double), ("virvdw", ctypes.c_double),
         ("engke", ctypes.c_double), ("vircon", ctypes.c_double),
         ("stress", ctypes.c_double * 9), ("strkin", ctypes.c_double * 9),
+        ("strcon", ctypes.c_double * 9),
         ("list_rebuilt", ctypes.c_int32), ("shake_iters", ctypes.c_int32),
         ("rattle_iters", ctypes.c_int32), ("mts_full", ctypes.c_int32),
     ]
@@ -104,6 +105,9 @@ class System:
     max_exclude: int = 0
     list_excl: np.ndarray | None = None
     vdw_direct: int = 0
+    type_names: tuple = ()      # site name per 1-based type (FIELD 'atoms' records)
+    epsq: float = 1.0           # relative dielectric constant
+    shake_maxit: int = 250
 
     @property
     def natms(self) -> int:
@@ -126,7 +130,7 @@ class System:
         p.rpad = self.rpad
         p.rvdw = self.rcut
         p.alpha = self.alpha
-        p.epsq = 1.0
+        p.epsq = self.epsq
         p.tstep = self.tstep
         p.shake_tol = self.shake_tol
         p.pdplnc = 50.0
@@ -136,7 +140,7 @@ class System:
         # bounds.F90:1249: padded spline halo, ~2% over the order
         p.spline_pad = self.nsplines + int(math.ceil(0.02 * self.nsplines))
         p.vdw_direct = self.vdw_direct
-        p.shake_maxit = 250
+        p.shake_maxit = self.shake_maxit
         dens = self.natms / self.volume()
         rcx = self.rcut + self.rpad
         # bounds.F90:907 style capacity: density * (7.5/3) * pi * rcx^3
@@ -201,7 +205,8 @@ def nacl_melt(n_side: int = 16, seed: int = 1234, spacing: float = 2.82, temp: f
                   lfrzn=np.zeros(n, np.int32), vdw_prm=np.array(prm, np.float64),
                   x=pos[:, 0].copy(), y=pos[:, 1].copy(), z=pos[:, 2].copy(),
                   vx=v[:, 0].copy(), vy=v[:, 1].copy(), vz=v[:, 2].copy(),
-                  rcut=rcut, rpad=1.0, alpha=alpha, kmax=(kmax, kmax, kmax), ntypes=2)
+                  rcut=rcut, rpad=1.0, alpha=alpha, kmax=(kmax, kmax, kmax), ntypes=2,
+                  type_names=("Na", "Cl"))
 
 
 def _random_rotations(rng, n):
@@ -274,7 +279,8 @@ def spce_water(n_side: int = 32, seed: int = 4321, temp: float = 300.0, rcut: fl
                   x=pos[:, 0].copy(), y=pos[:, 1].copy(), z=pos[:, 2].copy(),
                   vx=v[:, 0].copy(), vy=v[:, 1].copy(), vz=v[:, 2].copy(),
                   rcut=rcut, rpad=1.0, alpha=alpha, kmax=(kmax, kmax, kmax), ntypes=2,
-                  listcon=listcon, prmcon=prmcon, max_exclude=2, list_excl=excl)
+                  listcon=listcon, prmcon=prmcon, max_exclude=2, list_excl=excl,
+                  type_names=("OW", "HW"))
 
 
 def _rattle_project(v, pos, mass, listcon, L):
@@ -316,4 +322,5 @@ def lj_pair(eps: float = 1.0, sigma: float = 2.0, r: float = 1.0, box: float = 4
                   chge=np.zeros(2), weight=np.ones(2), lfrzn=np.zeros(2, np.int32),
                   vdw_prm=np.array([1.0, eps, sigma]), x=np.array([0.0, r]), y=np.zeros(2),
                   z=np.zeros(2), vx=np.zeros(2), vy=np.zeros(2), vz=np.zeros(2), rcut=10.0,
-                  rpad=0.5, alpha=0.3, kmax=(16, 16, 16), ntypes=1, vdw_direct=1)
+                  rpad=0.5, alpha=0.3, kmax=(16, 16, 16), ntypes=1, vdw_direct=1,
+                  type_names=("Ar",))

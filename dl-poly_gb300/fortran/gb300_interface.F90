@@ -25,7 +25,7 @@ Module gb300_interface
   Type, Bind(C), Public :: gb_step_stats
     Real(c_double) :: engcpe_rc, vircpe_rc, engcpe_rl, vircpe_rl, engcpe_ex, vircpe_ex, engvdw, virvdw
     Real(c_double) :: engke, vircon
-    Real(c_double) :: stress(9), strkin(9)
+    Real(c_double) :: stress(9), strkin(9), strcon(9)
     Integer(c_int32_t) :: list_rebuilt, shake_iters, rattle_iters, mts_full
   End Type gb_step_stats
 

@@ -86,6 +86,7 @@ typedef struct gb_step_stats {
   double vircon;                /* constraint virial */
   double stress[9];             /* configurational stress (two-body + SPME) */
   double strkin[9];             /* kinetic stress */
+  double strcon[9];             /* constraint stress of the SHAKE stage (stats%strcon) */
   int32_t list_rebuilt;         /* 1 if the Verlet list was rebuilt this step */
   int32_t shake_iters, rattle_iters;
   int32_t mts_full;             /* 1 if full SPME ran this step (learned-MTS form) */

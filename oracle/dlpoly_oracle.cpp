@@ -1538,7 +1538,7 @@ int orc_md_run(int nsteps, gb_step_stats* stats) {
     gb_step_stats S;
     std::memset(&S, 0, sizeof(S));
     int it = 0;
-    int st = nve_vv(1, nullptr, nullptr, &it, &S.vircon, nullptr);
+    int st = nve_vv(1, nullptr, nullptr, &it, &S.vircon, S.strcon);
     if (st) return st;
     S.shake_iters = it;
     int32_t upd = 0;

@@ -98,6 +98,8 @@ def test_md_steps_fp64(gpu_lib, oracle_lib, name, nsteps):
     for x, y in zip(sd, sr):
         assert x.engke == pytest.approx(y.engke, rel=1e-9)
         assert x.engcpe_rl == pytest.approx(y.engcpe_rl, rel=1e-9)
+        cs = max(np.abs(y.strcon[:]).max(), 1e-30)
+        assert np.abs(np.array(x.strcon[:]) - np.array(y.strcon[:])).max() <= 1e-8 * cs
 
 
 def test_cluster_constraints_match_global_sweeps(gpu_lib, monkeypatch):
