@@ -445,6 +445,8 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     mts_set_topology(ntcons, listcon, weight);
     list_setup();
     spme_setup();
+    g.nstep = 0;
+    thermo_setup(GB_NVE, 0.0, 0.0, 0.0, nullptr, 0.0);
     g.init = true;
     g.launches = 0;
     return GB_OK;
@@ -611,6 +613,51 @@ int gb_vv(int stage, double* strkin, double* engke, int32_t* iters, double* virc
   });
 }
 
+int gb_set_ensemble(int kind, double temp, double tau_t, double chi, const int32_t* seed, double degfre) {
+  return guarded([&]() {
+    if (!g.init) return (int)GB_ERR_NOT_INIT;
+    if (kind < GB_NVE || kind > GB_NVT_LANGEVIN) return (int)GB_ERR_ARG;
+    if (kind != GB_NVE && !(temp > 0.0)) return (int)GB_ERR_ARG;
+    if ((kind == GB_NVT_BERENDSEN || kind == GB_NVT_NOSE_HOOVER) && !(tau_t > 0.0)) return (int)GB_ERR_ARG;
+    if (kind == GB_NVT_LANGEVIN && !(chi >= 0.0)) return (int)GB_ERR_ARG;
+    thermo_setup(kind, temp, tau_t, chi, seed, degfre);
+    return (int)GB_OK;
+  });
+}
+
+int gb_set_step(int32_t nstep) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  g.nstep = nstep;
+  return GB_OK;
+}
+
+int gb_thermostat_state(double* chi_t, double* cint, double* consv) {
+  return guarded([&]() {
+    if (!g.init) return (int)GB_ERR_NOT_INIT;
+    thermo_state(chi_t, cint, consv);
+    return (int)GB_OK;
+  });
+}
+
+int gb_set_thermostat_state(double chi_t, double cint) {
+  return guarded([&]() {
+    if (!g.init) return (int)GB_ERR_NOT_INIT;
+    thermo_set_state(chi_t, cint);
+    return (int)GB_OK;
+  });
+}
+
+int gb_rng_eval(int mode, int n, const int64_t* a, const int64_t* b, const int64_t* c, double* out) {
+  return guarded([&]() {
+    if (!g.init) return (int)GB_ERR_NOT_INIT;
+    if ((mode != 0 && mode != 1) || n < 0 || (n > 0 && (!a || !b || !c || !out))) return (int)GB_ERR_ARG;
+    GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
+    rng_eval(mode, n, a, b, c, out);
+    gb_sync_scalars();
+    return (g.hsc->status & ST_RNG) ? (int)GB_ERR_RNG : (int)GB_OK;
+  });
+}
+
 int gb_md_run(int nsteps, gb_step_stats* stats) {
   return guarded([&]() {
     if (nsteps < 0) return (int)GB_ERR_ARG;
@@ -621,6 +668,7 @@ int gb_md_run(int nsteps, gb_step_stats* stats) {
       std::memset(&S, 0, sizeof(S));
       GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
       GB_CUDA(cudaEventRecord(g.ev[0], g.stream));
+      ++g.nstep;  // flow%step of this step (drivers.F90 advances it before stage 1)
       int it = 0;
       integ_vv(1, nullptr, nullptr, &it, &S.vircon, S.strcon);
       S.shake_iters = it;
@@ -644,6 +692,7 @@ int gb_md_run(int nsteps, gb_step_stats* stats) {
       integ_vv(2, S.strkin, &S.engke, &it, nullptr, nullptr);
       S.rattle_iters = it;
       S.mts_full = full ? 1 : 0;
+      S.consv = g.ens == GB_NVT_NOSE_HOOVER ? g.hsc->th[7] : 0.0;
       GB_CUDA(cudaEventRecord(g.ev[4], g.stream));
       GB_CUDA(cudaEventSynchronize(g.ev[4]));
       float ms;
@@ -811,6 +860,7 @@ const char* gb_strerror(int status) {
     case GB_ERR_ARG: return "invalid argument";
     case GB_ERR_NO_DEVICE: return "no CUDA device";
     case GB_ERR_NONFINITE: return "non-finite positions";
+    case GB_ERR_RNG: return "a Gaussian deviate's rejection loop hit its iteration cap";
     case GB_ERR_TOO_LARGE: return "size exceeds the fixed scratch limit of gb_kinstress_noalloc (1,048,576 atoms)";
     default: return "unknown status";
   }

@@ -21,6 +21,7 @@ enum : int {
   ST_NONFINITE = 16,
   ST_CELL_RANGE = 32,
   ST_SPME_RANGE = 64,
+  ST_RNG = 128,          // a Box-Muller rejection loop hit its cap
 };
 
 // Device-resident scalars: one small block so a single copy returns them all.
@@ -38,7 +39,8 @@ struct DevScalars {
   double maxdisp;   // largest displacement since the last rebuild
   unsigned long long npairs_list;  // half-list entries walked by the pair kernel
   unsigned long long npairs_rc;    // unique pairs inside the cutoff
-  double acc[64];   // energy / virial / stress accumulators
+  double acc[80];   // energy / virial / stress accumulators
+  double th[8];     // thermostat state: chi_t, cint, scale, vom(3), engke, consv
 };
 
 // accumulator slots in DevScalars::acc
@@ -49,7 +51,8 @@ enum {
   A_GATHER = 30,      // 4 slots: reciprocal energy, net force (before scale)
   A_STRKIN = 40,      // 6 slots
   A_STRCON = 50,      // 6 slots
-  A_NSLOTS = 64
+  A_KINMOM = 64,      // 9 slots: kinetic stress (6), momentum (3) of the thermostat stages
+  A_NSLOTS = 80
 };
 
 // Kernel regions timed with CUDA events when profiling is on.
@@ -106,6 +109,13 @@ struct Dev {
   int* list_excl = nullptr;    // (max_exclude+1)*natms
   bool lbook = false;
   int megfrz = 0;
+  // thermostat of the VV stages (gb_thermostat.cu)
+  int ens = 0;                 // GB_NVE, GB_NVT_BERENDSEN, GB_NVT_NOSE_HOOVER, GB_NVT_LANGEVIN
+  double temp = 0, tau_t = 0, chi_fric = 0;
+  double sigma = 0, qmass = 0, ceng = 0, totmas = 0, degfre = 0;
+  double lang_t0 = 0, lang_t1 = 0, lang_scr = 0, lang_scl = 0, lang_scv = 0;
+  int seed[3] = {0, 0, 0};
+  int nstep = 0;               // flow%step of the current (or next) stage-1 call
   // mixed-precision full list (derived, transposed by atom)
   int* flist = nullptr;        // full list entries
   int* fcount = nullptr;       // per atom count
@@ -297,6 +307,13 @@ int integ_vnl_check();
 void integ_zero_forces();
 void integ_forces_to_fp64();      // mixed: fixed point -> FP64 forces
 void integ_setup_constraints(const int32_t* listcon, const double* prmcon);
+// thermostats (gb_thermostat.cu)
+void thermo_setup(int kind, double temp, double tau_t, double chi, const int32_t* seed, double degfre);
+bool thermo_vv1(double hstep, double tstep);              // NH / Langevin stage-1 update; false: plain VV
+bool thermo_vv2_finish(double* strkin, double* engke);   // stage 2 after RATTLE; false: plain kinstress
+void thermo_state(double* chi_t, double* cint, double* consv);
+void thermo_set_state(double chi_t, double cint);
+void rng_eval(int mode, int n, const int64_t* a, const int64_t* b, const int64_t* c, double* out);
 // learned multiple-time-step form (gb_mlp.cu)
 void mts_set_topology(int ntcons, const int32_t* listcon, const double* weight);
 void mts_setup();

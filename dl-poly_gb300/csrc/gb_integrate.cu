@@ -697,8 +697,11 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
   }
   if (stage == 1) {
     prof_begin(P_VV);
-    k_vv1<<<nblocks(n, 256), 256, 0, st>>>(n, hstep, tstep, g.weight, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz, g.x, g.y, g.z);
-    GB_LAUNCHED();
+    if (!thermo_vv1(hstep, tstep)) {
+      k_vv1<<<nblocks(n, 256), 256, 0, st>>>(n, hstep, tstep, g.weight, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz, g.x, g.y,
+                                             g.z);
+      GB_LAUNCHED();
+    }
     prof_end(P_VV);
     if (g.ntcons > 0) {
       k_copy3<<<nblocks(n, 256), 256, 0, st>>>(n, g.x, g.y, g.z, g.ox, g.oy, g.oz);
@@ -757,17 +760,20 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
       GB_LAUNCHED();
       prof_end(P_RATTLE);
     }
-    const int nb = nblocks(n, 256);
-    double* blk = gb_blkacc(nb * 6);
-    k_kinstress<<<nb, 256, 0, st>>>(n, g.weight, g.lfrzn, g.vx, g.vy, g.vz, blk);
-    GB_LAUNCHED();
-    gb_reduce_blocks(blk, nb, 6, &g.sc->acc[A_STRKIN]);
-    gb_sync_scalars();
+    if (!thermo_vv2_finish(strkin, engke)) {
+      const int nb = nblocks(n, 256);
+      double* blk = gb_blkacc(nb * 6);
+      k_kinstress<<<nb, 256, 0, st>>>(n, g.weight, g.lfrzn, g.vx, g.vy, g.vz, blk);
+      GB_LAUNCHED();
+      gb_reduce_blocks(blk, nb, 6, &g.sc->acc[A_STRKIN]);
+      gb_sync_scalars();
+      const double* s = &g.hsc->acc[A_STRKIN];
+      double sk[9] = {s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]};
+      if (strkin) for (int k = 0; k < 9; ++k) strkin[k] = sk[k];
+      if (engke) *engke = 0.5 * (sk[0] + sk[4] + sk[8]);
+    }
     if (iters && g.ntcons > 0) *iters = g.hsc->rattle_iters;
-    const double* s = &g.hsc->acc[A_STRKIN];
-    double sk[9] = {s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]};
-    if (strkin) for (int k = 0; k < 9; ++k) strkin[k] = sk[k];
-    if (engke) *engke = 0.5 * (sk[0] + sk[4] + sk[8]);
     if (g.ntcons > 0 && (g.hsc->status & ST_RATTLE_FAIL)) throw (int)GB_ERR_RATTLE;
+    if (g.hsc->status & ST_RNG) throw (int)GB_ERR_RNG;
   }
 }

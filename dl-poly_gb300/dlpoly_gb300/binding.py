@@ -189,6 +189,44 @@ class PathLib:
         f.argtypes = args
         return f
 
+    # ------------------------------------------------ ensembles of the VV stages
+    ENSEMBLES = {"nve": 0, "berendsen": 1, "nose-hoover": 2, "langevin": 3}
+
+    def set_ensemble(self, kind, temp: float = 0.0, tau_t: float = 0.0, chi: float = 0.0, seed=None,
+                     degfre: float = 0.0):
+        k = self.ENSEMBLES[kind] if isinstance(kind, str) else int(kind)
+        sd = None if seed is None else np.ascontiguousarray(seed, np.int32)
+        st = self._opt("set_ensemble", c_int, [c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _i,
+                                               ctypes.c_double])(k, temp, tau_t, chi, _ptr(sd, _i), degfre)
+        if st != 0:
+            raise PathError(st, self.prefix + "set_ensemble", self.strerror(st))
+
+    def set_step(self, nstep: int):
+        self._opt("set_step", c_int, [ctypes.c_int32])(int(nstep))
+
+    def thermostat_state(self) -> dict:
+        v = np.zeros(3)
+        st = self._opt("thermostat_state", c_int, [_d, _d, _d])(_ptr(v[0:1], _d), _ptr(v[1:2], _d),
+                                                                _ptr(v[2:3], _d))
+        if st != 0:
+            raise PathError(st, self.prefix + "thermostat_state", self.strerror(st))
+        return {"chi_t": float(v[0]), "cint": float(v[1]), "consv": float(v[2])}
+
+    def set_thermostat_state(self, chi_t: float, cint: float):
+        st = self._opt("set_thermostat_state", c_int, [ctypes.c_double, ctypes.c_double])(chi_t, cint)
+        if st != 0:
+            raise PathError(st, self.prefix + "set_thermostat_state", self.strerror(st))
+
+    def rng_eval(self, mode: int, a, b, c):
+        _l = POINTER(ctypes.c_int64)
+        a, b, c = (np.ascontiguousarray(v, np.int64) for v in (a, b, c))
+        out = np.zeros(a.size * (1 if mode == 0 else 3))
+        st = self._opt("rng_eval", c_int, [c_int, c_int, _l, _l, _l, _d])(mode, a.size, _ptr(a, _l), _ptr(b, _l),
+                                                                       _ptr(c, _l), _ptr(out, _d))
+        if st != 0:
+            raise PathError(st, self.prefix + "rng_eval", self.strerror(st))
+        return out if mode == 0 else out.reshape(-1, 3)
+
     def mts_config(self, k: int, tol: float = 1e-4, train_steps: int = 0):
         st = self._opt("mts_config", c_int, [c_int, ctypes.c_double, c_int])(k, tol, train_steps)
         if st != 0:

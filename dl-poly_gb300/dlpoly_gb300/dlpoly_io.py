@@ -388,6 +388,10 @@ KEYS = {
     "time_run": ("float", "steps"),
     "time_equilibration": ("float", "steps"),
     "ensemble": ("option", None),
+    "ensemble_method": ("option", None),
+    "ensemble_thermostat_coupling": ("float", "time"),
+    "ensemble_thermostat_friction": ("float", "invtime"),
+    "random_seed": ("vector", None),
     "temperature": ("float", "temperature"),
     "restart": ("option", None),
     "coul_method": ("option", None),
@@ -425,6 +429,7 @@ _UNITS = {
                "bohr": 0.52917721092, "pm": 0.01},
     "invlength": {"": 1.0, "ang^-1": 1.0, "1/ang": 1.0, "internal_l^-1": 1.0, "nm^-1": 0.1},
     "time": {"": 1.0, "ps": 1.0, "internal_t": 1.0, "fs": 1.0e-3, "ns": 1.0e3},
+    "invtime": {"": 1.0, "ps^-1": 1.0, "1/ps": 1.0, "internal_t^-1": 1.0, "fs^-1": 1.0e3, "ns^-1": 1.0e-3},
     "temperature": {"": 1.0, "k": 1.0},
     "steps": {"": 1.0, "steps": 1.0, "step": 1.0},
 }
@@ -511,7 +516,8 @@ def read_control(path, keys=None) -> dict:
     return out
 
 
-_WRITE_UNITS = {"length": "ang", "invlength": "ang^-1", "time": "ps", "temperature": "K", "steps": "steps"}
+_WRITE_UNITS = {"length": "ang", "invlength": "ang^-1", "time": "ps", "invtime": "ps^-1", "temperature": "K",
+                "steps": "steps"}
 
 
 def write_control(path, values: dict, keys=None) -> None:
@@ -671,8 +677,7 @@ def system_from_files(cfg: Config, fld: Field, ctl: dict) -> System:
     i of the CONFIG; FIELD molecule types assign sites to atoms in the same order."""
     c = dict(CONTROL_DEFAULTS)
     c.update(ctl)
-    if c["ensemble"] != "nve":
-        raise NotImplementedError(f"ensemble '{c['ensemble']}': only nve runs on this path")
+    ensemble_from_control(c)                       # refuses ensembles outside the path
     if c["coul_method"] != "spme":
         raise NotImplementedError(f"coul_method '{c['coul_method']}': only spme runs on this path")
     if "cutoff" not in c:
@@ -753,6 +758,34 @@ def system_from_files(cfg: Config, fld: Field, ctl: dict) -> System:
         max_exclude=maxex, list_excl=list_excl, vdw_direct=1 if c["vdw_method"] == "direct" else 0,
         type_names=tuple(names), epsq=float(c["coul_dielectric_constant"]),
         shake_maxit=int(c["shake_max_iter"]))
+
+
+_NVT_METHODS = {"berendsen": "berendsen", "hoover": "nose-hoover", "nose": "nose-hoover",
+                "nose-hoover": "nose-hoover", "langevin": "langevin"}
+
+
+def ensemble_from_control(ctl: dict) -> dict:
+    """Ensemble of the VV stages from CONTROL, as control.F90:570-640 selects it:
+    'ensemble nve', or 'ensemble nvt' with 'ensemble_method' berendsen / hoover
+    (tau_t from ensemble_thermostat_coupling) or langevin (chi from
+    ensemble_thermostat_friction), at 'temperature', with 'random_seed' shifts."""
+    ens = str(ctl.get("ensemble", "nve")).lower()
+    if ens in ("nve", "pmf"):
+        return {"kind": "nve"}
+    if ens != "nvt":
+        raise NotImplementedError(f"ensemble '{ens}': nve and nvt run on this path")
+    method = str(ctl.get("ensemble_method", "")).lower()
+    if method not in _NVT_METHODS:
+        raise NotImplementedError(f"nvt ensemble_method '{method}': berendsen, hoover and langevin run here")
+    kind = _NVT_METHODS[method]
+    out = {"kind": kind, "temp": float(ctl.get("temperature", 0.0)),
+           "tau_t": float(ctl.get("ensemble_thermostat_coupling", 0.0)),
+           "chi": float(ctl.get("ensemble_thermostat_friction", 0.0))}
+    if "random_seed" in ctl:
+        out["seed"] = tuple(int(round(x)) for x in ctl["random_seed"][:3])
+    if kind == "langevin" and "ensemble_thermostat_friction" not in ctl:
+        raise ValueError("nvt langevin needs ensemble_thermostat_friction")
+    return out
 
 
 def emit_inputs(s: System, directory, steps: int, temperature: float, stats_every: int = 1,
@@ -874,8 +907,9 @@ class Statistics:
         al, be, ga = _cell_angles(cell)
         v = self.stpval
         v[:] = 0.0
-        v[0] = 0.0                                         # conserved-quantity extension (NVE: 0)
-        v[1] = stpeng / eu
+        consv = float(st.get("consv", 0.0))              # thermostat's conserved-energy term
+        v[0] = consv / eu
+        v[1] = (stpeng + consv) / eu
         v[2] = stptmp
         v[3] = stpcfg / eu
         v[4] = engsrp / eu
@@ -924,9 +958,10 @@ class Statistics:
     # REVIVE, unformatted branch of system_revive: records of reals, each framed by
     # 4-byte little-endian lengths as gfortran writes sequential unformatted files.
     def write_revive(self, path, rcut: float, megatm: int, nstep: int, tstep: float, time: float,
-                     tmst: float, strcon, stress, rbin: float = 0.05) -> None:
+                     tmst: float, strcon, stress, rbin: float = 0.05, chi_t: float = 0.0,
+                     cint: float = 0.0) -> None:
         recs = [np.array([rcut, rbin, float(megatm)]),
-                np.array([float(nstep), tstep, time, tmst, float(self.numacc), 0.0, 0.0, 0.0]),
+                np.array([float(nstep), tstep, time, tmst, float(self.numacc), chi_t, 0.0, cint]),
                 np.zeros(9),                              # thermo%eta
                 self.stpval, self.stpvl0, self.sumval, self.ssqval, self.zumval, self.ravval,
                 self.stkval.T.reshape(-1),                # stkval(1:mxstak, 0:mxnstk), column-major
@@ -957,4 +992,5 @@ class Statistics:
         self.numacc = int(recs[1][4])
         return {"rcut": recs[0][0], "rbin": recs[0][1], "megatm": int(recs[0][2]),
                 "nstep": int(recs[1][0]), "tstep": recs[1][1], "time": recs[1][2], "tmst": recs[1][3],
+                "chi_t": recs[1][5], "cint": recs[1][7],
                 "strcon": recs[10], "strpmf": recs[11], "stress": recs[12]}

@@ -13,8 +13,10 @@ gb_md_run) and writes what the reference's NVE run writes for this path:
   REVCON  levcfg 2 every data_dump_frequency steps and at the end (configuration.F90:2446)
   REVIVE  accumulators at the same points (system.F90:1831, unformatted branch)
 
-'restart noscale' keeps the CONFIG velocities, 'scale' rescales them to the
-temperature key, 'continue' keeps them and reads REVIVE.  'clean' draws new
+'ensemble nve' or 'ensemble nvt' with ensemble_method berendsen, hoover or
+langevin selects the VV stages (gb_set_ensemble).  'restart noscale' keeps the
+CONFIG velocities, 'scale' rescales them to the temperature key, 'continue' keeps
+them and reads REVIVE (statistics and the thermostat's chi_t and cint).  'clean' draws new
 Maxwell-Boltzmann velocities from a fixed seed (the reference's random stream is
 not reproduced) and is refused for systems with constraints.
 
@@ -114,6 +116,12 @@ def run(directory: str, steps: int | None = None, lib=None, quiet: bool = False)
         lib = load()
     precision = {"fp64": 0, "mixed": 1}[gb.get("gb_precision", "fp64")]
     lib.init(s, precision=precision, device=int(gb.get("gb_device", 0)))
+    ens = io.ensemble_from_control(ctl)
+    if ens["kind"] != "nve":
+        lib.set_ensemble(ens["kind"], ens["temp"], ens["tau_t"], ens["chi"], ens.get("seed"), stats.degfre)
+        if restart == "continue" and os.path.exists(revive):
+            lib.set_thermostat_state(info["chi_t"], info["cint"])
+    lib.set_step(nstep0)
     if int(gb.get("gb_mts_k", 1)) > 1:
         lib.mts_config(int(gb["gb_mts_k"]), float(gb.get("gb_mts_tol", 1e-4)), int(gb.get("gb_mts_train", 0)))
     e0, s0 = lib.start()
@@ -151,9 +159,10 @@ def run(directory: str, steps: int | None = None, lib=None, quiet: bool = False)
                          vel=np.stack([d["vx"], d["vy"], d["vz"]], 1), frc=frc,
                          step=nstep, tstep=s.tstep, time=tnow)
         io.write_config(j(ctl.get("io_file_revcon", "REVCON")), snap)
+        th = lib.thermostat_state()
         stats.write_revive(revive, s.rcut, s.natms, nstep, s.tstep, tnow, time0,
                            last_stats.get("strcon", np.zeros(9)), last_stats["stress"],
-                           rbin=float(ctl.get("rdf_binsize", 0.05)))
+                           rbin=float(ctl.get("rdf_binsize", 0.05)), chi_t=th["chi_t"], cint=th["cint"])
 
     t_wall = _time.perf_counter()
     nstep, done = nstep0, 0
@@ -173,6 +182,7 @@ def run(directory: str, steps: int | None = None, lib=None, quiet: bool = False)
             d["stress"] = np.array(rec.stress[:])
             d["strkin"] = np.array(rec.strkin[:])
             d["strcon"] = np.array(rec.strcon[:])
+            d["consv"] = rec.consv
             list_rebuilds += rec.list_rebuilt
             shake += rec.shake_iters
             rattle += rec.rattle_iters

@@ -64,6 +64,7 @@ class GbStepStats(ctypes.Structure):
         ("engke", ctypes.c_double), ("vircon", ctypes.c_double),
         ("stress", ctypes.c_double * 9), ("strkin", ctypes.c_double * 9),
         ("strcon", ctypes.c_double * 9),
+        ("consv", ctypes.c_double),
         ("list_rebuilt", ctypes.c_int32), ("shake_iters", ctypes.c_int32),
         ("rattle_iters", ctypes.c_int32), ("mts_full", ctypes.c_int32),
     ]

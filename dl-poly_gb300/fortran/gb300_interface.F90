@@ -26,6 +26,7 @@ Module gb300_interface
     Real(c_double) :: engcpe_rc, vircpe_rc, engcpe_rl, vircpe_rl, engcpe_ex, vircpe_ex, engvdw, virvdw
     Real(c_double) :: engke, vircon
     Real(c_double) :: stress(9), strkin(9), strcon(9)
+    Real(c_double) :: consv
     Integer(c_int32_t) :: list_rebuilt, shake_iters, rattle_iters, mts_full
   End Type gb_step_stats
 
@@ -33,7 +34,8 @@ Module gb300_interface
 
   Public :: gb_init, gb_upload_parts, gb_download_parts, gb_relocate, gb_list_build, gb_vnl_check, &
             gb_refresh, gb_forces, gb_spme, gb_vv, gb_md_run, gb_mts_config, gb_mts_stats, &
-            gb_set_precision, gb_finalize
+            gb_set_precision, gb_set_ensemble, gb_set_step, gb_thermostat_state, &
+            gb_set_thermostat_state, gb_finalize
 
   Interface
     Integer(c_int) Function gb_init(prm, natms, ltype, chge, weight, lfrzn, vdw_prm, ntcons, listcon, &
@@ -117,6 +119,29 @@ Module gb300_interface
       Import :: c_int
       Integer(c_int), Value :: precision
     End Function gb_set_precision
+
+    Integer(c_int) Function gb_set_ensemble(kind, temp, tau_t, chi, seed, degfre) &
+        Bind(C, name="gb_set_ensemble")
+      Import :: c_int, c_int32_t, c_double
+      Integer(c_int), Value :: kind
+      Real(c_double), Value :: temp, tau_t, chi, degfre
+      Integer(c_int32_t), Intent(In) :: seed(3)
+    End Function gb_set_ensemble
+
+    Integer(c_int) Function gb_set_step(nstep) Bind(C, name="gb_set_step")
+      Import :: c_int, c_int32_t
+      Integer(c_int32_t), Value :: nstep
+    End Function gb_set_step
+
+    Integer(c_int) Function gb_thermostat_state(chi_t, cint, consv) Bind(C, name="gb_thermostat_state")
+      Import :: c_int, c_double
+      Real(c_double), Intent(Out) :: chi_t, cint, consv
+    End Function gb_thermostat_state
+
+    Integer(c_int) Function gb_set_thermostat_state(chi_t, cint) Bind(C, name="gb_set_thermostat_state")
+      Import :: c_int, c_double
+      Real(c_double), Value :: chi_t, cint
+    End Function gb_set_thermostat_state
 
     Subroutine gb_finalize() Bind(C, name="gb_finalize")
     End Subroutine gb_finalize

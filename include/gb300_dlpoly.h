@@ -43,10 +43,17 @@ extern "C" {
 #define GB_ERR_NO_DEVICE (-4)
 #define GB_ERR_NONFINITE (-5)
 #define GB_ERR_TOO_LARGE (-6)  /* size beyond a fixed scratch limit (gb_kinstress_noalloc) */
+#define GB_ERR_RNG (-7)        /* a Gaussian deviate's rejection loop hit its iteration cap */
 
 /* Precision forms of the force path. */
 #define GB_FP64 0   /* plain: FP64 throughout */
 #define GB_MIXED 1  /* FP32 pair/spline/FFT arithmetic, int64 fixed-point forces (2^40) */
+
+/* Ensembles of the VV stages (thermo%ensemble, drivers.F90:1132-1175) */
+#define GB_NVE 0              /* nve_0_vv */
+#define GB_NVT_BERENDSEN 1    /* nvt_b0_vv */
+#define GB_NVT_NOSE_HOOVER 2  /* nvt_h0_vv */
+#define GB_NVT_LANGEVIN 3     /* nvt_l0_vv */
 
 /*
  * Run parameters.  Mirrors the CONTROL/FIELD-derived scalars the reference
@@ -87,6 +94,7 @@ typedef struct gb_step_stats {
   double stress[9];             /* configurational stress (two-body + SPME) */
   double strkin[9];             /* kinetic stress */
   double strcon[9];             /* constraint stress of the SHAKE stage (stats%strcon) */
+  double consv;                 /* thermostat's conserved-energy term (stats%consv; Nose-Hoover) */
   int32_t list_rebuilt;         /* 1 if the Verlet list was rebuilt this step */
   int32_t shake_iters, rattle_iters;
   int32_t mts_full;             /* 1 if full SPME ran this step (learned-MTS form) */
@@ -169,13 +177,44 @@ int gb_real(double* eng_out, double* stress_out);
 
 /* nve_0_vv (nve.F90:38): stage 1 = half kick + drift + SHAKE (apply_shake,
  * constraints.F90:1071); stage 2 = half kick + RATTLE (apply_rattle,
- * constraints.F90:1032) + kinstress (kinetics.F90:218). */
+ * constraints.F90:1032) + kinstress (kinetics.F90:218).  With an NVT ensemble
+ * set (gb_set_ensemble) the stages are those of nvt_b0_vv, nvt_h0_vv or
+ * nvt_l0_vv instead. */
 int gb_vv(int stage, double* strkin, double* engke, int32_t* iters, double* vircon,
           double* strcon);
 
 /* Resident MD loop (md_vv, drivers.F90:2059-2288): nsteps of VV1+SHAKE,
- * refresh, forces, VV2+RATTLE with no host round trip; stats[nsteps] may be NULL. */
+ * refresh, forces, VV2+RATTLE with no host round trip; stats[nsteps] may be NULL.
+ * Each step first advances the step counter (gb_set_step). */
 int gb_md_run(int nsteps, gb_step_stats* stats);
+
+/* Ensemble of the VV stages: the dispatch on thermo%ensemble (drivers.F90:1132-1175)
+ * for the non-rigid-body ensembles
+ *   GB_NVE               nve_0_vv (nve.F90:38)
+ *   GB_NVT_BERENDSEN     nvt_b0_vv (nvt_berendsen.F90:39), tau_t [ps]
+ *   GB_NVT_NOSE_HOOVER   nvt_h0_vv (nvt_nose_hoover.F90), tau_t [ps]
+ *   GB_NVT_LANGEVIN      nvt_l0_vv (nvt_langevin.F90), chi = friction [1/ps]
+ * temp [K] is thermo%temp; seed[3] the 'random_seed' shifts of sarurnd
+ * (numerics.F90:458; NULL = no shift); degfre the degrees of freedom
+ * (config%degfre; <= 0 computes 3*(free atoms) - 3 - constraints,
+ * temperature.F90:109-143).  Resets chi_t and cint to zero. */
+int gb_set_ensemble(int kind, double temp, double tau_t, double chi, const int32_t* seed,
+                    double degfre);
+
+/* flow%step used by the next stage-1 call (the Langevin random forces are keyed
+ * on it, langevin.F90:57); gb_md_run increments it before each step. */
+int gb_set_step(int32_t nstep);
+
+/* Thermostat state thermo%chi_t, thermo%cint and stats%consv (Nose-Hoover:
+ * 0.5*qmass*chi_t^2 + ceng*cint, else 0); the setter restores chi_t and cint
+ * (REVIVE, system.F90:1831). */
+int gb_thermostat_state(double* chi_t, double* cint, double* consv);
+int gb_set_thermostat_state(double chi_t, double cint);
+
+/* Test hook: the generator of the Langevin forces on the device.  mode 0: out[i] =
+ * sarurnd(a[i], b[i], c[i]) (numerics.F90:458); mode 1: out[3i..3i+2] =
+ * box_mueller_saru3(a[i], b[i]) with its counter starting at c[i] (numerics.F90:745). */
+int gb_rng_eval(int mode, int n, const int64_t* a, const int64_t* b, const int64_t* c, double* out);
 
 /* Learned multiple-time-step form (no counterpart in the reference: its
  * electro%nstfce key is parsed but SPME runs every step, two_body.F90:298-302).

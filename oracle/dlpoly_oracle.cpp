@@ -93,6 +93,12 @@ struct Ctx {
   // neighbour list update flag
   bool update = true;
   int nthreads = 1;
+  // thermostat (thermo%ensemble and its state)
+  int ens = GB_NVE;
+  double temp = 0, tau_t = 0, chi = 0, sigma = 0, qmass = 0, ceng = 0, totmas = 0;
+  double chi_t = 0, cint = 0, consv = 0;
+  int seed[3] = {0, 0, 0};
+  int nstep = 0;
 };
 
 Ctx g;
@@ -1263,21 +1269,232 @@ void kinstress(double* s) {
   s[3] = s[1]; s[6] = s[2]; s[7] = s[5];
 }
 
-// nve_0_vv: source/nve.F90:38-235 (lvar = .false.)
+// ------------------------------------------------------------------ thermostats
+// sarurnd (numerics.F90:458-635): the SARU generator as the reference evaluates it,
+// in 64-bit integers (Ishft is a logical shift) with the products formed in double
+// precision and reduced with Mod(., 2^32).
+static inline int64_t lshl(int64_t x, int n) { return (int64_t)((uint64_t)x << n); }
+static inline int64_t lshr(int64_t x, int n) { return (int64_t)((uint64_t)x >> n); }
+static inline int64_t int32of(int64_t x) { return (int64_t)(int32_t)(uint32_t)(uint64_t)x; }
+static inline int64_t prodmod(double a, double b) { return (int64_t)std::fmod(a * b, 4294967296.0); }
+
+double sarurnd(int64_t seeda, int64_t seedb, int64_t seedc) {
+  const int64_t two32 = 4294967296LL;
+  int64_t seed1 = seeda % two32; if (seed1 < 0) seed1 += two32;
+  int64_t seed2 = seedb % two32; if (seed2 < 0) seed2 += two32;
+  int64_t seed3 = seedc % two32; if (seed3 < 0) seed3 += two32;
+  int64_t itmp;
+  seed3 = (seed3 ^ (lshl(seed1, 7) ^ lshr(seed2, 6))) % two32;
+  itmp = lshr(seed1, 4) ^ lshr(seed3, 15);
+  seed2 = (seed2 + itmp) % two32;
+  seed1 = (seed1 ^ (lshl(seed2, 9) + lshl(seed3, 8))) % two32;
+  itmp = lshr(seed2, 11) ^ lshl(seed1, 1);
+  itmp = prodmod(2771807053.0, (double)itmp);
+  seed3 = (seed3 ^ itmp) % two32;
+  itmp = lshl(seed1, 4) ^ lshr(seed3, 16);
+  itmp = prodmod(1925059961.0, (double)itmp);
+  seed2 = (seed2 + itmp) % two32;
+  itmp = lshr(seed3, 5) ^ lshr(int32of(seed2), 22);
+  itmp = prodmod(1060677357.0, (double)itmp);
+  if (itmp < 0) itmp += two32;
+  seed1 = (seed1 ^ itmp) % two32;
+  itmp = prodmod((double)seed1, (double)seed3);
+  seed2 = (seed2 + itmp) % two32;
+  seed1 = (seed1 + (seed3 ^ lshr(seed2, 2))) % two32;
+  seed2 = seed2 ^ lshr(int32of(seed2), 17);
+  if (seed2 < 0) seed2 += two32;
+  itmp = seed1 ^ lshr(int32of(seed1), 14);
+  int64_t state = prodmod(2044649123.0, (double)itmp);
+  if (state < 0) state += two32;
+  int64_t wstate = ((state + seed2) ^ lshr(int32of(state), 8)) % two32;
+  if (wstate < 0) wstate += two32;
+  itmp = wstate ^ 3722418165LL;
+  itmp = prodmod((double)wstate, (double)itmp);
+  state = (state + itmp) % two32;
+  wstate = (2882246391LL + lshr(wstate, 1)) % two32;
+  itmp = prodmod(1273716057.0, (double)state);
+  state = (itmp + 637592055LL) % two32;
+  wstate = (wstate + 2148127051LL + (lshr(int32of(wstate), 31) & 3666320093LL)) % two32;
+  int64_t v = ((state ^ lshr(state, 26)) + wstate) % two32;
+  itmp = v ^ lshr(v, 20);
+  int64_t u32 = prodmod((double)itmp, 1767372199.0);
+  const double rtwo32 = 1.0 / 4294967296.0;
+  double p1 = (double)int32of(u32) * rtwo32 + (0.5 + 0.5 * rtwo32);
+  double p2 = (double)state * (rtwo32 * rtwo32);
+  return p1 + p2;
+}
+
+// box_mueller_saru3 (numerics.F90:745-803), counter starting at k0; seed shifts added
+int box_mueller_saru3(int64_t i, int64_t j, int64_t k0, double* g1, double* g2, double* g3) {
+  const int64_t a = i + g.seed[0], b = j + g.seed[1];
+  int64_t k = k0 + g.seed[2];
+  double ran0 = 1.0, ran1 = 0.0, ran2 = 0.0;
+  int guard = 0;
+  while (ran0 <= DBL_MIN || ran0 >= 1.0) {
+    ran1 = 2.0 * sarurnd(a, b, k) - 1.0;
+    ran2 = 2.0 * sarurnd(a, b, k + 1) - 1.0;
+    ran0 = ran1 * ran1 + ran2 * ran2;
+    k += 2;
+    if (++guard > 64) return GB_ERR_RNG;
+  }
+  ran0 = std::sqrt(-2.0 * std::log(ran0) / ran0);
+  *g1 = ran0 * ran1;
+  *g2 = ran0 * ran2;
+  ran0 = 1.0;
+  guard = 0;
+  while (ran0 <= DBL_MIN || ran0 >= 1.0) {
+    ran1 = 2.0 * sarurnd(a, b, k) - 1.0;
+    ran2 = 2.0 * sarurnd(a, b, k + 1) - 1.0;
+    ran0 = ran1 * ran1 + ran2 * ran2;
+    k += 2;
+    if (++guard > 64) return GB_ERR_RNG;
+  }
+  ran0 = std::sqrt(-2.0 * std::log(ran0) / ran0);
+  *g3 = ran0 * ran1;
+  return GB_OK;
+}
+
+// langevin_forces, setforces branch (langevin.F90:57-194; global id = i + 1)
+int langevin_forces(int nstep, double tstep, std::vector<double>& fx, std::vector<double>& fy,
+                    std::vector<double>& fz) {
+  const double scale = std::sqrt(2.0 * g.chi * 0.831451115 * g.temp / tstep);
+  fx.assign(g.natms, 0.0); fy.assign(g.natms, 0.0); fz.assign(g.natms, 0.0);
+  for (int i = 0; i < g.natms; ++i) {
+    if (g.lfrzn[i] == 0 && g.weight[i] > 1.0e-6) {
+      int st = box_mueller_saru3(i + 1, nstep, 0, &fx[i], &fy[i], &fz[i]);
+      if (st) return st;
+      double tmp = scale * std::sqrt(g.weight[i]);
+      fx[i] = fx[i] * tmp; fy[i] = fy[i] * tmp; fz[i] = fz[i] * tmp;
+    }
+  }
+  return GB_OK;
+}
+
+// langevin_scalers (nvt_langevin.F90:1552-1621)
+void langevin_scalers(double chi, double tstep, double* t0, double* t1, double* scr, double* scv, double* scl) {
+  const double stol = 1.0e-3;
+  *t0 = std::exp(-chi * tstep);
+  if (chi <= DBL_MIN) { *t1 = tstep; *scr = 0.0; *scl = 0.0; *scv = 0.0; return; }
+  *t1 = (1.0 - *t0) / chi;
+  double alpha = 0.5 * chi * tstep;
+  if (alpha < stol) {
+    *scr = (alpha - alpha * alpha + 0.5 * (alpha * alpha * alpha) - (alpha * alpha * alpha * alpha) / 6.0 +
+            0.075 * (alpha * alpha * alpha * alpha * alpha)) / chi;
+    *scl = (alpha - 0.2 * (alpha * alpha * alpha) + (32.0 * (alpha * alpha * alpha * alpha * alpha)) / 525.0) /
+           (chi * std::sqrt(3.0));
+    *scv = 1.0 - alpha + 5.0 * (alpha * alpha) / 6.0 - 0.5 * (alpha * alpha * alpha);
+  } else {
+    *scr = (1.0 - *t0) * (1.0 - *t0) / (std::sqrt(alpha * (1.0 - *t0 * *t0)) * 2.0 * chi);
+    *scl = std::sqrt(1.0 - std::tanh(alpha) / alpha) / chi;
+    *scv = std::sqrt((1.0 - *t0 * *t0) / (4.0 * alpha));
+  }
+}
+
+// getkin (kinetics.F90): 0.5 sum over non-frozen atoms of m v^2
+double getkin() {
+  double e = 0.0;
+  for (int i = 0; i < g.natms; ++i)
+    if (g.lfrzn[i] == 0) e += g.weight[i] * (g.vx[i] * g.vx[i] + g.vy[i] * g.vy[i] + g.vz[i] * g.vz[i]);
+  return 0.5 * e;
+}
+
+// getvom (kinetics.F90:365-419) and its subtraction from the free atoms
+void remove_vom() {
+  double vom[3] = {0, 0, 0};
+  for (int i = 0; i < g.natms; ++i)
+    if (g.lfrzn[i] == 0) {
+      vom[0] += g.weight[i] * g.vx[i]; vom[1] += g.weight[i] * g.vy[i]; vom[2] += g.weight[i] * g.vz[i];
+    }
+  if (g.totmas >= DBL_MIN) for (int k = 0; k < 3; ++k) vom[k] = vom[k] / g.totmas;
+  for (int i = 0; i < g.natms; ++i)
+    if (g.lfrzn[i] == 0 && g.weight[i] > 1.0e-6) { g.vx[i] -= vom[0]; g.vy[i] -= vom[1]; g.vz[i] -= vom[2]; }
+}
+
+// nvt_b0_scl (nvt_berendsen.F90:907-962); stage 1 scales, stage 0 only measures
+void nvt_b0_scl(int stage, double tstep, double* strkin, double* engke) {
+  kinstress(strkin);
+  *engke = 0.5 * (strkin[0] + strkin[4] + strkin[8]);
+  g.chi_t = std::sqrt(1.0 + tstep / g.tau_t * (g.sigma / *engke - 1.0));
+  if (stage == 0) return;
+  for (int i = 0; i < g.natms; ++i) { g.vx[i] *= g.chi_t; g.vy[i] *= g.chi_t; g.vz[i] *= g.chi_t; }
+  double tmp = g.chi_t * g.chi_t;
+  for (int k = 0; k < 9; ++k) strkin[k] *= tmp;
+  *engke *= tmp;
+}
+
+// nvt_h0_scl (nvt_nose_hoover.F90) with pmass = chip = 0
+void nvt_h0_scl(double tstep, double* engke) {
+  double hstep = 0.5 * tstep, qstep = 0.5 * hstep;
+  g.cint = g.cint + qstep * g.chi_t;
+  *engke = getkin();
+  g.chi_t = g.chi_t + hstep * (2.0 * *engke + 0.0 - g.ceng) / g.qmass;
+  g.cint = g.cint + hstep * g.chi_t;
+  double scale = std::exp(-tstep * g.chi_t);
+  for (int i = 0; i < g.natms; ++i) { g.vx[i] *= scale; g.vy[i] *= scale; g.vz[i] *= scale; }
+  *engke = *engke * (scale * scale);
+  g.chi_t = g.chi_t + hstep * (2.0 * *engke + 0.0 - g.ceng) / g.qmass;
+  g.cint = g.cint + qstep * g.chi_t;
+}
+
+int set_ensemble(int kind, double temp, double tau_t, double chi, const int32_t* seed, double degfre) {
+  g.ens = kind; g.temp = temp; g.tau_t = tau_t; g.chi = chi;
+  for (int k = 0; k < 3; ++k) g.seed[k] = seed ? seed[k] : 0;
+  if (degfre <= 0.0) degfre = 3.0 * (double)(g.natms - g.megfrz) - 3.0 - (double)g.ntcons;
+  g.sigma = 0.5 * degfre * 0.831451115 * temp;   // temperature.F90:178
+  g.qmass = 2.0 * g.sigma * tau_t * tau_t;
+  g.ceng = 2.0 * g.sigma;
+  g.totmas = 0.0;
+  for (int i = 0; i < g.natms; ++i) if (g.lfrzn[i] == 0) g.totmas += g.weight[i];
+  g.chi_t = 0.0; g.cint = 0.0; g.consv = 0.0;
+  return GB_OK;
+}
+
+// nve_0_vv: source/nve.F90:38-235 (lvar = .false.); with an NVT ensemble the
+// stages of nvt_b0_vv (nvt_berendsen.F90:39-258), nvt_h0_vv (nvt_nose_hoover.F90)
+// or nvt_l0_vv (nvt_langevin.F90)
 int nve_vv(int stage, double* strkin, double* engke, int* iters, double* vircon, double* strcon) {
   const double tstep = g.p.tstep, hstep = 0.5 * tstep, rstep = 1.0 / tstep;
   if (g.ntcons > 0) constraints_tags();
   *iters = 0;
   if (stage == 1) {
-    for (int i = 0; i < g.natms; ++i) {
-      if (g.weight[i] > 1.0e-6) {
-        double tmp = hstep / g.weight[i];
-        g.vx[i] = g.vx[i] + tmp * g.fx[i];
-        g.vy[i] = g.vy[i] + tmp * g.fy[i];
-        g.vz[i] = g.vz[i] + tmp * g.fz[i];
-        g.x[i] = g.x[i] + tstep * g.vx[i];
-        g.y[i] = g.y[i] + tstep * g.vy[i];
-        g.z[i] = g.z[i] + tstep * g.vz[i];
+    if (g.ens == GB_NVT_LANGEVIN) {
+      std::vector<double> fxr, fyr, fzr, fxl, fyl, fzl;
+      int st = langevin_forces(g.nstep, tstep, fxr, fyr, fzr);
+      if (st) return st;
+      st = langevin_forces(-g.nstep, tstep, fxl, fyl, fzl);
+      if (st) return st;
+      double t0, t1, scr1, scv1, scl1;
+      langevin_scalers(g.chi, tstep, &t0, &t1, &scr1, &scv1, &scl1);
+      for (int i = 0; i < g.natms; ++i) {
+        if (g.weight[i] > 1.0e-6) {
+          double tmp = hstep / g.weight[i];
+          g.vx[i] = g.vx[i] + tmp * g.fx[i];
+          g.vy[i] = g.vy[i] + tmp * g.fy[i];
+          g.vz[i] = g.vz[i] + tmp * g.fz[i];
+          tmp = tstep / g.weight[i];
+          g.x[i] = g.x[i] + g.vx[i] * t1 + tmp * (fxr[i] * scr1 + fxl[i] * scl1);
+          g.y[i] = g.y[i] + g.vy[i] * t1 + tmp * (fyr[i] * scr1 + fyl[i] * scl1);
+          g.z[i] = g.z[i] + g.vz[i] * t1 + tmp * (fzr[i] * scr1 + fzl[i] * scl1);
+          g.vx[i] = g.vx[i] * t0 + tmp * fxr[i] * scv1;
+          g.vy[i] = g.vy[i] * t0 + tmp * fyr[i] * scv1;
+          g.vz[i] = g.vz[i] * t0 + tmp * fzr[i] * scv1;
+        }
+      }
+    } else {
+      if (g.ens == GB_NVT_NOSE_HOOVER) {
+        double ek;
+        nvt_h0_scl(hstep, &ek);
+      }
+      for (int i = 0; i < g.natms; ++i) {
+        if (g.weight[i] > 1.0e-6) {
+          double tmp = hstep / g.weight[i];
+          g.vx[i] = g.vx[i] + tmp * g.fx[i];
+          g.vy[i] = g.vy[i] + tmp * g.fy[i];
+          g.vz[i] = g.vz[i] + tmp * g.fz[i];
+          g.x[i] = g.x[i] + tstep * g.vx[i];
+          g.y[i] = g.y[i] + tstep * g.vy[i];
+          g.z[i] = g.z[i] + tstep * g.vz[i];
+        }
       }
     }
     if (g.ntcons > 0) {
@@ -1311,10 +1528,22 @@ int nve_vv(int stage, double* strkin, double* engke, int* iters, double* vircon,
       int st = constraints_rattle(tstep, iters);
       if (st) return st;
     }
-    double sk[9];
-    kinstress(sk);
+    double sk[9], ek;
+    if (g.ens == GB_NVT_BERENDSEN) {
+      nvt_b0_scl(1, tstep, sk, &ek);
+      remove_vom();
+      nvt_b0_scl(0, tstep, sk, &ek);
+    } else if (g.ens == GB_NVT_NOSE_HOOVER) {
+      nvt_h0_scl(hstep, &ek);
+      g.consv = 0.5 * g.qmass * g.chi_t * g.chi_t + g.ceng * g.cint;
+      kinstress(sk);
+    } else {
+      if (g.ens == GB_NVT_LANGEVIN) remove_vom();
+      kinstress(sk);
+      ek = 0.5 * (sk[0] + sk[4] + sk[8]);
+    }
     if (strkin) for (int k = 0; k < 9; ++k) strkin[k] = sk[k];
-    if (engke) *engke = 0.5 * (sk[0] + sk[4] + sk[8]);
+    if (engke) *engke = ek;
   }
   return GB_OK;
 }
@@ -1416,6 +1645,8 @@ int orc_init(const gb_params* prm, int natms, const int32_t* ltype, const double
   g.prmcon.assign(prmcon ? prmcon : nullptr, prmcon ? prmcon + nct : nullptr);
   g.spme_newjob = true;
   g.update = true;
+  g.nstep = 0;
+  set_ensemble(GB_NVE, 0.0, 0.0, 0.0, nullptr, 0.0);
   g.init = true;
   return GB_OK;
 }
@@ -1522,6 +1753,50 @@ int orc_real(double* eng_out, double* stress_out) {
   return GB_OK;
 }
 
+int orc_set_ensemble(int kind, double temp, double tau_t, double chi, const int32_t* seed, double degfre) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  if (kind < GB_NVE || kind > GB_NVT_LANGEVIN) return GB_ERR_ARG;
+  if (kind != GB_NVE && !(temp > 0.0)) return GB_ERR_ARG;
+  if ((kind == GB_NVT_BERENDSEN || kind == GB_NVT_NOSE_HOOVER) && !(tau_t > 0.0)) return GB_ERR_ARG;
+  if (kind == GB_NVT_LANGEVIN && !(chi >= 0.0)) return GB_ERR_ARG;
+  return set_ensemble(kind, temp, tau_t, chi, seed, degfre);
+}
+
+int orc_set_step(int32_t nstep) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  g.nstep = nstep;
+  return GB_OK;
+}
+
+int orc_thermostat_state(double* chi_t, double* cint, double* consv) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  if (chi_t) *chi_t = g.chi_t;
+  if (cint) *cint = g.cint;
+  if (consv) *consv = g.ens == GB_NVT_NOSE_HOOVER ? g.consv : 0.0;
+  return GB_OK;
+}
+
+int orc_set_thermostat_state(double chi_t, double cint) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  g.chi_t = chi_t;
+  g.cint = cint;
+  return GB_OK;
+}
+
+// sarurnd / box_mueller_saru3 on arrays (no seed shifts); needs no gb_init
+int orc_rng_eval(int mode, int n, const int64_t* a, const int64_t* b, const int64_t* c, double* out) {
+  if ((mode != 0 && mode != 1) || n < 0) return GB_ERR_ARG;
+  int keep[3] = {g.seed[0], g.seed[1], g.seed[2]};
+  g.seed[0] = g.seed[1] = g.seed[2] = 0;
+  int st = GB_OK;
+  for (int i = 0; i < n && st == GB_OK; ++i) {
+    if (mode == 0) out[i] = sarurnd(a[i], b[i], c[i]);
+    else st = box_mueller_saru3(a[i], b[i], c[i], &out[3 * i], &out[3 * i + 1], &out[3 * i + 2]);
+  }
+  for (int k = 0; k < 3; ++k) g.seed[k] = keep[k];
+  return st;
+}
+
 int orc_vv(int stage, double* strkin, double* engke, int32_t* iters, double* vircon, double* strcon) {
   if (!g.init) return GB_ERR_NOT_INIT;
   int it = 0;
@@ -1538,6 +1813,7 @@ int orc_md_run(int nsteps, gb_step_stats* stats) {
     gb_step_stats S;
     std::memset(&S, 0, sizeof(S));
     int it = 0;
+    ++g.nstep;
     int st = nve_vv(1, nullptr, nullptr, &it, &S.vircon, S.strcon);
     if (st) return st;
     S.shake_iters = it;
@@ -1558,6 +1834,7 @@ int orc_md_run(int nsteps, gb_step_stats* stats) {
     if (st) return st;
     S.rattle_iters = it;
     S.mts_full = 1;
+    S.consv = g.ens == GB_NVT_NOSE_HOOVER ? g.consv : 0.0;
     if (stats) stats[s] = S;
   }
   return GB_OK;

@@ -281,3 +281,45 @@ def test_runner_host_logic_on_oracle(tmp_path, oracle_lib):
     heads = [x for x in open(os.path.join(d, "STATIS")).read().split("\n") if len(x) == 34]
     assert [int(x[:10]) for x in heads] == [0, 5, 10, 15]
     assert io.read_config(os.path.join(d, "REVCON")).step == 15
+
+
+def test_ensemble_keys_of_control(tmp_path):
+    p = tmp_path / "CONTROL"
+    p.write_text("title t\nensemble nvt\nensemble_method Hoover\nensemble_thermostat_coupling 50 fs\n"
+                 "temperature 300 K\nrandom_seed [1 2 3]\n")
+    e = io.ensemble_from_control(io.read_control(p))
+    assert e == {"kind": "nose-hoover", "temp": 300.0, "tau_t": pytest.approx(0.05), "chi": 0.0, "seed": (1, 2, 3)}
+    p.write_text("title t\nensemble nvt\nensemble_method langevin\nensemble_thermostat_friction 2 ps^-1\n"
+                 "temperature 300 K\n")
+    assert io.ensemble_from_control(io.read_control(p))["chi"] == 2.0
+    for bad in ("ensemble npt\n", "ensemble nvt\nensemble_method andersen\n"):
+        p.write_text("title t\n" + bad)
+        with pytest.raises(NotImplementedError):
+            io.ensemble_from_control(io.read_control(p))
+
+
+def test_runner_nose_hoover_restart_on_oracle(tmp_path, oracle_lib):
+    """NVT Nose-Hoover from CONTROL: STATIS carries the conserved-energy term and a
+    continued run restores chi_t and cint from REVIVE."""
+    d = str(tmp_path)
+    runner.emit("nacl_4096", d, steps=6, stats_every=3)
+    ctl = os.path.join(d, "CONTROL")
+    txt = open(ctl).read().replace("ensemble nve", "ensemble nvt\nensemble_method hoover\n"
+                                   "ensemble_thermostat_coupling 0.05 ps")
+    open(ctl, "w").write(txt)
+    runner.run(d, lib=oracle_lib, quiet=True)
+    th = oracle_lib.thermostat_state()
+    assert th["consv"] != 0.0
+    s = io.system_from_files(io.read_config(os.path.join(d, "REVCON")), io.read_field(os.path.join(d, "FIELD")),
+                             io.read_control(ctl))
+    info = io.Statistics(s).read_revive(os.path.join(d, "REVIVE"))
+    assert (info["chi_t"], info["cint"]) == (th["chi_t"], th["cint"])
+    rec = [x for x in open(os.path.join(d, "STATIS")).read().split("\n") if x]
+    last = rec[rec.index([x for x in rec if len(x) == 34][-1]) + 6].split()
+    assert float(last[2]) == pytest.approx(th["consv"] / 100.0, rel=1e-6)    # stpval(0) follows stpval(1:27)
+    os.replace(os.path.join(d, "REVCON"), os.path.join(d, "CONFIG"))
+    txt = open(ctl).read().replace("restart noscale", "restart continue").replace("time_run 6 steps", "time_run 3 steps")
+    open(ctl, "w").write(txt)
+    out = runner.run(d, lib=oracle_lib, quiet=True)
+    assert out["final_step"] == 9
+    assert oracle_lib.thermostat_state()["cint"] != th["cint"]
