@@ -408,9 +408,7 @@ def run_gb(args, dist):
     for _ in range(ke):
         lib.upload(host["x"], host["y"], host["z"], host["vx"], host["vy"], host["vz"])
         lib.md_vv(1)
-        out = lib.download()
-        for k in host:
-            host[k][:] = out[k]
+        lib.download(out=host)
     e1 = time.perf_counter()
     emax = dist.max(e1 - e0)
     e2e = {"value": dist.world * s.natms * ke / emax, "unit": "atom-steps/s",

@@ -89,6 +89,7 @@ void free_all() {
     if (p) cudaFree(p);
   mts_free();
   spme_free();
+  metal_free();
   if (g.hsc) cudaFreeHost(g.hsc);
   if (g.stream) {
     for (int k = 0; k < 8; ++k) cudaEventDestroy(g.ev[k]);
@@ -199,14 +200,16 @@ int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real, bo
   integ_zero_forces();
   if (g.precision == GB_MIXED) list_pos_f32();
   const bool mts = md_step && do_spme && mts_active();
-  const bool full = mts ? mts_step_needs_spme() : do_spme;
+  const bool full = mts ? mts_step_needs_spme() : (do_spme && g.has_coul);
   if (full) spme_forces(&erc, &vrc, strec);
   else if (mts) mts_inner(&erc, &vrc, strec);
   for (int k = 0; k < 9; ++k) st[k] += strec[k];
-  if (do_real) pair_forces(e6, st);
+  if (do_real && (g.has_coul || g.has_vdw)) pair_forces(e6, st);
+  for (int k = 0; k < 4; ++k) g.metal_e4[k] = 0.0;
+  if (do_real && g.has_metal) metal_forces(g.metal_e4, st);  // metal_ld_compute + metal_forces
   if (g.precision == GB_MIXED) integ_forces_to_fp64();
   if (mts && full) mts_after_full(erc, vrc, strec);
-  if (full_out) *full_out = full;
+  if (full_out) *full_out = mts ? full : true;
   if (eng8) {
     eng8[0] = erc; eng8[1] = vrc;
     eng8[2] = e6[0]; eng8[3] = e6[1]; eng8[4] = e6[2]; eng8[5] = e6[3]; eng8[6] = e6[4]; eng8[7] = e6[5];
@@ -271,7 +274,7 @@ static const char* kProfNames[P_NPROF] = {"halo",        "bin_sort",   "list_pai
                                           "excl_forces", "spme_prep",  "spme_spread", "fft_x_fwd", "fft_y",
                                           "fft_z_conv",  "fft_x_inv",  "spme_gather", "vv",        "shake",
                                           "rattle",      "mlp_infer",  "mts_inputs", "mlp_train",  "coarse_prep",
-                                          "coarse_spread", "coarse_fft", "coarse_gather"};
+                                          "coarse_spread", "coarse_fft", "coarse_gather", "metal_density", "metal_forces"};
 
 static int prof_event() {
   if (g.ev_used >= (int)g.evpool.size()) {
@@ -443,8 +446,13 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     g.ntcons = ntcons;
     if (ntcons > 0) integ_setup_constraints(listcon, prmcon);
     mts_set_topology(ntcons, listcon, weight);
+    g.has_coul = sq2 > 0.0;   // SPME on (electro%key == ELECTROSTATIC_SPME) only with charges
     list_setup();
-    spme_setup();
+    g.has_coul = sq2 > 0.0;
+    g.has_vdw = false;
+    for (int k = 0; k < g.nkey; ++k) g.has_vdw = g.has_vdw || g.h_vdw_kind[k] != 0;
+    g.has_metal = false;
+    if (g.has_coul) spme_setup();  // an uncharged system has no electrostatics to set up
     g.nstep = 0;
     thermo_setup(GB_NVE, 0.0, 0.0, 0.0, nullptr, 0.0);
     g.init = true;
@@ -583,6 +591,7 @@ int gb_forces(double* eng_out, double* stress_out) {
 
 int gb_spme(double* eng_rc, double* vir_rc, double* stress_out) {
   return guarded([&]() {
+    if (!g.init) return (int)GB_ERR_NOT_INIT;
     double e8[8], s9[9];
     int st = compute_forces(e8, s9, true, false);
     if (eng_rc) *eng_rc = e8[0];
@@ -658,6 +667,34 @@ int gb_rng_eval(int mode, int n, const int64_t* a, const int64_t* b, const int64
   });
 }
 
+int gb_set_metal_eam(int ntab, const int32_t* kind, const int32_t* t1, const int32_t* t2, const int32_t* ngrid,
+                     const double* start, const double* finish, const double* values, const int32_t* listed) {
+  return guarded([&]() {
+    if (!g.init) return (int)GB_ERR_NOT_INIT;
+    if (ntab < 0 || (ntab > 0 && (!kind || !t1 || !t2 || !ngrid || !start || !finish || !values)))
+      return (int)GB_ERR_ARG;
+    if (g.precision == GB_MIXED) return (int)GB_ERR_ARG;
+    if (ntab == 0) { metal_free(); return (int)GB_OK; }
+    return metal_setup(ntab, kind, t1, t2, ngrid, start, finish, values, listed);
+  });
+}
+
+int gb_metal_energies(double* out4) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  if (!out4) return GB_ERR_ARG;
+  for (int k = 0; k < 4; ++k) out4[k] = g.metal_e4[k];
+  return GB_OK;
+}
+
+int gb_metal_rho(double* out) {
+  return guarded([&]() {
+    if (!g.init) return (int)GB_ERR_NOT_INIT;
+    if (!out || !g.has_metal) return (int)GB_ERR_ARG;
+    metal_rho(out, g.natms);
+    return (int)GB_OK;
+  });
+}
+
 int gb_md_run(int nsteps, gb_step_stats* stats) {
   return guarded([&]() {
     if (nsteps < 0) return (int)GB_ERR_ARG;
@@ -693,6 +730,8 @@ int gb_md_run(int nsteps, gb_step_stats* stats) {
       S.rattle_iters = it;
       S.mts_full = full ? 1 : 0;
       S.consv = g.ens == GB_NVT_NOSE_HOOVER ? g.hsc->th[7] : 0.0;
+      S.engmet = g.metal_e4[0] + g.metal_e4[2];
+      S.virmet = g.metal_e4[1] + g.metal_e4[3];
       GB_CUDA(cudaEventRecord(g.ev[4], g.stream));
       GB_CUDA(cudaEventSynchronize(g.ev[4]));
       float ms;
@@ -718,6 +757,7 @@ int gb_mts_config(int k, double tol, int train_steps) {
     if (!g.init) return (int)GB_ERR_NOT_INIT;
     if (k < 1 || !(tol > 0.0) || train_steps < 0) return (int)GB_ERR_ARG;
     if (k > 1 && g.precision != GB_MIXED) return (int)GB_ERR_ARG;  // the surrogate feeds the fixed-point forces
+    if (k > 1 && !g.has_coul) return (int)GB_ERR_ARG;  // it replaces SPME: needs charges
     g.mts_k = k;
     g.mts_tol = tol;
     g.mts_train = train_steps;
@@ -730,6 +770,7 @@ int gb_mts_config(int k, double tol, int train_steps) {
 int gb_set_precision(int precision) {
   return guarded([&]() {
     if (precision != GB_FP64 && precision != GB_MIXED) return (int)GB_ERR_ARG;
+    if (precision == GB_MIXED && g.has_metal) return (int)GB_ERR_ARG;  // metals run in the FP64 form
     if (precision != GB_MIXED && mts_active()) {  // the learned form runs on the mixed path only
       mts_free();
       g.mts_k = 1;
@@ -860,6 +901,8 @@ const char* gb_strerror(int status) {
     case GB_ERR_ARG: return "invalid argument";
     case GB_ERR_NO_DEVICE: return "no CUDA device";
     case GB_ERR_NONFINITE: return "non-finite positions";
+    case GB_ERR_METAL_TABLE: return "metal table read below its first point (error 506)";
+    case GB_ERR_METAL_DENSITY: return "local density outside its embedding table (error 507)";
     case GB_ERR_RNG: return "a Gaussian deviate's rejection loop hit its iteration cap";
     case GB_ERR_TOO_LARGE: return "size exceeds the fixed scratch limit of gb_kinstress_noalloc (1,048,576 atoms)";
     default: return "unknown status";

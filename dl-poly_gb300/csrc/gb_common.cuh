@@ -22,6 +22,8 @@ enum : int {
   ST_CELL_RANGE = 32,
   ST_SPME_RANGE = 64,
   ST_RNG = 128,          // a Box-Muller rejection loop hit its cap
+  ST_METAL_TABLE = 256,  // a metal table read below its first point (error 506)
+  ST_METAL_DENSITY = 512,  // a local density outside its embedding table (error 507)
 };
 
 // Device-resident scalars: one small block so a single copy returns them all.
@@ -39,7 +41,7 @@ struct DevScalars {
   double maxdisp;   // largest displacement since the last rebuild
   unsigned long long npairs_list;  // half-list entries walked by the pair kernel
   unsigned long long npairs_rc;    // unique pairs inside the cutoff
-  double acc[80];   // energy / virial / stress accumulators
+  double acc[96];   // energy / virial / stress accumulators
   double th[8];     // thermostat state: chi_t, cint, scale, vom(3), engke, consv
 };
 
@@ -52,14 +54,15 @@ enum {
   A_STRKIN = 40,      // 6 slots
   A_STRCON = 50,      // 6 slots
   A_KINMOM = 64,      // 9 slots: kinetic stress (6), momentum (3) of the thermostat stages
-  A_NSLOTS = 80
+  A_METAL = 80,       // 9 slots: engmet, virmet, stress (6), engden
+  A_NSLOTS = 96
 };
 
 // Kernel regions timed with CUDA events when profiling is on.
 enum ProfId {
   P_HALO = 0, P_BIN, P_LIST, P_FULLLIST, P_PAIR, P_EXCL, P_SPME_PREP, P_SPME_SPREAD, P_FFT_XF, P_FFT_Y,
   P_FFT_Z, P_FFT_XI, P_SPME_GATHER, P_VV, P_SHAKE, P_RATTLE, P_MLP, P_MTS_DESC, P_MLP_TRAIN, P_COARSE_PREP,
-  P_COARSE_SPREAD, P_COARSE_FFT, P_COARSE_GATHER, P_NPROF
+  P_COARSE_SPREAD, P_COARSE_FFT, P_COARSE_GATHER, P_METAL_DENSITY, P_METAL_FORCES, P_NPROF
 };
 void prof_begin(int id);
 void prof_end(int id);
@@ -109,6 +112,8 @@ struct Dev {
   int* list_excl = nullptr;    // (max_exclude+1)*natms
   bool lbook = false;
   int megfrz = 0;
+  bool has_coul = true, has_vdw = true, has_metal = false;  // which force terms the system has
+  double metal_e4[4] = {0, 0, 0, 0};  // engmet, virmet, engden, virden of the last evaluation
   // thermostat of the VV stages (gb_thermostat.cu)
   int ens = 0;                 // GB_NVE, GB_NVT_BERENDSEN, GB_NVT_NOSE_HOOVER, GB_NVT_LANGEVIN
   double temp = 0, tau_t = 0, chi_fric = 0;
@@ -314,6 +319,13 @@ bool thermo_vv2_finish(double* strkin, double* engke);   // stage 2 after RATTLE
 void thermo_state(double* chi_t, double* cint, double* consv);
 void thermo_set_state(double chi_t, double cint);
 void rng_eval(int mode, int n, const int64_t* a, const int64_t* b, const int64_t* c, double* out);
+// tabulated EAM metals (gb_metal.cu)
+int metal_setup(int ntab, const int32_t* kind, const int32_t* t1, const int32_t* t2, const int32_t* ngrid,
+                const double* start, const double* finish, const double* values, const int32_t* listed);
+void metal_free();
+bool metal_active();
+void metal_forces(double* e4, double* stress9);   // engmet, virmet, engden, virden
+void metal_rho(double* out, int n);
 // learned multiple-time-step form (gb_mlp.cu)
 void mts_set_topology(int ntcons, const int32_t* listcon, const double* weight);
 void mts_setup();

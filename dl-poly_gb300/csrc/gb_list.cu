@@ -535,8 +535,9 @@ void list_setup() {
   invert_host(g.cell, h_halo.rc, &det);
   for (int d = 0; d < 3; ++d) {
     double cw = 1.0 / (double)(nl[d] * 1);
-    double ecw = (double)g.p.spline_pad / (double)g.p.kmax[d];
-    ecw = std::max(cw, ecw);
+    // SPME needs a wider negative-direction halo for its splines (halo.F90:218-231);
+    // without electrostatics the link-cell width alone
+    double ecw = g.has_coul ? std::max(cw, (double)g.p.spline_pad / (double)g.p.kmax[d]) : cw;
     h_halo.ecw[d] = std::nextafter((-0.5 + ecw) + 0.0 * 1.0, 2.0) + DBL_MIN;
     h_halo.cw[d] = std::nextafter((-0.5 - cw) + 1.0 * 1.0, -2.0) - DBL_MIN - (nl[d] == 1 ? cw * 1.0e-10 : 0.0);
   }

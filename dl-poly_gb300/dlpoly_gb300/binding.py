@@ -98,16 +98,62 @@ class PathLib:
                    _ptr(s.weight, _d), _ptr(s.lfrzn, _i), _ptr(s.vdw_prm, _d), s.ntcons,
                    _ptr(lc, _i), _ptr(pc, _d), _ptr(excl, _i))
         self.upload(s.x, s.y, s.z, s.vx, s.vy, s.vz)
+        if getattr(s, "eam", None):
+            self.set_metal_eam(s.eam, s.metal_listed)
+
+    # ------------------------------------------------ metals (tabulated EAM)
+    _EAM_KIND = {"pair": 1, "dens": 2, "embe": 3}
+
+    def set_metal_eam(self, tables, listed=None):
+        """tables: dicts with kind ('pair', 'dens', 'embe'), types (t1, t2), start, finish,
+        values (internal energy units), in TABEAM order."""
+        k = np.array([self._EAM_KIND[t["kind"]] for t in tables], np.int32)
+        t1 = np.array([t["types"][0] for t in tables], np.int32)
+        t2 = np.array([t["types"][1] for t in tables], np.int32)
+        ng = np.array([len(t["values"]) for t in tables], np.int32)
+        st = np.array([t["start"] for t in tables], np.float64)
+        fi = np.array([t["finish"] for t in tables], np.float64)
+        vals = np.ascontiguousarray(np.concatenate([np.asarray(t["values"], np.float64) for t in tables]))
+        lst = None if listed is None else np.ascontiguousarray(listed, np.int32)
+        self._keep_eam = [k, t1, t2, ng, st, fi, vals, lst]
+        code = self._opt("set_metal_eam", c_int, [c_int, _i, _i, _i, _i, _d, _d, _d, _i])(
+            len(tables), _ptr(k, _i), _ptr(t1, _i), _ptr(t2, _i), _ptr(ng, _i), _ptr(st, _d), _ptr(fi, _d),
+            _ptr(vals, _d), _ptr(lst, _i))
+        if code != 0:
+            raise PathError(code, self.prefix + "set_metal_eam", self.strerror(code))
+
+    def metal_energies(self) -> dict:
+        out = np.zeros(4)
+        code = self._opt("metal_energies", c_int, [_d])(_ptr(out, _d))
+        if code != 0:
+            raise PathError(code, self.prefix + "metal_energies", self.strerror(code))
+        return dict(zip(("engmet", "virmet", "engden", "virden"), out.tolist()))
+
+    def metal_rho(self):
+        out = np.zeros(self.sys.natms)
+        code = self._opt("metal_rho", c_int, [_d])(_ptr(out, _d))
+        if code != 0:
+            raise PathError(code, self.prefix + "metal_rho", self.strerror(code))
+        return out
 
     def upload(self, x, y, z, vx=None, vy=None, vz=None):
         a = [np.ascontiguousarray(v, np.float64) if v is not None else None for v in (x, y, z, vx, vy, vz)]
         self._call("upload_state", *[_ptr(v, _d) for v in a])
 
-    def download(self):
+    STATE_KEYS = ("x", "y", "z", "vx", "vy", "vz", "fx", "fy", "fz")
+
+    def download(self, out: dict | None = None):
+        """Positions, velocities and forces; into the caller's arrays when `out` holds
+        them (contiguous float64, e.g. pinned host buffers), else into new arrays."""
         n = self.sys.natms
-        out = [np.empty(n) for _ in range(9)]
-        self._call("download_state", *[_ptr(v, _d) for v in out])
-        return dict(zip(("x", "y", "z", "vx", "vy", "vz", "fx", "fy", "fz"), out))
+        if out is None:
+            out = {k: np.empty(n) for k in self.STATE_KEYS}
+        arrs = [out[k] for k in self.STATE_KEYS]
+        for a in arrs:
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != n:
+                raise ValueError("download buffers must be contiguous float64 arrays of natms values")
+        self._call("download_state", *[_ptr(v, _d) for v in arrs])
+        return out
 
     # ----------------------------------------------------------- path calls
     def relocate(self):

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(os.path.dirname(HERE), "csrc")
 OBJ = os.path.join(os.path.dirname(HERE), "_build")
 LIB = os.path.join(HERE, "libdlpoly_gb300.so")
-SOURCES = ["gb_api.cu", "gb_list.cu", "gb_pair.cu", "gb_spme.cu", "gb_integrate.cu", "gb_thermostat.cu", "gb_mlp.cu",
+SOURCES = ["gb_api.cu", "gb_list.cu", "gb_pair.cu", "gb_spme.cu", "gb_integrate.cu", "gb_thermostat.cu", "gb_metal.cu", "gb_mlp.cu",
            "gb_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")

@@ -12,6 +12,8 @@ nacl_melt(n_side)      rock-salt lattice of n_side^3 sites, spacing 2.82 A, +/-1
 spce_water(n_side)     rigid 3-site water on an n_side^3 cubic lattice at 1.0 g/cm^3,
                        random orientations, 300 K; O-O LJ only; SHAKE/RATTLE bonds;
                        rc 10 A.  n_side=32 -> 32,768 molecules (98,304 atoms, 100^3 grid).
+eam_alloy(n_side)      random fcc Cu-Ni alloy with Sutton-Chen EAM tables (TABEAM form),
+                       no charges; rc 7 A.  n_side=12 -> 6,912 atoms; n_side=40 -> 256,000.
 """
 from __future__ import annotations
 
@@ -65,6 +67,7 @@ class GbStepStats(ctypes.Structure):
         ("stress", ctypes.c_double * 9), ("strkin", ctypes.c_double * 9),
         ("strcon", ctypes.c_double * 9),
         ("consv", ctypes.c_double),
+        ("engmet", ctypes.c_double), ("virmet", ctypes.c_double),
         ("list_rebuilt", ctypes.c_int32), ("shake_iters", ctypes.c_int32),
         ("rattle_iters", ctypes.c_int32), ("mts_full", ctypes.c_int32),
     ]
@@ -109,6 +112,10 @@ class System:
     type_names: tuple = ()      # site name per 1-based type (FIELD 'atoms' records)
     epsq: float = 1.0           # relative dielectric constant
     shake_maxit: int = 250
+    # tabulated EAM metal tables (TABEAM order): list of dicts with kind ('pair', 'dens',
+    # 'embe'), types (t1, t2), start, finish and values (energies in internal units)
+    eam: list | None = None
+    metal_listed: np.ndarray | None = None   # per type-pair key: listed in FIELD 'metal'
 
     @property
     def natms(self) -> int:
@@ -325,3 +332,68 @@ def lj_pair(eps: float = 1.0, sigma: float = 2.0, r: float = 1.0, box: float = 4
                   z=np.zeros(2), vx=np.zeros(2), vy=np.zeros(2), vz=np.zeros(2), rcut=10.0,
                   rpad=0.5, alpha=0.3, kmax=(16, 16, 16), ntypes=1, vdw_direct=1,
                   type_names=("Ar",))
+
+
+# Sutton-Chen parameters (Sutton and Chen, Phil. Mag. Lett. 61 (1990) 139): epsilon [eV],
+# a [A], n, m, c for the two species of the synthetic alloy
+SUTTON_CHEN = {"Cu": (1.2382e-2, 3.61, 9, 6, 39.432), "Ni": (1.5707e-2, 3.52, 9, 6, 39.432)}
+EV = 9648.530821   # eV in internal energy units (constants.F90:112)
+
+
+def _taper(r, r_on, rc):
+    """1 below r_on, (1 - x^2)^2 with x = (r - r_on)/(rc - r_on) up to rc, 0 beyond:
+    value and slope continuous at both ends."""
+    x = np.clip((r - r_on) / (rc - r_on), 0.0, 1.0)
+    return (1.0 - x * x) ** 2
+
+
+def eam_tables(species=("Cu", "Ni"), rc: float = 7.0, r_on: float = 6.0, r_min: float = 1.5,
+               ngrid: int = 5000, rho_max: float = 400.0):
+    """Sutton-Chen EAM sampled as TABEAM tables: pair V_ab = eps_ab (a_ab/r)^n, density
+    rho_b(r) = (a_b/r)^m (contributed by a neighbour of species b), embedding
+    F_a(rho) = -c_a eps_a sqrt(rho); eps_ab = sqrt(eps_a eps_b), a_ab = (a_a + a_b)/2.
+    Pair and density taper smoothly to zero between r_on and rc."""
+    r = np.linspace(r_min, rc, ngrid)
+    rho = np.linspace(0.0, rho_max, ngrid)
+    tabs = []
+    nt = len(species)
+    for ia in range(nt):
+        for ib in range(ia + 1):
+            ea, aa, n, m, _ = SUTTON_CHEN[species[ia]]
+            eb, ab, _, _, _ = SUTTON_CHEN[species[ib]]
+            e, a = math.sqrt(ea * eb), 0.5 * (aa + ab)
+            v = e * (a / r) ** n * _taper(r, r_on, rc) * EV
+            tabs.append({"kind": "pair", "types": (ia + 1, ib + 1), "start": r_min, "finish": rc, "values": v})
+    for ia in range(nt):
+        _, a, _, m, _ = SUTTON_CHEN[species[ia]]
+        tabs.append({"kind": "dens", "types": (ia + 1, ia + 1), "start": r_min, "finish": rc,
+                     "values": (a / r) ** m * _taper(r, r_on, rc)})
+    for ia in range(nt):
+        e, _, _, _, c = SUTTON_CHEN[species[ia]]
+        tabs.append({"kind": "embe", "types": (ia + 1, ia + 1), "start": 0.0, "finish": rho_max,
+                     "values": -c * e * np.sqrt(rho) * EV})
+    return tabs
+
+
+def eam_alloy(n_side: int = 12, seed: int = 2468, lattice: float = 3.565, frac_ni: float = 0.5,
+              temp: float = 600.0, jitter: float = 0.05, rc: float = 7.0) -> System:
+    """Random fcc Cu-Ni alloy on n_side^3 cubic cells (4 sites each) with Sutton-Chen
+    EAM tables; no charges and no vdW.  n_side = 12 -> 6,912 atoms; 40 -> 256,000."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.arange(n_side)
+    cells = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    pos = ((cells[:, None, :] + basis[None, :, :]).reshape(-1, 3) + 0.25) * lattice
+    L = n_side * lattice
+    pos = pos - 0.5 * L + rng.uniform(-jitter, jitter, pos.shape)
+    n = pos.shape[0]
+    ltype = np.where(rng.random(n) < frac_ni, 2, 1).astype(np.int32)
+    weight = np.where(ltype == 1, 63.546, 58.6934)
+    v = _maxwell(rng, weight, temp)
+    cell = np.array([L, 0, 0, 0, L, 0, 0, 0, L], np.float64)
+    return System(name=f"eam_cuni_{n}", cell=cell, ltype=ltype, chge=np.zeros(n), weight=weight,
+                  lfrzn=np.zeros(n, np.int32), vdw_prm=np.zeros(9), x=pos[:, 0].copy(),
+                  y=pos[:, 1].copy(), z=pos[:, 2].copy(), vx=v[:, 0].copy(), vy=v[:, 1].copy(),
+                  vz=v[:, 2].copy(), rcut=rc, rpad=0.5, alpha=0.3, kmax=(16, 16, 16), ntypes=2,
+                  type_names=("Cu", "Ni"), eam=eam_tables(("Cu", "Ni"), rc=rc, r_on=rc - 1.0),
+                  metal_listed=np.ones(3, np.int32))

@@ -27,6 +27,7 @@ Module gb300_interface
     Real(c_double) :: engke, vircon
     Real(c_double) :: stress(9), strkin(9), strcon(9)
     Real(c_double) :: consv
+    Real(c_double) :: engmet, virmet
     Integer(c_int32_t) :: list_rebuilt, shake_iters, rattle_iters, mts_full
   End Type gb_step_stats
 

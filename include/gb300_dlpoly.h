@@ -36,6 +36,8 @@ extern "C" {
 #define GB_ERR_UNSAFE 505         /* unsafe pair/grid state (two_body.F90:751) */
 #define GB_ERR_RATTLE 515         /* RATTLE did not converge (constraints.F90:748) */
 #define GB_ERR_HALO 56            /* halo larger than mxatms (deport_data.F90:1870) */
+#define GB_ERR_METAL_TABLE 506    /* metal table read below its first point (metal.F90:946) */
+#define GB_ERR_METAL_DENSITY 507  /* local density outside its embedding table (metal.F90:1245) */
 /* library errors */
 #define GB_ERR_NOT_INIT (-1)
 #define GB_ERR_CUDA (-2)
@@ -95,6 +97,7 @@ typedef struct gb_step_stats {
   double strkin[9];             /* kinetic stress */
   double strcon[9];             /* constraint stress of the SHAKE stage (stats%strcon) */
   double consv;                 /* thermostat's conserved-energy term (stats%consv; Nose-Hoover) */
+  double engmet, virmet;        /* metal energy and virial: pair + embedding (engmet + engden) */
   int32_t list_rebuilt;         /* 1 if the Verlet list was rebuilt this step */
   int32_t shake_iters, rattle_iters;
   int32_t mts_full;             /* 1 if full SPME ran this step (learned-MTS form) */
@@ -215,6 +218,26 @@ int gb_set_thermostat_state(double chi_t, double cint);
  * sarurnd(a[i], b[i], c[i]) (numerics.F90:458); mode 1: out[3i..3i+2] =
  * box_mueller_saru3(a[i], b[i]) with its counter starting at c[i] (numerics.F90:745). */
 int gb_rng_eval(int mode, int n, const int64_t* a, const int64_t* b, const int64_t* c, double* out);
+
+/* Tabulated EAM metals ('metal ... eam' in FIELD with a TABEAM file: metal.F90 tab = 1).
+ * ntab tables in TABEAM order: kind[k] 1 = pair (types t1[k], t2[k]), 2 = density of
+ * type t1[k], 3 = embedding of type t1[k]; ngrid[k] points from start[k] to finish[k];
+ * values concatenated, energies already in internal units (metal_table_read,
+ * metal.F90:1489).  listed[nkey] (may be NULL = all) marks the type pairs the FIELD
+ * 'metal' directive lists; unlisted pairs exert no metal force (keypot -1).  Each force
+ * evaluation then runs metal_ld_compute (metal.F90:897) and metal_forces (:193) on the
+ * Verlet list; their energies go to gb_step_stats.engmet/virmet and gb_metal_energies.
+ * FP64 form only; ntab = 0 removes the metal terms. */
+int gb_set_metal_eam(int ntab, const int32_t* kind, const int32_t* t1, const int32_t* t2,
+                     const int32_t* ngrid, const double* start, const double* finish,
+                     const double* values, const int32_t* listed);
+
+/* engmet, virmet, engden, virden of the last force evaluation (two_body.F90:780-781). */
+int gb_metal_energies(double* out4);
+
+/* F'(rho_i) per local atom after the last force evaluation (met%rho after
+ * metal_ld_compute); test hook. */
+int gb_metal_rho(double* out);
 
 /* Learned multiple-time-step form (no counterpart in the reference: its
  * electro%nstfce key is parsed but SPME runs every step, two_body.F90:298-302).

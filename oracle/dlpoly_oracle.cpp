@@ -99,6 +99,13 @@ struct Ctx {
   double chi_t = 0, cint = 0, consv = 0;
   int seed[3] = {0, 0, 0};
   int nstep = 0;
+  // metals, tabulated EAM (met%tab = 1): tables by Fortran index, column 1 values, column 2 derivative
+  bool metal = false, metal_unsafe = false;
+  bool spme_on = true;   // electrostatics present (any charge): coul_method spme
+  std::vector<std::vector<double>> vmet1, vmet2, dmet1, dmet2, fmet1, fmet2;  // per key / per type
+  std::vector<int> met_listed;
+  std::vector<double> mrho;
+  double engmet = 0, virmet = 0, engden = 0, virden = 0;
 };
 
 Ctx g;
@@ -360,10 +367,12 @@ void set_halo_particles() {
   int nlz = fint(cp[8] / (cut * 1.0));
   double xdc = (double)(nlx * 1), ydc = (double)(nly * 1), zdc = (double)(nlz * 1);
   double cwx = 1.0 / xdc, cwy = 1.0 / ydc, cwz = 1.0 / zdc;
-  double ecwx = (double)g.p.spline_pad / (double)g.p.kmax[0];
-  double ecwy = (double)g.p.spline_pad / (double)g.p.kmax[1];
-  double ecwz = (double)g.p.spline_pad / (double)g.p.kmax[2];
-  ecwx = std::max(cwx, ecwx); ecwy = std::max(cwy, ecwy); ecwz = std::max(cwz, ecwz);
+  double ecwx = cwx, ecwy = cwy, ecwz = cwz;
+  if (g.spme_on) {  // halo.F90:218-231: only with SPME electrostatics
+    ecwx = std::max(cwx, (double)g.p.spline_pad / (double)g.p.kmax[0]);
+    ecwy = std::max(cwy, (double)g.p.spline_pad / (double)g.p.kmax[1]);
+    ecwz = std::max(cwz, (double)g.p.spline_pad / (double)g.p.kmax[2]);
+  }
   ecwx = std::nextafter((-0.5 + ecwx) + 0.0 * 1.0, 2.0) + kZeroPlus;
   ecwy = std::nextafter((-0.5 + ecwy) + 0.0 * 1.0, 2.0) + kZeroPlus;
   ecwz = std::nextafter((-0.5 + ecwz) + 0.0 * 1.0, 2.0) + kZeroPlus;
@@ -1561,14 +1570,274 @@ bool vnl_check() {
   return tol >= kHalfMinus * g.p.rpad;
 }
 
+// ------------------------------------------------------------------- metals (tabulated EAM)
+// metal_table_derivatives: source/metal.F90:2807-2897
+void metal_table_derivatives(const std::vector<double>& buffer, std::vector<double>& vvv) {
+  vvv[1] = buffer[1]; vvv[2] = buffer[2]; vvv[3] = buffer[3]; vvv[4] = buffer[4];
+  double delmet = buffer[4];
+  int v_end = (int)std::lround(buffer[1]);
+  int i_start = 5 + 2, i_end = v_end - 2;
+  for (int i = i_start; i <= i_end; ++i) {
+    double aa0 = buffer[i], f0, f1, f2, f3, f4;
+    if (std::fabs(aa0) <= kZeroPlus) {
+      f0 = 0.0; f1 = 0.0; f2 = 0.0; f3 = 0.0; f4 = 0.0;
+    } else {
+      f0 = buffer[i - 2] / aa0; f1 = buffer[i - 1] / aa0; f2 = 1.0;
+      f3 = buffer[i + 1] / aa0; f4 = buffer[i + 2] / aa0;
+    }
+    double d1y = (f1 - f0);
+    double d2y = (f2 - f1) - (f1 - f0);
+    double d3y = (f3 - f0) + 3.0 * (f1 - f2);
+    double d4y = (f4 - f3) + 3.0 * (f2 - f3) + 3.0 * (f2 - f1) + (f0 - f1);
+    aa0 = aa0 / delmet;
+    double aa4 = d4y / 24.0;
+    double aa3 = (d3y + 12.0 * aa4) / 6.0;
+    double aa2 = (d2y + 6.0 * aa3 - 14.0 * aa4) / 2.0;
+    double aa1 = d1y + 3.0 * aa2 - 7.0 * aa3 + 15.0 * aa4;
+    vvv[i] = aa1 * aa0;
+    if (i == i_start) {
+      vvv[i_start - 2] = (aa1 - 4.0 * aa2 + 12.0 * aa3 - 32.0 * aa4) * aa0;
+      vvv[i_start - 1] = (aa1 - 2.0 * aa2 + 3.0 * aa3 - 4.0 * aa4) * aa0;
+    } else if (i == i_end) {
+      vvv[i_end + 1] = (aa1 + 2.0 * aa2 + 3.0 * aa3 + 4.0 * aa4) * aa0;
+      vvv[i_end + 2] = (aa1 + 4.0 * aa2 + 12.0 * aa3 + 32.0 * aa4) * aa0;
+    }
+  }
+}
+
+// metal_table_read, tab = 1 (source/metal.F90:1489-1925), energies already in internal units
+int metal_tables(int ntab, const int32_t* kind, const int32_t* t1, const int32_t* t2, const int32_t* ngrid,
+                 const double* start, const double* finish, const double* values, const int32_t* listed) {
+  const int nt = g.p.ntypes, nkey = nt * (nt + 1) / 2;
+  int maxgrid = 8;
+  for (int k = 0; k < ntab; ++k) maxgrid = std::max(maxgrid, ngrid[k] + 4);
+  const size_t len = (size_t)maxgrid + 2;
+  g.vmet1.assign(nkey, std::vector<double>(len, 0.0)); g.vmet2 = g.vmet1;
+  g.dmet1.assign(nt, std::vector<double>(len, 0.0)); g.dmet2 = g.dmet1;
+  g.fmet1 = g.dmet1; g.fmet2 = g.dmet1;
+  size_t pos = 0;
+  for (int k = 0; k < ntab; ++k) {
+    int ng = ngrid[k];
+    if (ng < 5 || kind[k] < 1 || kind[k] > 3 || t1[k] < 1 || t1[k] > nt) return GB_ERR_ARG;
+    std::vector<double> buffer(len, 0.0);
+    buffer[1] = (double)(ng + 4);
+    buffer[4] = (finish[k] - start[k]) / (double)(ng - 1);
+    buffer[2] = start[k] - 5.0 * buffer[4];
+    buffer[3] = finish[k];
+    for (int i = 0; i < ng; ++i) buffer[5 + i] = values[pos + i];
+    pos += ng;
+    std::vector<double>*c1, *c2;
+    if (kind[k] == 1) {
+      if (t2[k] < 1 || t2[k] > nt) return GB_ERR_ARG;
+      int a = std::max(t1[k], t2[k]), b = std::min(t1[k], t2[k]);
+      int k0 = a * (a - 1) / 2 + b - 1;
+      c1 = &g.vmet1[k0]; c2 = &g.vmet2[k0];
+    } else if (kind[k] == 2) {
+      c1 = &g.dmet1[t1[k] - 1]; c2 = &g.dmet2[t1[k] - 1];
+    } else {
+      c1 = &g.fmet1[t1[k] - 1]; c2 = &g.fmet2[t1[k] - 1];
+    }
+    for (int i = 1; i <= 4; ++i) (*c1)[i] = buffer[i];
+    for (int i = 5; i < (int)len; ++i) (*c1)[i] = (i - 4 > ng) ? 0.0 : buffer[i];
+    metal_table_derivatives(buffer, *c2);
+    if (kind[k] == 2) for (int i = 1; i <= 4; ++i) (*c2)[i] = 0.0;
+    if (kind[k] != 3)
+      for (int i = 5; i <= ng + 4; ++i) (*c2)[i] = -((double)i * buffer[4] + buffer[2]) * (*c2)[i];
+  }
+  g.met_listed.assign(nkey, 1);
+  if (listed) for (int k = 0; k < nkey; ++k) g.met_listed[k] = listed[k];
+  g.metal = ntab > 0;
+  return GB_OK;
+}
+
+// three-point table interpolation of metal_ld_compute / metal_forces
+static bool met_index(const std::vector<double>& t, double r, int* l, double* ppp) {
+  double rdr = 1.0 / t[4];
+  double rr1 = r - t[2];
+  int k = std::min((int)std::lround(rr1 * rdr), (int)std::lround(t[1]) - 1);
+  bool ok = true;
+  if (k < 5) { ok = false; k = 6; }
+  *l = k;
+  *ppp = rr1 * rdr - (double)k;
+  return ok;
+}
+
+static double met_interp(const std::vector<double>& v, int l, double ppp, int density) {
+  double vk0 = v[l - 1], vk1 = v[l], vk2 = v[l + 1];
+  double t1 = vk1 + ppp * (vk1 - vk0);
+  double t2 = vk1 + ppp * (vk2 - vk1);
+  if (ppp < 0.0) {
+    double d = t1 + 0.5 * (t2 - t1) * (ppp + 1.0);
+    if (density && d < 0.0) d = t1;
+    return d;
+  } else if (l == 5) {
+    return t2;
+  }
+  double d = t2 + 0.5 * (t2 - t1) * (ppp - 1.0);
+  if (density && d < 0.0) d = t2;
+  return d;
+}
+
+// metal_ld_compute (metal.F90:897-1257) with metal_ld_collect_eam (:2207-2516) and
+// metal_ld_set_halo (:3146): rho becomes F'(rho) on local atoms and halo images
+int metal_ld_compute(double* stress) {
+  g.mrho.assign(g.nlast, 0.0);
+  bool safe = true;
+  g.engden = 0.0;
+  g.virden = 0.0;
+  std::vector<double> rrt(g.p.max_list + 1);
+  for (int i = 0; i < g.natms; ++i) {
+    int limit = L(0, i);
+    for (int k = 1; k <= limit; ++k) {
+      int j = L(k, i) - 1;
+      double xx = g.x[i] - g.x[j], yy = g.y[i] - g.y[j], zz = g.z[i] - g.z[j];
+      rrt[k] = std::sqrt(xx * xx + yy * yy + zz * zz);
+    }
+    int ai = g.ltype[i];
+    for (int m = 1; m <= limit; ++m) {
+      int j = L(m, i) - 1;
+      int aj = g.ltype[j];
+      int ki = ai, kj = aj;
+      double rrr = rrt[m];
+      const std::vector<double>& dj = g.dmet1[kj - 1];
+      if (std::fabs(dj[1]) > kZeroPlus && std::lround(dj[1]) > 5) {
+        if (rrr <= dj[3]) {
+          int l; double ppp;
+          if (!met_index(dj, rrr, &l, &ppp)) safe = false;
+          double density = met_interp(dj, l, ppp, 1);
+          g.mrho[i] += density;
+          if (ki == kj && j < g.natms) g.mrho[j] += density;
+        }
+      }
+      const std::vector<double>& di = g.dmet1[ki - 1];
+      if (std::fabs(di[1]) > kZeroPlus && std::lround(di[1]) > 5) {
+        if (ki != kj && j < g.natms) {
+          if (rrr <= di[3]) {
+            int l; double ppp;
+            if (!met_index(di, rrr, &l, &ppp)) safe = false;
+            g.mrho[j] += met_interp(di, l, ppp, 1);
+          }
+        }
+      }
+    }
+  }
+  if (!safe) return GB_ERR_METAL_TABLE;
+  for (int i = 0; i < g.natms; ++i) {
+    const std::vector<double>& f1 = g.fmet1[g.ltype[i] - 1];
+    const std::vector<double>& f2 = g.fmet2[g.ltype[i] - 1];
+    if (std::fabs(f1[1]) > kZeroPlus) {
+      double rhosqr = g.mrho[i];
+      if (rhosqr >= f1[2] + 5.0 * f1[4]) {
+        if (rhosqr <= f1[3]) {
+          int l; double ppp;
+          if (!met_index(f1, rhosqr, &l, &ppp)) safe = false;
+          g.engden += met_interp(f1, l, ppp, 0);
+          g.mrho[i] = met_interp(f2, l, ppp, 0);
+        } else {
+          int l = (int)std::lround(f1[1]);
+          g.engden += f1[l];
+          g.mrho[i] = 0.0;
+        }
+      } else {
+        safe = false;
+      }
+    }
+  }
+  if (!safe) return GB_ERR_METAL_DENSITY;
+  stress[0] -= g.virden / 3.0; stress[4] -= g.virden / 3.0; stress[8] -= g.virden / 3.0;
+  for (int k = g.natms; k < g.nlast; ++k) g.mrho[k] = g.mrho[g.src[k]];
+  return GB_OK;
+}
+
+// metal_forces, tabulated EAM branch (metal.F90:193-895), serial without HALF_HALO
+void metal_forces(double* stress) {
+  g.engmet = 0.0;
+  g.virmet = 0.0;
+  std::vector<double> xxt(g.p.max_list + 1), yyt(g.p.max_list + 1), zzt(g.p.max_list + 1), rrt(g.p.max_list + 1);
+  const int nt = g.p.ntypes;
+  (void)nt;
+  for (int i = 0; i < g.natms; ++i) {
+    int limit = L(0, i);
+    for (int k = 1; k <= limit; ++k) {
+      int j = L(k, i) - 1;
+      xxt[k] = g.x[i] - g.x[j]; yyt[k] = g.y[i] - g.y[j]; zzt[k] = g.z[i] - g.z[j];
+      rrt[k] = std::sqrt(xxt[k] * xxt[k] + yyt[k] * yyt[k] + zzt[k] * zzt[k]);
+    }
+    int idi = g.ltg[i], ai = g.ltype[i];
+    double fix = g.fx[i], fiy = g.fy[i], fiz = g.fz[i];
+    double s1 = 0, s2 = 0, s3 = 0, s5 = 0, s6 = 0, s9 = 0;
+    for (int m = 1; m <= limit; ++m) {
+      int j = L(m, i) - 1;
+      int aj = g.ltype[j];
+      int ki = ai, kj = aj;
+      int key = (ai > aj ? ai * (ai - 1) / 2 + aj : aj * (aj - 1) / 2 + ai) - 1;
+      double rrr = rrt[m];
+      if (!(g.met_listed[key] && rrr <= g.p.rcut)) continue;  // keypot >= 0 .and. rrr <= met%rcut
+      double rsq = rrr * rrr;
+      double eng = 0.0, gamma1 = 0.0, gamma2 = 0.0, gamma3 = 0.0;
+      const bool count = j < g.natms || idi < g.ltg[j];
+      const std::vector<double>& v1 = g.vmet1[key];
+      int l = 0; double ppp = 0.0;
+      if (std::fabs(v1[1]) > kZeroPlus) {
+        if (rrr <= v1[3]) {
+          if (!met_index(v1, rrr, &l, &ppp)) g.metal_unsafe = true;
+          gamma1 = met_interp(g.vmet2[key], l, ppp, 0);
+          if (count) eng = met_interp(v1, l, ppp, 0);
+        }
+      }
+      const std::vector<double>& dj = g.dmet1[kj - 1];
+      const std::vector<double>& di = g.dmet1[ki - 1];
+      if (std::fabs(dj[1]) > kZeroPlus && std::lround(di[1]) > 5) {
+        if (rrr <= dj[3]) {
+          int ld; double ppd;
+          if (!met_index(dj, rrr, &ld, &ppd)) g.metal_unsafe = true;
+          gamma2 = met_interp(g.dmet2[kj - 1], ld, ppd, 0);
+        }
+      }
+      if (ki == kj) {
+        gamma3 = gamma2;
+      } else if (std::fabs(di[1]) > kZeroPlus && std::lround(di[1]) > 5) {
+        if (rrr <= di[3]) {
+          int ld; double ppd;
+          if (!met_index(di, rrr, &ld, &ppd)) g.metal_unsafe = true;
+          gamma3 = met_interp(g.dmet2[ki - 1], ld, ppd, 0);
+        }
+      }
+      double gamma = (gamma1 + (gamma2 * g.mrho[i] + gamma3 * g.mrho[j])) / rsq;
+      double fx = gamma * xxt[m], fy = gamma * yyt[m], fz = gamma * zzt[m];
+      fix += fx; fiy += fy; fiz += fz;
+      if (j < g.natms) { g.fx[j] -= fx; g.fy[j] -= fy; g.fz[j] -= fz; }
+      if (count) {
+        g.engmet += eng;
+        g.virmet -= gamma * rsq;
+        s1 += xxt[m] * fx; s2 += xxt[m] * fy; s3 += xxt[m] * fz;
+        s5 += yyt[m] * fy; s6 += yyt[m] * fz; s9 += zzt[m] * fz;
+      }
+    }
+    g.fx[i] = fix; g.fy[i] = fiy; g.fz[i] = fiz;
+    stress[0] += s1; stress[1] += s2; stress[2] += s3; stress[3] += s2; stress[4] += s5;
+    stress[5] += s6; stress[6] += s3; stress[7] += s6; stress[8] += s9;
+  }
+}
+
 int calculate_forces(double* eng8, double* stress9) {
   for (int i = 0; i < g.nlast; ++i) { g.fx[i] = 0.0; g.fy[i] = 0.0; g.fz[i] = 0.0; }
   double st[9] = {0};
   double erc = 0, vrc = 0;
+  g.engmet = g.virmet = g.engden = g.virden = 0.0;
+  if (g.metal) {  // metal_ld_compute precedes the Ewald sums (two_body.F90:281-291)
+    int e = metal_ld_compute(st);
+    if (e) return e;
+  }
   spme(&erc, &vrc, st, g.fx.data(), g.fy.data(), g.fz.data());
   Acc A;
   two_body_real(A);
   for (int k = 0; k < 9; ++k) st[k] += A.str[k];
+  if (g.metal) {  // metal_forces inside the pair loop (two_body.F90:367-372)
+    g.metal_unsafe = false;
+    metal_forces(st);
+    if (g.metal_unsafe) return GB_ERR_METAL_TABLE;
+  }
   if (eng8) {
     eng8[0] = erc; eng8[1] = vrc; eng8[2] = A.engrl; eng8[3] = A.virrl;
     eng8[4] = A.engex; eng8[5] = A.virex; eng8[6] = A.engvdw; eng8[7] = A.virvdw;
@@ -1608,6 +1877,8 @@ int orc_init(const gb_params* prm, int natms, const int32_t* ltype, const double
     g.ltg[i] = i + 1; g.src[i] = i;
     if (lfrzn[i]) g.megfrz++;
   }
+  g.spme_on = false;
+  for (int i = 0; i < natms; ++i) g.spme_on = g.spme_on || chge[i] != 0.0;
   g.ld = prm->max_list + 4;
   g.list.assign((size_t)g.ld * natms, 0);
   int ldx = prm->max_exclude + 1;
@@ -1753,6 +2024,27 @@ int orc_real(double* eng_out, double* stress_out) {
   return GB_OK;
 }
 
+int orc_set_metal_eam(int ntab, const int32_t* kind, const int32_t* t1, const int32_t* t2, const int32_t* ngrid,
+                      const double* start, const double* finish, const double* values, const int32_t* listed) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  if (ntab < 0) return GB_ERR_ARG;
+  if (ntab == 0) { g.metal = false; return GB_OK; }
+  return metal_tables(ntab, kind, t1, t2, ngrid, start, finish, values, listed);
+}
+
+int orc_metal_energies(double* out4) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  out4[0] = g.engmet; out4[1] = g.virmet; out4[2] = g.engden; out4[3] = g.virden;
+  return GB_OK;
+}
+
+int orc_metal_rho(double* out) {
+  if (!g.init) return GB_ERR_NOT_INIT;
+  if (!g.metal || (int)g.mrho.size() < g.natms) return GB_ERR_ARG;
+  for (int i = 0; i < g.natms; ++i) out[i] = g.mrho[i];
+  return GB_OK;
+}
+
 int orc_set_ensemble(int kind, double temp, double tau_t, double chi, const int32_t* seed, double degfre) {
   if (!g.init) return GB_ERR_NOT_INIT;
   if (kind < GB_NVE || kind > GB_NVT_LANGEVIN) return GB_ERR_ARG;
@@ -1826,7 +2118,8 @@ int orc_md_run(int nsteps, gb_step_stats* stats) {
       if (st) return st;
     }
     double e8[8], st9[9];
-    calculate_forces(e8, st9);
+    st = calculate_forces(e8, st9);
+    if (st) return st;
     S.engcpe_rc = e8[0]; S.vircpe_rc = e8[1]; S.engcpe_rl = e8[2]; S.vircpe_rl = e8[3];
     S.engcpe_ex = e8[4]; S.vircpe_ex = e8[5]; S.engvdw = e8[6]; S.virvdw = e8[7];
     for (int k = 0; k < 9; ++k) S.stress[k] = st9[k];
@@ -1835,6 +2128,8 @@ int orc_md_run(int nsteps, gb_step_stats* stats) {
     S.rattle_iters = it;
     S.mts_full = 1;
     S.consv = g.ens == GB_NVT_NOSE_HOOVER ? g.consv : 0.0;
+    S.engmet = g.engmet + g.engden;
+    S.virmet = g.virmet + g.virden;
     if (stats) stats[s] = S;
   }
   return GB_OK;
