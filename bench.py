@@ -57,6 +57,12 @@ def workload(name):
     if name == "water_98304":
         return (systems.spce_water(32),
                 "SPC/E-style water 32,768 molecules (98,304 atoms), box 99.3 A, SPME 100^3 p=8, rc 10 A, SHAKE/RATTLE")
+    if name == "eam_256000":
+        return (systems.eam_alloy(40),
+                "fcc Cu-Ni alloy 256,000 atoms, box 142.6 A, tabulated Sutton-Chen EAM (5,000-point tables), "
+                "rc 7 A, skin 0.5 A, no electrostatics")
+    if name == "eam_6912":
+        return systems.eam_alloy(12), "fcc Cu-Ni alloy 6,912 atoms, tabulated Sutton-Chen EAM, rc 7 A"
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -161,6 +167,10 @@ def kernel_work(name, s, cnt, form):
         return 3.0 * N * (p * p + 3 * p), N * (32 + 3 * p * esz + 16)
     if name == "list_pairs":
         return 10.0 * P_list, 4.0 * P_list + N * 48
+    if name == "metal_density":   # distance + up to two density interpolations per entry; rho atomics
+        return 10.0 * P_list + 24.0 * P_rc, N * (24 + 4 + 8 + 8) + 4.0 * P_list
+    if name == "metal_forces":    # distance + three table interpolations + force, virial, stress
+        return 10.0 * P_list + 60.0 * P_rc, N * (24 + 4 + 8 + 24) + 4.0 * P_list + 8.0 * P_rc
     return None
 
 
@@ -381,6 +391,8 @@ def run_gb(args, dist):
     forms = {}
     if args.compare:
         for f in FORMS:
+            if s.eam and f != "fp64":
+                continue  # metals run in the FP64 form only
             if f != args.form:
                 forms[f], _ = measure(lib, L, s, f, args, dist, device, args.steps, detail=False)
     head, det = measure(lib, L, s, args.form, args, dist, device, args.steps, detail=True)
@@ -497,7 +509,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
     ap.add_argument("--form", default="fp64", choices=list(FORMS))
-    ap.add_argument("--workload", default="nacl_262144", choices=["nacl_262144", "nacl_175616", "nacl_4096", "water_98304"])
+    ap.add_argument("--workload", default="nacl_262144",
+                    choices=["nacl_262144", "nacl_175616", "nacl_4096", "water_98304", "eam_256000", "eam_6912"])
     ap.add_argument("--mts-train", type=int, default=200,
                     help="MD steps of online training (SPME every step) before the learned-MTS forms are timed")
     ap.add_argument("--no-compare", dest="compare", action="store_false",

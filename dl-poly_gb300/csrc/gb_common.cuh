@@ -235,6 +235,39 @@ __device__ __forceinline__ long long fix40(float x) {
   return (int)u < 0 ? -v : v;
 }
 
+// FP64 helpers for kernels bound by the FP64 pipe, where a compare or a conversion
+// costs a full FP64 issue slot: they work on IEEE bit patterns with integer ops.
+constexpr long long DBL_MIN_BITS = 0x0010000000000000ll;  // bits of DBL_MIN
+constexpr long long ONE_BITS = 0x3FF0000000000000ll;      // bits of 1.0
+
+// exact double of 0 <= k < 2^31 from its bits: (2^52 + k) - 2^52, one FP64 add
+__device__ __forceinline__ double int_to_dbl(int k) {
+  return __longlong_as_double(0x4330000000000000ll + (long long)k) - 4503599627370496.0;
+}
+
+// FP32 value of a positive normal double, mantissa truncated, by integer ops
+__device__ __forceinline__ float dbl_to_flt_trunc(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned e = ((hi >> 20) & 0x7FFu) - 1023u + 127u;
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | ((unsigned)b >> 29);
+  return __uint_as_float((e << 23) | m);
+}
+
+// exact FP64 value of a positive normal float, by integer ops
+__device__ __forceinline__ double flt_to_dbl(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long e = (unsigned long long)(((u >> 23) & 0xFFu) - 127u + 1023u);
+  return __longlong_as_double((long long)((e << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+
+// 1/sqrt(v) for a positive normal double: FP32 rsqrt seed of the truncated value and
+// one FP64 Newton step (relative error < 1e-13), three FP64 instructions
+__device__ __forceinline__ double rsqrt_seeded(double v) {
+  const double r = flt_to_dbl(rsqrtf(dbl_to_flt_trunc(v)));
+  return r * fma(-0.5 * v * r, r, 1.5);
+}
+
 // Block-wide reduction of NV doubles into per-block slots out[blockIdx.x*NV + k].
 template <int NV>
 __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* out) {

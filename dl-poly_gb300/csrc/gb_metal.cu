@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -28,6 +29,9 @@ namespace {
 
 inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
+__device__ __forceinline__ double interp3(const double* v, int l, double ppp);
+__device__ __forceinline__ double interp3_raw(const double* v, int l, double ppp) { return interp3(v, l, ppp); }
+
 struct MetTab {
   int n;          // Nint(buffer(1)) = ngrid + 4; 0 = no table
   int off;        // values at v[off + i], i = 1..n (Fortran index), derivatives at d[off + i]
@@ -35,7 +39,54 @@ struct MetTab {
   double rmax;    // finish
   double dr;
   double rdr;     // 1/dr as the reference forms it
+  int grid;       // tables with the same (r0, rdr, n) share a grid id: one index serves them all
+  int listed;     // pair tables: the FIELD 'metal' directive lists this type pair (keypot 0)
+  double nr0rdr;  // -r0 * rdr: x = r * rdr + nr0rdr
+  long long b_lo, b_hi;  // r <= rmax decided on rsq bits outside [rmax^2 (1 -+ 1e-12)]
 };
+
+// r <= rmax as the reference decides it (correctly rounded sqrt), from the bits of rsq
+// except inside a narrow band around rmax^2
+__device__ __forceinline__ bool within(long long rb, long long lo, long long hi, double rsq, double rmax) {
+  return rb < lo || (rb <= hi && sqrt(rsq) <= rmax);
+}
+
+// The three-point formula is the quadratic through (l-1, l, l+1) in both of its
+// ppp branches, so the force passes evaluate it from per-point coefficients
+// c0 + p (c1 + p c2), c0 = v_l, c1 = (v_{l+1} - v_{l-1})/2, c2 = (v_{l+1} - 2 v_l + v_{l-1})/2
+// (two FMAs).  Entry l = 5 holds the linear form the reference uses there for
+// ppp >= 0; the rare l = 5, ppp < 0 case and the density's negative fall-back read
+// the raw values.
+struct Coef {
+  double c0, c1, c2, pad;
+};
+
+__device__ __forceinline__ double qeval(const Coef* c, int l, double p) {
+  const double2 a = *reinterpret_cast<const double2*>(&c[l].c0);
+  const double b = c[l].c2;
+  return fma(p, fma(p, b, a.y), a.x);
+}
+
+// l = Nint((r - r0) / dr) clamped to [5, n-1] and ppp: the nearest integer comes from
+// adding 1.5*2^52 (no FP64 conversion); false if the reference's l < 5 guard fires
+__device__ __forceinline__ bool qindex(const MetTab& t, double r, int* l, double* ppp) {
+  const double x = fma(r, t.rdr, t.nr0rdr);
+  const double big = 6755399441055744.0;
+  const double tt = x + big;
+  int k = __double2loint(tt);
+  double kd = tt - big;
+  bool ok = true;
+  if (k > t.n - 1) { k = t.n - 1; kd = (double)k; }
+  if (k < 5) { ok = false; k = 6; kd = 6.0; }
+  *l = k;
+  *ppp = x - kd;
+  return ok;
+}
+
+__device__ __forceinline__ double qeval_full(const Coef* c, const double* raw, int l, double p) {
+  if (l == 5 && p < 0.0) return interp3_raw(raw, l, p);
+  return qeval(c, l, p);
+}
 
 // metal_ld_compute / metal_forces interpolation: index l and fraction ppp
 __device__ __forceinline__ bool tab_index(const MetTab& t, double r, int* l, double* ppp) {
@@ -73,37 +124,37 @@ __device__ __forceinline__ double interp3_density(const double* v, int l, double
 
 struct MetArgs {
   const MetTab* tab;    // [nkey pair | ntypes density | ntypes embedding]
-  const double* v;      // table values (column 1)
+  const double* v;      // table values (column 1), Fortran-indexed from off
   const double* d;      // column 2: -r dV/dr, -r drho/dr, dF/drho
+  const Coef* cv;       // quadratic coefficients of column 1 (same offsets)
+  const Coef* cd;       // and of column 2
   const int* listed;    // per pair key: 1 if the FIELD lists it (keypot = 0), else 0 (keypot = -1)
-  int nkey, ntypes;
+  int nkey, ntypes, ntab;
   double rcut;
+  long long b_rc_lo, b_rc_hi;   // rcut^2 band as bit patterns
 };
 
-// one pair's density contributions (metal_ld_collect_eam): to i from j's
-// species table kj, to j from i's species table ki
-__device__ __forceinline__ void pair_density(const MetArgs& A, int ai, int aj, double r, double* to_i,
-                                             double* to_j, bool* bad) {
-  const MetTab& tj = A.tab[A.nkey + aj - 1];
-  *to_i = 0.0;
-  *to_j = 0.0;
-  if (tj.n > 5 && r <= tj.rmax) {
-    int l;
-    double p;
-    if (!tab_index(tj, r, &l, &p)) *bad = true;
-    const double dens = interp3_density(A.v + tj.off, l, p);
-    *to_i = dens;
-    if (ai == aj) *to_j = dens;
-  }
-  if (ai != aj) {
-    const MetTab& ti = A.tab[A.nkey + ai - 1];
-    if (ti.n > 5 && r <= ti.rmax) {
-      int l;
-      double p;
-      if (!tab_index(ti, r, &l, &p)) *bad = true;
-      *to_j = interp3_density(A.v + ti.off, l, p);
-    }
-  }
+constexpr int MAX_TAB = 64;  // tables staged in shared memory (ntypes <= 8)
+
+__device__ __forceinline__ void stage_tables(const MetArgs& A, MetTab* st) {
+  for (int k = threadIdx.x; k < A.ntab; k += blockDim.x) st[k] = A.tab[k];
+  __syncthreads();
+}
+
+// density from one species table; a negative quadratic falls back to t1 / t2 (metal_ld_collect_eam)
+__device__ __forceinline__ double density_at(const MetArgs& A, const MetTab& t, int l, double p) {
+  double dens = qeval_full(A.cv + t.off, A.v + t.off, l, p);
+  const long long db = __double_as_longlong(dens);
+  if (db < 0 && db != (long long)0x8000000000000000ull) dens = interp3_density(A.v + t.off, l, p);  // < 0
+  return dens;
+}
+
+// r from rsq: seeded 1/sqrt (exact sqrt for a zero or subnormal rsq, which the table
+// guards then reject)
+__device__ __forceinline__ double dist_from(double rsq, long long rb, double* rinv) {
+  if (rb < DBL_MIN_BITS) { *rinv = 0.0; return sqrt(rsq); }
+  *rinv = rsqrt_seeded(rsq);
+  return rsq * (*rinv);
 }
 
 __global__ void __launch_bounds__(256) k_metal_density(int natms, const DevScalars* sc, const int* __restrict__ at_list,
@@ -112,6 +163,8 @@ __global__ void __launch_bounds__(256) k_metal_density(int natms, const DevScala
                                                        const int* __restrict__ ltype, const int* __restrict__ ltg,
                                                        const int* __restrict__ src, MetArgs A, double* rho,
                                                        int* status) {
+  __shared__ MetTab tabs[MAX_TAB];
+  stage_tables(A, tabs);
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nlast = sc->nlast;
@@ -121,6 +174,7 @@ __global__ void __launch_bounds__(256) k_metal_density(int natms, const DevScala
     if (i >= natms) continue;
     const double xi = x[i], yi = y[i], zi = z[i];
     const int ai = ltype[i], gi = ltg[i];
+    const MetTab& ti = tabs[A.nkey + ai - 1];
     const int* li = list + (size_t)i * ld + 3;
     const int n = li[0];
     double rho_i = 0.0;
@@ -132,11 +186,32 @@ __global__ void __launch_bounds__(256) k_metal_density(int natms, const DevScala
         jf = src[j];
       }
       const double dx = xi - x[j], dy = yi - y[j], dz = zi - z[j];
-      const double r = sqrt(dx * dx + dy * dy + dz * dz);
-      double ti, tj;
-      pair_density(A, ai, ltype[j], r, &ti, &tj, &bad);
-      rho_i += ti;
-      if (tj != 0.0) atomicAdd(&rho[jf], tj);
+      const double rsq = dx * dx + dy * dy + dz * dz;
+      const long long rb = __double_as_longlong(rsq);
+      const int aj = ltype[j];
+      const MetTab& tj = tabs[A.nkey + aj - 1];
+      const bool in_j = tj.n > 5 && within(rb, tj.b_lo, tj.b_hi, rsq, tj.rmax);
+      const bool in_i = ai != aj && ti.n > 5 && within(rb, ti.b_lo, ti.b_hi, rsq, ti.rmax);
+      if (!in_j && !in_i) continue;
+      double rinv;
+      const double r = dist_from(rsq, rb, &rinv);
+      // to i from j's species table, to j from i's (metal_ld_collect_eam)
+      int l = 0;
+      double p = 0.0;
+      int gl = -1;
+      double to_j = 0.0;
+      if (in_j) {
+        if (!qindex(tj, r, &l, &p)) bad = true;
+        gl = tj.grid;
+        const double dens = density_at(A, tj, l, p);
+        rho_i += dens;
+        if (ai == aj) to_j = dens;
+      }
+      if (in_i) {
+        if (ti.grid != gl && !qindex(ti, r, &l, &p)) bad = true;
+        to_j = density_at(A, ti, l, p);
+      }
+      if ((__double_as_longlong(to_j) & 0x7FFFFFFFFFFFFFFFll) != 0) atomicAdd(&rho[jf], to_j);
     }
     rho_i = warp_sum(rho_i);
     if (lane == 0 && rho_i != 0.0) atomicAdd(&rho[i], rho_i);
@@ -181,13 +256,15 @@ __global__ void k_metal_halo(int natms, const DevScalars* sc, const int* src, do
 
 constexpr int MACC = 8;  // engmet, virmet, stress (6)
 
-__global__ void __launch_bounds__(256) k_metal_forces(int natms, const DevScalars* sc, const int* __restrict__ at_list,
+__global__ void __launch_bounds__(256, 3) k_metal_forces(int natms, const DevScalars* sc, const int* __restrict__ at_list,
                                                       const int* __restrict__ list, int ld, const double* __restrict__ x,
                                                       const double* __restrict__ y, const double* __restrict__ z,
                                                       const int* __restrict__ ltype, const int* __restrict__ ltg,
                                                       const int* __restrict__ src, MetArgs A,
                                                       const double* __restrict__ rho, double* fx, double* fy, double* fz,
-                                                      double* blk, int* status) {
+                                                      double* blk, int* status, unsigned long long* cnt) {
+  __shared__ MetTab tabs[MAX_TAB];
+  stage_tables(A, tabs);
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nlast = sc->nlast;
@@ -200,9 +277,11 @@ __global__ void __launch_bounds__(256) k_metal_forces(int natms, const DevScalar
     if (i >= natms) continue;
     const double xi = x[i], yi = y[i], zi = z[i], rho_i = rho[i];
     const int ai = ltype[i], gi = ltg[i];
+    const MetTab& ti = tabs[A.nkey + ai - 1];
     const int* li = list + (size_t)i * ld + 3;
     const int n = li[0];
     double fix = 0.0, fiy = 0.0, fiz = 0.0;
+    int nrc = 0;
     for (int m = lane + 1; m <= n; m += 32) {
       const int j = li[m] - 1;
       int jf = j;
@@ -212,52 +291,59 @@ __global__ void __launch_bounds__(256) k_metal_forces(int natms, const DevScalar
       }
       const int aj = ltype[j];
       const int key = (ai > aj ? ai * (ai - 1) / 2 + aj : aj * (aj - 1) / 2 + ai) - 1;
-      if (!A.listed[key]) continue;  // keypot = -1
+      const MetTab& tp = tabs[key];
+      if (!tp.listed) continue;  // keypot = -1
       const double dx = xi - x[j], dy = yi - y[j], dz = zi - z[j];
-      const double rrr = sqrt(dx * dx + dy * dy + dz * dz);
-      if (!(rrr <= A.rcut)) continue;
-      const double rsq = rrr * rrr;
+      const double rsq = dx * dx + dy * dy + dz * dz;
+      const long long rb = __double_as_longlong(rsq);
+      if (!within(rb, A.b_rc_lo, A.b_rc_hi, rsq, A.rcut)) continue;   // rrr <= met%rcut
+      ++nrc;
+      double rinv;
+      const double rrr = dist_from(rsq, rb, &rinv);
+      const double inv_rsq = rinv * rinv;
       double eng = 0.0, gamma1 = 0.0, gamma2 = 0.0, gamma3 = 0.0;
-      const MetTab& tp = A.tab[key];
-      if (tp.n > 0 && rrr <= tp.rmax) {
-        int l;
-        double p;
-        if (!tab_index(tp, rrr, &l, &p)) bad = true;
-        gamma1 = interp3(A.d + tp.off, l, p);
-        eng = interp3(A.v + tp.off, l, p);
+      int l = 0, gl = -1;
+      double p = 0.0;
+      if (tp.n > 0 && within(rb, tp.b_lo, tp.b_hi, rsq, tp.rmax)) {
+        if (!qindex(tp, rrr, &l, &p)) bad = true;
+        gl = tp.grid;
+        gamma1 = qeval_full(A.cd + tp.off, A.d + tp.off, l, p);
+        eng = qeval_full(A.cv + tp.off, A.v + tp.off, l, p);
       }
-      const MetTab& tj = A.tab[A.nkey + aj - 1];
-      const MetTab& ti = A.tab[A.nkey + ai - 1];
-      if (tj.n > 0 && ti.n > 5 && rrr <= tj.rmax) {
-        int l;
-        double p;
-        if (!tab_index(tj, rrr, &l, &p)) bad = true;
-        gamma2 = interp3(A.d + tj.off, l, p);
+      const MetTab& tj = tabs[A.nkey + aj - 1];
+      if (tj.n > 0 && ti.n > 5 && within(rb, tj.b_lo, tj.b_hi, rsq, tj.rmax)) {
+        if (tj.grid != gl && !qindex(tj, rrr, &l, &p)) bad = true;
+        gl = tj.grid;
+        gamma2 = qeval_full(A.cd + tj.off, A.d + tj.off, l, p);
       }
       if (ai == aj) {
         gamma3 = gamma2;
-      } else if (ti.n > 5 && rrr <= ti.rmax) {
-        int l;
-        double p;
-        if (!tab_index(ti, rrr, &l, &p)) bad = true;
-        gamma3 = interp3(A.d + ti.off, l, p);
+      } else if (ti.n > 5 && within(rb, ti.b_lo, ti.b_hi, rsq, ti.rmax)) {
+        if (ti.grid != gl && !qindex(ti, rrr, &l, &p)) bad = true;
+        gamma3 = qeval_full(A.cd + ti.off, A.d + ti.off, l, p);
       }
-      const double gamma = (gamma1 + (gamma2 * rho_i + gamma3 * rho[j])) / rsq;
+      const double num = gamma1 + (gamma2 * rho_i + gamma3 * rho[j]);  // gamma * rsq
+      const double gamma = num * inv_rsq;
       const double fxx = gamma * dx, fyy = gamma * dy, fzz = gamma * dz;
       fix += fxx; fiy += fyy; fiz += fzz;
       atomicAdd(&fx[jf], -fxx);
       atomicAdd(&fy[jf], -fyy);
       atomicAdd(&fz[jf], -fzz);
       acc[0] += eng;
-      acc[1] -= gamma * rsq;
-      acc[2] += dx * fxx; acc[3] += dx * fyy; acc[4] += dx * fzz;
-      acc[5] += dy * fyy; acc[6] += dy * fzz; acc[7] += dz * fzz;
+      acc[1] -= num;
+      acc[2] = fma(dx, fxx, acc[2]); acc[3] = fma(dx, fyy, acc[3]); acc[4] = fma(dx, fzz, acc[4]);
+      acc[5] = fma(dy, fyy, acc[5]); acc[6] = fma(dy, fzz, acc[6]); acc[7] = fma(dz, fzz, acc[7]);
     }
     fix = warp_sum(fix); fiy = warp_sum(fiy); fiz = warp_sum(fiz);
+    if (cnt) nrc = warp_sumi(nrc);
     if (lane == 0) {
       atomicAdd(&fx[i], fix);
       atomicAdd(&fy[i], fiy);
       atomicAdd(&fz[i], fiz);
+      if (cnt) {  // list entries walked and pairs inside the cutoff, when no pair kernel counts them
+        atomicAdd(&cnt[0], (unsigned long long)n);
+        atomicAdd(&cnt[1], (unsigned long long)nrc);
+      }
     }
   }
   if (bad) atomicOr(status, ST_METAL_TABLE);
@@ -268,6 +354,8 @@ __global__ void __launch_bounds__(256) k_metal_forces(int natms, const DevScalar
 MetTab* d_tab = nullptr;
 double* d_val = nullptr;
 double* d_der = nullptr;
+Coef* d_cv = nullptr;
+Coef* d_cd = nullptr;
 int* d_listed = nullptr;
 double* d_rho = nullptr;
 int n_key = 0, n_tab = 0, occ_dens = 0, occ_force = 0;
@@ -312,10 +400,11 @@ void table_derivatives(const std::vector<double>& buf, std::vector<double>& der)
 }  // namespace
 
 void metal_free() {
-  void* p[] = {d_tab, d_val, d_der, d_listed, d_rho};
+  void* p[] = {d_tab, d_val, d_der, d_cv, d_cd, d_listed, d_rho};
   for (void* q : p)
     if (q) cudaFree(q);
-  d_tab = nullptr; d_val = nullptr; d_der = nullptr; d_listed = nullptr; d_rho = nullptr;
+  d_tab = nullptr; d_val = nullptr; d_der = nullptr; d_cv = nullptr; d_cd = nullptr; d_listed = nullptr;
+  d_rho = nullptr;
   n_key = n_tab = 0;
   g.has_metal = false;
 }
@@ -331,8 +420,12 @@ int metal_setup(int ntab, const int32_t* kind, const int32_t* t1, const int32_t*
   const int nt = g.p.ntypes;
   n_key = nt * (nt + 1) / 2;
   n_tab = n_key + 2 * nt;
+  if (n_tab > 64) return GB_ERR_ARG;  // MAX_TAB tables (8 species)
   std::vector<MetTab> tab(n_tab);
-  for (auto& t : tab) { t.n = 0; t.off = 0; t.r0 = t.rmax = t.dr = t.rdr = 0.0; }
+  for (auto& t : tab) {
+    t.n = 0; t.off = 0; t.r0 = t.rmax = t.dr = t.rdr = t.nr0rdr = 0.0; t.grid = -1; t.listed = 0;
+    t.b_lo = t.b_hi = 0;
+  }
   std::vector<double> val(1, 0.0), der(1, 0.0);
   size_t pos = 0;
   for (int k = 0; k < ntab; ++k) {
@@ -372,11 +465,49 @@ int metal_setup(int ntab, const int32_t* kind, const int32_t* t1, const int32_t*
       der.push_back(d[i]);
     }
   }
+  // quadratic coefficients per point (entry l = 5: the reference's linear form for ppp >= 0)
+  std::vector<Coef> cv(val.size()), cd(der.size());
+  for (auto& c : cv) c = Coef{0, 0, 0, 0};
+  for (auto& c : cd) c = Coef{0, 0, 0, 0};
+  for (int id = 0; id < n_tab; ++id) {
+    const MetTab& t = tab[id];
+    if (t.n == 0) continue;
+    for (int l = 5; l <= t.n - 1; ++l) {
+      for (int col = 0; col < 2; ++col) {
+        const std::vector<double>& w = col ? der : val;
+        const double v0 = w[t.off + l - 1], v1 = w[t.off + l], v2 = w[t.off + l + 1];
+        Coef& c = col ? cd[t.off + l] : cv[t.off + l];
+        if (l == 5) c = Coef{v1, v2 - v1, 0.0, 0.0};
+        else c = Coef{v1, 0.5 * (v2 - v0), 0.5 * ((v2 - v1) - (v1 - v0)), 0.0};
+      }
+    }
+  }
+  // grid ids: tables on the same grid share one index computation
+  int ngrid_ids = 0;
+  for (int id = 0; id < n_tab; ++id) {
+    if (tab[id].n == 0) continue;
+    for (int o = 0; o < id && tab[id].grid < 0; ++o)
+      if (tab[o].n == tab[id].n && tab[o].r0 == tab[id].r0 && tab[o].rdr == tab[id].rdr) tab[id].grid = tab[o].grid;
+    if (tab[id].grid < 0) tab[id].grid = ngrid_ids++;
+  }
   std::vector<int> lst(n_key, 0);
   for (int k = 0; k < n_key; ++k) lst[k] = listed ? listed[k] : 1;
+  auto bits = [](double v) { long long b; std::memcpy(&b, &v, 8); return b; };
+  for (int id = 0; id < n_tab; ++id) {
+    MetTab& t = tab[id];
+    if (id < n_key) t.listed = lst[id];
+    if (t.n == 0) continue;
+    t.nr0rdr = -t.r0 * t.rdr;
+    t.b_lo = bits(t.rmax * t.rmax * (1.0 - 1e-12));
+    t.b_hi = bits(t.rmax * t.rmax * (1.0 + 1e-12));
+  }
   GB_CUDA(cudaMalloc(&d_tab, sizeof(MetTab) * n_tab));
   GB_CUDA(cudaMalloc(&d_val, sizeof(double) * val.size()));
   GB_CUDA(cudaMalloc(&d_der, sizeof(double) * der.size()));
+  GB_CUDA(cudaMalloc(&d_cv, sizeof(Coef) * cv.size()));
+  GB_CUDA(cudaMalloc(&d_cd, sizeof(Coef) * cd.size()));
+  GB_CUDA(cudaMemcpy(d_cv, cv.data(), sizeof(Coef) * cv.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(d_cd, cd.data(), sizeof(Coef) * cd.size(), cudaMemcpyHostToDevice));
   GB_CUDA(cudaMalloc(&d_listed, sizeof(int) * n_key));
   GB_CUDA(cudaMalloc(&d_rho, sizeof(double) * std::max(g.mxatms, 1)));
   GB_CUDA(cudaMemcpy(d_tab, tab.data(), sizeof(MetTab) * n_tab, cudaMemcpyHostToDevice));
@@ -394,8 +525,13 @@ int metal_setup(int ntab, const int32_t* kind, const int32_t* t1, const int32_t*
 void metal_forces(double* e4, double* stress9) {
   cudaStream_t st = g.stream;
   MetArgs A;
-  A.tab = d_tab; A.v = d_val; A.d = d_der; A.listed = d_listed;
-  A.nkey = n_key; A.ntypes = g.p.ntypes; A.rcut = g.p.rcut;
+  A.tab = d_tab; A.v = d_val; A.d = d_der; A.cv = d_cv; A.cd = d_cd; A.listed = d_listed;
+  A.nkey = n_key; A.ntypes = g.p.ntypes; A.ntab = n_tab; A.rcut = g.p.rcut;
+  {
+    const double rc2 = g.p.rcut * g.p.rcut, lo = rc2 * (1.0 - 1e-12), hi = rc2 * (1.0 + 1e-12);
+    std::memcpy(&A.b_rc_lo, &lo, 8);
+    std::memcpy(&A.b_rc_hi, &hi, 8);
+  }
   const int T = 256;
   GB_CUDA(cudaMemsetAsync(d_rho, 0, sizeof(double) * g.mxatms, st));
   prof_begin(P_METAL_DENSITY);
@@ -414,8 +550,13 @@ void metal_forces(double* e4, double* stress9) {
   prof_begin(P_METAL_FORCES);
   nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, T), occ_force * g.nsm));
   double* blk2 = blk + std::max(nbe, 1);
+  unsigned long long* cnt = nullptr;
+  if (!g.has_coul && !g.has_vdw) {  // the pair kernel did not run: count here
+    GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
+    cnt = &g.sc->npairs_list;
+  }
   k_metal_forces<<<nb, T, 0, st>>>(g.natms, g.sc, g.at_list, g.list, g.ld, g.x, g.y, g.z, g.ltype, g.ltg, g.src, A,
-                                   d_rho, g.fx, g.fy, g.fz, blk2, &g.sc->status);
+                                   d_rho, g.fx, g.fy, g.fz, blk2, &g.sc->status, cnt);
   GB_LAUNCHED();
   gb_reduce_blocks(blk2, nb, MACC, &g.sc->acc[A_METAL]);
   prof_end(P_METAL_FORCES);

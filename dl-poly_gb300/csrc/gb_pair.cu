@@ -37,29 +37,7 @@ struct PairGeom {
   int nsamples, max_grid, ntypes;
 };
 
-constexpr long long DBL_MIN_BITS = 0x0010000000000000ll;  // bits of DBL_MIN
-constexpr long long ONE_BITS = 0x3FF0000000000000ll;      // bits of 1.0
 
-// exact double of 0 <= k < 2^31 from its bits: (2^52 + k) - 2^52, one FP64 add
-__device__ __forceinline__ double int_to_dbl(int k) {
-  return __longlong_as_double(0x4330000000000000ll + (long long)k) - 4503599627370496.0;
-}
-
-// FP32 value of a positive normal double, mantissa truncated, by integer ops
-__device__ __forceinline__ float dbl_to_flt_trunc(double v) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned hi = (unsigned)(b >> 32);
-  const unsigned e = ((hi >> 20) & 0x7FFu) - 1023u + 127u;
-  const unsigned m = ((hi & 0xFFFFFu) << 3) | ((unsigned)b >> 29);
-  return __uint_as_float((e << 23) | m);
-}
-
-// exact FP64 value of a positive normal float, by integer ops
-__device__ __forceinline__ double flt_to_dbl(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned long long e = (unsigned long long)(((u >> 23) & 0xFFu) - 127u + 1023u);
-  return __longlong_as_double((long long)((e << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29)));
-}
 
 __device__ __forceinline__ int vkey(int ai, int aj) {
   return ai > aj ? ai * (ai - 1) / 2 + aj : aj * (aj - 1) / 2 + ai;

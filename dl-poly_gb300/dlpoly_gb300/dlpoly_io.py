@@ -235,6 +235,7 @@ class Field:
     units: str                    # key of ENGUNIT
     molecules: list
     vdw: list                     # (name1, name2, 'lj', (epsilon [file units], sigma [A]))
+    metal: list = dc_field(default_factory=list)   # (name1, name2, 'eam'): tables in TABEAM
 
     def unique_names(self) -> list:
         """Atom types in order of first appearance (sites%unique_atom, ffield.F90:613-633)."""
@@ -247,7 +248,7 @@ class Field:
 
 
 _UNSUPPORTED_MOL = ("shell", "bond", "angl", "dihe", "inve", "rigi", "teth", "pmf")
-_UNSUPPORTED_TOP = ("tbp", "fbp", "metal", "tersoff", "extern", "multi", "neut")
+_UNSUPPORTED_TOP = ("tbp", "fbp", "tersoff", "extern", "multi", "neut")
 
 
 def write_field(path, fld: Field) -> None:
@@ -277,6 +278,10 @@ def write_field(path, fld: Field) -> None:
         out.append(f"vdw {len(fld.vdw)}")
         for a, b, kind, prm in fld.vdw:
             out.append(f"{a:<8s} {b:<8s} {kind:<4s} " + " ".join(f"{float(p)!r:>22s}" for p in prm))
+    if fld.metal:
+        out.append(f"metal {len(fld.metal)}")
+        for a, b, kind in fld.metal:
+            out.append(f"{a:<8s} {b:<8s} {kind}")
     out.append("close")
     with open(path, "w") as fh:
         fh.write("\n".join(out) + "\n")
@@ -300,7 +305,7 @@ def read_field(path) -> Field:
     title = rec[0].strip() if rec else ""
     pos[0] = 1
     units = None
-    mols, vdw = [], []
+    mols, vdw, metal = [], [], []
     while True:
         line, w = next_words()
         key = w[0].lower()
@@ -330,13 +335,20 @@ def read_field(path) -> Field:
                 if kind != "lj":
                     raise NotImplementedError(f"vdW form '{v[2]}': only 'lj' runs on this path")
                 vdw.append((v[0][:8], v[1][:8], "lj", (to_real(v[3]), to_real(v[4]))))
+        elif key.startswith("met"):
+            for _ in range(int(to_real(w[1]))):
+                _, v = next_words()
+                kind = v[2].lower()
+                if not kind.startswith("eam"):
+                    raise NotImplementedError(f"metal form '{v[2]}': only tabulated 'eam' runs on this path")
+                metal.append((v[0][:8], v[1][:8], "eam"))
         elif key.startswith("close"):
             break
         elif key.startswith(_UNSUPPORTED_TOP):
             raise NotImplementedError(f"FIELD directive '{w[0]}' is outside this path")
         else:
             raise ValueError(f"{path}: unknown FIELD directive '{w[0]}'")
-    return Field(title=title, units=units or "internal", molecules=mols, vdw=vdw)
+    return Field(title=title, units=units or "internal", molecules=mols, vdw=vdw, metal=metal)
 
 
 def _read_molecule(path, next_words) -> MoleculeType:
@@ -374,6 +386,67 @@ def _read_molecule(path, next_words) -> MoleculeType:
                 raise NotImplementedError(f"FIELD molecular directive '{w[0]}' is outside this path")
         else:
             raise ValueError(f"{path}: unknown molecular directive '{w[0]}'")
+
+
+# --------------------------------------------------------------------------------------
+# TABEAM (tabulated EAM: metal_table_read, metal.F90:1489-1925)
+# --------------------------------------------------------------------------------------
+_TABEAM_KINDS = {"pair": "pair", "dens": "dens", "dden": "dens", "embe": "embe", "demb": "embe"}
+
+
+def write_tabeam(path, tables, names, title="tabulated EAM", units="ev") -> None:
+    """TABEAM: a title record, the number of tables, then per table a header
+    'keyword atom1 [atom2] ngrid start finish' (atom2 for 'pair' only) and its values,
+    four per record; energies (pair, embedding) in the FIELD units."""
+    eng = ENGUNIT[units]
+    out = [title[:80], f"{len(tables)}"]
+    for t in tables:
+        a, b = (names[k - 1] for k in t["types"])
+        v = np.asarray(t["values"], np.float64)
+        if t["kind"] != "dens":
+            v = v / eng
+        head = f"{t['kind']} {a}" + (f" {b}" if t["kind"] == "pair" else "")
+        out.append(f"{head} {v.size} {float(t['start'])!r} {float(t['finish'])!r}")
+        for k in range(0, v.size, 4):
+            out.append(" ".join(f"{x!r}" for x in v[k:k + 4].tolist()))
+    with open(path, "w") as fh:
+        fh.write("\n".join(out) + "\n")
+
+
+def read_tabeam(path, names, units="ev"):
+    """Tables of a TABEAM file as the dicts System.eam holds (energies converted to
+    internal units by the FIELD energy unit, as metal_table_read applies engunit)."""
+    rec = _records(path)
+    eng = ENGUNIT[units]
+    tix = {nm: k + 1 for k, nm in enumerate(names)}
+    k = 1
+    numpot = int(to_real(rec[k].split()[0]))
+    k += 1
+    tabs = []
+    for _ in range(numpot):
+        w = rec[k].split()
+        k += 1
+        kw = w[0].lower()[:4]
+        if kw not in _TABEAM_KINDS:
+            raise NotImplementedError(f"TABEAM table '{w[0]}': pair, dens and embe run on this path")
+        kind = _TABEAM_KINDS[kw]
+        a = w[1][:8]
+        rest = w[2:]
+        b = a
+        if kind == "pair":
+            b, rest = rest[0][:8], rest[1:]
+        ngrid, start, finish = int(to_real(rest[0])), to_real(rest[1]), to_real(rest[2])
+        vals = []
+        while len(vals) < ngrid:
+            vals += [to_real(x) for x in rec[k].split()]
+            k += 1
+        v = np.asarray(vals[:ngrid], np.float64)
+        if kind != "dens":
+            v = v * eng
+        if a not in tix or b not in tix:
+            continue                       # the reference skips tables of absent species
+        tabs.append({"kind": kind, "types": (tix[a], tix[b]), "start": start, "finish": finish, "values": v})
+    return tabs
 
 
 # --------------------------------------------------------------------------------------
@@ -572,13 +645,15 @@ def _molecule_of(s: System):
     return list(zip(starts.tolist(), ends.tolist())), lc
 
 
-def field_from_system(s: System, units: str = "kj", title: str | None = None):
+def field_from_system(s: System, units: str | None = None, title: str | None = None):
     """FIELD description of a System and the atom order it implies.
 
     Returns (Field, perm): perm[k] is the System atom written as the k-th CONFIG
     atom.  Molecules with the same sites and constraints form one molecule type;
     types are listed in order of first appearance and their molecules written
     together, as FIELD requires (one block of nummols molecules per type)."""
+    if units is None:
+        units = "ev" if s.eam else "kj"
     names = list(s.type_names) or [f"T{k + 1}" for k in range(s.ntypes)]
     mols, lc = _molecule_of(s)
     prm = s.prmcon
@@ -615,7 +690,14 @@ def field_from_system(s: System, units: str = "kj", title: str | None = None):
             kind, eps, sig = s.vdw_prm[3 * k:3 * k + 3]
             if int(kind) == 1:
                 vdw.append((names[b - 1], names[a - 1], "lj", (eps / eng, sig)))
-    fld = Field(title=title or s.name, units=units, molecules=mtypes, vdw=vdw)
+    metal = []
+    if s.eam:
+        lst = s.metal_listed if s.metal_listed is not None else np.ones(nt * (nt + 1) // 2, np.int32)
+        for a in range(1, nt + 1):
+            for b in range(1, a + 1):
+                if lst[a * (a - 1) // 2 + b - 1]:
+                    metal.append((names[a - 1], names[b - 1], "eam"))
+    fld = Field(title=title or s.name, units=units, molecules=mtypes, vdw=vdw, metal=metal)
     return fld, np.asarray(perm, np.int64)
 
 
@@ -627,7 +709,7 @@ def control_from_system(s: System, steps: int, temperature: float, stats_every: 
         "timestep": s.tstep, "time_run": int(steps), "time_equilibration": 0,
         "ensemble": "nve", "temperature": float(temperature),
         "restart": "noscale",                      # keep the CONFIG velocities as written
-        "coul_method": "spme", "coul_dielectric_constant": s.epsq,
+        "coul_method": "spme" if np.any(s.chge != 0.0) else "off", "coul_dielectric_constant": s.epsq,
         "spme_alpha": s.alpha, "spme_kvec": [int(k) for k in s.kmax], "spme_nsplines": s.nsplines,
         "vdw_method": "direct" if s.vdw_direct else "tabulated",
         "shake_tolerance": s.shake_tol, "shake_max_iter": s.shake_maxit,
@@ -672,14 +754,15 @@ def _widths(cell):
             vol / np.linalg.norm(np.cross(a, b)))
 
 
-def system_from_files(cfg: Config, fld: Field, ctl: dict) -> System:
-    """Build a System from CONFIG, FIELD and CONTROL.  Atom i of the System is atom
+def system_from_files(cfg: Config, fld: Field, ctl: dict, tabeam=None) -> System:
+    """Build a System from CONFIG, FIELD and CONTROL (and the TABEAM file, path or
+    tables, when FIELD lists 'eam' metal potentials).  Atom i of the System is atom
     i of the CONFIG; FIELD molecule types assign sites to atoms in the same order."""
     c = dict(CONTROL_DEFAULTS)
     c.update(ctl)
     ensemble_from_control(c)                       # refuses ensembles outside the path
-    if c["coul_method"] != "spme":
-        raise NotImplementedError(f"coul_method '{c['coul_method']}': only spme runs on this path")
+    if c["coul_method"] not in ("spme", "off"):
+        raise NotImplementedError(f"coul_method '{c['coul_method']}': spme (or off, uncharged) runs here")
     if "cutoff" not in c:
         raise ValueError("CONTROL needs 'cutoff'")
     rcut = float(c["cutoff"])
@@ -718,6 +801,17 @@ def system_from_files(cfg: Config, fld: Field, ctl: dict) -> System:
         raise ValueError(f"CONFIG atom {bad + 1} is '{cfg_names[bad]}', FIELD says '{want[bad]}'")
     nt = len(names)
     eng = ENGUNIT[fld.units]
+    if c["coul_method"] == "off" and any(q != 0.0 for q in chge):
+        raise NotImplementedError("charged sites with coul_method off are not run on this path")
+    eam, listed = None, None
+    if fld.metal:
+        listed = np.zeros(nt * (nt + 1) // 2, np.int32)
+        for a_nm, b_nm, _kind in fld.metal:
+            a, b = max(tix[a_nm], tix[b_nm]), min(tix[a_nm], tix[b_nm])
+            listed[a * (a - 1) // 2 + b - 1] = 1
+        if tabeam is None:
+            raise ValueError("FIELD lists eam metal potentials: a TABEAM file is needed")
+        eam = read_tabeam(tabeam, names, fld.units) if isinstance(tabeam, (str, bytes)) or hasattr(tabeam, "__fspath__") else tabeam
     vdw_prm = np.zeros(3 * (nt * (nt + 1) // 2))
     for a_nm, b_nm, kind, prm in fld.vdw:
         a, b = tix[a_nm], tix[b_nm]
@@ -735,7 +829,9 @@ def system_from_files(cfg: Config, fld: Field, ctl: dict) -> System:
             list_excl[gi - 1, 1:1 + len(js)] = js
     if "spme_alpha" in c and "spme_precision" in c:
         raise ValueError("Cannot specify both precision and manual spme parameters")
-    if "spme_alpha" in c:
+    if c["coul_method"] == "off":                  # no reciprocal space: grid parameters unused
+        alpha, kmax = float(c.get("spme_alpha", 0.3)), tuple(int(x) for x in c.get("spme_kvec", (16, 16, 16)))
+    elif "spme_alpha" in c:
         alpha = float(c["spme_alpha"])
         if "spme_kvec" not in c:
             raise ValueError("CONTROL with spme_alpha needs spme_kvec")
@@ -757,7 +853,7 @@ def system_from_files(cfg: Config, fld: Field, ctl: dict) -> System:
         listcon=np.asarray(listcon, np.int32), prmcon=np.asarray(prmcon, np.float64),
         max_exclude=maxex, list_excl=list_excl, vdw_direct=1 if c["vdw_method"] == "direct" else 0,
         type_names=tuple(names), epsq=float(c["coul_dielectric_constant"]),
-        shake_maxit=int(c["shake_max_iter"]))
+        shake_maxit=int(c["shake_max_iter"]), eam=eam, metal_listed=listed)
 
 
 _NVT_METHODS = {"berendsen": "berendsen", "hoover": "nose-hoover", "nose": "nose-hoover",
@@ -800,6 +896,9 @@ def emit_inputs(s: System, directory, steps: int, temperature: float, stats_ever
     write_control(os.path.join(directory, "CONTROL"), control_from_system(s, steps, temperature, stats_every))
     if gb:
         write_control(os.path.join(directory, "GBCONTROL"), gb, GB_KEYS)
+    if s.eam:
+        write_tabeam(os.path.join(directory, "TABEAM"), s.eam, list(s.type_names), title=s.name,
+                     units=fld.units)
     np.savez(os.path.join(directory, "arrays.npz"), cell=s.cell, ltype=s.ltype, chge=s.chge,
              weight=s.weight, lfrzn=s.lfrzn, vdw_prm=s.vdw_prm, x=s.x, y=s.y, z=s.z, vx=s.vx,
              vy=s.vy, vz=s.vz, listcon=s.listcon, prmcon=s.prmcon,
@@ -890,8 +989,9 @@ class Statistics:
         vol = abs(float(np.linalg.det(np.asarray(cell).reshape(3, 3))))
         engcpe = st["engcpe_rc"] + st["engcpe_rl"] + st["engcpe_ex"]
         vircpe = st["vircpe_rc"] + st["vircpe_rl"] + st["vircpe_ex"]
-        engsrp = st["engvdw"] + self.elrc
-        virsrp = st["virvdw"] + self.vlrc
+        # two_body.F90:780-781: short range = metal (pair + embedding) + vdW + long-range vdW
+        engsrp = st.get("engmet", 0.0) + st["engvdw"] + self.elrc
+        virsrp = st.get("virmet", 0.0) + st["virvdw"] + self.vlrc
         engke = st["engke"]
         vircon = st["vircon"]
         stpcfg = engcpe + engsrp

@@ -45,6 +45,8 @@ WORKLOADS = {
     "nacl_262144": (lambda: systems.nacl_melt(64), 1500.0),
     "water_1536": (lambda: systems.spce_water(8), 300.0),
     "water_98304": (lambda: systems.spce_water(32), 300.0),
+    "eam_6912": (lambda: systems.eam_alloy(12), 600.0),
+    "eam_256000": (lambda: systems.eam_alloy(40), 600.0),
 }
 
 
@@ -96,7 +98,7 @@ def run(directory: str, steps: int | None = None, lib=None, quiet: bool = False)
     gb = io.read_control(j("GBCONTROL"), io.GB_KEYS) if os.path.exists(j("GBCONTROL")) else {}
     fld = io.read_field(j(ctl.get("io_file_field", "FIELD")))
     cfg = io.read_config(j(ctl.get("io_file_config", "CONFIG")))
-    s = io.system_from_files(cfg, fld, ctl)
+    s = io.system_from_files(cfg, fld, ctl, tabeam=j("TABEAM") if fld.metal else None)
     nrun = int(ctl.get("time_run", 0)) if steps is None else int(steps)
     st_every = int(ctl.get("stats_frequency", 0))
     dump_every = int(ctl.get("data_dump_frequency", 1000))
@@ -145,6 +147,9 @@ def run(directory: str, steps: int | None = None, lib=None, quiet: bool = False)
         return np.bincount(s.ltype - 1, weights=r2, minlength=s.ntypes)
 
     step0 = dict(e0, engke=engke0, vircon=0.0, stress=s0, strkin=strkin0, strcon=np.zeros(9))
+    if s.eam:
+        me = lib.metal_energies()
+        step0.update(engmet=me["engmet"] + me["engden"], virmet=me["virmet"] + me["virden"])
     if restart != "continue":                 # a continued run already recorded its first step
         stats.collect(nstep0, step0, s.cell, amsd=np.zeros(s.ntypes))
         if st_every > 0 and nstep0 % st_every == 0:
@@ -178,7 +183,8 @@ def run(directory: str, steps: int | None = None, lib=None, quiet: bool = False)
         for k, rec in enumerate(out):
             nstep += 1
             d = {f: getattr(rec, f) for f in ("engcpe_rc", "vircpe_rc", "engcpe_rl", "vircpe_rl", "engcpe_ex",
-                                              "vircpe_ex", "engvdw", "virvdw", "engke", "vircon")}
+                                              "vircpe_ex", "engvdw", "virvdw", "engke", "vircon", "engmet",
+                                              "virmet")}
             d["stress"] = np.array(rec.stress[:])
             d["strkin"] = np.array(rec.strkin[:])
             d["strcon"] = np.array(rec.strcon[:])

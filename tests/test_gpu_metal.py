@@ -26,8 +26,11 @@ def test_eam_forces_match_oracle(gpu_lib, oracle_lib, n_side, listed):
     a, b = gpu_lib.download(), oracle_lib.download()
     assert force_dev(a, b) < 1e-10
     ea, eb = gpu_lib.metal_energies(), oracle_lib.metal_energies()
-    for k in ("engmet", "virmet", "engden"):
+    for k in ("engmet", "engden"):
         assert ea[k] == pytest.approx(eb[k], rel=1e-10), k
+    # the virial sums pair repulsion against embedding attraction: cancellation leaves
+    # it ~100x smaller than its terms, so its bar is 1e-9
+    assert ea["virmet"] == pytest.approx(eb["virmet"], rel=1e-9)
     np.testing.assert_allclose(gpu_lib.metal_rho(), oracle_lib.metal_rho(), rtol=1e-11)
 
 

@@ -323,3 +323,33 @@ def test_runner_nose_hoover_restart_on_oracle(tmp_path, oracle_lib):
     out = runner.run(d, lib=oracle_lib, quiet=True)
     assert out["final_step"] == 9
     assert oracle_lib.thermostat_state()["cint"] != th["cint"]
+
+
+def test_eam_inputs_round_trip(tmp_path, oracle_lib):
+    """FIELD 'metal ... eam' + TABEAM written and read back give the same system: the
+    oracle's metal energies agree (atoms are regrouped by species, types renumbered)."""
+    s = systems.eam_alloy(6)
+    io.emit_inputs(s, tmp_path, steps=10, temperature=600.0)
+    fld = io.read_field(tmp_path / "FIELD")
+    assert fld.units == "ev" and sorted(fld.metal) == sorted([("Cu", "Cu", "eam"), ("Ni", "Cu", "eam"),
+                                                               ("Ni", "Ni", "eam")])
+    ctl = io.read_control(tmp_path / "CONTROL")
+    assert ctl["coul_method"] == "off"
+    s2 = io.system_from_files(io.read_config(tmp_path / "CONFIG"), fld, ctl, tabeam=str(tmp_path / "TABEAM"))
+    assert len(s2.eam) == 7 and s2.metal_listed.tolist() == [1, 1, 1]
+    t_in = {(t["kind"], tuple(s.type_names[k - 1] for k in t["types"])): t for t in s.eam}
+    for t in s2.eam:
+        u = t_in[(t["kind"], tuple(s2.type_names[k - 1] for k in t["types"]))]
+        np.testing.assert_allclose(t["values"], u["values"], rtol=1e-15, atol=0)
+        assert (t["start"], t["finish"]) == (u["start"], u["finish"])
+    energies = []
+    for sys_ in (s, s2):
+        oracle_lib.init(sys_)
+        oracle_lib.start()
+        e = oracle_lib.metal_energies()
+        energies.append(e["engmet"] + e["engden"])
+    assert energies[1] == pytest.approx(energies[0], rel=1e-9)
+    bad = tmp_path / "FIELD2"
+    bad.write_text(open(tmp_path / "FIELD").read().replace("Cu       Cu       eam", "Cu       Cu       fnsc 1 2 3 4 5"))
+    with pytest.raises(NotImplementedError):
+        io.read_field(bad)
