@@ -182,9 +182,12 @@ MEASURED_TRAFFIC = {
     ("pair_forces", "fp64"): ((200.795648e6 + 3.779072e6) / 40368337,
                               "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_fp64 on nacl_175616 "
                               "(profiles/pair_fp64_nacl175616.md), scaled by half-list entries"),
-    ("pair_forces", "mixed"): ((312.066816e6 + 6.53056e6) / 37054682,
-                               "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_mixed on nacl_175616 "
+    ("pair_forces", "mixed"): ((200.9e6 + 5.2e6) / 40368337,
+                               "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_mixed_half on nacl_175616 "
                                "(profiles/pair_mixed_nacl175616.md), scaled by half-list entries"),
+    ("metal_forces", "fp64"): ((131.494144e6 + 4.494848e6) / 19246179,
+                               "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_metal_forces on eam_256000 "
+                               "(profiles/metal_kernels_eam256000.md), scaled by half-list entries"),
 }
 
 
