@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(256, 4) k_pair_mixed_half(int natms, const Dev
         t[3] = fmaf(-eg, rsq, t[3]);
       }
       if (rsq < rv2) {
-        const float4 lj6 = s_lj[row + ltype[j]];
+        const float4 lj6 = s_lj[row + __float_as_int(lj.w)];  // xlo.w holds the type
         if (lj6.w != 0.f) {
           const float s2 = lj6.z * r2i;
           const float s6 = s2 * s2 * s2;
