@@ -36,7 +36,7 @@ Module gb300_interface
   Public :: gb_init, gb_upload_parts, gb_download_parts, gb_relocate, gb_list_build, gb_vnl_check, &
             gb_refresh, gb_forces, gb_spme, gb_vv, gb_md_run, gb_mts_config, gb_mts_stats, &
             gb_set_precision, gb_set_ensemble, gb_set_step, gb_thermostat_state, &
-            gb_set_thermostat_state, gb_finalize
+            gb_set_thermostat_state, gb_set_metal_eam, gb_metal_energies, gb_finalize
 
   Interface
     Integer(c_int) Function gb_init(prm, natms, ltype, chge, weight, lfrzn, vdw_prm, ntcons, listcon, &
@@ -143,6 +143,19 @@ Module gb300_interface
       Import :: c_int, c_double
       Real(c_double), Value :: chi_t, cint
     End Function gb_set_thermostat_state
+
+    Integer(c_int) Function gb_set_metal_eam(ntab, kind, t1, t2, ngrid, start, finish, values, listed) &
+        Bind(C, name="gb_set_metal_eam")
+      Import :: c_int, c_int32_t, c_double
+      Integer(c_int), Value :: ntab
+      Integer(c_int32_t), Intent(In) :: kind(*), t1(*), t2(*), ngrid(*), listed(*)
+      Real(c_double), Intent(In) :: start(*), finish(*), values(*)
+    End Function gb_set_metal_eam
+
+    Integer(c_int) Function gb_metal_energies(out4) Bind(C, name="gb_metal_energies")
+      Import :: c_int, c_double
+      Real(c_double), Intent(Out) :: out4(4)
+    End Function gb_metal_energies
 
     Subroutine gb_finalize() Bind(C, name="gb_finalize")
     End Subroutine gb_finalize
