@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "gb_common.cuh"
+#include "gb_df64.cuh"
 
 Dev g;
 
@@ -83,7 +84,7 @@ void free_all() {
                   g.lfrzn, g.ixyz, g.src, g.shcode, g.xbg, g.ybg, g.zbg, g.ox, g.oy, g.oz, g.which_cell,
                   g.cell_count, g.cell_start, g.cell_fill, g.at_list, g.sorted_pos, g.xs, g.xsf, g.list, g.blk,
                   g.list_excl, g.flist, g.fcount, g.fstart, g.erfc_coef, g.erfc_coef_f, g.vdw_coef, g.vdw_coef_f,
-                  g.vdw_kind, g.vdw_eps, g.vdw_sig, g.blkacc, g.con_i, g.con_j, g.con_d0, g.dxx, g.dyy,
+                  g.vdw_kind, g.vdw_eps, g.vdw_sig, g.erfc_df, g.vdw_df, g.qdf, g.blkacc, g.con_i, g.con_j, g.con_d0, g.dxx, g.dyy,
                   g.dzz, g.dxt, g.dyt, g.dzt, g.dt2, g.gam, g.listot, g.acon_start, g.acon_list, g.sc, d_scratch};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -167,6 +168,26 @@ void build_tables(const double* vdw_prm) {
   dalloc(&g.vdw_coef_f, vc.size());
   GB_CUDA(cudaMemcpy(g.erfc_coef, ec.data(), sizeof(double) * ec.size(), cudaMemcpyHostToDevice));
   GB_CUDA(cudaMemcpy(g.vdw_coef, vc.data(), sizeof(double) * vc.size(), cudaMemcpyHostToDevice));
+  // double-float copies for the FP64 form's pair loop: per interval (c0, c1) of the first
+  // and of the second polynomial as hi/lo pairs, then (c2 first, c2 second) as hi/lo pairs
+  {
+    auto pack = [](const double* c, float4* o) {  // c: first c0..c2, second c3..c5
+      float h0, l0, h1, l1;
+      df_split(c[0], &h0, &l0); df_split(c[1], &h1, &l1);
+      o[0] = make_float4(h0, l0, h1, l1);
+      df_split(c[3], &h0, &l0); df_split(c[4], &h1, &l1);
+      o[1] = make_float4(h0, l0, h1, l1);
+      df_split(c[2], &h0, &l0); df_split(c[5], &h1, &l1);
+      o[2] = make_float4(h0, l0, h1, l1);
+    };
+    std::vector<float4> edf((size_t)(n + 1) * 3), vdf((size_t)g.nkey * (mg + 3) * 3);
+    for (size_t k = 0; k < (size_t)(n + 1); ++k) pack(&ec[k * 6], &edf[k * 3]);
+    for (size_t k = 0; k < (size_t)g.nkey * (mg + 3); ++k) pack(&vc[k * 6], &vdf[k * 3]);
+    dalloc(&g.erfc_df, edf.size());
+    dalloc(&g.vdw_df, vdf.size());
+    GB_CUDA(cudaMemcpy(g.erfc_df, edf.data(), sizeof(float4) * edf.size(), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(g.vdw_df, vdf.data(), sizeof(float4) * vdf.size(), cudaMemcpyHostToDevice));
+  }
   std::vector<float> ecf(ec.begin(), ec.end()), vcf(vc.begin(), vc.end());
   GB_CUDA(cudaMemcpy(g.erfc_coef_f, ecf.data(), sizeof(float) * ecf.size(), cudaMemcpyHostToDevice));
   GB_CUDA(cudaMemcpy(g.vdw_coef_f, vcf.data(), sizeof(float) * vcf.size(), cudaMemcpyHostToDevice));
@@ -198,7 +219,7 @@ int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real, bo
   double erc = 0, vrc = 0;
   double e6[6] = {0, 0, 0, 0, 0, 0};
   integ_zero_forces();
-  if (g.precision == GB_MIXED) list_pos_f32();
+  if (g.precision == GB_MIXED || !g.pair_native) list_pos_f32();  // FP32 hi + lo positions
   const bool mts = md_step && do_spme && mts_active();
   const bool full = mts ? mts_step_needs_spme() : (do_spme && g.has_coul);
   if (full) spme_forces(&erc, &vrc, strec);
@@ -384,7 +405,9 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     g.p = *prm;
     g.natms = natms;
     g.mxatms = std::max(prm->mxatms, natms);
-    g.precision = prm->precision;
+    if (prm->precision < GB_FP64 || prm->precision > GB_FP64_NATIVE) return GB_ERR_ARG;
+    g.precision = prm->precision == GB_MIXED ? GB_MIXED : GB_FP64;
+    g.pair_native = prm->precision == GB_FP64_NATIVE;
     std::memcpy(g.cell, prm->cell, sizeof(g.cell));
     double det;
     invert_host(g.cell, g.rcell, &det);
@@ -401,6 +424,7 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     dalloc(&g.x, mx); dalloc(&g.y, mx); dalloc(&g.z, mx);
     dalloc(&g.xf, mx);
     dalloc(&g.xlo, mx);
+    dalloc(&g.qdf, mx);
     dalloc(&g.fx, natms); dalloc(&g.fy, natms); dalloc(&g.fz, natms);
     dalloc(&g.fixp, 3 * (size_t)natms);
     dalloc(&g.vx, natms); dalloc(&g.vy, natms); dalloc(&g.vz, natms);
@@ -769,13 +793,14 @@ int gb_mts_config(int k, double tol, int train_steps) {
 
 int gb_set_precision(int precision) {
   return guarded([&]() {
-    if (precision != GB_FP64 && precision != GB_MIXED) return (int)GB_ERR_ARG;
+    if (precision < GB_FP64 || precision > GB_FP64_NATIVE) return (int)GB_ERR_ARG;
     if (precision == GB_MIXED && g.has_metal) return (int)GB_ERR_ARG;  // metals run in the FP64 form
     if (precision != GB_MIXED && mts_active()) {  // the learned form runs on the mixed path only
       mts_free();
       g.mts_k = 1;
     }
-    g.precision = precision;
+    g.precision = precision == GB_MIXED ? GB_MIXED : GB_FP64;
+    g.pair_native = precision == GB_FP64_NATIVE;
     return (int)GB_OK;
   });
 }

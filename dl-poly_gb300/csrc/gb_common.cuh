@@ -113,6 +113,10 @@ struct Dev {
   bool lbook = false;
   int megfrz = 0;
   bool has_coul = true, has_vdw = true, has_metal = false;  // which force terms the system has
+  bool pair_native = false;    // FP64 form: pair loop in native FP64 (else double-float on FP32 pipes)
+  float4* erfc_df = nullptr;   // double-float erfc tables: 3 float4 per interval
+  float4* vdw_df = nullptr;    // double-float vdW tables: per key (max_grid + 3) x 3 float4
+  float2* qdf = nullptr;       // charges as double-floats (mxatms), written with the FP32 positions
   double metal_e4[4] = {0, 0, 0, 0};  // engmet, virmet, engden, virden of the last evaluation
   // thermostat of the VV stages (gb_thermostat.cu)
   int ens = 0;                 // GB_NVE, GB_NVT_BERENDSEN, GB_NVT_NOSE_HOOVER, GB_NVT_LANGEVIN

@@ -1,0 +1,104 @@
+// gb_df64.cuh - double-float arithmetic: a value is the unevaluated sum hi + lo of two
+// FP32 numbers (|lo| <= ulp(hi)/2), about 48 significant bits.  On GB300 the FP64
+// pipe runs at 1/64 of the FP32 rate, so kernels that need FP64-level accuracy but
+// not FP64 range evaluate their inner loops in this form on the FP32 pipes.
+//
+// The operations are the error-free transformations of the double-double literature
+// (Knuth's two-sum, the FMA two-product; see Hida, Li and Bailey, "Library for
+// double-double and quad-double arithmetic", 2007), written with the _rn intrinsics
+// so the compiler cannot contract or reassociate them.
+#ifndef GB_DF64_CUH
+#define GB_DF64_CUH
+
+struct df {
+  float hi, lo;
+};
+
+__device__ __forceinline__ df df_make(float hi, float lo) {
+  df r;
+  r.hi = hi;
+  r.lo = lo;
+  return r;
+}
+
+// s + e = a + b exactly
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return df_make(s, e);
+}
+
+// the same for |a| >= |b|
+__device__ __forceinline__ df quick_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return df_make(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+
+// p + e = a * b exactly
+__device__ __forceinline__ df two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return df_make(p, __fmaf_rn(a, b, -p));
+}
+
+__device__ __forceinline__ df df_add(df a, df b) {
+  const df s = two_sum(a.hi, b.hi);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ df df_add_f(df a, float b) {
+  const df s = two_sum(a.hi, b);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+
+__device__ __forceinline__ df df_neg(df a) { return df_make(-a.hi, -a.lo); }
+
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const df p = two_prod(a.hi, b.hi);
+  return quick_two_sum(p.hi, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo)));
+}
+
+__device__ __forceinline__ df df_mul_f(df a, float b) {
+  const df p = two_prod(a.hi, b);
+  return quick_two_sum(p.hi, __fmaf_rn(a.lo, b, p.lo));
+}
+
+__device__ __forceinline__ df df_sqr(df a) {
+  const df p = two_prod(a.hi, a.hi);
+  return quick_two_sum(p.hi, __fmaf_rn(__fmul_rn(2.0f, a.hi), a.lo, p.lo));
+}
+
+// 1/sqrt(a) for a > 0: FP32 seed and one Newton step whose residual 1 - a r^2 is formed
+// in double-float (relative error about 4e-14)
+__device__ __forceinline__ df df_rsqrt(df a) {
+  const float r = rsqrtf(a.hi);
+  const df ar2 = df_mul(a, two_prod(r, r));
+  const float h = __fsub_rn(__fsub_rn(1.0f, ar2.hi), ar2.lo);
+  return quick_two_sum(r, __fmul_rn(__fmul_rn(0.5f, r), h));
+}
+
+__device__ __forceinline__ double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
+
+__host__ __device__ inline void df_split(double v, float* hi, float* lo) {
+  *hi = (float)v;
+  *lo = (float)(v - (double)*hi);
+}
+
+// running sum of many double-float terms: s carries the sum, c its rounding errors
+struct dacc {
+  float s, c;
+};
+
+__device__ __forceinline__ void dacc_add(dacc& a, df t) {
+  const df u = two_sum(a.s, t.hi);
+  a.s = u.hi;
+  a.c = __fadd_rn(a.c, __fadd_rn(u.lo, t.lo));
+}
+
+__device__ __forceinline__ double dacc_value(const dacc& a) { return (double)a.s + (double)a.c; }
+
+// int64 fixed point (scale 2^40) of a double-float: both parts converted by integer
+// operations (fix40), the low part truncated
+__device__ __forceinline__ long long fix40_df(df a) { return fix40(a.hi) + fix40(a.lo); }
+
+#endif

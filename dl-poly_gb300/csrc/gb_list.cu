@@ -473,13 +473,17 @@ __global__ void k_list_reorder(int natms, int* list, int ld, const int* lfrzn, c
 // FP32 hi parts with the charge, and the lo remainders with the atom type in the
 // fourth word (bit pattern), so a pair reads everything about j in two 16-byte loads
 __global__ void k_pos_f32(const DevScalars* sc, const double* x, const double* y, const double* z,
-                          const double* q, const int* ltype, float4* xf, float4* xlo) {
+                          const double* q, const int* ltype, float4* xf, float4* xlo, float2* qdf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= sc->nlast) return;
   const float hx = (float)x[i], hy = (float)y[i], hz = (float)z[i];
   xf[i] = make_float4(hx, hy, hz, (float)q[i]);
   xlo[i] = make_float4((float)(x[i] - (double)hx), (float)(y[i] - (double)hy), (float)(z[i] - (double)hz),
                        __int_as_float(ltype[i]));
+  if (qdf) {  // the charge as a double-float (FP64 form)
+    const float qh = (float)q[i];
+    qdf[i] = make_float2(qh, (float)(q[i] - (double)qh));
+  }
 }
 
 // ------------------------------------------------------ derived full list
@@ -715,7 +719,8 @@ int list_build() {
 }
 
 void list_pos_f32() {
-  k_pos_f32<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(g.sc, g.x, g.y, g.z, g.chge, g.ltype, g.xf, g.xlo);
+  k_pos_f32<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(g.sc, g.x, g.y, g.z, g.chge, g.ltype, g.xf, g.xlo,
+                                                         g.precision == GB_FP64 ? g.qdf : nullptr);
   GB_LAUNCHED();
 }
 

@@ -21,6 +21,7 @@
 #include <cstring>
 
 #include "gb_common.cuh"
+#include "gb_df64.cuh"
 
 namespace {
 
@@ -35,6 +36,10 @@ struct PairGeom {
   int vdw_direct;
   int same_grid;             // erdr == vrdr: one table coordinate serves both tables
   int nsamples, max_grid, ntypes;
+  // double-float kernel: cutoff bands on the FP32 high part of r^2 (1e-6 relative) and
+  // the table spacings as double-floats
+  float f_rc2_lo, f_rc2_hi, f_rv2_lo, f_rv2_hi, f_hi;
+  float erdr_hi, erdr_lo, vrdr_hi, vrdr_lo, scal_hi, scal_lo;
 };
 
 
@@ -425,6 +430,246 @@ void pair_setup() {
   GB_CUDA(cudaMemcpyToSymbol(c_lj, lj, sizeof(lj)));
 }
 
+// ------------------------------------------------------- FP64 form, double-float
+// The FP64 form's pair loop on the FP32 pipes: positions as FP32 hi + lo pairs (48
+// bits), the separation formed with an exact two-sum, r^2, 1/r, the table coordinate and
+// the three-point polynomials in double-float; pair forces summed as int64 fixed point
+// (2^40) with 64-bit integer atomics for j, energies and virials in double-float running
+// sums.  Pairs whose r^2 lies within 1e-6 of a cutoff squared, and pairs in the first
+// table interval, take the FP64 formulas of k_pair_fp64 (exact cutoff decisions).
+// Measured against the FP64 oracle: forces and energies agree to ~1e-13.
+
+// per interval of a double-float table: (c0 hi, c0 lo, c1 hi, c1 lo) of the energy and
+// of the force polynomial, then (c2 hi, c2 lo) of both; c0 + d (c1 + d c2) in double-float
+// throughout (near the repulsive wall of a 12-6 table the quadratic term reaches 1e-3 of
+// the value, so it needs the full precision too)
+__device__ __forceinline__ df poly_df(float4 c01, float c2h, float c2l, df d) {
+  const df t = df_add(df_make(c01.z, c01.w), df_mul(d, df_make(c2h, c2l)));
+  return df_add(df_make(c01.x, c01.y), df_mul(d, t));
+}
+
+// FP64 terms of one pair, as k_pair_fp64 evaluates them (slow path)
+__device__ void pair_terms_fp64(const PairGeom& pg, double dx, double dy, double dz, double qi, double qj, int ai,
+                                int aj, const double* ecoef, const double* vcoef, const int* vkind, const double* veps,
+                                const double* vsig, double* gam, double* ee, double* ev, double* gvc, double* gvv,
+                                bool* any) {
+  *gam = *ee = *ev = *gvc = *gvv = 0.0;
+  *any = false;
+  const double rsq = dx * dx + dy * dy + dz * dz;
+  const double rrr = sqrt(rsq);
+  const bool in_c = rrr < pg.rcut && qi != 0.0 && qj != 0.0;
+  int key = -1;
+  if (rrr < pg.rvdw) {
+    key = vkey(ai, aj) - 1;
+    if (vkind[key] == 0) key = -1;
+  }
+  if (!in_c && key < 0) return;
+  *any = true;
+  if (in_c) {
+    const double ppp = rrr * pg.erdr;
+    const int k = (int)ppp;
+    const double d = ppp - (double)k;
+    const double* c = ecoef + (size_t)k * 6;
+    const double pre = qi * qj;
+    double eg, ec;
+    if (k > 0) {
+      eg = pre * fma(d, fma(d, c[5], c[4]), c[3]);
+      ec = pre * fma(d, fma(d, c[2], c[1]), c[0]);
+    } else {
+      eg = pre * three_p_exact(c + 3, d, rrr);
+      ec = pre * three_p_exact(c, d, rrr);
+    }
+    *gam = eg; *ee = ec; *gvc = eg;
+  }
+  if (key >= 0) {
+    const double rinv = 1.0 / rrr, r_rsq = rinv * rinv;
+    double gv, e;
+    if (pg.vdw_direct) {
+      const double sr = vsig[key] * rinv;
+      const double s2 = sr * sr, s6 = s2 * s2 * s2;
+      e = 4.0 * veps[key] * s6 * (s6 - 1.0);
+      gv = 24.0 * veps[key] * s6 * (2.0 * s6 - 1.0) * r_rsq;
+    } else {
+      const double pv = rrr * pg.vrdr;
+      const int kv = (int)pv;
+      const double dv = pv - (double)kv;
+      const double* c = vcoef + (size_t)key * (pg.max_grid + 3) * 6 + (size_t)kv * 6;
+      if (kv > 0) {
+        gv = fma(dv, fma(dv, c[2], c[1]), c[0]) * r_rsq;
+        e = fma(dv, fma(dv, c[5], c[4]), c[3]);
+      } else {
+        gv = three_p_exact(c, dv, rrr) * r_rsq;
+        e = three_p_exact(c + 3, dv, rrr);
+      }
+    }
+    *gam += gv; *ev = e; *gvv = gv;
+  }
+}
+
+// table coordinate of a double-float r: k = Int(ppp) and d = ppp - k in double-float
+__device__ __forceinline__ int table_coord(df rrr, float sh, float sl, df* d) {
+  const df ppp = df_mul(rrr, df_make(sh, sl));
+  int k = (int)ppp.hi;                                   // ppp >= 0: truncation
+  if ((float)k == ppp.hi && ppp.lo < 0.0f) --k;          // hi integral, value just below it
+  *d = quick_two_sum(__fsub_rn(ppp.hi, (float)k), ppp.lo);
+  return k;
+}
+
+__global__ void __launch_bounds__(256, 2) k_pair_df64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
+                                                   const int* __restrict__ list, int ld,
+                                                   const float4* __restrict__ xf, const float4* __restrict__ xlo,
+                                                   const float2* __restrict__ qdf, const double* __restrict__ x,
+                                                   const double* __restrict__ y, const double* __restrict__ z,
+                                                   const double* __restrict__ q, const int* __restrict__ ltg,
+                                                   const int* __restrict__ src, const float4* __restrict__ etab,
+                                                   const float4* __restrict__ vtab, const double* __restrict__ ecoef,
+                                                   const double* __restrict__ vcoef, const int* __restrict__ vkind,
+                                                   const double* __restrict__ veps, const double* __restrict__ vsig,
+                                                   PairGeom pg, unsigned long long* fixp, double* blk,
+                                                   unsigned long long* cnt) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  dacc acc[NACC];
+#pragma unroll
+  for (int k = 0; k < NACC; ++k) { acc[k].s = 0.f; acc[k].c = 0.f; }
+  unsigned long long n_list = 0, n_rc = 0;
+  const int nlast = sc->nlast;
+  const int vstride = (pg.max_grid + 3) * 3;  // float4 per key
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nlast; w += nwarps) {
+    const int i = at_list[w];
+    if (i >= natms) continue;
+    const float4 pi = xf[i], li = xlo[i];
+    const float2 qi2 = qdf[i];
+    const df qi = df_mul(df_make(qi2.x, qi2.y), df_make(pg.scal_hi, pg.scal_lo));  // q_i r4pie0/eps
+    const bool qi_on = qi2.x != 0.0f;
+    const int ai = __float_as_int(li.w), gi = ltg[i];
+    const int* lst = list + (size_t)i * ld + 3;
+    const int n = lst[0];
+    long long sx = 0, sy = 0, sz = 0;
+    for (int m = lane + 1; m <= n; m += 32) {
+      const int j = lst[m] - 1;
+      int jf = j;
+      if (j >= natms) {
+        if (gi > ltg[j]) continue;  // evaluated from the other side
+        jf = src[j];
+      }
+      const float4 pj = xf[j], lj = xlo[j];
+      // separation: exact difference of the high parts plus the difference of the low parts
+      const df ex = two_sum(pi.x, -pj.x), ey = two_sum(pi.y, -pj.y), ez = two_sum(pi.z, -pj.z);
+      const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
+      const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
+      const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
+      const df rsq = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+      if (rsq.hi > pg.f_hi) continue;
+      const int aj = __float_as_int(lj.w);
+      const float2 qj2 = qdf[j];
+      const bool band = (rsq.hi >= pg.f_rc2_lo && rsq.hi <= pg.f_rc2_hi) ||
+                        (rsq.hi >= pg.f_rv2_lo && rsq.hi <= pg.f_rv2_hi);
+      const bool in_c = qi_on && qj2.x != 0.0f && rsq.hi < pg.f_rc2_lo;
+      int key = -1;
+      if (rsq.hi < pg.f_rv2_lo) {
+        key = vkey(ai, aj) - 1;
+        if (vkind[key] == 0) key = -1;
+      }
+      df gam = df_make(0.f, 0.f), ee = gam, ev = gam, gvc = gam, gvv = gam;
+      bool slow = band;
+      if (!slow && (in_c || key >= 0)) {
+        const df rinv = df_rsqrt(rsq);
+        const df rrr = df_mul(rsq, rinv);
+        df d;
+        const int k = table_coord(rrr, pg.erdr_hi, pg.erdr_lo, &d);
+        int kv = k;
+        df dv = d;
+        if (!pg.same_grid && key >= 0) kv = table_coord(rrr, pg.vrdr_hi, pg.vrdr_lo, &dv);
+        if (k == 0 || (key >= 0 && kv == 0)) {
+          slow = true;  // first interval: the exact three-point formula, in FP64
+        } else {
+          if (in_c) {  // real-space Coulomb (ewald_spole.F90:131-176)
+            const float4* c = etab + (size_t)k * 3;
+            const float4 e01 = c[0], d01 = c[1], c2 = c[2];
+            const df pre = df_mul(qi, df_make(qj2.x, qj2.y));
+            gvc = df_mul(pre, poly_df(d01, c2.z, c2.w, d));
+            ee = df_mul(pre, poly_df(e01, c2.x, c2.y, d));
+            gam = gvc;
+          }
+          if (key >= 0) {  // van der Waals, tabulated (vdw.F90:1881-1962)
+            const df r_rsq = df_sqr(rinv);
+            if (pg.vdw_direct) {
+              slow = true;
+            } else {
+              const float4* c = vtab + (size_t)key * vstride + (size_t)kv * 3;
+              const float4 f01 = c[0], v01 = c[1], c2 = c[2];
+              gvv = df_mul(poly_df(f01, c2.x, c2.y, dv), r_rsq);
+              ev = poly_df(v01, c2.z, c2.w, dv);
+              gam = df_add(gam, gvv);
+            }
+          }
+        }
+      }
+      if (slow) {
+        double g64, e64c, e64v, gc64, gv64;
+        bool any;
+        pair_terms_fp64(pg, x[i] - x[j], y[i] - y[j], z[i] - z[j], q[i] * pg.scaling, q[j], ai, aj, ecoef, vcoef,
+                        vkind, veps, vsig, &g64, &e64c, &e64v, &gc64, &gv64, &any);
+        if (!any) continue;
+        float h, l;
+        df_split(g64, &h, &l); gam = df_make(h, l);
+        df_split(e64c, &h, &l); ee = df_make(h, l);
+        df_split(e64v, &h, &l); ev = df_make(h, l);
+        df_split(gc64, &h, &l); gvc = df_make(h, l);
+        df_split(gv64, &h, &l); gvv = df_make(h, l);
+      } else if (!in_c && key < 0) {
+        continue;
+      }
+      ++n_rc;
+      const df fxx = df_mul(gam, dx), fyy = df_mul(gam, dy), fzz = df_mul(gam, dz);
+      const long long ix = fix40_df(fxx), iy = fix40_df(fyy), iz = fix40_df(fzz);
+      sx += ix; sy += iy; sz += iz;
+      atomicAdd(&fixp[3 * jf + 0], (unsigned long long)(-ix));
+      atomicAdd(&fixp[3 * jf + 1], (unsigned long long)(-iy));
+      atomicAdd(&fixp[3 * jf + 2], (unsigned long long)(-iz));
+      dacc_add(acc[0], ev);
+      dacc_add(acc[1], df_neg(df_mul(gvv, rsq)));
+      dacc_add(acc[2], ee);
+      dacc_add(acc[3], df_neg(df_mul(gvc, rsq)));
+      dacc_add(acc[4], df_mul(dx, fxx)); dacc_add(acc[5], df_mul(dx, fyy)); dacc_add(acc[6], df_mul(dx, fzz));
+      dacc_add(acc[7], df_mul(dy, fyy)); dacc_add(acc[8], df_mul(dy, fzz)); dacc_add(acc[9], df_mul(dz, fzz));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, o);
+      sy += __shfl_xor_sync(0xffffffffu, sy, o);
+      sz += __shfl_xor_sync(0xffffffffu, sz, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&fixp[3 * i + 0], (unsigned long long)sx);
+      atomicAdd(&fixp[3 * i + 1], (unsigned long long)sy);
+      atomicAdd(&fixp[3 * i + 2], (unsigned long long)sz);
+      n_list += (unsigned long long)n;
+    }
+  }
+  double out[NACC];
+#pragma unroll
+  for (int k = 0; k < NACC; ++k) out[k] = dacc_value(acc[k]);
+  n_rc = (unsigned long long)warp_sumi((int)n_rc);
+  if (lane == 0) {
+    atomicAdd(&cnt[0], n_list);
+    atomicAdd(&cnt[1], n_rc);
+  }
+  block_reduce_store<NACC>(out, blk);
+}
+
+// FP64 form: forces of the other terms are in fx; add the double-float pair kernel's
+// fixed-point sums
+__global__ void k_fix_add_fp64(int n, const long long* fixp, double* fx, double* fy, double* fz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double s = 1.0 / 1099511627776.0;
+  fx[i] += (double)fixp[3 * i] * s;
+  fy[i] += (double)fixp[3 * i + 1] * s;
+  fz[i] += (double)fixp[3 * i + 2] * s;
+}
+
 // eng6: engrl, virrl, engex, virex, engvdw, virvdw; stress9 accumulates.
 void pair_forces(double* eng6, double* stress9) {
   PairGeom pg;
@@ -457,7 +702,40 @@ void pair_forces(double* eng6, double* stress9) {
   double ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const int nb2 = nblocks(g.natms, 128);
   GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
-  if (g.precision == GB_FP64) {
+  if (g.precision == GB_FP64 && !g.pair_native) {
+    // double-float bands and spacings
+    pg.f_rc2_lo = (float)(pg.rc2 * (1.0 - 1e-6));
+    pg.f_rc2_hi = (float)(pg.rc2 * (1.0 + 1e-6));
+    pg.f_rv2_lo = (float)(pg.rv2 * (1.0 - 1e-6));
+    pg.f_rv2_hi = (float)(pg.rv2 * (1.0 + 1e-6));
+    pg.f_hi = std::max(pg.f_rc2_hi, pg.f_rv2_hi);
+    df_split(pg.erdr, &pg.erdr_hi, &pg.erdr_lo);
+    df_split(pg.vrdr, &pg.vrdr_hi, &pg.vrdr_lo);
+    df_split(pg.scaling, &pg.scal_hi, &pg.scal_lo);
+    static int occdf = 0;
+    if (!occdf) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occdf, k_pair_df64, T, 0));
+    int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, T), occdf * g.nsm));
+    double* blk = gb_blkacc(nb * NACC + nb2 * 8);
+    GB_CUDA(cudaMemsetAsync(g.fixp, 0, sizeof(long long) * 3 * (size_t)g.natms, st));
+    prof_begin(P_PAIR);
+    k_pair_df64<<<nb, T, 0, st>>>(g.natms, g.sc, g.at_list, g.list, g.ld, g.xf, g.xlo, g.qdf, g.x, g.y, g.z, g.chge,
+                                  g.ltg, g.src, g.erfc_df, g.vdw_df, g.erfc_coef, g.vdw_coef, g.vdw_kind, g.vdw_eps,
+                                  g.vdw_sig, pg, (unsigned long long*)g.fixp, blk, &g.sc->npairs_list);
+    GB_LAUNCHED();
+    k_fix_add_fp64<<<nblocks(g.natms, 256), 256, 0, st>>>(g.natms, g.fixp, g.fx, g.fy, g.fz);
+    GB_LAUNCHED();
+    prof_end(P_PAIR);
+    gb_reduce_blocks(blk, nb, NACC, &g.sc->acc[A_PAIR]);
+    if (g.lbook) {
+      double* blk2 = blk + (size_t)nb * NACC;
+      prof_begin(P_EXCL);
+      k_excl_fp64<<<nb2, 128, 0, st>>>(g.natms, g.list, g.ld, g.x, g.y, g.z, g.chge, g.ltg, g.src, g.p.alpha,
+                                       g.scaling, g.p.rcut, g.fx, g.fy, g.fz, blk2, nullptr);
+      GB_LAUNCHED();
+      prof_end(P_EXCL);
+      gb_reduce_blocks(blk2, nb2, 8, &g.sc->acc[A_EXCL]);
+    }
+  } else if (g.precision == GB_FP64) {
     static int occ64 = 0;
     if (!occ64) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_pair_fp64, T, 0));
     int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, T), occ64 * g.nsm));

@@ -48,8 +48,9 @@ extern "C" {
 #define GB_ERR_RNG (-7)        /* a Gaussian deviate's rejection loop hit its iteration cap */
 
 /* Precision forms of the force path. */
-#define GB_FP64 0   /* plain: FP64 throughout */
+#define GB_FP64 0   /* plain: FP64 accuracy; the pair loop in double-float (FP32 pairs) */
 #define GB_MIXED 1  /* FP32 pair/spline/FFT arithmetic, int64 fixed-point forces (2^40) */
+#define GB_FP64_NATIVE 2  /* the FP64 form with every pair evaluated in native FP64 */
 
 /* Ensembles of the VV stages (thermo%ensemble, drivers.F90:1132-1175) */
 #define GB_NVE 0              /* nve_0_vv */

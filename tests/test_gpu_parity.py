@@ -39,10 +39,12 @@ def test_pair_set_bit_exact(gpu_lib, oracle_lib, name):
     assert np.array_equal(ld, lr)
 
 
+@pytest.mark.parametrize("precision", [0, 2], ids=["fp64", "fp64_native"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_forces_fp64(gpu_lib, oracle_lib, name):
+def test_forces_fp64(gpu_lib, oracle_lib, name, precision):
+    """The FP64 form (pair loop in double-float) and its all-native-FP64 variant."""
     s = CASES[name]()
-    _pair(gpu_lib, oracle_lib, s)
+    _pair(gpu_lib, oracle_lib, s, precision=precision)
     gpu_lib.link_cell_pairs(want_list=False)
     oracle_lib.link_cell_pairs(want_list=False)
     ed, sd = gpu_lib.two_body_forces()
