@@ -515,7 +515,7 @@ __device__ __forceinline__ int table_coord(df rrr, float sh, float sl, df* d) {
   return k;
 }
 
-__global__ void __launch_bounds__(256, 2) k_pair_df64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
+__global__ void __launch_bounds__(256, 3) k_pair_df64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
                                                    const int* __restrict__ list, int ld,
                                                    const float4* __restrict__ xf, const float4* __restrict__ xlo,
                                                    const float2* __restrict__ qdf, const double* __restrict__ x,
