@@ -219,7 +219,7 @@ int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real, bo
   double erc = 0, vrc = 0;
   double e6[6] = {0, 0, 0, 0, 0, 0};
   integ_zero_forces();
-  if (g.precision == GB_MIXED || !g.pair_native) list_pos_f32();  // FP32 hi + lo positions
+  if (g.precision == GB_MIXED || !g.fp64_native) list_pos_f32();  // FP32 hi + lo positions
   const bool mts = md_step && do_spme && mts_active();
   const bool full = mts ? mts_step_needs_spme() : (do_spme && g.has_coul);
   if (full) spme_forces(&erc, &vrc, strec);
@@ -407,7 +407,7 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     g.mxatms = std::max(prm->mxatms, natms);
     if (prm->precision < GB_FP64 || prm->precision > GB_FP64_NATIVE) return GB_ERR_ARG;
     g.precision = prm->precision == GB_MIXED ? GB_MIXED : GB_FP64;
-    g.pair_native = prm->precision == GB_FP64_NATIVE;
+    g.fp64_native = prm->precision == GB_FP64_NATIVE;
     std::memcpy(g.cell, prm->cell, sizeof(g.cell));
     double det;
     invert_host(g.cell, g.rcell, &det);
@@ -800,7 +800,7 @@ int gb_set_precision(int precision) {
       g.mts_k = 1;
     }
     g.precision = precision == GB_MIXED ? GB_MIXED : GB_FP64;
-    g.pair_native = precision == GB_FP64_NATIVE;
+    g.fp64_native = precision == GB_FP64_NATIVE;
     return (int)GB_OK;
   });
 }

@@ -113,7 +113,7 @@ struct Dev {
   bool lbook = false;
   int megfrz = 0;
   bool has_coul = true, has_vdw = true, has_metal = false;  // which force terms the system has
-  bool pair_native = false;    // FP64 form: pair loop in native FP64 (else double-float on FP32 pipes)
+  bool fp64_native = false;    // FP64 form: pair loop in native FP64 (else double-float on FP32 pipes)
   float4* erfc_df = nullptr;   // double-float erfc tables: 3 float4 per interval
   float4* vdw_df = nullptr;    // double-float vdW tables: per key (max_grid + 3) x 3 float4
   float2* qdf = nullptr;       // charges as double-floats (mxatms), written with the FP32 positions

@@ -702,7 +702,7 @@ void pair_forces(double* eng6, double* stress9) {
   double ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const int nb2 = nblocks(g.natms, 128);
   GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
-  if (g.precision == GB_FP64 && !g.pair_native) {
+  if (g.precision == GB_FP64 && !g.fp64_native) {
     // double-float bands and spacings
     pg.f_rc2_lo = (float)(pg.rc2 * (1.0 - 1e-6));
     pg.f_rc2_hi = (float)(pg.rc2 * (1.0 + 1e-6));

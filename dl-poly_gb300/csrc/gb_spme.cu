@@ -27,6 +27,7 @@
 #include <cmath>
 
 #include "gb_common.cuh"
+#include "gb_dfr.cuh"
 
 namespace {
 
@@ -36,6 +37,7 @@ constexpr int TX = 4;  // columns per tile in the strided passes
 template <typename T> struct V2;
 template <> struct V2<double> { using t = double2; };
 template <> struct V2<float> { using t = float2; };
+template <> struct V2<dfr> { using t = dfc; };
 
 template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
   T2 r;
@@ -816,6 +818,11 @@ struct SpmeGrid {
   int* gidx = nullptr;         // warp gather: first grid index per dimension (truncation convention)
   float* gw = nullptr;         // warp gather: fractional coordinate per dimension
   float* fout_f = nullptr;     // warp gather: unscaled reciprocal forces
+  // double-float copies for the FP64 form (main grid): influence function, stress
+  // factor and twiddles; the grids themselves reuse the FP64 buffers (same sizes)
+  dfr *theta_d = nullptr, *psi_d = nullptr;
+  dfc* tw_d[3] = {nullptr, nullptr, nullptr};
+  dfc* twh_d = nullptr;
 };
 
 SpmeGrid S_main, S_coarse;
@@ -855,7 +862,8 @@ void raise_smem(K kernel, int bytes) {
 void grid_free(SpmeGrid& S) {
   void* ptrs[] = {S.spl, S.nidx, S.brick_of, S.brick_count, S.brick_start, S.brick_fill, S.brick_atoms, S.Q, S.G,
                   S.Qf, S.Gf, S.theta, S.psi, S.theta_f, S.psi_f, S.tw[0], S.tw[1], S.tw[2], S.twf[0], S.twf[1],
-                  S.twf[2], S.twh, S.twhf, S.fspme, S.spread_ext, S.gidx, S.gw, S.fout_f};
+                  S.twf[2], S.twh, S.twhf, S.fspme, S.spread_ext, S.gidx, S.gw, S.fout_f, S.theta_d, S.psi_d,
+                  S.tw_d[0], S.tw_d[1], S.tw_d[2], S.twh_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   S = SpmeGrid();
@@ -915,6 +923,8 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
     GB_CUDA(cudaMalloc(&S.spread_ext, sizeof(double) * tsize * S.nbricks));
     raise_smem(k_spme_spread_tile<double, 8>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(double)));
     raise_smem(k_spme_spread_tile<double, 0>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(double)));
+    raise_smem(k_spme_spread_tile<dfr, 8>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(dfr)));
+    raise_smem(k_spme_spread_tile<dfr, 0>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(dfr)));
     raise_smem(k_spme_spread_tile<float, 8>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
     raise_smem(k_spme_spread_tile<float, 0>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
     raise_smem(k_spme_spread_fix<8>, (int)(tsize * sizeof(long long)));
@@ -992,22 +1002,29 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
     GB_CUDA(cudaMemcpy(S.psi, ps.data(), sizeof(double) * NG, cudaMemcpyHostToDevice));
   }
   // twiddles e^{+2 pi i t / K}
-  auto mk_tw = [](int K, double2** dd, float2** df) {
+  auto mk_tw = [&S](int K, double2** dd, float2** df, dfc** dc) {
     std::vector<double2> t(K);
     std::vector<float2> tf(K);
+    std::vector<dfc> tc(K);
     const double twopi = 2.0 * 3.14159265358979323846264338327950288;
     for (int i = 0; i < K; ++i) {
       double a = twopi * (double)i / (double)K;
       t[i] = make_double2(std::cos(a), std::sin(a));
       tf[i] = make_float2((float)t[i].x, (float)t[i].y);
+      tc[i].x = dfr(t[i].x);
+      tc[i].y = dfr(t[i].y);
     }
     GB_CUDA(cudaMalloc(dd, sizeof(double2) * K));
     GB_CUDA(cudaMalloc(df, sizeof(float2) * K));
     GB_CUDA(cudaMemcpy(*dd, t.data(), sizeof(double2) * K, cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(*df, tf.data(), sizeof(float2) * K, cudaMemcpyHostToDevice));
+    if (S.fp64) {
+      GB_CUDA(cudaMalloc(dc, sizeof(dfc) * K));
+      GB_CUDA(cudaMemcpy(*dc, tc.data(), sizeof(dfc) * K, cudaMemcpyHostToDevice));
+    }
   };
-  for (int d = 0; d < 3; ++d) mk_tw(S.K[d], &S.tw[d], &S.twf[d]);
-  mk_tw(S.K[0] / 2, &S.twh, &S.twhf);
+  for (int d = 0; d < 3; ++d) mk_tw(S.K[d], &S.tw[d], &S.twf[d], &S.tw_d[d]);
+  mk_tw(S.K[0] / 2, &S.twh, &S.twhf, &S.twh_d);
   // FP32 copies for the mixed form
   GB_CUDA(cudaMalloc(&S.Qf, sizeof(float) * NG));
   GB_CUDA(cudaMalloc(&S.Gf, sizeof(float2) * NG));
@@ -1017,6 +1034,14 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
   GB_LAUNCHED();
   k_cvt<float><<<nblocks((long long)NG, 256), 256, 0, g.stream>>>(S.psi, S.psi_f, NG);
   GB_LAUNCHED();
+  if (S.fp64) {  // double-float copies for the FP64 form
+    GB_CUDA(cudaMalloc(&S.theta_d, sizeof(dfr) * NG));
+    GB_CUDA(cudaMalloc(&S.psi_d, sizeof(dfr) * NG));
+    k_cvt<dfr><<<nblocks((long long)NG, 256), 256, 0, g.stream>>>(S.theta, S.theta_d, NG);
+    GB_LAUNCHED();
+    k_cvt<dfr><<<nblocks((long long)NG, 256), 256, 0, g.stream>>>(S.psi, S.psi_d, NG);
+    GB_LAUNCHED();
+  }
   // dynamic shared memory limits
   const int maxN = std::max(S.K[0], std::max(S.K[1], S.K[2]));
   int smem = (int)std::max(fft_smem(maxN, TX, sizeof(double2)), fft_smem(S.K[0], 8, sizeof(double2)));
@@ -1031,6 +1056,13 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
   raise_smem(k_fft_y<float, float2, +1>, smem);
   raise_smem(k_fft_y<float, float2, -1>, smem);
   raise_smem(k_fft_z_conv<float, float2>, smem);
+  if (S.fp64) {
+    raise_smem(k_fft_x_fwd<dfr, dfc>, smem);
+    raise_smem(k_fft_x_inv<dfr, dfc>, smem);
+    raise_smem(k_fft_y<dfr, dfc, +1>, smem);
+    raise_smem(k_fft_y<dfr, dfc, -1>, smem);
+    raise_smem(k_fft_z_conv<dfr, dfc>, smem);
+  }
   GB_CUDA(cudaStreamSynchronize(g.stream));
   S.ready = true;
 }
@@ -1042,7 +1074,8 @@ template <typename T, typename T2>
 void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_rc, double* stress9) {
   cudaStream_t st = g.stream;
   const int n = g.natms, p = S.p;
-  constexpr bool F64 = std::is_same<T, double>::value;
+  constexpr bool DF = std::is_same<T, dfr>::value;  // FP64 form in double-float
+  constexpr bool F64 = std::is_same<T, double>::value || DF;  // FP64-accuracy kernels and buffers
   auto pid = [coarse](int id) {
     if (!coarse) return id;
     if (id == P_SPME_PREP) return (int)P_COARSE_PREP;
@@ -1053,11 +1086,16 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   T* spl = reinterpret_cast<T*>(S.spl);
   T* Q = F64 ? reinterpret_cast<T*>(S.Q) : reinterpret_cast<T*>(S.Qf);
   T2* G = F64 ? reinterpret_cast<T2*>(S.G) : reinterpret_cast<T2*>(S.Gf);
-  const T* th = F64 ? reinterpret_cast<const T*>(S.theta) : reinterpret_cast<const T*>(S.theta_f);
-  const T* ps = F64 ? reinterpret_cast<const T*>(S.psi) : reinterpret_cast<const T*>(S.psi_f);
-  const T2* tw1 = F64 ? reinterpret_cast<const T2*>(S.tw[0]) : reinterpret_cast<const T2*>(S.twf[0]);
-  const T2* tw2 = F64 ? reinterpret_cast<const T2*>(S.tw[1]) : reinterpret_cast<const T2*>(S.twf[1]);
-  const T2* tw3 = F64 ? reinterpret_cast<const T2*>(S.tw[2]) : reinterpret_cast<const T2*>(S.twf[2]);
+  const T* th = DF ? reinterpret_cast<const T*>(S.theta_d)
+                   : (F64 ? reinterpret_cast<const T*>(S.theta) : reinterpret_cast<const T*>(S.theta_f));
+  const T* ps = DF ? reinterpret_cast<const T*>(S.psi_d)
+                   : (F64 ? reinterpret_cast<const T*>(S.psi) : reinterpret_cast<const T*>(S.psi_f));
+  const T2* tw1 = DF ? reinterpret_cast<const T2*>(S.tw_d[0])
+                     : (F64 ? reinterpret_cast<const T2*>(S.tw[0]) : reinterpret_cast<const T2*>(S.twf[0]));
+  const T2* tw2 = DF ? reinterpret_cast<const T2*>(S.tw_d[1])
+                     : (F64 ? reinterpret_cast<const T2*>(S.tw[1]) : reinterpret_cast<const T2*>(S.twf[1]));
+  const T2* tw3 = DF ? reinterpret_cast<const T2*>(S.tw_d[2])
+                     : (F64 ? reinterpret_cast<const T2*>(S.tw[2]) : reinterpret_cast<const T2*>(S.twf[2]));
   const int K1 = S.K[0], K2 = S.K[1], K3 = S.K[2];
   // splines + brick binning
   GB_CUDA(cudaMemsetAsync(S.brick_count, 0, sizeof(int) * (S.nbricks + 2), st));
@@ -1104,7 +1142,8 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   const int lines = 8;
   const int rows = K2 * K3;
   const int Kx = S.Kx, M = K1 / 2;
-  const T2* twh = F64 ? reinterpret_cast<const T2*>(S.twh) : reinterpret_cast<const T2*>(S.twhf);
+  const T2* twh = DF ? reinterpret_cast<const T2*>(S.twh_d)
+                     : (F64 ? reinterpret_cast<const T2*>(S.twh) : reinterpret_cast<const T2*>(S.twhf));
   const int ntx = (Kx + TX - 1) / TX;
   prof_begin(pid(P_FFT_XF));
   k_fft_x_fwd<T, T2><<<nblocks(rows, lines), 256, fft_smem(M, lines, sizeof(T2)), st>>>(Q, G, S.planh, twh, tw1, rows,
@@ -1193,7 +1232,8 @@ void spme_free() {
 
 void spme_forces(double* eng_rc, double* vir_rc, double* stress9) {
   float* rec = mts_rec_out();
-  if (g.precision == GB_FP64) grid_run<double, double2>(S_main, false, rec, eng_rc, vir_rc, stress9);
+  if (g.precision == GB_FP64 && g.fp64_native) grid_run<double, double2>(S_main, false, rec, eng_rc, vir_rc, stress9);
+  else if (g.precision == GB_FP64) grid_run<dfr, dfc>(S_main, false, rec, eng_rc, vir_rc, stress9);
   else grid_run<float, float2>(S_main, false, rec, eng_rc, vir_rc, stress9);
 }
 
