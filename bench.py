@@ -179,15 +179,26 @@ def kernel_work(name, s, cnt, form):
 # for a full-section capture); traffic grows with the list, so the bench scales
 # it by this launch's list entries.
 MEASURED_TRAFFIC = {
-    ("pair_forces", "fp64"): ((200.795648e6 + 3.779072e6) / 40368337,
-                              "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_fp64 on nacl_175616 "
-                              "(profiles/pair_fp64_nacl175616.md), scaled by half-list entries"),
+    ("pair_forces", "fp64"): ((202.284288e6 + 5.849856e6) / 40368337,
+                              "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_df64 on nacl_175616 "
+                              "(profiles/pair_df64_nacl175616.md), scaled by half-list entries"),
     ("pair_forces", "mixed"): ((200.9e6 + 5.2e6) / 40368337,
                                "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_mixed_half on nacl_175616 "
                                "(profiles/pair_mixed_nacl175616.md), scaled by half-list entries"),
     ("metal_forces", "fp64"): ((131.494144e6 + 4.494848e6) / 19246179,
                                "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_metal_forces on eam_256000 "
                                "(profiles/metal_kernels_eam256000.md), scaled by half-list entries"),
+}
+
+
+# Warp instructions executed per half-list entry by the double-float pair kernel (ncu
+# smsp__inst_executed.sum of one launch on the 175,616-ion melt over its list
+# entries).  That kernel runs on the FP32/ALU pipes and is bound by instruction
+# issue, so its roofline is issue slots: 4 warp instructions per clock per SM.
+MEASURED_INST = {
+    ("pair_forces", "fp64"): (967896482 / 40368337,
+                              "ncu smsp__inst_executed.sum of k_pair_df64 on nacl_175616 "
+                              "(profiles/pair_df64_nacl175616.md), scaled by half-list entries"),
 }
 
 
@@ -449,7 +460,30 @@ def run_gb(args, dist):
     if dom and kernel_work(dom, s, (P_list, P_rc), args.form):
         fl, by = kernel_work(dom, s, (P_list, P_rc), args.form)
         sec = prof[dom][0] / prof[dom][1] * 1e-3
-        if args.form == "fp64" and fp64_peak and fp64_peak > 0 and fl / by > fp64_peak * 1e3 / (hbm or 6751.1):
+        inst = MEASURED_INST.get((dom, args.form)) if precision == 0 else None
+        fp64_view = None
+        if args.form == "fp64" and fp64_peak and fp64_peak > 0:
+            fp64_view = {"achieved": fl / sec / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": fl / sec / 1e12 / fp64_peak,
+                         "peak_source": "FP64 DFMA loop measured in this run"}
+        if inst:
+            try:
+                import torch
+                nsm = torch.cuda.get_device_properties(device).multi_processor_count
+            except Exception:  # noqa: BLE001
+                nsm = 152
+            mhz = (clk or {}).get("sm_mhz") or 2070.0
+            peak_i = nsm * 4 * mhz * 1e6 / 1e9
+            ach_i = inst[0] * P_list / sec / 1e9
+            roof = {"bound": "issue", "kernel": dom, "achieved": ach_i, "peak": peak_i, "unit": "Gwarp-inst/s",
+                    "frac": ach_i / peak_i, "traffic": None,
+                    "peak_source": f"4 warp instructions per clock per SM x {nsm} SMs x {mhz:.0f} MHz "
+                                   "(median SM clock sampled in the timed region)",
+                    "inst_source": inst[1],
+                    "fp64_view": fp64_view,
+                    "hbm_view": {"achieved": by / sec / 1e9, "peak": hbm, "unit": "GB/s",
+                                 "frac": (by / sec / 1e9) / hbm if hbm else None}}
+        elif args.form == "fp64" and fp64_peak and fp64_peak > 0 and fl / by > fp64_peak * 1e3 / (hbm or 6751.1):
             roof = {"bound": "fp64", "kernel": dom, "achieved": fl / sec / 1e12, "peak": fp64_peak,
                     "unit": "TFLOP/s", "frac": fl / sec / 1e12 / fp64_peak, "traffic": None,
                     "peak_source": "FP64 DFMA loop measured in this run (MEASURED_PEAKS.json has no FP64 figure)",

@@ -38,7 +38,7 @@ __device__ __forceinline__ dfr operator/(dfr a, dfr b) {
 }
 
 // a * b + c
-__device__ __forceinline__ dfr fma(dfr a, dfr b, dfr c) { return to_dfr(df_add(df_mul(to_df(a), to_df(b)), to_df(c))); }
+__device__ __forceinline__ dfr fma(dfr a, dfr b, dfr c) { return to_dfr(df_fma(to_df(a), to_df(b), to_df(c))); }
 
 __device__ __forceinline__ bool nonzero_bits(dfr v) { return (__float_as_uint(v.hi) << 1) != 0u; }
 
@@ -46,13 +46,36 @@ struct dfc {
   dfr x, y;
 };
 
-// block sums of double-float values, as doubles
+__device__ __forceinline__ dfr shfl_xor_dfr(dfr v, int o) {
+  return dfr(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+
+// block sums of double-float values: reduced in double-float (no FP64 instruction per
+// thread), one thread converts the NV block totals to FP64
 template <int NV>
 __device__ __forceinline__ void block_reduce_store(dfr (&v)[NV], double* out) {
-  double d[NV];
+  __shared__ dfr redd[32][NV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < NV; ++k) d[k] = (double)v[k];
-  block_reduce_store<NV>(d, out);
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] += shfl_xor_dfr(v[k], o);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) redd[wid][k] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      dfr t = lane < nw ? redd[lane][k] : dfr();
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += shfl_xor_dfr(t, o);
+      if (lane == 0) out[(size_t)blockIdx.x * NV + k] = (double)t;
+    }
+  }
 }
 
 #endif

@@ -22,6 +22,7 @@
 
 #include "gb_common.cuh"
 #include "gb_df64.cuh"
+#include "gb_dfr.cuh"
 
 namespace {
 
@@ -444,8 +445,8 @@ void pair_setup() {
 // throughout (near the repulsive wall of a 12-6 table the quadratic term reaches 1e-3 of
 // the value, so it needs the full precision too)
 __device__ __forceinline__ df poly_df(float4 c01, float c2h, float c2l, df d) {
-  const df t = df_add(df_make(c01.z, c01.w), df_mul(d, df_make(c2h, c2l)));
-  return df_add(df_make(c01.x, c01.y), df_mul(d, t));
+  const df t = df_fma(d, df_make(c2h, c2l), df_make(c01.z, c01.w));
+  return df_fma(d, t, df_make(c01.x, c01.y));
 }
 
 // FP64 terms of one pair, as k_pair_fp64 evaluates them (slow path)
@@ -648,9 +649,9 @@ __global__ void __launch_bounds__(256, 3) k_pair_df64(int natms, const DevScalar
       n_list += (unsigned long long)n;
     }
   }
-  double out[NACC];
+  dfr out[NACC];
 #pragma unroll
-  for (int k = 0; k < NACC; ++k) out[k] = dacc_value(acc[k]);
+  for (int k = 0; k < NACC; ++k) out[k] = to_dfr(two_sum(acc[k].s, acc[k].c));
   n_rc = (unsigned long long)warp_sumi((int)n_rc);
   if (lane == 0) {
     atomicAdd(&cnt[0], n_list);

@@ -159,7 +159,7 @@ __device__ __forceinline__ void bspline_vals(T w, int p_rt, T* m /*p*/, T* dm /*
   // raise from order 2 to order p-1
 #pragma unroll
   for (int n = 3; n <= p - 1; ++n) {
-    const T rn = (T)1 / (T)(n - 1);
+    const T rn = T(1.0 / (double)(n - 1));
 #pragma unroll
     for (int j = p - n + 1; j <= p - 1; ++j) {
       const T pt = w + (T)(p - j);
@@ -174,7 +174,7 @@ __device__ __forceinline__ void bspline_vals(T w, int p_rt, T* m /*p*/, T* dm /*
   }
   {
     const int n = p;
-    const T rn = (T)1 / (T)(n - 1);
+    const T rn = T(1.0 / (double)(n - 1));
 #pragma unroll
     for (int j = 1; j <= p - 1; ++j) {
       const T pt = w + (T)(p - j);
@@ -189,14 +189,22 @@ __device__ __forceinline__ void bspline_vals(T w, int p_rt, T* m /*p*/, T* dm /*
 
 struct SpmeGeom {
   double rc[9];
+  float rch[9], rcl[9];  // rc as double-floats
   double Kr[3];
   int K[3], B[3], nb[3], p;
 };
 
+// a reciprocal-cell entry in the working precision (double-floats from the stored split)
+template <typename T>
+__device__ __forceinline__ T rc_at(const SpmeGeom& sg, int k) { return (T)sg.rc[k]; }
+template <>
+__device__ __forceinline__ dfr rc_at<dfr>(const SpmeGeom& sg, int k) { return dfr(sg.rch[k], sg.rcl[k]); }
+
 template <typename T, int P>
 __global__ void k_spme_prep(int natms, const double* __restrict__ x, const double* __restrict__ y,
                             const double* __restrict__ z, const double* __restrict__ q, SpmeGeom sg, T* spl,
-                            int* nidx, int* brick_of, int* brick_count, int* gidx, float* gw) {
+                            int* nidx, int* brick_of, int* brick_count, int* gidx, float* gw, float* gwl,
+                            float2* gq) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natms) return;
   const int p = P ? P : sg.p;
@@ -212,12 +220,21 @@ __global__ void k_spme_prep(int natms, const double* __restrict__ x, const doubl
       int g0 = ((int)tr - p + 1) % sg.K[d];
       if (g0 < 0) g0 += sg.K[d];
       gidx[3 * i + d] = g0;
-      gw[3 * i + d] = (float)(u - tr);
+      // u - tr is exact; the double-float gather also takes its low part
+      if (gwl) df_split(u - tr, &gw[3 * i + d], &gwl[3 * i + d]);
+      else gw[3 * i + d] = (float)(u - tr);
     }
     T m[PMAX];
     bspline_vals<T, P>(w, p, m, nullptr);
+    // the z splines carry the charge: the spreads weight a point by Mx (My (Mz q))
+    if (d == 2) {
+      const T qT = (T)q[i];
 #pragma unroll
-    for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t];
+      for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t] * qT;
+    } else {
+#pragma unroll
+      for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t];
+    }
     int nw = n % sg.K[d];
     if (nw < 0) nw += sg.K[d];
     nidx[3 * i + d] = nw;
@@ -225,6 +242,11 @@ __global__ void k_spme_prep(int natms, const double* __restrict__ x, const doubl
   }
   int b = bidx[0] + sg.nb[0] * (bidx[1] + sg.nb[1] * bidx[2]);
   if (fabs(q[i]) <= DBL_MIN) b = -1;
+  if (gq) {  // double-float gather: the charge, zero for atoms that take no part
+    float h = 0.f, l = 0.f;
+    if (b >= 0) df_split(q[i], &h, &l);
+    gq[i] = make_float2(h, l);
+  }
   brick_of[i] = b;
   if (b >= 0) atomicAdd(&brick_count[b], 1);
 }
@@ -251,13 +273,17 @@ __global__ void k_brick_sort(int nbricks, const int* start, const int* tmp, int*
 
 // ------------------------------------------------------------- spreading
 constexpr int SPREAD_CH = 32;
+constexpr int SPREAD_NT = 512;             // threads of a tile-spread CTA
+constexpr int SPREAD_NW = SPREAD_NT / 32;  // its warps (a power of two: plane owner = z & (NW - 1))
 constexpr int BMAX = 16;
 
 // Tile scatter: CTA = one brick and the atoms whose floor(u) lies in it.  The
 // CTA owns a (B+p-1)^3 shared-memory tile covering the brick plus the p-1
 // points below it that its atoms reach; atoms are scattered one after another
-// (one FMA per grid point, all lanes busy, no atomics), then the tile is
-// written to its own slot of `ext` for the halo reduction below.
+// (one FMA per grid point, no atomics; each warp owns every nw-th z plane of the
+// tile, so a chunk of atoms needs one barrier; launched with SPREAD_NT threads),
+// then the tile is written to its
+// own slot of `ext` for the halo reduction below.
 template <typename T, int P>
 __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, const int* __restrict__ batoms,
                                    const T* __restrict__ spl, const int* __restrict__ nidx,
@@ -275,7 +301,8 @@ __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, 
   int* off = reinterpret_cast<int*>(Mx + SPREAD_CH * p);  // [SPREAD_CH][3] tile offsets
   for (int e = threadIdx.x; e < tsize; e += blockDim.x) tile[e] = (T)0;
   const int s0 = bstart[b], s1 = bstart[b + 1];
-  const int p2 = p * p, p3 = p2 * p;
+  const int p2 = p * p;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int c = s0; c < s1; c += SPREAD_CH) {
     const int nc = min(SPREAD_CH, s1 - c);
     __syncthreads();
@@ -292,17 +319,22 @@ __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, 
     for (int e = threadIdx.x; e < nc * p2; e += blockDim.x) {
       const int a = e / p2, kl = e - a * p2, k = kl % p, l = kl / p;
       const int i = batoms[c + a];
-      Pkl[a * p2 + kl] = spl[((size_t)i * 3 + 1) * p + k] * (spl[((size_t)i * 3 + 2) * p + l] * (T)q[i]);
+      Pkl[a * p2 + kl] = spl[((size_t)i * 3 + 1) * p + k] * spl[((size_t)i * 3 + 2) * p + l];  // My (Mz q)
     }
     __syncthreads();
+    // tile plane z belongs to warp z mod NW: a point is only ever written by one warp, in
+    // atom order, so the warps run through the chunk without a barrier per atom
     for (int a = 0; a < nc; ++a) {
       const int ox = off[a * 3], oy = off[a * 3 + 1], oz = off[a * 3 + 2];
-      for (int e = threadIdx.x; e < p3; e += blockDim.x) {
-        const int j = e % p, kl = e / p, k = kl % p, l = kl / p;
-        T* dst = tile + ((oz + l) * TYd + (oy + k)) * TXd + (ox + j);
-        *dst = fma(Mx[a * p + j], Pkl[a * p2 + kl], *dst);
+      for (int l = (wid - oz) & (SPREAD_NW - 1); l < p; l += SPREAD_NW) {
+        T* plane = tile + (oz + l) * TYd * TXd;
+        for (int kj = lane; kj < p2; kj += 32) {
+          const int j = kj % p, k = kj / p;
+          T* dst = plane + (oy + k) * TXd + (ox + j);
+          *dst = fma(Mx[a * p + j], Pkl[a * p2 + l * p + k], *dst);
+        }
       }
-      __syncthreads();
+      __syncwarp();
     }
   }
   __syncthreads();
@@ -336,11 +368,10 @@ __global__ void k_spme_spread_fix(SpmeGeom sg, const int* __restrict__ bstart, c
     const float* sx = spl + ((size_t)i * 3 + 0) * p;
     const float* sy = sx + p;
     const float* sz = sy + p;
-    const float qi = (float)q[i];
     const int ox = nidx[3 * i] - g0x, oy = nidx[3 * i + 1] - g0y, oz = nidx[3 * i + 2] - g0z;
     for (int e = lane; e < p3; e += 32) {
       const int j = e % p, kl = e / p, k = kl % p, l = kl / p;
-      const float w = sx[j] * (sy[k] * (sz[l] * qi));
+      const float w = sx[j] * (sy[k] * sz[l]);  // sz carries q
       atomicAdd((unsigned long long*)&tile[((oz + l) * TYd + (oy + k)) * TXd + (ox + j)],
                 (unsigned long long)fix40(w));
     }
@@ -536,7 +567,7 @@ __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan
   T* rzt = reinterpret_cast<T*>(b + TX * pl.N);
   for (int zz = threadIdx.x; zz < K3; zz += blockDim.x) {
     int ll = zz; if (2 * ll > K3) ll -= K3;
-    rzt[zz] = (T)ll * (T)sg.rc[8];
+    rzt[zz] = (T)ll * rc_at<T>(sg, 8);
   }
   T2* r = fft_lines<T, T2, +1>(a, b, pl, TX, tw);
   // Reciprocal stress sum_m m_a m_b psi |Q(m)|^2 (ewald_spole.F90:1362-1371): with
@@ -578,7 +609,7 @@ __global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan
     const int jx = x0 + t;
     int jj = jx; if (2 * jj > K1) jj -= K1;
     int kk = yy; if (2 * kk > K2) kk -= K2;
-    const T rx = (T)jj * (T)sg.rc[0], ry = (T)kk * (T)sg.rc[4];
+    const T rx = (T)jj * rc_at<T>(sg, 0), ry = (T)kk * rc_at<T>(sg, 4);
     if (jx == 0 || 2 * jx == K1) {  // the line holds its own mirror: the full-spectrum sums
       const T Ball = B + Bn;
       st[0] = rx * rx * A; st[1] = rx * ry * A; st[2] = rx * Ball;
@@ -727,6 +758,119 @@ __global__ void __launch_bounds__(256) k_spme_gather_f32(int natms, const float*
   block_reduce_store<4>(acc, blk);
 }
 
+// FP64 form, the same warp-per-atom layout in double-float.  A warp takes 8 atoms at a
+// time: 24 lanes build the splines of the 8 atoms x 3 dimensions in parallel, then the
+// warp gathers the atoms one after another.  Lane pr = (j, k) of the p x p (x, y) rows
+// sums its z column against Mz and dMz, then weights the two sums with its x/y spline
+// products (separable in z, so 2 products per grid point); the four per-atom sums are
+// combined by a reduce-scatter over the warp (two values after the first butterfly
+// level, one after the second), which leaves the energy sum in lane 0 and the x, y, z
+// force sums in lanes 8, 16, 24.  No FP64 instruction: forces leave as double-floats.
+constexpr int GATHER_AB = 8;  // atoms per warp batch
+
+template <int P>
+__global__ void __launch_bounds__(256) k_spme_gather_wdf(int natms, SpmeGeom sg, const int* __restrict__ gidx,
+                                                         const float* __restrict__ gw, const float* __restrict__ gwl,
+                                                         const float2* __restrict__ gq, const dfr* __restrict__ phi,
+                                                         float2 rk0, float2 rk1, float2 rk2,
+                                                         float2* __restrict__ fout, double* blk) {
+  __shared__ dfr sp[8][GATHER_AB][2][3][P];  // per warp and atom: value/derivative, dimension, point
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
+  dacc acc[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) { acc[c].s = 0.f; acc[c].c = 0.f; }
+  for (int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * GATHER_AB; base < natms;
+       base += nwarps * GATHER_AB) {
+    if (lane < 3 * GATHER_AB) {
+      const int a = lane / 3, d = lane - 3 * a, i = base + a;
+      if (i < natms) {
+        dfr m[PMAX], dm[PMAX];
+        bspline_vals<dfr, P>(dfr(gw[3 * i + d], gwl[3 * i + d]), P, m, dm);
+#pragma unroll
+        for (int t = 0; t < P; ++t) { sp[wid][a][0][d][t] = m[t]; sp[wid][a][1][d][t] = dm[t]; }
+      }
+    }
+    __syncwarp();
+    const int na = min(GATHER_AB, natms - base);
+    for (int a = 0; a < na; ++a) {
+      const int i = base + a;
+      const float2 qv = gq[i];
+      if (qv.x == 0.f) {  // uniform over the warp
+        if (lane < 3) fout[3 * i + lane] = make_float2(0.f, 0.f);
+        continue;
+      }
+      const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
+      dfr v[4];  // energy, x, y, z sums
+#pragma unroll
+      for (int pr = lane; pr < P * P; pr += 32) {
+        const int j = pr % P, k = pr / P;
+        int xx = gx + j; if (xx >= K0) xx -= K0;
+        int yy = gy + k; if (yy >= K1) yy -= K1;
+        const dfr* col = phi + (size_t)yy * K0 + xx;
+        dfr ca, cc;
+#pragma unroll
+        for (int l = 0; l < P; ++l) {
+          int zz = gz + l; if (zz >= K2) zz -= K2;
+          const dfr ph = col[(size_t)zz * K1 * K0];
+          ca = fma(sp[wid][a][0][2][l], ph, ca);
+          cc = fma(sp[wid][a][1][2][l], ph, cc);
+        }
+        const dfr mx = sp[wid][a][0][0][j], dmx = sp[wid][a][1][0][j];
+        const dfr my = sp[wid][a][0][1][k], dmy = sp[wid][a][1][1][k];
+        const dfr w0 = mx * my;
+        v[0] = fma(w0, ca, v[0]);
+        v[1] = fma(dmx * my, ca, v[1]);
+        v[2] = fma(mx * dmy, ca, v[2]);
+        v[3] = fma(w0, cc, v[3]);
+      }
+      // reduce-scatter: level 16 keeps (v0, v1) in the lower half-warp, (v2, v3) in the upper
+      const bool up16 = lane & 16, up8 = lane & 8;
+      dfr k0 = up16 ? v[2] : v[0], k1 = up16 ? v[3] : v[1];
+      const dfr s0 = up16 ? v[0] : v[2], s1 = up16 ? v[1] : v[3];
+      k0 += dfr(__shfl_xor_sync(0xffffffffu, s0.hi, 16), __shfl_xor_sync(0xffffffffu, s0.lo, 16));
+      k1 += dfr(__shfl_xor_sync(0xffffffffu, s1.hi, 16), __shfl_xor_sync(0xffffffffu, s1.lo, 16));
+      dfr r = up8 ? k1 : k0;
+      const dfr sr = up8 ? k0 : k1;
+      r += dfr(__shfl_xor_sync(0xffffffffu, sr.hi, 8), __shfl_xor_sync(0xffffffffu, sr.lo, 8));
+#pragma unroll
+      for (int o = 4; o > 0; o >>= 1)
+        r += dfr(__shfl_xor_sync(0xffffffffu, r.hi, o), __shfl_xor_sync(0xffffffffu, r.lo, o));
+      // lane 0: energy; lanes 8, 16, 24: x, y, z
+      if ((lane & 7) == 0) {
+        const int comp = lane >> 3;
+        const dfr qr = dfr(qv.x, qv.y) * r;
+        if (comp == 0) {
+          dacc_add(acc[0], to_df(qr));
+        } else {
+          const float2 rk = comp == 1 ? rk0 : (comp == 2 ? rk1 : rk2);
+          const dfr f = -(qr * dfr(rk.x, rk.y));
+          fout[3 * i + comp - 1] = make_float2(f.hi, f.lo);
+          dacc_add(acc[comp], to_df(f));
+        }
+      }
+    }
+    __syncwarp();  // the batch's splines are read before the next batch writes them
+  }
+  dfr out[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) out[c] = to_dfr(two_sum(acc[c].s, acc[c].c));
+  block_reduce_store<4>(out, blk);
+}
+
+// FP64 form with the double-float gather: forces += (F - Fnet/N) * 2 * scale
+__global__ void k_spme_apply_df(int natms, const float2* __restrict__ f, const double* __restrict__ sums,
+                                double scale2, double rn, double* fx, double* fy, double* fz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natms) return;
+  const double m0 = sums[1] * rn, m1 = sums[2] * rn, m2 = sums[3] * rn;
+  const float2 a = f[3 * i], b = f[3 * i + 1], c = f[3 * i + 2];
+  fx[i] += (((double)a.x + (double)a.y) - m0) * scale2;
+  fy[i] += (((double)b.x + (double)b.y) - m1) * scale2;
+  fz[i] += (((double)c.x + (double)c.y) - m2) * scale2;
+}
+
 // mixed form: forces += (F - Fnet/N) * 2 * scale as 2^40 fixed point (FP32 math)
 __global__ void k_spme_apply_fix_f32(int natms, const float* __restrict__ f, const double* __restrict__ sums,
                                      float scale2, float rn, unsigned long long* fixp, float* rec) {
@@ -816,7 +960,8 @@ struct SpmeGrid {
   double* fspme = nullptr;     // 3*natms reciprocal forces (before scale, net removal)
   void* spread_ext = nullptr;  // per-brick spread tiles (nbricks x (B+p-1)^3)
   int* gidx = nullptr;         // warp gather: first grid index per dimension (truncation convention)
-  float* gw = nullptr;         // warp gather: fractional coordinate per dimension
+  float* gw = nullptr;         // warp gather: fractional coordinate per dimension (3n), then its low parts (3n),
+                               // then the double-float charges (2n)
   float* fout_f = nullptr;     // warp gather: unscaled reciprocal forces
   // double-float copies for the FP64 form (main grid): influence function, stress
   // factor and twiddles; the grids themselves reuse the FP64 buffers (same sizes)
@@ -892,6 +1037,7 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
   S.nbricks = S.nb[0] * S.nb[1] * S.nb[2];
   double det;
   invert_host(g.cell, S.sg.rc, &det);
+  for (int k = 0; k < 9; ++k) df_split(S.sg.rc[k], &S.sg.rch[k], &S.sg.rcl[k]);
   for (int d = 0; d < 3; ++d) {
     S.sg.K[d] = S.K[d];
     S.sg.Kr[d] = (double)S.K[d];
@@ -916,7 +1062,7 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
   }
   GB_CUDA(cudaMalloc(&S.fspme, sizeof(double) * 3 * n));
   GB_CUDA(cudaMalloc(&S.gidx, sizeof(int) * 3 * n));
-  GB_CUDA(cudaMalloc(&S.gw, sizeof(float) * 3 * n));
+  GB_CUDA(cudaMalloc(&S.gw, sizeof(float) * 8 * n));
   GB_CUDA(cudaMalloc(&S.fout_f, sizeof(float) * 3 * n));
   {
     const size_t tsize = (size_t)(S.B[0] + p - 1) * (S.B[1] + p - 1) * (S.B[2] + p - 1);
@@ -1101,10 +1247,12 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   GB_CUDA(cudaMemsetAsync(S.brick_count, 0, sizeof(int) * (S.nbricks + 2), st));
   GB_CUDA(cudaMemsetAsync(S.brick_fill, 0, sizeof(int) * (S.nbricks + 2), st));
   prof_begin(pid(P_SPME_PREP));
-  const bool warp_gather = !F64 && (p == 8 || p == 6);
+  const bool warp_gather = (!F64 || DF) && (p == 8 || p == 6);
   auto prep = p == 8 ? k_spme_prep<T, 8> : (p == 6 ? k_spme_prep<T, 6> : k_spme_prep<T, 0>);
   prep<<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, spl, S.nidx, S.brick_of, S.brick_count,
-                                         warp_gather ? S.gidx : nullptr, warp_gather ? S.gw : nullptr);
+                                         warp_gather ? S.gidx : nullptr, warp_gather ? S.gw : nullptr,
+                                         warp_gather && DF ? S.gw + 3 * (size_t)n : nullptr,
+                                         warp_gather && DF ? reinterpret_cast<float2*>(S.gw + 6 * (size_t)n) : nullptr);
   GB_LAUNCHED();
 
   scan_exclusive(S.brick_count, S.brick_start, S.nbricks + 1);
@@ -1122,7 +1270,7 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
     prof_begin(pid(P_SPME_SPREAD));
     if (F64) {
       auto spread = p == 8 ? k_spme_spread_tile<T, 8> : k_spme_spread_tile<T, 0>;
-      spread<<<S.nbricks, 512, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge, ext);
+      spread<<<S.nbricks, SPREAD_NT, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge, ext);
       GB_LAUNCHED();
       k_spme_tile_reduce<T><<<nblocks((long long)NG, 256), 256, 0, st>>>(S.sg, ext, Q);
       GB_LAUNCHED();
@@ -1177,10 +1325,21 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   for (int a = 0; a < 3; ++a) rk[a] = rc[a] * S.sg.Kr[0] + rc[a + 3] * S.sg.Kr[1] + rc[a + 6] * S.sg.Kr[2];
   static int occ_g = 0;
   if (!occ_g) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g, k_spme_gather_f32<8>, 256, 0));
-  const int nbg = warp_gather ? std::max(1, std::min(occ_g * g.nsm, nblocks((long long)n * 32, 256))) : nblocks(n, 128);
+  static int occ_gd = 0;
+  if (DF && !occ_gd) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_gd, k_spme_gather_wdf<8>, 256, 0));
+  const int nbg = warp_gather ? std::max(1, std::min((DF ? occ_gd : occ_g) * g.nsm,
+                                                     nblocks((long long)n * 32 / (DF ? GATHER_AB : 1), 256)))
+                              : nblocks(n, 128);
   double* blkg = blkz + (size_t)nbz * 6;
   prof_begin(pid(P_SPME_GATHER));
-  if (warp_gather) {
+  if (warp_gather && DF) {
+    auto kern = p == 8 ? k_spme_gather_wdf<8> : k_spme_gather_wdf<6>;
+    float2 rkd[3];
+    for (int a = 0; a < 3; ++a) df_split(rk[a], &rkd[a].x, &rkd[a].y);
+    kern<<<nbg, 256, 0, st>>>(n, S.sg, S.gidx, S.gw, S.gw + 3 * (size_t)n,
+                              reinterpret_cast<const float2*>(S.gw + 6 * (size_t)n), reinterpret_cast<const dfr*>(Q),
+                              rkd[0], rkd[1], rkd[2], reinterpret_cast<float2*>(S.fspme), blkg);
+  } else if (warp_gather) {
     auto kern = p == 8 ? k_spme_gather_f32<8> : k_spme_gather_f32<6>;
     kern<<<nbg, 256, 0, st>>>(n, reinterpret_cast<const float*>(g.xf), S.sg, S.gidx, S.gw,
                               reinterpret_cast<const float*>(Q), (float)rk[0], (float)rk[1], (float)rk[2], S.fout_f,
@@ -1197,7 +1356,11 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   const double scale = pi * std::sqrt(pi) * std::pow(g.p.alpha, 1 - 3) * (0.5 / g.volm) * g.scaling;
   unsigned long long* fixp = coarse ? nullptr : (unsigned long long*)g.fixp;
   prof_begin(pid(P_SPME_GATHER));
-  if (F64) {
+  if (DF && warp_gather) {
+    k_spme_apply_df<<<nblocks(n, 256), 256, 0, st>>>(n, reinterpret_cast<const float2*>(S.fspme),
+                                                      &g.sc->acc[A_GATHER], 2.0 * scale, 1.0 / (double)n, g.fx, g.fy,
+                                                      g.fz);
+  } else if (F64) {
     k_spme_apply<<<nblocks(n, 256), 256, 0, st>>>(n, S.fspme, &g.sc->acc[A_GATHER], 2.0 * scale, 1.0 / (double)n,
                                                    g.fx, g.fy, g.fz);
   } else if (warp_gather) {

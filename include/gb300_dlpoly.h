@@ -48,9 +48,9 @@ extern "C" {
 #define GB_ERR_RNG (-7)        /* a Gaussian deviate's rejection loop hit its iteration cap */
 
 /* Precision forms of the force path. */
-#define GB_FP64 0   /* plain: FP64 accuracy; the pair loop in double-float (FP32 pairs) */
+#define GB_FP64 0   /* plain: FP64 accuracy; pair loop and SPME in double-float (pairs of FP32) */
 #define GB_MIXED 1  /* FP32 pair/spline/FFT arithmetic, int64 fixed-point forces (2^40) */
-#define GB_FP64_NATIVE 2  /* the FP64 form with every pair evaluated in native FP64 */
+#define GB_FP64_NATIVE 2  /* the FP64 form with the pair loop and SPME in native FP64 */
 
 /* Ensembles of the VV stages (thermo%ensemble, drivers.F90:1132-1175) */
 #define GB_NVE 0              /* nve_0_vv */
@@ -80,7 +80,7 @@ typedef struct gb_params {
   int32_t max_list;     /* neigh%max_list */
   int32_t max_exclude;  /* neigh%max_exclude */
   int32_t mxatms;       /* config%mxatms: capacity for local + halo atoms */
-  int32_t precision;    /* GB_FP64 or GB_MIXED */
+  int32_t precision;    /* GB_FP64, GB_MIXED or GB_FP64_NATIVE */
   int32_t ntypes;       /* sites%ntype_atom */
   int32_t device;       /* CUDA device ordinal this context uses (one GPU per process) */
   int32_t reserved[6];
@@ -275,7 +275,7 @@ int gb_mlp_train_eval(int nb, const float* x, const float* target, const float* 
                       float* grad, float* y);
 int gb_mlp_infer_eval(int nb, const float* x, const float* params, float* y);
 
-/* Switch the force path between GB_FP64 and GB_MIXED after gb_init. */
+/* Switch the force path between GB_FP64, GB_MIXED and GB_FP64_NATIVE after gb_init. */
 int gb_set_precision(int precision);
 
 /* Device time (ms) of the last gb_md_run per region, CUDA events on the
