@@ -179,8 +179,8 @@ def kernel_work(name, s, cnt, form):
 # for a full-section capture); traffic grows with the list, so the bench scales
 # it by this launch's list entries.
 MEASURED_TRAFFIC = {
-    ("pair_forces", "fp64"): ((202.284288e6 + 5.849856e6) / 40368337,
-                              "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_df64 on nacl_175616 "
+    ("pair_forces", "fp64"): (207.98e6 / 40368337,
+                              "ncu dram__bytes.sum (rate x duration) of k_pair_df64 on nacl_175616 "
                               "(profiles/pair_df64_nacl175616.md), scaled by half-list entries"),
     ("pair_forces", "mixed"): ((200.9e6 + 5.2e6) / 40368337,
                                "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_mixed_half on nacl_175616 "
@@ -196,7 +196,7 @@ MEASURED_TRAFFIC = {
 # entries).  That kernel runs on the FP32/ALU pipes and is bound by instruction
 # issue, so its roofline is issue slots: 4 warp instructions per clock per SM.
 MEASURED_INST = {
-    ("pair_forces", "fp64"): (967896482 / 40368337,
+    ("pair_forces", "fp64"): (801187277 / 40368337,
                               "ncu smsp__inst_executed.sum of k_pair_df64 on nacl_175616 "
                               "(profiles/pair_df64_nacl175616.md), scaled by half-list entries"),
 }

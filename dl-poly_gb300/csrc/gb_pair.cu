@@ -516,7 +516,99 @@ __device__ __forceinline__ int table_coord(df rrr, float sh, float sl, df* d) {
   return k;
 }
 
-__global__ void __launch_bounds__(256, 3) k_pair_df64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
+// per-warp queue of pairs inside the outer cutoff: neighbour index and double-float r^2
+struct PairQueue {
+  int j[64];
+  float rh[64], rl[64];
+};
+constexpr int PAIR_DF_NT = 256;  // threads of a k_pair_df64 CTA
+
+// the pair terms of one queued pair (ewald_spole.F90:131-176, vdw.F90:1881-1962), its
+// fixed-point forces and the running energy, virial and stress sums
+__device__ __forceinline__ void pair_terms_df64(const PairGeom& pg, int i, int j, int jf, int ai, int aj, df qi,
+                                                bool qi_on, float2 qj2, df dx, df dy, df dz, df rsq,
+                                                const double* __restrict__ x, const double* __restrict__ y,
+                                                const double* __restrict__ z, const double* __restrict__ q,
+                                                const float4* __restrict__ etab, const float4* __restrict__ vtab,
+                                                const double* __restrict__ ecoef, const double* __restrict__ vcoef,
+                                                const int* __restrict__ vkind, const double* __restrict__ veps,
+                                                const double* __restrict__ vsig, int vstride,
+                                                unsigned long long* fixp, dacc (&acc)[NACC], long long& sx,
+                                                long long& sy, long long& sz, unsigned long long& n_rc) {
+  const bool band = (rsq.hi >= pg.f_rc2_lo && rsq.hi <= pg.f_rc2_hi) ||
+                    (rsq.hi >= pg.f_rv2_lo && rsq.hi <= pg.f_rv2_hi);
+  const bool in_c = qi_on && qj2.x != 0.0f && rsq.hi < pg.f_rc2_lo;
+  int key = -1;
+  if (rsq.hi < pg.f_rv2_lo) {
+    key = vkey(ai, aj) - 1;
+    if (vkind[key] == 0) key = -1;
+  }
+  df gam = df_make(0.f, 0.f), ee = gam, ev = gam, gvc = gam, gvv = gam;
+  bool slow = band;
+  if (!slow && (in_c || key >= 0)) {
+    const df rinv = df_rsqrt(rsq);
+    const df rrr = df_mul(rsq, rinv);
+    df d;
+    const int k = table_coord(rrr, pg.erdr_hi, pg.erdr_lo, &d);
+    int kv = k;
+    df dv = d;
+    if (!pg.same_grid && key >= 0) kv = table_coord(rrr, pg.vrdr_hi, pg.vrdr_lo, &dv);
+    if (k == 0 || (key >= 0 && kv == 0)) {
+      slow = true;  // first interval: the exact three-point formula, in FP64
+    } else {
+      if (in_c) {  // real-space Coulomb
+        const float4* c = etab + (size_t)k * 3;
+        const float4 e01 = c[0], d01 = c[1], c2 = c[2];
+        const df pre = df_mul(qi, df_make(qj2.x, qj2.y));
+        gvc = df_mul(pre, poly_df(d01, c2.z, c2.w, d));
+        ee = df_mul(pre, poly_df(e01, c2.x, c2.y, d));
+        gam = gvc;
+      }
+      if (key >= 0) {  // van der Waals, tabulated
+        const df r_rsq = df_sqr(rinv);
+        if (pg.vdw_direct) {
+          slow = true;
+        } else {
+          const float4* c = vtab + (size_t)key * vstride + (size_t)kv * 3;
+          const float4 f01 = c[0], v01 = c[1], c2 = c[2];
+          gvv = df_mul(poly_df(f01, c2.x, c2.y, dv), r_rsq);
+          ev = poly_df(v01, c2.z, c2.w, dv);
+          gam = df_add(gam, gvv);
+        }
+      }
+    }
+  }
+  if (slow) {
+    double g64, e64c, e64v, gc64, gv64;
+    bool any;
+    pair_terms_fp64(pg, x[i] - x[j], y[i] - y[j], z[i] - z[j], q[i] * pg.scaling, q[j], ai, aj, ecoef, vcoef,
+                    vkind, veps, vsig, &g64, &e64c, &e64v, &gc64, &gv64, &any);
+    if (!any) return;
+    float h, l;
+    df_split(g64, &h, &l); gam = df_make(h, l);
+    df_split(e64c, &h, &l); ee = df_make(h, l);
+    df_split(e64v, &h, &l); ev = df_make(h, l);
+    df_split(gc64, &h, &l); gvc = df_make(h, l);
+    df_split(gv64, &h, &l); gvv = df_make(h, l);
+  } else if (!in_c && key < 0) {
+    return;
+  }
+  ++n_rc;
+  const df fxx = df_mul(gam, dx), fyy = df_mul(gam, dy), fzz = df_mul(gam, dz);
+  const long long ix = fix40_df(fxx), iy = fix40_df(fyy), iz = fix40_df(fzz);
+  sx += ix; sy += iy; sz += iz;
+  atomicAdd(&fixp[3 * jf + 0], (unsigned long long)(-ix));
+  atomicAdd(&fixp[3 * jf + 1], (unsigned long long)(-iy));
+  atomicAdd(&fixp[3 * jf + 2], (unsigned long long)(-iz));
+  dacc_add(acc[0], ev);
+  dacc_add(acc[1], df_neg(df_mul(gvv, rsq)));
+  dacc_add(acc[2], ee);
+  dacc_add(acc[3], df_neg(df_mul(gvc, rsq)));
+  dacc_add(acc[4], df_mul(dx, fxx)); dacc_add(acc[5], df_mul(dx, fyy)); dacc_add(acc[6], df_mul(dx, fzz));
+  dacc_add(acc[7], df_mul(dy, fyy)); dacc_add(acc[8], df_mul(dy, fzz)); dacc_add(acc[9], df_mul(dz, fzz));
+}
+
+__global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
                                                    const int* __restrict__ list, int ld,
                                                    const float4* __restrict__ xf, const float4* __restrict__ xlo,
                                                    const float2* __restrict__ qdf, const double* __restrict__ x,
@@ -528,7 +620,8 @@ __global__ void __launch_bounds__(256, 3) k_pair_df64(int natms, const DevScalar
                                                    const double* __restrict__ veps, const double* __restrict__ vsig,
                                                    PairGeom pg, unsigned long long* fixp, double* blk,
                                                    unsigned long long* cnt) {
-  const int lane = threadIdx.x & 31;
+  __shared__ PairQueue pq[PAIR_DF_NT / 32];
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   dacc acc[NACC];
 #pragma unroll
@@ -547,94 +640,62 @@ __global__ void __launch_bounds__(256, 3) k_pair_df64(int natms, const DevScalar
     const int* lst = list + (size_t)i * ld + 3;
     const int n = lst[0];
     long long sx = 0, sy = 0, sz = 0;
-    for (int m = lane + 1; m <= n; m += 32) {
-      const int j = lst[m] - 1;
-      int jf = j;
-      if (j >= natms) {
-        if (gi > ltg[j]) continue;  // evaluated from the other side
-        jf = src[j];
-      }
-      const float4 pj = xf[j], lj = xlo[j];
-      // separation: exact difference of the high parts plus the difference of the low parts
-      const df ex = two_sum(pi.x, -pj.x), ey = two_sum(pi.y, -pj.y), ez = two_sum(pi.z, -pj.z);
-      const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
-      const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
-      const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
-      const df rsq = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
-      if (rsq.hi > pg.f_hi) continue;
-      const int aj = __float_as_int(lj.w);
-      const float2 qj2 = qdf[j];
-      const bool band = (rsq.hi >= pg.f_rc2_lo && rsq.hi <= pg.f_rc2_hi) ||
-                        (rsq.hi >= pg.f_rv2_lo && rsq.hi <= pg.f_rv2_hi);
-      const bool in_c = qi_on && qj2.x != 0.0f && rsq.hi < pg.f_rc2_lo;
-      int key = -1;
-      if (rsq.hi < pg.f_rv2_lo) {
-        key = vkey(ai, aj) - 1;
-        if (vkind[key] == 0) key = -1;
-      }
-      df gam = df_make(0.f, 0.f), ee = gam, ev = gam, gvc = gam, gvv = gam;
-      bool slow = band;
-      if (!slow && (in_c || key >= 0)) {
-        const df rinv = df_rsqrt(rsq);
-        const df rrr = df_mul(rsq, rinv);
-        df d;
-        const int k = table_coord(rrr, pg.erdr_hi, pg.erdr_lo, &d);
-        int kv = k;
-        df dv = d;
-        if (!pg.same_grid && key >= 0) kv = table_coord(rrr, pg.vrdr_hi, pg.vrdr_lo, &dv);
-        if (k == 0 || (key >= 0 && kv == 0)) {
-          slow = true;  // first interval: the exact three-point formula, in FP64
-        } else {
-          if (in_c) {  // real-space Coulomb (ewald_spole.F90:131-176)
-            const float4* c = etab + (size_t)k * 3;
-            const float4 e01 = c[0], d01 = c[1], c2 = c[2];
-            const df pre = df_mul(qi, df_make(qj2.x, qj2.y));
-            gvc = df_mul(pre, poly_df(d01, c2.z, c2.w, d));
-            ee = df_mul(pre, poly_df(e01, c2.x, c2.y, d));
-            gam = gvc;
-          }
-          if (key >= 0) {  // van der Waals, tabulated (vdw.F90:1881-1962)
-            const df r_rsq = df_sqr(rinv);
-            if (pg.vdw_direct) {
-              slow = true;
-            } else {
-              const float4* c = vtab + (size_t)key * vstride + (size_t)kv * 3;
-              const float4 f01 = c[0], v01 = c[1], c2 = c[2];
-              gvv = df_mul(poly_df(f01, c2.x, c2.y, dv), r_rsq);
-              ev = poly_df(v01, c2.z, c2.w, dv);
-              gam = df_add(gam, gvv);
-            }
+    // Pass 1 over 32 entries at a time: separation and r^2; the entries inside the outer
+    // cutoff join this warp's queue (ballot compaction), so pass 2, the pair terms, runs
+    // on 32 queued pairs at a time with every lane busy.  The queue holds < 64 pairs.
+    int nq = 0;  // queued pairs (uniform over the warp)
+    for (int base = 0;; base += 32) {
+      const bool more = base < n;
+      if (more) {
+        const int m = base + lane + 1;
+        bool keep = false;
+        int j = 0;
+        df dx, dy, dz, rsq;
+        if (m <= n) {
+          j = lst[m] - 1;
+          if (j < natms || gi <= ltg[j]) {  // halo pairs are evaluated from the smaller id
+            const float4 pj = xf[j], lj = xlo[j];
+            // separation: exact difference of the high parts plus the difference of the low parts
+            const df ex = two_sum(pi.x, -pj.x), ey = two_sum(pi.y, -pj.y), ez = two_sum(pi.z, -pj.z);
+            dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
+            dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
+            dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
+            rsq = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+            keep = rsq.hi <= pg.f_hi;
           }
         }
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const int slot = nq + __popc(bal & ((1u << lane) - 1u));
+          PairQueue& Q = pq[wq];
+          Q.j[slot] = j; Q.rh[slot] = rsq.hi; Q.rl[slot] = rsq.lo;
+        }
+        nq += __popc(bal);
+        __syncwarp();
       }
-      if (slow) {
-        double g64, e64c, e64v, gc64, gv64;
-        bool any;
-        pair_terms_fp64(pg, x[i] - x[j], y[i] - y[j], z[i] - z[j], q[i] * pg.scaling, q[j], ai, aj, ecoef, vcoef,
-                        vkind, veps, vsig, &g64, &e64c, &e64v, &gc64, &gv64, &any);
-        if (!any) continue;
-        float h, l;
-        df_split(g64, &h, &l); gam = df_make(h, l);
-        df_split(e64c, &h, &l); ee = df_make(h, l);
-        df_split(e64v, &h, &l); ev = df_make(h, l);
-        df_split(gc64, &h, &l); gvc = df_make(h, l);
-        df_split(gv64, &h, &l); gvv = df_make(h, l);
-      } else if (!in_c && key < 0) {
-        continue;
+      if (nq >= 32 || (!more && nq > 0)) {
+        const int take = min(nq, 32);
+        const int slot = nq - take + lane;
+        if (lane < take) {
+          const PairQueue& Q = pq[wq];
+          const int j = Q.j[slot];
+          const df rsq = df_make(Q.rh[slot], Q.rl[slot]);
+          // the separation again (the same operations as pass 1, so the same value)
+          const float4 pj = xf[j], lj = xlo[j];
+          const int aj = __float_as_int(lj.w);
+          const df ex = two_sum(pi.x, -pj.x), ey = two_sum(pi.y, -pj.y), ez = two_sum(pi.z, -pj.z);
+          const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
+          const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
+          const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
+          const int jf = j >= natms ? src[j] : j;
+          const float2 qj2 = qdf[j];
+          pair_terms_df64(pg, i, j, jf, ai, aj, qi, qi_on, qj2, dx, dy, dz, rsq, x, y, z, q, etab, vtab, ecoef,
+                          vcoef, vkind, veps, vsig, vstride, fixp, acc, sx, sy, sz, n_rc);
+        }
+        nq -= take;
+        __syncwarp();  // the taken slots are read before the next pass appends over them
       }
-      ++n_rc;
-      const df fxx = df_mul(gam, dx), fyy = df_mul(gam, dy), fzz = df_mul(gam, dz);
-      const long long ix = fix40_df(fxx), iy = fix40_df(fyy), iz = fix40_df(fzz);
-      sx += ix; sy += iy; sz += iz;
-      atomicAdd(&fixp[3 * jf + 0], (unsigned long long)(-ix));
-      atomicAdd(&fixp[3 * jf + 1], (unsigned long long)(-iy));
-      atomicAdd(&fixp[3 * jf + 2], (unsigned long long)(-iz));
-      dacc_add(acc[0], ev);
-      dacc_add(acc[1], df_neg(df_mul(gvv, rsq)));
-      dacc_add(acc[2], ee);
-      dacc_add(acc[3], df_neg(df_mul(gvc, rsq)));
-      dacc_add(acc[4], df_mul(dx, fxx)); dacc_add(acc[5], df_mul(dx, fyy)); dacc_add(acc[6], df_mul(dx, fzz));
-      dacc_add(acc[7], df_mul(dy, fyy)); dacc_add(acc[8], df_mul(dy, fzz)); dacc_add(acc[9], df_mul(dz, fzz));
+      if (!more && nq == 0) break;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -714,12 +775,12 @@ void pair_forces(double* eng6, double* stress9) {
     df_split(pg.vrdr, &pg.vrdr_hi, &pg.vrdr_lo);
     df_split(pg.scaling, &pg.scal_hi, &pg.scal_lo);
     static int occdf = 0;
-    if (!occdf) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occdf, k_pair_df64, T, 0));
-    int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, T), occdf * g.nsm));
+    if (!occdf) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occdf, k_pair_df64, PAIR_DF_NT, 0));
+    int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, PAIR_DF_NT), occdf * g.nsm));
     double* blk = gb_blkacc(nb * NACC + nb2 * 8);
     GB_CUDA(cudaMemsetAsync(g.fixp, 0, sizeof(long long) * 3 * (size_t)g.natms, st));
     prof_begin(P_PAIR);
-    k_pair_df64<<<nb, T, 0, st>>>(g.natms, g.sc, g.at_list, g.list, g.ld, g.xf, g.xlo, g.qdf, g.x, g.y, g.z, g.chge,
+    k_pair_df64<<<nb, PAIR_DF_NT, 0, st>>>(g.natms, g.sc, g.at_list, g.list, g.ld, g.xf, g.xlo, g.qdf, g.x, g.y, g.z, g.chge,
                                   g.ltg, g.src, g.erfc_df, g.vdw_df, g.erfc_coef, g.vdw_coef, g.vdw_kind, g.vdw_eps,
                                   g.vdw_sig, pg, (unsigned long long*)g.fixp, blk, &g.sc->npairs_list);
     GB_LAUNCHED();
