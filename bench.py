@@ -149,7 +149,7 @@ def kernel_work(name, s, cnt, form):
     K = s.kmax
     K3 = K[0] * K[1] * K[2]
     p = s.nsplines
-    esz = 8 if form == "fp64" else 4
+    esz = 8 if form.startswith("fp64") else 4
     P_list, P_rc = cnt
     if name == "pair_forces":
         return 10.0 * P_list + 55.0 * P_rc, N * (24 + 8 + 4 + 24) + 4.0 * P_list
@@ -182,6 +182,9 @@ MEASURED_TRAFFIC = {
     ("pair_forces", "fp64"): (207.98e6 / 40368337,
                               "ncu dram__bytes.sum (rate x duration) of k_pair_df64 on nacl_175616 "
                               "(profiles/pair_df64_nacl175616.md), scaled by half-list entries"),
+    ("pair_forces", "fp64_native"): ((200.795648e6 + 3.779072e6) / 40368337,
+                                     "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_fp64 on nacl_175616 "
+                                     "(profiles/pair_fp64_nacl175616.md), scaled by half-list entries"),
     ("pair_forces", "mixed"): ((200.9e6 + 5.2e6) / 40368337,
                                "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_mixed_half on nacl_175616 "
                                "(profiles/pair_mixed_nacl175616.md), scaled by half-list entries"),
@@ -262,7 +265,9 @@ def run_reference(args, dist):
 
 
 # ----------------------------------------------------------------- GPU arm
-FORMS = {"fp64": (0, 1), "mixed": (1, 1), "mts_k4": (1, 4), "mts_k8": (1, 8)}
+# form: (precision, MTS k).  fp64 evaluates the pair loop and SPME in double-float (FP64
+# accuracy on the FP32 pipes); fp64_native runs the same path in FP64 instructions.
+FORMS = {"fp64": (0, 1), "fp64_native": (2, 1), "mixed": (1, 1), "mts_k4": (1, 4), "mts_k8": (1, 8)}
 MTS_TOL = 1e-4
 
 
@@ -462,7 +467,7 @@ def run_gb(args, dist):
         sec = prof[dom][0] / prof[dom][1] * 1e-3
         inst = MEASURED_INST.get((dom, args.form)) if precision == 0 else None
         fp64_view = None
-        if args.form == "fp64" and fp64_peak and fp64_peak > 0:
+        if args.form.startswith("fp64") and fp64_peak and fp64_peak > 0:
             fp64_view = {"achieved": fl / sec / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": fl / sec / 1e12 / fp64_peak,
                          "peak_source": "FP64 DFMA loop measured in this run"}
@@ -483,7 +488,7 @@ def run_gb(args, dist):
                     "fp64_view": fp64_view,
                     "hbm_view": {"achieved": by / sec / 1e9, "peak": hbm, "unit": "GB/s",
                                  "frac": (by / sec / 1e9) / hbm if hbm else None}}
-        elif args.form == "fp64" and fp64_peak and fp64_peak > 0 and fl / by > fp64_peak * 1e3 / (hbm or 6751.1):
+        elif args.form.startswith("fp64") and fp64_peak and fp64_peak > 0 and fl / by > fp64_peak * 1e3 / (hbm or 6751.1):
             roof = {"bound": "fp64", "kernel": dom, "achieved": fl / sec / 1e12, "peak": fp64_peak,
                     "unit": "TFLOP/s", "frac": fl / sec / 1e12 / fp64_peak, "traffic": None,
                     "peak_source": "FP64 DFMA loop measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
@@ -494,7 +499,7 @@ def run_gb(args, dist):
                     "frac": (by / sec / 1e9) / (hbm or 6800.0), "traffic": None,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else "fallback 6.8 TB/s"}
         roof["algorithmic"] = {"flops_per_launch": fl, "bytes_per_launch": by, "launch_ms": sec * 1e3}
-        tr = MEASURED_TRAFFIC.get((dom, "fp64" if precision == 0 else "mixed"))
+        tr = MEASURED_TRAFFIC.get((dom, args.form if args.form.startswith("fp64") else "mixed"))
         if tr:
             roof["traffic"] = tr[0] * P_list
             roof["traffic_source"] = tr[1]
@@ -521,7 +526,9 @@ def run_gb(args, dist):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if precision == 0 else "f32+i64",
+        # fp64: pair loop and SPME in double-float (two f32 per value, FP64-level accuracy),
+        # list, integration and constraints in f64; mixed: f32 arithmetic, i64 fixed-point sums
+        "dtype": {0: "df64+f64", 2: "f64"}.get(precision, "f32+i64"),
         "data": "synthetic (seeded lattice + Maxwell-Boltzmann start)",
         "config": {"workload": desc, "form": args.form, "natms": s.natms, "dt_fs": 2.0,
                    "list_rebuilds_in_timed_steps": rebuilds, "parallelism": "replicas" if dist.world > 1 else "single",

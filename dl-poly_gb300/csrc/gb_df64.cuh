@@ -106,6 +106,16 @@ __device__ __forceinline__ void dacc_add(dacc& a, df t) {
 
 __device__ __forceinline__ double dacc_value(const dacc& a) { return (double)a.s + (double)a.c; }
 
+// a += x * y: the exact product's high part enters the compensated sum, its error term
+// and the cross terms go straight to the correction (no renormalised product)
+__device__ __forceinline__ void dacc_add_prod(dacc& a, df x, df y) {
+  const df p = two_prod(x.hi, y.hi);
+  const float t = __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, p.lo));
+  const df u = two_sum(a.s, p.hi);
+  a.s = u.hi;
+  a.c = __fadd_rn(a.c, __fadd_rn(u.lo, t));
+}
+
 // int64 fixed point (scale 2^40) of a double-float, each part rounded toward zero: the
 // scaling by 2^40 is exact, and for |a| < 2^23 the hardware conversion gives what fix40
 // gives.  The conversion runs on the FP64 unit, which the double-float kernels leave

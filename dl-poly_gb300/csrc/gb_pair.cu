@@ -601,11 +601,11 @@ __device__ __forceinline__ void pair_terms_df64(const PairGeom& pg, int i, int j
   atomicAdd(&fixp[3 * jf + 1], (unsigned long long)(-iy));
   atomicAdd(&fixp[3 * jf + 2], (unsigned long long)(-iz));
   dacc_add(acc[0], ev);
-  dacc_add(acc[1], df_neg(df_mul(gvv, rsq)));
+  dacc_add_prod(acc[1], df_neg(gvv), rsq);
   dacc_add(acc[2], ee);
-  dacc_add(acc[3], df_neg(df_mul(gvc, rsq)));
-  dacc_add(acc[4], df_mul(dx, fxx)); dacc_add(acc[5], df_mul(dx, fyy)); dacc_add(acc[6], df_mul(dx, fzz));
-  dacc_add(acc[7], df_mul(dy, fyy)); dacc_add(acc[8], df_mul(dy, fzz)); dacc_add(acc[9], df_mul(dz, fzz));
+  dacc_add_prod(acc[3], df_neg(gvc), rsq);
+  dacc_add_prod(acc[4], dx, fxx); dacc_add_prod(acc[5], dx, fyy); dacc_add_prod(acc[6], dx, fzz);
+  dacc_add_prod(acc[7], dy, fyy); dacc_add_prod(acc[8], dy, fzz); dacc_add_prod(acc[9], dz, fzz);
 }
 
 __global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
