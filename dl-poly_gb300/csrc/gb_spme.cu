@@ -28,118 +28,11 @@
 
 #include "gb_common.cuh"
 #include "gb_dfr.cuh"
+#include "gb_fft.cuh"
 
 namespace {
 
 constexpr int PMAX = 12;
-constexpr int TX = 4;  // columns per tile in the strided passes
-
-template <typename T> struct V2;
-template <> struct V2<double> { using t = double2; };
-template <> struct V2<float> { using t = float2; };
-template <> struct V2<dfr> { using t = dfc; };
-
-template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
-  T2 r;
-  r.x = a.x * b.x - a.y * b.y;
-  r.y = a.x * b.y + a.y * b.x;
-  return r;
-}
-template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { T2 r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
-template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { T2 r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
-// multiply by s*i
-// multiply by S*i with S = +1 or -1 known at compile time (a free operand negation)
-template <int S, typename T2> __device__ __forceinline__ T2 cmuli(T2 a) {
-  T2 r;
-  if (S > 0) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; }
-  return r;
-}
-
-// x != 0 tested on the bit pattern (no FP64 compare instruction)
-__device__ __forceinline__ bool nonzero_bits(double v) { return (__double_as_longlong(v) << 1) != 0; }
-__device__ __forceinline__ bool nonzero_bits(float v) { return (__float_as_uint(v) << 1) != 0u; }
-
-struct FftPlan {
-  int N;
-  int nrad;
-  int rad[16];
-};
-
-// one Stockham stage over nlines lines of length N held in shared memory
-template <typename T, typename T2, int ISIGN>
-__device__ void fft_stage(const T2* __restrict__ in, T2* __restrict__ out, int N, int nlines, int R, int Ns,
-                          const T2* __restrict__ tw) {
-  const int T_ = N / R;
-  const int total = nlines * T_;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int line = idx / T_;
-    const int j = idx - line * T_;
-    const int k = j % Ns;
-    const T2* src = in + line * N;
-    T2* dst = out + line * N;
-    T2 v[5];
-#pragma unroll 5
-    for (int r = 0; r < 5; ++r)
-      if (r < R) v[r] = src[j + r * T_];
-    if (Ns > 1) {
-      const int step = N / (Ns * R);
-#pragma unroll 5
-      for (int r = 1; r < 5; ++r) {
-        if (r < R) {
-          T2 w = tw[(r * k * step) % N];
-          if (ISIGN < 0) w.y = -w.y;
-          v[r] = cmul(v[r], w);
-        }
-      }
-    }
-    T2 o[5];
-    if (R == 4) {
-      T2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]), c = cadd(v[1], v[3]), d = csub(v[1], v[3]);
-      T2 di = cmuli<ISIGN>(d);
-      o[0] = cadd(a, c); o[2] = csub(a, c); o[1] = cadd(b, di); o[3] = csub(b, di);
-    } else if (R == 2) {
-      o[0] = cadd(v[0], v[1]); o[1] = csub(v[0], v[1]);
-    } else if (R == 3) {
-      const T h = (T)0.86602540378443864676;
-      T2 t = cadd(v[1], v[2]), u = csub(v[1], v[2]);
-      T2 m;
-      m.x = v[0].x - (T)0.5 * t.x; m.y = v[0].y - (T)0.5 * t.y;
-      T2 ui = cmuli<ISIGN>(u);
-      ui.x *= h; ui.y *= h;
-      o[0] = cadd(v[0], t); o[1] = cadd(m, ui); o[2] = csub(m, ui);
-    } else {  // R == 5
-      const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
-      const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;
-      T2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]), t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
-      o[0] = cadd(v[0], cadd(t1, t2));
-      T2 a1, a2, b1, b2;
-      a1.x = v[0].x + c1 * t1.x + c2 * t2.x; a1.y = v[0].y + c1 * t1.y + c2 * t2.y;
-      a2.x = v[0].x + c2 * t1.x + c1 * t2.x; a2.y = v[0].y + c2 * t1.y + c1 * t2.y;
-      b1.x = s1 * t3.x + s2 * t4.x; b1.y = s1 * t3.y + s2 * t4.y;
-      b2.x = s2 * t3.x - s1 * t4.x; b2.y = s2 * t3.y - s1 * t4.y;
-      T2 ib1 = cmuli<ISIGN>(b1), ib2 = cmuli<ISIGN>(b2);
-      o[1] = cadd(a1, ib1); o[4] = csub(a1, ib1); o[2] = cadd(a2, ib2); o[3] = csub(a2, ib2);
-    }
-    const int base = (j / Ns) * Ns * R + k;
-#pragma unroll 5
-    for (int r = 0; r < 5; ++r)
-      if (r < R) dst[base + r * Ns] = o[r];
-  }
-}
-
-// full transform of nlines lines; returns the buffer holding the result
-template <typename T, typename T2, int ISIGN>
-__device__ T2* fft_lines(T2* a, T2* b, const FftPlan& pl, int nlines, const T2* tw) {
-  int Ns = 1;
-  for (int s = 0; s < pl.nrad; ++s) {
-    __syncthreads();
-    fft_stage<T, T2, ISIGN>(a, b, pl.N, nlines, pl.rad[s], Ns, tw);
-    Ns *= pl.rad[s];
-    T2* t = a; a = b; b = t;
-  }
-  __syncthreads();
-  return a;
-}
 
 // ------------------------------------------------------------ spline prep
 // Cardinal B-spline values M_p(w + p - 1 - t), t = 0..p-1, by the order
@@ -186,19 +79,6 @@ __device__ __forceinline__ void bspline_vals(T w, int p_rt, T* m /*p*/, T* dm /*
 #pragma unroll
   for (int t = 0; t < p; ++t) m[t] = z[t + 1];
 }
-
-struct SpmeGeom {
-  double rc[9];
-  float rch[9], rcl[9];  // rc as double-floats
-  double Kr[3];
-  int K[3], B[3], nb[3], p;
-};
-
-// a reciprocal-cell entry in the working precision (double-floats from the stored split)
-template <typename T>
-__device__ __forceinline__ T rc_at(const SpmeGeom& sg, int k) { return (T)sg.rc[k]; }
-template <>
-__device__ __forceinline__ dfr rc_at<dfr>(const SpmeGeom& sg, int k) { return dfr(sg.rch[k], sg.rcl[k]); }
 
 template <typename T, int P>
 __global__ void k_spme_prep(int natms, const double* __restrict__ x, const double* __restrict__ y,
@@ -451,186 +331,6 @@ __global__ void k_spme_tile_reduce(SpmeGeom sg, const T* __restrict__ ext, T* __
 inline size_t spread_smem(int B0, int B1, int B2, int p, size_t esz) {
   const size_t tsize = (size_t)(B0 + p - 1) * (B1 + p - 1) * (B2 + p - 1);
   return esz * (tsize + (size_t)SPREAD_CH * p * p + (size_t)SPREAD_CH * p) + sizeof(int) * 3 * SPREAD_CH;
-}
-
-// ---------------------------------------------------------------- FFT passes
-// The charge grid is real, so the x pass is a real-to-complex transform: a row
-// of N = K1 reals is packed as M = N/2 complex values z_n = x_2n + i x_2n+1,
-// transformed with the half-length complex FFT and split into the N/2+1
-// non-redundant outputs
-//   X_k = E_k + w^k O_k,  E_k = (Z_k + conj Z_{M-k}) / 2,  O_k = (Z_k - conj Z_{M-k}) / 2i,
-// w = e^{+2 pi i/N} (the forward sign of the reference's transform).  The y and
-// z passes then run on Kx = N/2+1 columns.  The inverse rebuilds
-//   Z_k = (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) w^{-k},  k < M,
-// runs the half-length inverse and unpacks x_2n = Re z_n, x_2n+1 = Im z_n: the
-// real part of the full inverse transform, as before.
-template <typename T, typename T2>
-__global__ void k_fft_x_fwd(const T* __restrict__ Q, T2* __restrict__ G, FftPlan pl, const T2* __restrict__ tw,
-                            const T2* __restrict__ twN, int nrows, int lines) {
-  extern __shared__ unsigned char smem_raw[];
-  T2* a = reinterpret_cast<T2*>(smem_raw);
-  T2* b = a + lines * pl.N;
-  const int M = pl.N, Kx = M + 1;
-  const size_t row0 = (size_t)blockIdx.x * lines;
-  const int nl = (int)min((size_t)lines, (size_t)nrows - row0);
-  const T2* Qc = reinterpret_cast<const T2*>(Q);
-  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) a[e] = Qc[row0 * M + e];
-  T2* r = fft_lines<T, T2, +1>(a, b, pl, nl, tw);
-  for (int e = threadIdx.x; e < nl * Kx; e += blockDim.x) {
-    const int line = e / Kx, k = e - line * Kx;
-    const T2 zk = r[line * M + (k == M ? 0 : k)];
-    const T2 zc = r[line * M + (k == 0 ? 0 : M - k)];  // Z_{M-k}, conjugated below
-    const T ex = (T)0.5 * (zk.x + zc.x), ey = (T)0.5 * (zk.y - zc.y);
-    const T ox = (T)0.5 * (zk.y + zc.y), oy = (T)0.5 * (zc.x - zk.x);
-    const T2 w = twN[k];
-    T2 v;
-    v.x = ex + (w.x * ox - w.y * oy);
-    v.y = ey + (w.x * oy + w.y * ox);
-    G[(row0 + line) * Kx + k] = v;
-  }
-}
-
-template <typename T, typename T2>
-__global__ void k_fft_x_inv(const T2* __restrict__ G, T* __restrict__ Q, FftPlan pl, const T2* __restrict__ tw,
-                            const T2* __restrict__ twN, int nrows, int lines) {
-  extern __shared__ unsigned char smem_raw[];
-  T2* a = reinterpret_cast<T2*>(smem_raw);
-  T2* b = a + lines * pl.N;
-  const int M = pl.N, Kx = M + 1;
-  const size_t row0 = (size_t)blockIdx.x * lines;
-  const int nl = (int)min((size_t)lines, (size_t)nrows - row0);
-  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
-    const int line = e / M, k = e - line * M;
-    const T2 xk = G[(row0 + line) * Kx + k];
-    const T2 xc = G[(row0 + line) * Kx + (M - k)];  // X_{M-k}, conjugated below
-    const T ax = xk.x + xc.x, ay = xk.y - xc.y;     // X_k + conj X_{M-k}
-    const T dx = xk.x - xc.x, dy = xk.y + xc.y;     // X_k - conj X_{M-k}
-    const T2 w = twN[k];                            // w^{-k} = conj(w^k)
-    const T bx = dx * w.x + dy * w.y, by = dy * w.x - dx * w.y;
-    T2 v;
-    v.x = ax - by;
-    v.y = ay + bx;
-    a[e] = v;
-  }
-  T2* r = fft_lines<T, T2, -1>(a, b, pl, nl, tw);
-  T2* Qc = reinterpret_cast<T2*>(Q);
-  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) Qc[row0 * M + e] = r[e];
-}
-
-// Y pass (stride Kx): tile of TX columns x N lines, in place
-template <typename T, typename T2, int ISIGN>
-__global__ void k_fft_y(T2* __restrict__ G, int Kx, int K2, FftPlan pl, const T2* __restrict__ tw) {
-  extern __shared__ unsigned char smem_raw[];
-  T2* a = reinterpret_cast<T2*>(smem_raw);
-  T2* b = a + TX * pl.N;
-  const int ntx = (Kx + TX - 1) / TX;
-  const int x0 = (blockIdx.x % ntx) * TX;
-  const int zz = blockIdx.x / ntx;
-  const int nt = min(TX, Kx - x0);
-  T2* base = G + (size_t)zz * Kx * K2 + x0;
-  for (int e = threadIdx.x; e < TX * K2; e += blockDim.x) {
-    int yy = e / TX, t = e - yy * TX;
-    T2 v; v.x = (T)0; v.y = (T)0;
-    if (t < nt) v = base[(size_t)yy * Kx + t];
-    a[t * K2 + yy] = v;
-  }
-  T2* r = fft_lines<T, T2, ISIGN>(a, b, pl, TX, tw);
-  for (int e = threadIdx.x; e < TX * K2; e += blockDim.x) {
-    int yy = e / TX, t = e - yy * TX;
-    if (t < nt) base[(size_t)yy * Kx + t] = r[t * K2 + yy];
-  }
-}
-
-// Z pass: forward z FFT, influence function + stress, inverse z FFT on the
-// Kx = K1/2+1 columns of the half spectrum; columns 0 < x < K1/2 stand for
-// themselves and their conjugate mirror, so they count twice in the stress
-template <typename T, typename T2>
-__global__ void k_fft_z_conv(T2* __restrict__ G, int K1, int K2, int K3, FftPlan pl, const T2* __restrict__ tw,
-                             const T* __restrict__ theta, const T* __restrict__ psi, SpmeGeom sg, double* blk) {
-  extern __shared__ unsigned char smem_raw[];
-  T2* a = reinterpret_cast<T2*>(smem_raw);
-  T2* b = a + TX * pl.N;
-  const int Kx = K1 / 2 + 1;
-  const int ntx = (Kx + TX - 1) / TX;
-  const int x0 = (blockIdx.x % ntx) * TX;
-  const int yy = blockIdx.x / ntx;
-  const int nt = min(TX, Kx - x0);
-  const size_t plane = (size_t)Kx * K2;
-  T2* base = G + (size_t)yy * Kx + x0;
-  for (int e = threadIdx.x; e < TX * K3; e += blockDim.x) {
-    int zz = e / TX, t = e - zz * TX;
-    T2 v; v.x = (T)0; v.y = (T)0;
-    if (t < nt) v = base[(size_t)zz * plane + t];
-    a[t * K3 + zz] = v;
-  }
-  // m_z = ll * rcell(9) for the cubic cell (gb_init accepts cubic cells only)
-  T* rzt = reinterpret_cast<T*>(b + TX * pl.N);
-  for (int zz = threadIdx.x; zz < K3; zz += blockDim.x) {
-    int ll = zz; if (2 * ll > K3) ll -= K3;
-    rzt[zz] = (T)ll * rc_at<T>(sg, 8);
-  }
-  T2* r = fft_lines<T, T2, +1>(a, b, pl, TX, tw);
-  // Reciprocal stress sum_m m_a m_b psi |Q(m)|^2 (ewald_spole.F90:1362-1371): with
-  // m = (mx, my, mz) and mx, my fixed along a z line, each line needs only
-  // A = sum psi|Q|^2, B = sum mz psi|Q|^2, C = sum mz^2 psi|Q|^2.
-  const int tpl = blockDim.x / TX;          // threads per line
-  const int t = threadIdx.x / tpl;          // this thread's line
-  // Bn: the z-Nyquist point (mz = +K3/2 for a point and its mirror alike) kept apart
-  T A = 0, B = 0, Bn = 0, C = 0;
-  if (t < nt) {
-    const size_t line0 = (size_t)yy * Kx + x0 + t;
-    T2* rl = r + t * K3;
-    for (int zz = threadIdx.x - t * tpl; zz < K3; zz += tpl) {
-      const size_t gi = line0 * K3 + zz;  // theta/psi are stored z-contiguous per (x,y) line
-      const T th = theta[gi];
-      T2 v = rl[zz];
-      if (nonzero_bits(th)) {
-        const T pv = psi[gi] * (v.x * v.x + v.y * v.y);
-        const T u = pv * rzt[zz];
-        A += pv;
-        if (2 * zz == K3) Bn += u;
-        else B += u;
-        C = fma(u, rzt[zz], C);
-        v.x *= th; v.y *= th;
-      } else {
-        v.x = (T)0; v.y = (T)0;
-      }
-      rl[zz] = v;
-    }
-  }
-  // in the working precision T: the FP32 form issues no FP64 instruction here
-  // A line 0 < jx < K1/2 stands for itself and its mirror m' = -m, except that
-  // a Nyquist index (ky = K2/2, mz = K3/2) keeps its + sign in the mirror.
-  // The mirror's share of m_a m_b psi|Q|^2 is then +/- the line's own:
-  //   xx, yy, zz: +;  xy: - when ky is Nyquist;  xz: - for the Nyquist z point;
-  //   yz: - when exactly one of ky and the z point is Nyquist.
-  T st[6] = {0, 0, 0, 0, 0, 0};
-  if (t < nt) {
-    const int jx = x0 + t;
-    int jj = jx; if (2 * jj > K1) jj -= K1;
-    int kk = yy; if (2 * kk > K2) kk -= K2;
-    const T rx = (T)jj * rc_at<T>(sg, 0), ry = (T)kk * rc_at<T>(sg, 4);
-    if (jx == 0 || 2 * jx == K1) {  // the line holds its own mirror: the full-spectrum sums
-      const T Ball = B + Bn;
-      st[0] = rx * rx * A; st[1] = rx * ry * A; st[2] = rx * Ball;
-      st[3] = ry * ry * A; st[4] = ry * Ball; st[5] = C;
-    } else {
-      const bool ny = 2 * yy == K2;
-      st[0] = (T)2 * rx * rx * A;
-      st[1] = ny ? (T)0 : (T)2 * rx * ry * A;
-      st[2] = (T)2 * rx * B;
-      st[3] = (T)2 * ry * ry * A;
-      st[4] = (T)2 * ry * (ny ? Bn : B);
-      st[5] = (T)2 * C;
-    }
-  }
-  T2* o = (r == a) ? b : a;
-  T2* r2 = fft_lines<T, T2, -1>(r, o, pl, TX, tw);
-  for (int e = threadIdx.x; e < TX * K3; e += blockDim.x) {
-    int zz = e / TX, t = e - zz * TX;
-    if (t < nt) base[(size_t)zz * plane + t] = r2[t * K3 + zz];
-  }
-  block_reduce_store<6>(st, blk);
 }
 
 // --------------------------------------------------------------- gather
@@ -988,6 +688,14 @@ size_t fft_smem(int N, int lines, size_t esz) { return (size_t)2 * lines * N * e
 
 }  // namespace
 
+namespace gbspme {
+// the all-FP64 form keeps the runtime-plan transform at every length
+template <>
+FftKernels<double, double2> fft_kernels<double, double2>(int M, int K2, int K3) {
+  return fft_pick<double, double2>(FftLens<>(), FftLens<>(), M, K2, K3);
+}
+}  // namespace gbspme
+
 extern void invert_host(const double* a, double* b, double* d);
 extern void dcell_host(const double* aaa, double* bbb);
 
@@ -1004,6 +712,15 @@ void raise_smem(K kernel, int bytes) {
     GB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }
 
+// threads per FFT block: enough for one butterfly of the smallest radix per
+// thread over the block's lines (at most 256), in whole warps
+int fft_threads(const FftPlan& pl, int nlines) {
+  int rmin = 5;
+  for (int s = 0; s < pl.nrad; ++s) rmin = std::min(rmin, pl.rad[s]);
+  const int need = nlines * pl.N / std::max(rmin, 1);
+  return std::min(256, std::max(32, (need + 31) / 32 * 32));
+}
+
 void grid_free(SpmeGrid& S) {
   void* ptrs[] = {S.spl, S.nidx, S.brick_of, S.brick_count, S.brick_start, S.brick_fill, S.brick_atoms, S.Q, S.G,
                   S.Qf, S.Gf, S.theta, S.psi, S.theta_f, S.psi_f, S.tw[0], S.tw[1], S.tw[2], S.twf[0], S.twf[1],
@@ -1015,6 +732,17 @@ void grid_free(SpmeGrid& S) {
 }
 
 // grid of K[0..2] points and spline order p; fp64 = also the FP64 buffers
+// dynamic shared-memory limit of the FFT kernels this grid launches
+template <typename T, typename T2>
+void raise_fft(const SpmeGrid& S, int smem) {
+  const FftKernels<T, T2> k = fft_kernels<T, T2>(S.planh.N, S.K[1], S.K[2]);
+  raise_smem(k.x_fwd, smem);
+  raise_smem(k.x_inv, smem);
+  raise_smem(k.y_fwd, smem);
+  raise_smem(k.y_inv, smem);
+  raise_smem(k.z_conv, smem);
+}
+
 void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
   grid_free(S);
   if (p > PMAX || p < 3) throw (int)GB_ERR_ARG;
@@ -1192,23 +920,9 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
   const int maxN = std::max(S.K[0], std::max(S.K[1], S.K[2]));
   int smem = (int)std::max(fft_smem(maxN, TX, sizeof(double2)), fft_smem(S.K[0], 8, sizeof(double2)));
   smem = std::max(smem, 48 * 1024);
-  raise_smem(k_fft_x_fwd<double, double2>, smem);
-  raise_smem(k_fft_x_inv<double, double2>, smem);
-  raise_smem(k_fft_y<double, double2, +1>, smem);
-  raise_smem(k_fft_y<double, double2, -1>, smem);
-  raise_smem(k_fft_z_conv<double, double2>, smem);
-  raise_smem(k_fft_x_fwd<float, float2>, smem);
-  raise_smem(k_fft_x_inv<float, float2>, smem);
-  raise_smem(k_fft_y<float, float2, +1>, smem);
-  raise_smem(k_fft_y<float, float2, -1>, smem);
-  raise_smem(k_fft_z_conv<float, float2>, smem);
-  if (S.fp64) {
-    raise_smem(k_fft_x_fwd<dfr, dfc>, smem);
-    raise_smem(k_fft_x_inv<dfr, dfc>, smem);
-    raise_smem(k_fft_y<dfr, dfc, +1>, smem);
-    raise_smem(k_fft_y<dfr, dfc, -1>, smem);
-    raise_smem(k_fft_z_conv<dfr, dfc>, smem);
-  }
+  raise_fft<double, double2>(S, smem);
+  raise_fft<float, float2>(S, smem);
+  if (S.fp64) raise_fft<dfr, dfc>(S, smem);
   GB_CUDA(cudaStreamSynchronize(g.stream));
   S.ready = true;
 }
@@ -1294,28 +1008,30 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
                      : (F64 ? reinterpret_cast<const T2*>(S.twh) : reinterpret_cast<const T2*>(S.twhf));
   const int ntx = (Kx + TX - 1) / TX;
   prof_begin(pid(P_FFT_XF));
-  k_fft_x_fwd<T, T2><<<nblocks(rows, lines), 256, fft_smem(M, lines, sizeof(T2)), st>>>(Q, G, S.planh, twh, tw1, rows,
-                                                                                         lines);
+  const FftKernels<T, T2> fk = fft_kernels<T, T2>(M, K2, K3);
+  const int thx = fft_threads(S.planh, lines), thy = fft_threads(S.plan[1], TX), thz = fft_threads(S.plan[2], TX);
+  fk.x_fwd<<<nblocks(rows, lines), thx, fft_smem(M, lines, sizeof(T2)), st>>>(Q, G, S.planh, twh, tw1,
+                                                                                            rows, lines);
   GB_LAUNCHED();
   prof_end(pid(P_FFT_XF));
   prof_begin(pid(P_FFT_Y));
-  k_fft_y<T, T2, +1><<<ntx * K3, 256, fft_smem(K2, TX, sizeof(T2)), st>>>(G, Kx, K2, S.plan[1], tw2);
+  fk.y_fwd<<<ntx * K3, thy, fft_smem(K2, TX, sizeof(T2)), st>>>(G, Kx, K2, S.plan[1], tw2);
   GB_LAUNCHED();
   prof_end(pid(P_FFT_Y));
   const int nbz = ntx * K2;
   double* blkz = gb_blkacc(nbz * 6 + nblocks((long long)n * 32, 128) * 4);
   prof_begin(pid(P_FFT_Z));
-  k_fft_z_conv<T, T2><<<nbz, 256, fft_smem(K3, TX, sizeof(T2)) + K3 * sizeof(T), st>>>(G, K1, K2, K3, S.plan[2], tw3,
+  fk.z_conv<<<nbz, thz, fft_smem(K3, TX, sizeof(T2)) + K3 * sizeof(T), st>>>(G, K1, K2, K3, S.plan[2], tw3,
                                                                                        th, ps, S.sg, blkz);
   GB_LAUNCHED();
   prof_end(pid(P_FFT_Z));
   prof_begin(pid(P_FFT_Y));
-  k_fft_y<T, T2, -1><<<ntx * K3, 256, fft_smem(K2, TX, sizeof(T2)), st>>>(G, Kx, K2, S.plan[1], tw2);
+  fk.y_inv<<<ntx * K3, thy, fft_smem(K2, TX, sizeof(T2)), st>>>(G, Kx, K2, S.plan[1], tw2);
   GB_LAUNCHED();
   prof_end(pid(P_FFT_Y));
   prof_begin(pid(P_FFT_XI));
-  k_fft_x_inv<T, T2><<<nblocks(rows, lines), 256, fft_smem(M, lines, sizeof(T2)), st>>>(G, Q, S.planh, twh, tw1, rows,
-                                                                                         lines);
+  fk.x_inv<<<nblocks(rows, lines), thx, fft_smem(M, lines, sizeof(T2)), st>>>(G, Q, S.planh, twh, tw1,
+                                                                                            rows, lines);
   GB_LAUNCHED();
   prof_end(pid(P_FFT_XI));
   // gather

@@ -15,7 +15,7 @@ CSRC = os.path.join(os.path.dirname(HERE), "csrc")
 OBJ = os.path.join(os.path.dirname(HERE), "_build")
 LIB = os.path.join(HERE, "libdlpoly_gb300.so")
 SOURCES = ["gb_api.cu", "gb_list.cu", "gb_pair.cu", "gb_spme.cu", "gb_integrate.cu", "gb_thermostat.cu", "gb_metal.cu", "gb_mlp.cu",
-           "gb_noalloc.cu"]
+           "gb_noalloc.cu", "gb_fft_f32.cu", "gb_fft_df.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 
