@@ -261,71 +261,58 @@ __global__ void k_spme_spread_fix(SpmeGeom sg, const int* __restrict__ bstart, c
   long long* out = ext + (size_t)b * tsize;
   for (int e = threadIdx.x; e < tsize; e += blockDim.x) out[e] = tile[e];
 }
+// The tiles that cover grid index g along one dimension: its own brick b0 (tile
+// coordinate g - b0 B + p - 1) and, when g lies in the lower halo of the next
+// brick, that brick too (periodic).
+struct TileCover {
+  int b[2], t[2], n;
+};
+__device__ __forceinline__ TileCover tile_cover(int g, int B, int p, int nb) {
+  TileCover c;
+  const int b0 = g / B;
+  c.b[0] = b0;
+  c.t[0] = g - b0 * B + p - 1;
+  c.b[1] = b0 + 1 == nb ? 0 : b0 + 1;
+  c.t[1] = c.t[0] - B;
+  c.n = c.t[1] >= 0 ? 2 : 1;
+  return c;
+}
+
+// Halo reduction: every grid point sums, in a fixed order (z, then y, then x
+// covering tile), the tile entries of the (at most 2 per dimension) bricks
+// whose tiles cover it.  Launched on a (x blocks, K1, K2) grid: y and z come
+// from the block index, so the per-point index arithmetic is one division.
+template <typename T, typename S>
+__device__ __forceinline__ S tile_sum(const SpmeGeom& sg, const T* __restrict__ ext, int gx, int gy, int gz) {
+  const int p = sg.p;
+  const int TXd = sg.B[0] + p - 1, TYd = sg.B[1] + p - 1, TZd = sg.B[2] + p - 1;
+  const size_t tsize = (size_t)TXd * TYd * TZd;
+  const TileCover cx = tile_cover(gx, sg.B[0], p, sg.nb[0]);
+  const TileCover cy = tile_cover(gy, sg.B[1], p, sg.nb[1]);
+  const TileCover cz = tile_cover(gz, sg.B[2], p, sg.nb[2]);
+  S s = (S)0;
+  for (int iz = 0; iz < cz.n; ++iz)
+    for (int iy = 0; iy < cy.n; ++iy)
+      for (int ix = 0; ix < cx.n; ++ix) {
+        const int b = cx.b[ix] + sg.nb[0] * (cy.b[iy] + sg.nb[1] * cz.b[iz]);
+        s += ext[(size_t)b * tsize + ((size_t)cz.t[iz] * TYd + cy.t[iy]) * TXd + cx.t[ix]];
+      }
+  return s;
+}
 
 // fixed-point halo reduction for the mixed form (int64 sums, one conversion per point)
 __global__ void k_spme_tile_reduce_fix(SpmeGeom sg, const long long* __restrict__ ext, float* __restrict__ Q) {
-  const size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
-  if (gid >= (size_t)K0 * K1 * K2) return;
-  const int gg[3] = {(int)(gid % K0), (int)((gid / K0) % K1), (int)(gid / ((size_t)K0 * K1))};
-  const int p = sg.p;
-  const int TXd = sg.B[0] + p - 1, TYd = sg.B[1] + p - 1, TZd = sg.B[2] + p - 1;
-  const size_t tsize = (size_t)TXd * TYd * TZd;
-  int bb[3][2], tc[3][2], nbr[3];
-  for (int d = 0; d < 3; ++d) {
-    const int B = sg.B[d];
-    const int b0 = gg[d] / B;
-    bb[d][0] = b0;
-    tc[d][0] = gg[d] - b0 * B + p - 1;
-    nbr[d] = 1;
-    const int t1 = gg[d] - (b0 + 1) * B + p - 1;
-    if (t1 >= 0) { bb[d][1] = (b0 + 1) % sg.nb[d]; tc[d][1] = t1; nbr[d] = 2; }
-  }
-  long long s = 0;
-  for (int cz = 0; cz < nbr[2]; ++cz)
-    for (int cy = 0; cy < nbr[1]; ++cy)
-      for (int cx = 0; cx < nbr[0]; ++cx) {
-        const int b = bb[0][cx] + sg.nb[0] * (bb[1][cy] + sg.nb[1] * bb[2][cz]);
-        s += ext[(size_t)b * tsize + ((size_t)tc[2][cz] * TYd + tc[1][cy]) * TXd + tc[0][cx]];
-      }
-  Q[gid] = (float)s * 9.094947017729282e-13f;  // 2^-40
-  (void)TZd;
+  const int gx = blockIdx.x * blockDim.x + threadIdx.x, gy = blockIdx.y, gz = blockIdx.z;
+  if (gx >= sg.K[0]) return;
+  const long long s = tile_sum<long long, long long>(sg, ext, gx, gy, gz);
+  Q[((size_t)gz * sg.K[1] + gy) * sg.K[0] + gx] = (float)s * 9.094947017729282e-13f;  // 2^-40
 }
 
-// Halo reduction: every grid point sums, in a fixed order, the tile entries of
-// the (at most 2 per dimension) bricks whose tiles cover it.
 template <typename T>
 __global__ void k_spme_tile_reduce(SpmeGeom sg, const T* __restrict__ ext, T* __restrict__ Q) {
-  const size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
-  if (gid >= (size_t)K0 * K1 * K2) return;
-  const int gx = (int)(gid % K0), gy = (int)((gid / K0) % K1), gz = (int)(gid / ((size_t)K0 * K1));
-  const int p = sg.p;
-  const int TXd = sg.B[0] + p - 1, TYd = sg.B[1] + p - 1, TZd = sg.B[2] + p - 1;
-  const size_t tsize = (size_t)TXd * TYd * TZd;
-  int bb[3][2], tc[3][2], nbr[3];
-  const int gg[3] = {gx, gy, gz};
-  for (int d = 0; d < 3; ++d) {
-    const int B = sg.B[d];
-    const int b0 = gg[d] / B;
-    bb[d][0] = b0;
-    tc[d][0] = gg[d] - b0 * B + p - 1;
-    nbr[d] = 1;
-    const int t1 = gg[d] - (b0 + 1) * B + p - 1;
-    if (t1 >= 0) {
-      bb[d][1] = (b0 + 1) % sg.nb[d];
-      tc[d][1] = t1;
-      nbr[d] = 2;
-    }
-  }
-  T s = (T)0;
-  for (int cz = 0; cz < nbr[2]; ++cz)
-    for (int cy = 0; cy < nbr[1]; ++cy)
-      for (int cx = 0; cx < nbr[0]; ++cx) {
-        const int b = bb[0][cx] + sg.nb[0] * (bb[1][cy] + sg.nb[1] * bb[2][cz]);
-        s += ext[(size_t)b * tsize + ((size_t)tc[2][cz] * TYd + tc[1][cy]) * TXd + tc[0][cx]];
-      }
-  Q[gid] = s;
+  const int gx = blockIdx.x * blockDim.x + threadIdx.x, gy = blockIdx.y, gz = blockIdx.z;
+  if (gx >= sg.K[0]) return;
+  Q[((size_t)gz * sg.K[1] + gy) * sg.K[0] + gx] = tile_sum<T, T>(sg, ext, gx, gy, gz);
 }
 
 inline size_t spread_smem(int B0, int B1, int B2, int p, size_t esz) {
@@ -509,14 +496,19 @@ __global__ void __launch_bounds__(256) k_spme_gather_wdf(int natms, SpmeGeom sg,
         int xx = gx + j; if (xx >= K0) xx -= K0;
         int yy = gy + k; if (yy >= K1) yy -= K1;
         const dfr* col = phi + (size_t)yy * K0 + xx;
-        dfr ca, cc;
+        // the z column as two compensated dot products: each exact product's high
+        // part enters a two-sum, its error and cross terms the correction, and the
+        // pair is renormalised once per column
+        dacc za, zc;
+        za.s = za.c = zc.s = zc.c = 0.f;
 #pragma unroll
         for (int l = 0; l < P; ++l) {
           int zz = gz + l; if (zz >= K2) zz -= K2;
-          const dfr ph = col[(size_t)zz * K1 * K0];
-          ca = fma(sp[wid][a][0][2][l], ph, ca);
-          cc = fma(sp[wid][a][1][2][l], ph, cc);
+          const df ph = to_df(col[(size_t)zz * K1 * K0]);
+          dacc_add_prod(za, to_df(sp[wid][a][0][2][l]), ph);
+          dacc_add_prod(zc, to_df(sp[wid][a][1][2][l]), ph);
         }
+        const dfr ca = to_dfr(two_sum(za.s, za.c)), cc = to_dfr(two_sum(zc.s, zc.c));
         const dfr mx = sp[wid][a][0][0][j], dmx = sp[wid][a][1][0][j];
         const dfr my = sp[wid][a][0][1][k], dmy = sp[wid][a][1][1][k];
         const dfr w0 = mx * my;
@@ -981,12 +973,14 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
     T* ext = reinterpret_cast<T*>(S.spread_ext);
     const size_t smem = spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(T));
     const size_t NG = (size_t)K1 * K2 * K3;
+    const int red_nt = std::min(256, (K1 + 31) / 32 * 32);  // halo reduction: x in the block, y and z in the grid
+    const dim3 red_grid((unsigned)nblocks(K1, red_nt), (unsigned)K2, (unsigned)K3);
     prof_begin(pid(P_SPME_SPREAD));
     if (F64) {
       auto spread = p == 8 ? k_spme_spread_tile<T, 8> : k_spme_spread_tile<T, 0>;
       spread<<<S.nbricks, SPREAD_NT, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge, ext);
       GB_LAUNCHED();
-      k_spme_tile_reduce<T><<<nblocks((long long)NG, 256), 256, 0, st>>>(S.sg, ext, Q);
+      k_spme_tile_reduce<T><<<red_grid, red_nt, 0, st>>>(S.sg, ext, Q);
       GB_LAUNCHED();
     } else {
       long long* exti = reinterpret_cast<long long*>(S.spread_ext);
@@ -995,7 +989,7 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
       kern<<<S.nbricks, 256, tsz * sizeof(long long), st>>>(S.sg, S.brick_start, S.brick_atoms,
                                                             reinterpret_cast<const float*>(spl), S.nidx, g.chge, exti);
       GB_LAUNCHED();
-      k_spme_tile_reduce_fix<<<nblocks((long long)NG, 256), 256, 0, st>>>(S.sg, exti, reinterpret_cast<float*>(Q));
+      k_spme_tile_reduce_fix<<<red_grid, red_nt, 0, st>>>(S.sg, exti, reinterpret_cast<float*>(Q));
       GB_LAUNCHED();
     }
     prof_end(pid(P_SPME_SPREAD));
