@@ -426,7 +426,7 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     dalloc(&g.xlo, mx);
     dalloc(&g.qdf, mx);
     dalloc(&g.fx, natms); dalloc(&g.fy, natms); dalloc(&g.fz, natms);
-    dalloc(&g.fixp, 3 * (size_t)natms);
+    dalloc(&g.fixp, 3 * (size_t)mx);  // the double-float pair kernel also holds halo-image forces here
     dalloc(&g.vx, natms); dalloc(&g.vy, natms); dalloc(&g.vz, natms);
     dalloc(&g.chge, mx); dalloc(&g.weight, mx);
     dalloc(&g.ltype, mx); dalloc(&g.ltg, mx); dalloc(&g.lfrzn, mx);

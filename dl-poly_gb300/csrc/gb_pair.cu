@@ -67,6 +67,7 @@ __device__ __forceinline__ void acc_store(double (&v)[NV], double* blk) {
 // --------------------------------------------------------------- FP64 form
 // accumulator layout per block: engvdw, virvdw, engrl, virrl, str(6)
 constexpr int NACC = 10;
+constexpr int NACC_DF = 4;  // the double-float kernel: energies and virials (stress from k_pair_stress_fix)
 
 __global__ void __launch_bounds__(256, 3) k_pair_fp64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
                                                    const int* __restrict__ list, int ld,
@@ -533,7 +534,7 @@ __device__ __forceinline__ void pair_terms_df64(const PairGeom& pg, int i, int j
                                                 const double* __restrict__ ecoef, const double* __restrict__ vcoef,
                                                 const int* __restrict__ vkind, const double* __restrict__ veps,
                                                 const double* __restrict__ vsig, int vstride,
-                                                unsigned long long* fixp, dacc (&acc)[NACC], long long& sx,
+                                                unsigned long long* fixp, dacc (&acc)[NACC_DF], long long& sx,
                                                 long long& sy, long long& sz, unsigned long long& n_rc) {
   const bool band = (rsq.hi >= pg.f_rc2_lo && rsq.hi <= pg.f_rc2_hi) ||
                     (rsq.hi >= pg.f_rv2_lo && rsq.hi <= pg.f_rv2_hi);
@@ -604,8 +605,6 @@ __device__ __forceinline__ void pair_terms_df64(const PairGeom& pg, int i, int j
   dacc_add_prod(acc[1], df_neg(gvv), rsq);
   dacc_add(acc[2], ee);
   dacc_add_prod(acc[3], df_neg(gvc), rsq);
-  dacc_add_prod(acc[4], dx, fxx); dacc_add_prod(acc[5], dx, fyy); dacc_add_prod(acc[6], dx, fzz);
-  dacc_add_prod(acc[7], dy, fyy); dacc_add_prod(acc[8], dy, fzz); dacc_add_prod(acc[9], dz, fzz);
 }
 
 __global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
@@ -623,9 +622,9 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const De
   __shared__ PairQueue pq[PAIR_DF_NT / 32];
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  dacc acc[NACC];
+  dacc acc[NACC_DF];
 #pragma unroll
-  for (int k = 0; k < NACC; ++k) { acc[k].s = 0.f; acc[k].c = 0.f; }
+  for (int k = 0; k < NACC_DF; ++k) { acc[k].s = 0.f; acc[k].c = 0.f; }
   unsigned long long n_list = 0, n_rc = 0;
   const int nlast = sc->nlast;
   const int vstride = (pg.max_grid + 3) * 3;  // float4 per key
@@ -687,7 +686,7 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const De
           const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
           const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
           const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
-          const int jf = j >= natms ? src[j] : j;
+          const int jf = j;  // an image's force stays in its own slot until k_fold_images
           const float2 qj2 = qdf[j];
           pair_terms_df64(pg, i, j, jf, ai, aj, qi, qi_on, qj2, dx, dy, dz, rsq, x, y, z, q, etab, vtab, ecoef,
                           vcoef, vkind, veps, vsig, vstride, fixp, acc, sx, sy, sz, n_rc);
@@ -710,15 +709,48 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const De
       n_list += (unsigned long long)n;
     }
   }
-  dfr out[NACC];
+  dfr out[NACC_DF];
 #pragma unroll
-  for (int k = 0; k < NACC; ++k) out[k] = to_dfr(two_sum(acc[k].s, acc[k].c));
+  for (int k = 0; k < NACC_DF; ++k) out[k] = to_dfr(two_sum(acc[k].s, acc[k].c));
   n_rc = (unsigned long long)warp_sumi((int)n_rc);
   if (lane == 0) {
     atomicAdd(&cnt[0], n_list);
     atomicAdd(&cnt[1], n_rc);
   }
-  block_reduce_store<NACC>(out, blk);
+  block_reduce_store<NACC_DF>(out, blk);
+}
+
+// Pair stress of the double-float kernel from its per-slot forces: with every image's
+// force kept in the image's own slot, sum over pairs of d (x) f = sum over slots of
+// x (x) F (each pair's f enters its two slots with opposite signs, and d is the
+// difference of the two slots' positions), summed in FP64 from the exact fixed-point
+// forces.  Components xx, xy, xz, yy, yz, zz, as the per-pair sums of the FP64 kernels.
+__global__ void k_pair_stress_fix(const DevScalars* sc, const double* __restrict__ x, const double* __restrict__ y,
+                                  const double* __restrict__ z, const long long* __restrict__ fixp, double* blk) {
+  const int nlast = sc->nlast;
+  const double s = 1.0 / 1099511627776.0;
+  double st[6] = {0, 0, 0, 0, 0, 0};
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nlast; a += gridDim.x * blockDim.x) {
+    const double fa = (double)fixp[3 * a] * s, fb = (double)fixp[3 * a + 1] * s, fc = (double)fixp[3 * a + 2] * s;
+    const double xa = x[a], ya = y[a], za = z[a];
+    st[0] = fma(xa, fa, st[0]); st[1] = fma(xa, fb, st[1]); st[2] = fma(xa, fc, st[2]);
+    st[3] = fma(ya, fb, st[3]); st[4] = fma(ya, fc, st[4]); st[5] = fma(za, fc, st[5]);
+  }
+  block_reduce_store<6>(st, blk);
+}
+
+// image forces of the double-float kernel onto their source atoms (integer sums:
+// the order of the atomics does not matter)
+__global__ void k_fold_images(int natms, const DevScalars* sc, const int* __restrict__ src,
+                              unsigned long long* fixp) {
+  const int h = natms + blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= sc->nlast) return;
+  const int i = src[h];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const unsigned long long v = fixp[3 * h + c];
+    if (v) atomicAdd(&fixp[3 * i + c], v);
+  }
 }
 
 // FP64 form: forces of the other terms are in fx; add the double-float pair kernel's
@@ -777,17 +809,26 @@ void pair_forces(double* eng6, double* stress9) {
     static int occdf = 0;
     if (!occdf) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occdf, k_pair_df64, PAIR_DF_NT, 0));
     int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, PAIR_DF_NT), occdf * g.nsm));
-    double* blk = gb_blkacc(nb * NACC + nb2 * 8);
-    GB_CUDA(cudaMemsetAsync(g.fixp, 0, sizeof(long long) * 3 * (size_t)g.natms, st));
+    const int nbs = std::max(1, std::min(nblocks(g.mxatms, 256), 4 * g.nsm));  // stress blocks
+    double* blk = gb_blkacc(nb * NACC + nb2 * 8 + nbs * 6);
+    double* blks = blk + (size_t)nb * NACC + (size_t)nb2 * 8;
+    // local atoms and halo images: an image's force is folded onto its source after the stress sum
+    GB_CUDA(cudaMemsetAsync(g.fixp, 0, sizeof(long long) * 3 * (size_t)g.mxatms, st));
     prof_begin(P_PAIR);
     k_pair_df64<<<nb, PAIR_DF_NT, 0, st>>>(g.natms, g.sc, g.at_list, g.list, g.ld, g.xf, g.xlo, g.qdf, g.x, g.y, g.z, g.chge,
                                   g.ltg, g.src, g.erfc_df, g.vdw_df, g.erfc_coef, g.vdw_coef, g.vdw_kind, g.vdw_eps,
                                   g.vdw_sig, pg, (unsigned long long*)g.fixp, blk, &g.sc->npairs_list);
     GB_LAUNCHED();
+    k_pair_stress_fix<<<nbs, 256, 0, st>>>(g.sc, g.x, g.y, g.z, g.fixp, blks);
+    GB_LAUNCHED();
+    k_fold_images<<<std::max(1, nblocks(g.mxatms - g.natms, 256)), 256, 0, st>>>(g.natms, g.sc, g.src,
+                                                                    (unsigned long long*)g.fixp);
+    GB_LAUNCHED();
     k_fix_add_fp64<<<nblocks(g.natms, 256), 256, 0, st>>>(g.natms, g.fixp, g.fx, g.fy, g.fz);
     GB_LAUNCHED();
     prof_end(P_PAIR);
-    gb_reduce_blocks(blk, nb, NACC, &g.sc->acc[A_PAIR]);
+    gb_reduce_blocks(blk, nb, NACC_DF, &g.sc->acc[A_PAIR]);
+    gb_reduce_blocks(blks, nbs, 6, &g.sc->acc[A_PAIR + NACC_DF]);
     if (g.lbook) {
       double* blk2 = blk + (size_t)nb * NACC;
       prof_begin(P_EXCL);
