@@ -18,6 +18,7 @@
 // pair forces as int64 fixed point (scale 2^40), the reaction on j with 64-bit
 // integer atomics: order independent and bit-reproducible.
 #include <cfloat>
+#include <cmath>
 #include <cstring>
 
 #include "gb_common.cuh"
@@ -40,6 +41,7 @@ struct PairGeom {
   // double-float kernel: cutoff bands on the FP32 high part of r^2 (1e-6 relative) and
   // the table spacings as double-floats
   float f_rc2_lo, f_rc2_hi, f_rv2_lo, f_rv2_hi, f_hi;
+  float f_pre;  // FP32 prefilter on the high parts: f_hi plus a bound on their rounding
   float erdr_hi, erdr_lo, vrdr_hi, vrdr_lo, scal_hi, scal_lo;
 };
 
@@ -520,7 +522,6 @@ __device__ __forceinline__ int table_coord(df rrr, float sh, float sl, df* d) {
 // per-warp queue of pairs inside the outer cutoff: neighbour index and double-float r^2
 struct PairQueue {
   int j[64];
-  float rh[64], rl[64];
 };
 constexpr int PAIR_DF_NT = 256;  // threads of a k_pair_df64 CTA
 
@@ -639,9 +640,11 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const De
     const int* lst = list + (size_t)i * ld + 3;
     const int n = lst[0];
     long long sx = 0, sy = 0, sz = 0;
-    // Pass 1 over 32 entries at a time: separation and r^2; the entries inside the outer
-    // cutoff join this warp's queue (ballot compaction), so pass 2, the pair terms, runs
-    // on 32 queued pairs at a time with every lane busy.  The queue holds < 64 pairs.
+    // Pass 1 over 32 entries at a time: an FP32 r^2 of the coordinates' high parts, with
+    // a bound on their rounding added to the outer cutoff, so that every entry inside
+    // the cutoff (and a few just outside) joins this warp's queue (ballot compaction).
+    // Pass 2, the exact separation and the pair terms, runs on 32 queued pairs at a
+    // time with every lane busy.  The queue holds < 64 pairs.
     int nq = 0;  // queued pairs (uniform over the warp)
     for (int base = 0;; base += 32) {
       const bool more = base < n;
@@ -649,25 +652,18 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const De
         const int m = base + lane + 1;
         bool keep = false;
         int j = 0;
-        df dx, dy, dz, rsq;
         if (m <= n) {
           j = lst[m] - 1;
           if (j < natms || gi <= ltg[j]) {  // halo pairs are evaluated from the smaller id
-            const float4 pj = xf[j], lj = xlo[j];
-            // separation: exact difference of the high parts plus the difference of the low parts
-            const df ex = two_sum(pi.x, -pj.x), ey = two_sum(pi.y, -pj.y), ez = two_sum(pi.z, -pj.z);
-            dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
-            dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
-            dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
-            rsq = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
-            keep = rsq.hi <= pg.f_hi;
+            const float4 pj = xf[j];
+            const float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
+            keep = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= pg.f_pre;
           }
         }
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         if (keep) {
           const int slot = nq + __popc(bal & ((1u << lane) - 1u));
-          PairQueue& Q = pq[wq];
-          Q.j[slot] = j; Q.rh[slot] = rsq.hi; Q.rl[slot] = rsq.lo;
+          pq[wq].j[slot] = j;
         }
         nq += __popc(bal);
         __syncwarp();
@@ -676,20 +672,21 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const De
         const int take = min(nq, 32);
         const int slot = nq - take + lane;
         if (lane < take) {
-          const PairQueue& Q = pq[wq];
-          const int j = Q.j[slot];
-          const df rsq = df_make(Q.rh[slot], Q.rl[slot]);
-          // the separation again (the same operations as pass 1, so the same value)
+          const int j = pq[wq].j[slot];
+          // separation: exact difference of the high parts plus the difference of the low parts
           const float4 pj = xf[j], lj = xlo[j];
           const int aj = __float_as_int(lj.w);
           const df ex = two_sum(pi.x, -pj.x), ey = two_sum(pi.y, -pj.y), ez = two_sum(pi.z, -pj.z);
           const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
           const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
           const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
-          const int jf = j;  // an image's force stays in its own slot until k_fold_images
-          const float2 qj2 = qdf[j];
-          pair_terms_df64(pg, i, j, jf, ai, aj, qi, qi_on, qj2, dx, dy, dz, rsq, x, y, z, q, etab, vtab, ecoef,
-                          vcoef, vkind, veps, vsig, vstride, fixp, acc, sx, sy, sz, n_rc);
+          const df rsq = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+          if (rsq.hi <= pg.f_hi) {
+            const int jf = j;  // an image's force stays in its own slot until k_fold_images
+            const float2 qj2 = qdf[j];
+            pair_terms_df64(pg, i, j, jf, ai, aj, qi, qi_on, qj2, dx, dy, dz, rsq, x, y, z, q, etab, vtab, ecoef,
+                            vcoef, vkind, veps, vsig, vstride, fixp, acc, sx, sy, sz, n_rc);
+          }
         }
         nq -= take;
         __syncwarp();  // the taken slots are read before the next pass appends over them
@@ -803,6 +800,22 @@ void pair_forces(double* eng6, double* stress9) {
     pg.f_rv2_lo = (float)(pg.rv2 * (1.0 - 1e-6));
     pg.f_rv2_hi = (float)(pg.rv2 * (1.0 + 1e-6));
     pg.f_hi = std::max(pg.f_rc2_hi, pg.f_rv2_hi);
+    {
+      // |x - (float)x| <= u for every coordinate: R = twice the summed cell-vector
+      // lengths bounds the local atoms (reduced coordinates within +-(1/2 + drift)) and
+      // their halo images (the halo is under half a cell wide)
+      double R = 0.0;
+      for (int v = 0; v < 3; ++v)
+        R += std::sqrt(g.cell[3 * v] * g.cell[3 * v] + g.cell[3 * v + 1] * g.cell[3 * v + 1] +
+                       g.cell[3 * v + 2] * g.cell[3 * v + 2]);
+      R *= 2.0;
+      const double u = std::ldexp(1.0, std::ilogb(R) - 23);
+      const double eps = std::ldexp(1.0, -23);
+      const double D = std::sqrt((double)pg.f_hi) + 1.0;
+      const double dlt = 2.0 * u + eps * (D + 2.0 * u);  // error of a separation component
+      const double band = 4.0 * (2.0 * std::sqrt(3.0) * D * dlt + 3.0 * dlt * dlt) + 8.0 * eps * D * D;
+      pg.f_pre = std::nextafter((float)((double)pg.f_hi + band), 3.0e38f);
+    }
     df_split(pg.erdr, &pg.erdr_hi, &pg.erdr_lo);
     df_split(pg.vrdr, &pg.vrdr_hi, &pg.vrdr_lo);
     df_split(pg.scaling, &pg.scal_hi, &pg.scal_lo);
