@@ -608,7 +608,7 @@ __device__ __forceinline__ void pair_terms_df64(const PairGeom& pg, int i, int j
   dacc_add_prod(acc[3], df_neg(gvc), rsq);
 }
 
-__global__ void __launch_bounds__(PAIR_DF_NT, 3) k_pair_df64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
+__global__ void __launch_bounds__(PAIR_DF_NT, 4) k_pair_df64(int natms, const DevScalars* sc, const int* __restrict__ at_list,
                                                    const int* __restrict__ list, int ld,
                                                    const float4* __restrict__ xf, const float4* __restrict__ xlo,
                                                    const float2* __restrict__ qdf, const double* __restrict__ x,
