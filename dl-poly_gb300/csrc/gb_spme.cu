@@ -290,13 +290,25 @@ __device__ __forceinline__ S tile_sum(const SpmeGeom& sg, const T* __restrict__ 
   const TileCover cx = tile_cover(gx, sg.B[0], p, sg.nb[0]);
   const TileCover cy = tile_cover(gy, sg.B[1], p, sg.nb[1]);
   const TileCover cz = tile_cover(gz, sg.B[2], p, sg.nb[2]);
-  S s = (S)0;
-  for (int iz = 0; iz < cz.n; ++iz)
-    for (int iy = 0; iy < cy.n; ++iy)
-      for (int ix = 0; ix < cx.n; ++ix) {
-        const int b = cx.b[ix] + sg.nb[0] * (cy.b[iy] + sg.nb[1] * cz.b[iz]);
-        s += ext[(size_t)b * tsize + ((size_t)cz.t[iz] * TYd + cy.t[iy]) * TXd + cx.t[ix]];
+  // all (up to 8) covering entries are loaded before the sum; absent ones are zero,
+  // and adding an exact zero leaves the sum unchanged, so the order of the others holds
+  T v[8];
+#pragma unroll
+  for (int iz = 0; iz < 2; ++iz)
+#pragma unroll
+    for (int iy = 0; iy < 2; ++iy)
+#pragma unroll
+      for (int ix = 0; ix < 2; ++ix) {
+        T e = (T)0;
+        if (iz < cz.n && iy < cy.n && ix < cx.n) {
+          const int b = cx.b[ix] + sg.nb[0] * (cy.b[iy] + sg.nb[1] * cz.b[iz]);
+          e = ext[(size_t)b * tsize + ((size_t)cz.t[iz] * TYd + cy.t[iy]) * TXd + cx.t[ix]];
+        }
+        v[(iz * 2 + iy) * 2 + ix] = e;
       }
+  S s = (S)0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += v[k];
   return s;
 }
 
