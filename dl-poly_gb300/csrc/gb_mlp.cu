@@ -53,7 +53,6 @@ constexpr int NRAD = 8;
 constexpr float RCUT_DESC = 6.0f, GAUSS_W = 0.45f, GAUSS_MU0 = 0.5f;
 constexpr int TILE_I = 64;  // atoms per inference tile (4 warps x 16)
 constexpr int TILE_T = 32;  // atoms per training CTA
-constexpr int DESC_WARPS = 8, DESC_BUF = 64;  // input kernel: atoms per CTA, compacted neighbours per warp
 // FP32 parameter vector: W1[NIN][NH], b1[NH], W2[NH][NH], b2[NH], W3[NH][NOUT], b3[NOUT]
 constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NIN * NH, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH,
               OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + NH * NOUT, NPARAM = OFF_B3 + NOUT;
@@ -85,7 +84,7 @@ struct MtsDev {
   long long scap = 0, gen_seen = -1;
   float* target = nullptr;     // labels (3n)
   double* x0 = nullptr;        // positions at t0 (3n)
-  float* disp = nullptr;       // displacement since t0 (3n)
+  float* disp = nullptr;       // displacement since t0 (3 per local atom and halo image)
   float* frame = nullptr;      // local frame rows e1,e2,e3 (9n)
   int* triple = nullptr;       // frame atoms (a,b,c) per atom, -1 = lab frame
   float* scal = nullptr;       // [0,NIN) input scales, [NIN] force scale
@@ -127,20 +126,23 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], 
 // ------------------------------------------------------------ per-step inputs
 // displacement since t0 (minimum image: atoms may have been wrapped since t0)
 // and the local frame of every atom
-__global__ void k_mts_prep(int n, const double* __restrict__ x, const double* __restrict__ y,
-                           const double* __restrict__ z, const double* __restrict__ x0, const int* __restrict__ tri,
-                           double cell, float* __restrict__ disp, float* __restrict__ frame) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+__global__ void k_mts_prep(int n, const DevScalars* sc, const int* __restrict__ src, const double* __restrict__ x,
+                           const double* __restrict__ y, const double* __restrict__ z, const double* __restrict__ x0,
+                           const int* __restrict__ tri, double cell, float* __restrict__ disp,
+                           float* __restrict__ frame) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= sc->nlast) return;
+  const int i = a < n ? a : src[a];  // a halo image moves with its source atom
   const float L = (float)cell, rL = (float)(1.0 / cell);
   float d0 = (float)(x[i] - x0[3 * i]), d1 = (float)(y[i] - x0[3 * i + 1]), d2 = (float)(z[i] - x0[3 * i + 2]);
   d0 -= L * rintf(d0 * rL); d1 -= L * rintf(d1 * rL); d2 -= L * rintf(d2 * rL);
-  disp[3 * i] = d0; disp[3 * i + 1] = d1; disp[3 * i + 2] = d2;
+  disp[3 * a] = d0; disp[3 * a + 1] = d1; disp[3 * a + 2] = d2;
+  if (a >= n) return;
   float e[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-  const int a = tri[3 * i], b = tri[3 * i + 1], c = tri[3 * i + 2];
-  if (a >= 0) {
-    float bx = (float)(x[b] - x[a]), by = (float)(y[b] - y[a]), bz = (float)(z[b] - z[a]);
-    float cx = (float)(x[c] - x[a]), cy = (float)(y[c] - y[a]), cz = (float)(z[c] - z[a]);
+  const int ta = tri[3 * i], b = tri[3 * i + 1], c = tri[3 * i + 2];
+  if (ta >= 0) {
+    float bx = (float)(x[b] - x[ta]), by = (float)(y[b] - y[ta]), bz = (float)(z[b] - z[ta]);
+    float cx = (float)(x[c] - x[ta]), cy = (float)(y[c] - y[ta]), cz = (float)(z[c] - z[ta]);
     bx -= L * rintf(bx * rL); by -= L * rintf(by * rL); bz -= L * rintf(bz * rL);
     cx -= L * rintf(cx * rL); cy -= L * rintf(cy * rL); cz -= L * rintf(cz * rL);
     float e1x = bx + cx, e1y = by + cy, e1z = bz + cz;
@@ -228,21 +230,16 @@ __global__ void __launch_bounds__(256) k_short_fill(int n, const int* __restrict
   }
 }
 
-// inputs: one warp per atom over its short neighbour list (local and halo j)
-__global__ void __launch_bounds__(256) k_mts_desc(int n, const int* __restrict__ fstart, const int* __restrict__ fcount,
-                                                  const int* __restrict__ flist, const int* __restrict__ src,
-                                                  const float4* __restrict__ xf, const float* __restrict__ disp,
+// inputs: one thread per atom over its short neighbour list (local and halo j), in
+// the list's (index-sorted) order, so every sum has a fixed order; the 48 sums stay in
+// registers and are rotated into the atom's local frame at the end
+__global__ void __launch_bounds__(128) k_mts_desc(int n, const int* __restrict__ fstart, const int* __restrict__ fcount,
+                                                  const int* __restrict__ flist, const float4* __restrict__ xf,
+                                                  const float* __restrict__ disp,
                                                   const float* __restrict__ frame, const float* __restrict__ frec0,
                                                   const float* __restrict__ scal, __nv_bfloat16* __restrict__ X) {
-  // Neighbours inside 6 A (about a tenth of the list) are compacted per warp
-  // into shared memory with a ballot, so the Gaussian work runs on full warps;
-  // the 48 per-lane sums are then reduced by a transposing butterfly (48
-  // shuffles instead of 48 x 5), after which lane pairs own one xyz triple.
-  __shared__ float4 s_r[DESC_WARPS][DESC_BUF];  // dx, dy, dz, q_j
-  __shared__ float4 s_u[DESC_WARPS][DESC_BUF];  // u = d_j - d_i
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * DESC_WARPS + w;
-  if (i >= n) return;  // the whole warp leaves; no block-wide barrier below
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
   const float4 pi = xf[i];
   const float dix = disp[3 * i], diy = disp[3 * i + 1], diz = disp[3 * i + 2];
   float v[6 * NRAD];
@@ -251,96 +248,64 @@ __global__ void __launch_bounds__(256) k_mts_desc(int n, const int* __restrict__
   const float rc2 = RCUT_DESC * RCUT_DESC;
   const float dmu = (RCUT_DESC - GAUSS_MU0) / (float)(NRAD - 1), c2 = 1.0f / (2.0f * GAUSS_W * GAUSS_W);
   const float qi = pi.w;
-  auto accumulate = [&](const float4 rr, const float4 uu) {
-    const float r2 = rr.x * rr.x + rr.y * rr.y + rr.z * rr.z;
-    const float rinv = rsqrtf(r2), r = r2 * rinv;
-    const float wt = qi * rr.w * 0.5f * (1.0f + __cosf(3.14159265f * r * (1.0f / RCUT_DESC)));
-    const float hx = rr.x * rinv, hy = rr.y * rinv, hz = rr.z * rinv;
-    const float pu = hx * uu.x + hy * uu.y + hz * uu.z;
-    const float bx = pu * hx, by = pu * hy, bz = pu * hz;
-#pragma unroll
-    for (int k = 0; k < NRAD; ++k) {
-      const float t = r - (GAUSS_MU0 + dmu * (float)k);
-      const float gk = wt * __expf(-t * t * c2);
-      v[6 * k + 0] = fmaf(gk, uu.x, v[6 * k + 0]);
-      v[6 * k + 1] = fmaf(gk, uu.y, v[6 * k + 1]);
-      v[6 * k + 2] = fmaf(gk, uu.z, v[6 * k + 2]);
-      v[6 * k + 3] = fmaf(gk, bx, v[6 * k + 3]);
-      v[6 * k + 4] = fmaf(gk, by, v[6 * k + 4]);
-      v[6 * k + 5] = fmaf(gk, bz, v[6 * k + 5]);
-    }
-  };
   const int st = fstart[i], cnt = fcount[i];
-  const unsigned lt_mask = (1u << lane) - 1u;
-  int pending = 0;
-  for (int base = 0; base < cnt; base += 32) {
-    const int m = base + lane;
-    bool pass = false;
-    float4 rr = make_float4(0.f, 0.f, 0.f, 0.f), uu = rr;
-    if (m < cnt) {
-      const int j = flist[st + m];
-      const float4 pj = xf[j];
-      rr = make_float4(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z, pj.w);
-      const float r2 = rr.x * rr.x + rr.y * rr.y + rr.z * rr.z;
-      pass = r2 < rc2 && r2 > 0.f;
-      if (pass) {
-        const int js = src[j];
-        uu = make_float4(disp[3 * js] - dix, disp[3 * js + 1] - diy, disp[3 * js + 2] - diz, 0.f);
+  // four entries at a time: their indices, then their positions and displacements,
+  // are loaded before any is used (independent loads in flight)
+  for (int m0 = 0; m0 < cnt; m0 += 4) {
+    int jj[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) jj[u] = m0 + u < cnt ? flist[st + m0 + u] : i;
+    float4 pp[4];
+    float dd[4][3];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      pp[u] = xf[jj[u]];
+      dd[u][0] = disp[3 * jj[u]]; dd[u][1] = disp[3 * jj[u] + 1]; dd[u][2] = disp[3 * jj[u] + 2];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float rx = pp[u].x - pi.x, ry = pp[u].y - pi.y, rz = pp[u].z - pi.z;
+      const float r2 = rx * rx + ry * ry + rz * rz;
+      if (!(r2 < rc2 && r2 > 0.f)) continue;  // the padding entries (j = i) have r2 = 0
+      const float ux = dd[u][0] - dix, uy = dd[u][1] - diy, uz = dd[u][2] - diz;
+      const float rinv = rsqrtf(r2), r = r2 * rinv;
+      const float wt = qi * pp[u].w * 0.5f * (1.0f + __cosf(3.14159265f * r * (1.0f / RCUT_DESC)));
+      const float hx = rx * rinv, hy = ry * rinv, hz = rz * rinv;
+      const float pu = hx * ux + hy * uy + hz * uz;
+      const float bx = pu * hx, by = pu * hy, bz = pu * hz;
+#pragma unroll
+      for (int k = 0; k < NRAD; ++k) {
+        const float t = r - (GAUSS_MU0 + dmu * (float)k);
+        const float gk = wt * __expf(-t * t * c2);
+        v[6 * k + 0] = fmaf(gk, ux, v[6 * k + 0]);
+        v[6 * k + 1] = fmaf(gk, uy, v[6 * k + 1]);
+        v[6 * k + 2] = fmaf(gk, uz, v[6 * k + 2]);
+        v[6 * k + 3] = fmaf(gk, bx, v[6 * k + 3]);
+        v[6 * k + 4] = fmaf(gk, by, v[6 * k + 4]);
+        v[6 * k + 5] = fmaf(gk, bz, v[6 * k + 5]);
       }
     }
-    const unsigned b = __ballot_sync(0xffffffffu, pass);
-    if (pass) {
-      const int pos = pending + __popc(b & lt_mask);  // < 63: pending < 32 before every batch
-      s_r[w][pos] = rr;
-      s_u[w][pos] = uu;
-    }
-    pending += __popc(b);
-    __syncwarp();
-    if (pending >= 32) {
-      accumulate(s_r[w][lane], s_u[w][lane]);
-      const int rest = pending - 32;
-      float4 r2v = make_float4(0.f, 0.f, 0.f, 0.f), u2v = r2v;
-      if (lane < rest) { r2v = s_r[w][32 + lane]; u2v = s_u[w][32 + lane]; }
-      __syncwarp();
-      if (lane < rest) { s_r[w][lane] = r2v; s_u[w][lane] = u2v; }
-      pending = rest;
-      __syncwarp();
-    }
   }
-  if (lane < pending) accumulate(s_r[w][lane], s_u[w][lane]);
-  // transposing butterfly: 48 -> 24 -> 12 -> 6 -> 3 values per lane
+  // triple t = 2k holds A_k = sum g_k u, t = 2k + 1 holds B_k = sum g_k r^(r^.u); each
+  // goes out in the local frame
+  float e[9];
 #pragma unroll
-  for (int h = 24, o = 16; h >= 3; h >>= 1, o >>= 1) {
-    const bool up = (lane & o) != 0;
-#pragma unroll
-    for (int k = 0; k < h; ++k) {
-      const float keep = up ? v[h + k] : v[k];
-      const float send = up ? v[k] : v[h + k];
-      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], 1);
-  // lane owns triple t = 8 b4 + 4 b3 + 2 b2 + b1 (values 3t..3t+2: A_k for
-  // even t, B_k for odd t, k = t / 2); even lanes write it in the local frame
-  const int t = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
-  const float* e = frame + 9 * (size_t)i;
+  for (int k = 0; k < 9; ++k) e[k] = frame[9 * (size_t)i + k];
   __nv_bfloat16* xo = X + (size_t)i * KIN;
-  if ((lane & 1) == 0) {
+#pragma unroll
+  for (int t = 0; t < 2 * NRAD; ++t) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const float val = e[3 * c] * v[0] + e[3 * c + 1] * v[1] + e[3 * c + 2] * v[2];
+      const float val = e[3 * c] * v[3 * t] + e[3 * c + 1] * v[3 * t + 1] + e[3 * c + 2] * v[3 * t + 2];
       xo[3 * t + c] = __float2bfloat16(val * scal[3 * t + c]);
     }
-  } else if (lane == 1) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const float val = e[3 * c] * frec0[3 * i] + e[3 * c + 1] * frec0[3 * i + 1] + e[3 * c + 2] * frec0[3 * i + 2];
-      xo[6 * NRAD + c] = __float2bfloat16(val * scal[6 * NRAD + c]);
-    }
-  } else if (lane == 3) {
-    for (int c = NIN; c < KIN; ++c) xo[c] = __float2bfloat16(0.f);
   }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float val = e[3 * c] * frec0[3 * i] + e[3 * c + 1] * frec0[3 * i + 1] + e[3 * c + 2] * frec0[3 * i + 2];
+    xo[6 * NRAD + c] = __float2bfloat16(val * scal[6 * NRAD + c]);
+  }
+  for (int c = NIN; c < KIN; ++c) xo[c] = __float2bfloat16(0.f);
 }
 
 // ------------------------------------------------------------ inference (mma)
@@ -822,9 +787,10 @@ void mts_inputs() {
     prof_end(P_FULLLIST);
   }
   if (M.gen_seen != g.list_gen) mts_short_list();
-  k_mts_prep<<<nblocks(n, 256), 256, 0, g.stream>>>(n, g.x, g.y, g.z, M.x0, M.triple, g.cell[0], M.disp, M.frame);
+  k_mts_prep<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(n, g.sc, g.src, g.x, g.y, g.z, M.x0, M.triple, g.cell[0],
+                                                             M.disp, M.frame);
   GB_LAUNCHED();
-  k_mts_desc<<<nblocks(n, DESC_WARPS), DESC_WARPS * 32, 0, g.stream>>>(n, M.sstart, M.scount, M.slist, g.src, g.xf,
+  k_mts_desc<<<nblocks(n, 128), 128, 0, g.stream>>>(n, M.sstart, M.scount, M.slist, g.xf,
                                                                         M.disp, M.frame, M.frec0, M.scal, M.X);
   GB_LAUNCHED();
   prof_end(P_MTS_DESC);
@@ -974,8 +940,9 @@ void mts_setup() {
   GB_CUDA(cudaMalloc(&M.loss_part, sizeof(float) * M.gpart_tiles));
   net_alloc(M.net);
   GB_CUDA(cudaMalloc(&M.X, sizeof(__nv_bfloat16) * KIN * (size_t)n));
-  for (float** p : {&M.frec0, &M.frec, &M.truth, &M.target, &M.disp, &M.fc, &M.fc0})
+  for (float** p : {&M.frec0, &M.frec, &M.truth, &M.target, &M.fc, &M.fc0})
     GB_CUDA(cudaMalloc(p, sizeof(float) * 3 * (size_t)n));
+  GB_CUDA(cudaMalloc(&M.disp, sizeof(float) * 3 * (size_t)g.mxatms));  // local atoms and halo images
   // coarse grid: about half the main grid's points per dimension, order 6
   for (int d = 0; d < 3; ++d) M.Kc[d] = coarse_length((g.p.kmax[d] + 1) / 2);
   M.pc = 6;

@@ -128,16 +128,26 @@ __global__ void k_spme_prep(int natms, const double* __restrict__ x, const doubl
     gq[i] = make_float2(h, l);
   }
   brick_of[i] = b;
-  if (b >= 0) atomicAdd(&brick_count[b], 1);
+  // the lanes of a warp that share a brick add their count with one atomic (atoms of
+  // nearby index are near each other in the lattice start); counts are order-independent
+  const unsigned grp = __match_any_sync(__activemask(), b);
+  if (b >= 0 && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&brick_count[b], __popc(grp));
 }
 
+// atoms into their bricks' ranges; the lanes of a warp that share a brick take
+// consecutive slots with one atomic
 __global__ void k_brick_scatter(int natms, const int* brick_of, const int* start, int* fill, int* tmp) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natms) return;
-  int b = brick_of[i];
+  const int b = brick_of[i];
+  const int lane = threadIdx.x & 31;
+  const unsigned grp = __match_any_sync(__activemask(), b);
+  const int leader = __ffs(grp) - 1;
+  int base = 0;
+  if (b >= 0 && lane == leader) base = atomicAdd(&fill[b], __popc(grp));
+  base = __shfl_sync(grp, base, leader);
   if (b < 0) return;
-  int s = atomicAdd(&fill[b], 1);
-  tmp[start[b] + s] = i;
+  tmp[start[b] + base + __popc(grp & ((1u << lane) - 1u))] = i;
 }
 
 __global__ void k_brick_sort(int nbricks, const int* start, const int* tmp, int* out) {
@@ -678,10 +688,12 @@ SpmeGrid S_main, S_coarse;
 
 // Brick edge: a divisor of K of at least p-1 (a brick's atoms reach at most the
 // next brick).  Larger bricks cut the halo overlap (B+p-1)^3 / B^3 of the tiles
-// the fixed-order reduction reads back, so prefer one of at least BPREF.
-constexpr int BPREF = 12;
-int choose_brick(int K, int p) {
-  for (int B = std::max(p - 1, BPREF); B <= BMAX; ++B)
+// the fixed-order reduction reads back, so prefer one of at least bpref (BPREF for
+// the force grid; the coarse grid of the multiple-time-step form, with 8x fewer
+// points, prefers BPREF_COARSE so that its bricks hold as few atoms and are as many).
+constexpr int BPREF = 12, BPREF_COARSE = 8;
+int choose_brick(int K, int p, int bpref) {
+  for (int B = std::max(p - 1, bpref); B <= BMAX; ++B)
     if (K % B == 0) return B;
   for (int B = p - 1; B <= BMAX; ++B)
     if (K % B == 0) return B;
@@ -747,7 +759,7 @@ void raise_fft(const SpmeGrid& S, int smem) {
   raise_smem(k.z_conv, smem);
 }
 
-void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
+void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64, int bpref) {
   grid_free(S);
   if (p > PMAX || p < 3) throw (int)GB_ERR_ARG;
   for (int d = 0; d < 3; ++d) S.K[d] = Kin[d];
@@ -758,7 +770,7 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64) {
   S.planh = make_plan(S.K[0] / 2);
   S.Kx = S.K[0] / 2 + 1;
   for (int d = 0; d < 3; ++d) {
-    S.B[d] = choose_brick(S.K[d], p);
+    S.B[d] = choose_brick(S.K[d], p, bpref);
     if (S.B[d] < 0) {
       // fall back to the whole dimension as one brick if it is small enough
       if (S.K[d] <= BMAX) S.B[d] = S.K[d];
@@ -974,11 +986,17 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   GB_LAUNCHED();
 
   scan_exclusive(S.brick_count, S.brick_start, S.nbricks + 1);
-  int* tmp = gb_scan_scratch(n + 1);
-  k_brick_scatter<<<nblocks(n, 256), 256, 0, st>>>(n, S.brick_of, S.brick_start, S.brick_fill, tmp);
-  GB_LAUNCHED();
-  k_brick_sort<<<nblocks((long long)S.nbricks * 32, 256), 256, 0, st>>>(S.nbricks, S.brick_start, tmp, S.brick_atoms);
-  GB_LAUNCHED();
+  if (F64) {  // the FP64 spread adds a brick's atoms in ascending index order
+    int* tmp = gb_scan_scratch(n + 1);
+    k_brick_scatter<<<nblocks(n, 256), 256, 0, st>>>(n, S.brick_of, S.brick_start, S.brick_fill, tmp);
+    GB_LAUNCHED();
+    k_brick_sort<<<nblocks((long long)S.nbricks * 32, 256), 256, 0, st>>>(S.nbricks, S.brick_start, tmp,
+                                                                          S.brick_atoms);
+    GB_LAUNCHED();
+  } else {  // fixed-point sums do not depend on the order of a brick's atoms
+    k_brick_scatter<<<nblocks(n, 256), 256, 0, st>>>(n, S.brick_of, S.brick_start, S.brick_fill, S.brick_atoms);
+    GB_LAUNCHED();
+  }
   prof_end(pid(P_SPME_PREP));
   // spreading: tile scatter per brick, then the fixed-order halo reduction
   {
@@ -1108,7 +1126,7 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
 
 }  // namespace
 
-void spme_setup() { grid_setup(S_main, g.p.kmax, g.p.nsplines, true); }
+void spme_setup() { grid_setup(S_main, g.p.kmax, g.p.nsplines, true, BPREF); }
 
 void spme_free() {
   grid_free(S_main);
@@ -1122,7 +1140,7 @@ void spme_forces(double* eng_rc, double* vir_rc, double* stress9) {
   else grid_run<float, float2>(S_main, false, rec, eng_rc, vir_rc, stress9);
 }
 
-void spme_coarse_setup(const int* K, int p) { grid_setup(S_coarse, K, p, false); }
+void spme_coarse_setup(const int* K, int p) { grid_setup(S_coarse, K, p, false, BPREF_COARSE); }
 
 bool spme_coarse_ready() { return S_coarse.ready; }
 
