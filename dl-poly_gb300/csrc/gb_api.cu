@@ -83,7 +83,7 @@ void free_all() {
   void* ptrs[] = {g.x, g.y, g.z, g.xf, g.xlo, g.fx, g.fy, g.fz, g.fixp, g.vx, g.vy, g.vz, g.chge, g.weight, g.ltype, g.ltg,
                   g.lfrzn, g.ixyz, g.src, g.shcode, g.xbg, g.ybg, g.zbg, g.ox, g.oy, g.oz, g.which_cell,
                   g.cell_count, g.cell_start, g.cell_fill, g.at_list, g.sorted_pos, g.xs, g.xsf, g.list, g.blk,
-                  g.list_excl, g.flist, g.fcount, g.fstart, g.erfc_coef, g.erfc_coef_f, g.vdw_coef, g.vdw_coef_f,
+                  g.list_excl, g.erfc_coef, g.erfc_coef_f, g.vdw_coef, g.vdw_coef_f,
                   g.vdw_kind, g.vdw_eps, g.vdw_sig, g.erfc_df, g.vdw_df, g.qdf, g.blkacc, g.con_i, g.con_j, g.con_d0, g.dxx, g.dyy,
                   g.dzz, g.dxt, g.dyt, g.dzt, g.dt2, g.gam, g.listot, g.acon_start, g.acon_list, g.sc, d_scratch};
   for (void* p : ptrs)
@@ -291,7 +291,7 @@ void invert_host(const double* a, double* b, double* d) {
 }
 
 // ----------------------------------------------------------- event timers
-static const char* kProfNames[P_NPROF] = {"halo",        "bin_sort",   "list_pairs", "full_list",  "pair_forces",
+static const char* kProfNames[P_NPROF] = {"halo",        "bin_sort",   "list_pairs", "short_list", "pair_forces",
                                           "excl_forces", "spme_prep",  "spme_spread", "fft_x_fwd", "fft_y",
                                           "fft_z_conv",  "fft_x_inv",  "spme_gather", "vv",        "shake",
                                           "rattle",      "mlp_infer",  "mts_inputs", "mlp_train",  "coarse_prep",
@@ -437,8 +437,6 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     dalloc(&g.xs, mx); dalloc(&g.xsf, mx);
     g.ld = prm->max_list + 4;
     dalloc(&g.list, (size_t)g.ld * natms);
-    dalloc(&g.fcount, natms + 1);
-    dalloc(&g.fstart, natms + 1);
     dalloc(&g.sc, 1);
     GB_CUDA(cudaMallocHost(&g.hsc, sizeof(DevScalars)));
     std::memset(g.hsc, 0, sizeof(DevScalars));

@@ -60,7 +60,7 @@ enum {
 
 // Kernel regions timed with CUDA events when profiling is on.
 enum ProfId {
-  P_HALO = 0, P_BIN, P_LIST, P_FULLLIST, P_PAIR, P_EXCL, P_SPME_PREP, P_SPME_SPREAD, P_FFT_XF, P_FFT_Y,
+  P_HALO = 0, P_BIN, P_LIST, P_SHORTLIST, P_PAIR, P_EXCL, P_SPME_PREP, P_SPME_SPREAD, P_FFT_XF, P_FFT_Y,
   P_FFT_Z, P_FFT_XI, P_SPME_GATHER, P_VV, P_SHAKE, P_RATTLE, P_MLP, P_MTS_DESC, P_MLP_TRAIN, P_COARSE_PREP,
   P_COARSE_SPREAD, P_COARSE_FFT, P_COARSE_GATHER, P_METAL_DENSITY, P_METAL_FORCES, P_NPROF
 };
@@ -125,13 +125,7 @@ struct Dev {
   double lang_t0 = 0, lang_t1 = 0, lang_scr = 0, lang_scl = 0, lang_scv = 0;
   int seed[3] = {0, 0, 0};
   int nstep = 0;               // flow%step of the current (or next) stage-1 call
-  // mixed-precision full list (derived, transposed by atom)
-  int* flist = nullptr;        // full list entries
-  int* fcount = nullptr;       // per atom count
-  int* fstart = nullptr;       // per atom start
-  long long flist_cap = 0;
   long long list_gen = 0;      // incremented whenever the Verlet list is rebuilt
-  long long full_gen = -1;     // list generation the derived full list was built from
 
   // tables
   int nsamples = 0, max_grid = 0, nkey = 0;
@@ -330,7 +324,6 @@ int list_relocate_and_halo();     // pbcshift + halo + vnl_set_check (gb_list.cu
 int list_refresh_halo();          // refresh halo positions (gb_list.cu)
 int list_build();                 // binning + pairs (gb_list.cu)
 void list_setup();                // link-cell geometry (gb_list.cu)
-void list_full_build();           // derived full (symmetric) list, for the learned-MTS inputs
 void list_pos_f32();              // FP32 copy of positions and charges (mixed path)
 void scan_exclusive(const int* in, int* out, int n);
 void pair_forces(double* eng6, double* stress9);  // gb_pair.cu (adds into forces)

@@ -486,43 +486,6 @@ __global__ void k_pos_f32(const DevScalars* sc, const double* x, const double* y
   }
 }
 
-// ------------------------------------------------------ derived full list
-// Count, for every local atom, the entries of the full (symmetric) list: its
-// own half-list entries plus the reverse of every entry that names it.
-__global__ void k_full_count(int natms, const int* list, int ld, int* fcount) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= natms) return;
-  const int* li = list + (size_t)warp * ld + 3;
-  const int n = li[-1];  // non-frozen part incl. excluded (excluded are filtered below)
-  const int nx = li[0];
-  for (int k = lane; k < nx; k += 32) {
-    int j = li[k + 1] - 1;
-    if (j < natms) atomicAdd(&fcount[j], 1);
-  }
-  if (lane == 0) atomicAdd(&fcount[warp], nx);
-  (void)n;
-}
-
-// An atom's full list: its own half-list entries first, in list order (no
-// atomic), then the reverse entries, appended with one atomic per entry on the
-// receiving atom.
-__global__ void k_full_fill(int natms, const int* list, int ld, const int* fstart, int* ffill, int* flist) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= natms) return;
-  const int* li = list + (size_t)warp * ld + 3;
-  const int nx = li[0];
-  const int own0 = fstart[warp];
-  for (int k = lane; k < nx; k += 32) {
-    int j = li[k + 1] - 1;
-    flist[own0 + k] = j;
-    if (j < natms) {
-      const int nxj = list[(size_t)j * ld + 3];
-      int s2 = atomicAdd(&ffill[j], 1);
-      flist[fstart[j] + nxj + s2] = warp;
-    }
-  }
-}
-
 inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
@@ -724,25 +687,3 @@ void list_pos_f32() {
   GB_LAUNCHED();
 }
 
-void list_full_build() {
-  const int n = g.natms;
-  cudaStream_t st = g.stream;
-  GB_CUDA(cudaMemsetAsync(g.fcount, 0, sizeof(int) * (n + 1), st));
-  k_full_count<<<nblocks((long long)n * 32, 256), 256, 0, st>>>(n, g.list, g.ld, g.fcount);
-  GB_LAUNCHED();
-  k_scan_single<<<1, 1024, 0, st>>>(g.fcount, g.fstart, n + 1, nullptr);
-  GB_LAUNCHED();
-  int total = 0;
-  GB_CUDA(cudaMemcpyAsync(&total, g.fstart + n, sizeof(int), cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaStreamSynchronize(st));
-  if ((long long)total > g.flist_cap) {
-    cudaFree(g.flist);
-    g.flist_cap = (long long)(total * 1.25) + 1024;
-    GB_CUDA(cudaMalloc(&g.flist, sizeof(int) * g.flist_cap));
-  }
-  int* fill = gb_scan_scratch(n + 1);
-  GB_CUDA(cudaMemsetAsync(fill, 0, sizeof(int) * (n + 1), st));
-  k_full_fill<<<nblocks((long long)n * 32, 256), 256, 0, st>>>(n, g.list, g.ld, g.fstart, fill, g.flist);
-  GB_LAUNCHED();
-  g.full_gen = g.list_gen;
-}

@@ -81,6 +81,7 @@ struct MtsDev {
   double ec0 = 0.0, vc0 = 0.0, stc0[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // coarse at t0
   double err_coarse = -1.0, err_stale = -1.0;
   int *sstart = nullptr, *scount = nullptr, *slist = nullptr;  // short neighbour list (CSR)
+  int *sown = nullptr, *sfill = nullptr;  // own (half-list) entries per atom, reverse-entry fill counters
   long long scap = 0, gen_seen = -1;
   float* target = nullptr;     // labels (3n)
   double* x0 = nullptr;        // positions at t0 (3n)
@@ -162,66 +163,82 @@ __global__ void k_mts_prep(int n, const DevScalars* sc, const int* __restrict__ 
 }
 
 // ------------------------------------------------------ short neighbour list
-// Pairs within rs = 6 A + skin of the full list, rebuilt with it: between
-// rebuilds no atom moves more than half the skin, so every pair inside 6 A at
-// any step of the list's lifetime is in it.  Each atom's entries are sorted by
-// index, so the input sums do not depend on the full list's fill order.
+// Pairs within rs = 6 A + skin, rebuilt with the Verlet list: between rebuilds no
+// atom moves more than half the skin, so every pair inside 6 A at any step of the
+// list's lifetime is in it.  Built from the half list: an atom's entries are its own
+// half-list entries within rs (a pair across the periodic boundary is listed from both
+// sides, with the other side's halo image) plus, for each local partner that lists
+// it, that partner (the reverse of a local-local entry).  Each atom's entries are then
+// sorted by index, so the input sums do not depend on the fill order.
 constexpr int SHORT_CAP = 256;  // entries sorted in shared memory per atom
 
-__global__ void k_short_count(int n, const int* __restrict__ fstart, const int* __restrict__ fcount,
-                              const int* __restrict__ flist, const float4* __restrict__ xf, float rs2,
-                              int* __restrict__ scount) {
+// own entries within rs (sown) and the total per atom (scount, reverse entries by atomics)
+__global__ void k_short_count(int n, const int* __restrict__ list, int ld, const float4* __restrict__ xf, float rs2,
+                              int* __restrict__ sown, int* __restrict__ scount) {
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= n) return;
   const float4 pi = xf[i];
-  const int st = fstart[i], cnt = fcount[i];
+  const int* li = list + (size_t)i * ld + 3;
+  const int nx = li[0];  // non-excluded entries
   int c = 0;
-  for (int base = 0; base < cnt; base += 32) {
+  for (int base = 0; base < nx; base += 32) {
     bool in = false;
-    if (base + lane < cnt) {
-      const float4 pj = xf[flist[st + base + lane]];
+    if (base + lane < nx) {
+      const int j = li[base + lane + 1] - 1;
+      const float4 pj = xf[j];
       const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
       in = dx * dx + dy * dy + dz * dz < rs2;
+      if (in && j < n) atomicAdd(&scount[j], 1);
     }
     c += __popc(__ballot_sync(0xffffffffu, in));
   }
-  if (lane == 0) scount[i] = c;
+  if (lane == 0) {
+    sown[i] = c;
+    atomicAdd(&scount[i], c);
+  }
 }
 
-__global__ void __launch_bounds__(256) k_short_fill(int n, const int* __restrict__ fstart,
-                                                    const int* __restrict__ fcount, const int* __restrict__ flist,
-                                                    const float4* __restrict__ xf, float rs2,
-                                                    const int* __restrict__ sstart, int* __restrict__ slist) {
-  __shared__ int buf[8][SHORT_CAP];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * 8 + w;
-  if (i >= n) return;  // the whole warp leaves; no block-wide barrier below
+// own entries first (list order), then the reverse entries at sown[j] + an atomic slot
+__global__ void k_short_fill(int n, const int* __restrict__ list, int ld, const float4* __restrict__ xf, float rs2,
+                             const int* __restrict__ sstart, const int* __restrict__ sown, int* __restrict__ sfill,
+                             int* __restrict__ slist) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= n) return;
   const float4 pi = xf[i];
-  const int st = fstart[i], cnt = fcount[i];
-  const int s0 = sstart[i], ns = sstart[i + 1] - s0;
-  const bool sorted = ns <= SHORT_CAP;
+  const int* li = list + (size_t)i * ld + 3;
+  const int nx = li[0];
+  const int s0 = sstart[i];
   int c = 0;
-  for (int base = 0; base < cnt; base += 32) {
+  for (int base = 0; base < nx; base += 32) {
     bool in = false;
     int j = 0;
-    if (base + lane < cnt) {
-      j = flist[st + base + lane];
+    if (base + lane < nx) {
+      j = li[base + lane + 1] - 1;
       const float4 pj = xf[j];
       const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
       in = dx * dx + dy * dy + dz * dz < rs2;
     }
     const unsigned b = __ballot_sync(0xffffffffu, in);
     if (in) {
-      const int pos = c + __popc(b & ((1u << lane) - 1u));
-      if (sorted) buf[w][pos] = j;
-      else slist[s0 + pos] = j;  // too many to sort here: fill order
+      slist[s0 + c + __popc(b & ((1u << lane) - 1u))] = j;
+      if (j < n) slist[sstart[j] + sown[j] + atomicAdd(&sfill[j], 1)] = i;
     }
     c += __popc(b);
   }
+}
+
+// each atom's entries in ascending index order (rank sort; entries are distinct)
+__global__ void __launch_bounds__(256) k_short_sort(int n, const int* __restrict__ sstart, int* __restrict__ slist) {
+  __shared__ int buf[8][SHORT_CAP];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 8 + w;
+  if (i >= n) return;  // the whole warp leaves; no block-wide barrier below
+  const int s0 = sstart[i], ns = sstart[i + 1] - s0;
+  if (ns > SHORT_CAP) return;  // more than the buffer holds: left in fill order
+  for (int e = lane; e < ns; e += 32) buf[w][e] = slist[s0 + e];
   __syncwarp();
-  if (!sorted) return;
-  // rank sort (entries are distinct)
   for (int e = lane; e < ns; e += 32) {
     const int v = buf[w][e];
     int r = 0;
@@ -761,8 +778,8 @@ void mts_short_list() {
   const float rs = RCUT_DESC + (float)g.p.rpad;
   const float rs2 = rs * rs;
   GB_CUDA(cudaMemsetAsync(M.scount, 0, sizeof(int) * (n + 1), g.stream));
-  k_short_count<<<nblocks((long long)n * 32, 256), 256, 0, g.stream>>>(n, g.fstart, g.fcount, g.flist, g.xf, rs2,
-                                                                        M.scount);
+  GB_CUDA(cudaMemsetAsync(M.sfill, 0, sizeof(int) * n, g.stream));
+  k_short_count<<<nblocks((long long)n * 32, 256), 256, 0, g.stream>>>(n, g.list, g.ld, g.xf, rs2, M.sown, M.scount);
   GB_LAUNCHED();
   scan_exclusive(M.scount, M.sstart, n + 1);
   int total = 0;
@@ -773,7 +790,10 @@ void mts_short_list() {
     M.scap = (long long)(total * 1.25) + 1024;
     GB_CUDA(cudaMalloc(&M.slist, sizeof(int) * M.scap));
   }
-  k_short_fill<<<nblocks(n, 8), 256, 0, g.stream>>>(n, g.fstart, g.fcount, g.flist, g.xf, rs2, M.sstart, M.slist);
+  k_short_fill<<<nblocks((long long)n * 32, 256), 256, 0, g.stream>>>(n, g.list, g.ld, g.xf, rs2, M.sstart, M.sown,
+                                                                       M.sfill, M.slist);
+  GB_LAUNCHED();
+  k_short_sort<<<nblocks(n, 8), 256, 0, g.stream>>>(n, M.sstart, M.slist);
   GB_LAUNCHED();
   M.gen_seen = g.list_gen;
 }
@@ -781,12 +801,11 @@ void mts_short_list() {
 void mts_inputs() {
   const int n = g.natms;
   prof_begin(P_MTS_DESC);
-  if (g.full_gen != g.list_gen) {
-    prof_begin(P_FULLLIST);
-    list_full_build();
-    prof_end(P_FULLLIST);
+  if (M.gen_seen != g.list_gen) {
+    prof_begin(P_SHORTLIST);
+    mts_short_list();
+    prof_end(P_SHORTLIST);
   }
-  if (M.gen_seen != g.list_gen) mts_short_list();
   k_mts_prep<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(n, g.sc, g.src, g.x, g.y, g.z, M.x0, M.triple, g.cell[0],
                                                              M.disp, M.frame);
   GB_LAUNCHED();
@@ -916,7 +935,7 @@ void mts_set_topology(int ntcons, const int32_t* listcon, const double* weight) 
 void mts_free() {
   void* ptrs[] = {M.master, M.m1, M.m2, M.grad, M.gpart, M.loss_part, M.X, M.frec0, M.frec, M.truth, M.target,
                   M.fc, M.fc0, M.x0, M.disp, M.frame, M.triple, M.scal, M.red, M.idx, M.sstart, M.scount,
-                  M.slist};
+                  M.slist, M.sown, M.sfill};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   net_free(M.net);
@@ -955,6 +974,8 @@ void mts_setup() {
   GB_CUDA(cudaMalloc(&M.idx, sizeof(int) * (size_t)M.batch));
   GB_CUDA(cudaMalloc(&M.sstart, sizeof(int) * ((size_t)n + 1)));
   GB_CUDA(cudaMalloc(&M.scount, sizeof(int) * ((size_t)n + 1)));
+  GB_CUDA(cudaMalloc(&M.sown, sizeof(int) * (size_t)n));
+  GB_CUDA(cudaMalloc(&M.sfill, sizeof(int) * (size_t)n));
   if ((int)h_triple.size() != 3 * n) h_triple.assign(3 * (size_t)n, -1);
   GB_CUDA(cudaMemcpy(M.triple, h_triple.data(), sizeof(int) * 3 * (size_t)n, cudaMemcpyHostToDevice));
   std::vector<float> sc(NIN + 1, 1.0f);
