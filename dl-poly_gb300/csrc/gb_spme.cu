@@ -409,60 +409,82 @@ __global__ void k_spme_gather(int natms, const double* __restrict__ x, const dou
   block_reduce_store<4>(acc, blk);
 }
 
-// FP32 gather, one warp per atom.  Lane (j, k) = (lane & 7, lane >> 3) and
-// (j, k + 4) cover the p x p (x,y) rows for p = 8, so each warp load reads four
-// 8-wide rows (coalesced); lanes 0..2 build the splines of one dimension each
-// from the stored truncation-convention fraction.  No FP64 instruction.
+// FP32 gather, one warp per atom: lane pr = (j, k) of the p x p (x, y) rows sums its z
+// column (x fastest, so groups of p lanes read contiguous grid points).  A warp takes
+// GATHER_AB atoms at a time: 3 x GATHER_AB lanes build their splines in parallel, and
+// the four per-atom sums are combined by a reduce-scatter that leaves the energy sum in
+// lane 0 and the x, y, z force sums in lanes 8, 16, 24.
+constexpr int GATHER_AB = 8;  // atoms per warp batch
 template <int P>
-__global__ void __launch_bounds__(256) k_spme_gather_f32(int natms, const float* __restrict__ q4, SpmeGeom sg,
+__global__ void __launch_bounds__(256, 4) k_spme_gather_f32(int natms, const float* __restrict__ q4, SpmeGeom sg,
                                                          const int* __restrict__ gidx, const float* __restrict__ gw,
                                                          const float* __restrict__ phi, float rk0, float rk1,
                                                          float rk2, float* __restrict__ fout, double* blk) {
-  __shared__ float sp[8][2][3][P];  // per warp: value/derivative, dimension, point
+  __shared__ float sp[8][GATHER_AB][2][3][P];  // per warp and atom: value/derivative, dimension, point
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < natms; i += nwarps) {
-    const float qi = q4[4 * i + 3];
-    if (lane < 3) {
-      float m[PMAX], dm[PMAX];
-      bspline_vals<float, P>(gw[3 * i + lane], P, m, dm);
-      for (int t = 0; t < P; ++t) { sp[wid][0][lane][t] = m[t]; sp[wid][1][lane][t] = dm[t]; }
-    }
-    __syncwarp();
-    const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
-    float e = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
-    // (x, y) pairs of the p x p rows: x fastest, so groups of p lanes read
-    // contiguous grid points
+  for (int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * GATHER_AB; base < natms;
+       base += nwarps * GATHER_AB) {
+    if (lane < 3 * GATHER_AB) {
+      const int a = lane / 3, d = lane - 3 * a, i = base + a;
+      if (i < natms) {
+        float m[PMAX], dm[PMAX];
+        bspline_vals<float, P>(gw[3 * i + d], P, m, dm);
 #pragma unroll
-    for (int pr = lane; pr < P * P; pr += 32) {
-      const int j = pr % P, k = pr / P;
-      int xx = gx + j; if (xx >= K0) xx -= K0;
-      int yy = gy + k; if (yy >= K1) yy -= K1;
-      const float mx = sp[wid][0][0][j], dmx = sp[wid][1][0][j];
-      const float my = sp[wid][0][1][k], dmy = sp[wid][1][1][k];
-      const float p0 = mx * my, p1 = dmx * my, p2 = mx * dmy;
-      const float* col = phi + (size_t)yy * K0 + xx;
-#pragma unroll
-      for (int l = 0; l < P; ++l) {
-        int zz = gz + l; if (zz >= K2) zz -= K2;
-        const float pa = col[(size_t)zz * K1 * K0];
-        const float mz = sp[wid][0][2][l], dmz = sp[wid][1][2][l];
-        const float ta = mz * pa;
-        e = fmaf(p0, ta, e);
-        fx = fmaf(p1, ta, fx);
-        fy = fmaf(p2, ta, fy);
-        fz = fmaf(p0, dmz * pa, fz);
+        for (int t = 0; t < P; ++t) { sp[wid][a][0][d][t] = m[t]; sp[wid][a][1][d][t] = dm[t]; }
       }
     }
-    e = warp_sumf(e); fx = warp_sumf(fx); fy = warp_sumf(fy); fz = warp_sumf(fz);
-    const float f0 = -qi * fx * rk0, f1 = -qi * fy * rk1, f2 = -qi * fz * rk2;
-    if (lane == 0) {
-      fout[3 * i] = f0; fout[3 * i + 1] = f1; fout[3 * i + 2] = f2;
-      acc[0] += qi * e; acc[1] += f0; acc[2] += f1; acc[3] += f2;
-    }
     __syncwarp();
+    const int na = min(GATHER_AB, natms - base);
+    for (int a = 0; a < na; ++a) {
+      const int i = base + a;
+      const float qi = q4[4 * i + 3];
+      const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
+      float v[4] = {0.f, 0.f, 0.f, 0.f};  // energy, x, y, z sums
+#pragma unroll
+      for (int pr = lane; pr < P * P; pr += 32) {
+        const int j = pr % P, k = pr / P;
+        int xx = gx + j; if (xx >= K0) xx -= K0;
+        int yy = gy + k; if (yy >= K1) yy -= K1;
+        const float mx = sp[wid][a][0][0][j], dmx = sp[wid][a][1][0][j];
+        const float my = sp[wid][a][0][1][k], dmy = sp[wid][a][1][1][k];
+        const float p0 = mx * my, p1 = dmx * my, p2 = mx * dmy;
+        const float* col = phi + (size_t)yy * K0 + xx;
+#pragma unroll
+        for (int l = 0; l < P; ++l) {
+          int zz = gz + l; if (zz >= K2) zz -= K2;
+          const float pa = col[(size_t)zz * K1 * K0];
+          const float ta = sp[wid][a][0][2][l] * pa;
+          v[0] = fmaf(p0, ta, v[0]);
+          v[1] = fmaf(p1, ta, v[1]);
+          v[2] = fmaf(p2, ta, v[2]);
+          v[3] = fmaf(p0, sp[wid][a][1][2][l] * pa, v[3]);
+        }
+      }
+      // reduce-scatter: level 16 keeps (v0, v1) in the lower half-warp, (v2, v3) in the upper
+      const bool up16 = lane & 16, up8 = lane & 8;
+      float k0 = up16 ? v[2] : v[0], k1 = up16 ? v[3] : v[1];
+      const float s0 = up16 ? v[0] : v[2], s1 = up16 ? v[1] : v[3];
+      k0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+      k1 += __shfl_xor_sync(0xffffffffu, s1, 16);
+      float r = up8 ? k1 : k0;
+      r += __shfl_xor_sync(0xffffffffu, up8 ? k0 : k1, 8);
+#pragma unroll
+      for (int o = 4; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+      if ((lane & 7) == 0) {
+        const int comp = lane >> 3;
+        if (comp == 0) {
+          acc[0] += qi * r;
+        } else {
+          const float f = -qi * r * (comp == 1 ? rk0 : (comp == 2 ? rk1 : rk2));
+          fout[3 * i + comp - 1] = f;
+          acc[comp] += f;
+        }
+      }
+    }
+    __syncwarp();  // the batch's splines are read before the next batch writes them
   }
   block_reduce_store<4>(acc, blk);
 }
@@ -475,8 +497,6 @@ __global__ void __launch_bounds__(256) k_spme_gather_f32(int natms, const float*
 // combined by a reduce-scatter over the warp (two values after the first butterfly
 // level, one after the second), which leaves the energy sum in lane 0 and the x, y, z
 // force sums in lanes 8, 16, 24.  No FP64 instruction: forces leave as double-floats.
-constexpr int GATHER_AB = 8;  // atoms per warp batch
-
 template <int P>
 __global__ void __launch_bounds__(256) k_spme_gather_wdf(int natms, SpmeGeom sg, const int* __restrict__ gidx,
                                                          const float* __restrict__ gw, const float* __restrict__ gwl,
@@ -1068,7 +1088,7 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   static int occ_gd = 0;
   if (DF && !occ_gd) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_gd, k_spme_gather_wdf<8>, 256, 0));
   const int nbg = warp_gather ? std::max(1, std::min((DF ? occ_gd : occ_g) * g.nsm,
-                                                     nblocks((long long)n * 32 / (DF ? GATHER_AB : 1), 256)))
+                                                     nblocks((long long)n * 32 / GATHER_AB, 256)))
                               : nblocks(n, 128);
   double* blkg = blkz + (size_t)nbz * 6;
   prof_begin(pid(P_SPME_GATHER));
