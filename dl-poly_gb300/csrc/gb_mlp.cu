@@ -51,7 +51,8 @@ namespace {
 constexpr int NIN = 51, KIN = 64, NH = 128, NOUT = 3, NOUTP = 16;
 constexpr int NRAD = 8;
 constexpr float RCUT_DESC = 6.0f, GAUSS_W = 0.45f, GAUSS_MU0 = 0.5f;
-constexpr int TILE_I = 64;  // atoms per inference tile (4 warps x 16)
+constexpr int TILE_I = 256;            // atoms per inference tile (16 warps x 16 rows)
+constexpr int INFER_NT = TILE_I * 2;   // its threads: one warp per 16 rows
 constexpr int TILE_T = 32;  // atoms per training CTA
 // FP32 parameter vector: W1[NIN][NH], b1[NH], W2[NH][NH], b2[NH], W3[NH][NOUT], b3[NOUT]
 constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NIN * NH, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH,
@@ -373,7 +374,7 @@ __device__ __forceinline__ void mlp_layer(const __nv_bfloat16* in, int ldin, con
 
 // persistent: each CTA stages the weights once and walks tiles of 64 atoms.
 // out = frec0 + fs * R^T y (lab frame)
-__global__ void __launch_bounds__(128) k_mlp_infer(int n, const __nv_bfloat16* __restrict__ X, Net net,
+__global__ void __launch_bounds__(INFER_NT) k_mlp_infer(int n, const __nv_bfloat16* __restrict__ X, Net net,
                                                    const float* __restrict__ frec0, const float* __restrict__ frame,
                                                    const float* __restrict__ scal, float* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -732,7 +733,7 @@ void set_attrs() {
   GB_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem));
   GB_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem));
   int occ = 0;
-  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mlp_infer, 128, infer_smem));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mlp_infer, INFER_NT, infer_smem));
   g_infer_grid = std::max(1, occ) * g.nsm;
   dev_done = dev;
 }
@@ -740,7 +741,7 @@ void set_attrs() {
 void launch_infer(int n, const __nv_bfloat16* X, const Net& net, const float* frec0, const float* frame,
                   const float* scal, float* out) {
   const int grid = std::max(1, std::min(g_infer_grid, nblocks(n, TILE_I)));
-  k_mlp_infer<<<grid, 128, infer_smem, g.stream>>>(n, X, net, frec0, frame, scal, out);
+  k_mlp_infer<<<grid, INFER_NT, infer_smem, g.stream>>>(n, X, net, frec0, frame, scal, out);
   GB_LAUNCHED();
 }
 
