@@ -677,7 +677,7 @@ int list_build() {
   prof_end(P_LIST);
   gb_sync_scalars();
   if (g.hsc->status & ST_LIST_OVERFLOW) return GB_ERR_LIST_OVERFLOW;
-  ++g.list_gen;  // the derived full list (learned-MTS inputs) is rebuilt on demand
+  ++g.list_gen;  // the learned-MTS short list is rebuilt from this list on demand
   return GB_OK;
 }
 

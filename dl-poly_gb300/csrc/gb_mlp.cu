@@ -773,7 +773,7 @@ void read_scalars(const double* dev, double* host, int nv) {
 }
 
 // inputs of the current positions relative to t0
-// short list of the current full list (positions of this step in xf)
+// short list of the current half list (positions of this step in xf)
 void mts_short_list() {
   const int n = g.natms;
   const float rs = RCUT_DESC + (float)g.p.rpad;
