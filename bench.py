@@ -239,7 +239,8 @@ def run_reference(args, dist):
     if dist.rank != 0:
         return
     steps_cap = max(1, args.steps)
-    val, cores, n, dt = cpu_sample(s, steps_cap, budget_s=float(os.environ.get("GB_REF_BUDGET_S", "90")))
+    budget = float(os.environ.get("GB_REF_BUDGET_S", "240"))
+    val, cores, n, dt = cpu_sample(s, steps_cap, budget_s=budget)
     line = {
         "impl": "reference",
         "metric": "atom-steps/s",
@@ -247,7 +248,12 @@ def run_reference(args, dist):
         "unit": "atom-steps/s",
         "n_gpus": args.gpus,
         "steps": n,
+        "steps_requested": args.steps,
+        "steps_match": n == args.steps,
+        "time_budget_s": budget,
         "warmup": 1,
+        "warmup_note": "one untimed MD step (the CPU path has no compilation or cache state beyond it); "
+                       "the timed steps are --steps unless they would exceed time_budget_s",
         "ms_per_step": 1e3 * dt / n,
         "ns_per_day": (n / dt) * DT_PS * 86400 / 1000,
         "higher_is_better": True,
@@ -301,20 +307,29 @@ def measure(lib, L, s, form, args, dist, device, steps, detail):
         lib.md_vv(train)
         t_train = time.perf_counter() - t0
     lib.md_vv(max(3, args.warmup))
-    # ---- timed region: K resident MD steps (kernels timed with CUDA events)
+    # ---- timed region: `runs` times K resident MD steps (kernels timed with CUDA events);
+    # the line reports the median run, the kernel table sums all runs
     L.gb_profile(1)
     clocks = Clocks(device) if detail else None
-    dist.barrier()
-    l0 = L.gb_kernel_launches()
-    w0 = time.perf_counter()
-    stats = lib.md_vv(steps)
-    w1 = time.perf_counter()
-    l1 = L.gb_kernel_launches()
-    tm = (ctypes.c_double * 8)()
-    L.gb_last_timings(tm, 8)
-    span_s = tm[5] * 1e-3
-    dist.barrier()
+    spans, walls, stats_all, launches = [], [], [], 0
+    for _ in range(max(1, args.runs)):
+        dist.barrier()
+        l0 = L.gb_kernel_launches()
+        w0 = time.perf_counter()
+        stats = lib.md_vv(steps)
+        w1 = time.perf_counter()
+        l1 = L.gb_kernel_launches()
+        tm = (ctypes.c_double * 8)()
+        L.gb_last_timings(tm, 8)
+        dist.barrier()
+        spans.append(dist.max(tm[5] * 1e-3))
+        walls.append(w1 - w0)
+        stats_all += stats
+        launches += l1 - l0
     clk = clocks.stop() if clocks else None
+    order = sorted(range(len(spans)), key=lambda r: spans[r])
+    med = order[len(order) // 2]
+    tmax = spans[med]
     names = ctypes.create_string_buffer(32 * 32)
     ms = (ctypes.c_double * 32)()
     nl = (ctypes.c_int64 * 32)()
@@ -328,10 +343,12 @@ def measure(lib, L, s, form, args, dist, device, steps, detail):
     cnt = (ctypes.c_int64 * 3)()
     L.gb_pair_counts(cnt, 3)
     P_list, P_rc = int(cnt[0]), int(cnt[1])  # both forms walk the half list
-    tmax = dist.max(span_s)
+    stats = stats_all
     out = {"value": dist.world * s.natms * steps / tmax, "ms_per_step": tmax * 1e3 / steps,
            "ns_per_day": (steps / tmax) * DT_PS * 86400 / 1000, "steps": steps,
-           "list_rebuilds": sum(x.list_rebuilt for x in stats)}
+           "runs": len(spans), "ms_per_step_runs": [t * 1e3 / steps for t in spans],
+           "spread_rel": (max(spans) - min(spans)) / tmax,
+           "list_rebuilds": sum(x.list_rebuilt for x in stats) / len(spans)}
     if precision == 1 and k == 1:
         out["force_err_rms"], out["force_err_max"] = force_error(lib, L)
     if k > 1:
@@ -341,7 +358,10 @@ def measure(lib, L, s, form, args, dist, device, steps, detail):
                       "checked_err_last": m["last_err"], "checked_err_max": m["err_max"],
                       "err_without_network": m["err_no_network"], "err_stale_force": m["err_stale"],
                       "fallback_entries": int(m["n_fallback"]), "in_fallback": bool(m["in_fallback"])}
-    return out, dict(stats=stats, prof=prof, P=(P_list, P_rc), launches=l1 - l0, clk=clk, wall=w1 - w0, tmax=tmax)
+    if prof:
+        out["kernels_ms_per_step"] = {nm: v[0] / (len(spans) * steps) for nm, v in prof.items()}
+    return out, dict(stats=stats, prof=prof, P=(P_list, P_rc), launches=launches, clk=clk, wall=sum(walls),
+                     tmax=tmax, runs=len(spans))
 
 
 KB_INTERNAL = 0.831446261815324  # Boltzmann constant in DL_POLY internal energy units (10 J/mol) per K
@@ -350,47 +370,75 @@ KB_INTERNAL = 0.831446261815324  # Boltzmann constant in DL_POLY internal energy
 def run_drift(args):
     """NVE energy drift per form: slope of a linear fit to the total energy (after the first
     tenth of the run, and after MTS training; MTS forms use the full-SPME steps, whose energies
-    are exact), in kT per ns per atom."""
+    are exact), in kT per ns per atom.  --drift-dt, --drift-skin and --drift-seeds repeat the
+    measurement over time steps, Verlet skins and seeds of the synthetic start."""
     import dlpoly_gb300 as gb
 
-    s, desc = workload(args.drift_workload)
+    _, desc = workload(args.drift_workload)
     temp = 1500.0 if args.drift_workload.startswith("nacl") else 300.0
     lib = gb.load()
-    out = {"mode": "nve_drift", "workload": desc, "steps": args.drift_steps, "temperature_K": temp, "forms": {}}
-    for form in args.drift_forms.split(","):
-        precision, k = FORMS[form]
-        lib.init(s, precision=precision)
-        lib.start()
-        train = 0
-        if k > 1:
-            train = min(args.drift_train, args.drift_steps // 2)
-            lib.mts_config(k, MTS_TOL, train)
-        E, full = [], []
-        t0 = time.perf_counter()
-        done = 0
-        while done < args.drift_steps:
-            st = lib.md_vv(min(1000, args.drift_steps - done))
-            done += len(st)
-            for x in st:
-                E.append(x.engcpe_rc + x.engcpe_rl + x.engcpe_ex + x.engvdw + x.engke)
-                full.append(x.mts_full)
-        wall = time.perf_counter() - t0
-        E = np.array(E)
-        idx = np.arange(len(E))
-        sel = idx >= max(train + 10, len(E) // 10)
-        if k > 1:
-            sel &= np.array(full, bool)
-        slope = np.polyfit(idx[sel] * DT_PS, E[sel], 1)[0]  # energy units per ps
-        rec = {"drift_kT_per_ns_per_atom": float(slope * 1000.0 / (KB_INTERNAL * temp * s.natms)),
-               "energy_rel_std": float(np.std(E[sel]) / abs(np.mean(E[sel]))), "wall_s": wall}
-        if k > 1:
-            m = lib.mts_stats()
-            rec["mts"] = {"k": k, "train_steps": train, "checked_err_last": m["last_err"],
-                          "checked_err_max": m["err_max"], "err_without_network": m["err_no_network"],
-                          "inner_steps": int(m["n_inner"]), "fallback_entries": int(m["n_fallback"])}
-        out["forms"][form] = rec
+    out = {"mode": "nve_drift", "workload": desc, "steps": args.drift_steps, "temperature_K": temp, "runs": []}
+    for dt_fs in [float(v) for v in args.drift_dt.split(",")]:
+        for skin in [float(v) for v in args.drift_skin.split(",")]:
+            for seed in [int(v) for v in args.drift_seeds.split(",")]:
+                s = drift_system(args.drift_workload, seed)
+                s.tstep = dt_fs * 1e-3
+                s.rpad = skin
+                nsteps = int(round(args.drift_steps * 2.0 / dt_fs))  # the same simulated time
+                for form in args.drift_forms.split(","):
+                    rec = drift_one(lib, s, form, nsteps, temp, args)
+                    rec.update({"form": form, "dt_fs": dt_fs, "skin_A": skin, "seed": seed, "steps": nsteps})
+                    out["runs"].append(rec)
     lib.finalize()
     print(json.dumps(out), flush=True)
+
+
+def drift_system(name, seed):
+    if name == "nacl_4096":
+        return systems.nacl_melt(16, seed=seed)
+    if name == "nacl_262144":
+        return systems.nacl_melt(64, seed=seed)
+    if name == "water_98304":
+        return systems.spce_water(32, seed=seed)
+    raise SystemExit(f"no drift system {name}")
+
+
+def drift_one(lib, s, form, nsteps, temp, args):
+    precision, k = FORMS[form]
+    lib.init(s, precision=precision)
+    lib.start()
+    train = 0
+    if k > 1:
+        train = min(args.drift_train, nsteps // 2)
+        lib.mts_config(k, MTS_TOL, train)
+    E, full = [], []
+    t0 = time.perf_counter()
+    done = 0
+    rebuilds = 0
+    while done < nsteps:
+        st = lib.md_vv(min(1000, nsteps - done))
+        done += len(st)
+        for x in st:
+            E.append(x.engcpe_rc + x.engcpe_rl + x.engcpe_ex + x.engvdw + x.engke)
+            full.append(x.mts_full)
+            rebuilds += x.list_rebuilt
+    wall = time.perf_counter() - t0
+    E = np.array(E)
+    tps = s.tstep
+    idx = np.arange(len(E))
+    sel = idx >= max(train + 10, len(E) // 10)
+    if k > 1:
+        sel &= np.array(full, bool)
+    slope = np.polyfit(idx[sel] * tps, E[sel], 1)[0]  # energy units per ps
+    rec = {"drift_kT_per_ns_per_atom": float(slope * 1000.0 / (KB_INTERNAL * temp * s.natms)),
+           "energy_rel_std": float(np.std(E[sel]) / abs(np.mean(E[sel]))), "wall_s": wall,
+           "list_rebuilds": int(rebuilds)}
+    if k > 1:
+        m = lib.mts_stats()
+        rec["mts"] = {"k": k, "train_steps": train, "checked_err_last": m["last_err"],
+                      "checked_err_max": m["err_max"], "err_without_network": m["err_no_network"],
+                      "inner_steps": int(m["n_inner"]), "fallback_entries": int(m["n_fallback"])}
+    return rec
 
 
 def run_gb(args, dist):
@@ -417,7 +465,7 @@ def run_gb(args, dist):
     head, det = measure(lib, L, s, args.form, args, dist, device, args.steps, detail=True)
     forms[args.form] = head
     stats, prof, (P_list, P_rc), clk, tmax = det["stats"], det["prof"], det["P"], det["clk"], det["tmax"]
-    l0, l1, w0, w1 = 0, det["launches"], 0.0, det["wall"]
+    l0, l1, w0, w1 = 0, det["launches"] // det["runs"], 0.0, det["wall"] / det["runs"]
     steps = head["steps"]
     value = head["value"]
     rebuilds = head["list_rebuilds"]
@@ -503,6 +551,22 @@ def run_gb(args, dist):
         if tr:
             roof["traffic"] = tr[0] * P_list
             roof["traffic_source"] = tr[1]
+    # the all-FP64 form's pair kernel against the FP64 pipe (DFMA peak measured in this run)
+    nat = forms.get("fp64_native")
+    if nat and fp64_peak and fp64_peak > 0 and "pair_forces" in nat.get("kernels_ms_per_step", {}):
+        fl, by = kernel_work("pair_forces", s, (P_list, P_rc), "fp64_native")
+        t_pair = nat["kernels_ms_per_step"]["pair_forces"] * 1e-3
+        nat["roofline"] = {"bound": "fp64", "kernel": "pair_forces (k_pair_fp64)",
+                           "achieved": fl / t_pair / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                           "frac": fl / t_pair / 1e12 / fp64_peak,
+                           "peak_source": "FP64 DFMA loop measured in this run",
+                           "flops_per_launch": fl, "launch_ms": t_pair * 1e3}
+    # speed ratios between the forms of this workload (same steps, same clock record)
+    ratios = {}
+    for a, b in (("mixed", "fp64_native"), ("mixed", "fp64"), ("fp64", "fp64_native"), ("mts_k4", "mixed"),
+                 ("mts_k8", "mixed")):
+        if a in forms and b in forms:
+            ratios[f"{a}_over_{b}"] = forms[a]["value"] / forms[b]["value"]
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         try:
@@ -534,6 +598,10 @@ def run_gb(args, dist):
                    "list_rebuilds_in_timed_steps": rebuilds, "parallelism": "replicas" if dist.world > 1 else "single",
                    "l2": "working set > 129 MB L2 (list ~%.0f MB), no flush" % (4.0 * P_list / 1e6)},
         "forms": forms,
+        "ratios": ratios,
+        "runs": det["runs"],
+        "ms_per_step_runs": head["ms_per_step_runs"],
+        "spread_rel": head["spread_rel"],
         "e2e": e2e,
         "gpu_launches": int(l1 - l0),
         "clocks": clk,
@@ -550,12 +618,13 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--runs", type=int, default=3, help="timed runs of --steps steps each; the line reports the median")
     ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
     ap.add_argument("--form", default="fp64", choices=list(FORMS))
     ap.add_argument("--workload", default="nacl_262144",
                     choices=["nacl_262144", "nacl_175616", "nacl_4096", "water_98304", "eam_256000", "eam_6912"])
-    ap.add_argument("--mts-train", type=int, default=200,
+    ap.add_argument("--mts-train", type=int, default=2000,
                     help="MD steps of online training (SPME every step) before the learned-MTS forms are timed")
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="time only --form (default: every form of the workload, --form is the headline)")
@@ -565,6 +634,9 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=10000)
     ap.add_argument("--drift-train", type=int, default=2000)
     ap.add_argument("--drift-forms", default="fp64,mixed,mts_k4,mts_k8")
+    ap.add_argument("--drift-dt", default="2", help="time steps in fs (comma list); steps scale to equal time")
+    ap.add_argument("--drift-skin", default="1", help="Verlet skins in Angstrom (comma list)")
+    ap.add_argument("--drift-seeds", default="1234", help="seeds of the synthetic start (comma list)")
     ap.add_argument("--emit", metavar="DIR", default=None,
                     help="write the workload as DL_POLY CONFIG/FIELD/CONTROL plus raw arrays and exit")
     args = ap.parse_args()

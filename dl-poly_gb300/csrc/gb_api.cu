@@ -398,6 +398,7 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return GB_ERR_NO_DEVICE;
     if (prm->device < 0 || prm->device >= ndev) return GB_ERR_ARG;
+    if (prm->mxnode > 1) return GB_ERR_MULTI_RANK;  // one rank, one GPU: no domain decomposition
     GB_CUDA(cudaSetDevice(prm->device));
     cudaDeviceProp prop;
     GB_CUDA(cudaGetDeviceProperties(&prop, prm->device));
@@ -644,6 +645,34 @@ int gb_vv(int stage, double* strkin, double* engke, int32_t* iters, double* virc
   });
 }
 
+int gb_constraints_tags(void) {
+  return guarded([&]() {
+    integ_con_tags();
+    return (int)GB_OK;
+  });
+}
+
+int gb_shake(int32_t* iters, double* vircon, double* strcon) {
+  return guarded([&]() {
+    GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
+    int it = 0;
+    integ_shake(&it, vircon, strcon);
+    if (iters) *iters = it;
+    return (int)GB_OK;
+  });
+}
+
+int gb_rattle(int32_t* iters) {
+  return guarded([&]() {
+    GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
+    integ_rattle_launch();
+    gb_sync_scalars();
+    if (iters) *iters = g.ntcons > 0 ? g.hsc->rattle_iters : 0;
+    if (g.ntcons > 0 && (g.hsc->status & ST_RATTLE_FAIL)) return (int)GB_ERR_RATTLE;
+    return (int)GB_OK;
+  });
+}
+
 int gb_set_ensemble(int kind, double temp, double tau_t, double chi, const int32_t* seed, double degfre) {
   return guarded([&]() {
     if (!g.init) return (int)GB_ERR_NOT_INIT;
@@ -780,6 +809,8 @@ int gb_mts_config(int k, double tol, int train_steps) {
     if (k < 1 || !(tol > 0.0) || train_steps < 0) return (int)GB_ERR_ARG;
     if (k > 1 && g.precision != GB_MIXED) return (int)GB_ERR_ARG;  // the surrogate feeds the fixed-point forces
     if (k > 1 && !g.has_coul) return (int)GB_ERR_ARG;  // it replaces SPME: needs charges
+    // the network's neighbour sums reach 6 A: the half list and the halo must hold those pairs
+    if (k > 1 && g.p.rcut < MTS_RCUT_DESC) return (int)GB_ERR_ARG;
     g.mts_k = k;
     g.mts_tol = tol;
     g.mts_train = train_steps;
@@ -927,6 +958,7 @@ const char* gb_strerror(int status) {
     case GB_ERR_METAL_TABLE: return "metal table read below its first point (error 506)";
     case GB_ERR_METAL_DENSITY: return "local density outside its embedding table (error 507)";
     case GB_ERR_RNG: return "a Gaussian deviate's rejection loop hit its iteration cap";
+    case GB_ERR_MULTI_RANK: return "more than one MPI rank (comm%mxnode > 1): the device path runs one rank on one GPU";
     case GB_ERR_TOO_LARGE: return "size exceeds the fixed scratch limit of gb_kinstress_noalloc (1,048,576 atoms)";
     default: return "unknown status";
   }

@@ -338,6 +338,9 @@ bool spme_coarse_ready();
 // floats, net force removed); forces of the context are not touched
 void spme_coarse_forces(double* eng_rc, double* vir_rc, double* stress9, float* rec);
 void integ_vv(int stage, double* strkin, double* engke, int* iters, double* vircon, double* strcon);
+void integ_con_tags();            // constraints_tags: old bond vectors from the current positions
+void integ_shake(int* iters, double* vircon, double* strcon);  // apply_shake (throws GB_ERR_SHAKE)
+void integ_rattle_launch();       // apply_rattle, kit = 1 (status bit ST_RATTLE_FAIL)
 int integ_vnl_check();
 void integ_zero_forces();
 void integ_forces_to_fp64();      // mixed: fixed point -> FP64 forces
@@ -357,6 +360,7 @@ bool metal_active();
 void metal_forces(double* e4, double* stress9);   // engmet, virmet, engden, virden
 void metal_rho(double* out, int n);
 // learned multiple-time-step form (gb_mlp.cu)
+constexpr double MTS_RCUT_DESC = 6.0;  // reach of the network's neighbour sums (Angstrom)
 void mts_set_topology(int ntcons, const int32_t* listcon, const double* weight);
 void mts_setup();
 void mts_free();

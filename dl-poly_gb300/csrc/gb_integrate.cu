@@ -685,16 +685,87 @@ static void con_args(ConArgs& A) {
   A.flags = d_flags; A.sc = g.sc; A.blk = nullptr;
 }
 
-void integ_vv(int stage, double* strkin, double* engke, int* iters, double* vircon, double* strcon) {
+// constraints_tags (constraints.F90:438-586): old bond vectors from the current positions
+void integ_con_tags() {
+  if (g.ntcons <= 0) return;
+  k_con_tags<<<nblocks(g.ntcons, 256), 256, 0, g.stream>>>(g.ntcons, g.con_i, g.con_j, g.x, g.y, g.z, g.cell[0],
+                                                             1.0 / g.cell[0], g.dxx, g.dyy, g.dzz);
+  GB_LAUNCHED();
+}
+
+// apply_shake (constraints.F90:1071-1200): the current positions are the unconstrained
+// ones (oxt); SHAKE against the bond vectors of the last integ_con_tags, then the velocity
+// and force corrections.  Throws GB_ERR_SHAKE when the iteration does not converge.
+void integ_shake(int* iters, double* vircon, double* strcon) {
+  if (iters) *iters = 0;
+  if (g.ntcons <= 0) return;
   cudaStream_t st = g.stream;
   const int n = g.natms;
   const double tstep = g.p.tstep, hstep = 0.5 * tstep, rstep = 1.0 / tstep;
-  if (iters) *iters = 0;
-  if (g.ntcons > 0) {
-    k_con_tags<<<nblocks(g.ntcons, 256), 256, 0, st>>>(g.ntcons, g.con_i, g.con_j, g.x, g.y, g.z, g.cell[0],
-                                                         1.0 / g.cell[0], g.dxx, g.dyy, g.dzz);
-    GB_LAUNCHED();
+  k_copy3<<<nblocks(n, 256), 256, 0, st>>>(n, g.x, g.y, g.z, g.ox, g.oy, g.oz);
+  GB_LAUNCHED();
+  GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + CL_CHUNK + 2), st));
+  ConArgs A;
+  con_args(A);
+  const int nbs = n_clusters ? coop_blocks_cl : coop_blocks_shake;
+  A.blk = gb_blkacc(nbs * 6);
+  prof_begin(P_SHAKE);
+  if (n_clusters) {
+    const ClusterTab* tabs = d_cltab;
+    int ncl = n_clusters, rattle = 0;
+    double *ring = d_clring, *gsum = d_clgsum;
+    GB_CUDA(cudaMemsetAsync(d_clgsum, 0, sizeof(double) * CL_MAXC * n_clusters, st));
+    void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
+    GB_CUDA(cudaLaunchCooperativeKernel(cl_kernel, nbs, CL_THREADS, args, 0, st));
+  } else {
+    void* args[] = {&A};
+    GB_CUDA(cudaLaunchCooperativeKernel((void*)k_shake, nbs, 256, args, 0, st));
   }
+  GB_LAUNCHED();
+  prof_end(P_SHAKE);
+  gb_reduce_blocks(A.blk, nbs, 6, &g.sc->acc[A_STRCON]);
+  k_shake_post<<<nblocks(n, 256), 256, 0, st>>>(n, g.acon_start, g.lfrzn, rstep, hstep, g.weight, g.x, g.y, g.z,
+                                                 g.ox, g.oy, g.oz, g.vx, g.vy, g.vz, g.fx, g.fy, g.fz);
+  GB_LAUNCHED();
+  gb_sync_scalars();
+  if (iters) *iters = g.hsc->shake_iters;
+  const double* s = &g.hsc->acc[A_STRCON];
+  double str[9] = {s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]};
+  if (strcon) for (int k = 0; k < 9; ++k) strcon[k] = str[k];
+  if (vircon) *vircon = -(str[0] + str[4] + str[8]);
+  if (g.hsc->status & ST_SHAKE_FAIL) throw (int)GB_ERR_SHAKE;
+}
+
+// apply_rattle with kit = 1 (constraints.F90:1032-1069 -> constraints_rattle :587-775) on
+// the current velocities, against the bond vectors of the last integ_con_tags.  The
+// status is read by the caller (ST_RATTLE_FAIL).
+void integ_rattle_launch() {
+  if (g.ntcons <= 0) return;
+  cudaStream_t st = g.stream;
+  GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + CL_CHUNK + 2), st));
+  ConArgs A;
+  con_args(A);
+  prof_begin(P_RATTLE);
+  if (n_clusters) {
+    const ClusterTab* tabs = d_cltab;
+    int ncl = n_clusters, rattle = 1;
+    double *ring = d_clring, *gsum = d_clgsum;
+    void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
+    GB_CUDA(cudaLaunchCooperativeKernel(cl_kernel, coop_blocks_cl, CL_THREADS, args, 0, st));
+  } else {
+    void* args[] = {&A};
+    GB_CUDA(cudaLaunchCooperativeKernel((void*)k_rattle, coop_blocks_rattle, 256, args, 0, st));
+  }
+  GB_LAUNCHED();
+  prof_end(P_RATTLE);
+}
+
+void integ_vv(int stage, double* strkin, double* engke, int* iters, double* vircon, double* strcon) {
+  cudaStream_t st = g.stream;
+  const int n = g.natms;
+  const double tstep = g.p.tstep, hstep = 0.5 * tstep;
+  if (iters) *iters = 0;
+  integ_con_tags();
   if (stage == 1) {
     prof_begin(P_VV);
     if (!thermo_vv1(hstep, tstep)) {
@@ -703,63 +774,13 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
       GB_LAUNCHED();
     }
     prof_end(P_VV);
-    if (g.ntcons > 0) {
-      k_copy3<<<nblocks(n, 256), 256, 0, st>>>(n, g.x, g.y, g.z, g.ox, g.oy, g.oz);
-      GB_LAUNCHED();
-      GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + CL_CHUNK + 2), st));
-      ConArgs A;
-      con_args(A);
-      const int nbs = n_clusters ? coop_blocks_cl : coop_blocks_shake;
-      A.blk = gb_blkacc(nbs * 6);
-      prof_begin(P_SHAKE);
-      if (n_clusters) {
-        const ClusterTab* tabs = d_cltab;
-        int ncl = n_clusters, rattle = 0;
-        double *ring = d_clring, *gsum = d_clgsum;
-        GB_CUDA(cudaMemsetAsync(d_clgsum, 0, sizeof(double) * CL_MAXC * n_clusters, st));
-        void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
-        GB_CUDA(cudaLaunchCooperativeKernel(cl_kernel, nbs, CL_THREADS, args, 0, st));
-      } else {
-        void* args[] = {&A};
-        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_shake, nbs, 256, args, 0, st));
-      }
-      GB_LAUNCHED();
-      prof_end(P_SHAKE);
-      gb_reduce_blocks(A.blk, nbs, 6, &g.sc->acc[A_STRCON]);
-      k_shake_post<<<nblocks(n, 256), 256, 0, st>>>(n, g.acon_start, g.lfrzn, rstep, hstep, g.weight, g.x, g.y, g.z,
-                                                     g.ox, g.oy, g.oz, g.vx, g.vy, g.vz, g.fx, g.fy, g.fz);
-      GB_LAUNCHED();
-      gb_sync_scalars();
-      if (iters) *iters = g.hsc->shake_iters;
-      const double* s = &g.hsc->acc[A_STRCON];
-      double str[9] = {s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]};
-      if (strcon) for (int k = 0; k < 9; ++k) strcon[k] = str[k];
-      if (vircon) *vircon = -(str[0] + str[4] + str[8]);
-      if (g.hsc->status & ST_SHAKE_FAIL) throw (int)GB_ERR_SHAKE;
-    }
+    integ_shake(iters, vircon, strcon);
   } else {
     prof_begin(P_VV);
     k_vv2<<<nblocks(n, 256), 256, 0, st>>>(n, hstep, g.weight, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz);
     GB_LAUNCHED();
     prof_end(P_VV);
-    if (g.ntcons > 0) {
-      GB_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int) * (g.p.shake_maxit + CL_CHUNK + 2), st));
-      ConArgs A;
-      con_args(A);
-      prof_begin(P_RATTLE);
-      if (n_clusters) {
-        const ClusterTab* tabs = d_cltab;
-        int ncl = n_clusters, rattle = 1;
-        double *ring = d_clring, *gsum = d_clgsum;
-        void* args[] = {&A, &tabs, &ncl, &ring, &gsum, &rattle};
-        GB_CUDA(cudaLaunchCooperativeKernel(cl_kernel, coop_blocks_cl, CL_THREADS, args, 0, st));
-      } else {
-        void* args[] = {&A};
-        GB_CUDA(cudaLaunchCooperativeKernel((void*)k_rattle, coop_blocks_rattle, 256, args, 0, st));
-      }
-      GB_LAUNCHED();
-      prof_end(P_RATTLE);
-    }
+    integ_rattle_launch();
     if (!thermo_vv2_finish(strkin, engke)) {
       const int nb = nblocks(n, 256);
       double* blk = gb_blkacc(nb * 6);

@@ -50,7 +50,7 @@ namespace {
 
 constexpr int NIN = 51, KIN = 64, NH = 128, NOUT = 3, NOUTP = 16;
 constexpr int NRAD = 8;
-constexpr float RCUT_DESC = 6.0f, GAUSS_W = 0.45f, GAUSS_MU0 = 0.5f;
+constexpr float RCUT_DESC = (float)MTS_RCUT_DESC, GAUSS_W = 0.45f, GAUSS_MU0 = 0.5f;
 constexpr int TILE_I = 256;            // atoms per inference tile (16 warps x 16 rows)
 constexpr int INFER_NT = TILE_I * 2;   // its threads: one warp per 16 rows
 constexpr int TILE_T = 32;  // atoms per training CTA
@@ -82,6 +82,7 @@ struct MtsDev {
   double ec0 = 0.0, vc0 = 0.0, stc0[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // coarse at t0
   double err_coarse = -1.0, err_stale = -1.0;
   int *sstart = nullptr, *scount = nullptr, *slist = nullptr;  // short neighbour list (CSR)
+  int* stmp = nullptr;  // sort scratch of the atoms whose lists exceed the shared buffer
   int *sown = nullptr, *sfill = nullptr;  // own (half-list) entries per atom, reverse-entry fill counters
   long long scap = 0, gen_seen = -1;
   float* target = nullptr;     // labels (3n)
@@ -230,14 +231,27 @@ __global__ void k_short_fill(int n, const int* __restrict__ list, int ld, const 
   }
 }
 
-// each atom's entries in ascending index order (rank sort; entries are distinct)
-__global__ void __launch_bounds__(256) k_short_sort(int n, const int* __restrict__ sstart, int* __restrict__ slist) {
+// each atom's entries in ascending index order (rank sort; entries are distinct).  An
+// atom with more entries than the shared buffer holds is ranked straight from global
+// memory into stmp (same offsets as slist) and copied back, so every list is sorted.
+__global__ void __launch_bounds__(256) k_short_sort(int n, const int* __restrict__ sstart, int* __restrict__ slist,
+                                                    int* __restrict__ stmp) {
   __shared__ int buf[8][SHORT_CAP];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int i = blockIdx.x * 8 + w;
   if (i >= n) return;  // the whole warp leaves; no block-wide barrier below
   const int s0 = sstart[i], ns = sstart[i + 1] - s0;
-  if (ns > SHORT_CAP) return;  // more than the buffer holds: left in fill order
+  if (ns > SHORT_CAP) {
+    for (int e = lane; e < ns; e += 32) {
+      const int v = slist[s0 + e];
+      int r = 0;
+      for (int f = 0; f < ns; ++f) r += slist[s0 + f] < v;
+      stmp[s0 + r] = v;
+    }
+    __syncwarp();
+    for (int e = lane; e < ns; e += 32) slist[s0 + e] = stmp[s0 + e];
+    return;
+  }
   for (int e = lane; e < ns; e += 32) buf[w][e] = slist[s0 + e];
   __syncwarp();
   for (int e = lane; e < ns; e += 32) {
@@ -372,7 +386,7 @@ __device__ __forceinline__ void mlp_layer(const __nv_bfloat16* in, int ldin, con
   __syncwarp();
 }
 
-// persistent: each CTA stages the weights once and walks tiles of 64 atoms.
+// persistent: each CTA stages the weights once and walks tiles of TILE_I = 256 atoms.
 // out = frec0 + fs * R^T y (lab frame)
 __global__ void __launch_bounds__(INFER_NT) k_mlp_infer(int n, const __nv_bfloat16* __restrict__ X, Net net,
                                                    const float* __restrict__ frec0, const float* __restrict__ frame,
@@ -788,13 +802,15 @@ void mts_short_list() {
   GB_CUDA(cudaStreamSynchronize(g.stream));
   if ((long long)total > M.scap) {
     if (M.slist) cudaFree(M.slist);
+    if (M.stmp) cudaFree(M.stmp);
     M.scap = (long long)(total * 1.25) + 1024;
     GB_CUDA(cudaMalloc(&M.slist, sizeof(int) * M.scap));
+    GB_CUDA(cudaMalloc(&M.stmp, sizeof(int) * M.scap));
   }
   k_short_fill<<<nblocks((long long)n * 32, 256), 256, 0, g.stream>>>(n, g.list, g.ld, g.xf, rs2, M.sstart, M.sown,
                                                                        M.sfill, M.slist);
   GB_LAUNCHED();
-  k_short_sort<<<nblocks(n, 8), 256, 0, g.stream>>>(n, M.sstart, M.slist);
+  k_short_sort<<<nblocks(n, 8), 256, 0, g.stream>>>(n, M.sstart, M.slist, M.stmp);
   GB_LAUNCHED();
   M.gen_seen = g.list_gen;
 }
@@ -936,7 +952,7 @@ void mts_set_topology(int ntcons, const int32_t* listcon, const double* weight) 
 void mts_free() {
   void* ptrs[] = {M.master, M.m1, M.m2, M.grad, M.gpart, M.loss_part, M.X, M.frec0, M.frec, M.truth, M.target,
                   M.fc, M.fc0, M.x0, M.disp, M.frame, M.triple, M.scal, M.red, M.idx, M.sstart, M.scount,
-                  M.slist, M.sown, M.sfill};
+                  M.slist, M.stmp, M.sown, M.sfill};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   net_free(M.net);

@@ -86,8 +86,11 @@ class PathLib:
         return (f(st) or b"").decode()
 
     # ---------------------------------------------------------------- set-up
-    def init(self, s: System, precision: int = 0, max_list: int | None = None, device: int = 0):
+    def init(self, s: System, precision: int = 0, max_list: int | None = None, device: int = 0, **overrides):
+        """gb_init for system s; keyword overrides set gb_params fields (e.g. mxatms, shake_maxit)."""
         p = s.params(precision, max_list, device)
+        for k, v in overrides.items():
+            setattr(p, k, v)
         self.params = p
         self.sys = s
         excl = s.excl_array(p)
@@ -214,6 +217,30 @@ class PathLib:
         self._call("vv", stage, _ptr(sk, _d), _ptr(ek, _d), _ptr(it, _i), _ptr(vc, _d), _ptr(sc, _d))
         return dict(strkin=sk, engke=float(ek[0]), iters=int(it[0]), vircon=float(vc[0]), strcon=sc)
 
+    def constraints_tags(self):
+        """constraints_tags (constraints.F90:438): bond vectors of the current positions."""
+        st = self._opt("constraints_tags", c_int, [])()
+        if st != 0:
+            raise PathError(st, self.prefix + "constraints_tags", self.strerror(st))
+
+    def apply_shake(self):
+        """apply_shake (constraints.F90:1071) on the resident (unconstrained) positions."""
+        it = np.zeros(1, np.int32)
+        vc = np.zeros(1)
+        sc = np.zeros(9)
+        st = self._opt("shake", c_int, [_i, _d, _d])(_ptr(it, _i), _ptr(vc, _d), _ptr(sc, _d))
+        if st != 0:
+            raise PathError(st, self.prefix + "shake", self.strerror(st))
+        return dict(iters=int(it[0]), vircon=float(vc[0]), strcon=sc)
+
+    def apply_rattle(self):
+        """apply_rattle with kit = 1 (constraints.F90:1032) on the resident velocities."""
+        it = np.zeros(1, np.int32)
+        st = self._opt("rattle", c_int, [_i])(_ptr(it, _i))
+        if st != 0:
+            raise PathError(st, self.prefix + "rattle", self.strerror(st))
+        return int(it[0])
+
     def md_vv(self, nsteps: int):
         arr = (GbStepStats * max(1, nsteps))()
         self._call("md_run", nsteps, arr)
@@ -272,6 +299,15 @@ class PathLib:
         if st != 0:
             raise PathError(st, self.prefix + "rng_eval", self.strerror(st))
         return out if mode == 0 else out.reshape(-1, 3)
+
+    def pair_counts(self) -> list:
+        """[half-list entries, pairs inside rc, list candidates decided in exact FP64]
+        of the last force evaluation and list build (GPU library only)."""
+        out = np.zeros(3, np.int64)
+        st = self._opt("pair_counts", c_int, [POINTER(c_int64), c_int])(_ptr(out, POINTER(c_int64)), 3)
+        if st != 0:
+            raise PathError(st, self.prefix + "pair_counts", self.strerror(st))
+        return [int(v) for v in out]
 
     def mts_config(self, k: int, tol: float = 1e-4, train_steps: int = 0):
         st = self._opt("mts_config", c_int, [c_int, ctypes.c_double, c_int])(k, tol, train_steps)

@@ -51,7 +51,8 @@ class GbParams(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("ntypes", ctypes.c_int32),
         ("device", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("mxnode", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
     ]
 
 

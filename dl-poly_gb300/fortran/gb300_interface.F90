@@ -2,7 +2,7 @@
 !>
 !> Each procedure binds one entry point of include/gb300_dlpoly.h.  The call
 !> sites in the reference keep their signatures; a shim at the top of each
-!> replaced routine calls the device path and returns (see INTEGRATION.md).
+!> replaced routine calls the device path and returns.
 !> Status codes are DL_POLY error numbers: the shim passes them to error().
 Module gb300_interface
   Use, Intrinsic :: iso_c_binding, Only: c_int, c_int32_t, c_int64_t, c_double, c_ptr, c_char
@@ -18,7 +18,8 @@ Module gb300_interface
     Integer(c_int32_t) :: kmax(3)
     Integer(c_int32_t) :: nsplines, spline_pad, vdw_direct, shake_maxit, max_list, max_exclude, mxatms
     Integer(c_int32_t) :: precision, ntypes, device
-    Integer(c_int32_t) :: reserved(6)
+    Integer(c_int32_t) :: mxnode               ! comm%mxnode: gb_init refuses more than one rank
+    Integer(c_int32_t) :: reserved(5)
   End Type gb_params
 
   !> mirror of gb_step_stats
@@ -34,7 +35,7 @@ Module gb300_interface
   Logical, Public :: gb_active = .false.
 
   Public :: gb_init, gb_upload_parts, gb_download_parts, gb_relocate, gb_list_build, gb_vnl_check, &
-            gb_refresh, gb_forces, gb_spme, gb_vv, gb_md_run, gb_mts_config, gb_mts_stats, &
+            gb_refresh, gb_forces, gb_spme, gb_vv, gb_constraints_tags, gb_shake, gb_rattle, gb_md_run, gb_mts_config, gb_mts_stats, &
             gb_set_precision, gb_set_ensemble, gb_set_step, gb_thermostat_state, &
             gb_set_thermostat_state, gb_set_metal_eam, gb_metal_energies, gb_finalize
 
@@ -97,6 +98,21 @@ Module gb300_interface
       Real(c_double), Intent(Out) :: strkin(9), engke, vircon, strcon(9)
       Integer(c_int32_t), Intent(Out) :: iters
     End Function gb_vv
+
+    Integer(c_int) Function gb_constraints_tags() Bind(C, name="gb_constraints_tags")
+      Import :: c_int
+    End Function gb_constraints_tags
+
+    Integer(c_int) Function gb_shake(iters, vircon, strcon) Bind(C, name="gb_shake")
+      Import :: c_int, c_int32_t, c_double
+      Integer(c_int32_t), Intent(Out) :: iters
+      Real(c_double), Intent(Out) :: vircon, strcon(9)
+    End Function gb_shake
+
+    Integer(c_int) Function gb_rattle(iters) Bind(C, name="gb_rattle")
+      Import :: c_int, c_int32_t
+      Integer(c_int32_t), Intent(Out) :: iters
+    End Function gb_rattle
 
     Integer(c_int) Function gb_md_run(nsteps, stats) Bind(C, name="gb_md_run")
       Import :: c_int, gb_step_stats

@@ -46,6 +46,7 @@ extern "C" {
 #define GB_ERR_NONFINITE (-5)
 #define GB_ERR_TOO_LARGE (-6)  /* size beyond a fixed scratch limit (gb_kinstress_noalloc) */
 #define GB_ERR_RNG (-7)        /* a Gaussian deviate's rejection loop hit its iteration cap */
+#define GB_ERR_MULTI_RANK (-8) /* gb_params.mxnode > 1: a multi-rank run cannot use the device path */
 
 /* Precision forms of the force path. */
 #define GB_FP64 0   /* plain: FP64 accuracy; pair loop and SPME in double-float (pairs of FP32) */
@@ -83,7 +84,9 @@ typedef struct gb_params {
   int32_t precision;    /* GB_FP64, GB_MIXED or GB_FP64_NATIVE */
   int32_t ntypes;       /* sites%ntype_atom */
   int32_t device;       /* CUDA device ordinal this context uses (one GPU per process) */
-  int32_t reserved[6];
+  int32_t mxnode;       /* comm%mxnode, MPI ranks of the run: gb_init returns GB_ERR_MULTI_RANK when > 1
+                           (one rank drives one GPU; there is no domain decomposition, comms.F90) */
+  int32_t reserved[5];
 } gb_params;
 
 /* Per-step scalars returned by the resident MD loop. */
@@ -186,6 +189,23 @@ int gb_real(double* eng_out, double* stress_out);
  * nvt_l0_vv instead. */
 int gb_vv(int stage, double* strkin, double* engke, int32_t* iters, double* vircon,
           double* strcon);
+
+/* The constraint parts of the VV stages on their own, for a driver that runs its own
+ * stage update (another ensemble's Fortran stage) and calls apply_shake / apply_rattle
+ * itself; gb_vv calls the same code.  They act on the resident state (gb_upload_state
+ * first when the host changed it):
+ *   gb_constraints_tags  constraints_tags (constraints.F90:438-586): the old bond vectors
+ *                        from the current positions; call before the stage-1 drift.
+ *   gb_shake             apply_shake (constraints.F90:1071-1200): the current positions are
+ *                        the unconstrained ones; SHAKE (constraints_shake_vv :777-1030), then
+ *                        the velocity and force corrections; returns 105 when SHAKE does not
+ *                        converge in shake_maxit sweeps.
+ *   gb_rattle            apply_rattle with kit = 1 (constraints.F90:1032-1069 ->
+ *                        constraints_rattle :587-775) on the current velocities; returns 515
+ *                        when RATTLE does not converge. */
+int gb_constraints_tags(void);
+int gb_shake(int32_t* iters, double* vircon, double* strcon);
+int gb_rattle(int32_t* iters);
 
 /* Resident MD loop (md_vv, drivers.F90:2059-2288): nsteps of VV1+SHAKE,
  * refresh, forces, VV2+RATTLE with no host round trip; stats[nsteps] may be NULL.

@@ -92,7 +92,6 @@ struct Ctx {
   std::vector<double> oxt, oyt, ozt;
   // neighbour list update flag
   bool update = true;
-  int nthreads = 1;
   // thermostat (thermo%ensemble and its state)
   int ens = GB_NVE;
   double temp = 0, tau_t = 0, chi = 0, sigma = 0, qmass = 0, ceng = 0, totmas = 0;
@@ -109,6 +108,8 @@ struct Ctx {
 };
 
 Ctx g;
+// Host threads of the OpenMP build; kept outside Ctx so that orc_init does not reset it.
+int g_nthreads = 1;
 
 // ---------------------------------------------------------------- numerics
 // dcell: source/numerics.F90:1344-1443
@@ -832,7 +833,7 @@ void pair_loop(int i0, int i1, double* fxo, double* fyo, double* fzo, Acc& A) {
 void two_body_real(Acc& A) {
   const int nl = g.nlast;
 #ifdef ORACLE_OPENMP
-  int nt = g.nthreads;
+  int nt = g_nthreads;
   if (nt > 1) {
     std::vector<std::vector<double>> F(nt, std::vector<double>((size_t)3 * nl, 0.0));
     std::vector<Acc> As(nt);
@@ -936,21 +937,42 @@ void splines_1d(double u, double d[3][21]) {
 // In-place unnormalised complex DFT of length n along a strided line:
 // x(j) = sum_k c(k) exp(isign*2*pi*i*j*k/n)  (gpfa235.F90:39-132 definition).
 // Recursive mixed-radix Cooley-Tukey; the rounding differs from GPFA by O(1e-16).
-void fft1d(std::complex<double>* a, int n, int isign, std::vector<std::complex<double>>& tmp) {
+// The twiddle w(m) = exp(isign*2*pi*i*m/n) is tabulated per (n, isign) with the
+// angle formed as isign*2*pi*m/n, so every factor is the value the butterfly
+// would compute for the exponent (q*kk) mod n.
+const std::complex<double>* twiddles(int n, int isign) {
+  thread_local std::vector<std::vector<std::complex<double>>> tab[2];
+  auto& t = tab[isign > 0 ? 1 : 0];
+  if ((int)t.size() <= n) t.resize(n + 1);
+  auto& w = t[n];
+  if (w.empty()) {
+    w.resize(n);
+    for (int m = 0; m < n; ++m) {
+      double ang = (double)isign * 2.0 * kPi * (double)m / (double)n;
+      w[m] = std::complex<double>(std::cos(ang), std::sin(ang));
+    }
+  }
+  return w.data();
+}
+
+// work holds at least 2n values: this level's reordered copy, then the deeper levels'.
+void fft1d(std::complex<double>* a, int n, int isign, std::complex<double>* work) {
   if (n == 1) return;
   int r = (n % 2 == 0) ? 2 : (n % 3 == 0) ? 3 : (n % 5 == 0) ? 5 : n;
   int m = n / r;
-  std::vector<std::complex<double>> sub((size_t)n);
+  std::complex<double>* sub = work;
   for (int q = 0; q < r; ++q)
     for (int k = 0; k < m; ++k) sub[(size_t)q * m + k] = a[(size_t)k * r + q];
-  for (int q = 0; q < r; ++q) fft1d(&sub[(size_t)q * m], m, isign, tmp);
+  for (int q = 0; q < r; ++q) fft1d(&sub[(size_t)q * m], m, isign, work + n);
+  const std::complex<double>* w = twiddles(n, isign);
   for (int k = 0; k < m; ++k)
     for (int t = 0; t < r; ++t) {
       std::complex<double> acc(0.0, 0.0);
       int kk = k + t * m;
-      for (int q = 0; q < r; ++q) {
-        double ang = (double)isign * 2.0 * kPi * (double)(((long)q * kk) % n) / (double)n;
-        acc += sub[(size_t)q * m + k] * std::complex<double>(std::cos(ang), std::sin(ang));
+      for (int q = 0, e = 0; q < r; ++q) {  // e = (q * kk) mod n
+        acc += sub[(size_t)q * m + k] * w[e];
+        e += kk;
+        if (e >= n) e -= n;
       }
       a[kk] = acc;
     }
@@ -958,31 +980,30 @@ void fft1d(std::complex<double>* a, int n, int isign, std::vector<std::complex<d
 
 void fft3d(std::vector<std::complex<double>>& G, int isign) {
   const int K1 = g.p.kmax[0], K2 = g.p.kmax[1], K3 = g.p.kmax[2];
-  std::vector<std::complex<double>> tmp;
-  int nt = g.nthreads;
+  const int Kmax = std::max(K1, std::max(K2, K3));
+  int nt = g_nthreads;
   (void)nt;
-#pragma omp parallel for num_threads(nt) collapse(2) if (nt > 1)
-  for (int l = 0; l < K3; ++l)
-    for (int k = 0; k < K2; ++k) {
-      std::vector<std::complex<double>> t2;
-      fft1d(&G[((size_t)l * K2 + k) * K1], K1, isign, t2);
-    }
-#pragma omp parallel for num_threads(nt) collapse(2) if (nt > 1)
-  for (int l = 0; l < K3; ++l)
-    for (int j = 0; j < K1; ++j) {
-      std::vector<std::complex<double>> line(K2), t2;
-      for (int k = 0; k < K2; ++k) line[k] = G[((size_t)l * K2 + k) * K1 + j];
-      fft1d(line.data(), K2, isign, t2);
-      for (int k = 0; k < K2; ++k) G[((size_t)l * K2 + k) * K1 + j] = line[k];
-    }
-#pragma omp parallel for num_threads(nt) collapse(2) if (nt > 1)
-  for (int k = 0; k < K2; ++k)
-    for (int j = 0; j < K1; ++j) {
-      std::vector<std::complex<double>> line(K3), t2;
-      for (int l = 0; l < K3; ++l) line[l] = G[((size_t)l * K2 + k) * K1 + j];
-      fft1d(line.data(), K3, isign, t2);
-      for (int l = 0; l < K3; ++l) G[((size_t)l * K2 + k) * K1 + j] = line[l];
-    }
+#pragma omp parallel num_threads(nt) if (nt > 1)
+  {
+    std::vector<std::complex<double>> line(Kmax), work(2 * (size_t)Kmax);
+#pragma omp for collapse(2)
+    for (int l = 0; l < K3; ++l)
+      for (int k = 0; k < K2; ++k) fft1d(&G[((size_t)l * K2 + k) * K1], K1, isign, work.data());
+#pragma omp for collapse(2)
+    for (int l = 0; l < K3; ++l)
+      for (int j = 0; j < K1; ++j) {
+        for (int k = 0; k < K2; ++k) line[k] = G[((size_t)l * K2 + k) * K1 + j];
+        fft1d(line.data(), K2, isign, work.data());
+        for (int k = 0; k < K2; ++k) G[((size_t)l * K2 + k) * K1 + j] = line[k];
+      }
+#pragma omp for collapse(2)
+    for (int k = 0; k < K2; ++k)
+      for (int j = 0; j < K1; ++j) {
+        for (int l = 0; l < K3; ++l) line[l] = G[((size_t)l * K2 + k) * K1 + j];
+        fft1d(line.data(), K3, isign, work.data());
+        for (int l = 0; l < K3; ++l) G[((size_t)l * K2 + k) * K1 + j] = line[l];
+      }
+  }
 }
 
 // ewald_spme_forces_coul: source/ewald_spole.F90:244-477, with
@@ -1011,23 +1032,53 @@ void spme(double* eng_rc, double* vir_rc, double* stress9, double* fxo, double* 
       to_calc.push_back(i);
     for (int d = 0; d < 3; ++d) rind[3 * i + d] = fint(u[3 * i + d]);
   }
-  // charge spreading with clamping to the grid block (serial block = whole grid)
+  // charge spreading with clamping to the grid block (serial block = whole grid).
+  // The OpenMP build gives each thread a range of z planes; every grid point still
+  // receives its terms in atom order, so the grid equals the serial one bit for bit.
   std::vector<double> Q((size_t)K1 * K2 * K3, 0.0);
-  for (int i : to_calc) {
-    double spl[3][3][21];
-    for (int d = 0; d < 3; ++d) splines_1d(u[3 * i + d], spl[d]);
-    const int n1 = rind[3 * i], n2 = rind[3 * i + 1], n3 = rind[3 * i + 2];
-    int j_lo = std::max(1, n1 - 1 - s + 3), k_lo = std::max(1, n2 - 1 - s + 3), l_lo = std::max(1, n3 - 1 - s + 3);
-    int j_hi = std::min(K1, n1 + 1) - 1 + 1, k_hi = std::min(K2, n2 + 1) - 1 + 1, l_hi = std::min(K3, n3 + 1) - 1 + 1;
-    if (j_hi - j_lo < 0 || k_hi - k_lo < 0 || l_hi - l_lo < 0) continue;
-    int t1 = n1 - s - 1 + 2, t2 = n2 - s - 1 + 2, t3 = n3 - s - 1 + 2;
-    double q = g.chge[i];
-    for (int l = l_lo; l <= l_hi; ++l) {
-      double f1 = q * spl[2][0][l - t3];
-      for (int k = k_lo; k <= k_hi; ++k) {
-        double f2 = f1 * spl[1][0][k - t2];
-        double* row = &Q[((size_t)(l - 1) * K2 + (k - 1)) * K1];
-        for (int j = j_lo; j <= j_hi; ++j) row[j - 1] = row[j - 1] + f2 * spl[0][0][j - t1];
+  const int ncalc = (int)to_calc.size();
+  std::vector<double> sp0((size_t)ncalc * 3 * s);  // order-0 splines of the spread atoms
+  {
+    int nt = g_nthreads;
+    (void)nt;
+#pragma omp parallel for num_threads(nt) if (nt > 1)
+    for (int a = 0; a < ncalc; ++a) {
+      const int i = to_calc[a];
+      double spl[3][21];
+      for (int d = 0; d < 3; ++d) {
+        double dd[3][21];
+        splines_1d(u[3 * i + d], dd);
+        for (int t = 1; t <= s; ++t) sp0[((size_t)a * 3 + d) * s + (t - 1)] = dd[0][t];
+      }
+      (void)spl;
+    }
+#pragma omp parallel num_threads(nt) if (nt > 1)
+    {
+      int tid = 0, ntt = 1;
+#ifdef ORACLE_OPENMP
+      tid = omp_get_thread_num();
+      ntt = omp_get_num_threads();
+#endif
+      const int pl0 = 1 + (int)((long)K3 * tid / ntt), pl1 = (int)((long)K3 * (tid + 1) / ntt);
+      for (int a = 0; a < ncalc; ++a) {
+        const int i = to_calc[a];
+        const double* sx = &sp0[((size_t)a * 3 + 0) * s];
+        const double* sy = &sp0[((size_t)a * 3 + 1) * s];
+        const double* sz = &sp0[((size_t)a * 3 + 2) * s];
+        const int n1 = rind[3 * i], n2 = rind[3 * i + 1], n3 = rind[3 * i + 2];
+        int j_lo = std::max(1, n1 - 1 - s + 3), k_lo = std::max(1, n2 - 1 - s + 3), l_lo = std::max(1, n3 - 1 - s + 3);
+        int j_hi = std::min(K1, n1 + 1) - 1 + 1, k_hi = std::min(K2, n2 + 1) - 1 + 1, l_hi = std::min(K3, n3 + 1) - 1 + 1;
+        if (j_hi - j_lo < 0 || k_hi - k_lo < 0 || l_hi - l_lo < 0) continue;
+        int t1 = n1 - s - 1 + 2, t2 = n2 - s - 1 + 2, t3 = n3 - s - 1 + 2;
+        double q = g.chge[i];
+        for (int l = std::max(l_lo, pl0); l <= std::min(l_hi, pl1); ++l) {
+          double f1 = q * sz[l - t3 - 1];
+          for (int k = k_lo; k <= k_hi; ++k) {
+            double f2 = f1 * sy[k - t2 - 1];
+            double* row = &Q[((size_t)(l - 1) * K2 + (k - 1)) * K1];
+            for (int j = j_lo; j <= j_hi; ++j) row[j - 1] = row[j - 1] + f2 * sx[j - t1 - 1];
+          }
+        }
       }
     }
   }
@@ -1042,7 +1093,8 @@ void spme(double* eng_rc, double* vir_rc, double* stress9, double* fxo, double* 
   double cut_off = 0.5 * 1.05 * std::min(Kr[0] * rcp[6], std::min(Kr[1] * rcp[7], Kr[2] * rcp[8]));
   double cut_off_2 = cut_off * cut_off;
   double st[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  for (int l = 1; l <= K3; ++l) {
+  // one z plane of the influence-function multiply; its stress terms go to sp
+  auto influence_plane = [&](int l, double (&sp)[3][3]) {
     int ll = l - 1; if (2 * ll > K3) ll -= K3;
     double rp3[3] = {(double)ll * rc[2], (double)ll * rc[5], (double)ll * rc[8]};
     double bb3 = g.norm2[2][l - 1];
@@ -1061,13 +1113,31 @@ void spme(double* eng_rc, double* vir_rc, double* stress9, double* fxo, double* 
           std::complex<double> pc = bb1 * cell * std::exp(-(fpf * fpf)) / (kSqrpi * fpf * fpf);
           double pv = (pc * (-2.0 * ((1.0 + fpf * fpf) / k2)) * std::conj(cell)).real();
           for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) st[a][b] += rp1[a] * rp1[b] * pv;
+            for (int b = 0; b < 3; ++b) sp[a][b] += rp1[a] * rp1[b] * pv;
           cell = pc;
         } else {
           cell = {0.0, 0.0};
         }
       }
     }
+    };
+#ifdef ORACLE_OPENMP
+  if (g_nthreads > 1) {
+    std::vector<double> part((size_t)g_nthreads * 9, 0.0);
+#pragma omp parallel num_threads(g_nthreads)
+    {
+      double sp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma omp for schedule(static)
+      for (int l = 1; l <= K3; ++l) influence_plane(l, sp);
+      const int t = omp_get_thread_num();
+      for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) part[(size_t)t * 9 + 3 * a + b] = sp[a][b];
+    }
+    for (int t = 0; t < g_nthreads; ++t)
+      for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) st[a][b] += part[(size_t)t * 9 + 3 * a + b];
+  } else
+#endif
+  {
+    for (int l = 1; l <= K3; ++l) influence_plane(l, st);
   }
   fft3d(G, -1);
   // gather over local atoms with the periodic extended grid (real part)
@@ -1079,12 +1149,11 @@ void spme(double* eng_rc, double* vir_rc, double* stress9, double* fxo, double* 
     int a = ((jj % K1) + K1) % K1, b = ((kk % K2) + K2) % K2, c = ((ll % K3) + K3) % K3;
     return G[((size_t)c * K2 + b) * K1 + a].real();
   };
-  for (int i = 0; i < g.natms; ++i) {
-    if (std::fabs(g.chge[i]) <= kZeroPlus) continue;
+  // one atom's gather: its energy term et and force sums cf; the net-force terms go to ft
+  auto gather_atom = [&](int i, double& et, double (&cf)[3], double (&ft)[3]) {
     double spl[3][3][21];
     for (int d = 0; d < 3; ++d) splines_1d(u[3 * i + d], spl[d]);
     double q = g.chge[i];
-    double et = 0.0, cf[3] = {0, 0, 0};
     for (int l = 1; l <= s; ++l) {
       int ll = rind[3 * i + 2] + 1 - s + l - 1;  // 0-based
       double e2 = q * spl[2][0][l];
@@ -1099,14 +1168,44 @@ void spme(double* eng_rc, double* vir_rc, double* stress9, double* fxo, double* 
           double a0 = ft12 * spl[0][1][j] * ph * rkmax[0];
           double a1 = ft22 * spl[0][0][j] * ph * rkmax[1];
           double a2 = ft32 * spl[0][0][j] * ph * rkmax[2];
-          ftot[0] -= a0; ftot[1] -= a1; ftot[2] -= a2;
+          ft[0] -= a0; ft[1] -= a1; ft[2] -= a2;
           cf[0] += a0; cf[1] += a1; cf[2] += a2;
           et += e1 * spl[0][0][j] * ph;
         }
       }
     }
-    energy0 += et;
-    F[3 * i] -= cf[0]; F[3 * i + 1] -= cf[1]; F[3 * i + 2] -= cf[2];
+  };
+#ifdef ORACLE_OPENMP
+  if (g_nthreads > 1) {
+    std::vector<double> part((size_t)g_nthreads * 4, 0.0);
+#pragma omp parallel num_threads(g_nthreads)
+    {
+      double e = 0.0, ft[3] = {0, 0, 0};
+#pragma omp for schedule(static)
+      for (int i = 0; i < g.natms; ++i) {
+        if (std::fabs(g.chge[i]) <= kZeroPlus) continue;
+        double et = 0.0, cf[3] = {0, 0, 0};
+        gather_atom(i, et, cf, ft);
+        e += et;
+        F[3 * i] -= cf[0]; F[3 * i + 1] -= cf[1]; F[3 * i + 2] -= cf[2];
+      }
+      const int t = omp_get_thread_num();
+      part[4 * t] = e; part[4 * t + 1] = ft[0]; part[4 * t + 2] = ft[1]; part[4 * t + 3] = ft[2];
+    }
+    for (int t = 0; t < g_nthreads; ++t) {
+      energy0 += part[4 * t];
+      for (int a = 0; a < 3; ++a) ftot[a] += part[4 * t + 1 + a];
+    }
+  } else
+#endif
+  {
+    for (int i = 0; i < g.natms; ++i) {
+      if (std::fabs(g.chge[i]) <= kZeroPlus) continue;
+      double et = 0.0, cf[3] = {0, 0, 0};
+      gather_atom(i, et, cf, ftot);
+      energy0 += et;
+      F[3 * i] -= cf[0]; F[3 * i + 1] -= cf[1]; F[3 * i + 2] -= cf[2];
+    }
   }
   for (int a = 0; a < 3; ++a) ftot[a] /= (double)g.natms;  // megatm
   for (int i = 0; i < g.natms; ++i)
@@ -1922,7 +2021,7 @@ int orc_init(const gb_params* prm, int natms, const int32_t* ltype, const double
   return GB_OK;
 }
 
-int orc_set_threads(int n) { g.nthreads = n < 1 ? 1 : n; return GB_OK; }
+int orc_set_threads(int n) { g_nthreads = n < 1 ? 1 : n; return GB_OK; }
 
 int orc_upload_state(const double* x, const double* y, const double* z, const double* vx, const double* vy,
                      const double* vz) {

@@ -205,3 +205,105 @@ def test_cutoff_larger_than_half_cell_rejected(gpu_lib):
     with pytest.raises(Exception) as e:
         gpu_lib.init(s)
     assert getattr(e.value, "code", None) == 95
+
+
+def test_shake_nonconvergence_status(gpu_lib):
+    """SHAKE that does not converge within shake_maxit returns 105 (constraints.F90:996);
+    the context stays usable for a clean run afterwards."""
+    s = systems.spce_water(8)
+    gpu_lib.init(s, shake_maxit=2)  # the lattice start needs ~65 sweeps at tolerance 1e-8
+    gpu_lib.start()
+    with pytest.raises(Exception) as e:
+        gpu_lib.md_vv(1)
+    assert getattr(e.value, "code", None) == 105
+    gpu_lib.init(s)
+    gpu_lib.start()
+    st = gpu_lib.md_vv(2)
+    assert all(x.shake_iters > 2 for x in st)
+
+
+def test_rattle_nonconvergence_status(gpu_lib):
+    """RATTLE that does not converge within shake_maxit returns 515 (constraints.F90:748)."""
+    s = systems.spce_water(8)
+    gpu_lib.init(s, shake_maxit=2)
+    gpu_lib.start()
+    d = gpu_lib.download()
+    rng = np.random.default_rng(7)
+    # velocities far off the constraint manifold: RATTLE needs many sweeps
+    v = [d[k] + rng.normal(0.0, 5.0, s.natms) for k in ("vx", "vy", "vz")]
+    gpu_lib.upload(d["x"], d["y"], d["z"], *v)
+    gpu_lib.constraints_tags()
+    with pytest.raises(Exception) as e:
+        gpu_lib.apply_rattle()
+    assert getattr(e.value, "code", None) == 515
+    gpu_lib.init(s)
+    gpu_lib.start()
+    assert all(x.rattle_iters > 2 for x in gpu_lib.md_vv(2))
+
+
+def test_halo_overflow_status(gpu_lib):
+    """More halo images than mxatms holds returns 56 (deport_data.F90:1870)."""
+    s = systems.nacl_melt(16)
+    gpu_lib.init(s, mxatms=s.natms + 64)
+    with pytest.raises(Exception) as e:
+        gpu_lib.relocate()
+    assert getattr(e.value, "code", None) == 56
+    gpu_lib.init(s)
+    gpu_lib.relocate()
+    assert gpu_lib.list_build_status()[0] == 0
+
+
+def test_multi_rank_rejected(gpu_lib):
+    """A run with more than one MPI rank (comm%mxnode > 1) cannot use the device path."""
+    s = systems.nacl_melt(16)
+    with pytest.raises(Exception) as e:
+        gpu_lib.init(s, mxnode=2)
+    assert getattr(e.value, "code", None) == -8
+    gpu_lib.init(s, mxnode=1)
+
+
+def test_mts_rejects_cutoff_below_descriptor_reach(gpu_lib):
+    """The learned form's neighbour sums reach 6 A: a shorter pair cutoff is refused."""
+    s = systems.nacl_melt(16, rcut=5.0)
+    gpu_lib.init(s, precision=1)
+    with pytest.raises(Exception) as e:
+        gpu_lib.mts_config(4, 1e-4, 10)
+    assert getattr(e.value, "code", None) == -3
+
+
+def test_shake_rattle_exports_match_vv(gpu_lib):
+    """gb_constraints_tags + a host-side stage update + gb_shake / gb_rattle (the
+    apply_shake / apply_rattle shims) give the same state as gb_vv's stages."""
+    s = systems.spce_water(8)
+    out = []
+    for split in (False, True):
+        gpu_lib.init(s)
+        gpu_lib.start()
+        dt = s.tstep
+        if not split:
+            a = gpu_lib.nve_0_vv(1)
+            gpu_lib.refresh()
+            gpu_lib.two_body_forces()
+            b_it = gpu_lib.nve_0_vv(2)["iters"]
+            out.append((gpu_lib.download(), a["iters"], b_it, a["strcon"]))
+            continue
+        d = gpu_lib.download()
+        gpu_lib.constraints_tags()
+        m = s.weight
+        v = [d[k] + 0.5 * dt / m * d[f] for k, f in (("vx", "fx"), ("vy", "fy"), ("vz", "fz"))]
+        x = [d[k] + dt * vv for k, vv in zip(("x", "y", "z"), v)]
+        gpu_lib.upload(*x, *v)
+        sh = gpu_lib.apply_shake()
+        gpu_lib.refresh()
+        gpu_lib.two_body_forces()
+        d = gpu_lib.download()
+        gpu_lib.constraints_tags()
+        v = [d[k] + 0.5 * dt / m * d[f] for k, f in (("vx", "fx"), ("vy", "fy"), ("vz", "fz"))]
+        gpu_lib.upload(d["x"], d["y"], d["z"], *v)
+        r_it = gpu_lib.apply_rattle()
+        out.append((gpu_lib.download(), sh["iters"], r_it, sh["strcon"]))
+    (a, sa, ra, ca), (b, sb, rb, cb) = out
+    assert (sa, ra) == (sb, rb) and sa > 1 and ra > 1
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert np.abs(a[k] - b[k]).max() <= 1e-12 * np.abs(a[k]).max(), k
+    assert np.abs(ca - cb).max() <= 1e-10 * np.abs(ca).max()

@@ -1,0 +1,201 @@
+"""GPU parity at the sizes the benchmark times.
+
+The CUDA path against the FP64 oracle on the benchmark workloads themselves:
+  - the 262,144-ion NaCl melt (64^3 rock-salt sites, 180.48 A box, SPME 192^3):
+    the whole Verlet list bit-exact, forces / energies / virials / stress within
+    1e-10 at step 0 and at each of the first 10 resident MD steps;
+  - the 98,304-atom SPC/E-style water (32,768 rigid molecules, SPME 100^3):
+    the same, plus SHAKE/RATTLE iteration counts step by step;
+  - SPME alone on 100^3, 160^3 and 192^3 grids (radix-5 lengths and the
+    transform kernels compiled for those lengths) in all three forms.
+
+At these sizes the checker is the oracle's OpenMP build on all host cores: the
+same restatement, with only the order of a few reductions (per-thread partial
+sums of energies, stress and the net-force term) changed, which moves results by
+~1e-13 relative, far inside the 1e-10 bar.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import force_dev, force_rms_rel
+from dlpoly_gb300 import systems
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+FP64_TOL = 1e-10
+NSTEPS = 10
+
+
+@pytest.fixture(scope="module")
+def oracle_omp():
+    import oracle
+
+    lib = oracle.load(openmp=True)
+    lib.lib.orc_set_threads(os.cpu_count() or 1)
+    return lib
+
+
+def _close(a, b, tol, scale=1.0):
+    return abs(a - b) <= tol * max(abs(b), scale)
+
+
+def _check_forces(gpu_lib, oracle_omp, tol=FP64_TOL):
+    a, b = gpu_lib.download(), oracle_omp.download()
+    dev = force_dev(a, b)
+    assert dev < tol, dev
+    return a, b, dev
+
+
+STAT_KEYS = ("engcpe_rc", "vircpe_rc", "engcpe_rl", "vircpe_rl", "engcpe_ex", "vircpe_ex", "engvdw", "virvdw",
+             "engke", "vircon")
+
+
+def _check_stats(sd, sr, tol=FP64_TOL):
+    """Per-step scalars and tensors of gb_md_run against the oracle's md_vv."""
+    for x, y in zip(sd, sr):
+        # terms that cancel (virials, constraint virial) are compared against the step's energy scale
+        scale = max(abs(y.engcpe_rc), abs(y.engcpe_rl), abs(y.engvdw), 1.0)
+        for k in STAT_KEYS:
+            assert _close(getattr(x, k), getattr(y, k), tol, scale), (k, getattr(x, k), getattr(y, k))
+        st_scale = max(np.abs(np.array(y.stress[:])).max(), 1.0)
+        assert np.abs(np.array(x.stress[:]) - np.array(y.stress[:])).max() <= tol * st_scale
+        ks = max(np.abs(np.array(y.strkin[:])).max(), 1.0)
+        assert np.abs(np.array(x.strkin[:]) - np.array(y.strkin[:])).max() <= tol * ks
+
+
+def _start(gpu_lib, oracle_omp, s, precision=0):
+    gpu_lib.init(s, precision=precision)
+    oracle_omp.init(s)
+    gpu_lib.relocate()
+    oracle_omp.relocate()
+
+
+def test_nacl_262144_list_bit_exact(gpu_lib, oracle_omp):
+    """Config 2: 262,144 ions, 59 M half-list entries; the whole list(-3:max_list, natms)
+    array (markers, entries and their order) equals the oracle's."""
+    s = systems.nacl_melt(64)
+    assert s.natms == 262144 and tuple(s.kmax) == (192, 192, 192)
+    _start(gpu_lib, oracle_omp, s)
+    ld = gpu_lib.link_cell_pairs()
+    lr = oracle_omp.link_cell_pairs()
+    assert ld.shape == lr.shape
+    assert np.array_equal(ld, lr)
+    n_entries = int(lr[:, 3].astype(np.int64).sum())
+    cnt = gpu_lib.pair_counts()
+    # list entries whose FP32 distance fell inside the prefilter band around (rc+pad)^2
+    # and were decided by the exact FP64 test
+    print(f"\n262,144 ions: {n_entries} list entries, {cnt[2]} decided in exact FP64 near (rc+pad)^2")
+    assert n_entries > 50_000_000
+    assert cnt[2] > 0
+
+
+def test_nacl_262144_forces_and_10_steps(gpu_lib, oracle_omp):
+    """Config 2: forces, the 8 energies/virials and the stress at step 0, then the
+    per-step forces and scalars of the first 10 resident MD steps (NVE, dt 2 fs)."""
+    s = systems.nacl_melt(64)
+    _start(gpu_lib, oracle_omp, s)
+    gpu_lib.link_cell_pairs(want_list=False)
+    oracle_omp.link_cell_pairs(want_list=False)
+    ed, sd = gpu_lib.two_body_forces()
+    er, sr = oracle_omp.two_body_forces()
+    _check_forces(gpu_lib, oracle_omp)
+    scale = max(abs(er["engcpe_rc"]), abs(er["engcpe_rl"]), abs(er["engvdw"]))
+    for k in er:
+        assert _close(ed[k], er[k], FP64_TOL, scale), (k, ed[k], er[k])
+    assert np.abs(sd - sr).max() <= FP64_TOL * np.abs(sr).max()
+    devs = []
+    rebuilt = []
+    for _ in range(NSTEPS):
+        xd = gpu_lib.md_vv(1)
+        xr = oracle_omp.md_vv(1)
+        assert xd[0].list_rebuilt == xr[0].list_rebuilt
+        rebuilt.append(xr[0].list_rebuilt)
+        _check_stats(xd, xr)
+        devs.append(_check_forces(gpu_lib, oracle_omp)[2])
+    a, b = gpu_lib.download(), oracle_omp.download()
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert np.abs(a[k] - b[k]).max() <= 1e-10 * np.abs(b[k]).max(), k
+    print(f"\n262,144 ions: max force deviation per step {max(devs):.2e}, list rebuilt at steps "
+          f"{[k + 1 for k, r in enumerate(rebuilt) if r]}")
+
+
+def test_nacl_262144_mixed_error(gpu_lib, oracle_omp):
+    """Mixed form at config 2 size: rms force error <= 1e-5 relative to the FP64 oracle."""
+    s = systems.nacl_melt(64)
+    _start(gpu_lib, oracle_omp, s, precision=1)
+    gpu_lib.link_cell_pairs(want_list=False)
+    oracle_omp.link_cell_pairs(want_list=False)
+    gpu_lib.two_body_forces()
+    oracle_omp.two_body_forces()
+    err = force_rms_rel(gpu_lib.download(), oracle_omp.download())
+    print(f"\n262,144 ions, mixed form: rms force error {err:.2e}")
+    assert err <= 1e-5
+
+
+def test_water_98304_forces_and_10_steps(gpu_lib, oracle_omp):
+    """Config 4: 98,304-atom water (exclusion correction, 98,304 constraints): forces at
+    step 0, then 10 MD steps with SHAKE/RATTLE iteration counts equal to the oracle's."""
+    s = systems.spce_water(32)
+    assert s.natms == 98304 and tuple(s.kmax) == (100, 100, 100)
+    _start(gpu_lib, oracle_omp, s)
+    ld = gpu_lib.link_cell_pairs()
+    lr = oracle_omp.link_cell_pairs()
+    assert np.array_equal(ld, lr)
+    ed, sd = gpu_lib.two_body_forces()
+    er, sr = oracle_omp.two_body_forces()
+    _check_forces(gpu_lib, oracle_omp)
+    scale = max(abs(er["engcpe_rc"]), abs(er["engcpe_rl"]), abs(er["engcpe_ex"]))
+    for k in er:
+        assert _close(ed[k], er[k], FP64_TOL, scale), (k, ed[k], er[k])
+    assert np.abs(sd - sr).max() <= FP64_TOL * np.abs(sr).max()
+    sd_all, sr_all = [], []
+    for _ in range(NSTEPS):
+        xd = gpu_lib.md_vv(1)
+        xr = oracle_omp.md_vv(1)
+        sd_all += xd
+        sr_all += xr
+        assert (xd[0].shake_iters, xd[0].rattle_iters) == (xr[0].shake_iters, xr[0].rattle_iters)
+        assert xd[0].list_rebuilt == xr[0].list_rebuilt
+        _check_forces(gpu_lib, oracle_omp)
+    _check_stats(sd_all, sr_all)
+    for x, y in zip(sd_all, sr_all):
+        cs = max(np.abs(np.array(y.strcon[:])).max(), 1e-30)
+        assert np.abs(np.array(x.strcon[:]) - np.array(y.strcon[:])).max() <= 1e-9 * cs
+    a, b = gpu_lib.download(), oracle_omp.download()
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert np.abs(a[k] - b[k]).max() <= 1e-10 * np.abs(b[k]).max(), k
+    print(f"\n98,304-atom water: SHAKE iterations {[x.shake_iters for x in sr_all]}, "
+          f"RATTLE {[x.rattle_iters for x in sr_all]}")
+
+
+SPME_GRIDS = {
+    "water_98304_k100": lambda: systems.spce_water(32),
+    "nacl_262144_k160": lambda: systems.nacl_melt(64, kmax=160),
+    "nacl_262144_k192": lambda: systems.nacl_melt(64),
+}
+
+
+@pytest.mark.parametrize("name", list(SPME_GRIDS))
+def test_spme_alone_large_grids(gpu_lib, oracle_omp, name):
+    """ewald_spme_forces_coul alone on the 100^3, 160^3 and 192^3 grids: the double-float
+    and native FP64 forms within 1e-10 of the oracle, the mixed form within its bound."""
+    s = SPME_GRIDS[name]()
+    oracle_omp.init(s)
+    oracle_omp.relocate()
+    er, vr, sr = oracle_omp.ewald_spme_forces()
+    b = oracle_omp.download()
+    for precision in (0, 2, 1):
+        gpu_lib.init(s, precision=precision)
+        gpu_lib.relocate()
+        ed, vd, sd = gpu_lib.ewald_spme_forces()
+        a = gpu_lib.download()
+        if precision == 1:
+            assert force_rms_rel(a, b) <= 1e-5, precision
+            assert ed == pytest.approx(er, rel=1e-6)
+        else:
+            assert force_dev(a, b) < FP64_TOL, precision
+            assert ed == pytest.approx(er, rel=FP64_TOL)
+            assert vd == pytest.approx(vr, rel=1e-9)
+            assert np.abs(sd - sr).max() <= 1e-9 * np.abs(sr).max()

@@ -58,6 +58,57 @@ def test_kinstress_noalloc_matches_gb_vv(gpu_lib):
         out.fill_(float("nan"))
 
 
+def _kin_numpy(d, w, frozen=None):
+    """kinstress (kinetics.F90:218-262) in numpy: atoms with lfrzn != 0 are left out."""
+    v = np.stack([d["vx"], d["vy"], d["vz"]], 1)
+    m = w.copy()
+    if frozen is not None:
+        m = np.where(frozen != 0, 0.0, m)
+    return np.einsum("i,ia,ib->ab", m, v, v).reshape(9)
+
+
+def test_kinstress_noalloc_frozen_atoms_and_edge_sizes(gpu_lib):
+    """The lfrzn != 0 branch (some atoms frozen), lfrzn = NULL (no frozen atoms) and n = 0."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device visible to torch")
+    f = _bind(gpu_lib.lib)
+    s = systems.nacl_melt(16)
+    s.lfrzn = np.zeros(s.natms, np.int32)
+    s.lfrzn[::97] = 1
+    gpu_lib.init(s)
+    gpu_lib.start()
+    ref = gpu_lib.nve_0_vv(2)["strkin"]  # gb_vv stage 2: kinstress of the free atoms
+    d = gpu_lib.download()
+    dev = torch.device("cuda", 0)
+    vx, vy, vz = (torch.tensor(d[k], dtype=torch.float64, device=dev) for k in ("vx", "vy", "vz"))
+    w = torch.tensor(s.weight, dtype=torch.float64, device=dev)
+    fr = torch.tensor(s.lfrzn, dtype=torch.int32, device=dev)
+    out = torch.full((9,), float("nan"), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    expect_free = _kin_numpy(d, s.weight, s.lfrzn)
+    expect_all = _kin_numpy(d, s.weight)
+    # the frozen atoms carry velocity, so leaving them out changes the tensor
+    assert np.abs(expect_all - expect_free).max() > 1e-6 * np.abs(expect_all).max()
+    assert f(vx.data_ptr(), vy.data_ptr(), vz.data_ptr(), w.data_ptr(), fr.data_ptr(), s.natms, out.data_ptr(), sp) == 0
+    stream.synchronize()
+    got = out.cpu().numpy()
+    assert np.abs(got - ref).max() <= REL * np.abs(ref).max()
+    assert np.abs(got - expect_free).max() <= REL * np.abs(expect_free).max()
+    # lfrzn = NULL: every atom counts
+    out.fill_(float("nan"))
+    assert f(vx.data_ptr(), vy.data_ptr(), vz.data_ptr(), w.data_ptr(), None, s.natms, out.data_ptr(), sp) == 0
+    stream.synchronize()
+    got = out.cpu().numpy()
+    assert np.abs(got - expect_all).max() <= REL * np.abs(expect_all).max()
+    # n = 0: an all-zero tensor, the array pointers are not read
+    out.fill_(float("nan"))
+    assert f(vx.data_ptr(), vy.data_ptr(), vz.data_ptr(), w.data_ptr(), None, 0, out.data_ptr(), sp) == 0
+    stream.synchronize()
+    assert np.array_equal(out.cpu().numpy(), np.zeros(9))
+
+
 def test_kinstress_noalloc_rejects_too_many_atoms(gpu_lib):
     f = _bind(gpu_lib.lib)
     # nothing is launched for a size beyond the fixed scratch: pointers are never read
