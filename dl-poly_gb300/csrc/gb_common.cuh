@@ -37,7 +37,11 @@ struct DevScalars {
   int rattle_iters;
   int converged;    // constraint iteration flag
   int ncand_fp64;   // list-build candidates resolved in FP64
-  int pad[7];
+  int tile_over;    // cell tiles whose staged atoms exceed the first launch's capacity
+  int tile_max;     // most staged atoms of any cell tile
+  int halo_fwd;     // list entries with a halo image found in the forward half shell (evaluated)
+  int halo_bwd;     // list entries with a halo image found in the backward halo pass (skipped)
+  int pad[3];
   double maxdisp;   // largest displacement since the last rebuild
   unsigned long long npairs_list;  // half-list entries walked by the pair kernel
   unsigned long long npairs_rc;    // unique pairs inside the cutoff
@@ -56,6 +60,23 @@ enum {
   A_KINMOM = 64,      // 9 slots: kinetic stress (6), momentum (3) of the thermostat stages
   A_METAL = 80,       // 9 slots: engmet, virmet, stress (6), engden
   A_NSLOTS = 96
+};
+
+// Cell tiles of the list and pair kernels.  A tile is a run of m local link cells
+// along x at one (y, z); its CTA stages in shared memory every atom of the cells
+// that the forward half shell of its cells reaches, as one contiguous run of sorted
+// positions per row (dy, dz) of that shell.  A list entry then names its partner
+// by its slot in the tile's staged set (row base + position in the row).
+constexpr int TILE_MAX_ROWS = 32;
+constexpr int TILE_CAP_TARGET = 1600;  // staged atoms per tile of the first launches (2 pair CTAs per SM)
+constexpr int TILE_CAP_MAX = 3968;     // largest staged set a CTA can hold (57 B per atom in the pair kernel)
+constexpr unsigned short TILE_SKIP = 0xFFFFu;  // entry evaluated from the partner's side
+struct TilePlan {
+  int m;                    // local cells per tile along x
+  int ntx, nty, ntz, ntiles;
+  int nrows;                // rows (dy, dz) of the forward half shell
+  int r00;                  // the row (0, 0): it starts with the tile's own cells
+  int dy[TILE_MAX_ROWS], dz[TILE_MAX_ROWS], dxlo[TILE_MAX_ROWS], dxhi[TILE_MAX_ROWS];
 };
 
 // Kernel regions timed with CUDA events when profiling is on.
@@ -117,6 +138,22 @@ struct Dev {
   float4* erfc_df = nullptr;   // double-float erfc tables: 3 float4 per interval
   float4* vdw_df = nullptr;    // double-float vdW tables: per key (max_grid + 3) x 3 float4
   float2* qdf = nullptr;       // charges as double-floats (mxatms), written with the FP32 positions
+  // cell tiles (gb_list.cu plans and fills them at each list build)
+  TilePlan tp{};
+  int* tile_rows = nullptr;    // ntiles x nrows x (first sorted position, slot base)
+  int* tile_info = nullptr;    // ntiles x 4: staged atoms, first and end sorted position of the i atoms
+  int* tile_over = nullptr;    // ids of the tiles above the first launch's capacity
+  int tiles_alloc = 0;
+  unsigned short* tlist = nullptr;  // natms x ldt: per list entry the partner's tile slot (or TILE_SKIP)
+  int ldt = 0;
+  int tile_cap_list = 0, tile_cap_pair = 0;   // staged atoms per tile of the first launches
+  int n_tile_over = 0, tile_max_staged = 0;   // from the last list build
+  bool tiles_valid = false;    // the last list pairs every halo entry with its backward copy
+  bool use_tiles = true;       // cell-tile pair kernels (GB_PAIR_TILES=0: the per-atom kernels)
+  float4* xhs = nullptr;       // per sorted position: FP32 high parts (x, y, z, q)
+  float4* xls = nullptr;       // per sorted position: remainders (x, y, z, q) of the FP64 values
+  unsigned char* tys = nullptr;  // per sorted position: atom type
+  long long* fixs = nullptr;   // 3 x mxatms fixed-point pair forces per sorted position
   double metal_e4[4] = {0, 0, 0, 0};  // engmet, virmet, engden, virden of the last evaluation
   // thermostat of the VV stages (gb_thermostat.cu)
   int ens = 0;                 // GB_NVE, GB_NVT_BERENDSEN, GB_NVT_NOSE_HOOVER, GB_NVT_LANGEVIN
@@ -325,6 +362,7 @@ int list_refresh_halo();          // refresh halo positions (gb_list.cu)
 int list_build();                 // binning + pairs (gb_list.cu)
 void list_setup();                // link-cell geometry (gb_list.cu)
 void list_pos_f32();              // FP32 copy of positions and charges (mixed path)
+void list_pos_sorted();           // per sorted position: FP32 hi/lo positions, charge, type (cell tiles)
 void scan_exclusive(const int* in, int* out, int n);
 void pair_forces(double* eng6, double* stress9);  // gb_pair.cu (adds into forces)
 void pair_setup();                // gb_pair.cu: per-key constants

@@ -23,6 +23,7 @@ constexpr int MAX_SBC = 1024;  // semi-ball offsets capacity
 __constant__ int c_off[MAX_SBC];   // linear cell offset of each semi-ball cell
 __constant__ int c_nix[MAX_SBC], c_niy[MAX_SBC], c_niz[MAX_SBC];
 __constant__ unsigned char c_nir[MAX_SBC];
+__constant__ unsigned char c_row[MAX_SBC];  // cell-tile row (dy, dz) of each semi-ball cell
 
 struct HaloGeom {
   double rc[9];
@@ -420,19 +421,221 @@ __global__ void __launch_bounds__(256) k_list_pairs(int natms, const DevScalars*
   }
 }
 
+// Row tables of the cell tiles: per row (dy, dz) the first sorted position of its x run
+// of cells and its slot base in the tile's staged set; per tile the staged total and the
+// sorted-position range of its own (i) atoms.  Tiles above the capacity of the first
+// launches go to tile_over for a second launch with more shared memory.
+__global__ void k_tile_rows(TilePlan tp, CellGeom cg, const int* __restrict__ start, int* __restrict__ tile_rows,
+                            int* __restrict__ tile_info, int cap, int* __restrict__ tile_over, DevScalars* sc) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tp.ntiles) return;
+  const int tx = t % tp.ntx, ty = (t / tp.ntx) % tp.nty, tz = t / (tp.ntx * tp.nty);
+  const int nlp = cg.nlp;
+  const int x0 = nlp + tx * tp.m, x1 = min(x0 + tp.m, nlp + cg.nlx);  // own cells [x0, x1)
+  const int y = nlp + ty, z = nlp + tz;
+  int base = 0;
+  for (int r = 0; r < tp.nrows; ++r) {
+    const int plane = cg.NX * ((y + tp.dy[r]) + cg.NY * (z + tp.dz[r]));
+    const int clo = 1 + (x0 + tp.dxlo[r]) + plane, chi = 1 + (x1 - 1 + tp.dxhi[r]) + plane;
+    const int f = start[clo], e = start[chi + 1];
+    tile_rows[2 * (t * tp.nrows + r)] = f;
+    tile_rows[2 * (t * tp.nrows + r) + 1] = base;
+    base += e - f;
+  }
+  const int plane = cg.NX * (y + cg.NY * z);
+  tile_info[4 * t] = base;
+  tile_info[4 * t + 1] = start[1 + x0 + plane];
+  tile_info[4 * t + 2] = start[1 + (x1 - 1) + plane + 1];
+  tile_info[4 * t + 3] = 0;
+  if (base > cap) tile_over[atomicAdd(&sc->tile_over, 1)] = t;
+  atomicMax(&sc->tile_max, base);
+}
+
+// Half-shell Verlet list (neighbours.F90:876-1184), one CTA per cell tile: the tile's
+// forward half shell (FP32 positions and atom ids) is staged in shared memory and one
+// warp per local atom walks it in the reference order (semi-ball cell by cell, each
+// cell's members in ascending order), with ballot compaction.  Beside list(k, i) the
+// kernel writes tlist(k, i): the partner's slot in the tile's staged set, or TILE_SKIP
+// for the entries of the backward halo pass (pass 2), whose pairs the partner atom's
+// forward pass also lists, so each pair is evaluated once, from its forward side.
+__global__ void __launch_bounds__(256) k_list_tiles(int natms, CellGeom cg, TilePlan tp, int nsbcll,
+                                                    const int* __restrict__ tile_ids, int cap,
+                                                    const int* __restrict__ tile_rows, const int* __restrict__ tile_info,
+                                                    const int* __restrict__ at_list, const int* __restrict__ which_cell,
+                                                    const int* __restrict__ start, const double4_32a* __restrict__ xs,
+                                                    const float4* __restrict__ xsf, int* list, int ld,
+                                                    unsigned short* tlist, int ldt, int max_list, DevScalars* sc) {
+  extern __shared__ float4 s_x[];  // cap staged FP32 positions, then cap atom ids
+  int* s_at = reinterpret_cast<int*>(s_x + cap);
+  __shared__ int s_first[TILE_MAX_ROWS], s_base[TILE_MAX_ROWS + 1];
+  const int t = tile_ids ? tile_ids[blockIdx.x] : blockIdx.x;
+  const int nst = tile_info[4 * t];
+  if (nst > cap) return;  // the overflow launch builds this tile (uniform over the CTA)
+  const int nrows = tp.nrows;
+  if (threadIdx.x < nrows) {
+    s_first[threadIdx.x] = tile_rows[2 * (t * nrows + threadIdx.x)];
+    s_base[threadIdx.x] = tile_rows[2 * (t * nrows + threadIdx.x) + 1];
+  }
+  if (threadIdx.x == 0) s_base[nrows] = nst;
+  __syncthreads();
+  for (int r = 0; r < nrows; ++r) {
+    const int b = s_base[r], cnt = s_base[r + 1] - b, f = s_first[r];
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      s_x[b + e] = xsf[f + e];
+      s_at[b + e] = at_list[f + e];
+    }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const int ip0 = tile_info[4 * t + 1], ip1 = tile_info[4 * t + 2];
+  const int nlp = cg.nlp;
+  const int nlx0e = nlp - 1, nly0e = nlp - 1, nlz0e = nlp - 1;
+  const int nlx1s = cg.nlx + nlp, nly1s = cg.nly + nlp, nlz1s = cg.nlz + nlp;
+  int ncand64 = 0, nfwd = 0, nbwd = 0;
+  for (int p = ip0 + warp; p < ip1; p += nw) {
+    const int i0s = s_base[tp.r00] - s_first[tp.r00];
+    const int i = s_at[p + i0s];
+    const int ic = which_cell[i];
+    const int icm = ic - 1;
+    const int ix = icm % cg.NX;
+    const int iz = icm / (cg.NX * cg.NY);
+    const int iy = icm / cg.NX - cg.NY * iz;
+    const double4_32a xi = xs[p];
+    const float4 xif = s_x[p + i0s];
+    int* li = list + (size_t)i * ld + 3;  // li[k] == list(k, i)
+    unsigned short* ti = tlist + (size_t)i * ldt;
+    int count = 0;
+    // pass 1: the forward half shell, all of it staged
+    for (int kk = 0; kk < nsbcll; ++kk) {
+      const int jc = ic + c_off[kk];
+      const int r = c_row[kk];
+      const int sl0 = s_base[r] - s_first[r];  // slot = sorted position + sl0
+      const int s0 = (jc != ic) ? start[jc] : p + 1;
+      const int e = start[jc + 1];
+      const bool nir = c_nir[kk] != 0;
+      for (int b = s0; b < e; b += 32) {
+        const int jj = b + lane;
+        bool acc = false;
+        if (jj < e) {
+          if (nir) {
+            acc = true;
+          } else {
+            const float4 xj = s_x[jj + sl0];
+            const float dx = xj.x - xif.x, dy = xj.y - xif.y, dz = xj.z - xif.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 < cg.rcsq_lo) {
+              acc = true;
+            } else if (r2 <= cg.rcsq_hi) {
+              const double4_32a xd = xs[jj];
+              const double ddx = sub_rn(xd.x, xi.x), ddy = sub_rn(xd.y, xi.y), ddz = sub_rn(xd.z, xi.z);
+              const double rsq = add_rn(add_rn(mul_rn(ddx, ddx), mul_rn(ddy, ddy)), mul_rn(ddz, ddz));
+              acc = rsq <= cg.rcsq;
+              ++ncand64;
+            }
+          }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, acc);
+        if (acc) {
+          const int k = count + __popc(m & lt) + 1;
+          const int a = s_at[jj + sl0];
+          nfwd += a >= natms;
+          if (k <= max_list) {
+            li[k] = a + 1;
+            ti[k] = (unsigned short)(jj + sl0);
+          }
+        }
+        count += __popc(m);
+      }
+    }
+    // pass 2: backward cells that are halo cells (border atoms only), from global memory
+    const int ix1 = ix - nlx0e, ix2 = ix - nlx1s, iy1 = iy - nly0e, iy2 = iy - nly1s, iz1 = iz - nlz0e,
+              iz2 = iz - nlz1s;
+    const bool border = (ix1 >= 1 && ix1 <= nlp) || (ix2 <= -1 && ix2 >= -nlp) || (iy1 >= 1 && iy1 <= nlp) ||
+                        (iy2 <= -1 && iy2 >= -nlp) || (iz1 >= 1 && iz1 <= nlp) || (iz2 <= -1 && iz2 >= -nlp);
+    if (border) {
+      for (int kk = 1; kk < nsbcll; ++kk) {
+        const int jx = ix - c_nix[kk], jy = iy - c_niy[kk], jz = iz - c_niz[kk];
+        if (!(jx <= nlx0e || jx >= nlx1s || jy <= nly0e || jy >= nly1s || jz <= nlz0e || jz >= nlz1s)) continue;
+        const int jc = ic - c_off[kk];
+        const int s0 = start[jc], e = start[jc + 1];
+        const bool nir = c_nir[kk] != 0;
+        for (int b = s0; b < e; b += 32) {
+          const int jj = b + lane;
+          bool acc = false;
+          if (jj < e) {
+            if (nir) {
+              acc = true;
+            } else {
+              const float4 xj = xsf[jj];
+              const float dx = xj.x - xif.x, dy = xj.y - xif.y, dz = xj.z - xif.z;
+              const float r2 = dx * dx + dy * dy + dz * dz;
+              if (r2 < cg.rcsq_lo) {
+                acc = true;
+              } else if (r2 <= cg.rcsq_hi) {
+                const double4_32a xd = xs[jj];
+                const double ddx = sub_rn(xd.x, xi.x), ddy = sub_rn(xd.y, xi.y), ddz = sub_rn(xd.z, xi.z);
+                const double rsq = add_rn(add_rn(mul_rn(ddx, ddx), mul_rn(ddy, ddy)), mul_rn(ddz, ddz));
+                acc = rsq <= cg.rcsq;
+                ++ncand64;
+              }
+            }
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, acc);
+          if (acc) {
+            const int k = count + __popc(m & lt) + 1;
+            ++nbwd;
+            if (k <= max_list) {
+              li[k] = at_list[jj] + 1;
+              ti[k] = TILE_SKIP;
+            }
+          }
+          count += __popc(m);
+        }
+      }
+    }
+    if (lane == 0) {
+      // the stored length never exceeds max_list, so no later kernel can read
+      // past the column even when the overflow status is ignored
+      const int stored = min(count, max_list);
+      li[0] = stored;
+      li[-1] = stored;
+      li[-2] = stored;
+      li[-3] = stored;
+      if (count > max_list) {
+        atomicOr(&sc->status, ST_LIST_OVERFLOW);
+        atomicMax(&sc->ibig, count);
+      }
+    }
+  }
+  ncand64 = warp_sumi(ncand64);
+  nfwd = warp_sumi(nfwd);
+  nbwd = warp_sumi(nbwd);
+  if (lane == 0) {
+    if (ncand64) atomicAdd(&sc->ncand_fp64, ncand64);
+    if (nfwd) atomicAdd(&sc->halo_fwd, nfwd);
+    if (nbwd) atomicAdd(&sc->halo_bwd, nbwd);
+  }
+}
+
 // Frozen (neighbours.F90:1198-1225) and excluded (:1229-1306) reordering, one
 // thread per atom, sequential exactly as the reference swaps.
-__global__ void k_list_reorder(int natms, int* list, int ld, const int* lfrzn, const int* ltg,
-                               const int* list_excl, int ldx, int megfrz, int lbook) {
+// The tile slots in tlist follow their list entries through every swap.
+__global__ void k_list_reorder(int natms, int* list, int ld, unsigned short* tlist, int ldt, const int* lfrzn,
+                               const int* ltg, const int* list_excl, int ldx, int megfrz, int lbook) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natms) return;
   int* li = list + (size_t)i * ld + 3;
+  unsigned short* ti = tlist + (size_t)i * ldt;
   int l_end = li[0], m_end = l_end;
   if (megfrz > 1 && lfrzn[i] > 0) {
     for (int kk = l_end; kk >= 1; --kk) {
       int j = li[kk];
       if (lfrzn[j - 1] > 0) {
-        if (kk < m_end) { li[kk] = li[m_end]; li[m_end] = j; }
+        if (kk < m_end) {
+          li[kk] = li[m_end]; li[m_end] = j;
+          const unsigned short tk = ti[kk]; ti[kk] = ti[m_end]; ti[m_end] = tk;
+        }
         --m_end;
       }
     }
@@ -451,7 +654,10 @@ __global__ void k_list_reorder(int natms, int* list, int ld, const int* lfrzn, c
         bool hit = false;
         for (int t = 1; t <= ii; ++t) hit |= (ex[t] == jj);
         if (hit) {
-          if (kk < m_end) { li[kk] = li[m_end]; li[m_end] = j; }
+          if (kk < m_end) {
+            li[kk] = li[m_end]; li[m_end] = j;
+            const unsigned short tk = ti[kk]; ti[kk] = ti[m_end]; ti[m_end] = tk;
+          }
           --m_end;
         }
       }
@@ -484,6 +690,22 @@ __global__ void k_pos_f32(const DevScalars* sc, const double* x, const double* y
     const float qh = (float)q[i];
     qdf[i] = make_float2(qh, (float)(q[i] - (double)qh));
   }
+}
+
+// Per sorted position (cell order): FP32 high parts (x, y, z, q), the remainders of
+// the FP64 values and the atom type, read by the cell-tile pair kernels.
+__global__ void k_pos_sorted(const DevScalars* sc, const int* __restrict__ at_list, const double* __restrict__ x,
+                             const double* __restrict__ y, const double* __restrict__ z, const double* __restrict__ q,
+                             const int* __restrict__ ltype, float4* xhs, float4* xls, unsigned char* tys) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= sc->nlast) return;
+  const int a = at_list[p];
+  const double xa = x[a], ya = y[a], za = z[a], qa = q[a];
+  const float hx = (float)xa, hy = (float)ya, hz = (float)za, hq = (float)qa;
+  xhs[p] = make_float4(hx, hy, hz, hq);
+  xls[p] = make_float4((float)(xa - (double)hx), (float)(ya - (double)hy), (float)(za - (double)hz),
+                       (float)(qa - (double)hq));
+  tys[p] = (unsigned char)ltype[a];
 }
 
 inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
@@ -559,6 +781,58 @@ void list_setup() {
   }
   g.nsbcll = (int)off.size();
   if (g.nsbcll > MAX_SBC) throw (int)GB_ERR_ARG;
+  // cell tiles: the rows (dy, dz) of the forward half shell in the order they first
+  // appear, each with the range of dx its cells take
+  {
+    TilePlan& tp = g.tp;
+    tp = TilePlan{};
+    std::vector<unsigned char> row(off.size());
+    for (size_t k = 0; k < off.size(); ++k) {
+      int r = 0;
+      while (r < tp.nrows && !(tp.dy[r] == niy[k] && tp.dz[r] == niz[k])) ++r;
+      if (r == tp.nrows) {
+        if (tp.nrows == TILE_MAX_ROWS) throw (int)GB_ERR_ARG;
+        tp.dy[r] = niy[k]; tp.dz[r] = niz[k]; tp.dxlo[r] = nix[k]; tp.dxhi[r] = nix[k];
+        ++tp.nrows;
+      }
+      tp.dxlo[r] = std::min(tp.dxlo[r], nix[k]);
+      tp.dxhi[r] = std::max(tp.dxhi[r], nix[k]);
+      row[k] = (unsigned char)r;
+    }
+    tp.r00 = row[0];  // offset (0, 0, 0) comes first; its row starts at dx = 0
+    if (nix[0] != 0 || niy[0] != 0 || niz[0] != 0 || tp.dxlo[tp.r00] != 0) throw (int)GB_ERR_ARG;
+    GB_CUDA(cudaMemcpyToSymbol(c_row, row.data(), row.size()));
+    // tile width: the widest run of cells whose staged set stays near the capacity the
+    // pair kernel's shared memory allows at two CTAs per SM
+    const double apc = (double)g.natms / ((double)nlx * nly * nlz);
+    auto cells_of = [&](int m) {
+      int c = 0;
+      for (int r = 0; r < tp.nrows; ++r) c += m + tp.dxhi[r] - tp.dxlo[r];
+      return c;
+    };
+    int m = 1;
+    const char* em = getenv("GB_TILE_M");
+    if (em && atoi(em) > 0) {
+      m = std::min(atoi(em), nlx);
+    } else {
+      for (int t = 2; t <= std::min(nlx, 8); ++t)
+        if (1.3 * cells_of(t) * apc + 64.0 <= (double)TILE_CAP_TARGET) m = t;
+    }
+    tp.m = m;
+    tp.ntx = (nlx + m - 1) / m; tp.nty = nly; tp.ntz = nlz;
+    tp.ntiles = tp.ntx * tp.nty * tp.ntz;
+    int cap = (int)(1.3 * cells_of(m) * apc) + 64;
+    const char* ec = getenv("GB_TILE_CAP");  // a smaller first-launch capacity sends more tiles to the second launch
+    if (ec && atoi(ec) > 0) cap = atoi(ec);
+    g.tile_cap_list = g.tile_cap_pair = std::min(((cap + 31) / 32) * 32, (int)TILE_CAP_MAX);
+    if (g.tiles_alloc < tp.ntiles) {
+      cudaFree(g.tile_rows); cudaFree(g.tile_info); cudaFree(g.tile_over);
+      GB_CUDA(cudaMalloc(&g.tile_rows, sizeof(int) * 2 * (size_t)tp.ntiles * TILE_MAX_ROWS));
+      GB_CUDA(cudaMalloc(&g.tile_info, sizeof(int) * 4 * (size_t)tp.ntiles));
+      GB_CUDA(cudaMalloc(&g.tile_over, sizeof(int) * (size_t)tp.ntiles));
+      g.tiles_alloc = tp.ntiles;
+    }
+  }
   GB_CUDA(cudaMemcpyToSymbol(c_off, off.data(), sizeof(int) * off.size()));
   GB_CUDA(cudaMemcpyToSymbol(c_nix, nix.data(), sizeof(int) * nix.size()));
   GB_CUDA(cudaMemcpyToSymbol(c_niy, niy.data(), sizeof(int) * niy.size()));
@@ -664,21 +938,57 @@ int list_build() {
   GB_LAUNCHED();
   prof_end(P_BIN);
   GB_CUDA(cudaMemsetAsync(&g.sc->ibig, 0, sizeof(int), st));
+  GB_CUDA(cudaMemsetAsync(&g.sc->tile_over, 0, 4 * sizeof(int), st));  // tile_over, tile_max, halo_fwd, halo_bwd
   prof_begin(P_LIST);
-  k_list_pairs<<<nblocks((long long)mx * 32, T), T, 0, st>>>(g.natms, g.sc, h_cg, g.nsbcll, g.at_list, g.which_cell,
-                                                             g.cell_start, g.xs, g.xsf, g.list, g.ld, g.p.max_list,
-                                                             g.sc);
+  const TilePlan& tp = g.tp;
+  const int cap = g.tile_cap_list;
+  k_tile_rows<<<nblocks(tp.ntiles, 128), 128, 0, st>>>(tp, h_cg, g.cell_start, g.tile_rows, g.tile_info, cap,
+                                                        g.tile_over, g.sc);
   GB_LAUNCHED();
+  GB_CUDA(cudaFuncSetAttribute(k_list_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, 20 * TILE_CAP_MAX));
+  k_list_tiles<<<tp.ntiles, 256, (size_t)cap * 20, st>>>(g.natms, h_cg, tp, g.nsbcll, nullptr, cap, g.tile_rows,
+                                                          g.tile_info, g.at_list, g.which_cell, g.cell_start, g.xs,
+                                                          g.xsf, g.list, g.ld, g.tlist, g.ldt, g.p.max_list, g.sc);
+  GB_LAUNCHED();
+  gb_sync_scalars();
+  g.n_tile_over = g.hsc->tile_over;
+  g.tile_max_staged = g.hsc->tile_max;
+  bool tiled = true;
+  if (g.n_tile_over > 0 && g.tile_max_staged <= TILE_CAP_MAX) {
+    // the tiles above the capacity, with shared memory for the largest of them
+    k_list_tiles<<<g.n_tile_over, 256, (size_t)g.tile_max_staged * 20, st>>>(
+        g.natms, h_cg, tp, g.nsbcll, g.tile_over, g.tile_max_staged, g.tile_rows, g.tile_info, g.at_list,
+        g.which_cell, g.cell_start, g.xs, g.xsf, g.list, g.ld, g.tlist, g.ldt, g.p.max_list, g.sc);
+    GB_LAUNCHED();
+  } else if (g.n_tile_over > 0) {
+    // a tile too dense for one CTA's shared memory: the whole list from the per-atom
+    // kernel, and the pair kernels that walk it without tiles
+    tiled = false;
+    k_list_pairs<<<nblocks((long long)mx * 32, T), T, 0, st>>>(g.natms, g.sc, h_cg, g.nsbcll, g.at_list,
+                                                               g.which_cell, g.cell_start, g.xs, g.xsf, g.list, g.ld,
+                                                               g.p.max_list, g.sc);
+    GB_LAUNCHED();
+  }
   if (g.lbook || g.megfrz > 1) {
-    k_list_reorder<<<nblocks(g.natms, 128), 128, 0, st>>>(g.natms, g.list, g.ld, g.lfrzn, g.ltg, g.list_excl,
-                                                          g.p.max_exclude + 1, g.megfrz, g.lbook ? 1 : 0);
+    k_list_reorder<<<nblocks(g.natms, 128), 128, 0, st>>>(g.natms, g.list, g.ld, g.tlist, g.ldt, g.lfrzn, g.ltg,
+                                                          g.list_excl, g.p.max_exclude + 1, g.megfrz,
+                                                          g.lbook ? 1 : 0);
     GB_LAUNCHED();
   }
   prof_end(P_LIST);
   gb_sync_scalars();
   if (g.hsc->status & ST_LIST_OVERFLOW) return GB_ERR_LIST_OVERFLOW;
+  // every pair across the periodic boundary is listed from both of its atoms, once in a
+  // forward pass and once in the backward halo pass; the tile kernels evaluate the forward copy
+  g.tiles_valid = tiled && g.hsc->halo_fwd == g.hsc->halo_bwd;
   ++g.list_gen;  // the learned-MTS short list is rebuilt from this list on demand
   return GB_OK;
+}
+
+void list_pos_sorted() {
+  k_pos_sorted<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(g.sc, g.at_list, g.x, g.y, g.z, g.chge, g.ltype, g.xhs,
+                                                            g.xls, g.tys);
+  GB_LAUNCHED();
 }
 
 void list_pos_f32() {

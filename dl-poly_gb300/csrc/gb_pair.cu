@@ -717,6 +717,360 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 4) k_pair_df64(int natms, const De
   block_reduce_store<NACC_DF>(out, blk);
 }
 
+// ------------------------------------------------------------ cell-tile kernels
+// One CTA per cell tile (a run of link cells along x): the positions, charges and types
+// of every atom the tile's forward half shell reaches are staged in shared memory, in
+// one contiguous run of sorted positions per shell row, together with int64 fixed-point
+// force accumulators.  Warps take the tile's own atoms one at a time and walk each
+// atom's Verlet list through its tile slots (tlist): the partner's data come from
+// shared memory, its reaction goes to its shared accumulator with an integer atomic,
+// and at the end the CTA adds its accumulators to the per-sorted-position forces.
+// Pairs with a halo image are evaluated by the entry of the forward pass (the partner
+// atom's backward-pass copy is marked TILE_SKIP).  Integer sums make the forces
+// independent of the order of warps, tiles and atomics.
+constexpr int PAIR_TILE_NT = 256;
+constexpr int PAIR_TILE_BYTES = 57;  // shared bytes per staged atom: hi + lo float4, 3 x int64, type
+
+struct PairTileArgs {
+  int natms;
+  const int* tile_ids;  // nullptr: tile = blockIdx.x
+  int cap, nrows, r00, blk_off;
+  const int* tile_rows;
+  const int* tile_info;
+  const int* at_list;
+  const int* list;
+  int ld;
+  const unsigned short* tlist;
+  int ldt;
+  const float4* xhs;
+  const float4* xls;
+  const unsigned char* tys;
+  const double *x, *y, *z, *q;  // FP64 by atom index: the exact pair evaluation near a cutoff
+  const float4* etab;
+  const float4* vtab;
+  const double* ecoef;
+  const double* vcoef;
+  const int* vkind;
+  const double* veps;
+  const double* vsig;
+  int ntypes;
+  float rc2, rv2, alpha, a2rp, scaling;  // mixed form
+  unsigned long long* fixs;
+  double* blk;
+  unsigned long long* cnt;
+};
+
+// atom index of a tile slot (rows are contiguous runs of sorted positions)
+__device__ __forceinline__ int tile_slot_atom(int slot, int nrows, const int* s_first, const int* s_base,
+                                              const int* __restrict__ at_list) {
+  int r = 0;
+  while (r + 1 < nrows && s_base[r + 1] <= slot) ++r;
+  return at_list[s_first[r] + (slot - s_base[r])];
+}
+
+// The FP64 form's terms of one pair from tile data (the arithmetic of pair_terms_df64);
+// returns false when the pair exerts no force.
+__device__ __forceinline__ bool pair_df64_tile(const PairGeom& pg, const PairTileArgs& A, int i, int slot, int ai,
+                                               int aj, df qi, bool qi_on, float qjh, float qjl, df dx, df dy, df dz,
+                                               df rsq, int nrows, const int* s_first, const int* s_base,
+                                               dacc (&acc)[NACC_DF], long long& ix, long long& iy, long long& iz) {
+  const bool band = (rsq.hi >= pg.f_rc2_lo && rsq.hi <= pg.f_rc2_hi) ||
+                    (rsq.hi >= pg.f_rv2_lo && rsq.hi <= pg.f_rv2_hi);
+  const bool in_c = qi_on && qjh != 0.0f && rsq.hi < pg.f_rc2_lo;
+  int key = -1;
+  if (rsq.hi < pg.f_rv2_lo) {
+    key = vkey(ai, aj) - 1;
+    if (A.vkind[key] == 0) key = -1;
+  }
+  df gam = df_make(0.f, 0.f), ee = gam, ev = gam, gvc = gam, gvv = gam;
+  bool slow = band;
+  if (!slow && (in_c || key >= 0)) {
+    const df rinv = df_rsqrt(rsq);
+    const df rrr = df_mul(rsq, rinv);
+    df d;
+    const int k = table_coord(rrr, pg.erdr_hi, pg.erdr_lo, &d);
+    int kv = k;
+    df dv = d;
+    if (!pg.same_grid && key >= 0) kv = table_coord(rrr, pg.vrdr_hi, pg.vrdr_lo, &dv);
+    if (k == 0 || (key >= 0 && kv == 0)) {
+      slow = true;  // first interval: the exact three-point formula, in FP64
+    } else {
+      if (in_c) {
+        const float4* c = A.etab + (size_t)k * 3;
+        const float4 e01 = c[0], d01 = c[1], c2 = c[2];
+        const df pre = df_mul(qi, df_make(qjh, qjl));
+        gvc = df_mul(pre, poly_df(d01, c2.z, c2.w, d));
+        ee = df_mul(pre, poly_df(e01, c2.x, c2.y, d));
+        gam = gvc;
+      }
+      if (key >= 0) {
+        const df r_rsq = df_sqr(rinv);
+        if (pg.vdw_direct) {
+          slow = true;
+        } else {
+          const float4* c = A.vtab + (size_t)key * ((pg.max_grid + 3) * 3) + (size_t)kv * 3;
+          const float4 f01 = c[0], v01 = c[1], c2 = c[2];
+          gvv = df_mul(poly_df(f01, c2.x, c2.y, dv), r_rsq);
+          ev = poly_df(v01, c2.z, c2.w, dv);
+          gam = df_add(gam, gvv);
+        }
+      }
+    }
+  }
+  if (slow) {
+    const int j = tile_slot_atom(slot, nrows, s_first, s_base, A.at_list);
+    double g64, e64c, e64v, gc64, gv64;
+    bool any;
+    pair_terms_fp64(pg, A.x[i] - A.x[j], A.y[i] - A.y[j], A.z[i] - A.z[j], A.q[i] * pg.scaling, A.q[j], ai, aj,
+                    A.ecoef, A.vcoef, A.vkind, A.veps, A.vsig, &g64, &e64c, &e64v, &gc64, &gv64, &any);
+    if (!any) return false;
+    float h, l;
+    df_split(g64, &h, &l); gam = df_make(h, l);
+    df_split(e64c, &h, &l); ee = df_make(h, l);
+    df_split(e64v, &h, &l); ev = df_make(h, l);
+    df_split(gc64, &h, &l); gvc = df_make(h, l);
+    df_split(gv64, &h, &l); gvv = df_make(h, l);
+  } else if (!in_c && key < 0) {
+    return false;
+  }
+  ix = fix40_df(df_mul(gam, dx));
+  iy = fix40_df(df_mul(gam, dy));
+  iz = fix40_df(df_mul(gam, dz));
+  dacc_add(acc[0], ev);
+  dacc_add_prod(acc[1], df_neg(gvv), rsq);
+  dacc_add(acc[2], ee);
+  dacc_add_prod(acc[3], df_neg(gvc), rsq);
+  return true;
+}
+
+// The mixed form's terms of one pair (FP32, analytic erfc and 12-6 LJ, as k_pair_mixed_half)
+__device__ __forceinline__ bool pair_mixed_tile(const PairTileArgs& A, const float4* s_lj, int row, int aj, float qi,
+                                                float qj, float dx, float dy, float dz, dacc (&acc)[NACC_DF],
+                                                long long& ix, long long& iy, long long& iz) {
+  const float rsq = dx * dx + dy * dy + dz * dz;
+  if (rsq >= A.rc2 && rsq >= A.rv2) return false;
+  const float rinv = rsqrtf(rsq);
+  const float rrr = rsq * rinv;
+  const float r2i = rinv * rinv;
+  float gam = 0.f;
+  bool any = false;
+  if (rsq < A.rc2 && qj != 0.f) {
+    const float x = A.alpha * rrr;
+    const float ex = __expf(-x * x);
+    const float tt = __frcp_rn(fmaf(AS_P, x, 1.0f));
+    const float poly = tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, AS_A5, AS_A4), AS_A3), AS_A2), AS_A1);
+    const float pre = qi * qj;
+    const float ec = pre * poly * ex * rinv;
+    const float eg = fmaf(pre * A.a2rp, ex, ec) * r2i;
+    gam += eg;
+    dacc_add(acc[2], df_make(ec, 0.f));
+    dacc_add(acc[3], df_make(-eg * rsq, 0.f));
+    any = true;
+  }
+  if (rsq < A.rv2) {
+    const float4 lj6 = s_lj[row + aj];
+    if (lj6.w != 0.f) {
+      const float s2 = lj6.z * r2i;
+      const float s6 = s2 * s2 * s2;
+      const float gv = lj6.y * s6 * fmaf(2.0f, s6, -1.0f) * r2i;
+      gam += gv;
+      dacc_add(acc[0], df_make(lj6.x * s6 * (s6 - 1.0f), 0.f));
+      dacc_add(acc[1], df_make(-gv * rsq, 0.f));
+      any = true;
+    }
+  }
+  if (!any) return false;
+  ix = fix40(gam * dx);
+  iy = fix40(gam * dy);
+  iz = fix40(gam * dz);
+  return true;
+}
+
+template <int MIXED>
+__global__ void __launch_bounds__(PAIR_TILE_NT) k_pair_tile(PairTileArgs A, PairGeom pg) {
+  extern __shared__ float4 sm_tile[];
+  const int cap = A.cap;
+  float4* s_hi = sm_tile;
+  float4* s_lo = sm_tile + cap;
+  unsigned long long* s_f = reinterpret_cast<unsigned long long*>(sm_tile + 2 * cap);
+  unsigned char* s_ty = reinterpret_cast<unsigned char*>(s_f + 3 * cap);
+  __shared__ int s_first[TILE_MAX_ROWS], s_base[TILE_MAX_ROWS + 1];
+  __shared__ int s_next;
+  __shared__ PairQueue pq[PAIR_TILE_NT / 32];
+  __shared__ float4 s_lj[MIXED ? MAX_TYPES * MAX_TYPES : 1];
+  const int t = A.tile_ids ? A.tile_ids[blockIdx.x] : blockIdx.x;
+  const int nst = A.tile_info[4 * t];
+  double* blk = A.blk + (size_t)A.blk_off * NACC_DF;
+  if (nst > cap) {  // the overflow launch evaluates this tile; its accumulator slots stay zero
+    if (threadIdx.x < NACC_DF) blk[(size_t)blockIdx.x * NACC_DF + threadIdx.x] = 0.0;
+    return;
+  }
+  const int nrows = A.nrows;
+  if (threadIdx.x < nrows) {
+    s_first[threadIdx.x] = A.tile_rows[2 * (t * nrows + threadIdx.x)];
+    s_base[threadIdx.x] = A.tile_rows[2 * (t * nrows + threadIdx.x) + 1];
+  }
+  if (threadIdx.x == 0) {
+    s_base[nrows] = nst;
+    s_next = 0;
+  }
+  if (MIXED) {
+    for (int e = threadIdx.x; e < A.ntypes * A.ntypes; e += blockDim.x) {
+      const int ai = e / A.ntypes + 1, aj = e % A.ntypes + 1;
+      s_lj[e] = c_lj[vkey(ai, aj) - 1];
+    }
+  }
+  __syncthreads();
+  for (int r = 0; r < nrows; ++r) {
+    const int b = s_base[r], cnt = s_base[r + 1] - b, f = s_first[r];
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      s_hi[b + e] = A.xhs[f + e];
+      s_lo[b + e] = A.xls[f + e];
+      s_ty[b + e] = A.tys[f + e];
+    }
+  }
+  for (int e = threadIdx.x; e < 3 * nst; e += blockDim.x) s_f[e] = 0ull;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const int ip0 = A.tile_info[4 * t + 1], ip1 = A.tile_info[4 * t + 2];
+  const int i0s = s_base[A.r00] - s_first[A.r00];
+  dacc acc[NACC_DF];
+#pragma unroll
+  for (int k = 0; k < NACC_DF; ++k) { acc[k].s = 0.f; acc[k].c = 0.f; }
+  unsigned long long n_list = 0, n_rc = 0;
+  for (;;) {
+    int k = 0;
+    if (lane == 0) k = atomicAdd(&s_next, 1);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    const int p = ip0 + k;
+    if (p >= ip1) break;
+    const int islot = p + i0s;
+    const int i = A.at_list[p];
+    const float4 pi = s_hi[islot], li = s_lo[islot];
+    const int ai = s_ty[islot];
+    const df qi = df_mul(df_make(pi.w, li.w), df_make(pg.scal_hi, pg.scal_lo));  // q_i r4pie0/eps
+    const bool qi_on = pi.w != 0.0f;
+    const float qi32 = pi.w * A.scaling;
+    const int ljrow = (ai - 1) * A.ntypes - 1;
+    const int n = A.list[(size_t)i * A.ld + 3];
+    const unsigned short* tl = A.tlist + (size_t)i * A.ldt;
+    long long sx = 0, sy = 0, sz = 0;
+    // pass 1, 32 entries at a time: an FP32 r^2 of the high parts against the outer
+    // cutoff plus a bound on their rounding queues the candidates (ballot compaction);
+    // pass 2 evaluates 32 queued pairs at a time with every lane busy
+    int nq = 0;
+    for (int base = 0;; base += 32) {
+      const bool more = base < n;
+      if (more) {
+        const int m = base + lane + 1;
+        bool keep = false;
+        int slot = 0;
+        if (m <= n) {
+          slot = tl[m];
+          if (slot != TILE_SKIP) {
+            const float4 pj = s_hi[slot];
+            const float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
+            keep = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= pg.f_pre;
+          }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) pq[wq].j[nq + __popc(bal & ((1u << lane) - 1u))] = slot;
+        nq += __popc(bal);
+        __syncwarp();
+      }
+      if (nq >= 32 || (!more && nq > 0)) {
+        const int take = min(nq, 32);
+        if (lane < take) {
+          const int slot = pq[wq].j[nq - take + lane];
+          const float4 pj = s_hi[slot], lj = s_lo[slot];
+          const int aj = s_ty[slot];
+          long long ix = 0, iy = 0, iz = 0;
+          bool hit;
+          if (MIXED) {
+            const float dx = (pi.x - pj.x) + (li.x - lj.x), dy = (pi.y - pj.y) + (li.y - lj.y),
+                        dz = (pi.z - pj.z) + (li.z - lj.z);
+            hit = pair_mixed_tile(A, s_lj, ljrow, aj, qi32, pj.w, dx, dy, dz, acc, ix, iy, iz);
+          } else {
+            const df ex = two_sum(pi.x, -pj.x), ey = two_sum(pi.y, -pj.y), ez = two_sum(pi.z, -pj.z);
+            const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
+            const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
+            const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
+            const df rsq = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+            hit = rsq.hi <= pg.f_hi && pair_df64_tile(pg, A, i, slot, ai, aj, qi, qi_on, pj.w, lj.w, dx, dy, dz,
+                                                      rsq, nrows, s_first, s_base, acc, ix, iy, iz);
+          }
+          if (hit) {
+            ++n_rc;
+            sx += ix; sy += iy; sz += iz;
+            atomicAdd(&s_f[3 * slot + 0], (unsigned long long)(-ix));
+            atomicAdd(&s_f[3 * slot + 1], (unsigned long long)(-iy));
+            atomicAdd(&s_f[3 * slot + 2], (unsigned long long)(-iz));
+          }
+        }
+        nq -= take;
+        __syncwarp();  // the taken slots are read before the next pass appends over them
+      }
+      if (!more && nq == 0) break;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, o);
+      sy += __shfl_xor_sync(0xffffffffu, sy, o);
+      sz += __shfl_xor_sync(0xffffffffu, sz, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&s_f[3 * islot + 0], (unsigned long long)sx);
+      atomicAdd(&s_f[3 * islot + 1], (unsigned long long)sy);
+      atomicAdd(&s_f[3 * islot + 2], (unsigned long long)sz);
+      n_list += (unsigned long long)n;
+    }
+  }
+  __syncthreads();
+  // the tile's accumulators into the per-sorted-position forces (coalesced within each row)
+  for (int r = 0; r < nrows; ++r) {
+    const int b = s_base[r], cnt = s_base[r + 1] - b, f = s_first[r];
+    for (int e = threadIdx.x; e < 3 * cnt; e += blockDim.x) {
+      const unsigned long long v = s_f[3 * b + e];
+      if (v) atomicAdd(&A.fixs[3 * (size_t)f + e], v);
+    }
+  }
+  dfr out[NACC_DF];
+#pragma unroll
+  for (int k = 0; k < NACC_DF; ++k) out[k] = to_dfr(two_sum(acc[k].s, acc[k].c));
+  n_rc = (unsigned long long)warp_sumi((int)n_rc);
+  if (lane == 0) {
+    if (n_list) atomicAdd(&A.cnt[0], n_list);
+    if (n_rc) atomicAdd(&A.cnt[1], n_rc);
+  }
+  block_reduce_store<NACC_DF>(out, blk);
+}
+
+// Pair stress from the per-sorted-position forces (sum over slots of x (x) F, every halo
+// image at its own position, in FP64 from the exact fixed-point forces), then each
+// slot's force onto its atom (a halo image's onto its source): integer sums.
+__global__ void k_slot_stress_fold(int natms, const DevScalars* sc, const int* __restrict__ at_list,
+                                   const int* __restrict__ src, const double* __restrict__ x,
+                                   const double* __restrict__ y, const double* __restrict__ z,
+                                   const long long* __restrict__ fixs, unsigned long long* fixp, double* blk) {
+  const int nlast = sc->nlast;
+  const double s = 1.0 / 1099511627776.0;
+  double st[6] = {0, 0, 0, 0, 0, 0};
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nlast; p += gridDim.x * blockDim.x) {
+    const long long f0 = fixs[3 * (size_t)p], f1 = fixs[3 * (size_t)p + 1], f2 = fixs[3 * (size_t)p + 2];
+    if ((f0 | f1 | f2) == 0) continue;
+    const int a = at_list[p];
+    const double fa = (double)f0 * s, fb = (double)f1 * s, fc = (double)f2 * s;
+    const double xa = x[a], ya = y[a], za = z[a];
+    st[0] = fma(xa, fa, st[0]); st[1] = fma(xa, fb, st[1]); st[2] = fma(xa, fc, st[2]);
+    st[3] = fma(ya, fb, st[3]); st[4] = fma(ya, fc, st[4]); st[5] = fma(za, fc, st[5]);
+    const int tgt = a < natms ? a : src[a];
+    atomicAdd(&fixp[3 * tgt + 0], (unsigned long long)f0);
+    atomicAdd(&fixp[3 * tgt + 1], (unsigned long long)f1);
+    atomicAdd(&fixp[3 * tgt + 2], (unsigned long long)f2);
+  }
+  block_reduce_store<6>(st, blk);
+}
+
 // Pair stress of the double-float kernel from its per-slot forces: with every image's
 // force kept in the image's own slot, sum over pairs of d (x) f = sum over slots of
 // x (x) F (each pair's f enters its two slots with opposite signs, and d is the
@@ -761,6 +1115,106 @@ __global__ void k_fix_add_fp64(int n, const long long* fixp, double* fx, double*
   fz[i] += (double)fixp[3 * i + 2] * s;
 }
 
+namespace {
+
+// double-float cutoff bands, the FP32 prefilter bound and the split spacings
+void pair_geom_df(PairGeom& pg) {
+  pg.f_rc2_lo = (float)(pg.rc2 * (1.0 - 1e-6));
+  pg.f_rc2_hi = (float)(pg.rc2 * (1.0 + 1e-6));
+  pg.f_rv2_lo = (float)(pg.rv2 * (1.0 - 1e-6));
+  pg.f_rv2_hi = (float)(pg.rv2 * (1.0 + 1e-6));
+  pg.f_hi = std::max(pg.f_rc2_hi, pg.f_rv2_hi);
+  // |x - (float)x| <= u for every coordinate: R = twice the summed cell-vector lengths
+  // bounds the local atoms (reduced coordinates within +-(1/2 + drift)) and their halo
+  // images (the halo is under half a cell wide)
+  double R = 0.0;
+  for (int v = 0; v < 3; ++v)
+    R += std::sqrt(g.cell[3 * v] * g.cell[3 * v] + g.cell[3 * v + 1] * g.cell[3 * v + 1] +
+                   g.cell[3 * v + 2] * g.cell[3 * v + 2]);
+  R *= 2.0;
+  const double u = std::ldexp(1.0, std::ilogb(R) - 23);
+  const double eps = std::ldexp(1.0, -23);
+  const double D = std::sqrt((double)pg.f_hi) + 1.0;
+  const double dlt = 2.0 * u + eps * (D + 2.0 * u);  // error of a separation component
+  const double band = 4.0 * (2.0 * std::sqrt(3.0) * D * dlt + 3.0 * dlt * dlt) + 8.0 * eps * D * D;
+  pg.f_pre = std::nextafter((float)((double)pg.f_hi + band), 3.0e38f);
+  df_split(pg.erdr, &pg.erdr_hi, &pg.erdr_lo);
+  df_split(pg.vrdr, &pg.vrdr_hi, &pg.vrdr_lo);
+  df_split(pg.scaling, &pg.scal_hi, &pg.scal_lo);
+}
+
+// The cell-tile pair kernels (both forms) with the exclusion correction; results into
+// g.sc->acc like the per-atom kernels.
+void pair_forces_tiles(PairGeom& pg, int nb2) {
+  cudaStream_t st = g.stream;
+  pair_geom_df(pg);
+  const bool mixed = g.precision == GB_MIXED;
+  const TilePlan& tp = g.tp;
+  PairTileArgs A;
+  A.natms = g.natms;
+  A.tile_ids = nullptr;
+  A.cap = g.tile_cap_pair;
+  A.nrows = tp.nrows;
+  A.r00 = tp.r00;
+  A.blk_off = 0;
+  A.tile_rows = g.tile_rows; A.tile_info = g.tile_info; A.at_list = g.at_list;
+  A.list = g.list; A.ld = g.ld; A.tlist = g.tlist; A.ldt = g.ldt;
+  A.xhs = g.xhs; A.xls = g.xls; A.tys = g.tys;
+  A.x = g.x; A.y = g.y; A.z = g.z; A.q = g.chge;
+  A.etab = g.erfc_df; A.vtab = g.vdw_df; A.ecoef = g.erfc_coef; A.vcoef = g.vdw_coef;
+  A.vkind = g.vdw_kind; A.veps = g.vdw_eps; A.vsig = g.vdw_sig;
+  A.ntypes = g.p.ntypes;
+  A.rc2 = (float)pg.rc2; A.rv2 = (float)pg.rv2; A.alpha = (float)g.p.alpha;
+  A.a2rp = (float)(g.p.alpha * 2.0 / std::sqrt(3.14159265358979323846264338327950288));
+  A.scaling = (float)pg.scaling;
+  A.fixs = (unsigned long long*)g.fixs;
+  A.cnt = &g.sc->npairs_list;
+  const int n_over = g.n_tile_over;
+  const int nbt = tp.ntiles + n_over;
+  const int nbs = std::max(1, std::min(nblocks(g.mxatms, 256), 4 * g.nsm));  // stress blocks
+  double* blk = gb_blkacc(nbt * NACC_DF + nbs * 6 + nb2 * 8);
+  double* blks = blk + (size_t)nbt * NACC_DF;
+  double* blk2 = blks + (size_t)nbs * 6;
+  A.blk = blk;
+  auto kern = mixed ? k_pair_tile<1> : k_pair_tile<0>;
+  GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               PAIR_TILE_BYTES * TILE_CAP_MAX + 16));
+  GB_CUDA(cudaMemsetAsync(g.fixs, 0, sizeof(long long) * 3 * (size_t)g.mxatms, st));
+  if (!mixed) GB_CUDA(cudaMemsetAsync(g.fixp, 0, sizeof(long long) * 3 * (size_t)g.mxatms, st));
+  prof_begin(P_PAIR);
+  kern<<<tp.ntiles, PAIR_TILE_NT, (size_t)A.cap * PAIR_TILE_BYTES + 16, st>>>(A, pg);
+  GB_LAUNCHED();
+  if (n_over > 0) {
+    PairTileArgs B = A;
+    B.tile_ids = g.tile_over;
+    B.cap = g.tile_max_staged;
+    B.blk_off = tp.ntiles;
+    kern<<<n_over, PAIR_TILE_NT, (size_t)B.cap * PAIR_TILE_BYTES + 16, st>>>(B, pg);
+    GB_LAUNCHED();
+  }
+  k_slot_stress_fold<<<nbs, 256, 0, st>>>(g.natms, g.sc, g.at_list, g.src, g.x, g.y, g.z, g.fixs,
+                                          (unsigned long long*)g.fixp, blks);
+  GB_LAUNCHED();
+  if (!mixed) {
+    k_fix_add_fp64<<<nblocks(g.natms, 256), 256, 0, st>>>(g.natms, g.fixp, g.fx, g.fy, g.fz);
+    GB_LAUNCHED();
+  }
+  prof_end(P_PAIR);
+  gb_reduce_blocks(blk, nbt, NACC_DF, &g.sc->acc[A_PAIR]);
+  gb_reduce_blocks(blks, nbs, 6, &g.sc->acc[A_PAIR + NACC_DF]);
+  if (g.lbook) {
+    prof_begin(P_EXCL);
+    k_excl_fp64<<<nb2, 128, 0, st>>>(g.natms, g.list, g.ld, g.x, g.y, g.z, g.chge, g.ltg, g.src, g.p.alpha,
+                                     g.scaling, g.p.rcut, g.fx, g.fy, g.fz, blk2,
+                                     mixed ? (unsigned long long*)g.fixp : nullptr);
+    GB_LAUNCHED();
+    prof_end(P_EXCL);
+    gb_reduce_blocks(blk2, nb2, 8, &g.sc->acc[A_EXCL]);
+  }
+}
+
+}  // namespace
+
 // eng6: engrl, virrl, engex, virex, engvdw, virvdw; stress9 accumulates.
 void pair_forces(double* eng6, double* stress9) {
   PairGeom pg;
@@ -793,7 +1247,10 @@ void pair_forces(double* eng6, double* stress9) {
   double ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const int nb2 = nblocks(g.natms, 128);
   GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
-  if (g.precision == GB_FP64 && !g.fp64_native) {
+  const bool tiles = g.tiles_valid && g.use_tiles && !(g.precision == GB_FP64 && g.fp64_native);
+  if (tiles) {
+    pair_forces_tiles(pg, nb2);
+  } else if (g.precision == GB_FP64 && !g.fp64_native) {
     // double-float bands and spacings
     pg.f_rc2_lo = (float)(pg.rc2 * (1.0 - 1e-6));
     pg.f_rc2_hi = (float)(pg.rc2 * (1.0 + 1e-6));

@@ -301,10 +301,11 @@ class PathLib:
         return out if mode == 0 else out.reshape(-1, 3)
 
     def pair_counts(self) -> list:
-        """[half-list entries, pairs inside rc, list candidates decided in exact FP64]
-        of the last force evaluation and list build (GPU library only)."""
-        out = np.zeros(3, np.int64)
-        st = self._opt("pair_counts", c_int, [POINTER(c_int64), c_int])(_ptr(out, POINTER(c_int64)), 3)
+        """[half-list entries, pairs inside rc, list candidates decided in exact FP64,
+        forward halo entries, backward halo entries, cell tiles used, second-launch tiles,
+        cells per tile] of the last force evaluation and list build (GPU library only)."""
+        out = np.zeros(8, np.int64)
+        st = self._opt("pair_counts", c_int, [POINTER(c_int64), c_int])(_ptr(out, POINTER(c_int64)), 8)
         if st != 0:
             raise PathError(st, self.prefix + "pair_counts", self.strerror(st))
         return [int(v) for v in out]
