@@ -84,7 +84,7 @@ void free_all() {
                   g.lfrzn, g.ixyz, g.src, g.shcode, g.xbg, g.ybg, g.zbg, g.ox, g.oy, g.oz, g.which_cell,
                   g.cell_count, g.cell_start, g.cell_fill, g.at_list, g.sorted_pos, g.xs, g.xsf, g.list, g.blk,
                   g.list_excl, g.erfc_coef, g.erfc_coef_f, g.vdw_coef, g.vdw_coef_f,
-                  g.vdw_kind, g.vdw_eps, g.vdw_sig, g.erfc_df, g.vdw_df, g.qdf, g.tlist, g.xhs, g.xls, g.tys, g.fixs,
+                  g.vdw_kind, g.vdw_eps, g.vdw_sig, g.erfc_df, g.vdw_df, g.qdf, g.spos, g.xhs, g.xls, g.tys, g.fixs,
                   g.tile_rows, g.tile_info, g.tile_over, g.blkacc, g.con_i, g.con_j, g.con_d0, g.dxx, g.dyy,
                   g.dzz, g.dxt, g.dyt, g.dzt, g.dt2, g.gam, g.listot, g.acon_start, g.acon_list, g.sc, d_scratch};
   for (void* p : ptrs)
@@ -221,8 +221,8 @@ int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real, bo
   double e6[6] = {0, 0, 0, 0, 0, 0};
   integ_zero_forces();
   if (g.precision == GB_MIXED || !g.fp64_native) list_pos_f32();  // FP32 hi + lo positions
-  if (do_real && g.tiles_valid && g.use_tiles && (g.precision == GB_MIXED || !g.fp64_native))
-    list_pos_sorted();  // the same per sorted position, for the cell-tile pair kernels
+  if (do_real && g.spos_valid && g.use_sorted && (g.precision == GB_MIXED || !g.fp64_native))
+    list_pos_sorted();  // the same per sorted position, for the sorted-position pair kernels
   const bool mts = md_step && do_spme && mts_active();
   const bool full = mts ? mts_step_needs_spme() : (do_spme && g.has_coul);
   if (full) spme_forces(&erc, &vrc, strec);
@@ -441,8 +441,8 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     dalloc(&g.xs, mx); dalloc(&g.xsf, mx);
     g.ld = prm->max_list + 4;
     dalloc(&g.list, (size_t)g.ld * natms);
-    g.ldt = ((prm->max_list + 1 + 7) / 8) * 8;  // tlist(k, i), k = 1..max_list, rows 16-byte aligned
-    dalloc(&g.tlist, (size_t)g.ldt * natms);
+    g.ldt = ((prm->max_list + 1 + 3) / 4) * 4;  // spos(k, i), k = 1..max_list, rows 16-byte aligned
+    dalloc(&g.spos, (size_t)g.ldt * natms);
     dalloc(&g.xhs, mx); dalloc(&g.xls, mx); dalloc(&g.tys, mx);
     dalloc(&g.fixs, 3 * (size_t)mx);
     dalloc(&g.sc, 1);
@@ -485,8 +485,8 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     if (g.has_coul) spme_setup();  // an uncharged system has no electrostatics to set up
     g.nstep = 0;
     {
-      const char* e = getenv("GB_PAIR_TILES");
-      g.use_tiles = !(e && e[0] == '0');
+      const char* e = getenv("GB_PAIR_SORTED");
+      g.use_sorted = !(e && e[0] == '0');
     }
     thermo_setup(GB_NVE, 0.0, 0.0, 0.0, nullptr, 0.0);
     g.init = true;
@@ -913,7 +913,7 @@ int gb_pair_counts(int64_t* out, int n) {
     gb_sync_scalars();
     int64_t v[8] = {(int64_t)g.hsc->npairs_list, (int64_t)g.hsc->npairs_rc, (int64_t)g.hsc->ncand_fp64,
                     (int64_t)g.hsc->halo_fwd, (int64_t)g.hsc->halo_bwd,
-                    (int64_t)(g.tiles_valid && g.use_tiles), (int64_t)g.n_tile_over, (int64_t)g.tp.m};
+                    (int64_t)(g.spos_valid && g.use_sorted), (int64_t)g.n_tile_over, (int64_t)g.tp.m};
     for (int k = 0; k < n && k < 8; ++k) out[k] = v[k];
     return (int)GB_OK;
   });

@@ -62,15 +62,13 @@ enum {
   A_NSLOTS = 96
 };
 
-// Cell tiles of the list and pair kernels.  A tile is a run of m local link cells
-// along x at one (y, z); its CTA stages in shared memory every atom of the cells
-// that the forward half shell of its cells reaches, as one contiguous run of sorted
-// positions per row (dy, dz) of that shell.  A list entry then names its partner
-// by its slot in the tile's staged set (row base + position in the row).
+// Cell tiles of the list build.  A tile is a run of m local link cells along x at one
+// (y, z); its CTA stages in shared memory every atom of the cells that the forward half
+// shell of its cells reaches, as one contiguous run of sorted positions per row
+// (dy, dz) of that shell.
 constexpr int TILE_MAX_ROWS = 32;
-constexpr int TILE_CAP_TARGET = 1600;  // staged atoms per tile of the first launches (2 pair CTAs per SM)
-constexpr int TILE_CAP_MAX = 3968;     // largest staged set a CTA can hold (57 B per atom in the pair kernel)
-constexpr unsigned short TILE_SKIP = 0xFFFFu;  // entry evaluated from the partner's side
+constexpr int TILE_CAP_TARGET = 1600;  // staged atoms per tile of the list build's first launch
+constexpr int TILE_CAP_MAX = 8192;     // largest staged set a list CTA holds (20 B per atom)
 struct TilePlan {
   int m;                    // local cells per tile along x
   int ntx, nty, ntz, ntiles;
@@ -116,7 +114,7 @@ struct Dev {
   double *ox = nullptr, *oy = nullptr, *oz = nullptr;     // natms (SHAKE)
 
   // link cells / list
-  int nlx = 0, nly = 0, nlz = 0, nlp = 0, NX = 0, NY = 0, NZ = 0, ncells = 0, nsbcll = 0;
+  int nlx = 0, nly = 0, nlz = 0, nlp = 0, NX = 0, NY = 0, NZ = 0, ncells = 0, nsbcll = 0, nseg = 0;
   int* which_cell = nullptr;   // mxatms
   int* cell_count = nullptr;   // ncells+2
   int* cell_start = nullptr;   // ncells+2 (0-based start)
@@ -144,12 +142,12 @@ struct Dev {
   int* tile_info = nullptr;    // ntiles x 4: staged atoms, first and end sorted position of the i atoms
   int* tile_over = nullptr;    // ids of the tiles above the first launch's capacity
   int tiles_alloc = 0;
-  unsigned short* tlist = nullptr;  // natms x ldt: per list entry the partner's tile slot (or TILE_SKIP)
+  int* spos = nullptr;         // natms x ldt: per list entry the partner's sorted position (-1: backward copy)
   int ldt = 0;
-  int tile_cap_list = 0, tile_cap_pair = 0;   // staged atoms per tile of the first launches
+  int tile_cap_list = 0;       // staged atoms per tile of the list build's first launch
   int n_tile_over = 0, tile_max_staged = 0;   // from the last list build
-  bool tiles_valid = false;    // the last list pairs every halo entry with its backward copy
-  bool use_tiles = true;       // cell-tile pair kernels (GB_PAIR_TILES=0: the per-atom kernels)
+  bool spos_valid = false;     // the last list pairs every halo entry with its backward copy
+  bool use_sorted = true;      // sorted-position pair kernels (GB_PAIR_SORTED=0: the atom-index kernels)
   float4* xhs = nullptr;       // per sorted position: FP32 high parts (x, y, z, q)
   float4* xls = nullptr;       // per sorted position: remainders (x, y, z, q) of the FP64 values
   unsigned char* tys = nullptr;  // per sorted position: atom type
@@ -362,7 +360,7 @@ int list_refresh_halo();          // refresh halo positions (gb_list.cu)
 int list_build();                 // binning + pairs (gb_list.cu)
 void list_setup();                // link-cell geometry (gb_list.cu)
 void list_pos_f32();              // FP32 copy of positions and charges (mixed path)
-void list_pos_sorted();           // per sorted position: FP32 hi/lo positions, charge, type (cell tiles)
+void list_pos_sorted();           // per sorted position: FP32 hi/lo positions, charge, type
 void scan_exclusive(const int* in, int* out, int n);
 void pair_forces(double* eng6, double* stress9);  // gb_pair.cu (adds into forces)
 void pair_setup();                // gb_pair.cu: per-key constants

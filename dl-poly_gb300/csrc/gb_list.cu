@@ -24,6 +24,10 @@ __constant__ int c_off[MAX_SBC];   // linear cell offset of each semi-ball cell
 __constant__ int c_nix[MAX_SBC], c_niy[MAX_SBC], c_niz[MAX_SBC];
 __constant__ unsigned char c_nir[MAX_SBC];
 __constant__ unsigned char c_row[MAX_SBC];  // cell-tile row (dy, dz) of each semi-ball cell
+// The semi-ball cells in the reference order form, row by row, runs of consecutive cells
+// along x (contiguous sorted positions); a segment is such a run with one nir flag.
+__constant__ int c_seg_off0[MAX_SBC], c_seg_off1[MAX_SBC];  // linear offsets of its first and last cell
+__constant__ unsigned char c_seg_row[MAX_SBC], c_seg_nir[MAX_SBC];
 
 struct HaloGeom {
   double rc[9];
@@ -331,7 +335,7 @@ __global__ void k_cell_sort(int ncells_p1, const int* start, const int* tmp, int
 __global__ void __launch_bounds__(256) k_list_pairs(int natms, const DevScalars* sc_c, CellGeom cg, int nsbcll,
                                                     const int* at_list, const int* which_cell, const int* start,
                                                     const double4_32a* xs, const float4* xsf, int* list, int ld,
-                                                    int max_list, DevScalars* sc) {
+                                                    int* spos, int ldt, int max_list, DevScalars* sc) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int nlast = sc_c->nlast;
@@ -350,8 +354,9 @@ __global__ void __launch_bounds__(256) k_list_pairs(int natms, const DevScalars*
   const int nlx0e = nlp - 1, nly0e = nlp - 1, nlz0e = nlp - 1;
   const int nlx1s = cg.nlx + nlp, nly1s = cg.nly + nlp, nlz1s = cg.nlz + nlp;
   int* li = list + (size_t)i * ld + 3;  // li[k] == list(k, i)
+  int* si = spos + (size_t)i * ldt;
   int count = 0;
-  int ncand64 = 0;
+  int ncand64 = 0, nfwd = 0, nbwd = 0;
   const unsigned lt = (1u << lane) - 1u;
   for (int pass = 1; pass <= 2; ++pass) {
     if (pass == 2) {
@@ -398,13 +403,25 @@ __global__ void __launch_bounds__(256) k_list_pairs(int natms, const DevScalars*
         const unsigned m = __ballot_sync(0xffffffffu, acc);
         if (acc) {
           const int k = count + __popc(m & lt) + 1;
-          if (k <= max_list) li[k] = at_list[jj] + 1;
+          const int a = at_list[jj];
+          if (pass == 1) nfwd += a >= natms;
+          else ++nbwd;
+          if (k <= max_list) {
+            li[k] = a + 1;
+            si[k] = pass == 1 ? jj : -1;
+          }
         }
         count += __popc(m);
       }
     }
   }
   ncand64 = warp_sumi(ncand64);
+  nfwd = warp_sumi(nfwd);
+  nbwd = warp_sumi(nbwd);
+  if (lane == 0) {
+    if (nfwd) atomicAdd(&sc->halo_fwd, nfwd);
+    if (nbwd) atomicAdd(&sc->halo_bwd, nbwd);
+  }
   if (lane == 0) {
     // the stored length never exceeds max_list, so no later kernel can read
     // past the column even when the overflow status is ignored
@@ -454,17 +471,18 @@ __global__ void k_tile_rows(TilePlan tp, CellGeom cg, const int* __restrict__ st
 // Half-shell Verlet list (neighbours.F90:876-1184), one CTA per cell tile: the tile's
 // forward half shell (FP32 positions and atom ids) is staged in shared memory and one
 // warp per local atom walks it in the reference order (semi-ball cell by cell, each
-// cell's members in ascending order), with ballot compaction.  Beside list(k, i) the
-// kernel writes tlist(k, i): the partner's slot in the tile's staged set, or TILE_SKIP
-// for the entries of the backward halo pass (pass 2), whose pairs the partner atom's
-// forward pass also lists, so each pair is evaluated once, from its forward side.
-__global__ void __launch_bounds__(256) k_list_tiles(int natms, CellGeom cg, TilePlan tp, int nsbcll,
+// cell's members in ascending order), one run of consecutive cells at a time, with
+// ballot compaction.  Beside list(k, i) the kernel writes spos(k, i): the partner's
+// sorted position, or -1 for the entries of the backward halo pass (pass 2), whose
+// pairs the partner atom's forward pass also lists, so that the pair kernels evaluate
+// each pair once, from its forward copy.
+__global__ void __launch_bounds__(256) k_list_tiles(int natms, CellGeom cg, TilePlan tp, int nsbcll, int nseg,
                                                     const int* __restrict__ tile_ids, int cap,
                                                     const int* __restrict__ tile_rows, const int* __restrict__ tile_info,
                                                     const int* __restrict__ at_list, const int* __restrict__ which_cell,
                                                     const int* __restrict__ start, const double4_32a* __restrict__ xs,
-                                                    const float4* __restrict__ xsf, int* list, int ld,
-                                                    unsigned short* tlist, int ldt, int max_list, DevScalars* sc) {
+                                                    const float4* __restrict__ xsf, int* list, int ld, int* spos,
+                                                    int ldt, int max_list, DevScalars* sc) {
   extern __shared__ float4 s_x[];  // cap staged FP32 positions, then cap atom ids
   int* s_at = reinterpret_cast<int*>(s_x + cap);
   __shared__ int s_first[TILE_MAX_ROWS], s_base[TILE_MAX_ROWS + 1];
@@ -504,16 +522,15 @@ __global__ void __launch_bounds__(256) k_list_tiles(int natms, CellGeom cg, Tile
     const double4_32a xi = xs[p];
     const float4 xif = s_x[p + i0s];
     int* li = list + (size_t)i * ld + 3;  // li[k] == list(k, i)
-    unsigned short* ti = tlist + (size_t)i * ldt;
+    int* si = spos + (size_t)i * ldt;
     int count = 0;
-    // pass 1: the forward half shell, all of it staged
-    for (int kk = 0; kk < nsbcll; ++kk) {
-      const int jc = ic + c_off[kk];
-      const int r = c_row[kk];
+    // pass 1: the forward half shell, all of it staged, one run of cells at a time
+    for (int sg = 0; sg < nseg; ++sg) {
+      const int r = c_seg_row[sg];
       const int sl0 = s_base[r] - s_first[r];  // slot = sorted position + sl0
-      const int s0 = (jc != ic) ? start[jc] : p + 1;
-      const int e = start[jc + 1];
-      const bool nir = c_nir[kk] != 0;
+      const int s0 = sg == 0 ? p + 1 : start[ic + c_seg_off0[sg]];  // segment 0 starts with the own cell
+      const int e = start[ic + c_seg_off1[sg] + 1];
+      const bool nir = c_seg_nir[sg] != 0;
       for (int b = s0; b < e; b += 32) {
         const int jj = b + lane;
         bool acc = false;
@@ -542,7 +559,7 @@ __global__ void __launch_bounds__(256) k_list_tiles(int natms, CellGeom cg, Tile
           nfwd += a >= natms;
           if (k <= max_list) {
             li[k] = a + 1;
-            ti[k] = (unsigned short)(jj + sl0);
+            si[k] = jj;
           }
         }
         count += __popc(m);
@@ -587,7 +604,7 @@ __global__ void __launch_bounds__(256) k_list_tiles(int natms, CellGeom cg, Tile
             ++nbwd;
             if (k <= max_list) {
               li[k] = at_list[jj] + 1;
-              ti[k] = TILE_SKIP;
+              si[k] = -1;
             }
           }
           count += __popc(m);
@@ -620,13 +637,13 @@ __global__ void __launch_bounds__(256) k_list_tiles(int natms, CellGeom cg, Tile
 
 // Frozen (neighbours.F90:1198-1225) and excluded (:1229-1306) reordering, one
 // thread per atom, sequential exactly as the reference swaps.
-// The tile slots in tlist follow their list entries through every swap.
-__global__ void k_list_reorder(int natms, int* list, int ld, unsigned short* tlist, int ldt, const int* lfrzn,
+// The sorted positions in spos follow their list entries through every swap.
+__global__ void k_list_reorder(int natms, int* list, int ld, int* spos, int ldt, const int* lfrzn,
                                const int* ltg, const int* list_excl, int ldx, int megfrz, int lbook) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natms) return;
   int* li = list + (size_t)i * ld + 3;
-  unsigned short* ti = tlist + (size_t)i * ldt;
+  int* ti = spos + (size_t)i * ldt;
   int l_end = li[0], m_end = l_end;
   if (megfrz > 1 && lfrzn[i] > 0) {
     for (int kk = l_end; kk >= 1; --kk) {
@@ -634,7 +651,7 @@ __global__ void k_list_reorder(int natms, int* list, int ld, unsigned short* tli
       if (lfrzn[j - 1] > 0) {
         if (kk < m_end) {
           li[kk] = li[m_end]; li[m_end] = j;
-          const unsigned short tk = ti[kk]; ti[kk] = ti[m_end]; ti[m_end] = tk;
+          const int tk = ti[kk]; ti[kk] = ti[m_end]; ti[m_end] = tk;
         }
         --m_end;
       }
@@ -656,7 +673,7 @@ __global__ void k_list_reorder(int natms, int* list, int ld, unsigned short* tli
         if (hit) {
           if (kk < m_end) {
             li[kk] = li[m_end]; li[m_end] = j;
-            const unsigned short tk = ti[kk]; ti[kk] = ti[m_end]; ti[m_end] = tk;
+            const int tk = ti[kk]; ti[kk] = ti[m_end]; ti[m_end] = tk;
           }
           --m_end;
         }
@@ -802,6 +819,22 @@ void list_setup() {
     tp.r00 = row[0];  // offset (0, 0, 0) comes first; its row starts at dx = 0
     if (nix[0] != 0 || niy[0] != 0 || niz[0] != 0 || tp.dxlo[tp.r00] != 0) throw (int)GB_ERR_ARG;
     GB_CUDA(cudaMemcpyToSymbol(c_row, row.data(), row.size()));
+    // segments: consecutive semi-ball cells of one row, adjacent along x, with one nir flag
+    std::vector<int> s0, s1;
+    std::vector<unsigned char> srow, snir;
+    for (size_t k = 0; k < off.size(); ++k) {
+      const bool joins = k > 0 && row[k] == row[k - 1] && nix[k] == nix[k - 1] + 1 && nir[k] == nir[k - 1];
+      if (joins) {
+        s1.back() = off[k];
+      } else {
+        s0.push_back(off[k]); s1.push_back(off[k]); srow.push_back(row[k]); snir.push_back(nir[k]);
+      }
+    }
+    g.nseg = (int)s0.size();
+    GB_CUDA(cudaMemcpyToSymbol(c_seg_off0, s0.data(), sizeof(int) * s0.size()));
+    GB_CUDA(cudaMemcpyToSymbol(c_seg_off1, s1.data(), sizeof(int) * s1.size()));
+    GB_CUDA(cudaMemcpyToSymbol(c_seg_row, srow.data(), srow.size()));
+    GB_CUDA(cudaMemcpyToSymbol(c_seg_nir, snir.data(), snir.size()));
     // tile width: the widest run of cells whose staged set stays near the capacity the
     // pair kernel's shared memory allows at two CTAs per SM
     const double apc = (double)g.natms / ((double)nlx * nly * nlz);
@@ -824,7 +857,7 @@ void list_setup() {
     int cap = (int)(1.3 * cells_of(m) * apc) + 64;
     const char* ec = getenv("GB_TILE_CAP");  // a smaller first-launch capacity sends more tiles to the second launch
     if (ec && atoi(ec) > 0) cap = atoi(ec);
-    g.tile_cap_list = g.tile_cap_pair = std::min(((cap + 31) / 32) * 32, (int)TILE_CAP_MAX);
+    g.tile_cap_list = std::min(((cap + 31) / 32) * 32, (int)TILE_CAP_MAX);
     if (g.tiles_alloc < tp.ntiles) {
       cudaFree(g.tile_rows); cudaFree(g.tile_info); cudaFree(g.tile_over);
       GB_CUDA(cudaMalloc(&g.tile_rows, sizeof(int) * 2 * (size_t)tp.ntiles * TILE_MAX_ROWS));
@@ -863,6 +896,7 @@ void list_setup() {
 
 int list_relocate_and_halo() {
   const int n = g.natms;
+  g.spos_valid = false;  // new halo images: the sorted positions of the list are stale until the next build
   const int T = 256;
   cudaStream_t st = g.stream;
   prof_begin(P_HALO);
@@ -946,31 +980,30 @@ int list_build() {
                                                         g.tile_over, g.sc);
   GB_LAUNCHED();
   GB_CUDA(cudaFuncSetAttribute(k_list_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, 20 * TILE_CAP_MAX));
-  k_list_tiles<<<tp.ntiles, 256, (size_t)cap * 20, st>>>(g.natms, h_cg, tp, g.nsbcll, nullptr, cap, g.tile_rows,
-                                                          g.tile_info, g.at_list, g.which_cell, g.cell_start, g.xs,
-                                                          g.xsf, g.list, g.ld, g.tlist, g.ldt, g.p.max_list, g.sc);
+  k_list_tiles<<<tp.ntiles, 256, (size_t)cap * 20, st>>>(g.natms, h_cg, tp, g.nsbcll, g.nseg, nullptr, cap,
+                                                          g.tile_rows, g.tile_info, g.at_list, g.which_cell,
+                                                          g.cell_start, g.xs, g.xsf, g.list, g.ld, g.spos, g.ldt,
+                                                          g.p.max_list, g.sc);
   GB_LAUNCHED();
   gb_sync_scalars();
   g.n_tile_over = g.hsc->tile_over;
   g.tile_max_staged = g.hsc->tile_max;
-  bool tiled = true;
   if (g.n_tile_over > 0 && g.tile_max_staged <= TILE_CAP_MAX) {
     // the tiles above the capacity, with shared memory for the largest of them
     k_list_tiles<<<g.n_tile_over, 256, (size_t)g.tile_max_staged * 20, st>>>(
-        g.natms, h_cg, tp, g.nsbcll, g.tile_over, g.tile_max_staged, g.tile_rows, g.tile_info, g.at_list,
-        g.which_cell, g.cell_start, g.xs, g.xsf, g.list, g.ld, g.tlist, g.ldt, g.p.max_list, g.sc);
+        g.natms, h_cg, tp, g.nsbcll, g.nseg, g.tile_over, g.tile_max_staged, g.tile_rows, g.tile_info, g.at_list,
+        g.which_cell, g.cell_start, g.xs, g.xsf, g.list, g.ld, g.spos, g.ldt, g.p.max_list, g.sc);
     GB_LAUNCHED();
   } else if (g.n_tile_over > 0) {
-    // a tile too dense for one CTA's shared memory: the whole list from the per-atom
-    // kernel, and the pair kernels that walk it without tiles
-    tiled = false;
+    // a tile too dense for one CTA's shared memory: the whole list from the per-atom kernel
+    GB_CUDA(cudaMemsetAsync(&g.sc->halo_fwd, 0, 2 * sizeof(int), st));
     k_list_pairs<<<nblocks((long long)mx * 32, T), T, 0, st>>>(g.natms, g.sc, h_cg, g.nsbcll, g.at_list,
                                                                g.which_cell, g.cell_start, g.xs, g.xsf, g.list, g.ld,
-                                                               g.p.max_list, g.sc);
+                                                               g.spos, g.ldt, g.p.max_list, g.sc);
     GB_LAUNCHED();
   }
   if (g.lbook || g.megfrz > 1) {
-    k_list_reorder<<<nblocks(g.natms, 128), 128, 0, st>>>(g.natms, g.list, g.ld, g.tlist, g.ldt, g.lfrzn, g.ltg,
+    k_list_reorder<<<nblocks(g.natms, 128), 128, 0, st>>>(g.natms, g.list, g.ld, g.spos, g.ldt, g.lfrzn, g.ltg,
                                                           g.list_excl, g.p.max_exclude + 1, g.megfrz,
                                                           g.lbook ? 1 : 0);
     GB_LAUNCHED();
@@ -979,8 +1012,9 @@ int list_build() {
   gb_sync_scalars();
   if (g.hsc->status & ST_LIST_OVERFLOW) return GB_ERR_LIST_OVERFLOW;
   // every pair across the periodic boundary is listed from both of its atoms, once in a
-  // forward pass and once in the backward halo pass; the tile kernels evaluate the forward copy
-  g.tiles_valid = tiled && g.hsc->halo_fwd == g.hsc->halo_bwd;
+  // forward pass and once in the backward halo pass; the sorted-position pair kernels
+  // evaluate the forward copy (else the atom-index kernels run, by the smaller global id)
+  g.spos_valid = g.hsc->halo_fwd == g.hsc->halo_bwd;
   ++g.list_gen;  // the learned-MTS short list is rebuilt from this list on demand
   return GB_OK;
 }

@@ -717,30 +717,24 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 4) k_pair_df64(int natms, const De
   block_reduce_store<NACC_DF>(out, blk);
 }
 
-// ------------------------------------------------------------ cell-tile kernels
-// One CTA per cell tile (a run of link cells along x): the positions, charges and types
-// of every atom the tile's forward half shell reaches are staged in shared memory, in
-// one contiguous run of sorted positions per shell row, together with int64 fixed-point
-// force accumulators.  Warps take the tile's own atoms one at a time and walk each
-// atom's Verlet list through its tile slots (tlist): the partner's data come from
-// shared memory, its reaction goes to its shared accumulator with an integer atomic,
-// and at the end the CTA adds its accumulators to the per-sorted-position forces.
-// Pairs with a halo image are evaluated by the entry of the forward pass (the partner
-// atom's backward-pass copy is marked TILE_SKIP).  Integer sums make the forces
-// independent of the order of warps, tiles and atomics.
-constexpr int PAIR_TILE_NT = 256;
-constexpr int PAIR_TILE_BYTES = 57;  // shared bytes per staged atom: hi + lo float4, 3 x int64, type
+// ------------------------------------------------------- sorted-position kernels
+// The pair loop over the list's partners in cell (sorted) order.  The list build writes,
+// beside list(k, i), spos(k, i): the partner's position in the cell-sorted arrays, or -1
+// for an entry of the backward halo pass (that pair is also listed, in its forward
+// pass, by the partner atom and is evaluated there).  Persistent warps walk the local
+// atoms in sorted order, so the warps of a CTA work on one cell and read the same
+// neighbour cells: the partner data (FP32 high parts with the charge, remainders, type)
+// are contiguous runs that L1 holds, not gathers by atom index.  Pair forces go to
+// per-sorted-position int64 fixed-point sums (64-bit integer reductions: the result does
+// not depend on their order); k_slot_stress_fold sums the stress and moves them to atoms.
+constexpr int PAIR_SORTED_NT = 256;
 
-struct PairTileArgs {
+struct PairSortedArgs {
   int natms;
-  const int* tile_ids;  // nullptr: tile = blockIdx.x
-  int cap, nrows, r00, blk_off;
-  const int* tile_rows;
-  const int* tile_info;
   const int* at_list;
   const int* list;
   int ld;
-  const unsigned short* tlist;
+  const int* spos;
   int ldt;
   const float4* xhs;
   const float4* xls;
@@ -758,22 +752,16 @@ struct PairTileArgs {
   unsigned long long* fixs;
   double* blk;
   unsigned long long* cnt;
+  const DevScalars* sc;
 };
 
-// atom index of a tile slot (rows are contiguous runs of sorted positions)
-__device__ __forceinline__ int tile_slot_atom(int slot, int nrows, const int* s_first, const int* s_base,
-                                              const int* __restrict__ at_list) {
-  int r = 0;
-  while (r + 1 < nrows && s_base[r + 1] <= slot) ++r;
-  return at_list[s_first[r] + (slot - s_base[r])];
-}
-
-// The FP64 form's terms of one pair from tile data (the arithmetic of pair_terms_df64);
-// returns false when the pair exerts no force.
-__device__ __forceinline__ bool pair_df64_tile(const PairGeom& pg, const PairTileArgs& A, int i, int slot, int ai,
+// The FP64 form's terms of one pair (the arithmetic of pair_terms_df64, partner data
+// passed in); j is the partner's atom index for the exact FP64 evaluation near a cutoff.
+// Returns false when the pair exerts no force.
+__device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSortedArgs& A, int i, int j, int ai,
                                                int aj, df qi, bool qi_on, float qjh, float qjl, df dx, df dy, df dz,
-                                               df rsq, int nrows, const int* s_first, const int* s_base,
-                                               dacc (&acc)[NACC_DF], long long& ix, long long& iy, long long& iz) {
+                                               df rsq, dacc (&acc)[NACC_DF], long long& ix, long long& iy,
+                                               long long& iz) {
   const bool band = (rsq.hi >= pg.f_rc2_lo && rsq.hi <= pg.f_rc2_hi) ||
                     (rsq.hi >= pg.f_rv2_lo && rsq.hi <= pg.f_rv2_hi);
   const bool in_c = qi_on && qjh != 0.0f && rsq.hi < pg.f_rc2_lo;
@@ -818,7 +806,6 @@ __device__ __forceinline__ bool pair_df64_tile(const PairGeom& pg, const PairTil
     }
   }
   if (slow) {
-    const int j = tile_slot_atom(slot, nrows, s_first, s_base, A.at_list);
     double g64, e64c, e64v, gc64, gv64;
     bool any;
     pair_terms_fp64(pg, A.x[i] - A.x[j], A.y[i] - A.y[j], A.z[i] - A.z[j], A.q[i] * pg.scaling, A.q[j], ai, aj,
@@ -844,9 +831,9 @@ __device__ __forceinline__ bool pair_df64_tile(const PairGeom& pg, const PairTil
 }
 
 // The mixed form's terms of one pair (FP32, analytic erfc and 12-6 LJ, as k_pair_mixed_half)
-__device__ __forceinline__ bool pair_mixed_tile(const PairTileArgs& A, const float4* s_lj, int row, int aj, float qi,
-                                                float qj, float dx, float dy, float dz, dacc (&acc)[NACC_DF],
-                                                long long& ix, long long& iy, long long& iz) {
+__device__ __forceinline__ bool pair_mixed_eval(const PairSortedArgs& A, const float4* s_lj, int row, int aj,
+                                                float qi, float qj, float dx, float dy, float dz,
+                                                dacc (&acc)[NACC_DF], long long& ix, long long& iy, long long& iz) {
   const float rsq = dx * dx + dy * dy + dz * dz;
   if (rsq >= A.rc2 && rsq >= A.rv2) return false;
   const float rinv = rsqrtf(rsq);
@@ -887,73 +874,34 @@ __device__ __forceinline__ bool pair_mixed_tile(const PairTileArgs& A, const flo
 }
 
 template <int MIXED>
-__global__ void __launch_bounds__(PAIR_TILE_NT) k_pair_tile(PairTileArgs A, PairGeom pg) {
-  extern __shared__ float4 sm_tile[];
-  const int cap = A.cap;
-  float4* s_hi = sm_tile;
-  float4* s_lo = sm_tile + cap;
-  unsigned long long* s_f = reinterpret_cast<unsigned long long*>(sm_tile + 2 * cap);
-  unsigned char* s_ty = reinterpret_cast<unsigned char*>(s_f + 3 * cap);
-  __shared__ int s_first[TILE_MAX_ROWS], s_base[TILE_MAX_ROWS + 1];
-  __shared__ int s_next;
-  __shared__ PairQueue pq[PAIR_TILE_NT / 32];
+__global__ void __launch_bounds__(PAIR_SORTED_NT, 4) k_pair_sorted(PairSortedArgs A, PairGeom pg) {
+  __shared__ PairQueue pq[PAIR_SORTED_NT / 32];
   __shared__ float4 s_lj[MIXED ? MAX_TYPES * MAX_TYPES : 1];
-  const int t = A.tile_ids ? A.tile_ids[blockIdx.x] : blockIdx.x;
-  const int nst = A.tile_info[4 * t];
-  double* blk = A.blk + (size_t)A.blk_off * NACC_DF;
-  if (nst > cap) {  // the overflow launch evaluates this tile; its accumulator slots stay zero
-    if (threadIdx.x < NACC_DF) blk[(size_t)blockIdx.x * NACC_DF + threadIdx.x] = 0.0;
-    return;
-  }
-  const int nrows = A.nrows;
-  if (threadIdx.x < nrows) {
-    s_first[threadIdx.x] = A.tile_rows[2 * (t * nrows + threadIdx.x)];
-    s_base[threadIdx.x] = A.tile_rows[2 * (t * nrows + threadIdx.x) + 1];
-  }
-  if (threadIdx.x == 0) {
-    s_base[nrows] = nst;
-    s_next = 0;
-  }
   if (MIXED) {
     for (int e = threadIdx.x; e < A.ntypes * A.ntypes; e += blockDim.x) {
       const int ai = e / A.ntypes + 1, aj = e % A.ntypes + 1;
       s_lj[e] = c_lj[vkey(ai, aj) - 1];
     }
+    __syncthreads();
   }
-  __syncthreads();
-  for (int r = 0; r < nrows; ++r) {
-    const int b = s_base[r], cnt = s_base[r + 1] - b, f = s_first[r];
-    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-      s_hi[b + e] = A.xhs[f + e];
-      s_lo[b + e] = A.xls[f + e];
-      s_ty[b + e] = A.tys[f + e];
-    }
-  }
-  for (int e = threadIdx.x; e < 3 * nst; e += blockDim.x) s_f[e] = 0ull;
-  __syncthreads();
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-  const int ip0 = A.tile_info[4 * t + 1], ip1 = A.tile_info[4 * t + 2];
-  const int i0s = s_base[A.r00] - s_first[A.r00];
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   dacc acc[NACC_DF];
 #pragma unroll
   for (int k = 0; k < NACC_DF; ++k) { acc[k].s = 0.f; acc[k].c = 0.f; }
   unsigned long long n_list = 0, n_rc = 0;
-  for (;;) {
-    int k = 0;
-    if (lane == 0) k = atomicAdd(&s_next, 1);
-    k = __shfl_sync(0xffffffffu, k, 0);
-    const int p = ip0 + k;
-    if (p >= ip1) break;
-    const int islot = p + i0s;
+  const int nlast = A.sc->nlast;
+  for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < nlast; p += nwarps) {
     const int i = A.at_list[p];
-    const float4 pi = s_hi[islot], li = s_lo[islot];
-    const int ai = s_ty[islot];
+    if (i >= A.natms) continue;  // a halo image: no list of its own
+    const float4 pi = A.xhs[p], li = A.xls[p];
+    const int ai = A.tys[p];
     const df qi = df_mul(df_make(pi.w, li.w), df_make(pg.scal_hi, pg.scal_lo));  // q_i r4pie0/eps
     const bool qi_on = pi.w != 0.0f;
     const float qi32 = pi.w * A.scaling;
     const int ljrow = (ai - 1) * A.ntypes - 1;
     const int n = A.list[(size_t)i * A.ld + 3];
-    const unsigned short* tl = A.tlist + (size_t)i * A.ldt;
+    const int* sp = A.spos + (size_t)i * A.ldt;
     long long sx = 0, sy = 0, sz = 0;
     // pass 1, 32 entries at a time: an FP32 r^2 of the high parts against the outer
     // cutoff plus a bound on their rounding queues the candidates (ballot compaction);
@@ -964,47 +912,47 @@ __global__ void __launch_bounds__(PAIR_TILE_NT) k_pair_tile(PairTileArgs A, Pair
       if (more) {
         const int m = base + lane + 1;
         bool keep = false;
-        int slot = 0;
+        int j = 0;
         if (m <= n) {
-          slot = tl[m];
-          if (slot != TILE_SKIP) {
-            const float4 pj = s_hi[slot];
+          j = sp[m];
+          if (j >= 0) {
+            const float4 pj = A.xhs[j];
             const float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
             keep = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= pg.f_pre;
           }
         }
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
-        if (keep) pq[wq].j[nq + __popc(bal & ((1u << lane) - 1u))] = slot;
+        if (keep) pq[wq].j[nq + __popc(bal & ((1u << lane) - 1u))] = j;
         nq += __popc(bal);
         __syncwarp();
       }
       if (nq >= 32 || (!more && nq > 0)) {
         const int take = min(nq, 32);
         if (lane < take) {
-          const int slot = pq[wq].j[nq - take + lane];
-          const float4 pj = s_hi[slot], lj = s_lo[slot];
-          const int aj = s_ty[slot];
+          const int j = pq[wq].j[nq - take + lane];
+          const float4 pj = A.xhs[j], lj = A.xls[j];
+          const int aj = A.tys[j];
           long long ix = 0, iy = 0, iz = 0;
           bool hit;
           if (MIXED) {
             const float dx = (pi.x - pj.x) + (li.x - lj.x), dy = (pi.y - pj.y) + (li.y - lj.y),
                         dz = (pi.z - pj.z) + (li.z - lj.z);
-            hit = pair_mixed_tile(A, s_lj, ljrow, aj, qi32, pj.w, dx, dy, dz, acc, ix, iy, iz);
+            hit = pair_mixed_eval(A, s_lj, ljrow, aj, qi32, pj.w, dx, dy, dz, acc, ix, iy, iz);
           } else {
             const df ex = two_sum(pi.x, -pj.x), ey = two_sum(pi.y, -pj.y), ez = two_sum(pi.z, -pj.z);
             const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
             const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
             const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
             const df rsq = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
-            hit = rsq.hi <= pg.f_hi && pair_df64_tile(pg, A, i, slot, ai, aj, qi, qi_on, pj.w, lj.w, dx, dy, dz,
-                                                      rsq, nrows, s_first, s_base, acc, ix, iy, iz);
+            hit = rsq.hi <= pg.f_hi && pair_df64_eval(pg, A, i, A.at_list[j], ai, aj, qi, qi_on, pj.w, lj.w, dx,
+                                                      dy, dz, rsq, acc, ix, iy, iz);
           }
           if (hit) {
             ++n_rc;
             sx += ix; sy += iy; sz += iz;
-            atomicAdd(&s_f[3 * slot + 0], (unsigned long long)(-ix));
-            atomicAdd(&s_f[3 * slot + 1], (unsigned long long)(-iy));
-            atomicAdd(&s_f[3 * slot + 2], (unsigned long long)(-iz));
+            atomicAdd(&A.fixs[3 * (size_t)j + 0], (unsigned long long)(-ix));
+            atomicAdd(&A.fixs[3 * (size_t)j + 1], (unsigned long long)(-iy));
+            atomicAdd(&A.fixs[3 * (size_t)j + 2], (unsigned long long)(-iz));
           }
         }
         nq -= take;
@@ -1019,19 +967,10 @@ __global__ void __launch_bounds__(PAIR_TILE_NT) k_pair_tile(PairTileArgs A, Pair
       sz += __shfl_xor_sync(0xffffffffu, sz, o);
     }
     if (lane == 0) {
-      atomicAdd(&s_f[3 * islot + 0], (unsigned long long)sx);
-      atomicAdd(&s_f[3 * islot + 1], (unsigned long long)sy);
-      atomicAdd(&s_f[3 * islot + 2], (unsigned long long)sz);
+      atomicAdd(&A.fixs[3 * (size_t)p + 0], (unsigned long long)sx);
+      atomicAdd(&A.fixs[3 * (size_t)p + 1], (unsigned long long)sy);
+      atomicAdd(&A.fixs[3 * (size_t)p + 2], (unsigned long long)sz);
       n_list += (unsigned long long)n;
-    }
-  }
-  __syncthreads();
-  // the tile's accumulators into the per-sorted-position forces (coalesced within each row)
-  for (int r = 0; r < nrows; ++r) {
-    const int b = s_base[r], cnt = s_base[r + 1] - b, f = s_first[r];
-    for (int e = threadIdx.x; e < 3 * cnt; e += blockDim.x) {
-      const unsigned long long v = s_f[3 * b + e];
-      if (v) atomicAdd(&A.fixs[3 * (size_t)f + e], v);
     }
   }
   dfr out[NACC_DF];
@@ -1042,7 +981,7 @@ __global__ void __launch_bounds__(PAIR_TILE_NT) k_pair_tile(PairTileArgs A, Pair
     if (n_list) atomicAdd(&A.cnt[0], n_list);
     if (n_rc) atomicAdd(&A.cnt[1], n_rc);
   }
-  block_reduce_store<NACC_DF>(out, blk);
+  block_reduce_store<NACC_DF>(out, A.blk);
 }
 
 // Pair stress from the per-sorted-position forces (sum over slots of x (x) F, every halo
@@ -1143,22 +1082,16 @@ void pair_geom_df(PairGeom& pg) {
   df_split(pg.scaling, &pg.scal_hi, &pg.scal_lo);
 }
 
-// The cell-tile pair kernels (both forms) with the exclusion correction; results into
-// g.sc->acc like the per-atom kernels.
-void pair_forces_tiles(PairGeom& pg, int nb2) {
+// The sorted-position pair kernels (both forms) with the exclusion correction; results
+// into g.sc->acc like the per-atom kernels.
+void pair_forces_sorted(PairGeom& pg, int nb2) {
   cudaStream_t st = g.stream;
   pair_geom_df(pg);
   const bool mixed = g.precision == GB_MIXED;
-  const TilePlan& tp = g.tp;
-  PairTileArgs A;
+  PairSortedArgs A;
   A.natms = g.natms;
-  A.tile_ids = nullptr;
-  A.cap = g.tile_cap_pair;
-  A.nrows = tp.nrows;
-  A.r00 = tp.r00;
-  A.blk_off = 0;
-  A.tile_rows = g.tile_rows; A.tile_info = g.tile_info; A.at_list = g.at_list;
-  A.list = g.list; A.ld = g.ld; A.tlist = g.tlist; A.ldt = g.ldt;
+  A.at_list = g.at_list;
+  A.list = g.list; A.ld = g.ld; A.spos = g.spos; A.ldt = g.ldt;
   A.xhs = g.xhs; A.xls = g.xls; A.tys = g.tys;
   A.x = g.x; A.y = g.y; A.z = g.z; A.q = g.chge;
   A.etab = g.erfc_df; A.vtab = g.vdw_df; A.ecoef = g.erfc_coef; A.vcoef = g.vdw_coef;
@@ -1169,29 +1102,21 @@ void pair_forces_tiles(PairGeom& pg, int nb2) {
   A.scaling = (float)pg.scaling;
   A.fixs = (unsigned long long*)g.fixs;
   A.cnt = &g.sc->npairs_list;
-  const int n_over = g.n_tile_over;
-  const int nbt = tp.ntiles + n_over;
+  A.sc = g.sc;
+  auto kern = mixed ? k_pair_sorted<1> : k_pair_sorted<0>;
+  static int occ[2] = {0, 0};
+  if (!occ[mixed]) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[mixed], kern, PAIR_SORTED_NT, 0));
+  const int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, PAIR_SORTED_NT), occ[mixed] * g.nsm));
   const int nbs = std::max(1, std::min(nblocks(g.mxatms, 256), 4 * g.nsm));  // stress blocks
-  double* blk = gb_blkacc(nbt * NACC_DF + nbs * 6 + nb2 * 8);
-  double* blks = blk + (size_t)nbt * NACC_DF;
+  double* blk = gb_blkacc(nb * NACC_DF + nbs * 6 + nb2 * 8);
+  double* blks = blk + (size_t)nb * NACC_DF;
   double* blk2 = blks + (size_t)nbs * 6;
   A.blk = blk;
-  auto kern = mixed ? k_pair_tile<1> : k_pair_tile<0>;
-  GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               PAIR_TILE_BYTES * TILE_CAP_MAX + 16));
   GB_CUDA(cudaMemsetAsync(g.fixs, 0, sizeof(long long) * 3 * (size_t)g.mxatms, st));
   if (!mixed) GB_CUDA(cudaMemsetAsync(g.fixp, 0, sizeof(long long) * 3 * (size_t)g.mxatms, st));
   prof_begin(P_PAIR);
-  kern<<<tp.ntiles, PAIR_TILE_NT, (size_t)A.cap * PAIR_TILE_BYTES + 16, st>>>(A, pg);
+  kern<<<nb, PAIR_SORTED_NT, 0, st>>>(A, pg);
   GB_LAUNCHED();
-  if (n_over > 0) {
-    PairTileArgs B = A;
-    B.tile_ids = g.tile_over;
-    B.cap = g.tile_max_staged;
-    B.blk_off = tp.ntiles;
-    kern<<<n_over, PAIR_TILE_NT, (size_t)B.cap * PAIR_TILE_BYTES + 16, st>>>(B, pg);
-    GB_LAUNCHED();
-  }
   k_slot_stress_fold<<<nbs, 256, 0, st>>>(g.natms, g.sc, g.at_list, g.src, g.x, g.y, g.z, g.fixs,
                                           (unsigned long long*)g.fixp, blks);
   GB_LAUNCHED();
@@ -1200,7 +1125,7 @@ void pair_forces_tiles(PairGeom& pg, int nb2) {
     GB_LAUNCHED();
   }
   prof_end(P_PAIR);
-  gb_reduce_blocks(blk, nbt, NACC_DF, &g.sc->acc[A_PAIR]);
+  gb_reduce_blocks(blk, nb, NACC_DF, &g.sc->acc[A_PAIR]);
   gb_reduce_blocks(blks, nbs, 6, &g.sc->acc[A_PAIR + NACC_DF]);
   if (g.lbook) {
     prof_begin(P_EXCL);
@@ -1247,9 +1172,9 @@ void pair_forces(double* eng6, double* stress9) {
   double ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const int nb2 = nblocks(g.natms, 128);
   GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
-  const bool tiles = g.tiles_valid && g.use_tiles && !(g.precision == GB_FP64 && g.fp64_native);
-  if (tiles) {
-    pair_forces_tiles(pg, nb2);
+  const bool sorted = g.spos_valid && g.use_sorted && !(g.precision == GB_FP64 && g.fp64_native);
+  if (sorted) {
+    pair_forces_sorted(pg, nb2);
   } else if (g.precision == GB_FP64 && !g.fp64_native) {
     // double-float bands and spacings
     pg.f_rc2_lo = (float)(pg.rc2 * (1.0 - 1e-6));

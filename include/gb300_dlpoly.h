@@ -317,8 +317,8 @@ int gb_profile_read(char* names, double* ms, int64_t* launches, int max);
  * [1] unique pairs inside rc, [2] list-build candidates tested in exact FP64,
  * [3] list entries with a halo image from the forward half shell, [4] from the
  * backward halo pass (equal when every such pair is listed from both atoms),
- * [5] 1 when the cell-tile pair kernels ran, [6] tiles of the second (larger
- * shared memory) launch, [7] link cells per tile along x. */
+ * [5] 1 when the pair kernels walked the sorted-position list, [6] list-build
+ * tiles of the second (larger shared memory) launch, [7] link cells per tile along x. */
 int gb_pair_counts(int64_t* out, int n);
 
 /* FP64 FMA throughput of this device in TFLOP/s, measured by a register-

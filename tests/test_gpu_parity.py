@@ -311,34 +311,37 @@ def test_shake_rattle_exports_match_vv(gpu_lib):
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("name", ["nacl_4096", "water_5184"])
-def test_cell_tiles_match_per_atom_kernels(gpu_lib, monkeypatch, name, precision):
-    """The cell-tile pair kernels (partners staged in shared memory) against the per-atom
-    kernels on the same list: forces and energies agree to rounding, every halo entry of
-    the forward pass has its backward copy, and a small first-launch capacity (most tiles
-    in the second launch) changes nothing."""
+def test_sorted_pair_kernels_match_atom_index_kernels(gpu_lib, monkeypatch, name, precision):
+    """The pair kernels over the sorted-position list (partners in cell order, halo pairs
+    from their forward copy) against the atom-index kernels on the same list: forces and
+    energies agree to rounding and every forward halo entry has its backward copy.  A small
+    first-launch capacity of the tiled list build (most tiles in its second launch) changes
+    nothing."""
     s = CASES[name]()
     runs = {}
-    for mode, env in (("atom", {"GB_PAIR_TILES": "0"}), ("tile", {}), ("tile_small", {"GB_TILE_CAP": "64"})):
-        monkeypatch.delenv("GB_PAIR_TILES", raising=False)
+    for mode, env in (("atom", {"GB_PAIR_SORTED": "0"}), ("sorted", {}), ("small_cap", {"GB_TILE_CAP": "64"})):
+        monkeypatch.delenv("GB_PAIR_SORTED", raising=False)
         monkeypatch.delenv("GB_TILE_CAP", raising=False)
         for k, v in env.items():
             monkeypatch.setenv(k, v)
         gpu_lib.init(s, precision=precision)
         gpu_lib.relocate()
-        gpu_lib.link_cell_pairs(want_list=False)
+        lst = gpu_lib.link_cell_pairs()
         e, st = gpu_lib.two_body_forces()
-        runs[mode] = (e, st, gpu_lib.download(), gpu_lib.pair_counts())
+        runs[mode] = (e, st, gpu_lib.download(), gpu_lib.pair_counts(), lst)
     monkeypatch.delenv("GB_TILE_CAP", raising=False)
     a = runs["atom"]
-    for mode in ("tile", "tile_small"):
+    for mode in ("sorted", "small_cap"):
         b = runs[mode]
         cnt = b[3]
-        assert cnt[5] == 1, mode  # the tile kernels ran
+        assert cnt[5] == 1, mode  # the sorted-position kernels ran
         assert cnt[3] == cnt[4] and cnt[3] > 0
         assert cnt[0] == a[3][0] and cnt[1] == a[3][1]  # same list entries and pairs inside rc
-        tol = 1e-12 if precision == 0 else 1e-5
+        assert np.array_equal(b[4], a[4])
+        # the two kernels evaluate a halo pair from opposite sides: double-float rounding (~1e-12)
+        tol = 1e-11 if precision == 0 else 1e-5
         assert force_dev(b[2], a[2]) < tol, mode
         for k in a[0]:
             assert abs(b[0][k] - a[0][k]) <= tol * max(abs(a[0][k]), 1.0), (mode, k)
         assert np.abs(b[1] - a[1]).max() <= tol * np.abs(a[1]).max()
-    assert runs["tile_small"][3][6] > 0  # the second launch ran
+    assert runs["small_cap"][3][6] > 0  # the list build's second launch ran
