@@ -873,9 +873,14 @@ __device__ __forceinline__ bool pair_mixed_eval(const PairSortedArgs& A, const f
   return true;
 }
 
-template <int MIXED>
+template <int N>
+struct PairQueueN {
+  int j[N];
+};
+
+template <int MIXED, int U>
 __global__ void __launch_bounds__(PAIR_SORTED_NT, 4) k_pair_sorted(PairSortedArgs A, PairGeom pg) {
-  __shared__ PairQueue pq[PAIR_SORTED_NT / 32];
+  __shared__ PairQueueN<32 * (U + 1)> pq[PAIR_SORTED_NT / 32];
   __shared__ float4 s_lj[MIXED ? MAX_TYPES * MAX_TYPES : 1];
   if (MIXED) {
     for (int e = threadIdx.x; e < A.ntypes * A.ntypes; e += blockDim.x) {
@@ -903,30 +908,35 @@ __global__ void __launch_bounds__(PAIR_SORTED_NT, 4) k_pair_sorted(PairSortedArg
     const int n = A.list[(size_t)i * A.ld + 3];
     const int* sp = A.spos + (size_t)i * A.ldt;
     long long sx = 0, sy = 0, sz = 0;
-    // pass 1, 32 entries at a time: an FP32 r^2 of the high parts against the outer
-    // cutoff plus a bound on their rounding queues the candidates (ballot compaction);
-    // pass 2 evaluates 32 queued pairs at a time with every lane busy
+    // pass 1, 32 U entries at a time (U per lane, their loads in flight together): an FP32
+    // r^2 of the high parts against the outer cutoff plus a bound on their rounding queues
+    // the candidates (ballot compaction); pass 2 evaluates 32 queued pairs at a time with
+    // every lane busy.  The queue holds < 32 (U + 1) pairs.
     int nq = 0;
-    for (int base = 0;; base += 32) {
+    for (int base = 0;; base += 32 * U) {
       const bool more = base < n;
       if (more) {
-        const int m = base + lane + 1;
-        bool keep = false;
-        int j = 0;
-        if (m <= n) {
-          j = sp[m];
-          if (j >= 0) {
-            const float4 pj = A.xhs[j];
-            const float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
-            keep = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= pg.f_pre;
-          }
+        int jv[U];
+        float4 pv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int m = base + 32 * u + lane + 1;
+          jv[u] = m <= n ? sp[m] : -1;
         }
-        const unsigned bal = __ballot_sync(0xffffffffu, keep);
-        if (keep) pq[wq].j[nq + __popc(bal & ((1u << lane) - 1u))] = j;
-        nq += __popc(bal);
+#pragma unroll
+        for (int u = 0; u < U; ++u) pv[u] = jv[u] >= 0 ? A.xhs[jv[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const float ex = pi.x - pv[u].x, ey = pi.y - pv[u].y, ez = pi.z - pv[u].z;
+          const bool keep = jv[u] >= 0 && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= pg.f_pre;
+          const unsigned b = __ballot_sync(0xffffffffu, keep);
+          if (keep) pq[wq].j[nq + __popc(b & lt)] = jv[u];
+          nq += __popc(b);
+        }
         __syncwarp();
       }
-      if (nq >= 32 || (!more && nq > 0)) {
+      while (nq >= 32 || (!more && nq > 0)) {
         const int take = min(nq, 32);
         if (lane < take) {
           const int j = pq[wq].j[nq - take + lane];
@@ -958,7 +968,7 @@ __global__ void __launch_bounds__(PAIR_SORTED_NT, 4) k_pair_sorted(PairSortedArg
         nq -= take;
         __syncwarp();  // the taken slots are read before the next pass appends over them
       }
-      if (!more && nq == 0) break;
+      if (!more) break;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -1103,10 +1113,13 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   A.fixs = (unsigned long long*)g.fixs;
   A.cnt = &g.sc->npairs_list;
   A.sc = g.sc;
-  auto kern = mixed ? k_pair_sorted<1> : k_pair_sorted<0>;
-  static int occ[2] = {0, 0};
-  if (!occ[mixed]) GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[mixed], kern, PAIR_SORTED_NT, 0));
-  const int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, PAIR_SORTED_NT), occ[mixed] * g.nsm));
+  // four list entries per lane in the filter pass (measured at 262,144 ions, pair time
+  // per launch for 1 / 2 / 4 entries: double-float 1.46 / 1.37 / 1.34 ms, mixed 0.81 /
+  // 0.76 / 0.74 ms)
+  void (*kern)(PairSortedArgs, PairGeom) = mixed ? k_pair_sorted<1, 4> : k_pair_sorted<0, 4>;
+  int occ = 0;
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, PAIR_SORTED_NT, 0));
+  const int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, PAIR_SORTED_NT), occ * g.nsm));
   const int nbs = std::max(1, std::min(nblocks(g.mxatms, 256), 4 * g.nsm));  // stress blocks
   double* blk = gb_blkacc(nb * NACC_DF + nbs * 6 + nb2 * 8);
   double* blks = blk + (size_t)nb * NACC_DF;
