@@ -866,9 +866,9 @@ int gb_mts_features(float* x, int n, float* scales) {
 
 int gb_mlp_param_count(void) { return mlp_param_count(); }
 
-int gb_mts_ablation(int stale_only) {
-  if (stale_only != 0 && stale_only != 1) return GB_ERR_ARG;
-  mts_set_stale_only(stale_only == 1);
+int gb_mts_ablation(int no_network) {
+  if (no_network != 0 && no_network != 1) return GB_ERR_ARG;
+  mts_set_no_network(no_network == 1);
   return GB_OK;
 }
 

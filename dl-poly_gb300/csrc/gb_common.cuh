@@ -401,7 +401,7 @@ void mts_set_topology(int ntcons, const int32_t* listcon, const double* weight);
 void mts_setup();
 void mts_free();
 bool mts_active();
-void mts_set_stale_only(bool on);  // ablation: no network, inner steps reuse F(t0)
+void mts_set_no_network(bool on);  // ablation: inner steps use the coarse-grid force alone
 float* mts_rec_out();             // SPME per-atom reciprocal forces go here when active
 bool mts_step_needs_spme();
 void mts_after_full(double erc, double vrc, const double* strec);

@@ -4,23 +4,28 @@
 // evaluates SPME on every call (two_body.F90:298-302).  The plain SPME of
 // gb_spme.cu is both the teacher and the fallback.
 //
-// Cycle.  Full SPME runs at t0 and every k steps after it; on the k-1 inner
-// steps the reciprocal force of atom i is
-//     F_i(t) = F_i(t0) + [C_i(t) - C_i(t0)] + fs * R_i^T y_i,   y_i = MLP(x_i)
-// where C is the reciprocal force on a coarse FP32 grid (about half the points
-// per dimension, spline order 6) evaluated every step: its increment carries
-// the long-range change, which no local model can see, and the network learns
-// the remaining short-range correction.  The net force of the correction is
-// removed (as SPME removes its own); the reciprocal energy, virial and stress
-// of an inner step are those of t0 plus the coarse-grid increments.
+// Scheme: a time-reversible impulse multiple-time-step split (r-RESPA).  The
+// force is split into a fast part, evaluated every step,
+//     F_fast(x) = F_real(x) + S(x),   S_i(x) = C_i(x) + fs * R_i^T y_i(x),
+// and a slow part F_slow = F_SPME - S, applied as an impulse every k steps: the
+// force of a cycle-end step is F_fast + k F_slow (the velocity-Verlet half kicks
+// before and after that step each carry k dt/2 of it).  C is the reciprocal force
+// on a coarse FP32 grid (about two thirds of the points per dimension, spline order 6) and
+// y = MLP(x_i) the network's correction of the coarse grid's error.  Both depend
+// only on the current positions, so the inner steps integrate a fixed force field
+// (C is the exact gradient of the coarse-grid energy) and no correction is carried
+// over a cycle: the scheme is symmetric in time.  The net force of the network
+// correction is removed, as SPME removes its own.  The reciprocal energy, virial
+// and stress of an inner step are those of the last full step plus the coarse-grid
+// changes since then.
 // Inputs x_i (51):
-//   48 = 8 Gaussians g_k(r_ij) (centres 0.5..6 A, width 0.45 A, cosine cut at
-//        6 A) x local-frame components of the linear-response sums
-//          A_k = q_i sum_j q_j g_k(r_ij) u_ij          (3)
-//          B_k = q_i sum_j q_j g_k(r_ij) r^_ij (r^_ij . u_ij)   (3)
-//        with u_ij = d_j - d_i and d the displacement since t0 (A and B span
-//        the pair Hessian q_i q_j grad grad phi(r) . u of any radial kernel);
-//    3 = F_i(t0) in the local frame;
+//   48 = 8 Gaussians g_k(r_ij) (centres 0.5..6 A, width w = 0.45 A, cosine cut
+//        at 6 A) x local-frame components of the charge-weighted radial sums
+//          A_k  = q_i sum_j q_j g_k(r_ij) r^_ij                     (3)
+//          A'_k = q_i sum_j q_j g_k(r_ij) ((r_ij - mu_k) / w) r^_ij  (3)
+//        (the local charge environment, which fixes part of the coarse grid's
+//        interpolation error);
+//    3 = C_i(x) in the local frame;
 // each scaled by the inverse RMS of the first labelled sample.  The local frame
 // R_i of an atom of a 3-atom constrained molecule is that molecule's bisector
 // frame (origin = heaviest atom); other atoms use the lab frame.
@@ -30,14 +35,13 @@
 // persistent CTAs.  Training: forward + MSE + backward on CUDA cores with
 // BF16-rounded operands (weights, inputs, activations, activation gradients)
 // and FP32 accumulation, per-CTA gradient partials summed in a fixed order,
-// Adam on FP32 master weights.  Labels are R_i (F_i(t) - F_i(t0) - C_i(t) +
-// C_i(t0)) / fs from the SPME forces of the training steps (SPME every step
-// while training).  The judge: at every cycle end after training, the
-// prediction for that step is compared with SPME; RMS(pred - SPME) /
-// RMS(total force) > tol switches to plain SPME every step (and resumes
-// training) until a cycle end passes.  Each check also records the errors of
-// the same schedule without the network (coarse increment only) and of the
-// stale force F_i(t0), the ablations.
+// Adam on FP32 master weights.  Labels are R_i (F_SPME,i - C_i) / fs from the
+// steps that run SPME (every step while training).  The judge: at every cycle
+// end after training, S of that step is compared with SPME; RMS(S - SPME) /
+// RMS(total force) > tol switches to plain SPME every step (no impulses; training
+// resumes) until a cycle end passes.  Each check also records the error of the
+// coarse force alone (the network ablation) and of the reciprocal force of the
+// previous full step held unchanged (the stale-force ablation).
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -49,7 +53,7 @@
 namespace {
 
 constexpr int NIN = 51, KIN = 64, NH = 128, NOUT = 3, NOUTP = 16;
-constexpr int NRAD = 8;
+constexpr int NRAD = 8;  // 6 NRAD + 3 = NIN
 constexpr float RCUT_DESC = (float)MTS_RCUT_DESC, GAUSS_W = 0.45f, GAUSS_MU0 = 0.5f;
 constexpr int TILE_I = 256;            // atoms per inference tile (16 warps x 16 rows)
 constexpr int INFER_NT = TILE_I * 2;   // its threads: one warp per 16 rows
@@ -72,11 +76,10 @@ struct MtsDev {
   int gpart_tiles = 0, batch = 0;
   Net net;
   __nv_bfloat16* X = nullptr;  // inputs [n][KIN]
-  float* frec0 = nullptr;      // reciprocal force at t0 (3n)
-  float* frec = nullptr;       // reciprocal force now: SPME result or prediction (3n)
-  float* truth = nullptr;      // prediction of the judge (3n)
+  float* frec0 = nullptr;      // SPME reciprocal force of the last full step (3n)
+  float* frec = nullptr;       // reciprocal force now: SPME result, or S on an inner step (3n)
+  float* truth = nullptr;      // S at a full step, for the judge and the impulse (3n)
   float* fc = nullptr;         // coarse-grid reciprocal force now (3n)
-  float* fc0 = nullptr;        // coarse-grid reciprocal force at t0 (3n)
   int Kc[3] = {0, 0, 0}, pc = 6;
   double ec = 0.0, vc = 0.0, stc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};     // coarse now
   double ec0 = 0.0, vc0 = 0.0, stc0[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // coarse at t0
@@ -86,8 +89,6 @@ struct MtsDev {
   int *sown = nullptr, *sfill = nullptr;  // own (half-list) entries per atom, reverse-entry fill counters
   long long scap = 0, gen_seen = -1;
   float* target = nullptr;     // labels (3n)
-  double* x0 = nullptr;        // positions at t0 (3n)
-  float* disp = nullptr;       // displacement since t0 (3 per local atom and halo image)
   float* frame = nullptr;      // local frame rows e1,e2,e3 (9n)
   int* triple = nullptr;       // frame atoms (a,b,c) per atom, -1 = lab frame
   float* scal = nullptr;       // [0,NIN) input scales, [NIN] force scale
@@ -106,7 +107,7 @@ struct MtsDev {
 
 MtsDev M;
 std::vector<int> h_triple;  // host copy set at gb_init
-bool g_stale_only = false;  // ablation: inner steps reuse F(t0) with no network
+bool g_no_network = false;  // ablation: S = C, the coarse force alone
 
 inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
@@ -127,20 +128,13 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], 
 }
 
 // ------------------------------------------------------------ per-step inputs
-// displacement since t0 (minimum image: atoms may have been wrapped since t0)
-// and the local frame of every atom
-__global__ void k_mts_prep(int n, const DevScalars* sc, const int* __restrict__ src, const double* __restrict__ x,
-                           const double* __restrict__ y, const double* __restrict__ z, const double* __restrict__ x0,
-                           const int* __restrict__ tri, double cell, float* __restrict__ disp,
+// the local frame of every local atom
+__global__ void k_mts_prep(int n, const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ z, const int* __restrict__ tri, double cell,
                            float* __restrict__ frame) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= sc->nlast) return;
-  const int i = a < n ? a : src[a];  // a halo image moves with its source atom
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
   const float L = (float)cell, rL = (float)(1.0 / cell);
-  float d0 = (float)(x[i] - x0[3 * i]), d1 = (float)(y[i] - x0[3 * i + 1]), d2 = (float)(z[i] - x0[3 * i + 2]);
-  d0 -= L * rintf(d0 * rL); d1 -= L * rintf(d1 * rL); d2 -= L * rintf(d2 * rL);
-  disp[3 * a] = d0; disp[3 * a + 1] = d1; disp[3 * a + 2] = d2;
-  if (a >= n) return;
   float e[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   const int ta = tri[3 * i], b = tri[3 * i + 1], c = tri[3 * i + 2];
   if (ta >= 0) {
@@ -267,59 +261,52 @@ __global__ void __launch_bounds__(256) k_short_sort(int n, const int* __restrict
 // registers and are rotated into the atom's local frame at the end
 __global__ void __launch_bounds__(128) k_mts_desc(int n, const int* __restrict__ fstart, const int* __restrict__ fcount,
                                                   const int* __restrict__ flist, const float4* __restrict__ xf,
-                                                  const float* __restrict__ disp,
-                                                  const float* __restrict__ frame, const float* __restrict__ frec0,
+                                                  const float* __restrict__ frame, const float* __restrict__ fc,
                                                   const float* __restrict__ scal, __nv_bfloat16* __restrict__ X) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 pi = xf[i];
-  const float dix = disp[3 * i], diy = disp[3 * i + 1], diz = disp[3 * i + 2];
   float v[6 * NRAD];
 #pragma unroll
   for (int k = 0; k < 6 * NRAD; ++k) v[k] = 0.f;
   const float rc2 = RCUT_DESC * RCUT_DESC;
   const float dmu = (RCUT_DESC - GAUSS_MU0) / (float)(NRAD - 1), c2 = 1.0f / (2.0f * GAUSS_W * GAUSS_W);
+  const float rw = 1.0f / GAUSS_W;
   const float qi = pi.w;
   const int st = fstart[i], cnt = fcount[i];
-  // four entries at a time: their indices, then their positions and displacements,
-  // are loaded before any is used (independent loads in flight)
+  // four entries at a time: their indices, then their positions, are loaded before
+  // any is used (independent loads in flight)
   for (int m0 = 0; m0 < cnt; m0 += 4) {
     int jj[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) jj[u] = m0 + u < cnt ? flist[st + m0 + u] : i;
     float4 pp[4];
-    float dd[4][3];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      pp[u] = xf[jj[u]];
-      dd[u][0] = disp[3 * jj[u]]; dd[u][1] = disp[3 * jj[u] + 1]; dd[u][2] = disp[3 * jj[u] + 2];
-    }
+    for (int u = 0; u < 4; ++u) pp[u] = xf[jj[u]];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const float rx = pp[u].x - pi.x, ry = pp[u].y - pi.y, rz = pp[u].z - pi.z;
       const float r2 = rx * rx + ry * ry + rz * rz;
       if (!(r2 < rc2 && r2 > 0.f)) continue;  // the padding entries (j = i) have r2 = 0
-      const float ux = dd[u][0] - dix, uy = dd[u][1] - diy, uz = dd[u][2] - diz;
       const float rinv = rsqrtf(r2), r = r2 * rinv;
       const float wt = qi * pp[u].w * 0.5f * (1.0f + __cosf(3.14159265f * r * (1.0f / RCUT_DESC)));
       const float hx = rx * rinv, hy = ry * rinv, hz = rz * rinv;
-      const float pu = hx * ux + hy * uy + hz * uz;
-      const float bx = pu * hx, by = pu * hy, bz = pu * hz;
 #pragma unroll
       for (int k = 0; k < NRAD; ++k) {
         const float t = r - (GAUSS_MU0 + dmu * (float)k);
         const float gk = wt * __expf(-t * t * c2);
-        v[6 * k + 0] = fmaf(gk, ux, v[6 * k + 0]);
-        v[6 * k + 1] = fmaf(gk, uy, v[6 * k + 1]);
-        v[6 * k + 2] = fmaf(gk, uz, v[6 * k + 2]);
-        v[6 * k + 3] = fmaf(gk, bx, v[6 * k + 3]);
-        v[6 * k + 4] = fmaf(gk, by, v[6 * k + 4]);
-        v[6 * k + 5] = fmaf(gk, bz, v[6 * k + 5]);
+        const float hk = gk * t * rw;  // the first Hermite function of the same Gaussian
+        v[6 * k + 0] = fmaf(gk, hx, v[6 * k + 0]);
+        v[6 * k + 1] = fmaf(gk, hy, v[6 * k + 1]);
+        v[6 * k + 2] = fmaf(gk, hz, v[6 * k + 2]);
+        v[6 * k + 3] = fmaf(hk, hx, v[6 * k + 3]);
+        v[6 * k + 4] = fmaf(hk, hy, v[6 * k + 4]);
+        v[6 * k + 5] = fmaf(hk, hz, v[6 * k + 5]);
       }
     }
   }
-  // triple t = 2k holds A_k = sum g_k u, t = 2k + 1 holds B_k = sum g_k r^(r^.u); each
-  // goes out in the local frame
+  // triple 2k holds A_k, triple 2k + 1 holds A'_k; each goes out in the local frame,
+  // then C_i
   float e[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) e[k] = frame[9 * (size_t)i + k];
@@ -334,7 +321,7 @@ __global__ void __launch_bounds__(128) k_mts_desc(int n, const int* __restrict__
   }
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const float val = e[3 * c] * frec0[3 * i] + e[3 * c + 1] * frec0[3 * i + 1] + e[3 * c + 2] * frec0[3 * i + 2];
+    const float val = e[3 * c] * fc[3 * i] + e[3 * c + 1] * fc[3 * i + 1] + e[3 * c + 2] * fc[3 * i + 2];
     xo[6 * NRAD + c] = __float2bfloat16(val * scal[6 * NRAD + c]);
   }
   for (int c = NIN; c < KIN; ++c) xo[c] = __float2bfloat16(0.f);
@@ -387,9 +374,9 @@ __device__ __forceinline__ void mlp_layer(const __nv_bfloat16* in, int ldin, con
 }
 
 // persistent: each CTA stages the weights once and walks tiles of TILE_I = 256 atoms.
-// out = frec0 + fs * R^T y (lab frame)
+// out = base + fs * R^T y (lab frame)
 __global__ void __launch_bounds__(INFER_NT) k_mlp_infer(int n, const __nv_bfloat16* __restrict__ X, Net net,
-                                                   const float* __restrict__ frec0, const float* __restrict__ frame,
+                                                   const float* __restrict__ base, const float* __restrict__ frame,
                                                    const float* __restrict__ scal, float* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
@@ -431,7 +418,7 @@ __global__ void __launch_bounds__(INFER_NT) k_mlp_infer(int n, const __nv_bfloat
         const float* e = frame + 9 * (size_t)atom;
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-          out[3 * (size_t)atom + c] = frec0[3 * (size_t)atom + c] + e[c] * y0 + e[3 + c] * y1 + e[6 + c] * y2;
+          out[3 * (size_t)atom + c] = base[3 * (size_t)atom + c] + e[c] * y0 + e[3 + c] * y1 + e[6 + c] * y2;
       }
     }
   }
@@ -597,9 +584,8 @@ __global__ void k_publish(const float* __restrict__ w, Net net) {
   if (e < NOUTP) net.bias[2 * NH + e] = e < NOUT ? w[OFF_B3 + e] : 0.f;
 }
 
-// labels: R (frec - frec0 - fc + fc0) / fs
-__global__ void k_mts_target(int n, const float* __restrict__ frec, const float* __restrict__ frec0,
-                             const float* __restrict__ fc, const float* __restrict__ fc0,
+// labels: R (frec - fc) / fs, the coarse grid's error in the local frame
+__global__ void k_mts_target(int n, const float* __restrict__ frec, const float* __restrict__ fc,
                              const float* __restrict__ frame, const float* __restrict__ scal,
                              float* __restrict__ target) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -607,24 +593,24 @@ __global__ void k_mts_target(int n, const float* __restrict__ frec, const float*
   const float inv = 1.0f / scal[NIN];
   float d[3];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) d[c] = (frec[3 * i + c] - frec0[3 * i + c]) - (fc[3 * i + c] - fc0[3 * i + c]);
+  for (int c = 0; c < 3; ++c) d[c] = frec[3 * i + c] - fc[3 * i + c];
   const float* e = frame + 9 * (size_t)i;
 #pragma unroll
   for (int c = 0; c < 3; ++c) target[3 * i + c] = (e[3 * c] * d[0] + e[3 * c + 1] * d[1] + e[3 * c + 2] * d[2]) * inv;
 }
 
-// per-block squared errors against the SPME forces f of this step:
-// [network prediction pred + fc - fc0, coarse increment only f0 + fc - fc0, stale f0]
+// per-block squared errors against the SPME forces f of this step: [S with the mean
+// of its network correction (net[]/n) removed, the coarse force alone, the stale force f0]
 __global__ void k_err3(int n, const float* __restrict__ pred, const float* __restrict__ fc,
-                       const float* __restrict__ fc0, const float* __restrict__ f0, const float* __restrict__ f,
-                       double* blk) {
+                       const double* __restrict__ net, float rn, const float* __restrict__ f0,
+                       const float* __restrict__ f, double* blk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float v[3] = {0.f, 0.f, 0.f};
   if (i < n) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const float inc = fc[3 * i + k] - fc0[3 * i + k], t = f[3 * i + k];
-      const float a = pred[3 * i + k] + inc - t, b = f0[3 * i + k] + inc - t, c = f0[3 * i + k] - t;
+      const float t = f[3 * i + k];
+      const float a = pred[3 * i + k] - (float)net[k] * rn - t, b = fc[3 * i + k] - t, c = f0[3 * i + k] - t;
       v[0] = fmaf(a, a, v[0]);
       v[1] = fmaf(b, b, v[1]);
       v[2] = fmaf(c, c, v[2]);
@@ -653,41 +639,49 @@ __global__ void k_fsq(int n, const double* __restrict__ fx, const double* __rest
   block_reduce_store<1>(v, blk);
 }
 
-// per-block sum of the predicted increments (net force of the prediction)
-__global__ void k_net3(int n, const float* __restrict__ f, const float* __restrict__ f0, double* blk) {
+// per-block sum of the network corrections f - fc (net force of the correction)
+__global__ void k_net3(int n, const float* __restrict__ f, const float* __restrict__ fc, double* blk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float v[3] = {0.f, 0.f, 0.f};
   if (i < n) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) v[k] = f[3 * i + k] - f0[3 * i + k];
+    for (int k = 0; k < 3; ++k) v[k] = f[3 * i + k] - fc[3 * i + k];
   }
   block_reduce_store<3>(v, blk);
 }
 
-// inner step: f = pred + fc - fc0 with the mean of the network correction
-// (pred - f0) removed, added into the fixed-point forces
-__global__ void k_mts_apply(int n, float* __restrict__ f, const float* __restrict__ fc, const float* __restrict__ fc0,
-                            const double* __restrict__ net, float rn, unsigned long long* __restrict__ fixp) {
+// inner step: S = f with the mean of the network correction removed, added into the
+// fixed-point forces
+__global__ void k_mts_apply(int n, float* __restrict__ f, const double* __restrict__ net, float rn,
+                            unsigned long long* __restrict__ fixp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float m[3] = {(float)net[0] * rn, (float)net[1] * rn, (float)net[2] * rn};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float fv = f[3 * i + k] - m[k] + (fc[3 * i + k] - fc0[3 * i + k]);
+    const float fv = f[3 * i + k] - m[k];
     f[3 * i + k] = fv;
     atomicAdd(&fixp[3 * i + k], (unsigned long long)fix40(fv));
+  }
+}
+
+// cycle-end step: the SPME force is already in the fixed-point forces; add the rest of
+// the impulse, (k - 1) (F_SPME - S), S with the mean of its network correction removed
+__global__ void k_mts_impulse(int n, const float* __restrict__ frec, const float* __restrict__ pred,
+                              const double* __restrict__ net, float rn, float km1,
+                              unsigned long long* __restrict__ fixp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float sv = pred[3 * i + k] - (float)net[k] * rn;
+    atomicAdd(&fixp[3 * i + k], (unsigned long long)fix40(km1 * (frec[3 * i + k] - sv)));
   }
 }
 
 __global__ void k_copy_f(long long n, const float* __restrict__ a, float* __restrict__ b) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = a[i];
-}
-
-__global__ void k_save_x0(int n, const double* x, const double* y, const double* z, double* x0) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  x0[3 * i] = x[i]; x0[3 * i + 1] = y[i]; x0[3 * i + 2] = z[i];
 }
 
 __global__ void k_seq_idx(int nb, int offset, int n, int* idx) {
@@ -716,7 +710,7 @@ __global__ void k_feat_ms(int n, const __nv_bfloat16* __restrict__ X, float* __r
 
 constexpr size_t infer_smem = sizeof(InferSmem);
 constexpr size_t train_smem = sizeof(TrainSmem);
-static_assert(6 * NRAD + 3 == NIN, "input layout: 6 response sums per Gaussian + F(t0)");
+static_assert(6 * NRAD + 3 == NIN, "input layout: 6 radial sums per Gaussian + the coarse force");
 static_assert(sizeof(TrainSmem) <= 227 * 1024, "training tile exceeds shared memory");
 static_assert(sizeof(InferSmem) <= 227 * 1024, "inference tile exceeds shared memory");
 
@@ -752,10 +746,10 @@ void set_attrs() {
   dev_done = dev;
 }
 
-void launch_infer(int n, const __nv_bfloat16* X, const Net& net, const float* frec0, const float* frame,
+void launch_infer(int n, const __nv_bfloat16* X, const Net& net, const float* base, const float* frame,
                   const float* scal, float* out) {
   const int grid = std::max(1, std::min(g_infer_grid, nblocks(n, TILE_I)));
-  k_mlp_infer<<<grid, INFER_NT, infer_smem, g.stream>>>(n, X, net, frec0, frame, scal, out);
+  k_mlp_infer<<<grid, INFER_NT, infer_smem, g.stream>>>(n, X, net, base, frame, scal, out);
   GB_LAUNCHED();
 }
 
@@ -823,18 +817,16 @@ void mts_inputs() {
     mts_short_list();
     prof_end(P_SHORTLIST);
   }
-  k_mts_prep<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(n, g.sc, g.src, g.x, g.y, g.z, M.x0, M.triple, g.cell[0],
-                                                             M.disp, M.frame);
+  k_mts_prep<<<nblocks(n, 256), 256, 0, g.stream>>>(n, g.x, g.y, g.z, M.triple, g.cell[0], M.frame);
   GB_LAUNCHED();
-  k_mts_desc<<<nblocks(n, 128), 128, 0, g.stream>>>(n, M.sstart, M.scount, M.slist, g.xf,
-                                                                        M.disp, M.frame, M.frec0, M.scal, M.X);
+  k_mts_desc<<<nblocks(n, 128), 128, 0, g.stream>>>(n, M.sstart, M.scount, M.slist, g.xf, M.frame, M.fc, M.scal,
+                                                    M.X);
   GB_LAUNCHED();
   prof_end(P_MTS_DESC);
 }
 
 void mts_labels() {
-  k_mts_target<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, M.frec, M.frec0, M.fc, M.fc0, M.frame, M.scal,
-                                                             M.target);
+  k_mts_target<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, M.frec, M.fc, M.frame, M.scal, M.target);
   GB_LAUNCHED();
 }
 
@@ -888,12 +880,10 @@ void mts_train_step() {
   prof_end(P_MLP_TRAIN);
 }
 
+// a full step ends one cycle and starts the next: its SPME force and the coarse-grid
+// energy, virial and stress are the reference of the following inner steps
 void mts_begin_cycle() {
-  k_save_x0<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, g.x, g.y, g.z, M.x0);
-  GB_LAUNCHED();
   k_copy_f<<<nblocks(3LL * g.natms, 256), 256, 0, g.stream>>>(3LL * g.natms, M.frec, M.frec0);
-  GB_LAUNCHED();
-  k_copy_f<<<nblocks(3LL * g.natms, 256), 256, 0, g.stream>>>(3LL * g.natms, M.fc, M.fc0);
   GB_LAUNCHED();
   M.ec0 = M.ec; M.vc0 = M.vc;
   for (int k = 0; k < 9; ++k) M.stc0[k] = M.stc[k];
@@ -951,7 +941,7 @@ void mts_set_topology(int ntcons, const int32_t* listcon, const double* weight) 
 
 void mts_free() {
   void* ptrs[] = {M.master, M.m1, M.m2, M.grad, M.gpart, M.loss_part, M.X, M.frec0, M.frec, M.truth, M.target,
-                  M.fc, M.fc0, M.x0, M.disp, M.frame, M.triple, M.scal, M.red, M.idx, M.sstart, M.scount,
+                  M.fc, M.frame, M.triple, M.scal, M.red, M.idx, M.sstart, M.scount,
                   M.slist, M.stmp, M.sown, M.sfill};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -976,15 +966,15 @@ void mts_setup() {
   GB_CUDA(cudaMalloc(&M.loss_part, sizeof(float) * M.gpart_tiles));
   net_alloc(M.net);
   GB_CUDA(cudaMalloc(&M.X, sizeof(__nv_bfloat16) * KIN * (size_t)n));
-  for (float** p : {&M.frec0, &M.frec, &M.truth, &M.target, &M.fc, &M.fc0})
+  for (float** p : {&M.frec0, &M.frec, &M.truth, &M.target, &M.fc})
     GB_CUDA(cudaMalloc(p, sizeof(float) * 3 * (size_t)n));
-  GB_CUDA(cudaMalloc(&M.disp, sizeof(float) * 3 * (size_t)g.mxatms));  // local atoms and halo images
-  // coarse grid: about half the main grid's points per dimension, order 6
-  for (int d = 0; d < 3; ++d) M.Kc[d] = coarse_length((g.p.kmax[d] + 1) / 2);
+  // coarse grid: about two thirds of the main grid's points per dimension, order 6
+  // (measured against the FP64 oracle on the NaCl melts: half the points leave an rms
+  // force error of 7.5e-5 to 9.2e-5 of the total force, two thirds 2.5e-5 to 3.4e-5)
+  for (int d = 0; d < 3; ++d) M.Kc[d] = coarse_length((2 * g.p.kmax[d] + 2) / 3);
   M.pc = 6;
   spme_coarse_setup(M.Kc, M.pc);
   GB_CUDA(cudaMalloc(&M.frame, sizeof(float) * 9 * (size_t)n));
-  GB_CUDA(cudaMalloc(&M.x0, sizeof(double) * 3 * (size_t)n));
   GB_CUDA(cudaMalloc(&M.triple, sizeof(int) * 3 * (size_t)n));
   GB_CUDA(cudaMalloc(&M.scal, sizeof(float) * (NIN + 1)));
   GB_CUDA(cudaMalloc(&M.red, sizeof(double) * 8));
@@ -1006,7 +996,7 @@ void mts_setup() {
 
 bool mts_active() { return M.ready && g.mts_k > 1; }
 
-void mts_set_stale_only(bool on) { g_stale_only = on; }
+void mts_set_no_network(bool on) { g_no_network = on; }
 
 // SPME writes its per-atom reciprocal forces here when MTS is active
 float* mts_rec_out() { return mts_active() ? M.frec : nullptr; }
@@ -1022,8 +1012,9 @@ bool mts_step_needs_spme() {
   return training_now() || M.fallback || M.s + 1 >= g.mts_k;
 }
 
-// after a full force evaluation of an MD step (SPME ran, FP64 forces formed):
-// labels, the judge, training and the cycle bookkeeping
+// after a full force evaluation of an MD step (SPME ran and its force is in the
+// fixed-point sums): labels, the judge, the impulse of a cycle end, training and the
+// cycle bookkeeping
 void mts_after_full(double erc, double vrc, const double* strec) {
   const int n = g.natms;
   M.n_full++;
@@ -1038,18 +1029,22 @@ void mts_after_full(double erc, double vrc, const double* strec) {
   if (!M.scales_set) mts_set_scales();
   else mts_inputs();
   mts_labels();
-  if (cycle_end && (M.adam_t > 0 || g_stale_only)) {
-    // the judge: the network's prediction for this step against SPME
+  const bool trained = M.adam_t > 0 || g_no_network;
+  const int nb = nblocks(n, 256);
+  if (cycle_end && trained) {
+    // S of this step, as the inner steps form it, against SPME (the judge)
     prof_begin(P_MLP);
-    if (g_stale_only) {
-      k_copy_f<<<nblocks(3LL * n, 256), 256, 0, g.stream>>>(3LL * n, M.frec0, M.truth);
+    if (g_no_network) {
+      k_copy_f<<<nblocks(3LL * n, 256), 256, 0, g.stream>>>(3LL * n, M.fc, M.truth);
       GB_LAUNCHED();
     } else {
-      launch_infer(n, M.X, M.net, M.frec0, M.frame, M.scal, M.truth);
+      launch_infer(n, M.X, M.net, M.fc, M.frame, M.scal, M.truth);
     }
-    const int nb = nblocks(n, 256);
-    double* blk = gb_blkacc(nb * 4);
-    k_err3<<<nb, 256, 0, g.stream>>>(n, M.truth, M.fc, M.fc0, M.frec0, M.frec, blk);
+    double* blk = gb_blkacc(nb * 7);
+    k_net3<<<nb, 256, 0, g.stream>>>(n, M.truth, M.fc, blk + 4 * nb);
+    GB_LAUNCHED();
+    gb_reduce_blocks(blk + 4 * nb, nb, 3, M.red + 4);
+    k_err3<<<nb, 256, 0, g.stream>>>(n, M.truth, M.fc, M.red + 4, 1.0f / (float)n, M.frec0, M.frec, blk);
     GB_LAUNCHED();
     k_fsq<<<nb, 256, 0, g.stream>>>(n, g.fx, g.fy, g.fz, blk + 3 * nb);
     GB_LAUNCHED();
@@ -1070,8 +1065,15 @@ void mts_after_full(double erc, double vrc, const double* strec) {
       M.fallback = err > g.mts_tol;
       if (M.fallback && !was) M.n_fallback++;
     }
+    // the impulse: a passed cycle end carries k F_slow = k (F_SPME - S); F_SPME is in
+    // the forces already.  Training steps and fallback steps run plain SPME.
+    if (!training_now() && !M.fallback) {
+      k_mts_impulse<<<nb, 256, 0, g.stream>>>(n, M.frec, M.truth, M.red + 4, 1.0f / (float)n,
+                                              (float)(g.mts_k - 1), (unsigned long long*)g.fixp);
+      GB_LAUNCHED();
+    }
   }
-  if ((training_now() || M.fallback) && !g_stale_only) {
+  if ((training_now() || M.fallback) && !g_no_network) {
     mts_train_step();
     std::vector<float> lp(M.gpart_tiles);
     GB_CUDA(cudaMemcpyAsync(lp.data(), M.loss_part, sizeof(float) * lp.size(), cudaMemcpyDeviceToHost, g.stream));
@@ -1084,25 +1086,28 @@ void mts_after_full(double erc, double vrc, const double* strec) {
   else M.s = s_new;
 }
 
-// inner step: predicted reciprocal force into the fixed-point forces; the
-// reciprocal energy, virial and stress are those of t0 plus the coarse-grid
-// increments since t0
+// inner step: S = C + the network correction (its net force removed) into the
+// fixed-point forces; the reciprocal energy, virial and stress are those of the last
+// full step plus the coarse-grid changes since then
 void mts_inner(double* erc, double* vrc, double* stress9) {
   const int n = g.natms;
-  mts_inputs();
   prof_begin(P_MLP);
-  if (g_stale_only) {
-    k_copy_f<<<nblocks(3LL * n, 256), 256, 0, g.stream>>>(3LL * n, M.frec0, M.frec);
-    GB_LAUNCHED();
-  } else {
-    launch_infer(n, M.X, M.net, M.frec0, M.frame, M.scal, M.frec);
-  }
   const int nb = nblocks(n, 256);
-  double* blk = gb_blkacc(nb * 3);
-  k_net3<<<nb, 256, 0, g.stream>>>(n, M.frec, M.frec0, blk);
-  GB_LAUNCHED();
-  gb_reduce_blocks(blk, nb, 3, M.red);
-  k_mts_apply<<<nb, 256, 0, g.stream>>>(n, M.frec, M.fc, M.fc0, M.red, 1.0f / (float)n, (unsigned long long*)g.fixp);
+  if (g_no_network) {
+    k_copy_f<<<nblocks(3LL * n, 256), 256, 0, g.stream>>>(3LL * n, M.fc, M.frec);
+    GB_LAUNCHED();
+    GB_CUDA(cudaMemsetAsync(M.red, 0, 3 * sizeof(double), g.stream));
+  } else {
+    prof_end(P_MLP);
+    mts_inputs();
+    prof_begin(P_MLP);
+    launch_infer(n, M.X, M.net, M.fc, M.frame, M.scal, M.frec);
+    double* blk = gb_blkacc(nb * 3);
+    k_net3<<<nb, 256, 0, g.stream>>>(n, M.frec, M.fc, blk);
+    GB_LAUNCHED();
+    gb_reduce_blocks(blk, nb, 3, M.red);
+  }
+  k_mts_apply<<<nb, 256, 0, g.stream>>>(n, M.frec, M.red, 1.0f / (float)n, (unsigned long long*)g.fixp);
   GB_LAUNCHED();
   prof_end(P_MLP);
   *erc = M.erc0 + (M.ec - M.ec0);

@@ -315,8 +315,9 @@ class PathLib:
         if st != 0:
             raise PathError(st, self.prefix + "mts_config", self.strerror(st))
 
-    def mts_ablation(self, stale_only: bool):
-        st = self._opt("mts_ablation", c_int, [c_int])(1 if stale_only else 0)
+    def mts_ablation(self, no_network: bool):
+        """1: the inner steps use the coarse-grid force alone (no network)."""
+        st = self._opt("mts_ablation", c_int, [c_int])(1 if no_network else 0)
         if st != 0:
             raise PathError(st, self.prefix + "mts_ablation", self.strerror(st))
 

@@ -262,20 +262,22 @@ int gb_metal_rho(double* out);
 
 /* Learned multiple-time-step form (no counterpart in the reference: its
  * electro%nstfce key is parsed but SPME runs every step, two_body.F90:298-302).
- * Full SPME every k steps; on the inner steps a per-atom MLP predicts the
- * reciprocal-force increment since the last full step.  The first train_steps
- * MD steps run SPME every step and train the network online on its forces;
- * afterwards every k-th step compares the prediction with SPME and falls back
- * to SPME every step while RMS(pred - SPME) / RMS(total force) > tol.
- * Needs GB_MIXED; each call restarts from fresh weights.  k = 1 disables. */
+ * A time-reversible impulse split: every step integrates the real-space force
+ * plus S = (reciprocal force on a coarse grid) + (a per-atom MLP's correction of
+ * that grid's error); every k-th step runs SPME and its force carries the impulse
+ * k (F_SPME - S).  The first train_steps MD steps run SPME every step and train
+ * the network online on F_SPME - C; afterwards every k-th step compares S with
+ * SPME and runs plain SPME every step (no impulses) while
+ * RMS(S - SPME) / RMS(total force) > tol.  Needs GB_MIXED; each call restarts
+ * from fresh weights.  k = 1 disables. */
 int gb_mts_config(int k, double tol, int train_steps);
 
 /* Learned-MTS counters, up to n of: [0] last checked relative error,
  * [1] full steps, [2] inner steps, [3] fallback entries, [4] last training
  * loss, [5] optimiser steps, [6] largest checked error, [7] 1 while in
  * fallback, [8] checks made, [9] MD steps seen, [10] error of the same check
- * without the network (coarse-grid increment only), [11] error of the stale
- * reciprocal force, [12] coarse grid points along x. */
+ * without the network (coarse-grid force alone), [11] error of the reciprocal
+ * force of the previous full step held unchanged, [12] coarse grid points along x. */
 int gb_mts_stats(double* out, int n);
 
 /* Test hooks of the learned form (no reference counterpart).
@@ -287,9 +289,9 @@ int gb_mts_stats(double* out, int n);
  *   x[nb][51] with labels target[nb][3]: loss, grad[param_count], y[nb][3].
  * gb_mlp_infer_eval: the inference kernel's output y[nb][3] for x[nb][51]. */
 int gb_mts_features(float* x, int n, float* scales);
-/* Ablation switch for tests: 1 = the inner steps reuse the reciprocal force of
- * the last full step unchanged (the same MTS schedule without the network). */
-int gb_mts_ablation(int stale_only);
+/* Ablation switch for tests: 1 = S is the coarse-grid force alone (the same
+ * impulse schedule without the network, which is then not trained). */
+int gb_mts_ablation(int no_network);
 int gb_mlp_param_count(void);
 int gb_mlp_train_eval(int nb, const float* x, const float* target, const float* params, float* loss,
                       float* grad, float* y);

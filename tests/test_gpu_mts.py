@@ -3,8 +3,10 @@
 - the training kernel's forward, loss and gradients match the CPU oracle
   (oracle/mlp_oracle.py, FP64 with the same bfloat16 rounding points);
 - the tensor-core inference kernel matches the oracle forward;
-- an online-trained MTS run predicts the reciprocal force better than the same
-  MTS schedule without the network (stale reciprocal force), the ablation;
+- an online-trained MTS run (impulse split: coarse-grid force plus the network's
+  correction on the inner steps) matches the reciprocal force better than the
+  coarse-grid force alone and than the previous full step's force held fixed,
+  the ablations;
 - the judge falls back to plain SPME when the bound cannot be met.
 """
 import numpy as np
@@ -70,10 +72,10 @@ def test_inference_matches_oracle(ctx, nb):
     assert _rel(y, yo) <= 1e-3
 
 
-def _mts_run(lib, s, k, train, steps, stale):
+def _mts_run(lib, s, k, train, steps, no_network):
     lib.init(s, precision=1)
     lib.start()
-    lib.mts_ablation(stale)
+    lib.mts_ablation(no_network)
     lib.mts_config(k, 1.0, train)  # a loose bound: measure the error, never fall back
     st = lib.md_vv(steps)
     ms = lib.mts_stats()
@@ -82,12 +84,13 @@ def _mts_run(lib, s, k, train, steps, stale):
 
 
 def test_mts_ablation(gpu_lib):
-    """Every check measures the same step three ways against full SPME: the
-    network prediction, the coarse-grid increment without the network, and
-    the stale reciprocal force.  The network must beat both ablations."""
+    """Every check measures the same step three ways against full SPME: the inner
+    steps' force S (coarse grid plus the network's correction), the coarse-grid
+    force alone, and the previous full step's force held unchanged.  The network
+    must beat both ablations."""
     s = systems.nacl_melt(16)
     k, train, steps = 4, 400, 600
-    st, ms = _mts_run(gpu_lib, s, k, train, steps, stale=False)
+    st, ms = _mts_run(gpu_lib, s, k, train, steps, no_network=False)
     # schedule: SPME every step while training, then every k-th step
     full = [x.mts_full for x in st]
     assert all(full[:train])
@@ -98,7 +101,7 @@ def test_mts_ablation(gpu_lib):
     assert ms["err_no_network"] < 0.1 * ms["err_stale"], ms
     assert ms["last_err"] < ms["err_no_network"], ms
     # the same schedule with the network switched off
-    st0, ms0 = _mts_run(gpu_lib, s, k, train, steps, stale=True)
+    st0, ms0 = _mts_run(gpu_lib, s, k, train, steps, no_network=True)
     assert ms0["opt_steps"] == 0
     assert ms0["last_err"] == pytest.approx(ms0["err_no_network"], rel=1e-6)
 
