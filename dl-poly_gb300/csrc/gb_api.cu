@@ -93,6 +93,7 @@ void free_all() {
   spme_free();
   metal_free();
   if (g.hsc) cudaFreeHost(g.hsc);
+  if (g.ring) cudaFreeHost(g.ring);
   if (g.stream) {
     for (int k = 0; k < 8; ++k) cudaEventDestroy(g.ev[k]);
     cudaStreamDestroy(g.stream);
@@ -487,6 +488,8 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     {
       const char* e = getenv("GB_PAIR_SORTED");
       g.use_sorted = !(e && e[0] == '0');
+      const char* d = getenv("GB_MD_DEFER");  // 0: the MD loop reads every step's sums at the step
+      g.use_deferred = !(d && d[0] == '0');
     }
     thermo_setup(GB_NVE, 0.0, 0.0, 0.0, nullptr, 0.0);
     g.init = true;
@@ -757,9 +760,78 @@ int gb_metal_rho(double* out) {
   });
 }
 
+// The NVE loop without constraints, thermostat, metals or learned MTS: the host
+// waits only for the Verlet-list decision of each step (vnl_check); each step's
+// energy, virial and stress sums are copied to a pinned ring with the step's other
+// work and turned into gb_step_stats after the last step.  The per-region timings
+// of gb_last_timings are not taken on this path (the total is).
+static int md_run_deferred(int nsteps, gb_step_stats* stats) {
+  if (g.ring_cap < nsteps) {
+    if (g.ring) cudaFreeHost(g.ring);
+    g.ring = nullptr;
+    g.ring_cap = 0;
+    GB_CUDA(cudaMallocHost(&g.ring, sizeof(DevScalars) * (size_t)std::max(nsteps, 64)));
+    g.ring_cap = std::max(nsteps, 64);
+  }
+  std::vector<int32_t> rebuilt(nsteps, 0);
+  GB_CUDA(cudaEventRecord(g.ev[5], g.stream));
+  g.defer_scalars = true;
+  for (int s = 0; s < nsteps; ++s) {
+    GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
+    ++g.nstep;
+    int it = 0;
+    integ_vv(1, nullptr, nullptr, &it, nullptr, nullptr);
+    int32_t upd = 0;
+    int st = do_refresh(&upd);
+    if (st) { g.defer_scalars = false; return st; }
+    rebuilt[s] = upd;
+    if (upd) {
+      st = list_build();
+      if (st) { g.defer_scalars = false; return st; }
+    }
+    compute_forces(nullptr, nullptr, true, true, true, nullptr);
+    integ_vv(2, nullptr, nullptr, &it, nullptr, nullptr);
+    GB_CUDA(cudaMemcpyAsync(&g.ring[s], g.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, g.stream));
+  }
+  g.defer_scalars = false;
+  GB_CUDA(cudaEventRecord(g.ev[6], g.stream));
+  GB_CUDA(cudaEventSynchronize(g.ev[6]));
+  float span = 0.f;
+  cudaEventElapsedTime(&span, g.ev[5], g.ev[6]);
+  for (int k = 0; k < 5; ++k) g.last_ms[k] = 0.0;
+  g.last_ms[4] = span;
+  g.last_ms[5] = span;
+  if (stats) {
+    for (int s = 0; s < nsteps; ++s) {
+      gb_step_stats S;
+      std::memset(&S, 0, sizeof(S));
+      const DevScalars* h = &g.ring[s];
+      double strec[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, e6[6] = {0, 0, 0, 0, 0, 0};
+      if (g.has_coul) spme_scalars(h, &S.engcpe_rc, &S.vircpe_rc, strec);
+      if (g.has_coul || g.has_vdw) pair_scalars(h, e6, strec);
+      S.engcpe_rl = e6[0]; S.vircpe_rl = e6[1]; S.engcpe_ex = e6[2]; S.vircpe_ex = e6[3];
+      S.engvdw = e6[4]; S.virvdw = e6[5];
+      for (int k = 0; k < 9; ++k) S.stress[k] = strec[k];
+      kin_scalars(h, S.strkin, &S.engke);
+      S.list_rebuilt = rebuilt[s];
+      S.mts_full = 1;
+      stats[s] = S;
+    }
+  }
+  return (int)GB_OK;
+}
+
 int gb_md_run(int nsteps, gb_step_stats* stats) {
   return guarded([&]() {
     if (nsteps < 0) return (int)GB_ERR_ARG;
+    if (nsteps > 0 && g.use_deferred && g.ntcons == 0 && g.ens == GB_NVE && !g.has_metal && !mts_active()) {
+      try {
+        return md_run_deferred(nsteps, stats);
+      } catch (int e) {
+        g.defer_scalars = false;
+        throw;
+      }
+    }
     double tl[5] = {0, 0, 0, 0, 0};
     GB_CUDA(cudaEventRecord(g.ev[5], g.stream));
     for (int s = 0; s < nsteps; ++s) {

@@ -148,6 +148,13 @@ struct Dev {
   int n_tile_over = 0, tile_max_staged = 0;   // from the last list build
   bool spos_valid = false;     // the last list pairs every halo entry with its backward copy
   bool use_sorted = true;      // sorted-position pair kernels (GB_PAIR_SORTED=0: the atom-index kernels)
+  // NVE MD loop without constraints, thermostat, metals or learned MTS: the energy,
+  // virial and stress sums of each step are copied to a pinned ring and read after the
+  // last step, so the host waits only for the Verlet-list decision of each step
+  bool defer_scalars = false;
+  bool use_deferred = true;    // GB_MD_DEFER=0 keeps the per-step read-back
+  DevScalars* ring = nullptr;  // pinned, ring_cap steps
+  int ring_cap = 0;
   float4* xhs = nullptr;       // per sorted position: FP32 high parts (x, y, z, q)
   float4* xls = nullptr;       // per sorted position: remainders (x, y, z, q) of the FP64 values
   unsigned char* tys = nullptr;  // per sorted position: atom type
@@ -374,6 +381,10 @@ bool spme_coarse_ready();
 // floats, net force removed); forces of the context are not touched
 void spme_coarse_forces(double* eng_rc, double* vir_rc, double* stress9, float* rec);
 void integ_vv(int stage, double* strkin, double* engke, int* iters, double* vircon, double* strcon);
+// host-side results from a copy of the device scalars (the MD loop's deferred read-back)
+void spme_scalars(const DevScalars* h, double* eng_rc, double* vir_rc, double* stress9);
+void pair_scalars(const DevScalars* h, double* eng6, double* stress9);
+void kin_scalars(const DevScalars* h, double* strkin, double* engke);
 void integ_con_tags();            // constraints_tags: old bond vectors from the current positions
 void integ_shake(int* iters, double* vircon, double* strcon);  // apply_shake (throws GB_ERR_SHAKE)
 void integ_rattle_launch();       // apply_rattle, kit = 1 (status bit ST_RATTLE_FAIL)

@@ -787,14 +787,20 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
       k_kinstress<<<nb, 256, 0, st>>>(n, g.weight, g.lfrzn, g.vx, g.vy, g.vz, blk);
       GB_LAUNCHED();
       gb_reduce_blocks(blk, nb, 6, &g.sc->acc[A_STRKIN]);
+      if (g.defer_scalars) return;  // the MD loop reads the sums after its last step
       gb_sync_scalars();
-      const double* s = &g.hsc->acc[A_STRKIN];
-      double sk[9] = {s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]};
-      if (strkin) for (int k = 0; k < 9; ++k) strkin[k] = sk[k];
-      if (engke) *engke = 0.5 * (sk[0] + sk[4] + sk[8]);
+      kin_scalars(g.hsc, strkin, engke);
     }
     if (iters && g.ntcons > 0) *iters = g.hsc->rattle_iters;
     if (g.ntcons > 0 && (g.hsc->status & ST_RATTLE_FAIL)) throw (int)GB_ERR_RATTLE;
     if (g.hsc->status & ST_RNG) throw (int)GB_ERR_RNG;
   }
+}
+
+// kinetic stress (symmetric 3x3) and kinetic energy from the device sums
+void kin_scalars(const DevScalars* h, double* strkin, double* engke) {
+  const double* s = &h->acc[A_STRKIN];
+  double sk[9] = {s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]};
+  if (strkin) for (int k = 0; k < 9; ++k) strkin[k] = sk[k];
+  if (engke) *engke = 0.5 * (sk[0] + sk[4] + sk[8]);
 }

@@ -1181,8 +1181,6 @@ void pair_forces(double* eng6, double* stress9) {
   pg.ntypes = g.p.ntypes;
   cudaStream_t st = g.stream;
   const int T = 256;
-  double res[NACC];
-  double ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const int nb2 = nblocks(g.natms, 128);
   GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
   const bool sorted = g.spos_valid && g.use_sorted && !(g.precision == GB_FP64 && g.fp64_native);
@@ -1290,9 +1288,17 @@ void pair_forces(double* eng6, double* stress9) {
       gb_reduce_blocks(blk2, nb2, 8, &g.sc->acc[A_EXCL]);
     }
   }
+  if (g.defer_scalars) return;  // the MD loop reads the sums after its last step
   gb_sync_scalars();
-  for (int k = 0; k < NACC; ++k) res[k] = g.hsc->acc[A_PAIR + k];
-  if (g.lbook) for (int k = 0; k < 8; ++k) ex[k] = g.hsc->acc[A_EXCL + k];
+  pair_scalars(g.hsc, eng6, stress9);
+}
+
+// engrl, virrl, engex, virex, engvdw, virvdw and the pair stress from the device sums
+void pair_scalars(const DevScalars* h, double* eng6, double* stress9) {
+  double res[NACC];
+  double ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < NACC; ++k) res[k] = h->acc[A_PAIR + k];
+  if (g.lbook) for (int k = 0; k < 8; ++k) ex[k] = h->acc[A_EXCL + k];
   eng6[0] = res[2]; eng6[1] = res[3];
   eng6[2] = ex[0]; eng6[3] = ex[1];
   eng6[4] = res[0]; eng6[5] = res[1];

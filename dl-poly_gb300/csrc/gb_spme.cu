@@ -1132,8 +1132,18 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   }
   GB_LAUNCHED();
   prof_end(pid(P_SPME_GATHER));
+  if (g.defer_scalars && !coarse) return;  // the MD loop reads the sums after its last step
   gb_sync_scalars();
-  const double* A = g.hsc->acc;
+  spme_scalars(g.hsc, eng_rc, vir_rc, stress9);
+}
+
+}  // namespace
+
+// reciprocal energy (with the self-interaction), virial and stress from the device sums
+void spme_scalars(const DevScalars* h, double* eng_rc, double* vir_rc, double* stress9) {
+  const double pi = 3.14159265358979323846264338327950288;
+  const double scale = pi * std::sqrt(pi) * std::pow(g.p.alpha, 1 - 3) * (0.5 / g.volm) * g.scaling;
+  const double* A = h->acc;
   double eng = A[A_GATHER] * scale;
   double s6[6];
   for (int k = 0; k < 6; ++k) s6[k] = A[A_SPME_STR + k] * scale;
@@ -1143,8 +1153,6 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   for (int k = 0; k < 9; ++k) stress9[k] += stt[k];
   *vir_rc = -(stt[0] + stt[4] + stt[8]);
 }
-
-}  // namespace
 
 void spme_setup() { grid_setup(S_main, g.p.kmax, g.p.nsplines, true, BPREF); }
 

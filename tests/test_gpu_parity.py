@@ -345,3 +345,28 @@ def test_sorted_pair_kernels_match_atom_index_kernels(gpu_lib, monkeypatch, name
             assert abs(b[0][k] - a[0][k]) <= tol * max(abs(a[0][k]), 1.0), (mode, k)
         assert np.abs(b[1] - a[1]).max() <= tol * np.abs(a[1]).max()
     assert runs["small_cap"][3][6] > 0  # the list build's second launch ran
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_deferred_step_scalars_match_per_step_readback(gpu_lib, monkeypatch, precision):
+    """The NVE loop that reads each step's energy, virial and stress sums after its last
+    step gives the same per-step scalars and the same trajectory as the loop that reads
+    them at every step."""
+    s = systems.nacl_melt(16)
+    out = []
+    for env in ("0", "1"):
+        monkeypatch.setenv("GB_MD_DEFER", env)
+        gpu_lib.init(s, precision=precision)
+        gpu_lib.start()
+        st = gpu_lib.md_vv(30)
+        out.append((st, gpu_lib.download()))
+    monkeypatch.delenv("GB_MD_DEFER", raising=False)
+    (sa, a), (sb, b) = out
+    assert any(x.list_rebuilt for x in sa)
+    assert [x.list_rebuilt for x in sa] == [x.list_rebuilt for x in sb]
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    for x, y in zip(sa, sb):
+        for f in ("engcpe_rc", "vircpe_rc", "engcpe_rl", "vircpe_rl", "engvdw", "virvdw", "engke"):
+            assert getattr(x, f) == getattr(y, f), f
+        assert list(x.stress) == list(y.stress) and list(x.strkin) == list(y.strkin)
