@@ -80,7 +80,7 @@ void dalloc(T** p, size_t n) {
 }
 
 void free_all() {
-  void* ptrs[] = {g.x, g.y, g.z, g.xf, g.xlo, g.fx, g.fy, g.fz, g.fixp, g.vx, g.vy, g.vz, g.chge, g.weight, g.ltype, g.ltg,
+  void* ptrs[] = {g.x, g.y, g.z, g.xf, g.xlo, g.fx, g.fy, g.fz, g.fixp, g.vx, g.vy, g.vz, g.hdw, g.chge, g.weight, g.ltype, g.ltg,
                   g.lfrzn, g.ixyz, g.src, g.shcode, g.xbg, g.ybg, g.zbg, g.ox, g.oy, g.oz, g.which_cell,
                   g.cell_count, g.cell_start, g.cell_fill, g.at_list, g.sorted_pos, g.xs, g.xsf, g.list, g.blk,
                   g.list_excl, g.erfc_coef, g.erfc_coef_f, g.vdw_coef, g.vdw_coef_f,
@@ -411,6 +411,7 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     g.natms = natms;
     g.mxatms = std::max(prm->mxatms, natms);
     if (prm->precision < GB_FP64 || prm->precision > GB_FP64_NATIVE) return GB_ERR_ARG;
+    if (!(prm->tstep > 0.0)) return GB_ERR_ARG;
     g.precision = prm->precision == GB_MIXED ? GB_MIXED : GB_FP64;
     g.fp64_native = prm->precision == GB_FP64_NATIVE;
     std::memcpy(g.cell, prm->cell, sizeof(g.cell));
@@ -457,6 +458,13 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     GB_CUDA(cudaMemcpy(g.ltype, ltype, sizeof(int) * natms, cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(g.chge, chge, sizeof(double) * natms, cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(g.weight, weight, sizeof(double) * natms, cudaMemcpyHostToDevice));
+    {
+      std::vector<double> hdw(natms);
+      const double hstep = 0.5 * prm->tstep;
+      for (int i = 0; i < natms; ++i) hdw[i] = weight[i] > 1.0e-6 ? hstep / weight[i] : 0.0;
+      dalloc(&g.hdw, natms);
+      GB_CUDA(cudaMemcpy(g.hdw, hdw.data(), sizeof(double) * natms, cudaMemcpyHostToDevice));
+    }
     if (lfrzn) GB_CUDA(cudaMemcpy(g.lfrzn, lfrzn, sizeof(int) * natms, cudaMemcpyHostToDevice));
     const int ldx = prm->max_exclude + 1;
     dalloc(&g.list_excl, (size_t)ldx * natms);

@@ -106,6 +106,7 @@ struct Dev {
   double *fx = nullptr, *fy = nullptr, *fz = nullptr;  // natms, FP64 forces
   long long* fixp = nullptr;                        // 3*natms fixed-point forces (mixed)
   double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+  double* hdw = nullptr;                            // natms: (tstep/2) / weight, 0 where weight <= 1e-6
   double *chge = nullptr, *weight = nullptr;        // mxatms
   int *ltype = nullptr, *ltg = nullptr, *lfrzn = nullptr;  // mxatms
   int *ixyz = nullptr, *src = nullptr;              // mxatms

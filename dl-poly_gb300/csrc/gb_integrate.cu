@@ -33,12 +33,17 @@ __device__ __forceinline__ double image1(double d, double c, double a) {
   return sub_rn(d, mul_rn(c, round(mul_rn(a, d))));
 }
 
-__global__ void k_vv1(int n, double hstep, double tstep, const double* w, const double* fx, const double* fy,
-                      const double* fz, double* vx, double* vy, double* vz, double* x, double* y, double* z) {
+// Velocity Verlet stages (nve.F90:127-217).  hdw[i] = (tstep/2) / weight(i), formed once
+// with the same correctly rounded division the reference performs each step, and 0 for
+// an atom with weight <= 1e-6 (which the stages skip): the stages then read one array
+// instead of dividing on the FP64 unit.
+__global__ void k_vv1(int n, const double* __restrict__ hdw, double tstep, const double* __restrict__ fx,
+                      const double* __restrict__ fy, const double* __restrict__ fz, double* vx, double* vy, double* vz,
+                      double* x, double* y, double* z) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  if (w[i] > 1.0e-6) {
-    double tmp = hstep / w[i];
+  const double tmp = hdw[i];
+  if (tmp > 0.0) {
     vx[i] = vx[i] + tmp * fx[i];
     vy[i] = vy[i] + tmp * fy[i];
     vz[i] = vz[i] + tmp * fz[i];
@@ -48,12 +53,13 @@ __global__ void k_vv1(int n, double hstep, double tstep, const double* w, const 
   }
 }
 
-__global__ void k_vv2(int n, double hstep, const double* w, const double* fx, const double* fy, const double* fz,
-                      double* vx, double* vy, double* vz) {
+__global__ void k_vv2(int n, const double* __restrict__ hdw, const double* __restrict__ fx,
+                      const double* __restrict__ fy, const double* __restrict__ fz, double* vx, double* vy,
+                      double* vz) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  if (w[i] > 1.0e-6) {
-    double tmp = hstep / w[i];
+  const double tmp = hdw[i];
+  if (tmp > 0.0) {
     vx[i] = vx[i] + tmp * fx[i];
     vy[i] = vy[i] + tmp * fy[i];
     vz[i] = vz[i] + tmp * fz[i];
@@ -769,15 +775,14 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
   if (stage == 1) {
     prof_begin(P_VV);
     if (!thermo_vv1(hstep, tstep)) {
-      k_vv1<<<nblocks(n, 256), 256, 0, st>>>(n, hstep, tstep, g.weight, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz, g.x, g.y,
-                                             g.z);
+      k_vv1<<<nblocks(n, 256), 256, 0, st>>>(n, g.hdw, tstep, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz, g.x, g.y, g.z);
       GB_LAUNCHED();
     }
     prof_end(P_VV);
     integ_shake(iters, vircon, strcon);
   } else {
     prof_begin(P_VV);
-    k_vv2<<<nblocks(n, 256), 256, 0, st>>>(n, hstep, g.weight, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz);
+    k_vv2<<<nblocks(n, 256), 256, 0, st>>>(n, g.hdw, g.fx, g.fy, g.fz, g.vx, g.vy, g.vz);
     GB_LAUNCHED();
     prof_end(P_VV);
     integ_rattle_launch();
