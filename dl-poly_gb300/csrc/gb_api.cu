@@ -935,8 +935,10 @@ int64_t gb_kernel_launches(void) { return g.launches; }
 
 int gb_mts_stats(double* out, int n) {
   if (!out || n < 0) return GB_ERR_ARG;
-  mts_stats(out, n);
-  return GB_OK;
+  return guarded([&]() {
+    mts_stats(out, n);
+    return (int)GB_OK;
+  });
 }
 
 int gb_mts_features(float* x, int n, float* scales) {

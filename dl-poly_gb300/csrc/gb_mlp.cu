@@ -97,7 +97,7 @@ struct MtsDev {
   int adam_t = 0;
   int s = 0;                   // steps since t0
   int step = 0;                // MD steps since configuration
-  bool have_t0 = false, scales_set = false, fallback = false;
+  bool have_t0 = false, scales_set = false, fallback = false, loss_pending = false;
   long long n_full = 0, n_inner = 0, n_fallback = 0, n_judged = 0;
   double last_err = -1.0, last_loss = -1.0, err_max = -1.0;
   int batch_offset = 0;
@@ -1075,12 +1075,7 @@ void mts_after_full(double erc, double vrc, const double* strec) {
   }
   if ((training_now() || M.fallback) && !g_no_network) {
     mts_train_step();
-    std::vector<float> lp(M.gpart_tiles);
-    GB_CUDA(cudaMemcpyAsync(lp.data(), M.loss_part, sizeof(float) * lp.size(), cudaMemcpyDeviceToHost, g.stream));
-    GB_CUDA(cudaStreamSynchronize(g.stream));
-    double l = 0.0;
-    for (float v : lp) l += v;
-    M.last_loss = l;
+    M.loss_pending = true;  // read when the counters are asked for, not every training step
   }
   if (cycle_end) mts_begin_cycle();
   else M.s = s_new;
@@ -1118,6 +1113,15 @@ void mts_inner(double* erc, double* vrc, double* stress9) {
 }
 
 void mts_stats(double* out, int nv) {
+  if (M.loss_pending && M.loss_part) {
+    std::vector<float> lp(M.gpart_tiles);
+    GB_CUDA(cudaMemcpyAsync(lp.data(), M.loss_part, sizeof(float) * lp.size(), cudaMemcpyDeviceToHost, g.stream));
+    GB_CUDA(cudaStreamSynchronize(g.stream));
+    double l = 0.0;
+    for (float v : lp) l += v;
+    M.last_loss = l;
+    M.loss_pending = false;
+  }
   const double v[13] = {M.last_err, (double)M.n_full, (double)M.n_inner, (double)M.n_fallback, M.last_loss,
                         (double)M.adam_t, M.err_max, M.fallback ? 1.0 : 0.0, (double)M.n_judged, (double)M.step,
                         M.err_coarse, M.err_stale, (double)M.Kc[0]};

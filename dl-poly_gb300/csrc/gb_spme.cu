@@ -705,6 +705,9 @@ struct SpmeGrid {
 };
 
 SpmeGrid S_main, S_coarse;
+// FP32 grids: the tile spread (no atomics, atoms in index order per brick) unless
+// GB_SPREAD_FIX=1 selects the int64 fixed-point spread with shared-memory atomics
+bool g_spread_fix = false;
 
 // Brick edge: a divisor of K of at least p-1 (a brick's atoms reach at most the
 // next brick).  Larger bricks cut the halo overlap (B+p-1)^3 / B^3 of the tiles
@@ -1006,7 +1009,10 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   GB_LAUNCHED();
 
   scan_exclusive(S.brick_count, S.brick_start, S.nbricks + 1);
-  if (F64) {  // the FP64 spread adds a brick's atoms in ascending index order
+  // the tile spread adds a brick's atoms in ascending index order (deterministic sums);
+  // the fixed-point spread of the mixed form (GB_SPREAD_FIX=1) does not depend on it
+  const bool tile_spread = F64 || !g_spread_fix;
+  if (tile_spread) {
     int* tmp = gb_scan_scratch(n + 1);
     k_brick_scatter<<<nblocks(n, 256), 256, 0, st>>>(n, S.brick_of, S.brick_start, S.brick_fill, tmp);
     GB_LAUNCHED();
@@ -1026,7 +1032,7 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
     const int red_nt = std::min(256, (K1 + 31) / 32 * 32);  // halo reduction: x in the block, y and z in the grid
     const dim3 red_grid((unsigned)nblocks(K1, red_nt), (unsigned)K2, (unsigned)K3);
     prof_begin(pid(P_SPME_SPREAD));
-    if (F64) {
+    if (tile_spread) {
       auto spread = p == 8 ? k_spme_spread_tile<T, 8> : k_spme_spread_tile<T, 0>;
       spread<<<S.nbricks, SPREAD_NT, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge, ext);
       GB_LAUNCHED();
@@ -1154,7 +1160,11 @@ void spme_scalars(const DevScalars* h, double* eng_rc, double* vir_rc, double* s
   *vir_rc = -(stt[0] + stt[4] + stt[8]);
 }
 
-void spme_setup() { grid_setup(S_main, g.p.kmax, g.p.nsplines, true, BPREF); }
+void spme_setup() {
+  const char* e = getenv("GB_SPREAD_FIX");
+  g_spread_fix = e && e[0] == '1';
+  grid_setup(S_main, g.p.kmax, g.p.nsplines, true, BPREF);
+}
 
 void spme_free() {
   grid_free(S_main);
