@@ -272,6 +272,7 @@ __global__ void __launch_bounds__(128) k_mts_desc(int n, const int* __restrict__
   const float rc2 = RCUT_DESC * RCUT_DESC;
   const float dmu = (RCUT_DESC - GAUSS_MU0) / (float)(NRAD - 1), c2 = 1.0f / (2.0f * GAUSS_W * GAUSS_W);
   const float rw = 1.0f / GAUSS_W;
+  const float gam = __expf(-2.0f * dmu * dmu * c2);
   const float qi = pi.w;
   const int st = fstart[i], cnt = fcount[i];
   // four entries at a time: their indices, then their positions, are loaded before
@@ -291,10 +292,14 @@ __global__ void __launch_bounds__(128) k_mts_desc(int n, const int* __restrict__
       const float rinv = rsqrtf(r2), r = r2 * rinv;
       const float wt = qi * pp[u].w * 0.5f * (1.0f + __cosf(3.14159265f * r * (1.0f / RCUT_DESC)));
       const float hx = rx * rinv, hy = ry * rinv, hz = rz * rinv;
+      // g_k = exp(-(r - mu_k)^2 c2) by recurrence over the equally spaced centres:
+      // g_{k+1} = g_k rho_k, rho_{k+1} = rho_k gam (two exponentials per pair, not NRAD)
+      const float t0 = r - GAUSS_MU0;
+      float gk = wt * __expf(-t0 * t0 * c2);
+      float rho = __expf((2.0f * t0 * dmu - dmu * dmu) * c2);
 #pragma unroll
       for (int k = 0; k < NRAD; ++k) {
         const float t = r - (GAUSS_MU0 + dmu * (float)k);
-        const float gk = wt * __expf(-t * t * c2);
         const float hk = gk * t * rw;  // the first Hermite function of the same Gaussian
         v[6 * k + 0] = fmaf(gk, hx, v[6 * k + 0]);
         v[6 * k + 1] = fmaf(gk, hy, v[6 * k + 1]);
@@ -302,6 +307,8 @@ __global__ void __launch_bounds__(128) k_mts_desc(int n, const int* __restrict__
         v[6 * k + 3] = fmaf(hk, hx, v[6 * k + 3]);
         v[6 * k + 4] = fmaf(hk, hy, v[6 * k + 4]);
         v[6 * k + 5] = fmaf(hk, hz, v[6 * k + 5]);
+        gk *= rho;
+        rho *= gam;
       }
     }
   }

@@ -839,6 +839,9 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64, int bpref) {
     raise_smem(k_spme_spread_tile<dfr, 8>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(dfr)));
     raise_smem(k_spme_spread_tile<dfr, 0>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(dfr)));
     raise_smem(k_spme_spread_tile<float, 8>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
+    raise_smem(k_spme_spread_tile<float, 6>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
+    raise_smem(k_spme_spread_tile<double, 6>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(double)));
+    raise_smem(k_spme_spread_tile<dfr, 6>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(dfr)));
     raise_smem(k_spme_spread_tile<float, 0>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
     raise_smem(k_spme_spread_fix<8>, (int)(tsize * sizeof(long long)));
     raise_smem(k_spme_spread_fix<6>, (int)(tsize * sizeof(long long)));
@@ -1033,7 +1036,7 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
     const dim3 red_grid((unsigned)nblocks(K1, red_nt), (unsigned)K2, (unsigned)K3);
     prof_begin(pid(P_SPME_SPREAD));
     if (tile_spread) {
-      auto spread = p == 8 ? k_spme_spread_tile<T, 8> : k_spme_spread_tile<T, 0>;
+      auto spread = p == 8 ? k_spme_spread_tile<T, 8> : (p == 6 ? k_spme_spread_tile<T, 6> : k_spme_spread_tile<T, 0>);
       spread<<<S.nbricks, SPREAD_NT, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge, ext);
       GB_LAUNCHED();
       k_spme_tile_reduce<T><<<red_grid, red_nt, 0, st>>>(S.sg, ext, Q);
