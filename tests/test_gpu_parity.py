@@ -370,3 +370,32 @@ def test_deferred_step_scalars_match_per_step_readback(gpu_lib, monkeypatch, pre
         for f in ("engcpe_rc", "vircpe_rc", "engcpe_rl", "vircpe_rl", "engvdw", "virvdw", "engke"):
             assert getattr(x, f) == getattr(y, f), f
         assert list(x.stress) == list(y.stress) and list(x.strkin) == list(y.strkin)
+
+
+@pytest.mark.parametrize("name", ["nacl_4096", "water_5184"])
+def test_fp32_tile_spread_matches_fixed_point_spread(gpu_lib, oracle_lib, monkeypatch, name):
+    """FP32 grids (mixed form) spread by the atomic-free tile kernel, each brick's atoms in
+    atom-index order, against the fixed-point atomic spread (GB_SPREAD_FIX=1): both within
+    the mixed form's bound of the FP64 oracle, within FP32 rounding of each other, and the
+    tile spread gives the same bits on a second call."""
+    s = CASES[name]()
+    oracle_lib.init(s)
+    oracle_lib.relocate()
+    er, _, _ = oracle_lib.ewald_spme_forces()
+    b = oracle_lib.download()
+    runs = {}
+    for mode, env in (("fix", "1"), ("tile", "0")):
+        monkeypatch.setenv("GB_SPREAD_FIX", env)
+        gpu_lib.init(s, precision=1)
+        gpu_lib.relocate()
+        runs[mode] = [(gpu_lib.ewald_spme_forces(), gpu_lib.download()) for _ in range(2)]
+    monkeypatch.delenv("GB_SPREAD_FIX", raising=False)
+    for mode, r in runs.items():
+        (ed, _, _), a = r[0]
+        assert force_rms_rel(a, b) <= 1e-5, mode
+        assert ed == pytest.approx(er, rel=1e-6), mode
+    (t0, a0), (t1, a1) = runs["tile"]
+    assert t0[0] == t1[0]
+    for k in ("fx", "fy", "fz"):
+        assert np.array_equal(a0[k], a1[k]), k
+    assert force_rms_rel(runs["fix"][0][1], a0) <= 2e-6
