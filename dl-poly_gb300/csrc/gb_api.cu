@@ -69,6 +69,58 @@ __global__ void k_nonfinite(int n, const double* a, const double* b, const doubl
   if (!isfinite(a[i]) || !isfinite(b[i]) || !isfinite(c[i])) atomicOr(status, ST_NONFINITE);
 }
 
+// State transfer between the device arrays and caller buffers in pinned, mapped host
+// memory: each thread moves element i of every array, so one launch replaces one copy per
+// array.  Positions are checked for non-finite values on the way in; any thread that finds
+// one stores ST_NONFINITE to the flag (the host clears it before the launch).
+struct HostArrays {
+  const double* h[9];
+  double* d[9];
+  int n;
+};
+
+__global__ void k_upload_state(HostArrays a, int narr, int* flag) {
+  const int stride = gridDim.x * blockDim.x;
+  int bad = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      if (k < narr) {
+        const double v = a.h[k][i];
+        a.d[k][i] = v;
+        if (k < 3 && !isfinite(v)) bad = 1;
+      }
+    }
+  }
+  if (bad) *flag = ST_NONFINITE;
+}
+
+__global__ void k_download_state(HostArrays a) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      if (a.d[k]) const_cast<double*>(a.h[k])[i] = a.d[k][i];
+  }
+}
+
+// The device-side address of a caller buffer of n doubles when the whole buffer lies in
+// pinned host memory mapped into the device's address space, else nullptr.
+static double* mapped_span(const double* p, size_t n) {
+  if (!p || n == 0) return nullptr;
+  cudaPointerAttributes a0, a1;
+  if (cudaPointerGetAttributes(&a0, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  if (a0.type != cudaMemoryTypeHost || !a0.devicePointer) return nullptr;
+  const double* last = p + (n - 1);
+  if (cudaPointerGetAttributes(&a1, last) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  if (a1.type != cudaMemoryTypeHost || !a1.devicePointer) return nullptr;
+  double* d0 = static_cast<double*>(a0.devicePointer);
+  if (static_cast<double*>(a1.devicePointer) != d0 + (n - 1)) return nullptr;
+  return d0;
+}
+
+static int copy_grid(int n) { return std::max(1, std::min(nblocks(n, 256), 152 * 8)); }
+
 std::vector<double> h_tmp;
 int* d_scratch = nullptr;
 size_t d_scratch_n = 0;
@@ -94,6 +146,7 @@ void free_all() {
   metal_free();
   if (g.hsc) cudaFreeHost(g.hsc);
   if (g.ring) cudaFreeHost(g.ring);
+  if (g.hflag) cudaFreeHost(g.hflag);
   if (g.stream) {
     for (int k = 0; k < 8; ++k) cudaEventDestroy(g.ev[k]);
     cudaStreamDestroy(g.stream);
@@ -450,6 +503,9 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     dalloc(&g.sc, 1);
     GB_CUDA(cudaMallocHost(&g.hsc, sizeof(DevScalars)));
     std::memset(g.hsc, 0, sizeof(DevScalars));
+    GB_CUDA(cudaHostAlloc(&g.hflag, sizeof(int), cudaHostAllocMapped));
+    GB_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&g.dflag), g.hflag, 0));
+    *g.hflag = 0;
     // topology
     std::vector<int> ltg(natms);
     g.megfrz = 0;
@@ -498,6 +554,8 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
       g.use_sorted = !(e && e[0] == '0');
       const char* d = getenv("GB_MD_DEFER");  // 0: the MD loop reads every step's sums at the step
       g.use_deferred = !(d && d[0] == '0');
+      const char* m = getenv("GB_MAPPED_COPY");  // 0: state transfers by cudaMemcpyAsync only
+      g.use_mapped = !(m && m[0] == '0');
     }
     thermo_setup(GB_NVE, 0.0, 0.0, 0.0, nullptr, 0.0);
     g.init = true;
@@ -514,20 +572,32 @@ int gb_upload_state(const double* x, const double* y, const double* z, const dou
   return guarded([&]() {
     const size_t b = sizeof(double) * g.natms;
     if (!x || !y || !z) return (int)GB_ERR_ARG;
-    GB_CUDA(cudaMemcpyAsync(g.x, x, b, cudaMemcpyHostToDevice, g.stream));
-    GB_CUDA(cudaMemcpyAsync(g.y, y, b, cudaMemcpyHostToDevice, g.stream));
-    GB_CUDA(cudaMemcpyAsync(g.z, z, b, cudaMemcpyHostToDevice, g.stream));
-    if (vx && vy && vz) {
-      GB_CUDA(cudaMemcpyAsync(g.vx, vx, b, cudaMemcpyHostToDevice, g.stream));
-      GB_CUDA(cudaMemcpyAsync(g.vy, vy, b, cudaMemcpyHostToDevice, g.stream));
-      GB_CUDA(cudaMemcpyAsync(g.vz, vz, b, cudaMemcpyHostToDevice, g.stream));
+    const bool with_v = vx && vy && vz;
+    const int narr = with_v ? 6 : 3;
+    const double* src[6] = {x, y, z, vx, vy, vz};
+    double* dst[6] = {g.x, g.y, g.z, g.vx, g.vy, g.vz};
+    HostArrays a{};
+    a.n = g.natms;
+    bool mapped = g.use_mapped && g.natms > 0;
+    for (int k = 0; k < narr && mapped; ++k) {
+      a.h[k] = mapped_span(src[k], g.natms);
+      a.d[k] = dst[k];
+      mapped = a.h[k] != nullptr;
+    }
+    *g.hflag = 0;
+    if (mapped) {
+      k_upload_state<<<copy_grid(g.natms), 256, 0, g.stream>>>(a, narr, g.dflag);
+      GB_LAUNCHED();
+    } else {
+      for (int k = 0; k < narr; ++k)
+        GB_CUDA(cudaMemcpyAsync(dst[k], src[k], b, cudaMemcpyHostToDevice, g.stream));
+      if (g.natms > 0) {
+        k_nonfinite<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, g.x, g.y, g.z, g.dflag);
+        GB_LAUNCHED();
+      }
     }
     GB_CUDA(cudaStreamSynchronize(g.stream));
-    GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
-    k_nonfinite<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, g.x, g.y, g.z, &g.sc->status);
-    GB_LAUNCHED();
-    gb_sync_scalars();
-    if (g.hsc->status & ST_NONFINITE) return (int)GB_ERR_NONFINITE;
+    if (*static_cast<volatile int*>(g.hflag) & ST_NONFINITE) return (int)GB_ERR_NONFINITE;
     return (int)GB_OK;
   });
 }
@@ -556,15 +626,24 @@ int gb_download_state(double* x, double* y, double* z, double* vx, double* vy, d
                       double* fz) {
   return guarded([&]() {
     const size_t b = sizeof(double) * g.natms;
-    if (x) GB_CUDA(cudaMemcpyAsync(x, g.x, b, cudaMemcpyDeviceToHost, g.stream));
-    if (y) GB_CUDA(cudaMemcpyAsync(y, g.y, b, cudaMemcpyDeviceToHost, g.stream));
-    if (z) GB_CUDA(cudaMemcpyAsync(z, g.z, b, cudaMemcpyDeviceToHost, g.stream));
-    if (vx) GB_CUDA(cudaMemcpyAsync(vx, g.vx, b, cudaMemcpyDeviceToHost, g.stream));
-    if (vy) GB_CUDA(cudaMemcpyAsync(vy, g.vy, b, cudaMemcpyDeviceToHost, g.stream));
-    if (vz) GB_CUDA(cudaMemcpyAsync(vz, g.vz, b, cudaMemcpyDeviceToHost, g.stream));
-    if (fx) GB_CUDA(cudaMemcpyAsync(fx, g.fx, b, cudaMemcpyDeviceToHost, g.stream));
-    if (fy) GB_CUDA(cudaMemcpyAsync(fy, g.fy, b, cudaMemcpyDeviceToHost, g.stream));
-    if (fz) GB_CUDA(cudaMemcpyAsync(fz, g.fz, b, cudaMemcpyDeviceToHost, g.stream));
+    double* dst[9] = {x, y, z, vx, vy, vz, fx, fy, fz};
+    double* src[9] = {g.x, g.y, g.z, g.vx, g.vy, g.vz, g.fx, g.fy, g.fz};
+    HostArrays a{};
+    a.n = g.natms;
+    bool mapped = g.use_mapped && g.natms > 0;
+    for (int k = 0; k < 9 && mapped; ++k) {
+      if (!dst[k]) continue;
+      a.h[k] = mapped_span(dst[k], g.natms);
+      a.d[k] = src[k];
+      mapped = a.h[k] != nullptr;
+    }
+    if (mapped) {
+      k_download_state<<<copy_grid(g.natms), 256, 0, g.stream>>>(a);
+      GB_LAUNCHED();
+    } else {
+      for (int k = 0; k < 9; ++k)
+        if (dst[k]) GB_CUDA(cudaMemcpyAsync(dst[k], src[k], b, cudaMemcpyDeviceToHost, g.stream));
+    }
     GB_CUDA(cudaStreamSynchronize(g.stream));
     return (int)GB_OK;
   });

@@ -156,6 +156,11 @@ struct Dev {
   bool use_deferred = true;    // GB_MD_DEFER=0 keeps the per-step read-back
   DevScalars* ring = nullptr;  // pinned, ring_cap steps
   int ring_cap = 0;
+  // host state transfers: pinned and mapped caller buffers are read and written by one
+  // kernel each way (GB_MAPPED_COPY=0: one cudaMemcpyAsync per array)
+  bool use_mapped = true;
+  int* hflag = nullptr;        // pinned, mapped: the upload kernel's non-finite flag
+  int* dflag = nullptr;        // its device-side address
   float4* xhs = nullptr;       // per sorted position: FP32 high parts (x, y, z, q)
   float4* xls = nullptr;       // per sorted position: remainders (x, y, z, q) of the FP64 values
   unsigned char* tys = nullptr;  // per sorted position: atom type

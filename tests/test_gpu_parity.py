@@ -399,3 +399,45 @@ def test_fp32_tile_spread_matches_fixed_point_spread(gpu_lib, oracle_lib, monkey
     for k in ("fx", "fy", "fz"):
         assert np.array_equal(a0[k], a1[k]), k
     assert force_rms_rel(runs["fix"][0][1], a0) <= 2e-6
+
+
+def _pinned_rows(n, rows):
+    """`rows` float64 arrays of n values, views into one pinned host allocation."""
+    torch = pytest.importorskip("torch")
+    block = torch.zeros((rows, n), dtype=torch.float64).pin_memory().numpy()
+    return [block[k] for k in range(rows)], block
+
+
+def test_state_transfer_mapped_and_copy_paths(gpu_lib, monkeypatch):
+    """gb_upload_state / gb_download_state with pinned caller buffers (one transfer kernel
+    each way, reading and writing the mapped host memory) against the cudaMemcpyAsync path
+    (GB_MAPPED_COPY=0) and against pageable buffers: the same bits after 5 MD steps, and a
+    non-finite position rejected on both paths."""
+    s = systems.nacl_melt(16)
+    n = s.natms
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("GB_MAPPED_COPY", mode)
+        gpu_lib.init(s)
+        src, _ = _pinned_rows(n, 6)
+        for k, v in zip(("x", "y", "z", "vx", "vy", "vz"), src):
+            v[:] = getattr(s, k)
+        gpu_lib.upload(*src)
+        gpu_lib.start()
+        gpu_lib.md_vv(5)
+        rows, _ = _pinned_rows(n, 9)
+        pinned = gpu_lib.download(out=dict(zip(gpu_lib.STATE_KEYS, rows)))
+        pageable = gpu_lib.download()
+        for k in gpu_lib.STATE_KEYS:
+            assert np.array_equal(pinned[k], pageable[k]), (mode, k)
+        out[mode] = {k: v.copy() for k, v in pinned.items()}
+        bad, _ = _pinned_rows(n, 3)
+        for k, v in zip(("x", "y", "z"), bad):
+            v[:] = getattr(s, k)
+        bad[2][n - 1] = np.inf
+        with pytest.raises(Exception) as e:
+            gpu_lib.upload(*bad)
+        assert getattr(e.value, "code", None) == -5, mode
+    monkeypatch.delenv("GB_MAPPED_COPY", raising=False)
+    for k in gpu_lib.STATE_KEYS:
+        assert np.array_equal(out["1"][k], out["0"][k]), k
