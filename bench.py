@@ -307,9 +307,10 @@ def measure(lib, L, s, form, args, dist, device, steps, detail):
         lib.md_vv(train)
         t_train = time.perf_counter() - t0
     lib.md_vv(max(3, args.warmup))
-    # ---- timed region: `runs` times K resident MD steps (kernels timed with CUDA events);
-    # the line reports the median run, the kernel table sums all runs
-    L.gb_profile(1)
+    # ---- timed region: `runs` times K resident MD steps; the line reports the median run.
+    # SPME runs on the library's second stream while the pair kernel runs, so per-kernel
+    # times are taken afterwards in a one-stream pass of K more steps (gb_set_overlap(0)),
+    # where every kernel has the whole GPU: the kernel table and the roofline use that pass.
     clocks = Clocks(device) if detail else None
     spans, walls, stats_all, launches = [], [], [], 0
     for _ in range(max(1, args.runs)):
@@ -330,11 +331,18 @@ def measure(lib, L, s, form, args, dist, device, steps, detail):
     order = sorted(range(len(spans)), key=lambda r: spans[r])
     med = order[len(order) // 2]
     tmax = spans[med]
+    L.gb_set_overlap(0)
+    L.gb_profile(1)
+    lib.md_vv(steps)
+    tm = (ctypes.c_double * 8)()
+    L.gb_last_timings(tm, 8)
+    one_stream_ms = tm[5] / steps
     names = ctypes.create_string_buffer(32 * 32)
     ms = (ctypes.c_double * 32)()
     nl = (ctypes.c_int64 * 32)()
     nk = L.gb_profile_read(names, ms, nl, 32)
     L.gb_profile(0)
+    L.gb_set_overlap(1)
     prof = {}
     for j in range(nk):
         nm = names.raw[32 * j:32 * (j + 1)].split(b"\0")[0].decode()
@@ -348,6 +356,7 @@ def measure(lib, L, s, form, args, dist, device, steps, detail):
            "ns_per_day": (steps / tmax) * DT_PS * 86400 / 1000, "steps": steps,
            "runs": len(spans), "ms_per_step_runs": [t * 1e3 / steps for t in spans],
            "spread_rel": (max(spans) - min(spans)) / tmax,
+           "one_stream_ms_per_step": one_stream_ms,
            "list_rebuilds": sum(x.list_rebuilt for x in stats) / len(spans)}
     if precision == 1 and k == 1:
         out["force_err_rms"], out["force_err_max"] = force_error(lib, L)
@@ -359,7 +368,7 @@ def measure(lib, L, s, form, args, dist, device, steps, detail):
                       "err_without_network": m["err_no_network"], "err_stale_force": m["err_stale"],
                       "fallback_entries": int(m["n_fallback"]), "in_fallback": bool(m["in_fallback"])}
     if prof:
-        out["kernels_ms_per_step"] = {nm: v[0] / (len(spans) * steps) for nm, v in prof.items()}
+        out["kernels_ms_per_step"] = {nm: v[0] / steps for nm, v in prof.items()}
     return out, dict(stats=stats, prof=prof, P=(P_list, P_rc), launches=launches, clk=clk, wall=sum(walls),
                      tmax=tmax, runs=len(spans))
 
@@ -449,6 +458,7 @@ def run_gb(args, dist):
     lib = gb.load()
     L = lib.lib
     L.gb_profile.argtypes = [ctypes.c_int]
+    L.gb_set_overlap.argtypes = [ctypes.c_int]
     L.gb_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
                                   ctypes.c_int]
     L.gb_pair_counts.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]
@@ -607,6 +617,10 @@ def run_gb(args, dist):
         "clocks": clk,
         "roofline": roof,
         "kernels": kernels,
+        "kernels_timing": "CUDA events per phase in a one-stream pass of the same number of steps after the timed "
+                          "runs (SPME and the pair kernel on one stream: gb_set_overlap(0)); the timed runs overlap "
+                          "SPME on a second stream with the pair kernel",
+        "one_stream_ms_per_step": head["one_stream_ms_per_step"],
         "pairs": {"list_entries": P_list, "within_rc": P_rc},
         "wall_s_timed": w1 - w0,
         "cpu_baseline": cpu,

@@ -124,6 +124,8 @@ static int copy_grid(int n) { return std::max(1, std::min(nblocks(n, 256), 152 *
 std::vector<double> h_tmp;
 int* d_scratch = nullptr;
 size_t d_scratch_n = 0;
+int* d_scratch_s = nullptr;  // the side stream's
+size_t d_scratch_s_n = 0;
 
 template <typename T>
 void dalloc(T** p, size_t n) {
@@ -138,7 +140,8 @@ void free_all() {
                   g.list_excl, g.erfc_coef, g.erfc_coef_f, g.vdw_coef, g.vdw_coef_f,
                   g.vdw_kind, g.vdw_eps, g.vdw_sig, g.erfc_df, g.vdw_df, g.qdf, g.spos, g.xhs, g.xls, g.tys, g.fixs,
                   g.tile_rows, g.tile_info, g.tile_over, g.blkacc, g.con_i, g.con_j, g.con_d0, g.dxx, g.dyy,
-                  g.dzz, g.dxt, g.dyt, g.dzt, g.dt2, g.gam, g.listot, g.acon_start, g.acon_list, g.sc, d_scratch};
+                  g.dzz, g.dxt, g.dyt, g.dzt, g.dt2, g.gam, g.listot, g.acon_start, g.acon_list, g.sc, d_scratch,
+                  d_scratch_s, g.blkacc_s};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   mts_free();
@@ -147,12 +150,17 @@ void free_all() {
   if (g.hsc) cudaFreeHost(g.hsc);
   if (g.ring) cudaFreeHost(g.ring);
   if (g.hflag) cudaFreeHost(g.hflag);
-  if (g.stream) {
+  if (g.main_stream) {
     for (int k = 0; k < 8; ++k) cudaEventDestroy(g.ev[k]);
-    cudaStreamDestroy(g.stream);
+    cudaEventDestroy(g.ev_fork);
+    cudaEventDestroy(g.ev_join);
+    cudaStreamDestroy(g.main_stream);
+    cudaStreamDestroy(g.side_stream);
   }
   d_scratch = nullptr;
   d_scratch_n = 0;
+  d_scratch_s = nullptr;
+  d_scratch_s_n = 0;
   g = Dev();
 }
 
@@ -279,10 +287,49 @@ int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real, bo
     list_pos_sorted();  // the same per sorted position, for the sorted-position pair kernels
   const bool mts = md_step && do_spme && mts_active();
   const bool full = mts ? mts_step_needs_spme() : (do_spme && g.has_coul);
-  if (full) spme_forces(&erc, &vrc, strec);
-  else if (mts) mts_inner(&erc, &vrc, strec);
-  for (int k = 0; k < 9; ++k) st[k] += strec[k];
-  if (do_real && (g.has_coul || g.has_vdw)) pair_forces(e6, st);
+  // SPME on the side stream while the pair kernel runs (the plain FP64 form keeps one
+  // stream: its kernels are bound by the FP64 unit both sides share)
+  const bool overlap = g.use_overlap && full && !mts && do_real && !g.has_metal &&
+                       !(g.precision == GB_FP64 && g.fp64_native);
+  if (overlap) {
+    const bool deferred = g.defer_scalars;
+    g.defer_scalars = true;  // both sides leave their sums on the device; read once below
+    GB_CUDA(cudaEventRecord(g.ev_fork, g.main_stream));
+    GB_CUDA(cudaStreamWaitEvent(g.side_stream, g.ev_fork, 0));
+    struct SideGuard {
+      bool defer;
+      ~SideGuard() {
+        g.stream = g.main_stream;
+        g.side = false;
+        g.defer_scalars = defer;
+        if (g.join_pending) {  // left by an error between the fork and the join
+          cudaStreamWaitEvent(g.main_stream, g.ev_join, 0);
+          g.join_pending = false;
+        }
+      }
+    } guard{deferred};
+    g.stream = g.side_stream;
+    g.side = true;
+    spme_forces(&erc, &vrc, strec);
+    GB_CUDA(cudaEventRecord(g.ev_join, g.side_stream));
+    g.stream = g.main_stream;
+    g.side = false;
+    g.join_pending = true;
+    pair_forces(e6, st);  // waits for the side stream before it folds the pair forces
+    side_join();
+    g.defer_scalars = deferred;
+    if (!deferred) {
+      gb_sync_scalars();
+      spme_scalars(g.hsc, &erc, &vrc, strec);
+      for (int k = 0; k < 9; ++k) st[k] += strec[k];
+      pair_scalars(g.hsc, e6, st);
+    }
+  } else {
+    if (full) spme_forces(&erc, &vrc, strec);
+    else if (mts) mts_inner(&erc, &vrc, strec);
+    for (int k = 0; k < 9; ++k) st[k] += strec[k];
+    if (do_real && (g.has_coul || g.has_vdw)) pair_forces(e6, st);
+  }
   for (int k = 0; k < 4; ++k) g.metal_e4[k] = 0.0;
   if (do_real && g.has_metal) metal_forces(g.metal_e4, st);  // metal_ld_compute + metal_forces
   if (g.precision == GB_MIXED) integ_forces_to_fp64();
@@ -410,15 +457,23 @@ __global__ void k_dfma_peak(int iters, double a, double b, double* out) {
 }
 
 double* gb_blkacc(int n) {
-  if (n > g.blkacc_n) {
-    if (g.blkacc) {
-      GB_CUDA(cudaStreamSynchronize(g.stream));
-      cudaFree(g.blkacc);
+  double*& buf = g.side ? g.blkacc_s : g.blkacc;
+  int& cap = g.side ? g.blkacc_s_n : g.blkacc_n;
+  if (n > cap) {
+    if (buf) {
+      GB_CUDA(cudaDeviceSynchronize());
+      cudaFree(buf);
     }
-    g.blkacc_n = n + 4096;
-    GB_CUDA(cudaMalloc(&g.blkacc, sizeof(double) * g.blkacc_n));
+    cap = n + 4096;
+    GB_CUDA(cudaMalloc(&buf, sizeof(double) * cap));
   }
-  return g.blkacc;
+  return buf;
+}
+
+void side_join() {
+  if (!g.join_pending) return;
+  GB_CUDA(cudaStreamWaitEvent(g.stream, g.ev_join, 0));
+  g.join_pending = false;
 }
 
 void gb_reduce_blocks(const double* blk, int nblocks_, int nv, double* out_dev) {
@@ -427,15 +482,17 @@ void gb_reduce_blocks(const double* blk, int nblocks_, int nv, double* out_dev) 
 }
 
 int* gb_scan_scratch(int n) {
-  if ((size_t)n > d_scratch_n) {
-    if (d_scratch) {
-      GB_CUDA(cudaStreamSynchronize(g.stream));
-      cudaFree(d_scratch);
+  int*& buf = g.side ? d_scratch_s : d_scratch;
+  size_t& cap = g.side ? d_scratch_s_n : d_scratch_n;
+  if ((size_t)n > cap) {
+    if (buf) {
+      GB_CUDA(cudaDeviceSynchronize());
+      cudaFree(buf);
     }
-    d_scratch_n = (size_t)n + 4096;
-    GB_CUDA(cudaMalloc(&d_scratch, sizeof(int) * d_scratch_n));
+    cap = (size_t)n + 4096;
+    GB_CUDA(cudaMalloc(&buf, sizeof(int) * cap));
   }
-  return d_scratch;
+  return buf;
 }
 
 void scan_exclusive(const int* in, int* out, int n) {
@@ -477,7 +534,15 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     if (!ortho || !g.cubic) { free_all(); return GB_ERR_ARG; }  // cubic cells (imcon 1) only
     g.rcutx = prm->rcut + prm->rpad;
     if (g.rcutx >= std::min(g.celprp[6], std::min(g.celprp[7], g.celprp[8])) / 2.0) { free_all(); return GB_ERR_CUTOFF_CELL; }
-    GB_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    {
+      int lo = 0, hi = 0;
+      GB_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      GB_CUDA(cudaStreamCreateWithPriority(&g.main_stream, cudaStreamNonBlocking, lo));
+      GB_CUDA(cudaStreamCreateWithPriority(&g.side_stream, cudaStreamNonBlocking, hi));
+      g.stream = g.main_stream;
+      GB_CUDA(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
+      GB_CUDA(cudaEventCreateWithFlags(&g.ev_join, cudaEventDisableTiming));
+    }
     for (int k = 0; k < 8; ++k) GB_CUDA(cudaEventCreate(&g.ev[k]));
     const int mx = g.mxatms;
     dalloc(&g.x, mx); dalloc(&g.y, mx); dalloc(&g.z, mx);
@@ -556,6 +621,8 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
       g.use_deferred = !(d && d[0] == '0');
       const char* m = getenv("GB_MAPPED_COPY");  // 0: state transfers by cudaMemcpyAsync only
       g.use_mapped = !(m && m[0] == '0');
+      const char* o = getenv("GB_OVERLAP");  // 0: SPME and the pair kernel on one stream
+      g.use_overlap = !(o && o[0] == '0');
     }
     thermo_setup(GB_NVE, 0.0, 0.0, 0.0, nullptr, 0.0);
     g.init = true;
@@ -1051,6 +1118,13 @@ int gb_profile(int enable) {
     g.ev_used = 0;
     for (int k = 0; k < P_NPROF; ++k) { g.prof_ms[k] = 0.0; g.prof_n[k] = 0; }
     g.prof_on = enable != 0;
+    return (int)GB_OK;
+  });
+}
+
+int gb_set_overlap(int enable) {
+  return guarded([&]() {
+    g.use_overlap = enable != 0;
     return (int)GB_OK;
   });
 }

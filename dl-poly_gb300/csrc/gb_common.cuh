@@ -96,6 +96,13 @@ struct Dev {
   bool cubic = true;
   int precision = GB_FP64;
   cudaStream_t stream = nullptr;
+  // The reciprocal-space sum runs on a second stream of higher priority while the pair
+  // kernel runs on the first (GB_OVERLAP=0: both on the first).  During the SPME launches
+  // `stream` is the side stream and `side` is set; the first stream waits for the side
+  // stream before the pair forces are folded into the force arrays.
+  cudaStream_t main_stream = nullptr, side_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool side = false, join_pending = false, use_overlap = true;
   int nsm = 0;
   int64_t launches = 0;
 
@@ -192,6 +199,8 @@ struct Dev {
   // SPME grids live in gb_spme.cu (SpmeGrid); shared scratch here
   double* blkacc = nullptr;    // per-block partial accumulators
   int blkacc_n = 0;
+  double* blkacc_s = nullptr;  // the same for launches on the side stream
+  int blkacc_s_n = 0;
 
   // constraints
   int ntcons = 0;
@@ -366,6 +375,7 @@ void gb_sync_scalars();           // copy device scalars to the pinned mirror (s
 double* gb_blkacc(int n);         // per-block accumulator scratch with n doubles
 void gb_reduce_blocks(const double* blk, int nblocks, int nv, double* out_dev);  // sums into out_dev[0..nv)
 int* gb_scan_scratch(int n);
+void side_join();                 // the first stream waits for the side stream (no-op without a fork)
 
 // module entry points (host)
 int list_relocate_and_halo();     // pbcshift + halo + vnl_set_check (gb_list.cu)

@@ -1117,6 +1117,10 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   // per launch for 1 / 2 / 4 entries: double-float 1.46 / 1.37 / 1.34 ms, mixed 0.81 /
   // 0.76 / 0.74 ms)
   void (*kern)(PairSortedArgs, PairGeom) = mixed ? k_pair_sorted<1, 4> : k_pair_sorted<0, 4>;
+  // One set of resident CTAs walks all atoms.  Beside the side stream (SPME) this grid was
+  // also the fastest measured at 262,144 ions: grids of short-lived CTAs (1 to 8 atoms per
+  // warp), which retire and let the side stream's kernels in, fewer resident CTAs per SM
+  // and a larger shared-memory carveout were all slower.
   int occ = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, PAIR_SORTED_NT, 0));
   const int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, PAIR_SORTED_NT), occ * g.nsm));
@@ -1130,6 +1134,7 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   prof_begin(P_PAIR);
   kern<<<nb, PAIR_SORTED_NT, 0, st>>>(A, pg);
   GB_LAUNCHED();
+  side_join();  // the reciprocal-space forces are in place before the pair forces join them
   k_slot_stress_fold<<<nbs, 256, 0, st>>>(g.natms, g.sc, g.at_list, g.src, g.x, g.y, g.z, g.fixs,
                                           (unsigned long long*)g.fixp, blks);
   GB_LAUNCHED();
@@ -1184,6 +1189,7 @@ void pair_forces(double* eng6, double* stress9) {
   const int nb2 = nblocks(g.natms, 128);
   GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
   const bool sorted = g.spos_valid && g.use_sorted && !(g.precision == GB_FP64 && g.fp64_native);
+  if (!sorted) side_join();  // the atom-index kernels write the force arrays directly
   if (sorted) {
     pair_forces_sorted(pg, nb2);
   } else if (g.precision == GB_FP64 && !g.fp64_native) {

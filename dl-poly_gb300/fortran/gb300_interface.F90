@@ -36,7 +36,7 @@ Module gb300_interface
 
   Public :: gb_init, gb_upload_parts, gb_download_parts, gb_relocate, gb_list_build, gb_vnl_check, &
             gb_refresh, gb_forces, gb_spme, gb_vv, gb_constraints_tags, gb_shake, gb_rattle, gb_md_run, gb_mts_config, gb_mts_stats, &
-            gb_set_precision, gb_set_ensemble, gb_set_step, gb_thermostat_state, &
+            gb_set_precision, gb_set_overlap, gb_set_ensemble, gb_set_step, gb_thermostat_state, &
             gb_set_thermostat_state, gb_set_metal_eam, gb_metal_energies, gb_finalize
 
   Interface
@@ -136,6 +136,11 @@ Module gb300_interface
       Import :: c_int
       Integer(c_int), Value :: precision
     End Function gb_set_precision
+
+    Integer(c_int) Function gb_set_overlap(enable) Bind(C, name="gb_set_overlap")
+      Import :: c_int
+      Integer(c_int), Value :: enable
+    End Function gb_set_overlap
 
     Integer(c_int) Function gb_set_ensemble(kind, temp, tau_t, chi, seed, degfre) &
         Bind(C, name="gb_set_ensemble")

@@ -315,6 +315,12 @@ int64_t gb_kernel_launches(void);
 int gb_profile(int enable);
 int gb_profile_read(char* names, double* ms, int64_t* launches, int max);
 
+/* Reciprocal-space sum on a second stream, of higher priority, while the pair kernel runs
+ * (1, the default; GB_OVERLAP=0 in the environment at gb_init starts with 0) or both on
+ * one stream (0).  The results are the same bits either way; 0 gives each kernel the
+ * whole GPU, which the per-kernel timings of gb_profile want.  No reference counterpart. */
+int gb_set_overlap(int enable);
+
 /* Work counters of the last force evaluation and list build: [0] half-list entries,
  * [1] unique pairs inside rc, [2] list-build candidates tested in exact FP64,
  * [3] list entries with a halo image from the forward half shell, [4] from the

@@ -441,3 +441,32 @@ def test_state_transfer_mapped_and_copy_paths(gpu_lib, monkeypatch):
     monkeypatch.delenv("GB_MAPPED_COPY", raising=False)
     for k in gpu_lib.STATE_KEYS:
         assert np.array_equal(out["1"][k], out["0"][k]), k
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["nacl_4096", "water_5184"])
+def test_spme_side_stream_matches_one_stream(gpu_lib, monkeypatch, name, precision):
+    """SPME on the second stream while the pair kernel runs (the default) against both on
+    one stream (GB_OVERLAP=0): the same bits for forces, energies, virials and stress, at
+    the start-up force call and over 10 MD steps (per-step read-back and deferred)."""
+    s = CASES[name]()
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("GB_OVERLAP", mode)
+        gpu_lib.init(s, precision=precision)
+        e, st = gpu_lib.start()
+        f0 = gpu_lib.download()
+        steps = gpu_lib.md_vv(10)
+        out[mode] = (e, st, f0, steps, gpu_lib.download())
+    monkeypatch.delenv("GB_OVERLAP", raising=False)
+    a, b = out["0"], out["1"]
+    assert a[0] == b[0]
+    assert np.array_equal(a[1], b[1])
+    for k in gpu_lib.STATE_KEYS:
+        assert np.array_equal(a[2][k], b[2][k]), k
+        assert np.array_equal(a[4][k], b[4][k]), k
+    for x, y in zip(a[3], b[3]):
+        for f in ("engcpe_rc", "vircpe_rc", "engcpe_rl", "vircpe_rl", "engcpe_ex", "vircpe_ex", "engvdw", "virvdw",
+                  "engke"):
+            assert getattr(x, f) == getattr(y, f), f
+        assert list(x.stress) == list(y.stress)
