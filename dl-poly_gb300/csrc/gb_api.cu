@@ -1206,6 +1206,7 @@ const char* gb_strerror(int status) {
     case GB_ERR_METAL_TABLE: return "metal table read below its first point (error 506)";
     case GB_ERR_METAL_DENSITY: return "local density outside its embedding table (error 507)";
     case GB_ERR_RNG: return "a Gaussian deviate's rejection loop hit its iteration cap";
+    case GB_ERR_DEVICE_WAIT: return "a tensor-core completion wait hit its iteration limit";
     case GB_ERR_MULTI_RANK: return "more than one MPI rank (comm%mxnode > 1): the device path runs one rank on one GPU";
     case GB_ERR_TOO_LARGE: return "size exceeds the fixed scratch limit of gb_kinstress_noalloc (1,048,576 atoms)";
     default: return "unknown status";

@@ -24,6 +24,7 @@ enum : int {
   ST_RNG = 128,          // a Box-Muller rejection loop hit its cap
   ST_METAL_TABLE = 256,  // a metal table read below its first point (error 506)
   ST_METAL_DENSITY = 512,  // a local density outside its embedding table (error 507)
+  ST_DEVICE_WAIT = 1024,   // a kernel's wait on an mbarrier hit its iteration limit
 };
 
 // Device-resident scalars: one small block so a single copy returns them all.

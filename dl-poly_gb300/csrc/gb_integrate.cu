@@ -799,6 +799,7 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
     if (iters && g.ntcons > 0) *iters = g.hsc->rattle_iters;
     if (g.ntcons > 0 && (g.hsc->status & ST_RATTLE_FAIL)) throw (int)GB_ERR_RATTLE;
     if (g.hsc->status & ST_RNG) throw (int)GB_ERR_RNG;
+    if (g.hsc->status & ST_DEVICE_WAIT) throw (int)GB_ERR_DEVICE_WAIT;
   }
 }
 

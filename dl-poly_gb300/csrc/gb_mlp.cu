@@ -111,7 +111,9 @@ bool g_no_network = false;  // ablation: S = C, the coarse force alone
 
 inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU with the approximate quotient (two instructions; within 2 ulp, far below the BF16
+// rounding of the activations)
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float dsilu(float z) {
   const float s = 1.0f / (1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));
@@ -431,6 +433,259 @@ __global__ void __launch_bounds__(INFER_NT) k_mlp_infer(int n, const __nv_bfloat
   }
 }
 
+// ------------------------------------------------- inference (tcgen05 + TMEM)
+// The same network on the fifth-generation tensor cores.  A CTA of eight warps takes
+// tiles of 128 atoms (the MMA's M); operands sit in shared memory in the canonical
+// K-major layout without swizzle, and each layer's FP32 accumulator sits in tensor
+// memory (128 columns).  Warp w reads tensor-memory lanes 32 (w % 4) .. + 31 and half of
+// the columns for the bias, SiLU and BF16 rounding that form the next layer's operand.
+// One thread issues the MMAs; tcgen05.commit arrives on an mbarrier that the CTA waits on
+// with an iteration limit (on expiry the kernel records ST_DEVICE_WAIT, frees its tensor
+// memory and returns).  The next tile's inputs are fetched with cp.async while the
+// current tile's second and third layers run.
+namespace tc {
+constexpr int TM = 128;          // atoms per tile (MMA M)
+constexpr int NT = 256;          // threads
+constexpr int TMEM_COLS = 128;   // FP32 accumulator columns (N of the widest layer)
+constexpr int WAIT_LIMIT = 1 << 20;
+// shared-memory image (byte offsets); every operand block is 1024-byte aligned
+constexpr int S_A = 0;                        // X tile  [128 x 64]  bf16
+constexpr int S_H = S_A + TM * KIN * 2;       // hidden  [128 x 128] bf16
+constexpr int S_W1 = S_H + TM * NH * 2;       // W1^T    [128 x 64]
+constexpr int S_W2 = S_W1 + NH * KIN * 2;     // W2^T    [128 x 128]
+constexpr int S_W3 = S_W2 + NH * NH * 2;      // W3^T    [16 x 128]
+constexpr int S_BIAS = S_W3 + NOUTP * NH * 2;
+constexpr int S_BAR = S_BIAS + (2 * NH + NOUTP) * 4;
+constexpr int S_SLOT = S_BAR + 8;
+constexpr int SMEM = S_SLOT + 8;
+static_assert(S_BAR % 8 == 0, "mbarrier alignment");
+
+// byte offset of element (r, k) of a K-major operand with K columns: 8 x 16-byte core
+// matrices, the K-adjacent ones 128 bytes apart (leading-dimension offset), 8-row groups
+// K * 16 bytes apart (stride-dimension offset)
+__device__ __forceinline__ int core_off(int r, int k, int K) {
+  return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start, leading and stride byte offsets (>> 4), the
+// fixed version bit 46, base offset 0, no swizzle
+__device__ __forceinline__ unsigned long long sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (unsigned long long)((addr & 0x3FFFFu) >> 4) | ((unsigned long long)((lbo & 0x3FFFFu) >> 4) << 16) |
+         ((unsigned long long)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d_tmem, unsigned long long a, unsigned long long b, uint32_t idesc,
+                                    uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 bytes global -> shared without a register round trip; src_bytes 0 writes zeros
+__device__ __forceinline__ void cp16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's lane
+__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// a row-major [R][K] BF16 matrix into the canonical K-major layout (asynchronous copies)
+__device__ __forceinline__ void stage(uint32_t dst, const __nv_bfloat16* __restrict__ src, int R, int K) {
+  const int chunks = K / 8;
+  for (int e = threadIdx.x; e < R * chunks; e += blockDim.x) {
+    const int r = e / chunks, c = e - r * chunks;
+    cp16(dst + core_off(r, 8 * c, K), src + (size_t)r * K + 8 * c, 16u);
+  }
+}
+
+// the inputs of the tile starting at atom a0: 128 rows of 64 BF16 values (rows past n are zero)
+__device__ __forceinline__ void load_tile(uint32_t dst, const __nv_bfloat16* __restrict__ X, int a0, int n) {
+  for (int e = threadIdx.x; e < TM * (KIN / 8); e += blockDim.x) {
+    const int r = e >> 3, c = e & 7;
+    const bool in = a0 + r < n;
+    cp16(dst + core_off(r, 8 * c, KIN), in ? X + (size_t)(a0 + r) * KIN + 8 * c : X, in ? 16u : 0u);
+  }
+  cp_commit();
+}
+
+// 32 consecutive FP32 columns of this thread's lane, without waiting for them
+__device__ __forceinline__ void ld32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
+// bias, SiLU and BF16 rounding of 64 accumulator columns [c_lo, c_lo + 64) into the
+// hidden operand: both 32-column loads are in flight before the one wait
+__device__ __forceinline__ void hidden_epilogue(uint32_t tlane, int c_lo, const float* bias, unsigned char* H,
+                                                int row) {
+  uint32_t r[2][32];
+  ld32_nowait(tlane + (uint32_t)c_lo, r[0]);
+  ld32_nowait(tlane + (uint32_t)(c_lo + 32), r[1]);
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {  // 8 columns: one 16-byte row of a core matrix
+      const int c0 = c_lo + 32 * h + 8 * q;
+      uint32_t pk[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float v0 = __uint_as_float(r[h][8 * q + 2 * k]), v1 = __uint_as_float(r[h][8 * q + 2 * k + 1]);
+        const __nv_bfloat162 b2 = __floats2bfloat162_rn(silu(v0 + bias[c0 + 2 * k]), silu(v1 + bias[c0 + 2 * k + 1]));
+        pk[k] = *reinterpret_cast<const uint32_t*>(&b2);
+      }
+      *reinterpret_cast<uint4*>(H + core_off(row, c0, NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+  }
+}
+}  // namespace tc
+
+// persistent: each CTA stages the weights once and walks tiles of 128 atoms;
+// out = base + fs * R^T y (lab frame), as k_mlp_infer
+__global__ void __launch_bounds__(tc::NT) k_mlp_infer_tc(int n, const __nv_bfloat16* __restrict__ X, Net net,
+                                                         const float* __restrict__ base,
+                                                         const float* __restrict__ frame,
+                                                         const float* __restrict__ scal, float* __restrict__ out,
+                                                         int* status) {
+  using namespace tc;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int w = threadIdx.x >> 5;
+  const int row = 32 * (w & 3) + (threadIdx.x & 31);  // tensor-memory lane = atom row of the tile
+  const int half = w >> 2;                            // column half of the hidden layers
+  float* bias = reinterpret_cast<float*>(sm + S_BIAS);
+  const uint32_t bar = smem_addr(sm + S_BAR);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + S_SLOT);
+  const uint32_t aA = smem_addr(sm + S_A), aH = smem_addr(sm + S_H);
+  const uint32_t aW1 = smem_addr(sm + S_W1), aW2 = smem_addr(sm + S_W2), aW3 = smem_addr(sm + S_W3);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (w == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  stage(aW1, net.w1t, NH, KIN);
+  stage(aW2, net.w2t, NH, NH);
+  stage(aW3, net.w3t, NOUTP, NH);
+  cp_commit();
+  for (int e = threadIdx.x; e < 2 * NH + NOUTP; e += blockDim.x) bias[e] = net.bias[e];
+  const int ntiles = (n + TM - 1) / TM;
+  if ((int)blockIdx.x < ntiles) load_tile(aA, X, blockIdx.x * TM, n);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t tlane = tmem + ((uint32_t)(32 * (w & 3)) << 16);  // this warp's lanes
+  const float fs = scal[NIN];
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int a0 = tile * TM;
+#pragma unroll 1
+    for (int layer = 0; layer < 3 && ok; ++layer) {
+      if (layer == 0) cp_wait_all();  // this thread's copies of the tile (and the weights) landed
+      fence_async_smem();             // this thread's operand writes, visible to the tensor core
+      fence_before();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        fence_after();
+        const int K = layer == 0 ? KIN : NH;
+        const int N = layer == 2 ? NOUTP : NH;
+        const uint32_t a = layer == 0 ? aA : aH;
+        const uint32_t b = layer == 0 ? aW1 : (layer == 1 ? aW2 : aW3);
+        const uint32_t id = idesc_bf16(TM, N);
+        for (int s = 0; s < K / 16; ++s)
+          mma(tmem, sdesc(a + 256u * s, 128u, (uint32_t)K * 16u), sdesc(b + 256u * s, 128u, (uint32_t)K * 16u), id,
+              s > 0 ? 1u : 0u);
+        commit(bar);
+      }
+      const bool done = bar_wait(bar, phase);
+      phase ^= 1u;
+      if (__syncthreads_or(!done)) {
+        ok = false;
+        break;
+      }
+      fence_after();
+      if (layer == 0 && tile + (int)gridDim.x < ntiles)
+        load_tile(aA, X, (tile + gridDim.x) * TM, n);  // the first layer has read the inputs
+      if (layer < 2) {
+        hidden_epilogue(tlane, half * (NH / 2), bias + layer * NH, sm + S_H, row);
+      } else if (half == 0) {
+        float y[16];
+        ld16(tlane, y);
+        const int atom = a0 + row;
+        if (atom < n) {
+          const float* bo = bias + 2 * NH;
+          const float y0 = (y[0] + bo[0]) * fs, y1 = (y[1] + bo[1]) * fs, y2 = (y[2] + bo[2]) * fs;
+          const float* e = frame + 9 * (size_t)atom;
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            out[3 * (size_t)atom + c] = base[3 * (size_t)atom + c] + e[c] * y0 + e[3 + c] * y1 + e[6 + c] * y2;
+        }
+      }
+    }
+  }
+  cp_wait_all();  // no copy in flight when the CTA leaves
+  if (!ok && threadIdx.x == 0) atomicOr(status, ST_DEVICE_WAIT);
+  fence_before();
+  __syncthreads();
+  if (w == 0) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
 // ------------------------------------------------------------- training
 // forward + MSE + backward of TILE_T atoms; per-CTA gradient partial in gpart.
 // Row strides NH+1 keep the column walks of the backward pass conflict-free.
@@ -722,6 +977,7 @@ static_assert(sizeof(TrainSmem) <= 227 * 1024, "training tile exceeds shared mem
 static_assert(sizeof(InferSmem) <= 227 * 1024, "inference tile exceeds shared memory");
 
 int g_infer_grid = 0;
+int g_infer_tc_grid = 0;
 
 void net_alloc(Net& n) {
   GB_CUDA(cudaMalloc(&n.w1t, sizeof(__nv_bfloat16) * NH * KIN));
@@ -750,13 +1006,33 @@ void set_attrs() {
   int occ = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mlp_infer, INFER_NT, infer_smem));
   g_infer_grid = std::max(1, occ) * g.nsm;
+  GB_CUDA(cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
+  // the whole carveout as shared memory: two CTAs of 103.5 KB per SM
+  GB_CUDA(cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  // resident CTAs per SM from the SM's shared memory and registers (the occupancy query
+  // reports one here, while two fit and run)
+  cudaDeviceProp prop;
+  GB_CUDA(cudaGetDeviceProperties(&prop, dev));
+  cudaFuncAttributes fa;
+  GB_CUDA(cudaFuncGetAttributes(&fa, k_mlp_infer_tc));
+  const int by_smem = (int)(prop.sharedMemPerMultiprocessor / (tc::SMEM + prop.reservedSharedMemPerBlock));
+  const int by_regs = prop.regsPerMultiprocessor / (((fa.numRegs + 7) / 8 * 8) * tc::NT);
+  // every resident CTA holds TMEM_COLS of the SM's 512 tensor-memory columns
+  occ = std::max(1, std::min(std::min(by_smem, by_regs), 512 / tc::TMEM_COLS));
+  g_infer_tc_grid = occ * g.nsm;
   dev_done = dev;
 }
 
 void launch_infer(int n, const __nv_bfloat16* X, const Net& net, const float* base, const float* frame,
                   const float* scal, float* out) {
-  const int grid = std::max(1, std::min(g_infer_grid, nblocks(n, TILE_I)));
-  k_mlp_infer<<<grid, INFER_NT, infer_smem, g.stream>>>(n, X, net, base, frame, scal, out);
+  const char* e = getenv("GB_MLP_TC");  // 0: the mma.sync inference kernel
+  if (!(e && e[0] == '0')) {
+    const int grid = std::max(1, std::min(g_infer_tc_grid, nblocks(n, tc::TM)));
+    k_mlp_infer_tc<<<grid, tc::NT, tc::SMEM, g.stream>>>(n, X, net, base, frame, scal, out, &g.sc->status);
+  } else {
+    const int grid = std::max(1, std::min(g_infer_grid, nblocks(n, TILE_I)));
+    k_mlp_infer<<<grid, INFER_NT, infer_smem, g.stream>>>(n, X, net, base, frame, scal, out);
+  }
   GB_LAUNCHED();
 }
 
@@ -1204,12 +1480,13 @@ int mlp_infer_eval(int nb, const float* x, const float* params, float* yout) {
   GB_CUDA(cudaMemset(dF0, 0, sizeof(float) * 3 * (size_t)nb));
   GB_CUDA(cudaMemcpy(dFr, fr.data(), sizeof(float) * fr.size(), cudaMemcpyHostToDevice));
   GB_CUDA(cudaMemcpy(dS, sc.data(), sizeof(float) * sc.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
   launch_infer(nb, dX, net, dF0, dFr, dS, dOut);
   GB_CUDA(cudaMemcpyAsync(yout, dOut, sizeof(float) * 3 * (size_t)nb, cudaMemcpyDeviceToHost, g.stream));
-  GB_CUDA(cudaStreamSynchronize(g.stream));
+  gb_sync_scalars();
   for (void* p : {(void*)dP, (void*)dX, (void*)dF0, (void*)dFr, (void*)dS, (void*)dOut}) cudaFree(p);
   net_free(net);
-  return GB_OK;
+  return (g.hsc->status & ST_DEVICE_WAIT) ? GB_ERR_DEVICE_WAIT : GB_OK;
 }
 
 // copies the current inputs (nv <= natms rows of 51 floats) and the 52 scales

@@ -47,6 +47,7 @@ extern "C" {
 #define GB_ERR_TOO_LARGE (-6)  /* size beyond a fixed scratch limit (gb_kinstress_noalloc) */
 #define GB_ERR_RNG (-7)        /* a Gaussian deviate's rejection loop hit its iteration cap */
 #define GB_ERR_MULTI_RANK (-8) /* gb_params.mxnode > 1: a multi-rank run cannot use the device path */
+#define GB_ERR_DEVICE_WAIT (-9) /* a kernel's wait on its tensor-core completion hit its iteration limit */
 
 /* Precision forms of the force path. */
 #define GB_FP64 0   /* plain: FP64 accuracy; pair loop and SPME in double-float (pairs of FP32) */

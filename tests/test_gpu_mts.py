@@ -126,3 +126,20 @@ def test_mts_requires_mixed(gpu_lib):
     gpu_lib.init(systems.nacl_melt(16), precision=0)
     with pytest.raises(PathError):
         gpu_lib.mts_config(4, 1e-4, 10)
+
+
+@pytest.mark.parametrize("nb", [1, 127, 128, 129, 70000])
+def test_tcgen05_inference_matches_mma_sync_kernel(ctx, monkeypatch, nb):
+    """The tcgen05 inference kernel (operands in shared memory, FP32 accumulators in tensor
+    memory) against the mma.sync kernel on the same inputs and weights: both round the
+    same hidden activations to BF16 and accumulate in FP32, so they agree to the order of
+    the FP32 sums (a BF16 rounding flip of a hidden value at most), and both against the
+    oracle forward."""
+    x, _, p = _data(nb, 300 + nb)
+    monkeypatch.setenv("GB_MLP_TC", "0")
+    y_sync = ctx.mlp_infer_eval(x, p)
+    monkeypatch.delenv("GB_MLP_TC", raising=False)
+    y_tc = ctx.mlp_infer_eval(x, p)
+    yo, _ = mo.forward(x, p.astype(np.float64), bf16_points=True)
+    assert _rel(y_tc, yo) <= 1e-3
+    assert _rel(y_tc, y_sync) <= 1e-3
