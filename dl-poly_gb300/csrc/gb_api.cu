@@ -623,6 +623,8 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
       g.use_mapped = !(m && m[0] == '0');
       const char* o = getenv("GB_OVERLAP");  // 0: SPME and the pair kernel on one stream
       g.use_overlap = !(o && o[0] == '0');
+      const char* t = getenv("GB_PAIR_NT");  // 256: the sorted pair kernels in CTAs of 256 threads
+      g.pair_nt = (t && atoi(t) == 256) ? 256 : 1024;
     }
     thermo_setup(GB_NVE, 0.0, 0.0, 0.0, nullptr, 0.0);
     g.init = true;

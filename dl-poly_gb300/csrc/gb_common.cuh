@@ -104,6 +104,7 @@ struct Dev {
   cudaStream_t main_stream = nullptr, side_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool side = false, join_pending = false, use_overlap = true;
+  int pair_nt = 1024;  // threads per CTA of the sorted pair kernels (GB_PAIR_NT=256: four CTAs per SM)
   int nsm = 0;
   int64_t launches = 0;
 

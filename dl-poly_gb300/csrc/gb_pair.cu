@@ -727,7 +727,11 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 4) k_pair_df64(int natms, const De
 // are contiguous runs that L1 holds, not gathers by atom index.  Pair forces go to
 // per-sorted-position int64 fixed-point sums (64-bit integer reductions: the result does
 // not depend on their order); k_slot_stress_fold sums the stress and moves them to atoms.
-constexpr int PAIR_SORTED_NT = 256;
+// One CTA of 1024 threads per SM: its 32 warps take 32 consecutive sorted positions, whose
+// partners lie in the same few link cells (measured at 262,144 ions, pair time per launch
+// with 256-thread CTAs, four per SM / 1024-thread CTAs: double-float 1.353 / 1.288 ms,
+// mixed 0.740 / 0.728 ms; GB_PAIR_NT=256 selects the former)
+constexpr int PAIR_SORTED_NT = 1024;
 
 struct PairSortedArgs {
   int natms;
@@ -878,9 +882,9 @@ struct PairQueueN {
   int j[N];
 };
 
-template <int MIXED, int U>
-__global__ void __launch_bounds__(PAIR_SORTED_NT, 4) k_pair_sorted(PairSortedArgs A, PairGeom pg) {
-  __shared__ PairQueueN<32 * (U + 1)> pq[PAIR_SORTED_NT / 32];
+template <int MIXED, int U, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A, PairGeom pg) {
+  __shared__ PairQueueN<32 * (U + 1)> pq[NT / 32];
   __shared__ float4 s_lj[MIXED ? MAX_TYPES * MAX_TYPES : 1];
   if (MIXED) {
     for (int e = threadIdx.x; e < A.ntypes * A.ntypes; e += blockDim.x) {
@@ -890,13 +894,16 @@ __global__ void __launch_bounds__(PAIR_SORTED_NT, 4) k_pair_sorted(PairSortedArg
     __syncthreads();
   }
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   dacc acc[NACC_DF];
 #pragma unroll
   for (int k = 0; k < NACC_DF; ++k) { acc[k].s = 0.f; acc[k].c = 0.f; }
   unsigned long long n_list = 0, n_rc = 0;
   const int nlast = A.sc->nlast;
-  for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < nlast; p += nwarps) {
+  // The warps of a CTA take consecutive sorted positions (NT / 32 of them at a time), so
+  // they share the partners' link cells in the SM's L1.
+  for (int k = 0;; ++k) {
+    const int p = (blockIdx.x + k * gridDim.x) * (NT / 32) + wq;
+    if (p >= nlast) break;
     const int i = A.at_list[p];
     if (i >= A.natms) continue;  // a halo image: no list of its own
     const float4 pi = A.xhs[p], li = A.xls[p];
@@ -1116,14 +1123,21 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   // four list entries per lane in the filter pass (measured at 262,144 ions, pair time
   // per launch for 1 / 2 / 4 entries: double-float 1.46 / 1.37 / 1.34 ms, mixed 0.81 /
   // 0.76 / 0.74 ms)
-  void (*kern)(PairSortedArgs, PairGeom) = mixed ? k_pair_sorted<1, 4> : k_pair_sorted<0, 4>;
+  void (*kern)(PairSortedArgs, PairGeom) = nullptr;
+  int nt = PAIR_SORTED_NT;
+  if (g.pair_nt == 256) {
+    nt = 256;
+    kern = mixed ? k_pair_sorted<1, 4, 256> : k_pair_sorted<0, 4, 256>;
+  } else {
+    kern = mixed ? k_pair_sorted<1, 4, 1024> : k_pair_sorted<0, 4, 1024>;
+  }
   // One set of resident CTAs walks all atoms.  Beside the side stream (SPME) this grid was
   // also the fastest measured at 262,144 ions: grids of short-lived CTAs (1 to 8 atoms per
   // warp), which retire and let the side stream's kernels in, fewer resident CTAs per SM
   // and a larger shared-memory carveout were all slower.
   int occ = 0;
-  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, PAIR_SORTED_NT, 0));
-  const int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, PAIR_SORTED_NT), occ * g.nsm));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, 0));
+  const int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, nt), occ * g.nsm));
   const int nbs = std::max(1, std::min(nblocks(g.mxatms, 256), 4 * g.nsm));  // stress blocks
   double* blk = gb_blkacc(nb * NACC_DF + nbs * 6 + nb2 * 8);
   double* blks = blk + (size_t)nb * NACC_DF;
@@ -1132,7 +1146,7 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   GB_CUDA(cudaMemsetAsync(g.fixs, 0, sizeof(long long) * 3 * (size_t)g.mxatms, st));
   if (!mixed) GB_CUDA(cudaMemsetAsync(g.fixp, 0, sizeof(long long) * 3 * (size_t)g.mxatms, st));
   prof_begin(P_PAIR);
-  kern<<<nb, PAIR_SORTED_NT, 0, st>>>(A, pg);
+  kern<<<nb, nt, 0, st>>>(A, pg);
   GB_LAUNCHED();
   side_join();  // the reciprocal-space forces are in place before the pair forces join them
   k_slot_stress_fold<<<nbs, 256, 0, st>>>(g.natms, g.sc, g.at_list, g.src, g.x, g.y, g.z, g.fixs,

@@ -348,6 +348,33 @@ def test_sorted_pair_kernels_match_atom_index_kernels(gpu_lib, monkeypatch, name
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_pair_kernel_cta_sizes_agree(gpu_lib, monkeypatch, precision):
+    """The sorted pair kernels in CTAs of 1024 threads (the default) and of 256 threads
+    (GB_PAIR_NT=256) hand the atoms to warps in another order: the fixed-point forces are
+    bit-identical, the energy and virial sums agree to their rounding."""
+    s = CASES["nacl_13824"]()
+    runs = []
+    for env in ("256", None):
+        monkeypatch.delenv("GB_PAIR_NT", raising=False)
+        if env:
+            monkeypatch.setenv("GB_PAIR_NT", env)
+        gpu_lib.init(s, precision=precision)
+        gpu_lib.relocate()
+        gpu_lib.link_cell_pairs(want_list=False)
+        e, st = gpu_lib.two_body_forces()
+        runs.append((e, st, gpu_lib.download(), gpu_lib.pair_counts()))
+    monkeypatch.delenv("GB_PAIR_NT", raising=False)
+    (ea, sa, a, ca), (eb, sb, b, cb) = runs
+    assert ca[5] == 1 and cb[5] == 1  # the sorted-position kernels ran
+    for k in ("fx", "fy", "fz"):
+        assert np.array_equal(a[k], b[k]), k
+    tol = 1e-12 if precision == 0 else 1e-10
+    for k in ea:
+        assert abs(eb[k] - ea[k]) <= tol * max(abs(ea[k]), 1.0), k
+    assert np.abs(sb - sa).max() <= tol * np.abs(sa).max()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
 def test_deferred_step_scalars_match_per_step_readback(gpu_lib, monkeypatch, precision):
     """The NVE loop that reads each step's energy, virial and stress sums after its last
     step gives the same per-step scalars and the same trajectory as the loop that reads
