@@ -69,12 +69,19 @@ struct Net {  // published BF16 copy used by the inference kernel
   float* bias = nullptr;                                         // b1 | b2 | b3 padded to NOUTP
 };
 
+struct TrainW {  // BF16 operand copies of the FP32 master weights (k_train_weights)
+  __nv_bfloat16 *w1t = nullptr, *w2t = nullptr, *w3t = nullptr;  // [out][in]: forward B operands
+  __nv_bfloat16 *w2b = nullptr, *w3b = nullptr;                  // [in][out]: backward B operands
+  float* bias = nullptr;                                         // b1 | b2 | b3 padded to NOUTP
+};
+
 struct MtsDev {
   bool ready = false;
   int n = 0;
   float *master = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *gpart = nullptr, *loss_part = nullptr;
-  int gpart_tiles = 0, batch = 0;
+  int gpart_tiles = 0, batch = 0, train_tiles = 0;
   Net net;
+  TrainW tw;                   // operands of the tensor-core training kernel
   __nv_bfloat16* X = nullptr;  // inputs [n][KIN]
   float* frec0 = nullptr;      // SPME reciprocal force of the last full step (3n)
   float* frec = nullptr;       // reciprocal force now: SPME result, or S on an inner step (3n)
@@ -686,6 +693,328 @@ __global__ void __launch_bounds__(tc::NT) k_mlp_infer_tc(int n, const __nv_bfloa
   }
 }
 
+// ------------------------------------------------------ training (tcgen05 + TMEM)
+// Forward, MSE and backward of one tile of 128 atoms of the batch on the tensor cores:
+// the eight products of a training step,
+//   forward   Z1 = X W1, Z2 = H1 W2, Y = H2 W3                       (M = atoms)
+//   backward  dZ2' = dY W3^T, dZ1' = dZ2 W2^T                         (M = atoms)
+//             dW3 = H2^T dY, dW2^T = dZ2^T H1, dW1^T = dZ1^T X       (M = hidden units)
+// with BF16 operands (the rounding points of k_mlp_train: inputs, weights, activations and
+// activation gradients) and FP32 accumulators in tensor memory, 512 columns:
+//   Z1 [0,128)  Z2 [128,256)  Y [256,272)  dW3 [272,288)  dZ2' [384,512)
+//   then dZ1' [128,256)  dW2^T [256,384)  dW1^T [384,448)  as the earlier ones are read.
+// Every operand is K-major in shared memory: the epilogues write each activation (and
+// activation gradient) both as [atoms][units] and transposed as [units][atoms], so the
+// weight-gradient products contract over the atoms with the same descriptors as the
+// forward ones.  One thread issues each phase's MMAs and commits them to an mbarrier;
+// every wait has an iteration limit (ST_DEVICE_WAIT, tensor memory freed, no copy in
+// flight).  Per-CTA gradient partials go to gpart as in k_mlp_train (fixed-order sum in
+// k_grad_reduce), so a step is deterministic.
+
+namespace tct {
+using tc::core_off;
+using tc::sdesc;
+using tc::smem_addr;
+constexpr int TM = 128, NT = 256, TMEM_COLS = 512;
+// shared-memory image (byte offsets, operand blocks 4096-aligned)
+constexpr int S_X = 0;                  // X [128][64]; after the first product: dY [128][16], dY^T [16][128]
+constexpr int S_DY = S_X, S_DYT = S_X + TM * NOUTP * 2;
+constexpr int S_XT = S_X + TM * KIN * 2;  // X^T [64][128]
+constexpr int S_H1 = S_XT + KIN * TM * 2; // H1 [128][128]; later dZ2 [128][128]
+constexpr int S_H1T = S_H1 + TM * NH * 2; // H1^T
+constexpr int S_H2 = S_H1T + NH * TM * 2; // H2; later dZ2^T
+constexpr int S_H2T = S_H2 + TM * NH * 2; // H2^T; later dZ1^T
+constexpr int S_W = S_H2T + NH * TM * 2;  // W1^T [128][64] and W2^T [128][128]; later W2 [128][128], W3 [128][16]
+constexpr int S_W1T = S_W, S_W2T = S_W + NH * KIN * 2;
+constexpr int S_W2B = S_W, S_W3B = S_W + NH * NH * 2;
+constexpr int S_W3T = S_W + NH * KIN * 2 + NH * NH * 2;  // W3^T [16][128]
+constexpr int S_BIAS = S_W3T + NOUTP * NH * 2;
+constexpr int S_RED = S_BIAS + (2 * NH + NOUTP) * 4;     // per-row squared errors
+constexpr int S_BAR = S_RED + TM * 4;
+constexpr int S_SLOT = S_BAR + 8;
+constexpr int SMEM = S_SLOT + 8;
+static_assert(S_BAR % 8 == 0, "mbarrier alignment");
+static_assert(S_W3B + NH * NOUTP * 2 <= S_W3T, "backward weights fit the forward ones' space");
+static_assert(SMEM <= 227 * 1024, "training tile exceeds shared memory");
+constexpr uint32_t C_Z1 = 0, C_Z2 = 128, C_Y = 256, C_DW3 = 272, C_DZ2P = 384, C_DZ1P = 128, C_DW2 = 256,
+                   C_DW1 = 384;
+
+// K-steps of 16 of an M x N product with both operands K-major (K columns each)
+__device__ __forceinline__ void mma_k(uint32_t d, uint32_t a, uint32_t b, int K, int N) {
+  const uint32_t id = tc::idesc_bf16(TM, N);
+  for (int s = 0; s < K / 16; ++s)
+    tc::mma(d, sdesc(a + 256u * s, 128u, (uint32_t)K * 16u), sdesc(b + 256u * s, 128u, (uint32_t)K * 16u), id,
+            s > 0 ? 1u : 0u);
+}
+
+// 2-byte store of one BF16 value into a K-major [R][K] operand at (r, k)
+__device__ __forceinline__ void st_bf(unsigned char* base, int r, int k, int K, float v) {
+  *reinterpret_cast<__nv_bfloat16*>(base + core_off(r, k, K)) = __float2bfloat16(v);
+}
+__device__ __forceinline__ float ld_bf(const unsigned char* base, int r, int k, int K) {
+  return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(base + core_off(r, k, K)));
+}
+
+// 32 columns of this thread's lane
+__device__ __forceinline__ void ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  tc::ld32_nowait(taddr, r);
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// bias, SiLU and BF16 rounding of this thread's 64 columns of a hidden layer: the row of
+// H (K-major, 16-byte stores) and the column of H^T
+__device__ __forceinline__ void act_epilogue(uint32_t tl, int c_lo, const float* bias, unsigned char* H,
+                                             unsigned char* HT, int row) {
+#pragma unroll 1
+  for (int h = 0; h < 2; ++h) {
+    float v[32];
+    ld32(tl + (uint32_t)(c_lo + 32 * h), v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c0 = c_lo + 32 * h + 8 * q;
+      uint32_t pk[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const __nv_bfloat162 b2 = __floats2bfloat162_rn(silu(v[8 * q + 2 * k] + bias[c0 + 2 * k]),
+                                                        silu(v[8 * q + 2 * k + 1] + bias[c0 + 2 * k + 1]));
+        pk[k] = *reinterpret_cast<const uint32_t*>(&b2);
+        *reinterpret_cast<__nv_bfloat16*>(HT + core_off(c0 + 2 * k, row, TM)) = b2.x;
+        *reinterpret_cast<__nv_bfloat16*>(HT + core_off(c0 + 2 * k + 1, row, TM)) = b2.y;
+      }
+      *reinterpret_cast<uint4*>(H + core_off(row, c0, NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+  }
+}
+
+// dZ = BF16(dZ' * silu'(Z + b)) for this thread's 64 columns: into D ([atoms][units],
+// when given) and DT ([units][atoms])
+__device__ __forceinline__ void grad_epilogue(uint32_t tl, uint32_t c_pre, uint32_t c_z, int c_lo,
+                                              const float* bias, unsigned char* D, unsigned char* DT, int row) {
+#pragma unroll 1
+  for (int h = 0; h < 2; ++h) {
+    float pv[32], zv[32];
+    ld32(tl + c_pre + (uint32_t)(c_lo + 32 * h), pv);
+    ld32(tl + c_z + (uint32_t)(c_lo + 32 * h), zv);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c0 = c_lo + 32 * h + 8 * q;
+      uint32_t pk[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int e = 8 * q + 2 * k;
+        const __nv_bfloat162 b2 = __floats2bfloat162_rn(pv[e] * dsilu(zv[e] + bias[c0 + 2 * k]),
+                                                        pv[e + 1] * dsilu(zv[e + 1] + bias[c0 + 2 * k + 1]));
+        pk[k] = *reinterpret_cast<const uint32_t*>(&b2);
+        *reinterpret_cast<__nv_bfloat16*>(DT + core_off(c0 + 2 * k, row, TM)) = b2.x;
+        *reinterpret_cast<__nv_bfloat16*>(DT + core_off(c0 + 2 * k + 1, row, TM)) = b2.y;
+      }
+      if (D) *reinterpret_cast<uint4*>(D + core_off(row, c0, NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+  }
+}
+
+// sum over the 128 atoms of row u of a [units][atoms] operand, in atom order
+__device__ __forceinline__ float row_sum(const unsigned char* T, int u) {
+  float s = 0.f;
+  for (int r = 0; r < TM; ++r) s += ld_bf(T, u, r, TM);
+  return s;
+}
+}  // namespace tct
+
+// BF16 operand copies of the master weights for the tensor-core training kernel
+__global__ void k_train_weights(const float* __restrict__ w, TrainW t) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < NH * KIN) {
+    const int o = e / KIN, k = e % KIN;
+    t.w1t[e] = __float2bfloat16(k < NIN ? w[OFF_W1 + k * NH + o] : 0.f);
+  }
+  if (e < NH * NH) {
+    const int o = e / NH, k = e % NH;
+    t.w2t[e] = __float2bfloat16(w[OFF_W2 + k * NH + o]);  // [out][in]
+    t.w2b[e] = __float2bfloat16(w[OFF_W2 + e]);           // [in][out]
+  }
+  if (e < NOUTP * NH) {
+    const int o = e / NH, k = e % NH;
+    t.w3t[e] = __float2bfloat16(o < NOUT ? w[OFF_W3 + k * NOUT + o] : 0.f);
+    const int i = e / NOUTP, c = e % NOUTP;
+    t.w3b[e] = __float2bfloat16(c < NOUT ? w[OFF_W3 + i * NOUT + c] : 0.f);  // [in][out padded]
+  }
+  if (e < NH) { t.bias[e] = w[OFF_B1 + e]; t.bias[NH + e] = w[OFF_B2 + e]; }
+  if (e < NOUTP) t.bias[2 * NH + e] = e < NOUT ? w[OFF_B3 + e] : 0.f;
+}
+
+__global__ void __launch_bounds__(tct::NT, 1) k_mlp_train_tc(int nb, const int* __restrict__ idx,
+                                                            const __nv_bfloat16* __restrict__ X,
+                                                            const float* __restrict__ target, TrainW tw,
+                                                            float inv_count, float* __restrict__ gpart,
+                                                            float* __restrict__ loss_part, float* __restrict__ yout,
+                                                            int* status) {
+  using namespace tct;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int w = threadIdx.x >> 5, tid = threadIdx.x;
+  const int row = 32 * (w & 3) + (threadIdx.x & 31);  // tensor-memory lane
+  const int half = w >> 2;
+  float* bias = reinterpret_cast<float*>(sm + S_BIAS);
+  float* red = reinterpret_cast<float*>(sm + S_RED);
+  const uint32_t bar = smem_addr(sm + S_BAR);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + S_SLOT);
+  const uint32_t base = smem_addr(sm);
+  const int a0 = blockIdx.x * TM;
+  float* gp = gpart + (size_t)blockIdx.x * NPARAM;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (w == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc::stage(base + S_W1T, tw.w1t, NH, KIN);
+  tc::stage(base + S_W2T, tw.w2t, NH, NH);
+  tc::stage(base + S_W3T, tw.w3t, NOUTP, NH);
+  for (int e = tid; e < TM * (KIN / 8); e += NT) {  // the tile's input rows, gathered by idx
+    const int r = e >> 3, c = e & 7;
+    const bool in = a0 + r < nb;
+    tc::cp16(base + S_X + core_off(r, 8 * c, KIN), in ? X + (size_t)idx[a0 + r] * KIN + 8 * c : X, in ? 16u : 0u);
+  }
+  tc::cp_commit();
+  for (int e = tid; e < 2 * NH + NOUTP; e += NT) bias[e] = tw.bias[e];
+  tc::cp_wait_all();
+  __syncthreads();
+  for (int e = tid; e < KIN * TM; e += NT) {  // X^T for the last product
+    const int k = e / TM, r = e % TM;
+    *reinterpret_cast<__nv_bfloat16*>(sm + S_XT + core_off(k, r, TM)) =
+        *reinterpret_cast<const __nv_bfloat16*>(sm + S_X + core_off(r, k, KIN));
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t tl = tmem + ((uint32_t)(32 * (w & 3)) << 16);
+  uint32_t phase = 0;
+  bool ok = true;
+  // one phase: operand writes visible to the tensor core, MMAs by one thread, the wait
+  auto run = [&](int which) -> bool {
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+      switch (which) {
+        case 0: mma_k(tmem + C_Z1, base + S_X, base + S_W1T, KIN, NH); break;
+        case 1: mma_k(tmem + C_Z2, base + S_H1, base + S_W2T, NH, NH); break;
+        case 2: mma_k(tmem + C_Y, base + S_H2, base + S_W3T, NH, NOUTP); break;
+        case 3:
+          mma_k(tmem + C_DZ2P, base + S_DY, base + S_W3B, NOUTP, NH);
+          mma_k(tmem + C_DW3, base + S_H2T, base + S_DYT, TM, NOUTP);
+          break;
+        case 4:
+          mma_k(tmem + C_DZ1P, base + S_H1, base + S_W2B, NH, NH);   // dZ2 sits where H1 was
+          mma_k(tmem + C_DW2, base + S_H2, base + S_H1T, TM, NH);    // dZ2^T where H2 was
+          break;
+        default: mma_k(tmem + C_DW1, base + S_H2T, base + S_XT, TM, KIN); break;  // dZ1^T where H2^T was
+      }
+      tc::commit(bar);
+    }
+    const bool done = tc::bar_wait(bar, phase);
+    phase ^= 1u;
+    if (__syncthreads_or(!done)) return false;
+    tc::fence_after();
+    return true;
+  };
+  const int c_lo = half * (NH / 2);
+  // forward
+  ok = run(0);
+  if (ok) act_epilogue(tl + C_Z1, c_lo, bias, sm + S_H1, sm + S_H1T, row);
+  if (ok) ok = run(1);
+  if (ok) {
+    tc::stage(base + S_W2B, tw.w2b, NH, NH);  // the forward weights W1^T, W2^T are read
+    tc::stage(base + S_W3B, tw.w3b, NH, NOUTP);
+    tc::cp_commit();
+    act_epilogue(tl + C_Z2, c_lo, bias + NH, sm + S_H2, sm + S_H2T, row);
+  }
+  if (ok) ok = run(2);
+  if (ok) {
+    // output, loss and dY = BF16(2 (y - t) / count) (rows past the batch: zero)
+    if (half == 0) {
+      float y[16];
+      tc::ld16(tl + C_Y, y);
+      const int atom = a0 + row;
+      float dy[NOUT] = {0.f, 0.f, 0.f}, l = 0.f;
+      if (atom < nb) {
+#pragma unroll
+        for (int c = 0; c < NOUT; ++c) {
+          const float yc = y[c] + bias[2 * NH + c];
+          const float d = yc - target[3 * (size_t)idx[atom] + c];
+          if (yout) yout[3 * (size_t)atom + c] = yc;
+          dy[c] = 2.0f * d * inv_count;
+          l += d * d;
+        }
+      }
+      red[row] = l;
+      for (int c = 0; c < NOUTP; ++c) {
+        const float v = c < NOUT ? dy[c] : 0.f;
+        st_bf(sm + S_DY, row, c, NOUTP, v);
+        st_bf(sm + S_DYT, c, row, TM, v);
+      }
+    }
+    tc::cp_wait_all();  // the backward weights landed
+  }
+  if (ok) ok = run(3);
+  if (ok) {
+    if (tid == 0) {
+      float l = 0.f;
+      for (int r = 0; r < TM; ++r) l += red[r];
+      loss_part[blockIdx.x] = l * inv_count;
+    }
+    if (tid < NOUT) gp[OFF_B3 + tid] = row_sum(sm + S_DYT, tid);
+    if (half == 0) {  // dW3 [hidden][out]
+      float v[16];
+      tc::ld16(tl + C_DW3, v);
+#pragma unroll
+      for (int c = 0; c < NOUT; ++c) gp[OFF_W3 + row * NOUT + c] = v[c];
+    }
+    // dZ2 over H1 ([atoms][units]) and H2 (transposed): both read by the last phase
+    grad_epilogue(tl, C_DZ2P, C_Z2, c_lo, bias + NH, sm + S_H1, sm + S_H2, row);
+  }
+  if (ok) ok = run(4);
+  if (ok) {
+    if (tid < NH) gp[OFF_B2 + tid] = row_sum(sm + S_H2, tid);
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {  // dW2^T [out][in] -> W2[in][out]
+      float v[32];
+      ld32(tl + C_DW2 + (uint32_t)(c_lo + 32 * h), v);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) gp[OFF_W2 + (size_t)(c_lo + 32 * h + k) * NH + row] = v[k];
+    }
+    grad_epilogue(tl, C_DZ1P, C_Z1, c_lo, bias, nullptr, sm + S_H2T, row);  // dZ1^T over H2^T
+  }
+  if (ok) ok = run(5);
+  if (ok) {
+    if (tid < NH) gp[OFF_B1 + tid] = row_sum(sm + S_H2T, tid);
+    float v[32];  // dW1^T [hidden][in] -> W1[in][hidden]
+    ld32(tl + C_DW1 + (uint32_t)(32 * half), v);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      const int in = 32 * half + k;
+      if (in < NIN) gp[OFF_W1 + (size_t)in * NH + row] = v[k];
+    }
+  }
+  tc::cp_wait_all();  // no copy in flight when the CTA leaves
+  if (!ok && tid == 0) atomicOr(status, ST_DEVICE_WAIT);
+  tc::fence_before();
+  __syncthreads();
+  if (w == 0) {
+    tc::fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
 // ------------------------------------------------------------- training
 // forward + MSE + backward of TILE_T atoms; per-CTA gradient partial in gpart.
 // Row strides NH+1 keep the column walks of the backward pass conflict-free.
@@ -990,6 +1319,47 @@ void net_free(Net& n) {
     if (p) cudaFree(p);
   n = Net();
 }
+void train_w_alloc(TrainW& t) {
+  GB_CUDA(cudaMalloc(&t.w1t, sizeof(__nv_bfloat16) * NH * KIN));
+  GB_CUDA(cudaMalloc(&t.w2t, sizeof(__nv_bfloat16) * NH * NH));
+  GB_CUDA(cudaMalloc(&t.w3t, sizeof(__nv_bfloat16) * NOUTP * NH));
+  GB_CUDA(cudaMalloc(&t.w2b, sizeof(__nv_bfloat16) * NH * NH));
+  GB_CUDA(cudaMalloc(&t.w3b, sizeof(__nv_bfloat16) * NH * NOUTP));
+  GB_CUDA(cudaMalloc(&t.bias, sizeof(float) * (2 * NH + NOUTP)));
+}
+void train_w_free(TrainW& t) {
+  for (void* p : {(void*)t.w1t, (void*)t.w2t, (void*)t.w3t, (void*)t.w2b, (void*)t.w3b, (void*)t.bias})
+    if (p) cudaFree(p);
+  t = TrainW();
+}
+
+// GB_MLP_TC=0: the mma.sync inference kernel and the CUDA-core training kernel
+bool use_tc() {
+  const char* e = getenv("GB_MLP_TC");
+  return !(e && e[0] == '0');
+}
+
+// forward, loss and backward of nb rows (per-tile gradient partials, their fixed-order
+// sum in grad); returns the number of tiles, i.e. of loss partials
+int launch_train(int nb, const int* idx, const __nv_bfloat16* X, const float* target, const float* master,
+                 TrainW& tw, float* gpart, float* loss_part, float* yout, float* grad) {
+  const float inv = 1.0f / (float)(nb * NOUT);
+  int nt;
+  if (use_tc()) {
+    k_train_weights<<<nblocks(NH * NH, 256), 256, 0, g.stream>>>(master, tw);
+    GB_LAUNCHED();
+    nt = nblocks(nb, tct::TM);
+    k_mlp_train_tc<<<nt, tct::NT, tct::SMEM, g.stream>>>(nb, idx, X, target, tw, inv, gpart, loss_part, yout,
+                                                         &g.sc->status);
+  } else {
+    nt = nblocks(nb, TILE_T);
+    k_mlp_train<<<nt, 256, train_smem, g.stream>>>(nb, idx, X, target, master, inv, gpart, loss_part, yout);
+  }
+  GB_LAUNCHED();
+  k_grad_reduce<<<nblocks(NPARAM, 256), 256, 0, g.stream>>>(nt, gpart, grad);
+  GB_LAUNCHED();
+  return nt;
+}
 
 void publish(const float* master, Net& net) {
   k_publish<<<nblocks(NH * NH, 256), 256, 0, g.stream>>>(master, net);
@@ -1003,6 +1373,7 @@ void set_attrs() {
   if (dev_done == dev) return;
   GB_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem));
   GB_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem));
+  GB_CUDA(cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tct::SMEM));
   int occ = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mlp_infer, INFER_NT, infer_smem));
   g_infer_grid = std::max(1, occ) * g.nsm;
@@ -1025,8 +1396,7 @@ void set_attrs() {
 
 void launch_infer(int n, const __nv_bfloat16* X, const Net& net, const float* base, const float* frame,
                   const float* scal, float* out) {
-  const char* e = getenv("GB_MLP_TC");  // 0: the mma.sync inference kernel
-  if (!(e && e[0] == '0')) {
+  if (use_tc()) {
     const int grid = std::max(1, std::min(g_infer_tc_grid, nblocks(n, tc::TM)));
     k_mlp_infer_tc<<<grid, tc::NT, tc::SMEM, g.stream>>>(n, X, net, base, frame, scal, out, &g.sc->status);
   } else {
@@ -1146,13 +1516,8 @@ void mts_train_step() {
   k_seq_idx<<<nblocks(nb, 256), 256, 0, g.stream>>>(nb, M.batch_offset, n, M.idx);
   GB_LAUNCHED();
   M.batch_offset = (int)(((long long)M.batch_offset + nb) % n);
-  const int nt = nblocks(nb, TILE_T);
   prof_begin(P_MLP_TRAIN);
-  k_mlp_train<<<nt, 256, train_smem, g.stream>>>(nb, M.idx, M.X, M.target, M.master, 1.0f / (float)(nb * NOUT),
-                                                 M.gpart, M.loss_part, nullptr);
-  GB_LAUNCHED();
-  k_grad_reduce<<<nblocks(NPARAM, 256), 256, 0, g.stream>>>(nt, M.gpart, M.grad);
-  GB_LAUNCHED();
+  M.train_tiles = launch_train(nb, M.idx, M.X, M.target, M.master, M.tw, M.gpart, M.loss_part, nullptr, M.grad);
   ++M.adam_t;
   const float lr = 1e-3f;
   const float b1 = 0.9f, b2 = 0.999f;
@@ -1229,6 +1594,7 @@ void mts_free() {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   net_free(M.net);
+  train_w_free(M.tw);
   M = MtsDev();
 }
 
@@ -1248,6 +1614,7 @@ void mts_setup() {
   GB_CUDA(cudaMalloc(&M.gpart, sizeof(float) * NPARAM * (size_t)M.gpart_tiles));
   GB_CUDA(cudaMalloc(&M.loss_part, sizeof(float) * M.gpart_tiles));
   net_alloc(M.net);
+  train_w_alloc(M.tw);
   GB_CUDA(cudaMalloc(&M.X, sizeof(__nv_bfloat16) * KIN * (size_t)n));
   for (float** p : {&M.frec0, &M.frec, &M.truth, &M.target, &M.fc})
     GB_CUDA(cudaMalloc(p, sizeof(float) * 3 * (size_t)n));
@@ -1397,7 +1764,7 @@ void mts_inner(double* erc, double* vrc, double* stress9) {
 
 void mts_stats(double* out, int nv) {
   if (M.loss_pending && M.loss_part) {
-    std::vector<float> lp(M.gpart_tiles);
+    std::vector<float> lp(M.train_tiles > 0 ? M.train_tiles : M.gpart_tiles);  // the last step's partials
     GB_CUDA(cudaMemcpyAsync(lp.data(), M.loss_part, sizeof(float) * lp.size(), cudaMemcpyDeviceToHost, g.stream));
     GB_CUDA(cudaStreamSynchronize(g.stream));
     double l = 0.0;
@@ -1417,7 +1784,7 @@ int mlp_train_eval(int nb, const float* x, const float* target, const float* par
                    float* yout) {
   if (nb <= 0 || nb > 65536 || !x || !target || !params || !loss || !grad || !yout) return GB_ERR_ARG;
   set_attrs();
-  const int nt = nblocks(nb, TILE_T);
+  const int nt = nblocks(nb, TILE_T);  // partials: at least as many as either kernel's tiles
   std::vector<__nv_bfloat16> hx((size_t)nb * KIN);
   for (int r = 0; r < nb; ++r)
     for (int c = 0; c < KIN; ++c) hx[(size_t)r * KIN + c] = __float2bfloat16(c < NIN ? x[(size_t)r * NIN + c] : 0.f);
@@ -1438,20 +1805,21 @@ int mlp_train_eval(int nb, const float* x, const float* target, const float* par
   GB_CUDA(cudaMemcpy(dT, target, sizeof(float) * 3 * nb, cudaMemcpyHostToDevice));
   GB_CUDA(cudaMemcpy(dP, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice));
   GB_CUDA(cudaMemcpy(dI, hi.data(), sizeof(int) * nb, cudaMemcpyHostToDevice));
-  k_mlp_train<<<nt, 256, train_smem, g.stream>>>(nb, dI, dX, dT, dP, 1.0f / (float)(nb * NOUT), dGp, dL, dY);
-  GB_LAUNCHED();
-  k_grad_reduce<<<nblocks(NPARAM, 256), 256, 0, g.stream>>>(nt, dGp, dG);
-  GB_LAUNCHED();
-  std::vector<float> hl(nt);
+  TrainW tw;
+  train_w_alloc(tw);
+  GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
+  const int ntr = launch_train(nb, dI, dX, dT, dP, tw, dGp, dL, dY, dG);
+  std::vector<float> hl(ntr);
   GB_CUDA(cudaMemcpyAsync(grad, dG, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g.stream));
-  GB_CUDA(cudaMemcpyAsync(hl.data(), dL, sizeof(float) * nt, cudaMemcpyDeviceToHost, g.stream));
+  GB_CUDA(cudaMemcpyAsync(hl.data(), dL, sizeof(float) * ntr, cudaMemcpyDeviceToHost, g.stream));
   GB_CUDA(cudaMemcpyAsync(yout, dY, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost, g.stream));
-  GB_CUDA(cudaStreamSynchronize(g.stream));
+  gb_sync_scalars();
   float l = 0.f;
   for (float v : hl) l += v;
   *loss = l;
   for (void* p : {(void*)dX, (void*)dT, (void*)dP, (void*)dG, (void*)dGp, (void*)dL, (void*)dY, (void*)dI}) cudaFree(p);
-  return GB_OK;
+  train_w_free(tw);
+  return (g.hsc->status & ST_DEVICE_WAIT) ? GB_ERR_DEVICE_WAIT : GB_OK;
 }
 
 // the inference kernel on nb given rows (lab frame, zero base force, unit scales)

@@ -143,3 +143,29 @@ def test_tcgen05_inference_matches_mma_sync_kernel(ctx, monkeypatch, nb):
     yo, _ = mo.forward(x, p.astype(np.float64), bf16_points=True)
     assert _rel(y_tc, yo) <= 1e-3
     assert _rel(y_tc, y_sync) <= 1e-3
+
+
+@pytest.mark.parametrize("nb", [1, 129, 8192])
+def test_tcgen05_training_matches_cuda_core_kernel(ctx, monkeypatch, nb):
+    """The tcgen05 training kernel (the three forward and five backward products of a
+    128-atom tile on the tensor cores, FP32 accumulators in tensor memory) against the
+    CUDA-core training kernel (GB_MLP_TC=0) on the same batch: the same BF16 rounding
+    points and FP32 accumulation, so loss, outputs and every gradient block agree to the
+    order of the FP32 sums, and both against the FP64 oracle; the tensor-core step is
+    deterministic."""
+    x, t, p = _data(nb, 500 + nb)
+    monkeypatch.setenv("GB_MLP_TC", "0")
+    lc, gc, yc = ctx.mlp_train_eval(x, t, p)
+    monkeypatch.delenv("GB_MLP_TC", raising=False)
+    lt, gt, yt = ctx.mlp_train_eval(x, t, p)
+    lo, go, yo = mo.loss_and_grad(x, t, p.astype(np.float64), bf16_points=True)
+    assert lt == pytest.approx(lo, rel=2e-3) and lt == pytest.approx(lc, rel=2e-3)
+    assert _rel(yt, yo) <= 1e-3 and _rel(yt, yc) <= 1e-3
+    assert _rel(gt, go) <= 2e-3 and _rel(gt, gc) <= 2e-3
+    o = 0
+    for name, shape in mo.SHAPES:
+        n = int(np.prod(shape))
+        assert _rel(gt[o:o + n], go[o:o + n]) <= 5e-3, name
+        o += n
+    again = ctx.mlp_train_eval(x, t, p)
+    assert again[0] == lt and np.array_equal(again[1], gt)
