@@ -834,10 +834,16 @@ __device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSor
   return true;
 }
 
-// The mixed form's terms of one pair (FP32, analytic erfc and 12-6 LJ, as k_pair_mixed_half)
+// The mixed form's terms of one pair (FP32, analytic erfc and 12-6 LJ, as k_pair_mixed_half).
+// The four energy and virial terms go to the lane's FP32 sums of the current atom (e4:
+// vdW energy, vdW virial, Coulomb energy, Coulomb virial), which enter the compensated
+// running sums once per atom; the forces leave as 2^40 fixed point, truncated toward zero
+// by the hardware float-to-int64 conversion (the value fix40 forms with integer operations).
+__device__ __forceinline__ long long fix40_cvt(float x) { return __float2ll_rz(__fmul_rn(x, 1099511627776.0f)); }
+
 __device__ __forceinline__ bool pair_mixed_eval(const PairSortedArgs& A, const float4* s_lj, int row, int aj,
-                                                float qi, float qj, float dx, float dy, float dz,
-                                                dacc (&acc)[NACC_DF], long long& ix, long long& iy, long long& iz) {
+                                                float qi, float qj, float dx, float dy, float dz, float (&e4)[4],
+                                                long long& ix, long long& iy, long long& iz) {
   const float rsq = dx * dx + dy * dy + dz * dz;
   if (rsq >= A.rc2 && rsq >= A.rv2) return false;
   const float rinv = rsqrtf(rsq);
@@ -854,8 +860,8 @@ __device__ __forceinline__ bool pair_mixed_eval(const PairSortedArgs& A, const f
     const float ec = pre * poly * ex * rinv;
     const float eg = fmaf(pre * A.a2rp, ex, ec) * r2i;
     gam += eg;
-    dacc_add(acc[2], df_make(ec, 0.f));
-    dacc_add(acc[3], df_make(-eg * rsq, 0.f));
+    e4[2] += ec;
+    e4[3] -= eg * rsq;
     any = true;
   }
   if (rsq < A.rv2) {
@@ -865,15 +871,15 @@ __device__ __forceinline__ bool pair_mixed_eval(const PairSortedArgs& A, const f
       const float s6 = s2 * s2 * s2;
       const float gv = lj6.y * s6 * fmaf(2.0f, s6, -1.0f) * r2i;
       gam += gv;
-      dacc_add(acc[0], df_make(lj6.x * s6 * (s6 - 1.0f), 0.f));
-      dacc_add(acc[1], df_make(-gv * rsq, 0.f));
+      e4[0] += lj6.x * s6 * (s6 - 1.0f);
+      e4[1] -= gv * rsq;
       any = true;
     }
   }
   if (!any) return false;
-  ix = fix40(gam * dx);
-  iy = fix40(gam * dy);
-  iz = fix40(gam * dz);
+  ix = fix40_cvt(gam * dx);
+  iy = fix40_cvt(gam * dy);
+  iz = fix40_cvt(gam * dz);
   return true;
 }
 
@@ -915,6 +921,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A,
     const int n = A.list[(size_t)i * A.ld + 3];
     const int* sp = A.spos + (size_t)i * A.ldt;
     long long sx = 0, sy = 0, sz = 0;
+    float e4[4] = {0.f, 0.f, 0.f, 0.f};  // mixed form: this atom's energy and virial terms
     // pass 1, 32 U entries at a time (U per lane, their loads in flight together): an FP32
     // r^2 of the high parts against the outer cutoff plus a bound on their rounding queues
     // the candidates (ballot compaction); pass 2 evaluates 32 queued pairs at a time with
@@ -954,7 +961,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A,
           if (MIXED) {
             const float dx = (pi.x - pj.x) + (li.x - lj.x), dy = (pi.y - pj.y) + (li.y - lj.y),
                         dz = (pi.z - pj.z) + (li.z - lj.z);
-            hit = pair_mixed_eval(A, s_lj, ljrow, aj, qi32, pj.w, dx, dy, dz, acc, ix, iy, iz);
+            hit = pair_mixed_eval(A, s_lj, ljrow, aj, qi32, pj.w, dx, dy, dz, e4, ix, iy, iz);
           } else {
             const df ex = two_sum(pi.x, -pj.x), ey = two_sum(pi.y, -pj.y), ez = two_sum(pi.z, -pj.z);
             const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
@@ -976,6 +983,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A,
         __syncwarp();  // the taken slots are read before the next pass appends over them
       }
       if (!more) break;
+    }
+    if (MIXED) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dacc_add(acc[q], df_make(e4[q], 0.f));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
