@@ -104,7 +104,7 @@ struct Dev {
   cudaStream_t main_stream = nullptr, side_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool side = false, join_pending = false, use_overlap = true;
-  int pair_nt = 1024;  // threads per CTA of the sorted pair kernels (GB_PAIR_NT=256: four CTAs per SM)
+  int pair_nt = 0;  // threads per CTA of the sorted pair kernels: 256 or 1024 (GB_PAIR_NT), 0: by form
   int nsm = 0;
   int64_t launches = 0;
 
@@ -170,6 +170,7 @@ struct Dev {
   bool use_mapped = true;
   int* hflag = nullptr;        // pinned, mapped: the upload kernel's non-finite flag
   int* dflag = nullptr;        // its device-side address
+  int* loc_sp = nullptr;       // natms: the sorted positions of the local atoms, in sorted order
   float4* xhs = nullptr;       // per sorted position: FP32 high parts (x, y, z, q)
   float4* xls = nullptr;       // per sorted position: remainders (x, y, z, q) of the FP64 values
   unsigned char* tys = nullptr;  // per sorted position: atom type

@@ -953,6 +953,40 @@ int list_refresh_halo() {
   return GB_OK;
 }
 
+// The sorted positions of the local atoms, in sorted (cell) order: loc_sp[0, natms).  Per
+// block of 1024 positions a count, then (after a scan of the counts) each block's local
+// positions at its offset, ranked by a ballot prefix within each warp.
+constexpr int LOC_NT = 1024;
+__global__ void __launch_bounds__(LOC_NT) k_local_count(int natms, int mx, const DevScalars* sc,
+                                                        const int* __restrict__ at_list, int* blkcount) {
+  __shared__ int s[LOC_NT / 32];
+  const int p = blockIdx.x * LOC_NT + threadIdx.x;
+  const bool loc = p < min(sc->nlast, mx) && at_list[p] < natms;
+  const unsigned b = __ballot_sync(0xffffffffu, loc);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < LOC_NT / 32; ++w) t += s[w];
+    blkcount[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(LOC_NT) k_local_scatter(int natms, int mx, const DevScalars* sc,
+                                                          const int* __restrict__ at_list,
+                                                          const int* __restrict__ blkoff, int* loc_sp) {
+  __shared__ int s[LOC_NT / 32];
+  const int p = blockIdx.x * LOC_NT + threadIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const bool loc = p < min(sc->nlast, mx) && at_list[p] < natms;
+  const unsigned b = __ballot_sync(0xffffffffu, loc);
+  if (lane == 0) s[w] = __popc(b);
+  __syncthreads();
+  int before = 0;
+  for (int k = 0; k < w; ++k) before += s[k];
+  const int r = blkoff[blockIdx.x] + before + __popc(b & ((1u << lane) - 1u));
+  if (loc && r < natms) loc_sp[r] = p;
+}
+
 int list_build() {
   const int T = 256;
   cudaStream_t st = g.stream;
@@ -970,6 +1004,16 @@ int list_build() {
   k_cell_sort<<<nblocks((long long)(g.ncells + 1) * 32, T), T, 0, st>>>(g.ncells + 1, g.cell_start, tmp, g.at_list,
                                                                        g.sorted_pos, g.x, g.y, g.z, g.xs, g.xsf);
   GB_LAUNCHED();
+  {
+    const int nb = nblocks(mx, LOC_NT);
+    int* cnt = gb_scan_scratch(2 * nb + 2);
+    k_local_count<<<nb, LOC_NT, 0, st>>>(g.natms, mx, g.sc, g.at_list, cnt);
+    GB_LAUNCHED();
+    k_scan_single<<<1, 1024, 0, st>>>(cnt, cnt + nb + 1, nb, nullptr);
+    GB_LAUNCHED();
+    k_local_scatter<<<nb, LOC_NT, 0, st>>>(g.natms, mx, g.sc, g.at_list, cnt + nb + 1, g.loc_sp);
+    GB_LAUNCHED();
+  }
   prof_end(P_BIN);
   GB_CUDA(cudaMemsetAsync(&g.sc->ibig, 0, sizeof(int), st));
   GB_CUDA(cudaMemsetAsync(&g.sc->tile_over, 0, 4 * sizeof(int), st));  // tile_over, tile_max, halo_fwd, halo_bwd

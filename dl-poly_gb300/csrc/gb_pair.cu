@@ -727,15 +727,17 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 4) k_pair_df64(int natms, const De
 // are contiguous runs that L1 holds, not gathers by atom index.  Pair forces go to
 // per-sorted-position int64 fixed-point sums (64-bit integer reductions: the result does
 // not depend on their order); k_slot_stress_fold sums the stress and moves them to atoms.
-// One CTA of 1024 threads per SM: its 32 warps take 32 consecutive sorted positions, whose
-// partners lie in the same few link cells (measured at 262,144 ions, pair time per launch
-// with 256-thread CTAs, four per SM / 1024-thread CTAs: double-float 1.353 / 1.288 ms,
-// mixed 0.740 / 0.728 ms; GB_PAIR_NT=256 selects the former)
+// CTA size by form (measured at 262,144 ions, each CTA on a contiguous run of the local
+// atoms; pair time per launch and MD step with SPME on the side stream, 1024-thread CTAs
+// (one per SM) / 256-thread CTAs (four per SM)): double-float 1.192 / 1.285 ms, step 2.77 /
+// 2.84 ms; mixed 0.687 / 0.687 ms, step 1.52 / 1.48 ms (the side stream's kernels find room
+// beside the smaller CTAs).  GB_PAIR_NT=256 or 1024 sets it for both forms.
 constexpr int PAIR_SORTED_NT = 1024;
 
 struct PairSortedArgs {
   int natms;
   const int* at_list;
+  const int* loc_sp;  // the local atoms' sorted positions, in sorted order
   const int* list;
   int ld;
   const int* spos;
@@ -904,14 +906,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A,
 #pragma unroll
   for (int k = 0; k < NACC_DF; ++k) { acc[k].s = 0.f; acc[k].c = 0.f; }
   unsigned long long n_list = 0, n_rc = 0;
-  const int nlast = A.sc->nlast;
-  // The warps of a CTA take consecutive sorted positions (NT / 32 of them at a time), so
-  // they share the partners' link cells in the SM's L1.
-  for (int k = 0;; ++k) {
-    const int p = (blockIdx.x + k * gridDim.x) * (NT / 32) + wq;
-    if (p >= nlast) break;
+  // Each CTA takes an equal, contiguous run of the local atoms in sorted (cell) order, its
+  // warps NT / 32 consecutive atoms at a time: the partners of the atoms in flight are the
+  // same few link cells, and the next atoms' mostly the same, which the SM's L1 holds.
+  const int per = (A.natms + gridDim.x - 1) / gridDim.x;
+  const int a_end = min(A.natms, (int)(blockIdx.x + 1) * per);
+  for (int a = blockIdx.x * per + wq; a < a_end; a += NT / 32) {
+    const int p = A.loc_sp[a];
     const int i = A.at_list[p];
-    if (i >= A.natms) continue;  // a halo image: no list of its own
     const float4 pi = A.xhs[p], li = A.xls[p];
     const int ai = A.tys[p];
     const df qi = df_mul(df_make(pi.w, li.w), df_make(pg.scal_hi, pg.scal_lo));  // q_i r4pie0/eps
@@ -1119,6 +1121,7 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   PairSortedArgs A;
   A.natms = g.natms;
   A.at_list = g.at_list;
+  A.loc_sp = g.loc_sp;
   A.list = g.list; A.ld = g.ld; A.spos = g.spos; A.ldt = g.ldt;
   A.xhs = g.xhs; A.xls = g.xls; A.tys = g.tys;
   A.x = g.x; A.y = g.y; A.z = g.z; A.q = g.chge;
@@ -1136,7 +1139,7 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   // 0.76 / 0.74 ms)
   void (*kern)(PairSortedArgs, PairGeom) = nullptr;
   int nt = PAIR_SORTED_NT;
-  if (g.pair_nt == 256) {
+  if (g.pair_nt == 256 || (g.pair_nt == 0 && mixed)) {
     nt = 256;
     kern = mixed ? k_pair_sorted<1, 4, 256> : k_pair_sorted<0, 4, 256>;
   } else {

@@ -349,15 +349,13 @@ def test_sorted_pair_kernels_match_atom_index_kernels(gpu_lib, monkeypatch, name
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
 def test_pair_kernel_cta_sizes_agree(gpu_lib, monkeypatch, precision):
-    """The sorted pair kernels in CTAs of 1024 threads (the default) and of 256 threads
-    (GB_PAIR_NT=256) hand the atoms to warps in another order: the fixed-point forces are
-    bit-identical, the energy and virial sums agree to their rounding."""
+    """The sorted pair kernels in CTAs of 1024 threads (the FP64 form's default) and of 256
+    threads (the mixed form's) hand the atoms to warps in another order: the fixed-point
+    forces are bit-identical, the energy and virial sums agree to their rounding."""
     s = CASES["nacl_13824"]()
     runs = []
-    for env in ("256", None):
-        monkeypatch.delenv("GB_PAIR_NT", raising=False)
-        if env:
-            monkeypatch.setenv("GB_PAIR_NT", env)
+    for env in ("256", "1024"):
+        monkeypatch.setenv("GB_PAIR_NT", env)
         gpu_lib.init(s, precision=precision)
         gpu_lib.relocate()
         gpu_lib.link_cell_pairs(want_list=False)
