@@ -631,7 +631,7 @@ def run_gb(args, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--runs", type=int, default=3, help="timed runs of --steps steps each; the line reports the median")
     ap.add_argument("--impl", default="gb", choices=["gb", "reference"])

@@ -212,19 +212,38 @@ __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, 
       Pkl[a * p2 + kl] = spl[((size_t)i * 3 + 1) * p + k] * spl[((size_t)i * 3 + 2) * p + l];  // My (Mz q)
     }
     __syncthreads();
-    // tile plane z belongs to warp z mod NW: a point is only ever written by one warp, in
-    // atom order, so the warps run through the chunk without a barrier per atom
-    for (int a = 0; a < nc; ++a) {
-      const int ox = off[a * 3], oy = off[a * 3 + 1], oz = off[a * 3 + 2];
-      for (int l = (wid - oz) & (SPREAD_NW - 1); l < p; l += SPREAD_NW) {
-        T* plane = tile + (oz + l) * TYd * TXd;
-        for (int kj = lane; kj < p2; kj += 32) {
-          const int j = kj % p, k = kj / p;
-          T* dst = plane + (oy + k) * TXd + (ox + j);
+    // every tile point is only ever written by one warp, in atom order, so the warps run
+    // through the chunk without a barrier per atom.  Orders up to 8: the points of tile
+    // plane z and row y belong to warp (z mod 8) + 8 (y mod 2), so every warp takes one
+    // plane and every other row of each atom (for p = 8 one point per lane); higher orders:
+    // plane z belongs to warp z mod NW.
+    static_assert(SPREAD_NW == 16, "the split below gives warps w and w + 8 the even and odd rows");
+    if (p <= 8) {
+      const int grp = wid & 7, half = wid >> 3;
+      const int m = lane / p, j = lane - m * p;  // this lane's row pair and column
+      for (int a = 0; a < nc; ++a) {
+        const int oz = off[a * 3 + 2], oy = off[a * 3 + 1];
+        const int l = (grp - oz) & 7;
+        const int k = ((half - oy) & 1) + 2 * m;
+        if (l < p && k < p) {
+          T* dst = tile + ((oz + l) * TYd + (oy + k)) * TXd + (off[a * 3] + j);
           *dst = fma(Mx[a * p + j], Pkl[a * p2 + l * p + k], *dst);
         }
       }
       __syncwarp();
+    } else {
+      for (int a = 0; a < nc; ++a) {
+        const int ox = off[a * 3], oy = off[a * 3 + 1], oz = off[a * 3 + 2];
+        for (int l = (wid - oz) & (SPREAD_NW - 1); l < p; l += SPREAD_NW) {
+          T* plane = tile + (oz + l) * TYd * TXd;
+          for (int kj = lane; kj < p2; kj += 32) {
+            const int j = kj % p, k = kj / p;
+            T* dst = plane + (oy + k) * TXd + (ox + j);
+            *dst = fma(Mx[a * p + j], Pkl[a * p2 + l * p + k], *dst);
+          }
+        }
+        __syncwarp();
+      }
     }
   }
   __syncthreads();

@@ -65,6 +65,31 @@ def test_spme_alone_fp64(gpu_lib, oracle_lib):
     assert force_dev(gpu_lib.download(), oracle_lib.download()) < FP64_TOL
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_spme_with_uncharged_atoms(gpu_lib, oracle_lib, precision):
+    """Atoms without charge take no part in the spread (no brick) and gather nothing: their
+    reciprocal force is only the removal of the mean net force, the same for each of them,
+    and every atom's force matches the oracle (FP64 bar, or the mixed form's error bound)."""
+    s = systems.nacl_melt(16)
+    q = s.chge.copy()
+    q[np.flatnonzero(q > 0)[::7]] = 0.0
+    q[np.flatnonzero(q < 0)[::7]] = 0.0
+    s.chge = q
+    _pair(gpu_lib, oracle_lib, s, precision=precision)
+    ed, vd, sd = gpu_lib.ewald_spme_forces()
+    er, vr, sr = oracle_lib.ewald_spme_forces()
+    a, b = gpu_lib.download(), oracle_lib.download()
+    z = q == 0.0
+    for k in ("fx", "fy", "fz"):
+        assert np.ptp(a[k][z]) == 0.0, k
+    if precision == 0:
+        assert ed == pytest.approx(er, rel=FP64_TOL)
+        assert force_dev(a, b) < FP64_TOL
+    else:  # FP32 grid arithmetic, relative to the reciprocal force alone
+        assert ed == pytest.approx(er, rel=1e-5)
+        assert force_rms_rel(a, b) <= 1e-4
+
+
 def test_vdw_known_answer_on_gpu(gpu_lib):
     """source/unit_tests/test_vdw.F90:46-59 entry 2 (LJ eps=1 sigma=2 at r=1) through the device path."""
     s = systems.lj_pair(eps=1.0, sigma=2.0, r=1.0)
