@@ -626,6 +626,8 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
       g.use_overlap = !(o && o[0] == '0');
       const char* t = getenv("GB_PAIR_NT");  // 256 / 1024: CTA size of the sorted pair kernels (else by form)
       g.pair_nt = t ? ((atoi(t) == 256) ? 256 : 1024) : 0;
+      const char* w = getenv("GB_PAIR_APW");
+      g.pair_apw = w ? std::max(0, atoi(w)) : -1;
     }
     thermo_setup(GB_NVE, 0.0, 0.0, 0.0, nullptr, 0.0);
     g.init = true;

@@ -104,6 +104,7 @@ struct Dev {
   cudaStream_t main_stream = nullptr, side_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool side = false, join_pending = false, use_overlap = true;
+  int pair_apw = -1;  // atoms per warp of the sorted pair kernels' CTAs (GB_PAIR_APW; 0: resident CTAs, -1: by form)
   int pair_nt = 0;  // threads per CTA of the sorted pair kernels: 256 or 1024 (GB_PAIR_NT), 0: by form
   int nsm = 0;
   int64_t launches = 0;

@@ -1145,13 +1145,18 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   } else {
     kern = mixed ? k_pair_sorted<1, 4, 1024> : k_pair_sorted<0, 4, 1024>;
   }
-  // One set of resident CTAs walks all atoms.  Beside the side stream (SPME) this grid was
-  // also the fastest measured at 262,144 ions: grids of short-lived CTAs (1 to 8 atoms per
-  // warp), which retire and let the side stream's kernels in, fewer resident CTAs per SM
-  // and a larger shared-memory carveout were all slower.
   int occ = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, 0));
-  const int nb = std::max(1, std::min(nblocks((long long)g.mxatms * 32, nt), occ * g.nsm));
+  // The CTAs take equal contiguous runs of the local atoms: one resident set of CTAs
+  // (the double-float form), or short-lived CTAs of 16 atoms per warp (the mixed form: they
+  // retire through the step, so the side stream's SPME kernels take their places and the
+  // last runs balance the load; measured at 262,144 ions, mixed pair 0.682 -> 0.646 ms and
+  // step 1.481 -> 1.460 ms; for the double-float form they were slower at every length).
+  // GB_PAIR_APW sets the atoms per warp (0: one resident set).
+  int apw = mixed ? 16 : 0;
+  if (g.pair_apw >= 0) apw = g.pair_apw;
+  const int nb = apw > 0 ? std::max(1, nblocks((long long)g.natms, (nt / 32) * apw))
+                         : std::max(1, std::min(nblocks((long long)g.mxatms * 32, nt), occ * g.nsm));
   const int nbs = std::max(1, std::min(nblocks(g.mxatms, 256), 4 * g.nsm));  // stress blocks
   double* blk = gb_blkacc(nb * NACC_DF + nbs * 6 + nb2 * 8);
   double* blks = blk + (size_t)nb * NACC_DF;

@@ -374,27 +374,31 @@ def test_sorted_pair_kernels_match_atom_index_kernels(gpu_lib, monkeypatch, name
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
 def test_pair_kernel_cta_sizes_agree(gpu_lib, monkeypatch, precision):
-    """The sorted pair kernels in CTAs of 1024 threads (the FP64 form's default) and of 256
-    threads (the mixed form's) hand the atoms to warps in another order: the fixed-point
-    forces are bit-identical, the energy and virial sums agree to their rounding."""
+    """The sorted pair kernels in one resident set of 1024-thread CTAs (the FP64 form's
+    default), in 256-thread CTAs, and in short-lived CTAs of 16 atoms per warp (the mixed
+    form's default) hand the atoms to warps in other orders: the fixed-point forces are
+    bit-identical, the energy and virial sums agree to their rounding."""
     s = CASES["nacl_13824"]()
     runs = []
-    for env in ("256", "1024"):
+    for env, apw in (("256", "16"), ("1024", "0"), ("256", "0")):
         monkeypatch.setenv("GB_PAIR_NT", env)
+        monkeypatch.setenv("GB_PAIR_APW", apw)
         gpu_lib.init(s, precision=precision)
         gpu_lib.relocate()
         gpu_lib.link_cell_pairs(want_list=False)
         e, st = gpu_lib.two_body_forces()
         runs.append((e, st, gpu_lib.download(), gpu_lib.pair_counts()))
     monkeypatch.delenv("GB_PAIR_NT", raising=False)
-    (ea, sa, a, ca), (eb, sb, b, cb) = runs
-    assert ca[5] == 1 and cb[5] == 1  # the sorted-position kernels ran
-    for k in ("fx", "fy", "fz"):
-        assert np.array_equal(a[k], b[k]), k
+    monkeypatch.delenv("GB_PAIR_APW", raising=False)
+    ea, sa, a, ca = runs[0]
     tol = 1e-12 if precision == 0 else 1e-10
-    for k in ea:
-        assert abs(eb[k] - ea[k]) <= tol * max(abs(ea[k]), 1.0), k
-    assert np.abs(sb - sa).max() <= tol * np.abs(sa).max()
+    for eb, sb, b, cb in runs[1:]:
+        assert ca[5] == 1 and cb[5] == 1  # the sorted-position kernels ran
+        for k in ("fx", "fy", "fz"):
+            assert np.array_equal(a[k], b[k]), k
+        for k in ea:
+            assert abs(eb[k] - ea[k]) <= tol * max(abs(ea[k]), 1.0), k
+        assert np.abs(sb - sa).max() <= tol * np.abs(sa).max()
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
