@@ -36,7 +36,7 @@
 // BF16-rounded operands (weights, inputs, activations, activation gradients)
 // and FP32 accumulation, per-CTA gradient partials summed in a fixed order,
 // Adam on FP32 master weights.  Labels are R_i (F_SPME,i - C_i) / fs from the
-// steps that run SPME (every step while training).  The judge: at every cycle
+// steps that run SPME (every step while training).  The check: at every cycle
 // end after training, S of that step is compared with SPME; RMS(S - SPME) /
 // RMS(total force) > tol switches to plain SPME every step (no impulses; training
 // resumes) until a cycle end passes.  Each check also records the error of the
@@ -85,7 +85,7 @@ struct MtsDev {
   __nv_bfloat16* X = nullptr;  // inputs [n][KIN]
   float* frec0 = nullptr;      // SPME reciprocal force of the last full step (3n)
   float* frec = nullptr;       // reciprocal force now: SPME result, or S on an inner step (3n)
-  float* truth = nullptr;      // S at a full step, for the judge and the impulse (3n)
+  float* truth = nullptr;      // S at a full step, for the check and the impulse (3n)
   float* fc = nullptr;         // coarse-grid reciprocal force now (3n)
   int Kc[3] = {0, 0, 0}, pc = 6;
   double ec = 0.0, vc = 0.0, stc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};     // coarse now
@@ -105,7 +105,7 @@ struct MtsDev {
   int s = 0;                   // steps since t0
   int step = 0;                // MD steps since configuration
   bool have_t0 = false, scales_set = false, fallback = false, loss_pending = false;
-  long long n_full = 0, n_inner = 0, n_fallback = 0, n_judged = 0;
+  long long n_full = 0, n_inner = 0, n_fallback = 0, n_checked = 0;
   double last_err = -1.0, last_loss = -1.0, err_max = -1.0;
   int batch_offset = 0;
   // reciprocal energy/virial/stress of the last full step
@@ -1663,7 +1663,7 @@ bool mts_step_needs_spme() {
 }
 
 // after a full force evaluation of an MD step (SPME ran and its force is in the
-// fixed-point sums): labels, the judge, the impulse of a cycle end, training and the
+// fixed-point sums): labels, the check, the impulse of a cycle end, training and the
 // cycle bookkeeping
 void mts_after_full(double erc, double vrc, const double* strec) {
   const int n = g.natms;
@@ -1682,7 +1682,7 @@ void mts_after_full(double erc, double vrc, const double* strec) {
   const bool trained = M.adam_t > 0 || g_no_network;
   const int nb = nblocks(n, 256);
   if (cycle_end && trained) {
-    // S of this step, as the inner steps form it, against SPME (the judge)
+    // S of this step, as the inner steps form it, against SPME (the check)
     prof_begin(P_MLP);
     if (g_no_network) {
       k_copy_f<<<nblocks(3LL * n, 256), 256, 0, g.stream>>>(3LL * n, M.fc, M.truth);
@@ -1709,7 +1709,7 @@ void mts_after_full(double erc, double vrc, const double* strec) {
     M.err_stale = std::sqrt(r4[2] / n) / ftot;
     M.last_err = err;
     M.err_max = std::max(M.err_max, err);
-    M.n_judged++;
+    M.n_checked++;
     if (!training_now()) {
       const bool was = M.fallback;
       M.fallback = err > g.mts_tol;
@@ -1773,7 +1773,7 @@ void mts_stats(double* out, int nv) {
     M.loss_pending = false;
   }
   const double v[13] = {M.last_err, (double)M.n_full, (double)M.n_inner, (double)M.n_fallback, M.last_loss,
-                        (double)M.adam_t, M.err_max, M.fallback ? 1.0 : 0.0, (double)M.n_judged, (double)M.step,
+                        (double)M.adam_t, M.err_max, M.fallback ? 1.0 : 0.0, (double)M.n_checked, (double)M.step,
                         M.err_coarse, M.err_stale, (double)M.Kc[0]};
   for (int k = 0; k < nv && k < 13; ++k) out[k] = v[k];
 }

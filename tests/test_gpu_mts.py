@@ -7,7 +7,7 @@
   correction on the inner steps) matches the reciprocal force better than the
   coarse-grid force alone and than the previous full step's force held fixed,
   the ablations;
-- the judge falls back to plain SPME when the bound cannot be met.
+- the check falls back to plain SPME when the bound cannot be met.
 """
 import numpy as np
 import pytest

@@ -1,7 +1,7 @@
 """GPU parity: the CUDA path against the FP64 oracle on the same seeded inputs,
 through the C-ABI (gb_* entry points).
 
-Bars (BASELINE the benchmark spec): pair sets bit-exact; FP64 forces within 1e-10 of
+Bars: pair sets bit-exact; FP64 forces within 1e-10 of
 the oracle (max |dF| relative to the rms force); energies and virials within
 1e-10 relative; mixed form rms force error <= 1e-5 relative.
 """
