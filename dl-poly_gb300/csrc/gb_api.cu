@@ -287,6 +287,10 @@ int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real, bo
     list_pos_sorted();  // the same per sorted position, for the sorted-position pair kernels
   const bool mts = md_step && do_spme && mts_active();
   const bool full = mts ? mts_step_needs_spme() : (do_spme && g.has_coul);
+  // a learned-MTS inner step: the coarse grid, the network's inputs and inference go to the
+  // side stream once the pair kernel is launched, and run beside it
+  const bool mts_side = mts && !full && g.use_overlap && do_real && !g.has_metal;
+  if (mts && !mts_side) mts_coarse();
   // SPME on the side stream while the pair kernel runs (the plain FP64 form keeps one
   // stream: its kernels are bound by the FP64 unit both sides share)
   const bool overlap = g.use_overlap && full && !mts && do_real && !g.has_metal &&
@@ -324,6 +328,39 @@ int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real, bo
       for (int k = 0; k < 9; ++k) st[k] += strec[k];
       pair_scalars(g.hsc, e6, st);
     }
+  } else if (mts_side) {
+    struct SideWork {
+      double *erc, *vrc, *strec, *st;
+    } work{&erc, &vrc, strec, st};
+    struct SideGuard {
+      ~SideGuard() {
+        g.stream = g.main_stream;
+        g.side = false;
+        g.side_hook = nullptr;
+        if (g.join_pending) {  // left by an error between the fork and the join
+          cudaStreamWaitEvent(g.main_stream, g.ev_join, 0);
+          g.join_pending = false;
+        }
+      }
+    } guard;
+    GB_CUDA(cudaEventRecord(g.ev_fork, g.main_stream));
+    g.side_hook_arg = &work;
+    g.side_hook = [](void* a) {
+      SideWork* w = static_cast<SideWork*>(a);
+      GB_CUDA(cudaStreamWaitEvent(g.side_stream, g.ev_fork, 0));
+      g.stream = g.side_stream;
+      g.side = true;
+      mts_coarse();
+      mts_inner(w->erc, w->vrc, w->strec);
+      for (int k = 0; k < 9; ++k) w->st[k] += w->strec[k];  // before the pair stress joins st
+      GB_CUDA(cudaEventRecord(g.ev_join, g.side_stream));
+      g.stream = g.main_stream;
+      g.side = false;
+      g.join_pending = true;
+    };
+    if (do_real && (g.has_coul || g.has_vdw)) pair_forces(e6, st);
+    run_side_hook();  // (when pair_forces had nothing to launch)
+    side_join();
   } else {
     if (full) spme_forces(&erc, &vrc, strec);
     else if (mts) mts_inner(&erc, &vrc, strec);
@@ -468,6 +505,13 @@ double* gb_blkacc(int n) {
     GB_CUDA(cudaMalloc(&buf, sizeof(double) * cap));
   }
   return buf;
+}
+
+void run_side_hook() {
+  if (!g.side_hook) return;
+  void (*h)(void*) = g.side_hook;
+  g.side_hook = nullptr;
+  h(g.side_hook_arg);
 }
 
 void side_join() {

@@ -105,6 +105,10 @@ struct Dev {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool side = false, join_pending = false, use_overlap = true;
   int pair_apw = -1;  // atoms per warp of the sorted pair kernels' CTAs (GB_PAIR_APW; 0: resident CTAs, -1: by form)
+  // work to put on the side stream once the pair kernel is launched (run by pair_forces
+  // before it joins the side stream)
+  void (*side_hook)(void*) = nullptr;
+  void* side_hook_arg = nullptr;
   int pair_nt = 0;  // threads per CTA of the sorted pair kernels: 256 or 1024 (GB_PAIR_NT), 0: by form
   int nsm = 0;
   int64_t launches = 0;
@@ -380,6 +384,7 @@ double* gb_blkacc(int n);         // per-block accumulator scratch with n double
 void gb_reduce_blocks(const double* blk, int nblocks, int nv, double* out_dev);  // sums into out_dev[0..nv)
 int* gb_scan_scratch(int n);
 void side_join();                 // the first stream waits for the side stream (no-op without a fork)
+void run_side_hook();             // enqueue the pending side-stream work (g.side_hook), if any
 
 // module entry points (host)
 int list_relocate_and_halo();     // pbcshift + halo + vnl_set_check (gb_list.cu)
@@ -435,6 +440,7 @@ bool mts_active();
 void mts_set_no_network(bool on);  // ablation: inner steps use the coarse-grid force alone
 float* mts_rec_out();             // SPME per-atom reciprocal forces go here when active
 bool mts_step_needs_spme();
+void mts_coarse();
 void mts_after_full(double erc, double vrc, const double* strec);
 void mts_inner(double* erc, double* vrc, double* stress9);
 void mts_stats(double* out, int nv);

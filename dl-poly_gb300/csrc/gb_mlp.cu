@@ -1653,13 +1653,20 @@ float* mts_rec_out() { return mts_active() ? M.frec : nullptr; }
 
 // at the start of the force evaluation of an MD step: the coarse-grid forces
 // of this step, and whether the step needs the full SPME
+// whether this MD step runs the full SPME (host state only: the step count, training,
+// the fallback, the cycle position)
 bool mts_step_needs_spme() {
   ++M.step;
+  if (!M.have_t0) return true;
+  return training_now() || M.fallback || M.s + 1 >= g.mts_k;
+}
+
+// the coarse-grid reciprocal forces of the current positions (every MD step: inner steps
+// build S from them, full steps label and check against them)
+void mts_coarse() {
   double st[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   spme_coarse_forces(&M.ec, &M.vc, st, M.fc);
   for (int k = 0; k < 9; ++k) M.stc[k] = st[k];
-  if (!M.have_t0) return true;
-  return training_now() || M.fallback || M.s + 1 >= g.mts_k;
 }
 
 // after a full force evaluation of an MD step (SPME ran and its force is in the

@@ -1167,6 +1167,7 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   prof_begin(P_PAIR);
   kern<<<nb, nt, 0, st>>>(A, pg);
   GB_LAUNCHED();
+  run_side_hook();  // side-stream work enqueued behind the pair kernel's launch
   side_join();  // the reciprocal-space forces are in place before the pair forces join them
   k_slot_stress_fold<<<nbs, 256, 0, st>>>(g.natms, g.sc, g.at_list, g.src, g.x, g.y, g.z, g.fixs,
                                           (unsigned long long*)g.fixp, blks);
@@ -1222,7 +1223,10 @@ void pair_forces(double* eng6, double* stress9) {
   const int nb2 = nblocks(g.natms, 128);
   GB_CUDA(cudaMemsetAsync(&g.sc->npairs_list, 0, 2 * sizeof(unsigned long long), st));
   const bool sorted = g.spos_valid && g.use_sorted && !(g.precision == GB_FP64 && g.fp64_native);
-  if (!sorted) side_join();  // the atom-index kernels write the force arrays directly
+  if (!sorted) {  // the atom-index kernels write the force arrays directly
+    run_side_hook();
+    side_join();
+  }
   if (sorted) {
     pair_forces_sorted(pg, nb2);
   } else if (g.precision == GB_FP64 && !g.fp64_native) {
