@@ -1155,6 +1155,8 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   // GB_PAIR_APW sets the atoms per warp (0: one resident set).
   int apw = mixed ? 16 : 0;
   if (g.pair_apw >= 0) apw = g.pair_apw;
+  // a small system keeps at least one CTA per resident slot (fewer atoms per warp)
+  if (apw > 0) apw = std::max(1, std::min(apw, g.natms / ((nt / 32) * std::max(1, occ) * g.nsm)));
   const int nb = apw > 0 ? std::max(1, nblocks((long long)g.natms, (nt / 32) * apw))
                          : std::max(1, std::min(nblocks((long long)g.mxatms * 32, nt), occ * g.nsm));
   const int nbs = std::max(1, std::min(nblocks(g.mxatms, 256), 4 * g.nsm));  // stress blocks
