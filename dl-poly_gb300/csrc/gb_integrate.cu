@@ -66,30 +66,35 @@ __global__ void k_vv2(int n, const double* __restrict__ hdw, const double* __res
   }
 }
 
+// m v (x) v summed over the atoms (kinetics.F90:218-262): a grid-stride loop, so each
+// thread reduces its own atoms in registers and the FP64 block reduction runs once per
+// thread rather than once per atom (the FP64 unit bounds this kernel)
 __global__ void k_kinstress(int n, const double* w, const int* lfrzn, const double* vx, const double* vy,
                             const double* vz, double* blk) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
   double a[6] = {0, 0, 0, 0, 0, 0};
-  if (i < n && lfrzn[i] == 0) {
-    double m = w[i];
-    a[0] = m * vx[i] * vx[i]; a[1] = m * vx[i] * vy[i]; a[2] = m * vx[i] * vz[i];
-    a[3] = m * vy[i] * vy[i]; a[4] = m * vy[i] * vz[i]; a[5] = m * vz[i] * vz[i];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (lfrzn[i] != 0) continue;
+    const double m = w[i], u = vx[i], v = vy[i], t = vz[i];
+    a[0] += m * u * u; a[1] += m * u * v; a[2] += m * u * t;
+    a[3] += m * v * v; a[4] += m * v * t; a[5] += m * t * t;
   }
   block_reduce_store<6>(a, blk);
 }
 
-// largest |r - r_checkpoint| with minimum image; doubles >= 0 order as their bits
+// largest |r - r_checkpoint|^2 with minimum image, over a grid-stride loop; the caller takes
+// the square root of the maximum (the square root is monotone and correctly rounded, so
+// it equals the largest of the per-atom square roots); doubles >= 0 order as their bits
 __global__ void k_maxdisp(int n, const double* x, const double* y, const double* z, const double* xb,
                           const double* yb, const double* zb, double c0, double a0, unsigned long long* out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double r = 0.0;
-  if (i < n) {
-    double dx = image1(x[i] - xb[i], c0, a0), dy = image1(y[i] - yb[i], c0, a0), dz = image1(z[i] - zb[i], c0, a0);
-    r = sqrt(dx * dx + dy * dy + dz * dz);
+  double r2 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double dx = image1(x[i] - xb[i], c0, a0), dy = image1(y[i] - yb[i], c0, a0),
+                 dz = image1(z[i] - zb[i], c0, a0);
+    r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(r));
+  for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(r2));
 }
 
 __global__ void k_zero3(int n, double* a, double* b, double* c) {
@@ -673,11 +678,11 @@ void integ_forces_to_fp64() {
 
 int integ_vnl_check() {
   GB_CUDA(cudaMemsetAsync(&g.sc->maxdisp, 0, sizeof(double), g.stream));
-  k_maxdisp<<<nblocks(g.natms, 256), 256, 0, g.stream>>>(g.natms, g.x, g.y, g.z, g.xbg, g.ybg, g.zbg, g.cell[0],
-                                                          1.0 / g.cell[0], (unsigned long long*)&g.sc->maxdisp);
+  k_maxdisp<<<std::min(nblocks(g.natms, 256), 2 * g.nsm), 256, 0, g.stream>>>(
+      g.natms, g.x, g.y, g.z, g.xbg, g.ybg, g.zbg, g.cell[0], 1.0 / g.cell[0], (unsigned long long*)&g.sc->maxdisp);
   GB_LAUNCHED();
   gb_sync_scalars();
-  return g.hsc->maxdisp >= std::nextafter(0.5, 0.0) * g.p.rpad ? 1 : 0;
+  return std::sqrt(g.hsc->maxdisp) >= std::nextafter(0.5, 0.0) * g.p.rpad ? 1 : 0;
 }
 
 static void con_args(ConArgs& A) {
@@ -787,7 +792,7 @@ void integ_vv(int stage, double* strkin, double* engke, int* iters, double* virc
     prof_end(P_VV);
     integ_rattle_launch();
     if (!thermo_vv2_finish(strkin, engke)) {
-      const int nb = nblocks(n, 256);
+      const int nb = std::min(nblocks(n, 256), 2 * g.nsm);
       double* blk = gb_blkacc(nb * 6);
       k_kinstress<<<nb, 256, 0, st>>>(n, g.weight, g.lfrzn, g.vx, g.vy, g.vz, blk);
       GB_LAUNCHED();
