@@ -282,9 +282,9 @@ int compute_forces(double* eng8, double* stress9, bool do_spme, bool do_real, bo
   double erc = 0, vrc = 0;
   double e6[6] = {0, 0, 0, 0, 0, 0};
   integ_zero_forces();
-  if (g.precision == GB_MIXED || !g.fp64_native) list_pos_f32();  // FP32 hi + lo positions
-  if (do_real && g.spos_valid && g.use_sorted && (g.precision == GB_MIXED || !g.fp64_native))
-    list_pos_sorted();  // the same per sorted position, for the sorted-position pair kernels
+  // FP32 hi + lo positions by atom index and, for the sorted-position pair kernels, the same
+  // per sorted position (one pass)
+  if (g.precision == GB_MIXED || !g.fp64_native) list_pos_records(do_real && g.spos_valid && g.use_sorted);
   const bool mts = md_step && do_spme && mts_active();
   const bool full = mts ? mts_step_needs_spme() : (do_spme && g.has_coul);
   // a learned-MTS inner step: the coarse grid, the network's inputs and inference go to the

@@ -391,8 +391,7 @@ int list_relocate_and_halo();     // pbcshift + halo + vnl_set_check (gb_list.cu
 int list_refresh_halo();          // refresh halo positions (gb_list.cu)
 int list_build();                 // binning + pairs (gb_list.cu)
 void list_setup();                // link-cell geometry (gb_list.cu)
-void list_pos_f32();              // FP32 copy of positions and charges (mixed path)
-void list_pos_sorted();           // per sorted position: FP32 hi/lo positions, charge, type
+void list_pos_records(bool sorted);  // FP32 hi/lo positions by atom index and (sorted) per sorted position
 void scan_exclusive(const int* in, int* out, int n);
 void pair_forces(double* eng6, double* stress9);  // gb_pair.cu (adds into forces)
 void pair_setup();                // gb_pair.cu: per-key constants

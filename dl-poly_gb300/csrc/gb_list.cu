@@ -695,34 +695,29 @@ __global__ void k_list_reorder(int natms, int* list, int ld, int* spos, int ldt,
 // separations to FP32 precision of the separation itself.
 // FP32 hi parts with the charge, and the lo remainders with the atom type in the
 // fourth word (bit pattern), so a pair reads everything about j in two 16-byte loads
-__global__ void k_pos_f32(const DevScalars* sc, const double* x, const double* y, const double* z,
-                          const double* q, const int* ltype, float4* xf, float4* xlo, float2* qdf) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Both records in one pass over the atoms (the FP64 values converted once): by atom index
+// (xf, xlo: the type in xlo.w) and, for the sorted-position pair kernels, per sorted
+// position sorted_pos[i] (xhs, xls: the charge's remainder in xls.w, tys)
+__global__ void k_pos_records(const DevScalars* sc, const int* __restrict__ sorted_pos, const double* __restrict__ x,
+                              const double* __restrict__ y, const double* __restrict__ z, const double* __restrict__ q,
+                              const int* __restrict__ ltype, float4* xf, float4* xlo, float2* qdf, float4* xhs,
+                              float4* xls, unsigned char* tys) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= sc->nlast) return;
-  const float hx = (float)x[i], hy = (float)y[i], hz = (float)z[i];
-  xf[i] = make_float4(hx, hy, hz, (float)q[i]);
-  xlo[i] = make_float4((float)(x[i] - (double)hx), (float)(y[i] - (double)hy), (float)(z[i] - (double)hz),
-                       __int_as_float(ltype[i]));
-  if (qdf) {  // the charge as a double-float (FP64 form)
-    const float qh = (float)q[i];
-    qdf[i] = make_float2(qh, (float)(q[i] - (double)qh));
-  }
-}
-
-// Per sorted position (cell order): FP32 high parts (x, y, z, q), the remainders of
-// the FP64 values and the atom type, read by the cell-tile pair kernels.
-__global__ void k_pos_sorted(const DevScalars* sc, const int* __restrict__ at_list, const double* __restrict__ x,
-                             const double* __restrict__ y, const double* __restrict__ z, const double* __restrict__ q,
-                             const int* __restrict__ ltype, float4* xhs, float4* xls, unsigned char* tys) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= sc->nlast) return;
-  const int a = at_list[p];
-  const double xa = x[a], ya = y[a], za = z[a], qa = q[a];
+  const double xa = x[i], ya = y[i], za = z[i], qa = q[i];
+  const int ta = ltype[i];
   const float hx = (float)xa, hy = (float)ya, hz = (float)za, hq = (float)qa;
-  xhs[p] = make_float4(hx, hy, hz, hq);
-  xls[p] = make_float4((float)(xa - (double)hx), (float)(ya - (double)hy), (float)(za - (double)hz),
-                       (float)(qa - (double)hq));
-  tys[p] = (unsigned char)ltype[a];
+  const float lx = (float)(xa - (double)hx), ly = (float)(ya - (double)hy), lz = (float)(za - (double)hz);
+  xf[i] = make_float4(hx, hy, hz, hq);
+  xlo[i] = make_float4(lx, ly, lz, __int_as_float(ta));
+  const float lq = (float)(qa - (double)hq);
+  if (qdf) qdf[i] = make_float2(hq, lq);
+  if (xhs) {
+    const int p = sorted_pos[i];
+    xhs[p] = make_float4(hx, hy, hz, hq);
+    xls[p] = make_float4(lx, ly, lz, lq);
+    tys[p] = (unsigned char)ta;
+  }
 }
 
 inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
@@ -1063,15 +1058,11 @@ int list_build() {
   return GB_OK;
 }
 
-void list_pos_sorted() {
-  k_pos_sorted<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(g.sc, g.at_list, g.x, g.y, g.z, g.chge, g.ltype, g.xhs,
-                                                            g.xls, g.tys);
+void list_pos_records(bool sorted) {
+  k_pos_records<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(
+      g.sc, g.sorted_pos, g.x, g.y, g.z, g.chge, g.ltype, g.xf, g.xlo, g.precision == GB_FP64 ? g.qdf : nullptr,
+      sorted ? g.xhs : nullptr, g.xls, g.tys);
   GB_LAUNCHED();
 }
 
-void list_pos_f32() {
-  k_pos_f32<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(g.sc, g.x, g.y, g.z, g.chge, g.ltype, g.xf, g.xlo,
-                                                         g.precision == GB_FP64 ? g.qdf : nullptr);
-  GB_LAUNCHED();
-}
 
