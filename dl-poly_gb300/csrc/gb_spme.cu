@@ -24,6 +24,7 @@
 // inside the spherical cut) and accumulates the reciprocal stress, then runs
 // the inverse z transform on the same tile before writing it back.
 #include <cfloat>
+#include <climits>
 #include <cmath>
 
 #include "gb_common.cuh"
@@ -83,8 +84,8 @@ __device__ __forceinline__ void bspline_vals(T w, int p_rt, T* m /*p*/, T* dm /*
 template <typename T, int P>
 __global__ void k_spme_prep(int natms, const double* __restrict__ x, const double* __restrict__ y,
                             const double* __restrict__ z, const double* __restrict__ q, SpmeGeom sg, T* spl,
-                            int* nidx, int* brick_of, int* brick_count, int* gidx, float* gw, float* gwl,
-                            float2* gq) {
+                            int* nidx, int* brick_of, int* brick_count, int* gidx, float* gw, float2* gq,
+                            T* gsp) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natms) return;
   const int p = P ? P : sg.p;
@@ -94,26 +95,39 @@ __global__ void k_spme_prep(int natms, const double* __restrict__ x, const doubl
     double fl = floor(u);
     int n = (int)fl;
     T w = (T)(u - fl);
+    double tr = fl;
     if (gidx) {
       // the gather's own convention: Int(u), u - Aint(u) (ewald_spole.F90:387, bspline.F90:216)
-      const double tr = trunc(u);
+      tr = trunc(u);
       int g0 = ((int)tr - p + 1) % sg.K[d];
       if (g0 < 0) g0 += sg.K[d];
       gidx[3 * i + d] = g0;
-      // u - tr is exact; the double-float gather also takes its low part
-      if (gwl) df_split(u - tr, &gw[3 * i + d], &gwl[3 * i + d]);
-      else gw[3 * i + d] = (float)(u - tr);
+      if (gw) gw[3 * i + d] = (float)(u - tr);
     }
-    T m[PMAX];
-    bspline_vals<T, P>(w, p, m, nullptr);
+    T m[PMAX], dm[PMAX];
+    bspline_vals<T, P>(w, p, m, gsp ? dm : nullptr);
     // the z splines carry the charge: the spreads weight a point by Mx (My (Mz q))
+    const T qT = d == 2 ? (T)q[i] : T(1);
     if (d == 2) {
-      const T qT = (T)q[i];
 #pragma unroll
       for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t] * qT;
     } else {
 #pragma unroll
       for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t];
+    }
+    if (gsp) {
+      // the double-float gather's splines, values then derivatives, z ones times the
+      // charge, component-major ([value, derivative][x, y, z][point][atom]: coalesced
+      // here and in the gather's copy).  u - Aint(u) differs from u - floor(u) only for
+      // u < 0 (an atom just below the cell's lower face)
+      if (tr != fl) bspline_vals<T, P>((T)(u - tr), p, m, dm);
+      T* o = gsp + (size_t)d * p * natms + i;
+      const size_t dstep = (size_t)3 * p * natms;
+#pragma unroll
+      for (int t = 0; t < p; ++t) {
+        o[(size_t)t * natms] = d == 2 ? m[t] * qT : m[t];
+        o[dstep + (size_t)t * natms] = d == 2 ? dm[t] * qT : dm[t];
+      }
     }
     int nw = n % sg.K[d];
     if (nw < 0) nw += sg.K[d];
@@ -508,99 +522,177 @@ __global__ void __launch_bounds__(256, 4) k_spme_gather_f32(int natms, const flo
   block_reduce_store<4>(acc, blk);
 }
 
-// FP64 form, the same warp-per-atom layout in double-float.  A warp takes 8 atoms at a
-// time: 24 lanes build the splines of the 8 atoms x 3 dimensions in parallel, then the
-// warp gathers the atoms one after another.  Lane pr = (j, k) of the p x p (x, y) rows
-// sums its z column against Mz and dMz, then weights the two sums with its x/y spline
-// products (separable in z, so 2 products per grid point); the four per-atom sums are
-// combined by a reduce-scatter over the warp (two values after the first butterfly
-// level, one after the second), which leaves the energy sum in lane 0 and the x, y, z
-// force sums in lanes 8, 16, 24.  No FP64 instruction: forces leave as double-floats.
+// a * b as an unnormalised compensated pair: the exact product's high part and, in the
+// correction, its rounding error and the cross terms
+__device__ __forceinline__ dacc dacc_prod(df x, df y) {
+  const df p = two_prod(x.hi, y.hi);
+  dacc r;
+  r.s = p.hi;
+  r.c = __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, p.lo));
+  return r;
+}
+
+// a + b of two compensated pairs
+__device__ __forceinline__ dacc dacc_sum(dacc a, dacc b) {
+  const df u = two_sum(a.s, b.s);
+  dacc r;
+  r.s = u.hi;
+  r.c = __fadd_rn(__fadd_rn(a.c, b.c), u.lo);
+  return r;
+}
+
+__device__ __forceinline__ dacc shfl_xor_dacc(dacc v, int o) {
+  dacc r;
+  r.s = __shfl_xor_sync(0xffffffffu, v.s, o);
+  r.c = __shfl_xor_sync(0xffffffffu, v.c, o);
+  return r;
+}
+
+__device__ __forceinline__ df ld_df(const dfr* p) {
+  const float2 v = *reinterpret_cast<const float2*>(p);
+  return df_make(v.x, v.y);
+}
+
+// FP64 form, the same warp-per-atom layout in double-float.  The splines come from the
+// preparation kernel (values and derivatives in the gather's truncation convention, the z
+// ones times the charge, component-major); a warp copies those of 8 atoms at a time into
+// shared memory (64 contiguous bytes per component) and gathers the atoms one after
+// another.  Lane (j, k) of the p x p
+// (x, y) rows sums its z columns against Mz q and dMz q as compensated dot products (each
+// exact product's high part enters a two-sum, its error and cross terms the correction;
+// 2 products per grid point, the z-plane offsets computed once per atom).  For p = 8 a
+// lane holds the columns (j, k) and (j, k + 4), which it contracts with My and dMy, then
+// with Mx and dMx; otherwise each column is weighted with its x/y spline products.  The
+// four per-atom sums (energy, x, y, z) stay unnormalised compensated pairs through a
+// reduce-scatter over the warp (two values after the first butterfly level, one after
+// the second) that leaves them in lanes 0, 8, 16, 24.  No FP64 instruction: forces leave
+// as double-floats.
 template <int P>
 __global__ void __launch_bounds__(256) k_spme_gather_wdf(int natms, SpmeGeom sg, const int* __restrict__ gidx,
-                                                         const float* __restrict__ gw, const float* __restrict__ gwl,
+                                                         const dfr* __restrict__ gsp,
                                                          const float2* __restrict__ gq, const dfr* __restrict__ phi,
                                                          float2 rk0, float2 rk1, float2 rk2,
                                                          float2* __restrict__ fout, double* blk) {
-  __shared__ dfr sp[8][GATHER_AB][2][3][P];  // per warp and atom: value/derivative, dimension, point
+  constexpr int NS = 6 * P;  // spline components per atom: [value, derivative][x, y, z][point]
+  static_assert(GATHER_AB == 8, "8 atoms per batch");
+  __shared__ __align__(16) dfr sp[8][NS][GATHER_AB];  // per warp: component, atom
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int K0 = sg.K[0], K1 = sg.K[1], K2 = sg.K[2];
+  const int K01 = K0 * K1;
   dacc acc[4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) { acc[c].s = 0.f; acc[c].c = 0.f; }
   for (int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * GATHER_AB; base < natms;
        base += nwarps * GATHER_AB) {
-    if (lane < 3 * GATHER_AB) {
-      const int a = lane / 3, d = lane - 3 * a, i = base + a;
-      if (i < natms) {
-        dfr m[PMAX], dm[PMAX];
-        bspline_vals<dfr, P>(dfr(gw[3 * i + d], gwl[3 * i + d]), P, m, dm);
+    const int na = min(GATHER_AB, natms - base);
 #pragma unroll
-        for (int t = 0; t < P; ++t) { sp[wid][a][0][d][t] = m[t]; sp[wid][a][1][d][t] = dm[t]; }
-      }
+    for (int e = lane; e < NS * GATHER_AB; e += 32) {
+      const int c = e >> 3, a = e & 7;
+      if (a < na)
+        reinterpret_cast<float2*>(&sp[wid][c][a])[0] =
+            reinterpret_cast<const float2*>(gsp + (size_t)c * natms + base + a)[0];
     }
     __syncwarp();
-    const int na = min(GATHER_AB, natms - base);
     for (int a = 0; a < na; ++a) {
       const int i = base + a;
-      const float2 qv = gq[i];
-      if (qv.x == 0.f) {  // uniform over the warp
+      if (gq[i].x == 0.f) {  // uniform over the warp
         if (lane < 3) fout[3 * i + lane] = make_float2(0.f, 0.f);
         continue;
       }
       const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
-      dfr v[4];  // energy, x, y, z sums
+      // spline component (value or derivative, dimension, point) of this atom
+      auto spv = [&](int part, int d, int t) { return ld_df(&sp[wid][(part * 3 + d) * P + t][a]); };
+      int zo[P];
 #pragma unroll
-      for (int pr = lane; pr < P * P; pr += 32) {
-        const int j = pr % P, k = pr / P;
+      for (int l = 0; l < P; ++l) {
+        int zz = gz + l;
+        if (zz >= K2) zz -= K2;
+        zo[l] = zz * K01;
+      }
+      dacc v[4];  // energy, x, y, z sums of this lane
+      if constexpr (P == 8) {
+        const int j = lane & 7, k = lane >> 3;
         int xx = gx + j; if (xx >= K0) xx -= K0;
-        int yy = gy + k; if (yy >= K1) yy -= K1;
-        const dfr* col = phi + (size_t)yy * K0 + xx;
-        // the z column as two compensated dot products: each exact product's high
-        // part enters a two-sum, its error and cross terms the correction, and the
-        // pair is renormalised once per column
-        dacc za, zc;
-        za.s = za.c = zc.s = zc.c = 0.f;
+        int y0 = gy + k; if (y0 >= K1) y0 -= K1;
+        int y1 = gy + k + 4; if (y1 >= K1) y1 -= K1;
+        const dfr* c0 = phi + (y0 * K0 + xx);
+        const dfr* c1 = phi + (y1 * K0 + xx);
+        dacc a0, b0, a1, b1;
+        a0.s = a0.c = b0.s = b0.c = a1.s = a1.c = b1.s = b1.c = 0.f;
 #pragma unroll
         for (int l = 0; l < P; ++l) {
-          int zz = gz + l; if (zz >= K2) zz -= K2;
-          const df ph = to_df(col[(size_t)zz * K1 * K0]);
-          dacc_add_prod(za, to_df(sp[wid][a][0][2][l]), ph);
-          dacc_add_prod(zc, to_df(sp[wid][a][1][2][l]), ph);
+          const df mz = spv(0, 2, l), dmz = spv(1, 2, l);
+          const df p0 = ld_df(c0 + zo[l]), p1 = ld_df(c1 + zo[l]);
+          dacc_add_prod(a0, mz, p0);
+          dacc_add_prod(b0, dmz, p0);
+          dacc_add_prod(a1, mz, p1);
+          dacc_add_prod(b1, dmz, p1);
         }
-        const dfr ca = to_dfr(two_sum(za.s, za.c)), cc = to_dfr(two_sum(zc.s, zc.c));
-        const dfr mx = sp[wid][a][0][0][j], dmx = sp[wid][a][1][0][j];
-        const dfr my = sp[wid][a][0][1][k], dmy = sp[wid][a][1][1][k];
-        const dfr w0 = mx * my;
-        v[0] = fma(w0, ca, v[0]);
-        v[1] = fma(dmx * my, ca, v[1]);
-        v[2] = fma(mx * dmy, ca, v[2]);
-        v[3] = fma(w0, cc, v[3]);
+        // y: My and dMy against the two columns' sums
+        const df my0 = spv(0, 1, k), dmy0 = spv(1, 1, k);
+        const df my1 = spv(0, 1, k + 4), dmy1 = spv(1, 1, k + 4);
+        const df ca0 = df_make(a0.s, a0.c), cc0 = df_make(b0.s, b0.c);
+        const df ca1 = df_make(a1.s, a1.c), cc1 = df_make(b1.s, b1.c);
+        dacc A = dacc_prod(my0, ca0), B = dacc_prod(dmy0, ca0), C = dacc_prod(my0, cc0);
+        dacc_add_prod(A, my1, ca1);
+        dacc_add_prod(B, dmy1, ca1);
+        dacc_add_prod(C, my1, cc1);
+        // x: Mx and dMx
+        const df mx = spv(0, 0, j), dmx = spv(1, 0, j);
+        const df Ad = df_make(A.s, A.c);
+        v[0] = dacc_prod(mx, Ad);
+        v[1] = dacc_prod(dmx, Ad);
+        v[2] = dacc_prod(mx, df_make(B.s, B.c));
+        v[3] = dacc_prod(mx, df_make(C.s, C.c));
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) { v[c].s = 0.f; v[c].c = 0.f; }
+#pragma unroll
+        for (int pr = lane; pr < P * P; pr += 32) {
+          const int j = pr % P, k = pr / P;
+          int xx = gx + j; if (xx >= K0) xx -= K0;
+          int yy = gy + k; if (yy >= K1) yy -= K1;
+          const dfr* col = phi + (yy * K0 + xx);
+          dacc za, zc;
+          za.s = za.c = zc.s = zc.c = 0.f;
+#pragma unroll
+          for (int l = 0; l < P; ++l) {
+            const df ph = ld_df(col + zo[l]);
+            dacc_add_prod(za, spv(0, 2, l), ph);
+            dacc_add_prod(zc, spv(1, 2, l), ph);
+          }
+          const df ca = df_make(za.s, za.c), cc = df_make(zc.s, zc.c);
+          const df mx = spv(0, 0, j), dmx = spv(1, 0, j);
+          const df my = spv(0, 1, k), dmy = spv(1, 1, k);
+          const df w0 = df_mul(mx, my);
+          dacc_add_prod(v[0], w0, ca);
+          dacc_add_prod(v[1], df_mul(dmx, my), ca);
+          dacc_add_prod(v[2], df_mul(mx, dmy), ca);
+          dacc_add_prod(v[3], w0, cc);
+        }
       }
       // reduce-scatter: level 16 keeps (v0, v1) in the lower half-warp, (v2, v3) in the upper
       const bool up16 = lane & 16, up8 = lane & 8;
-      dfr k0 = up16 ? v[2] : v[0], k1 = up16 ? v[3] : v[1];
-      const dfr s0 = up16 ? v[0] : v[2], s1 = up16 ? v[1] : v[3];
-      k0 += dfr(__shfl_xor_sync(0xffffffffu, s0.hi, 16), __shfl_xor_sync(0xffffffffu, s0.lo, 16));
-      k1 += dfr(__shfl_xor_sync(0xffffffffu, s1.hi, 16), __shfl_xor_sync(0xffffffffu, s1.lo, 16));
-      dfr r = up8 ? k1 : k0;
-      const dfr sr = up8 ? k0 : k1;
-      r += dfr(__shfl_xor_sync(0xffffffffu, sr.hi, 8), __shfl_xor_sync(0xffffffffu, sr.lo, 8));
+      dacc k0 = up16 ? v[2] : v[0], k1 = up16 ? v[3] : v[1];
+      const dacc s0 = up16 ? v[0] : v[2], s1 = up16 ? v[1] : v[3];
+      k0 = dacc_sum(k0, shfl_xor_dacc(s0, 16));
+      k1 = dacc_sum(k1, shfl_xor_dacc(s1, 16));
+      dacc r = up8 ? k1 : k0;
+      r = dacc_sum(r, shfl_xor_dacc(up8 ? k0 : k1, 8));
 #pragma unroll
-      for (int o = 4; o > 0; o >>= 1)
-        r += dfr(__shfl_xor_sync(0xffffffffu, r.hi, o), __shfl_xor_sync(0xffffffffu, r.lo, o));
-      // lane 0: energy; lanes 8, 16, 24: x, y, z
+      for (int o = 4; o > 0; o >>= 1) r = dacc_sum(r, shfl_xor_dacc(r, o));
+      // lane 0: energy; lanes 8, 16, 24: x, y, z (the charge is in the z splines)
       if ((lane & 7) == 0) {
         const int comp = lane >> 3;
-        const dfr qr = dfr(qv.x, qv.y) * r;
+        const df qr = two_sum(r.s, r.c);
         if (comp == 0) {
-          dacc_add(acc[0], to_df(qr));
+          dacc_add(acc[0], qr);
         } else {
           const float2 rk = comp == 1 ? rk0 : (comp == 2 ? rk1 : rk2);
-          const dfr f = -(qr * dfr(rk.x, rk.y));
+          const df f = df_neg(df_mul(qr, df_make(rk.x, rk.y)));
           fout[3 * i + comp - 1] = make_float2(f.hi, f.lo);
-          dacc_add(acc[comp], to_df(f));
+          dacc_add(acc[comp], f);
         }
       }
     }
@@ -713,8 +805,9 @@ struct SpmeGrid {
   double* fspme = nullptr;     // 3*natms reciprocal forces (before scale, net removal)
   void* spread_ext = nullptr;  // per-brick spread tiles (nbricks x (B+p-1)^3)
   int* gidx = nullptr;         // warp gather: first grid index per dimension (truncation convention)
-  float* gw = nullptr;         // warp gather: fractional coordinate per dimension (3n), then its low parts (3n),
-                               // then the double-float charges (2n)
+  float* gw = nullptr;         // warp gather: fractional coordinate per dimension (3n), then (at 6n) the
+                               // double-float charges (2n)
+  double* gsp = nullptr;       // double-float gather (main grid): natms x 6p splines (dfr)
   float* fout_f = nullptr;     // warp gather: unscaled reciprocal forces
   // double-float copies for the FP64 form (main grid): influence function, stress
   // factor and twiddles; the grids themselves reuse the FP64 buffers (same sizes)
@@ -782,7 +875,7 @@ int fft_threads(const FftPlan& pl, int nlines) {
 void grid_free(SpmeGrid& S) {
   void* ptrs[] = {S.spl, S.nidx, S.brick_of, S.brick_count, S.brick_start, S.brick_fill, S.brick_atoms, S.Q, S.G,
                   S.Qf, S.Gf, S.theta, S.psi, S.theta_f, S.psi_f, S.tw[0], S.tw[1], S.tw[2], S.twf[0], S.twf[1],
-                  S.twf[2], S.twh, S.twhf, S.fspme, S.spread_ext, S.gidx, S.gw, S.fout_f, S.theta_d, S.psi_d,
+                  S.twf[2], S.twh, S.twhf, S.fspme, S.spread_ext, S.gidx, S.gw, S.gsp, S.fout_f, S.theta_d, S.psi_d,
                   S.tw_d[0], S.tw_d[1], S.tw_d[2], S.twh_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -832,6 +925,7 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64, int bpref) {
   }
   S.sg.p = p;
   const size_t NG = (size_t)S.K[0] * S.K[1] * S.K[2];
+  if (NG > (size_t)INT_MAX) throw (int)GB_ERR_ARG;  // the gathers index grid points with int offsets
   const size_t n = (size_t)g.natms;
   GB_CUDA(cudaMalloc(&S.spl, sizeof(double) * n * 3 * p));
   GB_CUDA(cudaMalloc(&S.nidx, sizeof(int) * 3 * n));
@@ -849,6 +943,7 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64, int bpref) {
   GB_CUDA(cudaMalloc(&S.fspme, sizeof(double) * 3 * n));
   GB_CUDA(cudaMalloc(&S.gidx, sizeof(int) * 3 * n));
   GB_CUDA(cudaMalloc(&S.gw, sizeof(float) * 8 * n));
+  if (fp64) GB_CUDA(cudaMalloc(&S.gsp, sizeof(double) * n * 6 * p));
   GB_CUDA(cudaMalloc(&S.fout_f, sizeof(float) * 3 * n));
   {
     const size_t tsize = (size_t)(S.B[0] + p - 1) * (S.B[1] + p - 1) * (S.B[2] + p - 1);
@@ -1025,9 +1120,9 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   const bool warp_gather = (!F64 || DF) && (p == 8 || p == 6);
   auto prep = p == 8 ? k_spme_prep<T, 8> : (p == 6 ? k_spme_prep<T, 6> : k_spme_prep<T, 0>);
   prep<<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, spl, S.nidx, S.brick_of, S.brick_count,
-                                         warp_gather ? S.gidx : nullptr, warp_gather ? S.gw : nullptr,
-                                         warp_gather && DF ? S.gw + 3 * (size_t)n : nullptr,
-                                         warp_gather && DF ? reinterpret_cast<float2*>(S.gw + 6 * (size_t)n) : nullptr);
+                                         warp_gather ? S.gidx : nullptr, warp_gather && !DF ? S.gw : nullptr,
+                                         warp_gather && DF ? reinterpret_cast<float2*>(S.gw + 6 * (size_t)n) : nullptr,
+                                         warp_gather && DF ? reinterpret_cast<T*>(S.gsp) : nullptr);
   GB_LAUNCHED();
 
   scan_exclusive(S.brick_count, S.brick_start, S.nbricks + 1);
@@ -1124,7 +1219,7 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
     auto kern = p == 8 ? k_spme_gather_wdf<8> : k_spme_gather_wdf<6>;
     float2 rkd[3];
     for (int a = 0; a < 3; ++a) df_split(rk[a], &rkd[a].x, &rkd[a].y);
-    kern<<<nbg, 256, 0, st>>>(n, S.sg, S.gidx, S.gw, S.gw + 3 * (size_t)n,
+    kern<<<nbg, 256, 0, st>>>(n, S.sg, S.gidx, reinterpret_cast<const dfr*>(S.gsp),
                               reinterpret_cast<const float2*>(S.gw + 6 * (size_t)n), reinterpret_cast<const dfr*>(Q),
                               rkd[0], rkd[1], rkd[2], reinterpret_cast<float2*>(S.fspme), blkg);
   } else if (warp_gather) {
