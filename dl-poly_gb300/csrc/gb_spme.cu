@@ -181,28 +181,46 @@ constexpr int SPREAD_NT = 512;             // threads of a tile-spread CTA
 constexpr int SPREAD_NW = SPREAD_NT / 32;  // its warps (a power of two: plane owner = z & (NW - 1))
 constexpr int BMAX = 16;
 
+// tile point += a * b.  Double-float tiles hold unnormalised compensated pairs: the exact
+// product's high part enters a two-sum with the point's sum, its rounding error and cross
+// terms the correction (12 FP32 operations; the halo reduction renormalises)
+template <typename T>
+__device__ __forceinline__ void tile_acc(T* dst, T a, T b) { *dst = fma(a, b, *dst); }
+template <>
+__device__ __forceinline__ void tile_acc<dfr>(dfr* dst, dfr a, dfr b) {
+  float2* d = reinterpret_cast<float2*>(dst);
+  const float2 t = *d;
+  dacc c;
+  c.s = t.x;
+  c.c = t.y;
+  dacc_add_prod(c, to_df(a), to_df(b));
+  *d = make_float2(c.s, c.c);
+}
+
 // Tile scatter: CTA = one brick and the atoms whose floor(u) lies in it.  The
 // CTA owns a (B+p-1)^3 shared-memory tile covering the brick plus the p-1
 // points below it that its atoms reach; atoms are scattered one after another
 // (one FMA per grid point, no atomics; each warp owns every nw-th z plane of the
 // tile, so a chunk of atoms needs one barrier; launched with SPREAD_NT threads),
-// then the tile is written to its
-// own slot of `ext` for the halo reduction below.
+// then the tile is written to its own slot of `ext` for the halo reduction below.
+// Per chunk atom the set-up stores Mx, the p x p products My (Mz q) and the atom's
+// tile offset with its z and y offsets (one 16-byte read per atom in the scatter).
 template <typename T, int P>
 __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, const int* __restrict__ batoms,
                                    const T* __restrict__ spl, const int* __restrict__ nidx,
                                    const double* __restrict__ q, T* __restrict__ ext) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int p = P ? P : sg.p;
   const int b = blockIdx.x;
   const int bx = b % sg.nb[0], by = (b / sg.nb[0]) % sg.nb[1], bz = b / (sg.nb[0] * sg.nb[1]);
   const int g0x = bx * sg.B[0], g0y = by * sg.B[1], g0z = bz * sg.B[2];
   const int TXd = sg.B[0] + p - 1, TYd = sg.B[1] + p - 1, TZd = sg.B[2] + p - 1;
-  const int tsize = TXd * TYd * TZd;
-  T* tile = reinterpret_cast<T*>(smem_raw);
-  T* Pkl = tile + tsize;                     // [SPREAD_CH][p*p] My(k) * q Mz(l)
-  T* Mx = Pkl + SPREAD_CH * p * p;           // [SPREAD_CH][p]
-  int* off = reinterpret_cast<int*>(Mx + SPREAD_CH * p);  // [SPREAD_CH][3] tile offsets
+  const int PL = TXd * TYd;
+  const int tsize = PL * TZd;
+  int4* info = reinterpret_cast<int4*>(smem_raw);  // [SPREAD_CH] tile offset, z offset, y offset, x offset
+  T* Pkl = reinterpret_cast<T*>(info + SPREAD_CH);  // [SPREAD_CH][p*p] My(k) * q Mz(l)
+  T* Mx = Pkl + SPREAD_CH * p * p;                   // [SPREAD_CH][p]
+  T* tile = Mx + SPREAD_CH * p;
   for (int e = threadIdx.x; e < tsize; e += blockDim.x) tile[e] = (T)0;
   const int s0 = bstart[b], s1 = bstart[b + 1];
   const int p2 = p * p;
@@ -215,9 +233,8 @@ __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, 
       const int i = batoms[c + a];
       Mx[a * p + t] = spl[((size_t)i * 3 + 0) * p + t];
       if (t == 0) {
-        off[a * 3 + 0] = nidx[3 * i + 0] - g0x;
-        off[a * 3 + 1] = nidx[3 * i + 1] - g0y;
-        off[a * 3 + 2] = nidx[3 * i + 2] - g0z;
+        const int ox = nidx[3 * i + 0] - g0x, oy = nidx[3 * i + 1] - g0y, oz = nidx[3 * i + 2] - g0z;
+        info[a] = make_int4(oz * PL + oy * TXd + ox, oz, oy, ox);
       }
     }
     for (int e = threadIdx.x; e < nc * p2; e += blockDim.x) {
@@ -235,25 +252,23 @@ __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, 
     if (p <= 8) {
       const int grp = wid & 7, half = wid >> 3;
       const int m = lane / p, j = lane - m * p;  // this lane's row pair and column
+      const T* mxj = Mx + j;
+      T* tj = tile + j;
       for (int a = 0; a < nc; ++a) {
-        const int oz = off[a * 3 + 2], oy = off[a * 3 + 1];
-        const int l = (grp - oz) & 7;
-        const int k = ((half - oy) & 1) + 2 * m;
-        if (l < p && k < p) {
-          T* dst = tile + ((oz + l) * TYd + (oy + k)) * TXd + (off[a * 3] + j);
-          *dst = fma(Mx[a * p + j], Pkl[a * p2 + l * p + k], *dst);
-        }
+        const int4 f = info[a];
+        const int l = (grp - f.y) & 7;
+        const int k = ((half - f.z) & 1) + 2 * m;
+        if (l < p && k < p) tile_acc(tj + (f.x + l * PL + k * TXd), mxj[a * p], Pkl[a * p2 + l * p + k]);
       }
       __syncwarp();
     } else {
       for (int a = 0; a < nc; ++a) {
-        const int ox = off[a * 3], oy = off[a * 3 + 1], oz = off[a * 3 + 2];
-        for (int l = (wid - oz) & (SPREAD_NW - 1); l < p; l += SPREAD_NW) {
-          T* plane = tile + (oz + l) * TYd * TXd;
+        const int4 f = info[a];
+        for (int l = (wid - f.y) & (SPREAD_NW - 1); l < p; l += SPREAD_NW) {
+          T* plane = tile + f.x + l * PL;
           for (int kj = lane; kj < p2; kj += 32) {
             const int j = kj % p, k = kj / p;
-            T* dst = plane + (oy + k) * TXd + (ox + j);
-            *dst = fma(Mx[a * p + j], Pkl[a * p2 + l * p + k], *dst);
+            tile_acc(plane + (k * TXd + j), Mx[a * p + j], Pkl[a * p2 + l * p + k]);
           }
         }
         __syncwarp();
@@ -372,7 +387,7 @@ __global__ void k_spme_tile_reduce(SpmeGeom sg, const T* __restrict__ ext, T* __
 
 inline size_t spread_smem(int B0, int B1, int B2, int p, size_t esz) {
   const size_t tsize = (size_t)(B0 + p - 1) * (B1 + p - 1) * (B2 + p - 1);
-  return esz * (tsize + (size_t)SPREAD_CH * p * p + (size_t)SPREAD_CH * p) + sizeof(int) * 3 * SPREAD_CH;
+  return esz * (tsize + (size_t)SPREAD_CH * p * p + (size_t)SPREAD_CH * p) + sizeof(int4) * SPREAD_CH;
 }
 
 // --------------------------------------------------------------- gather
