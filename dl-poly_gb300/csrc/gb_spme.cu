@@ -81,20 +81,25 @@ __device__ __forceinline__ void bspline_vals(T w, int p_rt, T* m /*p*/, T* dm /*
   for (int t = 0; t < p; ++t) m[t] = z[t + 1];
 }
 
+// Splines and brick binning: a CTA takes PREP_AT atoms with one thread per atom and
+// dimension (threads d * PREP_AT + a), so that each thread builds one spline; the
+// dimension-0 threads then combine the three brick coordinates through shared memory.
+constexpr int PREP_AT = 64;
 template <typename T, int P>
-__global__ void k_spme_prep(int natms, const double* __restrict__ x, const double* __restrict__ y,
-                            const double* __restrict__ z, const double* __restrict__ q, SpmeGeom sg, T* spl,
-                            int* nidx, int* brick_of, int* brick_count, int* gidx, float* gw, float2* gq,
-                            T* gsp) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= natms) return;
+__global__ void __launch_bounds__(3 * PREP_AT) k_spme_prep(int natms, const double* __restrict__ x,
+                                                           const double* __restrict__ y, const double* __restrict__ z,
+                                                           const double* __restrict__ q, SpmeGeom sg, T* spl,
+                                                           int* nidx, int* brick_of, int* brick_count, int* gidx,
+                                                           float* gw, float2* gq, T* gsp) {
+  __shared__ int bsh[3][PREP_AT];
+  const int d = threadIdx.x / PREP_AT, a = threadIdx.x - d * PREP_AT;
+  const int i = blockIdx.x * PREP_AT + a;
   const int p = P ? P : sg.p;
-  int bidx[3];
-  for (int d = 0; d < 3; ++d) {
-    double u = sg.Kr[d] * (((sg.rc[d] * x[i] + sg.rc[d + 3] * y[i]) + sg.rc[d + 6] * z[i]) + 0.5);
-    double fl = floor(u);
-    int n = (int)fl;
-    T w = (T)(u - fl);
+  if (i < natms) {
+    const double u = sg.Kr[d] * (((sg.rc[d] * x[i] + sg.rc[d + 3] * y[i]) + sg.rc[d + 6] * z[i]) + 0.5);
+    const double fl = floor(u);
+    const int n = (int)fl;
+    const T w = (T)(u - fl);
     double tr = fl;
     if (gidx) {
       // the gather's own convention: Int(u), u - Aint(u) (ewald_spole.F90:387, bspline.F90:216)
@@ -108,13 +113,8 @@ __global__ void k_spme_prep(int natms, const double* __restrict__ x, const doubl
     bspline_vals<T, P>(w, p, m, gsp ? dm : nullptr);
     // the z splines carry the charge: the spreads weight a point by Mx (My (Mz q))
     const T qT = d == 2 ? (T)q[i] : T(1);
-    if (d == 2) {
 #pragma unroll
-      for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t] * qT;
-    } else {
-#pragma unroll
-      for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = m[t];
-    }
+    for (int t = 0; t < p; ++t) spl[((size_t)i * 3 + d) * p + t] = d == 2 ? m[t] * qT : m[t];
     if (gsp) {
       // the double-float gather's splines, values then derivatives, z ones times the
       // charge, component-major ([value, derivative][x, y, z][point][atom]: coalesced
@@ -132,9 +132,11 @@ __global__ void k_spme_prep(int natms, const double* __restrict__ x, const doubl
     int nw = n % sg.K[d];
     if (nw < 0) nw += sg.K[d];
     nidx[3 * i + d] = nw;
-    bidx[d] = nw / sg.B[d];
+    bsh[d][a] = nw / sg.B[d];
   }
-  int b = bidx[0] + sg.nb[0] * (bidx[1] + sg.nb[1] * bidx[2]);
+  __syncthreads();
+  if (d != 0 || i >= natms) return;
+  int b = bsh[0][a] + sg.nb[0] * (bsh[1][a] + sg.nb[1] * bsh[2][a]);
   if (fabs(q[i]) <= DBL_MIN) b = -1;
   if (gq) {  // double-float gather: the charge, zero for atoms that take no part
     float h = 0.f, l = 0.f;
@@ -1134,7 +1136,7 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
   prof_begin(pid(P_SPME_PREP));
   const bool warp_gather = (!F64 || DF) && (p == 8 || p == 6);
   auto prep = p == 8 ? k_spme_prep<T, 8> : (p == 6 ? k_spme_prep<T, 6> : k_spme_prep<T, 0>);
-  prep<<<nblocks(n, 128), 128, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, spl, S.nidx, S.brick_of, S.brick_count,
+  prep<<<nblocks(n, PREP_AT), 3 * PREP_AT, 0, st>>>(n, g.x, g.y, g.z, g.chge, S.sg, spl, S.nidx, S.brick_of, S.brick_count,
                                          warp_gather ? S.gidx : nullptr, warp_gather && !DF ? S.gw : nullptr,
                                          warp_gather && DF ? reinterpret_cast<float2*>(S.gw + 6 * (size_t)n) : nullptr,
                                          warp_gather && DF ? reinterpret_cast<T*>(S.gsp) : nullptr);
