@@ -90,6 +90,56 @@ def test_spme_with_uncharged_atoms(gpu_lib, oracle_lib, precision):
         assert force_rms_rel(a, b) <= 1e-4
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("order", [4, 6, 10, 12])
+def test_spme_spline_orders(gpu_lib, oracle_lib, order, precision):
+    """Spline orders other than the workloads' 8: order 6 through the kernels instantiated
+    for it (the warp gathers included), 4, 10 and 12 through the run-time-order kernels
+    (the spread's plane-per-warp branch above order 8 among them)."""
+    s = systems.nacl_melt(16)
+    s.nsplines = order
+    _pair(gpu_lib, oracle_lib, s, precision=precision)
+    ed, vd, sd = gpu_lib.ewald_spme_forces()
+    er, vr, sr = oracle_lib.ewald_spme_forces()
+    a, b = gpu_lib.download(), oracle_lib.download()
+    if precision == 0:
+        assert ed == pytest.approx(er, rel=FP64_TOL)
+        assert vd == pytest.approx(vr, rel=1e-9)
+        assert force_dev(a, b) < FP64_TOL
+    else:
+        assert ed == pytest.approx(er, rel=1e-5)
+        assert force_rms_rel(a, b) <= 1e-4
+
+
+def test_md_atoms_below_lower_face(gpu_lib, oracle_lib):
+    """Between relocations an atom can drift below the cell's lower face, where its
+    fractional grid coordinate u is negative: the spread takes floor(u) and u - floor(u),
+    the gather Int(u) and u - Aint(u) (ewald_spole.F90:387), so the two use different
+    splines for that atom.  The NaCl lattice shifted by -1.35 A puts a layer of atoms at
+    the lower faces; 8 steps without a list rebuild carry dozens of them across (the
+    oracle's halo images stand in for them in its spread), against the oracle."""
+    s = systems.nacl_melt(16)
+    L = s.cell[0]
+    for c in ("x", "y", "z"):
+        setattr(s, c, getattr(s, c) - 1.35)
+    gpu_lib.init(s)
+    oracle_lib.init(s)
+    gpu_lib.start()
+    oracle_lib.start()
+    sd = gpu_lib.md_vv(8)
+    sr = oracle_lib.md_vv(8)
+    assert [x.list_rebuilt for x in sd] == [x.list_rebuilt for x in sr]
+    assert not any(x.list_rebuilt for x in sr)
+    a, b = gpu_lib.download(), oracle_lib.download()
+    assert sum(int((b[c] < -0.5 * L).sum()) for c in ("x", "y", "z")) >= 20
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert np.abs(a[k] - b[k]).max() <= 1e-9 * np.abs(b[k]).max(), k
+    assert force_dev(a, b) < 1e-8
+    for x, y in zip(sd, sr):
+        assert x.engcpe_rc == pytest.approx(y.engcpe_rc, rel=1e-9)
+        assert x.engcpe_rl == pytest.approx(y.engcpe_rl, rel=1e-9)
+
+
 def test_vdw_known_answer_on_gpu(gpu_lib):
     """source/unit_tests/test_vdw.F90:46-59 entry 2 (LJ eps=1 sigma=2 at r=1) through the device path."""
     s = systems.lj_pair(eps=1.0, sigma=2.0, r=1.0)
