@@ -133,6 +133,63 @@ void dalloc(T** p, size_t n) {
   GB_CUDA(cudaMemset(*p, 0, sizeof(T) * std::max<size_t>(n, 1)));
 }
 
+// Captures the work body() issues on the main stream (and on the side stream it forks
+// and joins) into *exec: a new graph, or the update of the existing one when its topology
+// is unchanged.  Nothing runs during a capture.  *nk: the kernels of one launch (the launch
+// counter is restored: graph launches add them).  Returns false, with nothing captured and
+// the stream out of capture, when the body does something a capture cannot hold.
+template <typename F>
+static bool capture_graph(cudaGraphExec_t* exec, int64_t* nk, F&& body) {
+  const int64_t l0 = g.launches;
+  GB_CUDA(cudaStreamBeginCapture(g.main_stream, cudaStreamCaptureModeThreadLocal));
+  bool ok = true;
+  try {
+    body();
+  } catch (int) {
+    ok = false;
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(g.main_stream, &graph);
+  *nk = g.launches - l0;
+  g.launches = l0;
+  g.stream = g.main_stream;
+  g.side = false;
+  g.join_pending = false;
+  if (!ok || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return false;
+  }
+  if (*exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(*exec, graph, &info) != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(*exec);
+      *exec = nullptr;
+    }
+  }
+  cudaError_t ei = cudaSuccess;
+  if (!*exec) ei = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) {
+    cudaGetLastError();
+    *exec = nullptr;
+    return false;
+  }
+  return true;
+}
+
+static void launch_graph(cudaGraphExec_t exec, int64_t nk) {
+  GB_CUDA(cudaGraphLaunch(exec, g.main_stream));
+  g.launches += nk;
+}
+
+void free_graphs() {
+  if (g.gx_vv1) cudaGraphExecDestroy(g.gx_vv1);
+  if (g.gx_step) cudaGraphExecDestroy(g.gx_step);
+  g.gx_vv1 = g.gx_step = nullptr;
+}
+
 void free_all() {
   void* ptrs[] = {g.x, g.y, g.z, g.xf, g.xlo, g.fx, g.fy, g.fz, g.fixp, g.vx, g.vy, g.vz, g.hdw, g.chge, g.weight, g.ltype, g.ltg,
                   g.lfrzn, g.ixyz, g.src, g.shcode, g.xbg, g.ybg, g.zbg, g.ox, g.oy, g.oz, g.which_cell,
@@ -144,6 +201,7 @@ void free_all() {
                   d_scratch_s, g.blkacc_s};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  free_graphs();
   mts_free();
   spme_free();
   metal_free();
@@ -668,6 +726,8 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
       g.use_mapped = !(m && m[0] == '0');
       const char* o = getenv("GB_OVERLAP");  // 0: SPME and the pair kernel on one stream
       g.use_overlap = !(o && o[0] == '0');
+      const char* gr = getenv("GB_GRAPHS");  // 0: the NVE loop's kernels launched one by one
+      g.use_graphs = !(gr && gr[0] == '0');
       const char* t = getenv("GB_PAIR_NT");  // 256 / 1024: CTA size of the sorted pair kernels (else by form)
       g.pair_nt = t ? ((atoi(t) == 256) ? 256 : 1024) : 0;
       const char* w = getenv("GB_PAIR_APW");
@@ -966,8 +1026,13 @@ int gb_metal_rho(double* out) {
 // The NVE loop without constraints, thermostat, metals or learned MTS: the host
 // waits only for the Verlet-list decision of each step (vnl_check); each step's
 // energy, virial and stress sums are copied to a pinned ring with the step's other
-// work and turned into gb_step_stats after the last step.  The per-region timings
-// of gb_last_timings are not taken on this path (the total is).
+// work and turned into gb_step_stats after the last step.  With 3 or more steps the
+// steps run as two CUDA graphs each: stage 1 with the displacement check (its sums
+// copied to the pinned scalars), then, after the host's decision, either the rebuild
+// step launched kernel by kernel or the graph of a step without rebuild (halo refresh,
+// forces with SPME forked to the side stream, stage 2), captured again after every
+// rebuild.  The per-region timings of gb_last_timings are not taken on this path (the
+// total is).
 static int md_run_deferred(int nsteps, gb_step_stats* stats) {
   if (g.ring_cap < nsteps) {
     if (g.ring) cudaFreeHost(g.ring);
@@ -979,21 +1044,43 @@ static int md_run_deferred(int nsteps, gb_step_stats* stats) {
   std::vector<int32_t> rebuilt(nsteps, 0);
   GB_CUDA(cudaEventRecord(g.ev[5], g.stream));
   g.defer_scalars = true;
-  for (int s = 0; s < nsteps; ++s) {
+  auto stage1 = [&]() {
     GB_CUDA(cudaMemsetAsync(&g.sc->status, 0, sizeof(int), g.stream));
-    ++g.nstep;
     int it = 0;
     integ_vv(1, nullptr, nullptr, &it, nullptr, nullptr);
-    int32_t upd = 0;
-    int st = do_refresh(&upd);
-    if (st) { g.defer_scalars = false; return st; }
+    integ_vnl_launch();
+    GB_CUDA(cudaMemcpyAsync(g.hsc, g.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, g.stream));
+  };
+  auto step_rest = [&]() {
+    list_refresh_halo();
+    compute_forces(nullptr, nullptr, true, true, true, nullptr);
+    int it = 0;
+    integ_vv(2, nullptr, nullptr, &it, nullptr, nullptr);
+  };
+  bool graphs = g.use_graphs && !g.prof_on && nsteps >= 3;
+  if (graphs) graphs = capture_graph(&g.gx_vv1, &g.gl_vv1, stage1);
+  bool step_ok = false;  // gx_step holds a step of the current list
+  for (int s = 0; s < nsteps; ++s) {
+    ++g.nstep;
+    if (graphs) launch_graph(g.gx_vv1, g.gl_vv1);
+    else stage1();
+    GB_CUDA(cudaStreamSynchronize(g.stream));
+    if (g.prof_on) gb_sync_scalars();  // resolves the pending profile events
+    const int32_t upd = integ_vnl_result();
     rebuilt[s] = upd;
     if (upd) {
-      st = list_build();
+      int st = list_relocate_and_halo();
+      if (!st) st = list_build();
       if (st) { g.defer_scalars = false; return st; }
+      compute_forces(nullptr, nullptr, true, true, true, nullptr);
+      int it = 0;
+      integ_vv(2, nullptr, nullptr, &it, nullptr, nullptr);
+      step_ok = false;
+    } else {
+      if (graphs && !step_ok) step_ok = capture_graph(&g.gx_step, &g.gl_step, step_rest);
+      if (graphs && step_ok) launch_graph(g.gx_step, g.gl_step);
+      else step_rest();
     }
-    compute_forces(nullptr, nullptr, true, true, true, nullptr);
-    integ_vv(2, nullptr, nullptr, &it, nullptr, nullptr);
     GB_CUDA(cudaMemcpyAsync(&g.ring[s], g.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, g.stream));
   }
   g.defer_scalars = false;

@@ -168,6 +168,13 @@ struct Dev {
   // last step, so the host waits only for the Verlet-list decision of each step
   bool defer_scalars = false;
   bool use_deferred = true;    // GB_MD_DEFER=0 keeps the per-step read-back
+  // that loop as CUDA graphs (GB_GRAPHS=0: every kernel launched by the host): stage 1 with
+  // the Verlet-list check, and a step without a list rebuild (halo refresh, forces, stage
+  // 2), captured once per call and again after each rebuild; the launch counter adds each
+  // graph's kernels per launch
+  bool use_graphs = true;
+  cudaGraphExec_t gx_vv1 = nullptr, gx_step = nullptr;
+  int64_t gl_vv1 = 0, gl_step = 0;
   DevScalars* ring = nullptr;  // pinned, ring_cap steps
   int ring_cap = 0;
   // host state transfers: pinned and mapped caller buffers are read and written by one
@@ -413,6 +420,8 @@ void integ_con_tags();            // constraints_tags: old bond vectors from the
 void integ_shake(int* iters, double* vircon, double* strcon);  // apply_shake (throws GB_ERR_SHAKE)
 void integ_rattle_launch();       // apply_rattle, kit = 1 (status bit ST_RATTLE_FAIL)
 int integ_vnl_check();
+void integ_vnl_launch();          // the displacement check, its sums copied to the pinned scalars
+int integ_vnl_result();           // its decision from the copied scalars (after a wait)
 void integ_zero_forces();
 void integ_forces_to_fp64();      // mixed: fixed point -> FP64 forces
 void integ_setup_constraints(const int32_t* listcon, const double* prmcon);

@@ -676,13 +676,19 @@ void integ_forces_to_fp64() {
   GB_LAUNCHED();
 }
 
-int integ_vnl_check() {
+void integ_vnl_launch() {
   GB_CUDA(cudaMemsetAsync(&g.sc->maxdisp, 0, sizeof(double), g.stream));
   k_maxdisp<<<std::min(nblocks(g.natms, 256), 2 * g.nsm), 256, 0, g.stream>>>(
       g.natms, g.x, g.y, g.z, g.xbg, g.ybg, g.zbg, g.cell[0], 1.0 / g.cell[0], (unsigned long long*)&g.sc->maxdisp);
   GB_LAUNCHED();
+}
+
+int integ_vnl_result() { return std::sqrt(g.hsc->maxdisp) >= std::nextafter(0.5, 0.0) * g.p.rpad ? 1 : 0; }
+
+int integ_vnl_check() {
+  integ_vnl_launch();
   gb_sync_scalars();
-  return std::sqrt(g.hsc->maxdisp) >= std::nextafter(0.5, 0.0) * g.p.rpad ? 1 : 0;
+  return integ_vnl_result();
 }
 
 static void con_args(ConArgs& A) {

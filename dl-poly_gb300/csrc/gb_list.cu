@@ -12,6 +12,7 @@
 // only candidates inside the margin band are re-tested in exact FP64.
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 
 #include "gb_common.cuh"
 
@@ -937,11 +938,18 @@ int list_relocate_and_halo() {
 }
 
 int list_refresh_halo() {
+  // the image shifts on the device, copied again only when they change (a step captured
+  // into a CUDA graph then holds no copy from pageable host memory)
   static double* d_adds = nullptr;
+  static double last[18];
   if (!d_adds) {
     GB_CUDA(cudaMalloc(&d_adds, sizeof(double) * 18));
+    GB_CUDA(cudaMemcpy(d_adds, h_add, sizeof(double) * 18, cudaMemcpyHostToDevice));
+    std::memcpy(last, h_add, sizeof(last));
+  } else if (std::memcmp(last, h_add, sizeof(last)) != 0) {
+    GB_CUDA(cudaMemcpyAsync(d_adds, h_add, sizeof(double) * 18, cudaMemcpyHostToDevice, g.stream));
+    std::memcpy(last, h_add, sizeof(last));
   }
-  GB_CUDA(cudaMemcpyAsync(d_adds, h_add, sizeof(double) * 18, cudaMemcpyHostToDevice, g.stream));
   k_halo_refresh<<<nblocks(g.mxatms - g.natms, 256), 256, 0, g.stream>>>(g.natms, g.sc, g.src, g.shcode, g.x, g.y,
                                                                           g.z, d_adds);
   GB_LAUNCHED();

@@ -476,6 +476,34 @@ def test_deferred_step_scalars_match_per_step_readback(gpu_lib, monkeypatch, pre
         assert list(x.stress) == list(y.stress) and list(x.strkin) == list(y.strkin)
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_graph_steps_match_launched_steps(gpu_lib, monkeypatch, precision):
+    """The NVE loop's steps replayed as CUDA graphs (stage 1 with the list check; a step
+    without rebuild, captured again after each rebuild) run the same kernels as the loop
+    that launches them one by one: the same trajectory and step scalars bit for bit, and
+    the same kernel count."""
+    s = systems.nacl_melt(16)
+    out = []
+    for env in ("0", "1"):
+        monkeypatch.setenv("GB_GRAPHS", env)
+        gpu_lib.init(s, precision=precision)
+        gpu_lib.start()
+        l0 = gpu_lib.lib.gb_kernel_launches()
+        st = gpu_lib.md_vv(40)
+        out.append((st, gpu_lib.download(), gpu_lib.lib.gb_kernel_launches() - l0))
+    monkeypatch.delenv("GB_GRAPHS", raising=False)
+    (sa, a, na), (sb, b, nb) = out
+    assert sum(x.list_rebuilt for x in sa) >= 2
+    assert [x.list_rebuilt for x in sa] == [x.list_rebuilt for x in sb]
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    for x, y in zip(sa, sb):
+        for f in ("engcpe_rc", "vircpe_rc", "engcpe_rl", "vircpe_rl", "engvdw", "virvdw", "engke"):
+            assert getattr(x, f) == getattr(y, f), f
+        assert list(x.stress) == list(y.stress) and list(x.strkin) == list(y.strkin)
+    assert na == nb
+
+
 @pytest.mark.parametrize("name", ["nacl_4096", "water_5184"])
 def test_fp32_tile_spread_matches_fixed_point_spread(gpu_lib, oracle_lib, monkeypatch, name):
     """FP32 grids (mixed form) spread by the atomic-free tile kernel, each brick's atoms in
