@@ -729,6 +729,8 @@ inline int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
 extern void dcell_host(const double* aaa, double* bbb);
 extern void invert_host(const double* a, double* b, double* d);
 
+static void upload_adds();
+
 void list_setup() {
   // set_halo_particles constants (halo.F90:184-247)
   double cut = g.rcutx + 1.0e-6;
@@ -755,6 +757,7 @@ void list_setup() {
     h_add[m][1] = c[1] * u + c[4] * v + c[7] * w;
     h_add[m][2] = c[2] * u + c[5] * v + c[8] * w;
   }
+  upload_adds();
   // link-cell geometry (neighbours.F90:396-463)
   double cut2 = g.rcutx + 1.0e-6;
   double disp[3] = {1.0 * cp[6] / cut2, 1.0 * cp[7] / cut2, 1.0 * cp[8] / cut2};
@@ -937,19 +940,19 @@ int list_relocate_and_halo() {
   return GB_OK;
 }
 
+// the image shifts on the device for the halo refresh: allocated and written where the
+// list geometry is set up, copied again only when they change (a step captured into a CUDA
+// graph then holds neither an allocation nor a copy from pageable host memory)
+static double* d_adds = nullptr;
+static double d_adds_host[18];
+static void upload_adds() {
+  if (!d_adds) GB_CUDA(cudaMalloc(&d_adds, sizeof(double) * 18));
+  GB_CUDA(cudaMemcpy(d_adds, h_add, sizeof(double) * 18, cudaMemcpyHostToDevice));
+  std::memcpy(d_adds_host, h_add, sizeof(d_adds_host));
+}
+
 int list_refresh_halo() {
-  // the image shifts on the device, copied again only when they change (a step captured
-  // into a CUDA graph then holds no copy from pageable host memory)
-  static double* d_adds = nullptr;
-  static double last[18];
-  if (!d_adds) {
-    GB_CUDA(cudaMalloc(&d_adds, sizeof(double) * 18));
-    GB_CUDA(cudaMemcpy(d_adds, h_add, sizeof(double) * 18, cudaMemcpyHostToDevice));
-    std::memcpy(last, h_add, sizeof(last));
-  } else if (std::memcmp(last, h_add, sizeof(last)) != 0) {
-    GB_CUDA(cudaMemcpyAsync(d_adds, h_add, sizeof(double) * 18, cudaMemcpyHostToDevice, g.stream));
-    std::memcpy(last, h_add, sizeof(last));
-  }
+  if (!d_adds || std::memcmp(d_adds_host, h_add, sizeof(d_adds_host)) != 0) upload_adds();
   k_halo_refresh<<<nblocks(g.mxatms - g.natms, 256), 256, 0, g.stream>>>(g.natms, g.sc, g.src, g.shcode, g.x, g.y,
                                                                           g.z, d_adds);
   GB_LAUNCHED();
