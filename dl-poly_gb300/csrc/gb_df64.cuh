@@ -93,6 +93,20 @@ __host__ __device__ inline void df_split(double v, float* hi, float* lo) {
   *lo = (float)(v - (double)*hi);
 }
 
+// x^2 + y^2 + z^2: the squares' exact high parts summed by two two-sums, their rounding
+// errors, cross terms and the sums' errors in one correction, renormalised once (31 FP32
+// operations instead of the 40 of three squares and two additions)
+__device__ __forceinline__ df df_norm2(df x, df y, df z) {
+  const df px = two_prod(x.hi, x.hi), py = two_prod(y.hi, y.hi), pz = two_prod(z.hi, z.hi);
+  const float cx = __fmaf_rn(__fadd_rn(x.hi, x.hi), x.lo, px.lo);
+  const float cy = __fmaf_rn(__fadd_rn(y.hi, y.hi), y.lo, py.lo);
+  const float cz = __fmaf_rn(__fadd_rn(z.hi, z.hi), z.lo, pz.lo);
+  const df s1 = two_sum(px.hi, py.hi);
+  const df s2 = two_sum(s1.hi, pz.hi);
+  const float c = __fadd_rn(__fadd_rn(__fadd_rn(cx, cy), __fadd_rn(cz, s1.lo)), s2.lo);
+  return quick_two_sum(s2.hi, c);
+}
+
 // running sum of many double-float terms: s carries the sum, c its rounding errors
 struct dacc {
   float s, c;

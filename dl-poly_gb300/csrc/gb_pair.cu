@@ -680,7 +680,7 @@ __global__ void __launch_bounds__(PAIR_DF_NT, 4) k_pair_df64(int natms, const De
           const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
           const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
           const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
-          const df rsq = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+          const df rsq = df_norm2(dx, dy, dz);
           if (rsq.hi <= pg.f_hi) {
             const int jf = j;  // an image's force stays in its own slot until k_fold_images
             const float2 qj2 = qdf[j];
@@ -762,9 +762,10 @@ struct PairSortedArgs {
 };
 
 // The FP64 form's terms of one pair (the arithmetic of pair_terms_df64, partner data
-// passed in); j is the partner's atom index for the exact FP64 evaluation near a cutoff.
+// passed in); jp is the partner's sorted position, whose atom index the exact FP64
+// evaluation near a cutoff looks up.
 // Returns false when the pair exerts no force.
-__device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSortedArgs& A, int i, int j, int ai,
+__device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSortedArgs& A, int i, int jp, int ai,
                                                int aj, df qi, bool qi_on, float qjh, float qjl, df dx, df dy, df dz,
                                                df rsq, dacc (&acc)[NACC_DF], long long& ix, long long& iy,
                                                long long& iz) {
@@ -814,6 +815,7 @@ __device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSor
   if (slow) {
     double g64, e64c, e64v, gc64, gv64;
     bool any;
+    const int j = A.at_list[jp];
     pair_terms_fp64(pg, A.x[i] - A.x[j], A.y[i] - A.y[j], A.z[i] - A.z[j], A.q[i] * pg.scaling, A.q[j], ai, aj,
                     A.ecoef, A.vcoef, A.vkind, A.veps, A.vsig, &g64, &e64c, &e64v, &gc64, &gv64, &any);
     if (!any) return false;
@@ -969,8 +971,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A,
             const df dx = quick_two_sum(ex.hi, __fadd_rn(ex.lo, __fsub_rn(li.x, lj.x)));
             const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
             const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
-            const df rsq = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
-            hit = rsq.hi <= pg.f_hi && pair_df64_eval(pg, A, i, A.at_list[j], ai, aj, qi, qi_on, pj.w, lj.w, dx,
+            const df rsq = df_norm2(dx, dy, dz);
+            hit = rsq.hi <= pg.f_hi && pair_df64_eval(pg, A, i, j, ai, aj, qi, qi_on, pj.w, lj.w, dx,
                                                       dy, dz, rsq, acc, ix, iy, iz);
           }
           if (hit) {
