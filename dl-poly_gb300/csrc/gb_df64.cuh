@@ -139,4 +139,13 @@ __device__ __forceinline__ long long fix40_df(df a) {
   return __float2ll_rz(__fmul_rn(a.hi, 1099511627776.0f)) + __float2ll_rz(__fmul_rn(a.lo, 1099511627776.0f));
 }
 
+// fix40 of the product a * b without renormalising it: the exact product's high part and
+// the sum of its rounding error and cross terms, each scaled by 2^40 and truncated toward
+// zero (the parts fix40_df truncates, up to where the renormalisation would split them)
+__device__ __forceinline__ long long fix40_prod(df a, df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float t = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.hi, -p)));
+  return __float2ll_rz(__fmul_rn(p, 1099511627776.0f)) + __float2ll_rz(__fmul_rn(t, 1099511627776.0f));
+}
+
 #endif

@@ -777,7 +777,8 @@ __device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSor
     key = vkey(ai, aj) - 1;
     if (A.vkind[key] == 0) key = -1;
   }
-  df gam = df_make(0.f, 0.f), ee = gam, ev = gam, gvc = gam, gvv = gam;
+  // wv: the vdW virial term -gvv r^2 (-G(r) of the table itself on the fast path)
+  df gam = df_make(0.f, 0.f), ee = gam, ev = gam, gvc = gam, gvv = gam, wv = gam;
   bool slow = band;
   if (!slow && (in_c || key >= 0)) {
     const df rinv = df_rsqrt(rsq);
@@ -805,7 +806,9 @@ __device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSor
         } else {
           const float4* c = A.vtab + (size_t)key * ((pg.max_grid + 3) * 3) + (size_t)kv * 3;
           const float4 f01 = c[0], v01 = c[1], c2 = c[2];
-          gvv = df_mul(poly_df(f01, c2.x, c2.y, dv), r_rsq);
+          const df G = poly_df(f01, c2.x, c2.y, dv);
+          gvv = df_mul(G, r_rsq);
+          wv = df_neg(G);
           ev = poly_df(v01, c2.z, c2.w, dv);
           gam = df_add(gam, gvv);
         }
@@ -825,14 +828,15 @@ __device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSor
     df_split(e64v, &h, &l); ev = df_make(h, l);
     df_split(gc64, &h, &l); gvc = df_make(h, l);
     df_split(gv64, &h, &l); gvv = df_make(h, l);
+    wv = df_neg(df_mul(gvv, rsq));
   } else if (!in_c && key < 0) {
     return false;
   }
-  ix = fix40_df(df_mul(gam, dx));
-  iy = fix40_df(df_mul(gam, dy));
-  iz = fix40_df(df_mul(gam, dz));
+  ix = fix40_prod(gam, dx);
+  iy = fix40_prod(gam, dy);
+  iz = fix40_prod(gam, dz);
   dacc_add(acc[0], ev);
-  dacc_add_prod(acc[1], df_neg(gvv), rsq);
+  dacc_add(acc[1], wv);
   dacc_add(acc[2], ee);
   dacc_add_prod(acc[3], df_neg(gvc), rsq);
   return true;
