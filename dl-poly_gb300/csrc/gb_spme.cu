@@ -493,6 +493,12 @@ __global__ void __launch_bounds__(256, 4) k_spme_gather_f32(int natms, const flo
       const float qi = q4[4 * i + 3];
       const int gx = gidx[3 * i], gy = gidx[3 * i + 1], gz = gidx[3 * i + 2];
       float v[4] = {0.f, 0.f, 0.f, 0.f};  // energy, x, y, z sums
+      int zo[P];  // z-plane offsets of this atom
+#pragma unroll
+      for (int l = 0; l < P; ++l) {
+        int zz = gz + l; if (zz >= K2) zz -= K2;
+        zo[l] = zz * K1 * K0;
+      }
 #pragma unroll
       for (int pr = lane; pr < P * P; pr += 32) {
         const int j = pr % P, k = pr / P;
@@ -500,18 +506,21 @@ __global__ void __launch_bounds__(256, 4) k_spme_gather_f32(int natms, const flo
         int yy = gy + k; if (yy >= K1) yy -= K1;
         const float mx = sp[wid][a][0][0][j], dmx = sp[wid][a][1][0][j];
         const float my = sp[wid][a][0][1][k], dmy = sp[wid][a][1][1][k];
-        const float p0 = mx * my, p1 = dmx * my, p2 = mx * dmy;
-        const float* col = phi + (size_t)yy * K0 + xx;
+        const float* col = phi + (yy * K0 + xx);
+        // the z column against Mz and dMz (separable: 2 products per grid point), then the
+        // column's x/y spline products
+        float za = 0.f, zc = 0.f;
 #pragma unroll
         for (int l = 0; l < P; ++l) {
-          int zz = gz + l; if (zz >= K2) zz -= K2;
-          const float pa = col[(size_t)zz * K1 * K0];
-          const float ta = sp[wid][a][0][2][l] * pa;
-          v[0] = fmaf(p0, ta, v[0]);
-          v[1] = fmaf(p1, ta, v[1]);
-          v[2] = fmaf(p2, ta, v[2]);
-          v[3] = fmaf(p0, sp[wid][a][1][2][l] * pa, v[3]);
+          const float pa = col[zo[l]];
+          za = fmaf(sp[wid][a][0][2][l], pa, za);
+          zc = fmaf(sp[wid][a][1][2][l], pa, zc);
         }
+        const float p0 = mx * my;
+        v[0] = fmaf(p0, za, v[0]);
+        v[1] = fmaf(dmx * my, za, v[1]);
+        v[2] = fmaf(mx * dmy, za, v[2]);
+        v[3] = fmaf(p0, zc, v[3]);
       }
       // reduce-scatter: level 16 keeps (v0, v1) in the lower half-warp, (v2, v3) in the upper
       const bool up16 = lane & 16, up8 = lane & 8;
