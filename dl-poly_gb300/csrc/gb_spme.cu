@@ -187,17 +187,17 @@ constexpr int BMAX = 16;
 // product's high part enters a two-sum with the point's sum, its rounding error and cross
 // terms the correction (12 FP32 operations; the halo reduction renormalises)
 template <typename T>
-__device__ __forceinline__ void tile_acc(T* dst, T a, T b) { *dst = fma(a, b, *dst); }
+__device__ __forceinline__ T tile_upd(T v, T a, T b) { return fma(a, b, v); }
 template <>
-__device__ __forceinline__ void tile_acc<dfr>(dfr* dst, dfr a, dfr b) {
-  float2* d = reinterpret_cast<float2*>(dst);
-  const float2 t = *d;
+__device__ __forceinline__ dfr tile_upd<dfr>(dfr v, dfr a, dfr b) {
   dacc c;
-  c.s = t.x;
-  c.c = t.y;
+  c.s = v.hi;
+  c.c = v.lo;
   dacc_add_prod(c, to_df(a), to_df(b));
-  *d = make_float2(c.s, c.c);
+  return dfr(c.s, c.c);
 }
+template <typename T>
+__device__ __forceinline__ void tile_acc(T* dst, T a, T b) { *dst = tile_upd(*dst, a, b); }
 
 // Tile scatter: CTA = one brick and the atoms whose floor(u) lies in it.  The
 // CTA owns a (B+p-1)^3 shared-memory tile covering the brick plus the p-1
@@ -207,7 +207,9 @@ __device__ __forceinline__ void tile_acc<dfr>(dfr* dst, dfr a, dfr b) {
 // then the tile is written to its own slot of `ext` for the halo reduction below.
 // Per chunk atom the set-up stores Mx, the p x p products My (Mz q) and the atom's
 // tile offset with its z and y offsets (one 16-byte read per atom in the scatter).
-template <typename T, int P>
+// NT = 256 (order 8): warp w owns the tile planes z = w (mod 8) and takes the whole plane
+// of each atom, two points per lane (rows k and k + 4), two independent updates.
+template <typename T, int P, int NT = SPREAD_NT>
 __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, const int* __restrict__ batoms,
                                    const T* __restrict__ spl, const int* __restrict__ nidx,
                                    const double* __restrict__ q, T* __restrict__ ext) {
@@ -250,8 +252,26 @@ __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, 
     // plane z and row y belong to warp (z mod 8) + 8 (y mod 2), so every warp takes one
     // plane and every other row of each atom (for p = 8 one point per lane); higher orders:
     // plane z belongs to warp z mod NW.
-    static_assert(SPREAD_NW == 16, "the split below gives warps w and w + 8 the even and odd rows");
-    if (p <= 8) {
+    constexpr int NW = NT / 32;
+    if constexpr (NT == 256) {
+      static_assert(P == 8, "eight warps: one plane of an order-8 atom each");
+      const int j = lane & 7, m = lane >> 3;  // column, first row
+      const T* mxj = Mx + j;
+      T* tj = tile + j;
+      for (int a = 0; a < nc; ++a) {
+        const int4 f = info[a];
+        const int l = (wid - f.y) & 7;
+        T* d0 = tj + (f.x + l * PL + m * TXd);
+        T* d1 = d0 + 4 * TXd;
+        const T mx = mxj[a * 8];
+        const T* pk = Pkl + a * 64 + l * 8;
+        const T v0 = *d0, v1 = *d1;
+        *d0 = tile_upd(v0, mx, pk[m]);
+        *d1 = tile_upd(v1, mx, pk[m + 4]);
+      }
+      __syncwarp();
+    } else if (p <= 8) {
+      static_assert(NW == 16, "the split below gives warps w and w + 8 the even and odd rows");
       const int grp = wid & 7, half = wid >> 3;
       const int m = lane / p, j = lane - m * p;  // this lane's row pair and column
       const T* mxj = Mx + j;
@@ -266,7 +286,7 @@ __global__ void k_spme_spread_tile(SpmeGeom sg, const int* __restrict__ bstart, 
     } else {
       for (int a = 0; a < nc; ++a) {
         const int4 f = info[a];
-        for (int l = (wid - f.y) & (SPREAD_NW - 1); l < p; l += SPREAD_NW) {
+        for (int l = (wid - f.y) & (NW - 1); l < p; l += NW) {
           T* plane = tile + f.x + l * PL;
           for (int kj = lane; kj < p2; kj += 32) {
             const int j = kj % p, k = kj / p;
@@ -978,7 +998,7 @@ void grid_setup(SpmeGrid& S, const int* Kin, int p, bool fp64, int bpref) {
     raise_smem(k_spme_spread_tile<double, 0>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(double)));
     raise_smem(k_spme_spread_tile<dfr, 8>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(dfr)));
     raise_smem(k_spme_spread_tile<dfr, 0>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(dfr)));
-    raise_smem(k_spme_spread_tile<float, 8>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
+    raise_smem(k_spme_spread_tile<float, 8, 256>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
     raise_smem(k_spme_spread_tile<float, 6>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(float)));
     raise_smem(k_spme_spread_tile<double, 6>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(double)));
     raise_smem(k_spme_spread_tile<dfr, 6>, (int)spread_smem(S.B[0], S.B[1], S.B[2], p, sizeof(dfr)));
@@ -1176,8 +1196,14 @@ void grid_run(SpmeGrid& S, bool coarse, float* rec, double* eng_rc, double* vir_
     const dim3 red_grid((unsigned)nblocks(K1, red_nt), (unsigned)K2, (unsigned)K3);
     prof_begin(pid(P_SPME_SPREAD));
     if (tile_spread) {
-      auto spread = p == 8 ? k_spme_spread_tile<T, 8> : (p == 6 ? k_spme_spread_tile<T, 6> : k_spme_spread_tile<T, 0>);
-      spread<<<S.nbricks, SPREAD_NT, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge, ext);
+      // order 8 in FP32: eight warps of two points per lane (every tile point is one FMA, so
+      // the per-atom indexing dominates and halves); the double-float and FP64 tiles keep
+      // sixteen warps, whose longer update chains need the warps more than the shared indexing
+      constexpr bool EIGHT = std::is_same<T, float>::value;
+      constexpr int NT8 = EIGHT ? 256 : SPREAD_NT;
+      auto spread = p == 8 ? k_spme_spread_tile<T, 8, NT8> : (p == 6 ? k_spme_spread_tile<T, 6> : k_spme_spread_tile<T, 0>);
+      spread<<<S.nbricks, p == 8 ? NT8 : SPREAD_NT, smem, st>>>(S.sg, S.brick_start, S.brick_atoms, spl, S.nidx, g.chge,
+                                                              ext);
       GB_LAUNCHED();
       k_spme_tile_reduce<T><<<red_grid, red_nt, 0, st>>>(S.sg, ext, Q);
       GB_LAUNCHED();
