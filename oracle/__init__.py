@@ -1,7 +1,8 @@
 """CPU FP64 oracle of the DL_POLY force/update path -- test infrastructure only.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this
-package, as the checker (or the timed CPU baseline); the product never does.
+package, as the reference results of the parity tests (or the timed CPU baseline); the
+product never does.
 """
 import ctypes
 import os

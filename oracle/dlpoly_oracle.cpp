@@ -3,7 +3,8 @@
 //
 // TEST INFRASTRUCTURE ONLY.  This file is the parity oracle for the GB300
 // library: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
-// leg may load it, and only as the checker or the timed CPU baseline.  It is
+// leg may load it, and only for the parity tests' reference results or the timed CPU
+// baseline.  It is
 // never part of the product path.
 //
 // The reference is Fortran 2008 and cannot be compiled here (no Fortran

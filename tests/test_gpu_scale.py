@@ -9,7 +9,7 @@ The CUDA path against the FP64 oracle on the benchmark workloads themselves:
   - SPME alone on 100^3, 160^3 and 192^3 grids (radix-5 lengths and the
     transform kernels compiled for those lengths) in all three forms.
 
-At these sizes the checker is the oracle's OpenMP build on all host cores: the
+At these sizes the reference results come from the oracle's OpenMP build on all host cores: the
 same restatement, with only the order of a few reductions (per-thread partial
 sums of energies, stress and the net-force term) changed, which moves results by
 ~1e-13 relative, far inside the 1e-10 bar.
