@@ -614,7 +614,7 @@ __device__ __forceinline__ df ld_df(const dfr* p) {
 // the second) that leaves them in lanes 0, 8, 16, 24.  No FP64 instruction: forces leave
 // as double-floats.
 template <int P>
-__global__ void __launch_bounds__(256) k_spme_gather_wdf(int natms, SpmeGeom sg, const int* __restrict__ gidx,
+__global__ void __launch_bounds__(256, 6) k_spme_gather_wdf(int natms, SpmeGeom sg, const int* __restrict__ gidx,
                                                          const dfr* __restrict__ gsp,
                                                          const float2* __restrict__ gq, const dfr* __restrict__ phi,
                                                          float2 rk0, float2 rk1, float2 rk2,
