@@ -86,7 +86,7 @@ __device__ __forceinline__ void bspline_vals(T w, int p_rt, T* m /*p*/, T* dm /*
 // dimension-0 threads then combine the three brick coordinates through shared memory.
 constexpr int PREP_AT = 64;
 template <typename T, int P>
-__global__ void __launch_bounds__(3 * PREP_AT) k_spme_prep(int natms, const double* __restrict__ x,
+__global__ void __launch_bounds__(3 * PREP_AT, std::is_same<T, dfr>::value ? 5 : 0) k_spme_prep(int natms, const double* __restrict__ x,
                                                            const double* __restrict__ y, const double* __restrict__ z,
                                                            const double* __restrict__ q, SpmeGeom sg, T* spl,
                                                            int* nidx, int* brick_of, int* brick_count, int* gidx,
