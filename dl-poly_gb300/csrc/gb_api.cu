@@ -195,7 +195,7 @@ void free_all() {
                   g.lfrzn, g.ixyz, g.src, g.shcode, g.xbg, g.ybg, g.zbg, g.ox, g.oy, g.oz, g.which_cell,
                   g.cell_count, g.cell_start, g.cell_fill, g.at_list, g.sorted_pos, g.xs, g.xsf, g.list, g.blk,
                   g.list_excl, g.erfc_coef, g.erfc_coef_f, g.vdw_coef, g.vdw_coef_f,
-                  g.vdw_kind, g.vdw_eps, g.vdw_sig, g.erfc_df, g.vdw_df, g.qdf, g.spos, g.xhs, g.xls, g.tys, g.fixs, g.loc_sp,
+                  g.vdw_kind, g.vdw_eps, g.vdw_sig, g.erfc_df, g.vdw_df, g.qdf, g.spos, g.xhs, g.xls, g.tys, g.xlh, g.fixs, g.loc_sp,
                   g.tile_rows, g.tile_info, g.tile_over, g.blkacc, g.con_i, g.con_j, g.con_d0, g.dxx, g.dyy,
                   g.dzz, g.dxt, g.dyt, g.dzt, g.dt2, g.gam, g.listot, g.acon_start, g.acon_list, g.sc, d_scratch,
                   d_scratch_s, g.blkacc_s};
@@ -665,7 +665,7 @@ int gb_init(const gb_params* prm, int natms, const int32_t* ltype, const double*
     dalloc(&g.list, (size_t)g.ld * natms);
     g.ldt = ((prm->max_list + 1 + 3) / 4) * 4;  // spos(k, i), k = 1..max_list, rows 16-byte aligned
     dalloc(&g.spos, (size_t)g.ldt * natms);
-    dalloc(&g.xhs, mx); dalloc(&g.xls, mx); dalloc(&g.tys, mx);
+    dalloc(&g.xhs, mx); dalloc(&g.xls, mx); dalloc(&g.tys, mx); dalloc(&g.xlh, mx);
     dalloc(&g.loc_sp, natms);
     dalloc(&g.fixs, 3 * (size_t)mx);
     dalloc(&g.sc, 1);

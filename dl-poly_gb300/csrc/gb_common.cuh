@@ -2,6 +2,7 @@
 // helpers for the GB300 DL_POLY force/update path.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -186,6 +187,7 @@ struct Dev {
   float4* xhs = nullptr;       // per sorted position: FP32 high parts (x, y, z, q)
   float4* xls = nullptr;       // per sorted position: remainders (x, y, z, q) of the FP64 values
   unsigned char* tys = nullptr;  // per sorted position: atom type
+  uint2* xlh = nullptr;        // mixed form, per sorted position: remainders x 2^20 as half floats, and the type
   long long* fixs = nullptr;   // 3 x mxatms fixed-point pair forces per sorted position
   double metal_e4[4] = {0, 0, 0, 0};  // engmet, virmet, engden, virden of the last evaluation
   // thermostat of the VV stages (gb_thermostat.cu)
@@ -269,6 +271,26 @@ extern Dev g;
   } while (0)
 
 // ------------------------------------------------------------ device helpers
+// The mixed form's per-sorted-position record of the FP32 remainders x - (float)x (at most
+// half an FP32 ulp of the coordinate) and the atom type in 8 bytes: the remainders times
+// 2^20 as half floats (11 significant bits of the remainder: ~1e-9 A for coordinates below
+// 128 A; a remainder times 2^20 stays below the half range for coordinates below 2^19 A),
+// the type in the top 16 bits.
+__device__ __forceinline__ uint2 pack_lo_type(float lx, float ly, float lz, int type) {
+  const __half2 h = __floats2half2_rn(lx * 1048576.0f, ly * 1048576.0f);
+  uint2 r;
+  r.x = *reinterpret_cast<const unsigned int*>(&h);
+  r.y = (unsigned int)__half_as_ushort(__float2half_rn(lz * 1048576.0f)) | ((unsigned int)type << 16);
+  return r;
+}
+__device__ __forceinline__ void pair_lo_type(uint2 r, float& lx, float& ly, float& lz, int& type) {
+  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&r.x));
+  lx = a.x * 9.5367431640625e-07f;  // 2^-20
+  ly = a.y * 9.5367431640625e-07f;
+  lz = __half2float(__ushort_as_half((unsigned short)(r.y & 0xffffu))) * 9.5367431640625e-07f;
+  type = (int)(r.y >> 16);
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -702,7 +702,7 @@ __global__ void k_list_reorder(int natms, int* list, int ld, int* spos, int ldt,
 __global__ void k_pos_records(const DevScalars* sc, const int* __restrict__ sorted_pos, const double* __restrict__ x,
                               const double* __restrict__ y, const double* __restrict__ z, const double* __restrict__ q,
                               const int* __restrict__ ltype, float4* xf, float4* xlo, float2* qdf, float4* xhs,
-                              float4* xls, unsigned char* tys) {
+                              float4* xls, unsigned char* tys, uint2* xlh) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= sc->nlast) return;
   const double xa = x[i], ya = y[i], za = z[i], qa = q[i];
@@ -716,8 +716,12 @@ __global__ void k_pos_records(const DevScalars* sc, const int* __restrict__ sort
   if (xhs) {
     const int p = sorted_pos[i];
     xhs[p] = make_float4(hx, hy, hz, hq);
-    xls[p] = make_float4(lx, ly, lz, lq);
-    tys[p] = (unsigned char)ta;
+    if (xlh) {  // the mixed form's 8-byte record (pair_lo_type decodes it)
+      xlh[p] = pack_lo_type(lx, ly, lz, ta);
+    } else {
+      xls[p] = make_float4(lx, ly, lz, lq);
+      tys[p] = (unsigned char)ta;
+    }
   }
 }
 
@@ -1072,7 +1076,7 @@ int list_build() {
 void list_pos_records(bool sorted) {
   k_pos_records<<<nblocks(g.mxatms, 256), 256, 0, g.stream>>>(
       g.sc, g.sorted_pos, g.x, g.y, g.z, g.chge, g.ltype, g.xf, g.xlo, g.precision == GB_FP64 ? g.qdf : nullptr,
-      sorted ? g.xhs : nullptr, g.xls, g.tys);
+      sorted ? g.xhs : nullptr, g.xls, g.tys, g.precision == GB_MIXED ? g.xlh : nullptr);
   GB_LAUNCHED();
 }
 

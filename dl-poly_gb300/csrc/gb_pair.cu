@@ -745,6 +745,7 @@ struct PairSortedArgs {
   const float4* xhs;
   const float4* xls;
   const unsigned char* tys;
+  const uint2* xlh;  // mixed form: remainders and type in 8 bytes (pair_lo_type)
   const double *x, *y, *z, *q;  // FP64 by atom index: the exact pair evaluation near a cutoff
   const float4* etab;
   const float4* vtab;
@@ -920,8 +921,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A,
   for (int a = blockIdx.x * per + wq; a < a_end; a += NT / 32) {
     const int p = A.loc_sp[a];
     const int i = A.at_list[p];
-    const float4 pi = A.xhs[p], li = A.xls[p];
-    const int ai = A.tys[p];
+    const float4 pi = A.xhs[p];
+    float4 li;
+    int ai;
+    if (MIXED) {
+      pair_lo_type(A.xlh[p], li.x, li.y, li.z, ai);
+      li.w = 0.f;
+    } else {
+      li = A.xls[p];
+      ai = A.tys[p];
+    }
     const df qi = df_mul(df_make(pi.w, li.w), df_make(pg.scal_hi, pg.scal_lo));  // q_i r4pie0/eps
     const bool qi_on = pi.w != 0.0f;
     const float qi32 = pi.w * A.scaling;
@@ -962,8 +971,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A,
         const int take = min(nq, 32);
         if (lane < take) {
           const int j = pq[wq].j[nq - take + lane];
-          const float4 pj = A.xhs[j], lj = A.xls[j];
-          const int aj = A.tys[j];
+          const float4 pj = A.xhs[j];
+          float4 lj;
+          int aj;
+          if (MIXED) {
+            pair_lo_type(A.xlh[j], lj.x, lj.y, lj.z, aj);
+            lj.w = 0.f;
+          } else {
+            lj = A.xls[j];
+            aj = A.tys[j];
+          }
           long long ix = 0, iy = 0, iz = 0;
           bool hit;
           if (MIXED) {
@@ -1129,7 +1146,7 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   A.at_list = g.at_list;
   A.loc_sp = g.loc_sp;
   A.list = g.list; A.ld = g.ld; A.spos = g.spos; A.ldt = g.ldt;
-  A.xhs = g.xhs; A.xls = g.xls; A.tys = g.tys;
+  A.xhs = g.xhs; A.xls = g.xls; A.tys = g.tys; A.xlh = g.xlh;
   A.x = g.x; A.y = g.y; A.z = g.z; A.q = g.chge;
   A.etab = g.erfc_df; A.vtab = g.vdw_df; A.ecoef = g.erfc_coef; A.vcoef = g.vdw_coef;
   A.vkind = g.vdw_kind; A.veps = g.vdw_eps; A.vsig = g.vdw_sig;
