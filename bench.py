@@ -185,7 +185,7 @@ MEASURED_TRAFFIC = {
     ("pair_forces", "fp64_native"): ((200.795648e6 + 3.779072e6) / 40368337,
                                      "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_fp64 on nacl_175616 "
                                      "(profiles/pair_fp64_nacl175616.md), scaled by half-list entries"),
-    ("pair_forces", "mixed"): ((225.09824e6 + 4.418816e6) / 40368337,
+    ("pair_forces", "mixed"): ((219.659264e6 + 6.057216e6) / 40368337,
                                "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_sorted<1, 4, 256> on nacl_175616 "
                                "(profiles/pair_sorted_mixed_nacl175616.md), scaled by half-list entries"),
     ("metal_forces", "fp64"): ((131.494144e6 + 4.494848e6) / 19246179,
