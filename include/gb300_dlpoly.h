@@ -210,7 +210,9 @@ int gb_rattle(int32_t* iters);
 
 /* Resident MD loop (md_vv, drivers.F90:2059-2288): nsteps of VV1+SHAKE,
  * refresh, forces, VV2+RATTLE with no host round trip; stats[nsteps] may be NULL.
- * Each step first advances the step counter (gb_set_step). */
+ * Each step first advances the step counter (gb_set_step).  In NVE without
+ * constraints, thermostat, metals or learned MTS, a call of 3 or more steps replays
+ * each step as CUDA graphs captured inside the call (same kernels and results). */
 int gb_md_run(int nsteps, gb_step_stats* stats);
 
 /* Ensemble of the VV stages: the dispatch on thermo%ensemble (drivers.F90:1132-1175)
