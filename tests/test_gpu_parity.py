@@ -476,14 +476,19 @@ def test_deferred_step_scalars_match_per_step_readback(gpu_lib, monkeypatch, pre
         assert list(x.stress) == list(y.stress) and list(x.strkin) == list(y.strkin)
 
 
-@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
-def test_graph_steps_match_launched_steps(gpu_lib, monkeypatch, precision):
+@pytest.mark.parametrize("precision,overlap", [(0, "1"), (1, "1"), (2, "1"), (0, "0")],
+                         ids=["fp64", "mixed", "fp64_native", "fp64_one_stream"])
+def test_graph_steps_match_launched_steps(gpu_lib, monkeypatch, precision, overlap):
     """The NVE loop's steps replayed as CUDA graphs (stage 1 with the list check; a step
     without rebuild, captured again after each rebuild) run the same kernels as the loop
     that launches them one by one: the same trajectory and step scalars bit for bit, and
-    the same kernel count."""
+    the same kernel count; with SPME on the side stream (forked and joined inside the
+    graph) or on one stream.  The all-native-FP64 form sums its pair forces with FP64
+    atomics, whose order varies from run to run with or without graphs: it is compared
+    at the MD-trajectory bar (1e-9) instead."""
     s = systems.nacl_melt(16)
     out = []
+    monkeypatch.setenv("GB_OVERLAP", overlap)
     for env in ("0", "1"):
         monkeypatch.setenv("GB_GRAPHS", env)
         gpu_lib.init(s, precision=precision)
@@ -492,15 +497,24 @@ def test_graph_steps_match_launched_steps(gpu_lib, monkeypatch, precision):
         st = gpu_lib.md_vv(40)
         out.append((st, gpu_lib.download(), gpu_lib.lib.gb_kernel_launches() - l0))
     monkeypatch.delenv("GB_GRAPHS", raising=False)
+    monkeypatch.delenv("GB_OVERLAP", raising=False)
     (sa, a, na), (sb, b, nb) = out
     assert sum(x.list_rebuilt for x in sa) >= 2
     assert [x.list_rebuilt for x in sa] == [x.list_rebuilt for x in sb]
+    exact = precision != 2
     for k in a:
-        assert np.array_equal(a[k], b[k]), k
+        if exact:
+            assert np.array_equal(a[k], b[k]), k
+        else:
+            assert np.abs(a[k] - b[k]).max() <= 1e-9 * np.abs(b[k]).max(), k
     for x, y in zip(sa, sb):
         for f in ("engcpe_rc", "vircpe_rc", "engcpe_rl", "vircpe_rl", "engvdw", "virvdw", "engke"):
-            assert getattr(x, f) == getattr(y, f), f
-        assert list(x.stress) == list(y.stress) and list(x.strkin) == list(y.strkin)
+            if exact:
+                assert getattr(x, f) == getattr(y, f), f
+            else:
+                assert getattr(x, f) == pytest.approx(getattr(y, f), rel=1e-9), f
+        if exact:
+            assert list(x.stress) == list(y.stress) and list(x.strkin) == list(y.strkin)
     assert na == nb
 
 
