@@ -748,6 +748,7 @@ struct PairSortedArgs {
   const uint2* xlh;  // mixed form: remainders and type in 8 bytes (pair_lo_type)
   const double *x, *y, *z, *q;  // FP64 by atom index: the exact pair evaluation near a cutoff
   const float4* etab;
+  int netab;  // float4 entries of etab (the FP64 form copies the table into shared memory)
   const float4* vtab;
   const double* ecoef;
   const double* vcoef;
@@ -766,7 +767,8 @@ struct PairSortedArgs {
 // passed in); jp is the partner's sorted position, whose atom index the exact FP64
 // evaluation near a cutoff looks up.
 // Returns false when the pair exerts no force.
-__device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSortedArgs& A, int i, int jp, int ai,
+__device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSortedArgs& A, const float4* etab,
+                                               int i, int jp, int ai,
                                                int aj, df qi, bool qi_on, float qjh, float qjl, df dx, df dy, df dz,
                                                df rsq, dacc (&acc)[NACC_DF], long long& ix, long long& iy,
                                                long long& iz) {
@@ -793,7 +795,7 @@ __device__ __forceinline__ bool pair_df64_eval(const PairGeom& pg, const PairSor
       slow = true;  // first interval: the exact three-point formula, in FP64
     } else {
       if (in_c) {
-        const float4* c = A.etab + (size_t)k * 3;
+        const float4* c = etab + k * 3;
         const float4 e01 = c[0], d01 = c[1], c2 = c[2];
         const df pre = df_mul(qi, df_make(qjh, qjl));
         gvc = df_mul(pre, poly_df(d01, c2.z, c2.w, d));
@@ -901,11 +903,15 @@ template <int MIXED, int U, int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A, PairGeom pg) {
   __shared__ PairQueueN<32 * (U + 1)> pq[NT / 32];
   __shared__ float4 s_lj[MIXED ? MAX_TYPES * MAX_TYPES : 1];
+  extern __shared__ float4 s_etab[];  // FP64 form: the double-float erfc table
   if (MIXED) {
     for (int e = threadIdx.x; e < A.ntypes * A.ntypes; e += blockDim.x) {
       const int ai = e / A.ntypes + 1, aj = e % A.ntypes + 1;
       s_lj[e] = c_lj[vkey(ai, aj) - 1];
     }
+    __syncthreads();
+  } else {
+    for (int e = threadIdx.x; e < A.netab; e += blockDim.x) s_etab[e] = A.etab[e];
     __syncthreads();
   }
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
@@ -993,7 +999,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_pair_sorted(PairSortedArgs A,
             const df dy = quick_two_sum(ey.hi, __fadd_rn(ey.lo, __fsub_rn(li.y, lj.y)));
             const df dz = quick_two_sum(ez.hi, __fadd_rn(ez.lo, __fsub_rn(li.z, lj.z)));
             const df rsq = df_norm2(dx, dy, dz);
-            hit = rsq.hi <= pg.f_hi && pair_df64_eval(pg, A, i, j, ai, aj, qi, qi_on, pj.w, lj.w, dx,
+            hit = rsq.hi <= pg.f_hi && pair_df64_eval(pg, A, s_etab, i, j, ai, aj, qi, qi_on, pj.w, lj.w, dx,
                                                       dy, dz, rsq, acc, ix, iy, iz);
           }
           if (hit) {
@@ -1149,6 +1155,7 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   A.xhs = g.xhs; A.xls = g.xls; A.tys = g.tys; A.xlh = g.xlh;
   A.x = g.x; A.y = g.y; A.z = g.z; A.q = g.chge;
   A.etab = g.erfc_df; A.vtab = g.vdw_df; A.ecoef = g.erfc_coef; A.vcoef = g.vdw_coef;
+  A.netab = (g.nsamples + 1) * 3;
   A.vkind = g.vdw_kind; A.veps = g.vdw_eps; A.vsig = g.vdw_sig;
   A.ntypes = g.p.ntypes;
   A.rc2 = (float)pg.rc2; A.rv2 = (float)pg.rv2; A.alpha = (float)g.p.alpha;
@@ -1168,8 +1175,11 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   } else {
     kern = mixed ? k_pair_sorted<1, 4, 1024> : k_pair_sorted<0, 4, 1024>;
   }
+  // the FP64 form reads its erfc table from shared memory
+  const size_t dsm = mixed ? 0 : sizeof(float4) * (size_t)A.netab;
+  if (dsm > 0) GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
   int occ = 0;
-  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, 0));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, dsm));
   // The CTAs take equal contiguous runs of the local atoms: one resident set of CTAs
   // (the double-float form), or short-lived CTAs of 16 atoms per warp (the mixed form: they
   // retire through the step, so the side stream's SPME kernels take their places and the
@@ -1190,7 +1200,7 @@ void pair_forces_sorted(PairGeom& pg, int nb2) {
   GB_CUDA(cudaMemsetAsync(g.fixs, 0, sizeof(long long) * 3 * (size_t)g.mxatms, st));
   if (!mixed) GB_CUDA(cudaMemsetAsync(g.fixp, 0, sizeof(long long) * 3 * (size_t)g.mxatms, st));
   prof_begin(P_PAIR);
-  kern<<<nb, nt, 0, st>>>(A, pg);
+  kern<<<nb, nt, dsm, st>>>(A, pg);
   GB_LAUNCHED();
   run_side_hook();  // side-stream work enqueued behind the pair kernel's launch
   side_join();  // the reciprocal-space forces are in place before the pair forces join them
