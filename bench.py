@@ -179,7 +179,7 @@ def kernel_work(name, s, cnt, form):
 # for a full-section capture); traffic grows with the list, so the bench scales
 # it by this launch's list entries.
 MEASURED_TRAFFIC = {
-    ("pair_forces", "fp64"): ((223.242496e6 + 4.80512e6) / 40368337,
+    ("pair_forces", "fp64"): ((223.553536e6 + 4.797952e6) / 40368337,
                               "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_pair_sorted<0, 4, 1024> on nacl_175616 "
                               "(profiles/pair_sorted_df64_nacl175616.md), scaled by half-list entries"),
     ("pair_forces", "fp64_native"): ((200.795648e6 + 3.779072e6) / 40368337,
@@ -199,7 +199,7 @@ MEASURED_TRAFFIC = {
 # entries).  That kernel runs on the FP32/ALU pipes and is bound by instruction
 # issue, so its roofline is issue slots: 4 warp instructions per clock per SM.
 MEASURED_INST = {
-    ("pair_forces", "fp64"): (604503396 / 40368337,
+    ("pair_forces", "fp64"): (601732163 / 40368337,
                               "ncu smsp__inst_executed.sum of k_pair_sorted<0, 4, 1024> on nacl_175616 "
                               "(profiles/pair_sorted_df64_nacl175616.md), scaled by half-list entries"),
 }
